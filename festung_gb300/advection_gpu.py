@@ -1,0 +1,294 @@
+"""The ``advection_gpu`` problem: the step-function interface of FESTUNG's ``advection`` problem
+with the stage loop on the GPU.
+
+The reference drives a problem through ``main(problemName, key, value, ...)`` (main.m:115-178):
+pre-processing steps configureProblem, preprocessProblem, initializeProblem; then per time step
+preprocessStep, solveStep, postprocessStep, outputStep until ``isFinished``; then
+postprocessProblem.  This module provides the same functions over the same ``problemData``
+fields (``cDisc`` K x N, ``K``, ``N``, ``tau``, ``isFinished``, ``error``, ...), so
+``main('advection_gpu', ...)`` is a drop-in for ``main('advection', ...)`` on triangles.
+
+Differences in mechanism (not in results):
+  * preprocessProblem uploads the mesh, tables and the (time-independent) velocity once; the
+    reference re-assembles sparse operators every stage (advection/preprocessSubStep.m:56-99).
+  * solveStep enqueues one time step with all its RK stages (advection/solveStep.m:57-73 and the
+    sub-steps advection/solveSubStep.m:57-99) and returns without waiting; ``cDisc`` is read back
+    lazily, when postprocessProblem or the caller asks for it.
+  * source and Dirichlet data are time-separable terms (see ``festung_gb300.testcases``).
+Host-side set-up work (projections of the initial data and of the velocity, boundary vectors,
+L2 error) runs in numpy with the library's quadrature rules and basis values, as the
+reference's host code does with its core functions.
+"""
+import numpy as np
+
+from . import _lib as L
+from . import testcases as TC
+from .solver import DeviceSolver
+
+
+class Struct(dict):
+    def __getattr__(self, k):
+        try:
+            return self[k]
+        except KeyError as e:
+            raise AttributeError(k) from e
+
+    def __setattr__(self, k, v):
+        self[k] = v
+
+
+def setdefault(pd, key, value):
+    if key not in pd:
+        pd[key] = value
+
+
+# ---------------------------------------------------------------------------------------------
+# Host-side set-up helpers (restate the reference's core functions for the set-up phase).
+class Tables:
+    """Quadrature rules and basis values by quadrature order (core/computeBasesOnQuad.m)."""
+
+    def __init__(self, N):
+        self.N = N
+        self._r2, self._r1, self._phi2D, self._phi1D = {}, {}, {}, {}
+
+    def rule2(self, qOrd):
+        if qOrd not in self._r2:
+            self._r2[qOrd] = L.quad_rule_2d(qOrd)
+        return self._r2[qOrd]
+
+    def rule1(self, qOrd):
+        if qOrd not in self._r1:
+            self._r1[qOrd] = L.quad_rule_1d(qOrd)
+        return self._r1[qOrd]
+
+    def phi2D(self, qOrd):
+        if qOrd not in self._phi2D:
+            Q1, Q2, _ = self.rule2(qOrd)
+            self._phi2D[qOrd] = L.basis_eval(self.N, Q1, Q2)
+        return self._phi2D[qOrd]
+
+    def phi1D(self, qOrd):
+        """R x N x 3: basis on the edge points gammaMap(n, Q) (core/gammaMap.m:50-57)."""
+        if qOrd not in self._phi1D:
+            Q, _ = self.rule1(qOrd)
+            out = np.zeros((Q.size, self.N, 3))
+            for n in range(3):
+                X1, X2 = gamma_map(n, Q)
+                out[:, :, n] = L.basis_eval(self.N, X1, X2)
+            self._phi1D[qOrd] = out
+        return self._phi1D[qOrd]
+
+
+def gamma_map(n, S):
+    S = np.asarray(S, dtype=np.float64)
+    if n == 0:
+        return 1 - S, S
+    if n == 1:
+        return np.zeros_like(S), 1 - S
+    return S, np.zeros_like(S)
+
+
+def map_ref_to_phy(g, i, X1, X2):
+    X1 = np.asarray(X1).reshape(1, -1); X2 = np.asarray(X2).reshape(1, -1)
+    return (g['B'][:, i, 0:1] * X1 + g['B'][:, i, 1:2] * X2) + g['coordV0T'][:, 0, i:i + 1] * np.ones_like(X1)
+
+
+def project(g, tables, func, qOrd, hatM):
+    """projectFuncCont2DataDisc (core/projectFuncCont2DataDisc.m:94-102)."""
+    qOrd = max(qOrd, 1)
+    Q1, Q2, W = tables.rule2(qOrd)
+    F = func(map_ref_to_phy(g, 0, Q1, Q2), map_ref_to_phy(g, 1, Q1, Q2))
+    rhs = F @ (W[:, None] * tables.phi2D(qOrd))
+    return np.linalg.solve(hatM.T, rhs.T).T
+
+
+def normal_velocity(g, tables, u1, u2, qOrd):
+    """computeFuncContNuOnQuadEdge (core/computeFuncContNuOnQuadEdge.m:46-67): K x 3 x R."""
+    Q, _ = tables.rule1(qOrd)
+    out = np.zeros((g['numT'], 3, Q.size))
+    for n in range(3):
+        X1, X2 = gamma_map(n, Q)
+        x, y = map_ref_to_phy(g, 0, X1, X2), map_ref_to_phy(g, 1, X1, X2)
+        out[:, n, :] = g['nuE0T'][:, n, 0:1] * u1(x, y) + g['nuE0T'][:, n, 1:2] * u2(x, y)
+    return out
+
+
+def dirichlet_vector(g, tables, markD, func, vN, qOrd):
+    """assembleVecEdgePhiIntFuncContVal (core/assembleVecEdgePhiIntFuncContVal.m:162-185): K x N."""
+    Q, W = tables.rule1(qOrd)
+    P = tables.phi1D(qOrd)
+    out = np.zeros((g['numT'], tables.N))
+    for n in range(3):
+        X1, X2 = gamma_map(n, Q)
+        f = func(map_ref_to_phy(g, 0, X1, X2), map_ref_to_phy(g, 1, X1, X2))
+        Kkn = markD[:, n] * g['areaE0T'][:, n]
+        v = vN[:, n, :]
+        out += Kkn[:, None] * ((f * ((v < 0) * v)) @ (W[:, None] * P[:, :, n]))
+    return out
+
+
+def l2_error(g, tables, cDisc, func, qOrd):
+    """computeL2Error (core/computeL2Error.m:97-114)."""
+    qOrd = max(qOrd, 1)
+    Q1, Q2, W = tables.rule2(qOrd)
+    x, y = map_ref_to_phy(g, 0, Q1, Q2), map_ref_to_phy(g, 1, Q1, Q2)
+    d = cDisc @ tables.phi2D(qOrd).T - func(x, y)
+    return float(np.sqrt(2 * np.dot((d ** 2) @ W, g['areaT'])))
+
+
+def vertex_values(g, func):
+    """computeFuncContV0T (core/computeFuncContV0T.m:41-51): K x 3."""
+    return np.stack([func(g['coordV0T'][:, n, 0], g['coordV0T'][:, n, 1]) for n in range(3)], axis=1)
+
+
+# ---------------------------------------------------------------------------------------------
+# Step functions
+def configureProblem(pd):
+    """advection/configureProblem.m:61-151 (triangle path)."""
+    setdefault(pd, 'testcase', 'solid_body')
+    setdefault(pd, 'hmax', 2 ** -6)
+    setdefault(pd, 'isQuadri', False)
+    setdefault(pd, 'p', 0)
+    setdefault(pd, 'qOrd', 2 * pd.p + 1)
+    setdefault(pd, 'ordRK', min(pd.p + 1, 3))
+    setdefault(pd, 'numSteps', 100)
+    setdefault(pd, 'tEnd', (pd.numSteps / (3142 * 1.5)) * 2 * np.pi)
+    setdefault(pd, 'isSlopeLim', False)
+    setdefault(pd, 'typeSlopeLim', 'linear')
+    setdefault(pd, 'isVisSol', False)
+    setdefault(pd, 'precision', 'fp64')
+    setdefault(pd, 'device', 0)
+    setdefault(pd, 'gpuFlags', 0)
+    assert not pd.isQuadri, 'advection_gpu supports triangles only (isQuadri = false).'
+    assert 0 <= pd.p <= 4, 'Polynomial order must be zero to four.'
+    assert 1 <= pd.ordRK <= 3, 'Order of Runge Kutta must be zero to three.'
+    assert pd.hmax > 0, 'Maximum edge length must be positive.'
+    assert pd.numSteps > 0, 'Number of time steps must be positive.'
+    assert (not pd.isSlopeLim) or pd.p > 0, 'Slope limiting only available for p > 0.'
+    TC.configure(pd)
+    return pd
+
+
+def preprocessProblem(pd):
+    """advection/preprocessProblem.m:48-112: grid, markers, tables; device upload."""
+    coordV, V0T, dim, h = TC.square_coords(pd.hmax)
+    coordV = TC.jitter_coords(coordV, h, pd.jitter, pd.meshSeed)
+    g = L.grid_build(coordV, V0T)
+    g['coordV'], g['V0T'] = coordV, V0T
+    g['idE'] = TC.boundary_ids(g['baryE'])
+    g['idE0T'] = g['idE'][g['E0T']]
+    g['markE0Tint'] = g['idE0T'] == 0
+    g['markE0TbdrN'] = np.zeros((g['numT'], 3), dtype=bool)
+    g['markE0TbdrD'] = ~(g['markE0Tint'] | g['markE0TbdrN'])
+    pd.g = g
+    pd.K = g['numT']
+    pd.N = (pd.p + 1) * (pd.p + 2) // 2
+    pd.tau = pd.tEnd / pd.numSteps
+    tables = Tables(pd.N)
+    pd.tables = tables
+    qv = max(2 * pd.p, 1)
+    _, _, W = tables.rule2(qv)
+    P = tables.phi2D(qv)
+    pd.hatM = (W[:, None] * P).T @ P
+    pd.solver = DeviceSolver(coordV, V0T, pd.p, pd.ordRK, precision=pd.precision,
+                             isSlopeLim=pd.isSlopeLim, typeSlopeLim=pd.typeSlopeLim,
+                             idE0T=g['idE0T'], markE0TbdrD=g['markE0TbdrD'],
+                             markE0TbdrN=g['markE0TbdrN'], device=pd.device, flags=pd.gpuFlags)
+    # velocity data of advection/preprocessSubStep.m:72-79 (time-independent)
+    u1Disc = project(g, tables, pd.u1Cont, 2 * pd.p, pd.hatM)
+    u2Disc = project(g, tables, pd.u2Cont, 2 * pd.p, pd.hatM)
+    vN = normal_velocity(g, tables, pd.u1Cont, pd.u2Cont, 2 * pd.p + 1)
+    pd.u1Disc, pd.u2Disc, pd.vNormalOnQuadEdge = u1Disc, u2Disc, vN
+    pd.solver.set_velocity(u1Disc, u2Disc, vN)
+    # separable right-hand-side terms rhs_m = M f_m - K_D,m  (K_N = 0: no Neumann data)
+    terms = {}
+    detJ = g['detJ0T']
+    for fn, f in pd.fTerms:
+        fd = project(g, tables, f, 2 * pd.p, pd.hatM)
+        terms.setdefault(fn, [np.zeros((pd.K, pd.N)), np.zeros((pd.K, 3))])[0][...] += \
+            detJ[:, None] * (fd @ pd.hatM.T)
+    for fn, f in pd.cDTerms:
+        e = terms.setdefault(fn, [np.zeros((pd.K, pd.N)), np.zeros((pd.K, 3))])
+        e[0][...] -= dirichlet_vector(g, tables, g['markE0TbdrD'], f, vN, pd.qOrd)
+        e[1][...] += vertex_values(g, f)
+    codes = {'const': L.TIME_CONST, 'exp_neg': L.TIME_EXP_NEG}
+    names = sorted(terms)
+    pd.solver.set_source_terms([codes[n] for n in names], [terms[n][0] for n in names],
+                               [terms[n][1] for n in names] if pd.cDTerms else None)
+    return pd
+
+
+def initializeProblem(pd):
+    """advection/initializeProblem.m:46-86: L2 projection of c0, initial limiting, error."""
+    pd.isFinished = False
+    c = project(pd.g, pd.tables, pd.c0Cont, pd.qOrd, pd.hatM)
+    pd.solver.set_state(c)
+    if pd.isSlopeLim:
+        pd.solver.limit_state(0.0)
+        c = pd.solver.get_state()
+    pd._cDisc = np.ascontiguousarray(c)
+    pd._stale = False
+    pd.initialError = l2_error(pd.g, pd.tables, pd._cDisc, pd.c0Cont, 2 * pd.p)
+    return pd
+
+
+def cDisc(pd):
+    """Current coefficients K x N (read back from the device when stale)."""
+    if pd._stale:
+        pd._cDisc = np.ascontiguousarray(pd.solver.get_state())
+        pd._stale = False
+    return pd._cDisc
+
+
+def preprocessStep(pd, nStep):
+    return pd
+
+
+def solveStep(pd, nStep):
+    """One SSP-RK step with all sub-steps, enqueued on the device (advection/solveStep.m:57-73)."""
+    pd.solver.step(1, nStep - 1, pd.tau)
+    pd._stale = True
+    return pd
+
+
+def postprocessStep(pd, nStep):
+    """advection/postprocessStep.m:54-61 (cDisc is read back lazily)."""
+    pd.isFinished = nStep >= pd.numSteps
+    return pd
+
+
+def outputStep(pd, nStep):
+    return pd
+
+
+def postprocessProblem(pd):
+    """advection/postprocessProblem.m:43-82 (error against the exact or the initial data)."""
+    pd.cDisc = cDisc(pd)
+    if pd.isAnalytical:
+        f = lambda x1, x2: pd.cCont(pd.tEnd, x1, x2)
+    else:
+        f = pd.c0Cont
+    pd.error = l2_error(pd.g, pd.tables, pd.cDisc, f, pd.qOrd)
+    return pd
+
+
+PRE = (configureProblem, preprocessProblem, initializeProblem)
+STEP = (preprocessStep, solveStep, postprocessStep, outputStep)
+POST = (postprocessProblem,)
+
+
+def main(problemData=None, **kwargs):
+    """main('advection_gpu', key, value, ...) (main.m:115-178)."""
+    pd = Struct(problemData or {})
+    pd.update(kwargs)
+    pd.problemName = 'advection_gpu'
+    for f in PRE:
+        pd = f(pd)
+    nStep = 0
+    while not pd.isFinished:
+        nStep += 1
+        for f in STEP:
+            pd = f(pd, nStep)
+    for f in POST:
+        pd = f(pd)
+    return pd

@@ -1,0 +1,66 @@
+// Device kernels of the DG advection stage.  One thread owns one element; all per-element
+// arrays are structure-of-arrays with leading dimension Kp (coalesced loads across a warp).
+//
+// Stage pipeline (stage s of an SSP-RK step, advection/solveSubStep.m:57-99):
+//   limiter off:          k_stage_op  (volume + upwind flux + mass + SSP)            -> c^(s)
+//   limiter on, p = 1:    k_stage_op  -> Taylor(c^(s)), centroid values q
+//                         k_vertex_minmax (CSR vertex patches)  -> vertex min/max
+//                         k_limit     -> limited modal c^(s)
+//   limiter on, p >= 2:   k_stage_op  -> Taylor(cDot), q
+//                         k_vertex_minmax
+//                         k_limit_dot (limit cDot, Taylor mass correction, SSP) -> Taylor(c^(s)), q
+//                         k_vertex_minmax
+//                         k_limit     -> limited modal c^(s)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dgadv {
+
+template <int P> struct Dims {
+  static constexpr int N = (P + 1) * (P + 2) / 2;
+  static constexpr int Q = P == 0 ? 1 : (P == 1 ? 3 : (P == 2 ? 6 : 12));   // quadRule2D(max(2p,1))
+  static constexpr int R = P + 1;                                            // quadRule1D(2p+1)
+  static constexpr int NMT = N * (N + 1) / 2;                                // packed Taylor mass
+  static constexpr int NC_HIER = P * (P + 1) / 2;                            // hierarchical sub-limiters
+};
+
+template <typename T, int P> struct Tab {
+  static constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
+  T phiQ[Q][N];       // phi_j at the volume points
+  T g1[Q][N];         // d/dx1 phi_i at the volume points
+  T g2[Q][N];         // d/dx2 phi_i at the volume points
+  T phi1D[3][R][N];   // phi_j at the edge points of edge n
+  T thetaPhi[3][3][R][N];  // phi_j of the neighbour at the same points (theta_{n,np} o gamma_n)
+  T hatMinv[N][N];
+  T DM[N][N];         // modal -> reference derivatives at the barycentre (times hatM)
+  T DMinv[N][N];
+};
+
+// Static per-element data of one mesh (device pointers, SoA with stride Kp).
+template <typename T> struct Geo {
+  int K, Kp, numV, Vp;
+  const T *F;        // 2Q x Kp  volume flux factors W_q (B22 u1 - B12 u2)/detJ, W_q (B11 u2 - B21 u1)/detJ
+  const T *Vn;       // 3R x Kp  markNotN * |E| * w_r * (u.nu)_r / detJ
+  const int *nbr;    // 3 x Kp   neighbour element across edge n, -1 on the boundary
+  const int *code;   // Kp       bits 2n..2n+1: neighbour's local edge; bit 6+n: outflow counted;
+                     //          bit 9+n: local vertex n lies on a Dirichlet edge
+  const T *Bm;       // 4 x Kp   B11, B12, B21, B22
+  const T *MT;       // NMT x Kp packed Taylor mass blocks (time-derivative limiting)
+  const int *V0T;    // 3 x Kp   vertex ids
+  const int *vptr;   // numV+1   CSR vertex -> elements
+  const int *vidx;
+  const T *rhs;      // nTerms x N x Kp   (L - K_D - K_N)_m / detJ
+  const T *cDV0T;    // nTerms x 3 x Kp   boundary values at the vertices
+  int nTerms;
+  int timeFn[4];
+};
+
+struct LimArgs {
+  int type;              // 0 linear, 1 hierarchical vertex
+  int nc;                // number of centroid quantities
+  int shift;             // replicate the reference's global shift
+  const unsigned long long *gmm;   // 2 x nc encoded global min / max
+};
+
+}  // namespace dgadv

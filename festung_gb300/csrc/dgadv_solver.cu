@@ -1,0 +1,1190 @@
+// Device solver of the explicit DG advection step and its C-ABI entry points.
+//
+// Per-stage operator (advection/preprocessSubStep.m:56-99 + advection/solveSubStep.m:57-99),
+// matrix-free and element-centric:
+//   volume  (G1+G2)c |_{k,i} = sum_q c(x_q) [d1 phi_i (B22 u1 - B12 u2) + d2 phi_i (B11 u2 - B21 u1)] W_q
+//           (core/assembleMatElemDphiPhiFuncDisc.m:181-202; same rule of order 2p as hatG)
+//   flux    (R c)_{k,i} = sum_n |E_kn| sum_r w_r v_knr phi_i(g_n(q_r)) * (v>0 ? c_k : c_k+) traces
+//           (core/assembleMatEdgePhiPhiValUpwind.m:261-299: the upwind side is gathered through
+//           the neighbour map, so every element writes only its own rows: no atomics)
+//   mass    cDot = hatM^-1 rhs / detJ (FP64; the FP32 path uses hatM = I, |hatM - I| < 2e-14)
+//   SSP     c^(s) = w_s c^n + (1-w_s)(c^(s-1) + tau cDot)          advection/solveSubStep.m:83
+// Limiter: core/applySlopeLimiterTaylor*.m with patch min/max over CSR vertex patches
+// (core/computeMinMaxV0TElementPatch.m:66-112) and the Taylor transform in closed form
+// (Taylor coefficients = mean and scaled derivatives at the barycentre).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <type_traits>
+#include <string>
+#include <vector>
+
+#include "../../include/dgadv.h"
+#include "dgadv_host.h"
+#include "dgadv_kernels.cuh"
+
+namespace dgadv {
+
+// ---------------------------------------------------------------------------------------------
+// Constant tables, one instance per (precision, degree).
+__constant__ Tab<double, 0> cTd0;
+__constant__ Tab<double, 1> cTd1;
+__constant__ Tab<double, 2> cTd2;
+__constant__ Tab<double, 3> cTd3;
+__constant__ Tab<float, 0> cTf0;
+__constant__ Tab<float, 1> cTf1;
+__constant__ Tab<float, 2> cTf2;
+__constant__ Tab<float, 3> cTf3;
+
+template <typename T, int P> __device__ __forceinline__ const Tab<T, P> &tab();
+template <> __device__ __forceinline__ const Tab<double, 0> &tab<double, 0>() { return cTd0; }
+template <> __device__ __forceinline__ const Tab<double, 1> &tab<double, 1>() { return cTd1; }
+template <> __device__ __forceinline__ const Tab<double, 2> &tab<double, 2>() { return cTd2; }
+template <> __device__ __forceinline__ const Tab<double, 3> &tab<double, 3>() { return cTd3; }
+template <> __device__ __forceinline__ const Tab<float, 0> &tab<float, 0>() { return cTf0; }
+template <> __device__ __forceinline__ const Tab<float, 1> &tab<float, 1>() { return cTf1; }
+template <> __device__ __forceinline__ const Tab<float, 2> &tab<float, 2>() { return cTf2; }
+template <> __device__ __forceinline__ const Tab<float, 3> &tab<float, 3>() { return cTf3; }
+
+constexpr int kBlock = 128;
+
+// ---------------------------------------------------------------------------------------------
+// Ordered integer keys: atomicMin/atomicMax on the key order like on the real numbers.
+__device__ __forceinline__ unsigned long long okey(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ unsigned long long okey(float x) {
+  const unsigned int u = __float_as_uint(x);
+  return (unsigned long long)((u >> 31) ? ~u : (u | 0x80000000u));
+}
+template <typename T> __device__ __forceinline__ T okey_inv(unsigned long long k);
+template <> __device__ __forceinline__ double okey_inv<double>(unsigned long long k) {
+  const unsigned long long u = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFULL) : ~k;
+  return __longlong_as_double((long long)u);
+}
+template <> __device__ __forceinline__ float okey_inv<float>(unsigned long long k) {
+  const unsigned int kk = (unsigned int)k;
+  const unsigned int u = (kk >> 31) ? (kk & 0x7FFFFFFFu) : ~kk;
+  return __uint_as_float(u);
+}
+template <typename T> __host__ __device__ constexpr unsigned long long key_max();
+template <> __host__ __device__ constexpr unsigned long long key_max<double>() { return ~0ULL; }
+template <> __host__ __device__ constexpr unsigned long long key_max<float>() { return 0xFFFFFFFFULL; }
+
+__device__ __forceinline__ bool finite_(double x) { return isfinite(x); }
+__device__ __forceinline__ bool finite_(float x) { return isfinite(x); }
+
+// ---------------------------------------------------------------------------------------------
+// Element geometry for the Taylor transform.
+template <typename T> struct Affine {
+  T B11, B12, B21, B22;   // B(:,m,n): m = coordinate, n = column
+  T A11, A12, A21, A22;   // A = B^-1
+  T dX, idX;              // dX = 2 / sqrt(detJ)
+  T ox[3], oy[3];         // vertex offsets from the barycentre
+};
+
+template <typename T> __device__ __forceinline__ Affine<T> load_affine(const Geo<T> &g, int k) {
+  Affine<T> a;
+  a.B11 = g.Bm[k]; a.B12 = g.Bm[g.Kp + k]; a.B21 = g.Bm[2 * g.Kp + k]; a.B22 = g.Bm[3 * g.Kp + k];
+  const T det = a.B11 * a.B22 - a.B12 * a.B21;
+  const T idet = T(1) / det;
+  a.A11 = a.B22 * idet; a.A12 = -a.B12 * idet; a.A21 = -a.B21 * idet; a.A22 = a.B11 * idet;
+  a.dX = T(2) / sqrt(det);
+  a.idX = T(1) / a.dX;
+  const T bx = -(a.B11 + a.B12) / T(3), by = -(a.B21 + a.B22) / T(3);
+  a.ox[0] = bx; a.oy[0] = by;
+  a.ox[1] = a.B11 + bx; a.oy[1] = a.B21 + by;
+  a.ox[2] = a.B12 + bx; a.oy[2] = a.B22 + by;
+  return a;
+}
+
+// Coefficients of (a + b z)^(D-m) (c + e z)^m in z^j, for m, j = 0..D.
+template <typename T, int D>
+__device__ __forceinline__ void deriv_block(T a, T b, T c, T e, T S[D + 1][D + 1]) {
+#pragma unroll
+  for (int m = 0; m <= D; ++m) {
+    T poly[D + 1];
+#pragma unroll
+    for (int j = 0; j <= D; ++j) poly[j] = (j == 0) ? T(1) : T(0);
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      const bool first = r < D - m;
+      const T x0 = first ? a : c, x1 = first ? b : e;
+#pragma unroll
+      for (int j = D; j >= 0; --j) poly[j] = poly[j] * x0 + (j > 0 ? poly[j - 1] * x1 : T(0));
+    }
+#pragma unroll
+    for (int j = 0; j <= D; ++j) S[m][j] = poly[j];
+  }
+}
+
+// modal c -> Taylor coefficients cT (core/projectDataDisc2DataTaylor.m:56-61 in closed form)
+template <typename T, int P>
+__device__ __forceinline__ void to_taylor(const T *c, const Affine<T> &af, T *cT) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T u[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    T s = 0;
+#pragma unroll
+    for (int j = 0; j < N; ++j) s += tb.DM[i][j] * c[j];
+    u[i] = s;
+  }
+  cT[0] = u[0];
+  T sc = T(1);
+#pragma unroll
+  for (int d = 1; d <= P; ++d) {
+    sc *= af.idX;
+    const int off = d * (d + 1) / 2;
+    if (d == 1) {
+      T S[2][2]; deriv_block<T, 1>(af.A11, af.A21, af.A12, af.A22, S);
+#pragma unroll
+      for (int m = 0; m <= 1; ++m) { T s = 0;
+#pragma unroll
+        for (int j = 0; j <= 1; ++j) s += S[m][j] * u[off + j]; cT[off + m] = s * sc; }
+    } else if (d == 2) {
+      T S[3][3]; deriv_block<T, 2>(af.A11, af.A21, af.A12, af.A22, S);
+#pragma unroll
+      for (int m = 0; m <= 2; ++m) { T s = 0;
+#pragma unroll
+        for (int j = 0; j <= 2; ++j) s += S[m][j] * u[off + j]; cT[off + m] = s * sc; }
+    } else if (d == 3) {
+      T S[4][4]; deriv_block<T, 3>(af.A11, af.A21, af.A12, af.A22, S);
+#pragma unroll
+      for (int m = 0; m <= 3; ++m) { T s = 0;
+#pragma unroll
+        for (int j = 0; j <= 3; ++j) s += S[m][j] * u[off + j]; cT[off + m] = s * sc; }
+    }
+  }
+}
+
+// Taylor coefficients -> modal (core/projectDataTaylor2DataDisc.m:56-61 in closed form)
+template <typename T, int P>
+__device__ __forceinline__ void from_taylor(const T *cT, const Affine<T> &af, T *c) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T w[N];
+  w[0] = cT[0];
+  T sc = T(1);
+#pragma unroll
+  for (int d = 1; d <= P; ++d) {
+    sc *= af.dX;
+    const int off = d * (d + 1) / 2;
+    if (d == 1) {
+      T S[2][2]; deriv_block<T, 1>(af.B11, af.B21, af.B12, af.B22, S);
+#pragma unroll
+      for (int m = 0; m <= 1; ++m) { T s = 0;
+#pragma unroll
+        for (int j = 0; j <= 1; ++j) s += S[m][j] * cT[off + j]; w[off + m] = s * sc; }
+    } else if (d == 2) {
+      T S[3][3]; deriv_block<T, 2>(af.B11, af.B21, af.B12, af.B22, S);
+#pragma unroll
+      for (int m = 0; m <= 2; ++m) { T s = 0;
+#pragma unroll
+        for (int j = 0; j <= 2; ++j) s += S[m][j] * cT[off + j]; w[off + m] = s * sc; }
+    } else if (d == 3) {
+      T S[4][4]; deriv_block<T, 3>(af.B11, af.B21, af.B12, af.B22, S);
+#pragma unroll
+      for (int m = 0; m <= 3; ++m) { T s = 0;
+#pragma unroll
+        for (int j = 0; j <= 3; ++j) s += S[m][j] * cT[off + j]; w[off + m] = s * sc; }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    T s = 0;
+#pragma unroll
+    for (int j = 0; j < N; ++j) s += tb.DMinv[i][j] * w[j];
+    c[i] = s;
+  }
+}
+
+// Index of the Taylor DOF with multi-index (a1, a2) (core/mult2ind.m:57-62, 0-based).
+__host__ __device__ constexpr int mind(int a1, int a2) { return (a1 + a2) * (a1 + a2 + 1) / 2 + a2; }
+
+// Centroid quantities of the sub-limiters (one per computeVertexBasedLimiter call).
+template <typename T, int P>
+__device__ __forceinline__ void centroid_quantities(const T *cT, int type, T *q, int k, int Kp) {
+  if (type == 0) {
+    q[k] = cT[0];
+  } else {
+    int s = 0;
+#pragma unroll
+    for (int ord = P; ord >= 1; --ord)
+#pragma unroll
+      for (int i = 1; i <= ord; ++i) { q[(size_t)s * Kp + k] = cT[mind(ord - i, i - 1)]; ++s; }
+  }
+}
+
+// alpha of one computeVertexBasedLimiter call (core/computeVertexBasedLimiter.m:78-106)
+template <typename T>
+__device__ __forceinline__ T vertex_alpha(T cbar, const T v[3], const T mn[3], const T mx[3]) {
+  const T tol = T(1.e-8);
+  T alpha = T(1);
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const T dV = v[n] - cbar, dMin = mn[n] - cbar, dMax = mx[n] - cbar;
+    T a = T(1);
+    if (dV < dMin + tol) a = fmax(T(0), fmin(T(1), dMin / (dV - tol)));
+    if (dV > dMax - tol) a = fmax(T(0), fmin(T(1), dMax / (dV + tol)));
+    alpha = (n == 0) ? a : fmin(alpha, a);
+  }
+  return alpha;
+}
+
+// Patch min / max of quantity s at the three vertices, with the reference's global shift
+// (min over the patch of (v - sNeg), then + sNeg; a monotone shift commutes with min).
+template <typename T>
+__device__ __forceinline__ void patch_minmax(const Geo<T> &g, const T *vmm, const LimArgs &la, int s,
+                                             const int vid[3], const T valD[3], T mn[3], T mx[3]) {
+  T sNeg = 0, sPos = 0;
+  if (la.shift) {
+    const T gmin = okey_inv<T>(la.gmm[2 * s]), gmax = okey_inv<T>(la.gmm[2 * s + 1]);
+    sPos = fabs(gmin) + T(1);
+    sNeg = fabs(gmax) + T(1);
+  }
+  const T *vmin = vmm + (size_t)(2 * s) * g.Vp, *vmax = vmm + (size_t)(2 * s + 1) * g.Vp;
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    T a = vmin[vid[n]], b = vmax[vid[n]];
+    if (la.shift) { a = (a - sNeg) + sNeg; b = (b + sPos) - sPos; }
+    mn[n] = fmin(a, valD[n]);
+    mx[n] = fmax(b, valD[n]);
+  }
+}
+
+// Limit Taylor coefficients in place (linear / hierarchical vertex).  dataV0T: boundary values
+// at the three vertices for Dirichlet vertices (NaN means "no data").
+template <typename T, int P>
+__device__ __forceinline__ void limit_taylor(const Geo<T> &g, const T *vmm, const LimArgs &la, int k,
+                                             const Affine<T> &af, const int vid[3], int dmask,
+                                             const T dataV0T[3], T *cT) {
+  constexpr int N = Dims<P>::N;
+  const T nan_ = T(NAN);
+  T pt1[3], pt2[3];   // Taylor basis 2 and 3 at the vertices
+#pragma unroll
+  for (int n = 0; n < 3; ++n) { pt1[n] = af.ox[n] * af.dX; pt2[n] = af.oy[n] * af.dX; }
+  if (la.type == 0) {
+    T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      v[n] = (cT[0] * T(1) + cT[1] * pt1[n]) + cT[2] * pt2[n];
+      valD[n] = ((dmask >> n) & 1) ? dataV0T[n] : nan_;
+    }
+    patch_minmax(g, vmm, la, 0, vid, valD, mn, mx);
+    const T alpha = vertex_alpha(cT[0], v, mn, mx);
+    cT[1] *= alpha; cT[2] *= alpha;
+    const T keep = (alpha == T(1)) ? T(1) : T(0);
+#pragma unroll
+    for (int i = 3; i < N; ++i) cT[i] *= keep;
+  } else {
+    T orig[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) orig[i] = cT[i];
+    T alpha = T(0);
+    int s = 0;
+#pragma unroll
+    for (int ord = P; ord >= 1; --ord) {
+      T aOrd = T(1);
+#pragma unroll
+      for (int i = 1; i <= ord; ++i) {
+        const int i0 = mind(ord - i, i - 1), i1 = mind(ord - i + 1, i - 1), i2 = mind(ord - i, i);
+        T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+          v[n] = (orig[i0] * T(1) + orig[i1] * pt1[n]) + orig[i2] * pt2[n];
+          valD[n] = ((dmask >> n) & 1) ? (ord > 1 ? v[n] : dataV0T[n]) : nan_;
+        }
+        patch_minmax(g, vmm, la, s, vid, valD, mn, mx);
+        aOrd = fmin(aOrd, vertex_alpha(orig[i0], v, mn, mx));
+        ++s;
+      }
+      alpha = fmax(alpha, aOrd);
+#pragma unroll
+      for (int i = ord * (ord + 1) / 2; i < (ord + 1) * (ord + 2) / 2; ++i) cT[i] = alpha * orig[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Stage operator.  MODE 0: write c^(s);  MODE 1: write Taylor(c^(s)) and q;
+// MODE 2: write Taylor(cDot) and q (time-derivative limiting follows).
+struct StageScalars {
+  double omega, tau;
+  double gco[4];        // g_m(t_s) of the source terms
+  int *flag;            // bit 0: non-finite value seen
+  unsigned long long *gmm_reset;   // slots reset by this producer (or null)
+  int nc_reset;
+};
+
+template <typename T, int P, int MODE, bool RHS>
+__global__ void __launch_bounds__(kBlock)
+k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ out,
+           T *__restrict__ q, const LimArgs la, const StageScalars sc) {
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
+  const Tab<T, P> &tb = tab<T, P>();
+  if (sc.gmm_reset && blockIdx.x == 0 && threadIdx.x < 2 * sc.nc_reset)
+    sc.gmm_reset[threadIdx.x] = (threadIdx.x & 1) ? 0ULL : key_max<T>();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.K) return;
+  const int Kp = g.Kp;
+  T c[N], rhs[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) { c[i] = cin[(size_t)i * Kp + k]; rhs[i] = T(0); }
+  if (RHS) {
+    for (int m = 0; m < g.nTerms; ++m) {
+      const T gm = T(sc.gco[m]);
+#pragma unroll
+      for (int i = 0; i < N; ++i) rhs[i] += gm * g.rhs[((size_t)m * N + i) * Kp + k];
+    }
+  }
+  // volume term
+#pragma unroll
+  for (int qq = 0; qq < Q; ++qq) {
+    T cq = T(0);
+#pragma unroll
+    for (int j = 0; j < N; ++j) cq += tb.phiQ[qq][j] * c[j];
+    const T f1 = g.F[(size_t)qq * Kp + k] * cq;
+    const T f2 = g.F[(size_t)(Q + qq) * Kp + k] * cq;
+#pragma unroll
+    for (int i = 0; i < N; ++i) rhs[i] += tb.g1[qq][i] * f1 + tb.g2[qq][i] * f2;
+  }
+  // upwind edge term
+  const int code = g.code[k];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const int nb = g.nbr[(size_t)n * Kp + k];
+    const int np = (code >> (2 * n)) & 3;
+    const bool outOk = (code >> (6 + n)) & 1;
+    T v[R];
+    bool anyIn = false;
+#pragma unroll
+    for (int r = 0; r < R; ++r) { v[r] = g.Vn[(size_t)(n * R + r) * Kp + k]; anyIn |= v[r] < T(0); }
+    T cn[N];
+    const bool gather = anyIn && nb >= 0;
+#pragma unroll
+    for (int j = 0; j < N; ++j) cn[j] = gather ? cin[(size_t)j * Kp + nb] : T(0);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      T tr = T(0);
+      if (v[r] > T(0) && outOk) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r][j] * c[j];
+      } else if (v[r] < T(0) && nb >= 0) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r][j] * cn[j];
+      }
+      const T fl = v[r] * tr;
+#pragma unroll
+      for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r][i] * fl;
+    }
+  }
+  // mass solve
+  T cdot[N];
+  if (sizeof(T) == 8) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T s = T(0);
+#pragma unroll
+      for (int j = 0; j < N; ++j) s += tb.hatMinv[i][j] * rhs[j];
+      cdot[i] = s;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) cdot[i] = rhs[i];
+  }
+  bool bad = false;
+  if (MODE == 2) {
+    const Affine<T> af = load_affine(g, k);
+    T cT[N];
+    to_taylor<T, P>(cdot, af, cT);
+#pragma unroll
+    for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cT[i]; bad |= !finite_(cT[i]); }
+    centroid_quantities<T, P>(cT, la.type, q, k, Kp);
+  } else {
+    const T w = T(sc.omega), tau = T(sc.tau);
+    T cnew[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cnew[i] = w * c0[(size_t)i * Kp + k] + (T(1) - w) * (c[i] + tau * cdot[i]);
+    if (MODE == 0) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+    } else {
+      const Affine<T> af = load_affine(g, k);
+      T cT[N];
+      to_taylor<T, P>(cnew, af, cT);
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cT[i]; bad |= !finite_(cT[i]); }
+      centroid_quantities<T, P>(cT, la.type, q, k, Kp);
+    }
+  }
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Vertex pass: min / max of every centroid quantity over the elements of each vertex patch
+// (CSR vertex -> elements), and the global min / max of each quantity for the shift.
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+k_vertex_minmax(const Geo<T> g, const T *__restrict__ q, int nc, T *__restrict__ vmm,
+                unsigned long long *gmm) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = v < g.numV;
+  int b = 0, e = 0;
+  if (active) { b = g.vptr[v]; e = g.vptr[v + 1]; }
+  for (int s = 0; s < nc; ++s) {
+    T mn = T(INFINITY), mx = T(-INFINITY);
+    const T *qs = q + (size_t)s * g.Kp;
+    for (int i = b; i < e; ++i) {
+      const T x = qs[g.vidx[i]];
+      mn = fmin(mn, x); mx = fmax(mx, x);
+    }
+    if (active) { vmm[(size_t)(2 * s) * g.Vp + v] = mn; vmm[(size_t)(2 * s + 1) * g.Vp + v] = mx; }
+    // block reduction for the global extremes
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0 && mn <= mx) {
+      atomicMin(&gmm[2 * s], okey(mn));
+      atomicMax(&gmm[2 * s + 1], okey(mx));
+    }
+  }
+}
+
+// Time-derivative limiting and SSP update (advection/solveSubStep.m:69-83), then the Taylor
+// form of the new stage value and its centroid quantities for the solution limiter.
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit_dot(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ tbuf,
+            T *__restrict__ q, const T *__restrict__ vmm, const LimArgs laDot, const LimArgs laSol,
+            const StageScalars sc) {
+  constexpr int N = Dims<P>::N, NMT = Dims<P>::NMT;
+  if (sc.gmm_reset && blockIdx.x == 0 && threadIdx.x < 2 * sc.nc_reset)
+    sc.gmm_reset[threadIdx.x] = (threadIdx.x & 1) ? 0ULL : key_max<T>();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.K) return;
+  const int Kp = g.Kp;
+  const Affine<T> af = load_affine(g, k);
+  T cT[N], lim[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) { cT[i] = tbuf[(size_t)i * Kp + k]; lim[i] = cT[i]; }
+  const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
+  const int dmask = (g.code[k] >> 9) & 7;
+  const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
+  limit_taylor<T, P>(g, vmm, laDot, k, af, vid, dmask, nan3, lim);
+  // Taylor mass correction M_corr = diag(1/diag(M_T)) M_T applied to (cT - lim)
+  T d[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) d[i] = cT[i] - lim[i];
+  T cor[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    T s = T(0), dii = T(1);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const int a = i < j ? i : j, b = i < j ? j : i;
+      const int idx = a * N - a * (a - 1) / 2 + (b - a);
+      const T m = g.MT[(size_t)idx * Kp + k];
+      s += m * d[j];
+      if (j == i) dii = m;
+    }
+    cor[i] = lim[i] + s / dii;
+  }
+  (void)NMT;
+  T cdot[N];
+  from_taylor<T, P>(cor, af, cdot);
+  const T w = T(sc.omega), tau = T(sc.tau);
+  T cnew[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    cnew[i] = w * c0[(size_t)i * Kp + k] + (T(1) - w) * (cin[(size_t)i * Kp + k] + tau * cdot[i]);
+  T cT2[N];
+  to_taylor<T, P>(cnew, af, cT2);
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < N; ++i) { tbuf[(size_t)i * Kp + k] = cT2[i]; bad |= !finite_(cT2[i]); }
+  centroid_quantities<T, P>(cT2, laSol.type, q, k, Kp);
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Solution limiter: limited Taylor coefficients back to the modal basis
+// (core/applySlopeLimiterDisc.m:77-86).
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const T *__restrict__ vmm,
+        const LimArgs la, const StageScalars sc) {
+  constexpr int N = Dims<P>::N;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.K) return;
+  const int Kp = g.Kp;
+  const Affine<T> af = load_affine(g, k);
+  T cT[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) cT[i] = tbuf[(size_t)i * Kp + k];
+  const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
+  const int dmask = (g.code[k] >> 9) & 7;
+  T data[3] = {T(0), T(0), T(0)};
+  if (g.cDV0T) {
+    for (int m = 0; m < g.nTerms; ++m) {
+      const T gm = T(sc.gco[m]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
+    }
+  }
+  limit_taylor<T, P>(g, vmm, la, k, af, vid, dmask, data, cT);
+  T c[N];
+  from_taylor<T, P>(cT, af, c);
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = c[i]; bad |= !finite_(c[i]); }
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Modal state -> Taylor form and centroid quantities (initial limiting).
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_to_taylor(const Geo<T> g, const T *__restrict__ c, T *__restrict__ tbuf, T *__restrict__ q,
+            const LimArgs la, const StageScalars sc) {
+  constexpr int N = Dims<P>::N;
+  if (sc.gmm_reset && blockIdx.x == 0 && threadIdx.x < 2 * sc.nc_reset)
+    sc.gmm_reset[threadIdx.x] = (threadIdx.x & 1) ? 0ULL : key_max<T>();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.K) return;
+  const Affine<T> af = load_affine(g, k);
+  T cc[N], cT[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) cc[i] = c[(size_t)i * g.Kp + k];
+  to_taylor<T, P>(cc, af, cT);
+#pragma unroll
+  for (int i = 0; i < N; ++i) tbuf[(size_t)i * g.Kp + k] = cT[i];
+  centroid_quantities<T, P>(cT, la.type, q, k, g.Kp);
+}
+
+// External (caller order, K x N column-major, FP64) <-> internal (SoA, stride Kp, precision T).
+template <typename T>
+__global__ void k_scatter_in(int K, int Kp, int N, const int *__restrict__ perm,
+                             const double *__restrict__ ext, T *__restrict__ c) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  const int e = perm[k];
+  for (int i = 0; i < N; ++i) c[(size_t)i * Kp + k] = T(ext[(size_t)i * K + e]);
+}
+template <typename T>
+__global__ void k_gather_out(int K, int Kp, int N, const int *__restrict__ perm,
+                             const T *__restrict__ c, double *__restrict__ ext) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  const int e = perm[k];
+  for (int i = 0; i < N; ++i) ext[(size_t)i * K + e] = double(c[(size_t)i * Kp + k]);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Host side.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace dgadv
+
+struct dgadv_handle {
+  int device = 0;
+  int K = 0, Kp = 0, numV = 0, Vp = 0, p = 0, N = 0, Q = 0, R = 0, ordRK = 1, prec = 0;
+  int lim = 0, limType = 0, flags = 0, nc = 0;
+  bool limdot = false;
+  cudaStream_t stream = nullptr;
+  std::vector<void *> allocs;
+  // device arrays (element type depends on prec)
+  void *F = nullptr, *Vn = nullptr, *Bm = nullptr, *MT = nullptr, *rhs = nullptr, *cDV0T = nullptr;
+  int *nbr = nullptr, *code = nullptr, *V0T = nullptr, *vptr = nullptr, *vidx = nullptr, *perm = nullptr;
+  void *cn = nullptr, *cA = nullptr, *cB = nullptr, *tbuf = nullptr, *q = nullptr, *vmm = nullptr;
+  unsigned long long *gmm = nullptr;   // 2 sets x 2 x nc
+  int *flag = nullptr;
+  double *stage_ext = nullptr;         // K x N staging for set/get state
+  int nTerms = 0;
+  int timeFn[4] = {0, 0, 0, 0};
+  bool hasVelocity = false;
+  // host copies needed later
+  std::vector<double> detJ, areaE0T, Bhost;   // internal order
+  std::vector<uint8_t> markNotN;              // internal order, 3 per element
+  std::vector<int> permv;                     // internal -> external element id
+  dgadv::RefTables tables;
+  // CUDA graph of one step
+  cudaGraphExec_t graph = nullptr;
+  double graphTau = -1.0;
+  int graphSteps = 0;
+  std::string err;
+};
+
+namespace dgadv {
+
+static std::mutex g_tab_mutex;
+static bool g_tab_loaded[64][2][kMaxP + 1];
+
+template <typename T, int P>
+static cudaError_t upload_tables(const RefTables &rt) {
+  Tab<T, P> t;
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
+  for (int q = 0; q < Q; ++q)
+    for (int i = 0; i < N; ++i) {
+      t.phiQ[q][i] = T(rt.phiQ[q * N + i]);
+      t.g1[q][i] = T(rt.gradQ[q * N + i]);
+      t.g2[q][i] = T(rt.gradQ[Q * N + q * N + i]);
+    }
+  for (int n = 0; n < 3; ++n)
+    for (int r = 0; r < R; ++r)
+      for (int i = 0; i < N; ++i) t.phi1D[n][r][i] = T(rt.phi1D[(n * R + r) * N + i]);
+  for (int nn = 0; nn < 3; ++nn)
+    for (int np = 0; np < 3; ++np)
+      for (int r = 0; r < R; ++r)
+        for (int i = 0; i < N; ++i) t.thetaPhi[nn][np][r][i] = T(rt.thetaPhi[((nn * 3 + np) * R + r) * N + i]);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      t.hatMinv[i][j] = T(rt.hatMinv[i * N + j]);
+      t.DM[i][j] = T(rt.DM[i * N + j]);
+      t.DMinv[i][j] = T(rt.DMinv[i * N + j]);
+    }
+  const void *sym = nullptr;
+  if (std::is_same<T, double>::value) {
+    if (P == 0) sym = &cTd0; else if (P == 1) sym = &cTd1; else if (P == 2) sym = &cTd2; else sym = &cTd3;
+  } else {
+    if (P == 0) sym = &cTf0; else if (P == 1) sym = &cTf1; else if (P == 2) sym = &cTf2; else sym = &cTf3;
+  }
+  return cudaMemcpyToSymbol(sym, &t, sizeof(t));
+}
+
+template <typename T>
+static Geo<T> make_geo(const dgadv_handle *h) {
+  Geo<T> g;
+  g.K = h->K; g.Kp = h->Kp; g.numV = h->numV; g.Vp = h->Vp;
+  g.F = (const T *)h->F; g.Vn = (const T *)h->Vn; g.nbr = h->nbr; g.code = h->code;
+  g.Bm = (const T *)h->Bm; g.MT = (const T *)h->MT; g.V0T = h->V0T; g.vptr = h->vptr; g.vidx = h->vidx;
+  g.rhs = (const T *)h->rhs; g.cDV0T = (const T *)h->cDV0T; g.nTerms = h->nTerms;
+  for (int i = 0; i < 4; ++i) g.timeFn[i] = h->timeFn[i];
+  return g;
+}
+
+static double time_factor(int fn, double t) { return fn == DGADV_TIME_EXP_NEG ? std::exp(-t) : 1.0; }
+
+// SSP-RK tables (core/rungeKuttaExplicit.m:64-78)
+static int rk_table(int ord, double omega[3], double cstage[3]) {
+  if (ord == 1) { omega[0] = 0; cstage[0] = 0; return 1; }
+  if (ord == 2) { omega[0] = 0; omega[1] = 0.5; cstage[0] = 0; cstage[1] = 1; return 2; }
+  omega[0] = 0; omega[1] = 3.0 / 4.0; omega[2] = 1.0 / 3.0;
+  cstage[0] = 0; cstage[1] = 1; cstage[2] = 0.5;
+  return 3;
+}
+
+template <typename T, int P>
+static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
+  const Geo<T> g = make_geo<T>(h);
+  const int grid = (h->K + kBlock - 1) / kBlock;
+  const int vgrid = (h->numV + kBlock - 1) / kBlock;
+  double omega[3], cst[3];
+  const int S = rk_table(h->ordRK, omega, cst);
+  T *cn = (T *)h->cn, *cA = (T *)h->cA, *cB = (T *)h->cB, *tb = (T *)h->tbuf, *q = (T *)h->q;
+  T *vmm = (T *)h->vmm;
+  unsigned long long *gmmDot = h->gmm, *gmmSol = h->gmm + 2 * h->nc;
+  LimArgs laDot{h->limType, h->nc, (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1, gmmDot};
+  LimArgs laSol{h->limType, h->nc, (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1, gmmSol};
+  const bool rhs = h->nTerms > 0 && h->rhs;
+  for (int s = 0; s < S; ++s) {
+    T *in = (s == 0) ? cn : (s == 1 ? cA : cB);
+    T *out = (s == S - 1) ? (S == 1 ? cA : cn) : (s == 0 ? cA : cB);
+    StageScalars sc{};
+    sc.omega = omega[s]; sc.tau = tau; sc.flag = h->flag;
+    const double ts = t0 + cst[s] * tau;
+    for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = time_factor(h->timeFn[m], ts);
+    if (!h->lim) {
+      if (rhs) k_stage_op<T, P, 0, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, out, q, laSol, sc);
+      else k_stage_op<T, P, 0, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, out, q, laSol, sc);
+    } else {
+      // limiter boundary data at tBC = t(s+1) or t(1) + tau (advection/solveSubStep.m:88)
+      const double tBC = (s + 1 < S) ? t0 + cst[s + 1] * tau : t0 + tau;
+      StageScalars scBC = sc;
+      for (int m = 0; m < h->nTerms; ++m) scBC.gco[m] = time_factor(h->timeFn[m], tBC);
+      scBC.gmm_reset = nullptr;
+      if (h->limdot) {
+        StageScalars s1 = sc; s1.gmm_reset = gmmDot; s1.nc_reset = h->nc;
+        if (rhs) k_stage_op<T, P, 2, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, laDot, s1);
+        else k_stage_op<T, P, 2, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, laDot, s1);
+        k_vertex_minmax<T><<<vgrid, kBlock, 0, h->stream>>>(g, q, h->nc, vmm, gmmDot);
+        StageScalars s2 = sc; s2.gmm_reset = gmmSol; s2.nc_reset = h->nc;
+        k_limit_dot<T, P><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, vmm, laDot, laSol, s2);
+      } else {
+        StageScalars s1 = sc; s1.gmm_reset = gmmSol; s1.nc_reset = h->nc;
+        if (rhs) k_stage_op<T, P, 1, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, laSol, s1);
+        else k_stage_op<T, P, 1, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, laSol, s1);
+      }
+      k_vertex_minmax<T><<<vgrid, kBlock, 0, h->stream>>>(g, q, h->nc, vmm, gmmSol);
+      k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, tb, out, vmm, laSol, scBC);
+    }
+  }
+  if (S == 1)
+    cudaMemcpyAsync(cn, cA, (size_t)h->N * h->Kp * sizeof(T), cudaMemcpyDeviceToDevice, h->stream);
+  return cudaGetLastError();
+}
+
+template <typename T, int P>
+static cudaError_t launch_limit_state(dgadv_handle *h, double t) {
+  const Geo<T> g = make_geo<T>(h);
+  const int grid = (h->K + kBlock - 1) / kBlock;
+  const int vgrid = (h->numV + kBlock - 1) / kBlock;
+  unsigned long long *gmmSol = h->gmm + 2 * h->nc;
+  LimArgs la{h->limType, h->nc, (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1, gmmSol};
+  StageScalars sc{};
+  sc.flag = h->flag;
+  for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = time_factor(h->timeFn[m], t);
+  StageScalars s1 = sc; s1.gmm_reset = gmmSol; s1.nc_reset = h->nc;
+  k_to_taylor<T, P><<<grid, kBlock, 0, h->stream>>>(g, (const T *)h->cn, (T *)h->tbuf, (T *)h->q, la, s1);
+  k_vertex_minmax<T><<<vgrid, kBlock, 0, h->stream>>>(g, (const T *)h->q, h->nc, (T *)h->vmm, gmmSol);
+  k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, (const T *)h->tbuf, (T *)h->cn, (const T *)h->vmm, la, sc);
+  return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t dispatch_step(dgadv_handle *h, double t0, double tau) {
+  switch (h->p) {
+    case 0: return launch_step<T, 0>(h, t0, tau);
+    case 1: return launch_step<T, 1>(h, t0, tau);
+    case 2: return launch_step<T, 2>(h, t0, tau);
+    default: return launch_step<T, 3>(h, t0, tau);
+  }
+}
+template <typename T>
+static cudaError_t dispatch_limit(dgadv_handle *h, double t) {
+  switch (h->p) {
+    case 1: return launch_limit_state<T, 1>(h, t);
+    case 2: return launch_limit_state<T, 2>(h, t);
+    default: return launch_limit_state<T, 3>(h, t);
+  }
+}
+
+}  // namespace dgadv
+
+// ---------------------------------------------------------------------------------------------
+// C-ABI
+using namespace dgadv;
+
+#define DG_CUDA(call)                                                               \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);                  \
+      return DGADV_ECUDA;                                                           \
+    }                                                                               \
+  } while (0)
+
+static int dev_alloc(dgadv_handle *h, void **p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) { h->err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return DGADV_ENOMEM; }
+  h->allocs.push_back(*p);
+  return DGADV_OK;
+}
+
+static int upload(dgadv_handle *h, void *dst, const void *src, size_t bytes) {
+  DG_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+  return DGADV_OK;
+}
+
+template <typename T>
+static int upload_real(dgadv_handle *h, void *dst, const std::vector<double> &src) {
+  if (sizeof(T) == 8) return upload(h, dst, src.data(), src.size() * sizeof(double));
+  std::vector<float> tmp(src.size());
+  for (size_t i = 0; i < src.size(); ++i) tmp[i] = (float)src[i];
+  return upload(h, dst, tmp.data(), tmp.size() * sizeof(float));
+}
+
+static uint32_t morton2(uint32_t x, uint32_t y) {
+  auto spread = [](uint32_t v) {
+    v &= 0xFFFF;
+    v = (v | (v << 8)) & 0x00FF00FF;
+    v = (v | (v << 4)) & 0x0F0F0F0F;
+    v = (v | (v << 2)) & 0x33333333;
+    v = (v | (v << 1)) & 0x55555555;
+    return v;
+  };
+  return spread(x) | (spread(y) << 1);
+}
+
+extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dgadv_handle **out) {
+  if (!out) return DGADV_EINVAL;
+  *out = nullptr;
+  if (!mesh || !prm) return DGADV_EINVAL;
+  if (prm->p < 0 || prm->p > 4 || prm->ordRK < 1 || prm->ordRK > 3) return DGADV_EINVAL;
+  if (prm->precision != DGADV_FP64 && prm->precision != DGADV_FP32) return DGADV_EINVAL;
+  if (prm->isSlopeLim && prm->p < 1) return DGADV_EINVAL;
+  if (prm->p > kMaxP) return DGADV_EUNSUPPORTED;
+  if (prm->isSlopeLim && prm->typeSlopeLim != DGADV_LIM_LINEAR && prm->typeSlopeLim != DGADV_LIM_HIERARCH_VERT)
+    return prm->typeSlopeLim == DGADV_LIM_STRICT ? DGADV_EUNSUPPORTED : DGADV_EINVAL;
+  dgadv_handle *h = new (std::nothrow) dgadv_handle();
+  if (!h) return DGADV_ENOMEM;
+  *out = h;
+  h->device = prm->device;
+  h->p = prm->p; h->N = N_of_p(prm->p); h->ordRK = prm->ordRK; h->prec = prm->precision;
+  h->lim = prm->isSlopeLim ? 1 : 0; h->limType = prm->typeSlopeLim; h->flags = prm->flags;
+  h->limdot = h->lim && h->p > 1;
+  h->nc = h->lim ? (h->limType == DGADV_LIM_LINEAR ? 1 : h->p * (h->p + 1) / 2) : 1;
+  DG_CUDA(cudaSetDevice(h->device));
+  DG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  // static grid data (core/generateGridData.m semantics)
+  Grid gr;
+  if (!build_grid(mesh->numV, mesh->coordV, mesh->numT, mesh->V0T, gr, h->err)) return DGADV_EMESH;
+  if (!build_ref_tables(h->p, h->tables, h->err)) return DGADV_EINVAL;
+  const int K = gr.numT, N = h->N;
+  h->K = K; h->Kp = (K + 63) / 64 * 64; h->numV = gr.numV; h->Vp = (gr.numV + 63) / 64 * 64;
+  h->Q = h->tables.Q; h->R = h->tables.R;
+  const int Kp = h->Kp;
+  // element order on the device: Morton order of the barycentres
+  std::vector<int> perm(K);
+  std::iota(perm.begin(), perm.end(), 0);
+  if (!(h->flags & DGADV_FLAG_NO_REORDER)) {
+    double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+    for (int t = 0; t < K; ++t) {
+      xmin = std::min(xmin, gr.baryT[2 * t]); xmax = std::max(xmax, gr.baryT[2 * t]);
+      ymin = std::min(ymin, gr.baryT[2 * t + 1]); ymax = std::max(ymax, gr.baryT[2 * t + 1]);
+    }
+    const double sx = 65535.0 / std::max(xmax - xmin, 1e-300), sy = 65535.0 / std::max(ymax - ymin, 1e-300);
+    std::vector<uint32_t> key(K);
+    for (int t = 0; t < K; ++t)
+      key[t] = morton2((uint32_t)((gr.baryT[2 * t] - xmin) * sx), (uint32_t)((gr.baryT[2 * t + 1] - ymin) * sy));
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return key[a] < key[b]; });
+  }
+  std::vector<int> inv(K);
+  for (int k = 0; k < K; ++k) inv[perm[k]] = k;
+  h->permv = perm;
+  // vertex ids renumbered by first appearance in the device element order
+  std::vector<int> vnew(gr.numV, -1);
+  int nv = 0;
+  for (int k = 0; k < K; ++k)
+    for (int n = 0; n < 3; ++n) {
+      const int v = gr.V0T[3 * (size_t)perm[k] + n];
+      if (vnew[v] < 0) vnew[v] = nv++;
+    }
+  h->numV = nv; h->Vp = (nv + 63) / 64 * 64;
+  // boundary markers
+  std::vector<uint8_t> bdrD(3 * (size_t)K), bdrN(3 * (size_t)K, 0), idOk(3 * (size_t)K, 1);
+  for (int t = 0; t < K; ++t)
+    for (int n = 0; n < 3; ++n) {
+      const int e = gr.E0T[3 * (size_t)t + n];
+      const bool interior = gr.T0E[2 * (size_t)e + 1] >= 0;
+      const size_t cm = (size_t)n * K + t;
+      if (mesh->markE0TbdrN) bdrN[3 * (size_t)t + n] = mesh->markE0TbdrN[cm] ? 1 : 0;
+      if (mesh->markE0TbdrD) bdrD[3 * (size_t)t + n] = mesh->markE0TbdrD[cm] ? 1 : 0;
+      else bdrD[3 * (size_t)t + n] = (!interior && !bdrN[3 * (size_t)t + n]) ? 1 : 0;
+      if (mesh->idE0T) idOk[3 * (size_t)t + n] = (interior || mesh->idE0T[cm] != 0) ? 1 : 0;
+    }
+  // markV0TbdrD: vertices of Dirichlet edges (advection/preprocessProblem.m:75-76)
+  std::vector<uint8_t> vD(gr.numV, 0);
+  for (int t = 0; t < K; ++t)
+    for (int n = 0; n < 3; ++n)
+      if (bdrD[3 * (size_t)t + n]) {
+        const int e = gr.E0T[3 * (size_t)t + n];
+        vD[gr.V0E[2 * (size_t)e]] = 1; vD[gr.V0E[2 * (size_t)e + 1]] = 1;
+      }
+  // per-element device arrays (internal order)
+  std::vector<int> nbr(3 * (size_t)Kp, -1), code(Kp, 0), V0T(3 * (size_t)Kp, 0);
+  h->detJ.assign(K, 0); h->areaE0T.assign(3 * (size_t)K, 0); h->Bhost.assign(4 * (size_t)K, 0);
+  h->markNotN.assign(3 * (size_t)K, 0);
+  std::vector<double> Bsoa(4 * (size_t)Kp, 0.0);
+  for (int k = 0; k < K; ++k) {
+    const int t = perm[k];
+    int cd = 0;
+    for (int n = 0; n < 3; ++n) {
+      const int e = gr.E0T[3 * (size_t)t + n];
+      int other = gr.T0E[2 * (size_t)e] == t ? gr.T0E[2 * (size_t)e + 1] : gr.T0E[2 * (size_t)e];
+      int np = gr.T0E[2 * (size_t)e] == t ? gr.E0E[2 * (size_t)e + 1] : gr.E0E[2 * (size_t)e];
+      if (other < 0) np = 3;
+      nbr[(size_t)n * Kp + k] = other >= 0 ? inv[other] : -1;
+      cd |= (np & 3) << (2 * n);
+      if (idOk[3 * (size_t)t + n]) cd |= 1 << (6 + n);
+      if (vD[gr.V0T[3 * (size_t)t + n]]) cd |= 1 << (9 + n);
+      V0T[(size_t)n * Kp + k] = vnew[gr.V0T[3 * (size_t)t + n]];
+      h->areaE0T[3 * (size_t)k + n] = gr.areaE0T[3 * (size_t)t + n];
+      h->markNotN[3 * (size_t)k + n] = bdrN[3 * (size_t)t + n] ? 0 : 1;
+    }
+    code[k] = cd;
+    h->detJ[k] = gr.detJ0T[t];
+    for (int i = 0; i < 4; ++i) { Bsoa[(size_t)i * Kp + k] = gr.B[4 * (size_t)t + i]; h->Bhost[4 * (size_t)k + i] = gr.B[4 * (size_t)t + i]; }
+  }
+  // CSR vertex -> elements (internal ids)
+  std::vector<int> vptr(h->numV + 1, 0), vidx(3 * (size_t)K);
+  for (int k = 0; k < K; ++k)
+    for (int n = 0; n < 3; ++n) vptr[V0T[(size_t)n * Kp + k] + 1]++;
+  for (int v = 0; v < h->numV; ++v) vptr[v + 1] += vptr[v];
+  {
+    std::vector<int> fill(vptr.begin(), vptr.end() - 1);
+    for (int k = 0; k < K; ++k)
+      for (int n = 0; n < 3; ++n) vidx[fill[V0T[(size_t)n * Kp + k]]++] = k;
+  }
+  const size_t w = h->prec == DGADV_FP64 ? 8 : 4;
+  int st;
+  const int Q = h->Q, R = h->R, nc = h->nc;
+  if ((st = dev_alloc(h, &h->F, 2 * (size_t)Q * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->Vn, 3 * (size_t)R * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->Bm, 4 * (size_t)Kp * w))) return st;
+  if ((st = dev_alloc(h, (void **)&h->nbr, 3 * (size_t)Kp * 4))) return st;
+  if ((st = dev_alloc(h, (void **)&h->code, (size_t)Kp * 4))) return st;
+  if ((st = dev_alloc(h, (void **)&h->V0T, 3 * (size_t)Kp * 4))) return st;
+  if ((st = dev_alloc(h, (void **)&h->vptr, (size_t)(h->numV + 1) * 4))) return st;
+  if ((st = dev_alloc(h, (void **)&h->vidx, 3 * (size_t)K * 4))) return st;
+  if ((st = dev_alloc(h, (void **)&h->perm, (size_t)K * 4))) return st;
+  if ((st = dev_alloc(h, &h->cn, (size_t)N * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->cA, (size_t)N * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->cB, (size_t)N * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->tbuf, (size_t)N * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->q, (size_t)nc * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->vmm, 2 * (size_t)nc * h->Vp * w))) return st;
+  if ((st = dev_alloc(h, (void **)&h->gmm, 4 * (size_t)nc * 8))) return st;
+  if ((st = dev_alloc(h, (void **)&h->flag, 16))) return st;
+  if ((st = dev_alloc(h, (void **)&h->stage_ext, (size_t)N * K * 8))) return st;
+  DG_CUDA(cudaMemset(h->F, 0, 2 * (size_t)Q * Kp * w));
+  DG_CUDA(cudaMemset(h->Vn, 0, 3 * (size_t)R * Kp * w));
+  DG_CUDA(cudaMemset(h->cn, 0, (size_t)N * Kp * w));
+  DG_CUDA(cudaMemset(h->cA, 0, (size_t)N * Kp * w));
+  DG_CUDA(cudaMemset(h->cB, 0, (size_t)N * Kp * w));
+  DG_CUDA(cudaMemset(h->tbuf, 0, (size_t)N * Kp * w));
+  DG_CUDA(cudaMemset(h->q, 0, (size_t)nc * Kp * w));
+  DG_CUDA(cudaMemset(h->flag, 0, 16));
+  if (h->prec == DGADV_FP64) { if ((st = upload_real<double>(h, h->Bm, Bsoa))) return st; }
+  else { if ((st = upload_real<float>(h, h->Bm, Bsoa))) return st; }
+  if ((st = upload(h, h->nbr, nbr.data(), nbr.size() * 4))) return st;
+  if ((st = upload(h, h->code, code.data(), code.size() * 4))) return st;
+  if ((st = upload(h, h->V0T, V0T.data(), V0T.size() * 4))) return st;
+  if ((st = upload(h, h->vptr, vptr.data(), vptr.size() * 4))) return st;
+  if ((st = upload(h, h->vidx, vidx.data(), vidx.size() * 4))) return st;
+  if ((st = upload(h, h->perm, perm.data(), perm.size() * 4))) return st;
+  if (h->limdot) {
+    std::vector<double> mt;
+    taylor_mass_packed(gr, h->p, mt);
+    const int NMT = N * (N + 1) / 2;
+    std::vector<double> soa((size_t)NMT * Kp, 0.0);
+    for (int k = 0; k < K; ++k)
+      for (int i = 0; i < NMT; ++i) soa[(size_t)i * Kp + k] = mt[(size_t)perm[k] * NMT + i];
+    if ((st = dev_alloc(h, &h->MT, soa.size() * w))) return st;
+    if (h->prec == DGADV_FP64) { if ((st = upload_real<double>(h, h->MT, soa))) return st; }
+    else { if ((st = upload_real<float>(h, h->MT, soa))) return st; }
+  }
+  // constant tables (once per device, precision and degree)
+  {
+    std::lock_guard<std::mutex> lk(g_tab_mutex);
+    const int pi = h->prec == DGADV_FP64 ? 0 : 1;
+    if (h->device < 0 || h->device >= 64) { h->err = "device ordinal out of range"; return DGADV_EINVAL; }
+    if (!g_tab_loaded[h->device][pi][h->p]) {
+      cudaError_t e = cudaSuccess;
+      if (pi == 0) {
+        switch (h->p) { case 0: e = upload_tables<double, 0>(h->tables); break; case 1: e = upload_tables<double, 1>(h->tables); break;
+                        case 2: e = upload_tables<double, 2>(h->tables); break; default: e = upload_tables<double, 3>(h->tables); }
+      } else {
+        switch (h->p) { case 0: e = upload_tables<float, 0>(h->tables); break; case 1: e = upload_tables<float, 1>(h->tables); break;
+                        case 2: e = upload_tables<float, 2>(h->tables); break; default: e = upload_tables<float, 3>(h->tables); }
+      }
+      if (e != cudaSuccess) { h->err = std::string("table upload: ") + cudaGetErrorString(e); return DGADV_ECUDA; }
+      g_tab_loaded[h->device][pi][h->p] = true;
+    }
+  }
+  DG_CUDA(cudaDeviceSynchronize());
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_set_velocity(dgadv_handle *h, const double *u1, const double *u2, const double *vN) {
+  if (!h || !u1 || !u2 || !vN) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  const int K = h->K, Kp = h->Kp, N = h->N, Q = h->Q, R = h->R;
+  const RefTables &t = h->tables;
+  std::vector<double> F(2 * (size_t)Q * Kp, 0.0), Vn(3 * (size_t)R * Kp, 0.0);
+  for (int k = 0; k < K; ++k) {
+    const int e = h->permv[k];
+    const double B11 = h->Bhost[4 * (size_t)k], B12 = h->Bhost[4 * (size_t)k + 1];
+    const double B21 = h->Bhost[4 * (size_t)k + 2], B22 = h->Bhost[4 * (size_t)k + 3];
+    const double dj = h->detJ[k];
+    for (int q = 0; q < Q; ++q) {
+      double a = 0, b = 0;
+      for (int l = 0; l < N; ++l) {
+        a += t.phiQ[q * N + l] * u1[(size_t)l * K + e];
+        b += t.phiQ[q * N + l] * u2[(size_t)l * K + e];
+      }
+      F[(size_t)q * Kp + k] = t.vol.W[q] * (B22 * a - B12 * b) / dj;
+      F[(size_t)(Q + q) * Kp + k] = t.vol.W[q] * (B11 * b - B21 * a) / dj;
+    }
+    for (int n = 0; n < 3; ++n)
+      for (int r = 0; r < R; ++r) {
+        const double v = vN[(size_t)e + (size_t)K * n + (size_t)3 * K * r];
+        Vn[(size_t)(n * R + r) * Kp + k] =
+            h->markNotN[3 * (size_t)k + n] ? h->areaE0T[3 * (size_t)k + n] * t.edge.W[r] * v / dj : 0.0;
+      }
+  }
+  int st;
+  if (h->prec == DGADV_FP64) {
+    if ((st = upload_real<double>(h, h->F, F))) return st;
+    if ((st = upload_real<double>(h, h->Vn, Vn))) return st;
+  } else {
+    if ((st = upload_real<float>(h, h->F, F))) return st;
+    if ((st = upload_real<float>(h, h->Vn, Vn))) return st;
+  }
+  h->hasVelocity = true;
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_set_source_terms(dgadv_handle *h, int32_t nTerms, const int32_t *timeFn,
+                                      const double *rhsTerms, const double *cDV0T) {
+  if (!h || nTerms < 0 || nTerms > 4) return DGADV_EINVAL;
+  if (nTerms > 0 && (!timeFn || !rhsTerms)) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  const int K = h->K, Kp = h->Kp, N = h->N;
+  const size_t w = h->prec == DGADV_FP64 ? 8 : 4;
+  for (int m = 0; m < nTerms; ++m)
+    if (timeFn[m] != DGADV_TIME_CONST && timeFn[m] != DGADV_TIME_EXP_NEG) return DGADV_EINVAL;
+  h->nTerms = nTerms;
+  for (int m = 0; m < 4; ++m) h->timeFn[m] = m < nTerms ? timeFn[m] : 0;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  if (nTerms == 0) return DGADV_OK;
+  std::vector<double> r((size_t)nTerms * N * Kp, 0.0), d((size_t)nTerms * 3 * Kp, 0.0);
+  for (int m = 0; m < nTerms; ++m)
+    for (int k = 0; k < K; ++k) {
+      const int e = h->permv[k];
+      for (int i = 0; i < N; ++i)
+        r[((size_t)m * N + i) * Kp + k] = rhsTerms[(size_t)m * K * N + (size_t)i * K + e] / h->detJ[k];
+      if (cDV0T)
+        for (int n = 0; n < 3; ++n) d[((size_t)m * 3 + n) * Kp + k] = cDV0T[(size_t)m * K * 3 + (size_t)n * K + e];
+    }
+  int st;
+  if (!h->rhs && (st = dev_alloc(h, &h->rhs, 4 * (size_t)N * Kp * w))) return st;
+  if (cDV0T && !h->cDV0T && (st = dev_alloc(h, &h->cDV0T, 4 * (size_t)3 * Kp * w))) return st;
+  if (h->prec == DGADV_FP64) {
+    if ((st = upload_real<double>(h, h->rhs, r))) return st;
+    if (cDV0T && (st = upload_real<double>(h, h->cDV0T, d))) return st;
+  } else {
+    if ((st = upload_real<float>(h, h->rhs, r))) return st;
+    if (cDV0T && (st = upload_real<float>(h, h->cDV0T, d))) return st;
+  }
+  if (!cDV0T && h->cDV0T) DG_CUDA(cudaMemset(h->cDV0T, 0, 4 * (size_t)3 * Kp * w));
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_set_state(dgadv_handle *h, const double *c) {
+  if (!h || !c) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  DG_CUDA(cudaMemcpyAsync(h->stage_ext, c, (size_t)h->N * h->K * 8, cudaMemcpyHostToDevice, h->stream));
+  const int grid = (h->K + 255) / 256;
+  if (h->prec == DGADV_FP64)
+    k_scatter_in<double><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, h->stage_ext, (double *)h->cn);
+  else
+    k_scatter_in<float><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, h->stage_ext, (float *)h->cn);
+  DG_CUDA(cudaGetLastError());
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_sync(dgadv_handle *h) {
+  if (!h) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  int flag = 0;
+  DG_CUDA(cudaMemcpy(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag & 1) { h->err = "non-finite value in the state"; return DGADV_ENONFINITE; }
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_get_state(dgadv_handle *h, double *c) {
+  if (!h || !c) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  const int grid = (h->K + 255) / 256;
+  if (h->prec == DGADV_FP64)
+    k_gather_out<double><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, (const double *)h->cn, h->stage_ext);
+  else
+    k_gather_out<float><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, (const float *)h->cn, h->stage_ext);
+  DG_CUDA(cudaGetLastError());
+  DG_CUDA(cudaMemcpyAsync(c, h->stage_ext, (size_t)h->N * h->K * 8, cudaMemcpyDeviceToHost, h->stream));
+  return dgadv_sync(h);
+}
+
+extern "C" int dgadv_limit_state(dgadv_handle *h, double t) {
+  if (!h) return DGADV_EINVAL;
+  if (!h->lim) { h->err = "limiter is off for this handle"; return DGADV_EINVAL; }
+  DG_CUDA(cudaSetDevice(h->device));
+  cudaError_t e = h->prec == DGADV_FP64 ? dispatch_limit<double>(h, t) : dispatch_limit<float>(h, t);
+  if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
+  return dgadv_sync(h);
+}
+
+static bool time_dependent(const dgadv_handle *h) {
+  for (int m = 0; m < h->nTerms; ++m)
+    if (h->timeFn[m] != DGADV_TIME_CONST) return true;
+  return false;
+}
+
+extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau) {
+  if (!h || nSteps < 0 || !(tau > 0)) return DGADV_EINVAL;
+  if (!h->hasVelocity) { if (h) h->err = "dgadv_set_velocity was not called"; return DGADV_EINVAL; }
+  DG_CUDA(cudaSetDevice(h->device));
+  const bool useGraph = !(h->flags & DGADV_FLAG_NO_GRAPH) && !time_dependent(h);
+  if (!useGraph) {
+    for (int s = 0; s < nSteps; ++s) {
+      const double t0 = (double)(nStep0 + s) * tau;   // (nStep - 1) * tau
+      cudaError_t e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, t0, tau) : dispatch_step<float>(h, t0, tau);
+      if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
+    }
+    return DGADV_OK;
+  }
+  // time-independent data: one captured graph of several steps, replayed
+  const int chunk = 10;
+  if (!h->graph || h->graphTau != tau) {
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    cudaGraph_t gph;
+    DG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int s = 0; s < chunk && e == cudaSuccess; ++s)
+      e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, 0.0, tau) : dispatch_step<float>(h, 0.0, tau);
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &gph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+      return DGADV_ECUDA;
+    }
+    DG_CUDA(cudaGraphInstantiate(&h->graph, gph, 0));
+    cudaGraphDestroy(gph);
+    h->graphTau = tau;
+    h->graphSteps = chunk;
+  }
+  int done = 0;
+  while (nSteps - done >= h->graphSteps) {
+    DG_CUDA(cudaGraphLaunch(h->graph, h->stream));
+    done += h->graphSteps;
+  }
+  for (; done < nSteps; ++done) {
+    cudaError_t e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, 0.0, tau) : dispatch_step<float>(h, 0.0, tau);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
+  }
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count) {
+  if (!h || !count) return DGADV_EINVAL;
+  const int S = h->ordRK;
+  int perStage = 1;
+  if (h->lim) perStage = h->limdot ? 5 : 3;
+  *count = S * perStage + (S == 1 ? 0 : 0);
+  return DGADV_OK;
+}
+
+extern "C" const char *dgadv_last_error(const dgadv_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+extern "C" void dgadv_destroy(dgadv_handle *h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (void *p : h->allocs) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}

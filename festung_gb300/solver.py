@@ -1,0 +1,111 @@
+"""Python handle over the C-ABI device solver (``dgadv_*`` in ``include/dgadv.h``)."""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+
+class DeviceSolver:
+    """One mesh + one configuration on one GPU.
+
+    Arrays use the reference's shapes: ``cDisc`` K x N, ``u1Disc``/``u2Disc`` K x N,
+    ``vNormalOnQuadEdge`` K x 3 x R.
+    """
+
+    def __init__(self, coordV, V0T, p, ordRK, precision='fp64', isSlopeLim=False,
+                 typeSlopeLim='linear', idE0T=None, markE0TbdrD=None, markE0TbdrN=None,
+                 device=0, flags=0):
+        self._lib = L.load()
+        self._h = None
+        self.coordV = L.f64(coordV)
+        self.V0T = np.require(np.asarray(V0T, dtype=np.int32), requirements=['F', 'A'])
+        self.K = self.V0T.shape[0]
+        self.N = (p + 1) * (p + 2) // 2
+        self.p = p
+        keep = [self.coordV, self.V0T]
+        mesh = L.Mesh()
+        mesh.numT = self.K
+        mesh.numV = self.coordV.shape[0]
+        mesh.coordV = L.ptr(self.coordV)
+        mesh.V0T = L.ptr(self.V0T, L._i32p)
+        if idE0T is not None:
+            a = np.require(np.asarray(idE0T, dtype=np.int32), requirements=['F', 'A']); keep.append(a)
+            mesh.idE0T = L.ptr(a, L._i32p)
+        for name, m in (('markE0TbdrD', markE0TbdrD), ('markE0TbdrN', markE0TbdrN)):
+            if m is not None:
+                a = np.require(np.asarray(m, dtype=np.uint8), requirements=['F', 'A']); keep.append(a)
+                setattr(mesh, name, L.ptr(a, L._u8p))
+        prm = L.Params()
+        prm.p = p; prm.ordRK = ordRK
+        prm.precision = {'fp64': L.FP64, 'fp32': L.FP32}[precision]
+        prm.isSlopeLim = 1 if isSlopeLim else 0
+        prm.typeSlopeLim = L.LIMITER_TYPES[typeSlopeLim]
+        prm.device = device; prm.flags = flags
+        h = ctypes.c_void_p()
+        st = self._lib.dgadv_create(ctypes.byref(mesh), ctypes.byref(prm), ctypes.byref(h))
+        self._h = h.value
+        if st != L.DGADV_OK:
+            try:
+                L.check(st, self._h)
+            finally:
+                self.close()
+
+    # -------------------------------------------------------------------------------------
+    def _c(self, st):
+        L.check(st, self._h)
+
+    def set_velocity(self, u1Disc, u2Disc, vNormalOnQuadEdge):
+        u1, u2, vn = L.f64(u1Disc), L.f64(u2Disc), L.f64(vNormalOnQuadEdge)
+        assert u1.shape == (self.K, self.N) and u2.shape == (self.K, self.N)
+        assert vn.shape[:2] == (self.K, 3)
+        self._c(self._lib.dgadv_set_velocity(self._h, L.ptr(u1), L.ptr(u2), L.ptr(vn)))
+
+    def set_source_terms(self, timeFn, rhsTerms, cDV0T=None):
+        n = len(timeFn)
+        tf = np.asarray(timeFn, dtype=np.int32)
+        if n == 0:
+            self._c(self._lib.dgadv_set_source_terms(self._h, 0, None, None, None))
+            return
+        r = np.stack([L.f64(x) for x in rhsTerms], axis=2)       # K x N x n
+        r = np.require(np.transpose(r, (0, 1, 2)), requirements=['F', 'A'])
+        d = None
+        if cDV0T is not None:
+            d = np.require(np.stack([L.f64(x) for x in cDV0T], axis=2), requirements=['F', 'A'])
+        self._c(self._lib.dgadv_set_source_terms(self._h, n, L.ptr(tf, L._i32p), L.ptr(r), L.ptr(d)))
+
+    def set_state(self, cDisc):
+        c = L.f64(cDisc)
+        assert c.shape == (self.K, self.N)
+        self._c(self._lib.dgadv_set_state(self._h, L.ptr(c)))
+
+    def get_state(self, out=None):
+        if out is None:
+            out = np.zeros((self.K, self.N), order='F')
+        self._c(self._lib.dgadv_get_state(self._h, L.ptr(out)))
+        return out
+
+    def limit_state(self, t):
+        self._c(self._lib.dgadv_limit_state(self._h, float(t)))
+
+    def step(self, nSteps, nStep0, tau):
+        self._c(self._lib.dgadv_step(self._h, int(nSteps), int(nStep0), float(tau)))
+
+    def sync(self):
+        self._c(self._lib.dgadv_sync(self._h))
+
+    def kernels_per_step(self):
+        n = ctypes.c_int32()
+        self._c(self._lib.dgadv_kernels_per_step(self._h, ctypes.byref(n)))
+        return n.value
+
+    def close(self):
+        if self._h:
+            self._lib.dgadv_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

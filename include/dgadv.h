@@ -1,0 +1,157 @@
+/*
+ * dgadv.h -- C-ABI of the GB300-native explicit DG advection step.
+ *
+ * One library (libdgadv.so) holds (a) host helpers that rebuild the reference's static data
+ * (grid incidence maps, quadrature rules, basis values) and (b) the device solver for the
+ * per-stage operator of FESTUNG's advection problem:
+ *     cDot = M^-1 ( L - K_D - K_N + (G1+G2) c - R c )          advection/solveSubStep.m:62-66
+ *     c^(i) = w_i c^n + (1-w_i) (c^(i-1) + tau cDot)            advection/solveSubStep.m:83
+ * with the vertex-based Taylor slope limiter              advection/solveSubStep.m:69-98.
+ *
+ * Every entry point returns a status code (DGADV_OK on success); no C++ exception and no
+ * longjmp crosses this boundary.  Arrays are column-major (Fortran order) with the shapes the
+ * reference keeps them in (K x N for cDisc, K x 3 x R for vNormalOnQuadEdge, ...), so a
+ * MEX/oct gateway can pass mxArray data without transposes.  Integer inputs are 0-based int32;
+ * integer outputs that the reference stores as "index or 0 for none" keep its values.
+ *
+ * Threading: calls for one handle must come from one host thread at a time.  Each handle owns
+ * one CUDA stream; dgadv_step only enqueues work, dgadv_sync / dgadv_get_state wait for it.
+ */
+#ifndef DGADV_H
+#define DGADV_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------------------- */
+enum {
+  DGADV_OK = 0,
+  DGADV_EINVAL = 1,        /* invalid argument (null pointer, size, option)                */
+  DGADV_ECUDA = 2,         /* CUDA runtime error                                           */
+  DGADV_ENOMEM = 3,        /* host or device allocation failed                             */
+  DGADV_EMESH = 4,         /* inconsistent mesh (non-manifold edge, bad vertex id, ...)     */
+  DGADV_ENONFINITE = 5,    /* a kernel found NaN/Inf in the state                          */
+  DGADV_ETIMEOUT = 6,      /* a bounded device-side wait gave up                           */
+  DGADV_EUNSUPPORTED = 7   /* option not supported by this build (e.g. p > 3 on the GPU)  */
+};
+
+enum { DGADV_FP64 = 0, DGADV_FP32 = 1 };
+enum { DGADV_LIM_LINEAR = 0, DGADV_LIM_HIERARCH_VERT = 1, DGADV_LIM_STRICT = 2 };
+enum { DGADV_TIME_CONST = 0, DGADV_TIME_EXP_NEG = 1 };     /* g(t) = 1 or exp(-t) */
+
+/* flags of dgadv_params.flags */
+enum {
+  DGADV_FLAG_NO_REORDER = 1,   /* keep the caller's element order on the device            */
+  DGADV_FLAG_NO_SHIFT = 2,     /* patch min/max without the reference's global shift       */
+  DGADV_FLAG_NO_GRAPH = 4      /* launch stage kernels one by one instead of a CUDA graph  */
+};
+
+/* ---- host helpers: static data ------------------------------------------------------- */
+
+/* Output of generateGridData (core/generateGridData.m:130-198).  Allocated by
+ * dgadv_grid_build, released by dgadv_grid_free. */
+typedef struct dgadv_grid {
+  int32_t numT, numV, numE;
+  int32_t *V0E;      /* numE x 2   0-based vertex ids (reference V0E - 1)                  */
+  int32_t *T0E;      /* numE x 2   1-based element ids, 0 = none (reference T0E)           */
+  int32_t *E0T;      /* numT x 3   0-based edge ids (reference E0T - 1)                    */
+  int32_t *E0E;      /* numE x 2   1-based local edge index, 0 = none (reference E0E)      */
+  double *areaE;     /* numE                                                               */
+  double *nuE;       /* numE x 2                                                           */
+  double *baryE;     /* numE x 2                                                           */
+  double *areaT;     /* numT                                                               */
+  double *baryT;     /* numT x 2                                                           */
+  double *B;         /* numT x 2 x 2                                                       */
+  double *areaE0T;   /* numT x 3                                                           */
+  double *nuE0T;     /* numT x 3 x 2                                                       */
+  double *coordV0T;  /* numT x 3 x 2                                                       */
+  double *detJ0T;    /* numT                                                               */
+} dgadv_grid;
+
+/* Replaces generateGridData(coordV, V0T), core/generateGridData.m:130-198 (without the K x K
+ * masks markE0TE0T / markV0TV0T, whose content is carried by T0E/E0E). */
+int dgadv_grid_build(int32_t numV, const double *coordV, int32_t numT, const int32_t *V0T,
+                     dgadv_grid **out);
+void dgadv_grid_free(dgadv_grid *grid);
+
+/* Replaces quadRule1D(qOrd) (core/quadRule1D.m:48-95), points on [0,1].  With Q == NULL only
+ * *R is written. */
+int dgadv_quad_rule_1d(int32_t qOrd, int32_t *R, double *Q, double *W);
+/* Replaces quadRule2D(qOrd) (core/quadRule2D.m:64-109; orders >= 7 as core/triquad.m). */
+int dgadv_quad_rule_2d(int32_t qOrd, int32_t *R, double *Q1, double *Q2, double *W);
+/* Replaces phi(i,X1,X2) / gradPhi(i,m,X1,X2) for i = 1..N (core/phi.m:40-61,
+ * core/gradPhi.m:42-87): phi is nPts x N, gradPhi nPts x N x 2 (may be NULL). */
+int dgadv_basis_eval(int32_t N, int32_t nPts, const double *X1, const double *X2, double *phi,
+                     double *gradPhi);
+
+/* ---- device solver -------------------------------------------------------------------- */
+
+typedef struct dgadv_mesh {
+  int32_t numT, numV;
+  const double *coordV;        /* numV x 2                                                  */
+  const int32_t *V0T;          /* numT x 3, 0-based, counter-clockwise                      */
+  const int32_t *idE0T;        /* numT x 3 boundary ids (0 = interior) or NULL: every
+                                  boundary edge counts as identified                       */
+  const uint8_t *markE0TbdrD;  /* numT x 3 Dirichlet boundary edges or NULL: all boundary   */
+  const uint8_t *markE0TbdrN;  /* numT x 3 Neumann boundary edges or NULL: none             */
+} dgadv_mesh;
+
+typedef struct dgadv_params {
+  int32_t p;             /* polynomial degree 0..3 (the reference allows 0..4)              */
+  int32_t ordRK;         /* SSP-RK order 1..3 (core/rungeKuttaExplicit.m:64-78)             */
+  int32_t precision;     /* DGADV_FP64 or DGADV_FP32                                        */
+  int32_t isSlopeLim;    /* vertex-based Taylor limiter on/off                              */
+  int32_t typeSlopeLim;  /* DGADV_LIM_*                                                     */
+  int32_t device;        /* CUDA device ordinal                                             */
+  int32_t flags;         /* DGADV_FLAG_*                                                    */
+} dgadv_params;
+
+typedef struct dgadv_handle dgadv_handle;
+
+/* Replaces the device-independent part of advection/preprocessProblem.m:48-112: grid, tables,
+ * mass and Taylor data for one mesh; uploads everything once. */
+int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *params, dgadv_handle **out);
+
+/* Velocity data of advection/preprocessSubStep.m:72-79: u1Disc, u2Disc (K x N, projections of
+ * order 2p) and vNormalOnQuadEdge (K x 3 x R, order 2p+1).  Held until replaced. */
+int dgadv_set_velocity(dgadv_handle *h, const double *u1Disc, const double *u2Disc,
+                       const double *vNormalOnQuadEdge);
+
+/* Right-hand-side data of advection/preprocessSubStep.m:87-98 and the limiter's boundary
+ * values (advection/solveSubStep.m:86-88) as separable terms:
+ *     sysV(t)  = sum_m g_m(t) rhs_m          rhs_m = L_m - K_D,m - K_N,m      (K x N each)
+ *     cDV0T(t) = sum_m g_m(t) cDV0T_m                                         (K x 3 each)
+ * g_m = timeFn[m] (DGADV_TIME_*).  nTerms = 0 means zero data (the default).  cDV0T may be
+ * NULL (zero boundary values). */
+int dgadv_set_source_terms(dgadv_handle *h, int32_t nTerms, const int32_t *timeFn,
+                           const double *rhsTerms, const double *cDV0T);
+
+/* cDisc (K x N) in and out (advection/solveStep.m:67-68, advection/postprocessStep.m:58). */
+int dgadv_set_state(dgadv_handle *h, const double *cDisc);
+int dgadv_get_state(dgadv_handle *h, double *cDisc);
+
+/* applySlopeLimiterDisc on the current state with boundary data at time t
+ * (advection/initializeProblem.m:56-67). */
+int dgadv_limit_state(dgadv_handle *h, double t);
+
+/* Enqueues time steps nStep0+1 .. nStep0+nSteps (advection/solveStep.m:57-73 with all its
+ * sub-steps); step n uses t0 = (n-1)*tau as the reference.  Asynchronous. */
+int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau);
+
+/* Waits for enqueued work; reports DGADV_ENONFINITE if a kernel saw NaN/Inf. */
+int dgadv_sync(dgadv_handle *h);
+
+/* Number of kernels one time step launches (for launch accounting). */
+int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count);
+
+const char *dgadv_last_error(const dgadv_handle *h);
+const char *dgadv_status_string(int status);
+void dgadv_destroy(dgadv_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DGADV_H */

@@ -73,8 +73,12 @@ def taylor_blocks(g, N, bases):
 class MatFree:
     """Holds a preprocessed oracle problem and advances it with matrix-free stages."""
 
-    def __init__(self, pd):
+    def __init__(self, pd, rounding='lu'):
+        """``rounding='inverse'`` applies explicit block inverses instead of LU solves for the
+        Taylor projections: the same algebra with different rounding, used to measure how
+        sensitive a configuration is to roundoff (the spread that bounds any parity claim)."""
         self.pd = pd
+        self.rounding = rounding
         g, N = pd.g, pd.N
         self.nbr, self.nbrEdge = neighbour_maps(g)
         self.ptr, self.idx = vertex_csr(g.V0T, g.numV)
@@ -139,9 +143,17 @@ class MatFree:
 
     # ------------------------------------------------------------------ limiter pieces
     def to_taylor(self, c):
+        if self.rounding == 'inverse':
+            if not hasattr(self, '_P'):
+                self._P = np.linalg.inv(self.MDT) @ self.M
+            return np.einsum('kij,kj->ki', self._P, c)
         return np.linalg.solve(self.MDT, np.einsum('kij,kj->ki', self.M, c)[..., None])[..., 0]
 
     def from_taylor(self, cT):
+        if self.rounding == 'inverse':
+            if not hasattr(self, '_Q'):
+                self._Q = np.linalg.inv(self.M) @ self.MDT
+            return np.einsum('kij,kj->ki', self._Q, cT)
         return np.linalg.solve(self.M, np.einsum('kij,kj->ki', self.MDT, cT)[..., None])[..., 0]
 
     def patch_minmax(self, valCentroid, markV0TbdrD, dataV0T):
@@ -248,12 +260,27 @@ class MatFree:
         return pd
 
 
-def main_matfree(problemData=None, **kwargs):
+def main_matfree(problemData=None, rounding='lu', **kwargs):
     """Same pre/loop/post phases as ``oracle.advection.main`` with matrix-free stages."""
     pd = adv.Struct(problemData or {})
     pd.update(kwargs)
     pd.problemName = 'advection'
-    for f in (adv.configureProblem, adv.preprocessProblem, adv.initializeProblem):
+    for f in (adv.configureProblem, adv.preprocessProblem):
         pd = f(pd)
-    MatFree(pd).run()
+    mf = MatFree(pd, rounding=rounding)
+    # initializeProblem with this object's limiter (advection/initializeProblem.m:46-86)
+    pd.isFinished = False
+    pd.cDisc = A.projectFuncCont2DataDisc(pd.g, pd.c0Cont, pd.qOrd, pd.hatM, pd.basesOnQuad)
+    if pd.isSlopeLim:
+        cDV0T = A.computeFuncContV0T(pd.g, lambda x1, x2: pd.cDCont(0, x1, x2))
+        pd.cDisc = mf.limit_disc(pd.cDisc, pd.g.markV0TbdrD, cDV0T)
+    pd.initialError = A.computeL2Error(pd.g, pd.cDisc, pd.c0Cont, 2 * pd.p, pd.basesOnQuad)
+    mf.run()
     return adv.postprocessProblem(pd)
+
+
+def roundoff_spread(**kwargs):
+    """Relative L2 distance between two roundings of the same oracle computation."""
+    a = main_matfree(rounding='lu', **kwargs).cDisc
+    b = main_matfree(rounding='inverse', **kwargs).cDisc
+    return float(np.linalg.norm(a - b) / np.linalg.norm(a))
