@@ -1,0 +1,412 @@
+"""Benchmark of the explicit DG advection step on one GB300 (or N replicas under torchrun).
+
+Workload (default): the 131072-triangle production case -- domainSquare hmax=2^-8, p=2 (N=6),
+SSP-RK3, tau=1e-4, 500 steps per solve, rotating Gaussian hump + slotted cylinder, linear
+vertex-based Taylor limiter on.  One bench "step" is one full 500-step solve
+(1500 RK stages).  The headline precision is FP32; the FP64 path and the FP32-vs-FP64 error
+are reported beside it.
+
+Metric: DOF-stage updates per second = K * N * stages / seconds.
+  value  -- device time (CUDA events on the library's stream) with the state resident in HBM;
+            L2 is flushed (512 MB memset) before every timed solve.
+  e2e    -- the same metric through the C-ABI with host buffers: every step copies the initial
+            coefficients in from pinned host memory (dgadv_set_state), runs the 500 steps and
+            reads the result back (dgadv_get_state); wall-clock time.
+  roofline -- the dominant kernel's algorithmic bytes per launch / its mean launch time (CUDA
+            events around each launch), against the measured HBM copy bandwidth.
+  cpu_baseline -- the oracle's restatement of the reference (per-stage sparse assembly, as the
+            reference) on this machine's cores for a bounded sample of steps.
+
+``--impl reference`` times the reference's algorithm on the host (the oracle port; there is no
+Matlab/Octave to run the reference itself) on the same workload, a bounded number of time steps
+per bench step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    'cfg2': dict(testcase='gauss_slot', hmax=2 ** -8, p=2, numSteps=500, tEnd=500 * 1e-4,
+                 isSlopeLim=True, typeSlopeLim='linear', ordRK=3),
+    'cfg1': dict(testcase='gauss_slot', hmax=2 ** -5, p=1, numSteps=500, tEnd=0.5,
+                 isSlopeLim=True, typeSlopeLim='linear', ordRK=2),
+    'cfg5': dict(testcase='gauss_slot', hmax=2 ** -10, p=3, numSteps=100, tEnd=100 * 2e-5,
+                 isSlopeLim=True, typeSlopeLim='hierarch_vert', ordRK=3, jitter=0.1, meshSeed=5),
+}
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------------------------
+def algorithmic_bytes(kind, w, N, Q, R, nc):
+    """Unique bytes per element a launch of each kernel kind must move (its own element's
+    inputs and outputs plus the static per-element data; neighbour gathers re-read the same
+    arrays and count once)."""
+    csr = 14                                    # vertex CSR (vptr ~ 2 B, vidx 12 B per element)
+    if kind == 'op0':                           # stage operator, limiter off: c, c^n, F, Vn, ints, out
+        return w * (3 * N + 2 * Q + 3 * R) + 16
+    if kind == 'op1':                           # + B, Taylor out, centroid quantities
+        return w * (3 * N + 2 * Q + 3 * R + 4 + nc) + 16
+    if kind == 'op2':                           # c, F, Vn, B, ints; Taylor(cDot) and q out
+        return w * (2 * N + 2 * Q + 3 * R + 4 + nc) + 16
+    if kind == 'limdot':                        # Taylor in/out, B, M_T, c^n, c^(s-1), q in/out
+        return w * (4 * N + 4 + N * (N + 1) // 2 + 2 * nc) + 16 + csr
+    if kind == 'lim':                           # Taylor in, B, q, modal out
+        return w * (2 * N + 4 + nc) + 16 + csr
+    raise ValueError(kind)
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.device), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(n)
+        if not sm:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': [], 'samples': 0}
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(mx), 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 'fallback'
+
+
+def setup_problem(wl, precision, device):
+    from festung_gb300 import advection_gpu as G
+    pd = G.Struct(dict(WORKLOADS[wl], precision=precision, device=device))
+    pd.problemName = 'advection_gpu'
+    for f in G.PRE:
+        pd = f(pd)
+    return pd
+
+
+class OracleStages:
+    """Runs RK stages of the oracle restatement (per-stage sparse assembly and solve, as
+    advection/preprocessSubStep.m + advection/solveSubStep.m) one at a time: a bounded sample of
+    the workload for the CPU baseline."""
+
+    def __init__(self, wl):
+        from oracle import advection as adv
+        from oracle import assembly as A
+        self.adv, self.A = adv, A
+        pd = adv.Struct(dict(WORKLOADS[wl]))
+        pd.problemName = 'advection'
+        for f in (adv.configureProblem, adv.preprocessProblem, adv.initializeProblem):
+            pd = f(pd)
+        self.pd = pd
+        self.S = len(A.rungeKuttaExplicit(pd.ordRK, 1.0, 0.0)[1])
+        self.nStep, self.sub = 0, self.S
+
+    def stage(self):
+        adv, pd = self.adv, self.pd
+        if self.sub >= self.S:
+            if self.nStep > 0:
+                adv.postprocessStep(pd, self.nStep)
+            self.nStep += 1
+            pd.t, pd.omega = self.A.rungeKuttaExplicit(pd.ordRK, pd.tau, (self.nStep - 1) * pd.tau)
+            pd.cDiscRK = [None] * (len(pd.t) + 1)
+            pd.cDiscRK[0] = pd.cDisc.reshape(-1).copy()
+            self.sub = 0
+        self.sub += 1
+        adv.preprocessSubStep(pd, self.nStep, self.sub)
+        adv.solveSubStep(pd, self.nStep, self.sub)
+        adv.postprocessSubStep(pd, self.nStep, self.sub)
+
+    def dofs_per_stage(self):
+        return self.pd.K * self.pd.N
+
+
+def cpu_baseline(wl, nstages):
+    """DOF-stage updates/s of the oracle restatement over ``nstages`` RK stages."""
+    o = OracleStages(wl)
+    t = time.perf_counter()
+    for _ in range(nstages):
+        o.stage()
+    dt = time.perf_counter() - t
+    return o.dofs_per_stage() * nstages / dt, dt, o.pd
+
+
+def thread_count():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------------------------
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    n = str(thread_count())
+    for v in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+        os.environ.setdefault(v, n)
+    o = OracleStages(args.workload)
+    per = args.ref_stages_per_step
+    for _ in range(args.warmup):
+        for _ in range(per):
+            o.stage()
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        for _ in range(per):
+            o.stage()
+        times.append(time.perf_counter() - t)
+    pd, S = o.pd, o.S
+    ms = 1e3 * statistics.mean(times)
+    value = o.dofs_per_stage() * per / (ms / 1e3)
+    sample = ('%d RK stage(s) of the %s workload per bench step (of %d steps x %d stages per solve), '
+              'sparse operators re-assembled every stage as the reference does'
+              % (per, args.workload, pd.numSteps, S))
+    line = {
+        'impl': 'reference', 'metric': 'DG DOF-stage updates/s', 'value': value,
+        'unit': 'DOF-stage/s', 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64', 'data': 'synthetic',
+        'config': workload_config(args.workload, pd.K, pd.N, S, pd.numSteps),
+        'cpu_baseline': {'value': value, 'unit': 'DOF-stage/s', 'cores': thread_count(),
+                         'kind': 'port', 'sample': sample},
+        'e2e': {'value': value, 'unit': 'DOF-stage/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(wl, K, N, S, steps):
+    kw = WORKLOADS[wl]
+    return {'workload': '%s: domainSquare hmax=2^%d, K=%d triangles, p=%d (N=%d), SSP-RK%d, '
+                        '%d steps per solve, %s limiter, %s' % (
+                            wl, int(round(np.log2(kw['hmax']))), K, kw['p'], N, S, steps,
+                            kw['typeSlopeLim'] if kw['isSlopeLim'] else 'no', kw['testcase']),
+            'K': K, 'p': kw['p'], 'N': N, 'rk_stages': S, 'steps_per_solve': steps,
+            'limiter': kw['typeSlopeLim'] if kw['isSlopeLim'] else None,
+            'l2_flush_between_steps': True, 'parallelism': 'replicas'}
+
+
+def run_ours(args):
+    rank, world, local = dist_env()
+    device = local
+    import torch
+    torch.cuda.set_device(device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
+    from festung_gb300.build import build
+    if rank == 0:
+        build()
+    if world > 1:
+        torch.distributed.barrier()
+    wl = args.workload
+    pd = setup_problem(wl, 'fp32', device)
+    s = pd.solver
+    steps = pd.numSteps
+    S = pd.ordRK
+    K, N = pd.K, pd.N
+    units = K * N * S * steps
+    c0 = np.asfortranarray(pd._cDisc)
+    flush = torch.empty(512 * 2 ** 20, dtype=torch.uint8, device='cuda')
+
+    for _ in range(args.warmup):
+        s.step(steps, 0, pd.tau)
+    s.sync()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    times = []
+    sampler = ClockSampler(device)
+    with sampler:
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            times.append(s.time_steps(steps, (args.warmup + i) * steps, pd.tau))
+    torch.cuda.synchronize()
+    total_ms = sum(times)
+    if world > 1:
+        t = torch.tensor([total_ms], device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * units / (ms_per_step / 1e3)
+
+    # per-kernel launch times (CUDA events around each launch) for the roofline
+    kpl, nlaunch = s.profile_kernels(20, 0, pd.tau)
+    w = 4
+    Q = {0: 1, 1: 3, 2: 6, 3: 12}[pd.p]
+    R = pd.p + 1
+    nc = 1 if pd.typeSlopeLim == 'linear' else pd.p * (pd.p + 1) // 2
+    op_kind = 'op0' if not pd.isSlopeLim else ('op2' if pd.p > 1 else 'op1')
+    kinds = [op_kind, 'limdot', 'lim']
+    names = {'op0': 'k_stage_op', 'op1': 'k_stage_op', 'op2': 'k_stage_op', 'limdot': 'k_limit_dot',
+             'lim': 'k_limit'}
+    shares = [kpl[i] * nlaunch[i] for i in range(3)]
+    dom = int(np.argmax(shares))
+    peak, peak_kind = measured_peaks()
+    bytes_launch = algorithmic_bytes(kinds[dom], w, N, Q, R, nc) * K
+    achieved = bytes_launch / (kpl[dom] * 1e-3) / 1e9
+    kernel_profile = {names[kinds[i]] + ('' if i else ''): {'ms_per_launch': kpl[i], 'launches': int(nlaunch[i]),
+                      'share': shares[i] / max(sum(shares), 1e-30),
+                      'algorithmic_bytes_per_launch': algorithmic_bytes(kinds[i], w, N, Q, R, nc) * K,
+                      'achieved_GBps': algorithmic_bytes(kinds[i], w, N, Q, R, nc) * K / (kpl[i] * 1e-3) / 1e9
+                      if kpl[i] > 0 else None}
+                      for i in range(3) if nlaunch[i]}
+
+    # end to end through the C-ABI with pinned host buffers
+    hin = torch.empty((N, K), dtype=torch.float64, pin_memory=True)
+    hout = torch.empty((N, K), dtype=torch.float64, pin_memory=True)
+    hin.numpy()[...] = c0.T
+    cin = hin.numpy().T            # K x N Fortran-ordered view of pinned memory
+    cout = hout.numpy().T
+    e2e_times = []
+    for i in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s.set_state(cin)
+        s.step(steps, 0, pd.tau)
+        s.get_state(cout)
+        e2e_times.append(time.perf_counter() - t)
+    e2e_s = statistics.mean(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_s], device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * units / e2e_s
+    c32 = np.array(cout)
+
+    result = {
+        'metric': 'DG DOF-stage updates/s (FP32; FP64 and FP32-vs-FP64 error beside it)',
+        'value': value, 'unit': 'DOF-stage/s', 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+        'config': workload_config(wl, K, N, S, steps),
+        'clocks': sampler.summary(),
+        'e2e': {'value': e2e_value, 'unit': 'DOF-stage/s', 'h2d_bytes_per_step': K * N * 8,
+                'd2h_bytes_per_step': K * N * 8},
+        'gpu_launches': int(s.kernels_per_step() * steps * args.steps),
+        'roofline': {'bound': 'hbm', 'kernel': names[kinds[dom]], 'achieved': achieved,
+                     'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+                     'peak_source': peak_kind, 'traffic': None},
+        'kernels': kernel_profile,
+    }
+    s.close()
+
+    if rank == 0 and not args.no_fp64:
+        p64 = setup_problem(wl, 'fp64', device)
+        s64 = p64.solver
+        s64.step(steps, 0, p64.tau)
+        s64.sync()
+        flush.zero_(); torch.cuda.synchronize()
+        s64.set_state(c0)
+        ms64 = s64.time_steps(steps, 0, p64.tau)
+        c64 = s64.get_state()
+        s64.close()
+        result['fp64'] = {'value': units / (ms64 / 1e3), 'unit': 'DOF-stage/s', 'ms_per_step': ms64}
+        result['fp32_vs_fp64_rel_l2'] = float(np.linalg.norm(c32 - c64) / np.linalg.norm(c64))
+
+    if rank == 0 and not args.no_cpu:
+        n = thread_count()
+        v, dt, _ = cpu_baseline(wl, args.cpu_stages)
+        result['cpu_baseline'] = {
+            'value': v, 'unit': 'DOF-stage/s', 'cores': 1, 'kind': 'port',
+            'sample': '%d RK stage(s) of the workload with the oracle restatement (per-stage sparse '
+                      'assembly as the reference; scipy sparse is single-threaded), %.1f s on a %d-core host'
+                      % (args.cpu_stages, dt, n)}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--workload', default='cfg2', choices=sorted(WORKLOADS))
+    ap.add_argument('--no-fp64', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--cpu-stages', type=int, default=1)
+    ap.add_argument('--ref-stages-per-step', type=int, default=1)
+    ap.add_argument('--ncu-case', default=None, choices=sorted(WORKLOADS),
+                    help='profiling driver: set up the workload and run --ncu-steps steps, no timing')
+    ap.add_argument('--ncu-steps', type=int, default=2)
+    ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
+    args = ap.parse_args()
+    if args.ncu_case:
+        pd = setup_problem(args.ncu_case, args.precision, 0)
+        pd.solver.step(args.ncu_steps, 0, pd.tau)
+        pd.solver.sync()
+        pd.solver.close()
+        return 0
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -65,6 +65,9 @@ SYMBOLS = {
     'dgadv_step': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double]),
     'dgadv_sync': (ctypes.c_int, [ctypes.c_void_p]),
     'dgadv_kernels_per_step': (ctypes.c_int, [ctypes.c_void_p, _i32p]),
+    'dgadv_time_steps': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _dp]),
+    'dgadv_profile_kernels': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                             _dp, _i32p]),
     'dgadv_last_error': (ctypes.c_char_p, [ctypes.c_void_p]),
     'dgadv_status_string': (ctypes.c_char_p, [ctypes.c_int]),
     'dgadv_destroy': (None, [ctypes.c_void_p]),

@@ -209,18 +209,94 @@ __device__ __forceinline__ void from_taylor(const T *cT, const Affine<T> &af, T 
 // Index of the Taylor DOF with multi-index (a1, a2) (core/mult2ind.m:57-62, 0-based).
 __host__ __device__ constexpr int mind(int a1, int a2) { return (a1 + a2) * (a1 + a2 + 1) / 2 + a2; }
 
+template <int P> struct NCQ { static constexpr int value = P * (P + 1) / 2 > 1 ? P * (P + 1) / 2 : 1; };
+
 // Centroid quantities of the sub-limiters (one per computeVertexBasedLimiter call).
 template <typename T, int P>
-__device__ __forceinline__ void centroid_quantities(const T *cT, int type, T *q, int k, int Kp) {
+__device__ __forceinline__ void centroid_quantities(const T *cT, int type, T *qv) {
   if (type == 0) {
-    q[k] = cT[0];
+    qv[0] = cT[0];
   } else {
     int s = 0;
 #pragma unroll
     for (int ord = P; ord >= 1; --ord)
 #pragma unroll
-      for (int i = 1; i <= ord; ++i) { q[(size_t)s * Kp + k] = cT[mind(ord - i, i - 1)]; ++s; }
+      for (int i = 1; i <= ord; ++i) { qv[s] = cT[mind(ord - i, i - 1)]; ++s; }
   }
+}
+
+// Limiter pass plumbing.  Pass j scatters its centroid quantities into per-vertex min / max
+// slots vkeys[j%3] with atomicMin / atomicMax on order-preserving integer keys (each element
+// updates its three vertices: the patch of a vertex is exactly the elements that update it,
+// core/computeMinMaxV0TElementPatch.m:99-111), and the global extremes (for the reference's
+// shift) into slots[j%3].  The producer of pass j resets the slots of pass j+1; three sets keep
+// the kernel that consumes pass j and produces pass j+1 clear of both.
+template <typename T> struct KeyOf { using type = unsigned int; };
+template <> struct KeyOf<double> { using type = unsigned long long; };
+
+__device__ __forceinline__ unsigned int okey32(float x) { return (unsigned int)okey(x); }
+__device__ __forceinline__ unsigned int vkey(float x) { return okey32(x); }
+__device__ __forceinline__ unsigned long long vkey(double x) { return okey(x); }
+template <typename T> __device__ __forceinline__ T vkey_inv(typename KeyOf<T>::type k) { return okey_inv<T>(k); }
+template <typename T> __host__ __device__ constexpr typename KeyOf<T>::type vkey_max() {
+  return (typename KeyOf<T>::type)key_max<T>();
+}
+
+template <typename T> struct LimOut {
+  typename KeyOf<T>::type *vkeys;   // nc x 2 x Vp vertex min / max keys of this pass
+  typename KeyOf<T>::type *vreset;  // the next pass's vertex keys, reset here
+  unsigned long long *slots;        // 2 x nc encoded global min / max (atomic)
+  unsigned long long *reset;        // slots of the next pass, reset by block 0
+  int nc, type;
+};
+template <typename T> struct LimIn {
+  const typename KeyOf<T>::type *vkeys;
+  const unsigned long long *slots;
+  int nc, type, shift;
+};
+
+// Scatter of the element's centroid quantities to its vertices and the block's global extremes.
+template <typename T, int NQ>
+__device__ __forceinline__ void scatter_quantities(const Geo<T> &g, const LimOut<T> &lo, const T *qv,
+                                                   const int vid[3], bool active) {
+  if (active) {
+#pragma unroll
+    for (int s = 0; s < NQ; ++s) {
+      if (s >= lo.nc) break;
+      const auto key = vkey(qv[s]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        atomicMin(&lo.vkeys[(size_t)(2 * s) * g.Vp + vid[n]], key);
+        atomicMax(&lo.vkeys[(size_t)(2 * s + 1) * g.Vp + vid[n]], key);
+      }
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < NQ; ++s) {
+    if (s >= lo.nc) break;
+    T mn = active ? qv[s] : T(INFINITY), mx = active ? qv[s] : T(-INFINITY);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0 && mn <= mx) {
+      atomicMin(&lo.slots[2 * s], okey(mn));
+      atomicMax(&lo.slots[2 * s + 1], okey(mx));
+    }
+  }
+}
+
+// Reset of the next pass's vertex keys (thread t owns vertex t) and global slots (block 0).
+template <typename T>
+__device__ __forceinline__ void reset_next(const Geo<T> &g, const LimOut<T> &lo, int t) {
+  if (t < g.numV)
+    for (int s = 0; s < lo.nc; ++s) {
+      lo.vreset[(size_t)(2 * s) * g.Vp + t] = vkey_max<T>();
+      lo.vreset[(size_t)(2 * s + 1) * g.Vp + t] = 0;
+    }
+  if (blockIdx.x == 0 && threadIdx.x < 2 * lo.nc)
+    lo.reset[threadIdx.x] = (threadIdx.x & 1) ? 0ULL : key_max<T>();
 }
 
 // alpha of one computeVertexBasedLimiter call (core/computeVertexBasedLimiter.m:78-106)
@@ -239,46 +315,47 @@ __device__ __forceinline__ T vertex_alpha(T cbar, const T v[3], const T mn[3], c
   return alpha;
 }
 
-// Patch min / max of quantity s at the three vertices, with the reference's global shift
-// (min over the patch of (v - sNeg), then + sNeg; a monotone shift commutes with min).
+// Patch min / max of quantity s at the three vertices (read from the pass's vertex keys),
+// with the reference's global shift (min over the patch of (v - sNeg), then + sNeg; a monotone
+// shift commutes with min), then combined with the Dirichlet data (NaN = none; fmin / fmax
+// ignore NaN like Matlab's min / max).
 template <typename T>
-__device__ __forceinline__ void patch_minmax(const Geo<T> &g, const T *vmm, const LimArgs &la, int s,
-                                             const int vid[3], const T valD[3], T mn[3], T mx[3]) {
+__device__ __forceinline__ void patch_minmax(const Geo<T> &g, const LimIn<T> &li, int s, const int vid[3],
+                                             const T valD[3], T mn[3], T mx[3]) {
   T sNeg = 0, sPos = 0;
-  if (la.shift) {
-    const T gmin = okey_inv<T>(la.gmm[2 * s]), gmax = okey_inv<T>(la.gmm[2 * s + 1]);
+  if (li.shift) {
+    const T gmin = okey_inv<T>(li.slots[2 * s]), gmax = okey_inv<T>(li.slots[2 * s + 1]);
     sPos = fabs(gmin) + T(1);
     sNeg = fabs(gmax) + T(1);
   }
-  const T *vmin = vmm + (size_t)(2 * s) * g.Vp, *vmax = vmm + (size_t)(2 * s + 1) * g.Vp;
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
-    T a = vmin[vid[n]], b = vmax[vid[n]];
-    if (la.shift) { a = (a - sNeg) + sNeg; b = (b + sPos) - sPos; }
+    T a = vkey_inv<T>(li.vkeys[(size_t)(2 * s) * g.Vp + vid[n]]);
+    T c = vkey_inv<T>(li.vkeys[(size_t)(2 * s + 1) * g.Vp + vid[n]]);
+    if (li.shift) { a = (a - sNeg) + sNeg; c = (c + sPos) - sPos; }
     mn[n] = fmin(a, valD[n]);
-    mx[n] = fmax(b, valD[n]);
+    mx[n] = fmax(c, valD[n]);
   }
 }
 
 // Limit Taylor coefficients in place (linear / hierarchical vertex).  dataV0T: boundary values
 // at the three vertices for Dirichlet vertices (NaN means "no data").
 template <typename T, int P>
-__device__ __forceinline__ void limit_taylor(const Geo<T> &g, const T *vmm, const LimArgs &la, int k,
-                                             const Affine<T> &af, const int vid[3], int dmask,
-                                             const T dataV0T[3], T *cT) {
+__device__ __forceinline__ void limit_taylor(const Geo<T> &g, const LimIn<T> &li, const Affine<T> &af,
+                                             const int vid[3], int dmask, const T dataV0T[3], T *cT) {
   constexpr int N = Dims<P>::N;
   const T nan_ = T(NAN);
-  T pt1[3], pt2[3];   // Taylor basis 2 and 3 at the vertices
+  T pt1[3], pt2[3];   // Taylor basis functions 2 and 3 at the vertices
 #pragma unroll
   for (int n = 0; n < 3; ++n) { pt1[n] = af.ox[n] * af.dX; pt2[n] = af.oy[n] * af.dX; }
-  if (la.type == 0) {
+  if (li.type == 0) {
     T v[3], valD[3], mn[3], mx[3];
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
       v[n] = (cT[0] * T(1) + cT[1] * pt1[n]) + cT[2] * pt2[n];
       valD[n] = ((dmask >> n) & 1) ? dataV0T[n] : nan_;
     }
-    patch_minmax(g, vmm, la, 0, vid, valD, mn, mx);
+    patch_minmax(g, li, 0, vid, valD, mn, mx);
     const T alpha = vertex_alpha(cT[0], v, mn, mx);
     cT[1] *= alpha; cT[2] *= alpha;
     const T keep = (alpha == T(1)) ? T(1) : T(0);
@@ -302,7 +379,7 @@ __device__ __forceinline__ void limit_taylor(const Geo<T> &g, const T *vmm, cons
           v[n] = (orig[i0] * T(1) + orig[i1] * pt1[n]) + orig[i2] * pt2[n];
           valD[n] = ((dmask >> n) & 1) ? (ord > 1 ? v[n] : dataV0T[n]) : nan_;
         }
-        patch_minmax(g, vmm, la, s, vid, valD, mn, mx);
+        patch_minmax(g, li, s, vid, valD, mn, mx);
         aOrd = fmin(aOrd, vertex_alpha(orig[i0], v, mn, mx));
         ++s;
       }
@@ -314,149 +391,121 @@ __device__ __forceinline__ void limit_taylor(const Geo<T> &g, const T *vmm, cons
 }
 
 // ---------------------------------------------------------------------------------------------
-// Stage operator.  MODE 0: write c^(s);  MODE 1: write Taylor(c^(s)) and q;
-// MODE 2: write Taylor(cDot) and q (time-derivative limiting follows).
+// Stage operator.  MODE 0: write c^(s);  MODE 1: write Taylor(c^(s)) and its centroid
+// quantities;  MODE 2: write Taylor(cDot) and its quantities (time-derivative limiting follows).
 struct StageScalars {
   double omega, tau;
-  double gco[4];        // g_m(t_s) of the source terms
+  double gco[4];        // g_m(t) of the source terms / boundary data
   int *flag;            // bit 0: non-finite value seen
-  unsigned long long *gmm_reset;   // slots reset by this producer (or null)
-  int nc_reset;
 };
 
 template <typename T, int P, int MODE, bool RHS>
 __global__ void __launch_bounds__(kBlock)
 k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ out,
-           T *__restrict__ q, const LimArgs la, const StageScalars sc) {
-  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
+           const LimOut<T> lo, const StageScalars sc) {
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
   const Tab<T, P> &tb = tab<T, P>();
-  if (sc.gmm_reset && blockIdx.x == 0 && threadIdx.x < 2 * sc.nc_reset)
-    sc.gmm_reset[threadIdx.x] = (threadIdx.x & 1) ? 0ULL : key_max<T>();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= g.K) return;
+  if (MODE != 0) reset_next<T>(g, lo, k);
+  const bool active = k < g.K;
   const int Kp = g.Kp;
-  T c[N], rhs[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) { c[i] = cin[(size_t)i * Kp + k]; rhs[i] = T(0); }
-  if (RHS) {
-    for (int m = 0; m < g.nTerms; ++m) {
-      const T gm = T(sc.gco[m]);
-#pragma unroll
-      for (int i = 0; i < N; ++i) rhs[i] += gm * g.rhs[((size_t)m * N + i) * Kp + k];
-    }
-  }
-  // volume term
-#pragma unroll
-  for (int qq = 0; qq < Q; ++qq) {
-    T cq = T(0);
-#pragma unroll
-    for (int j = 0; j < N; ++j) cq += tb.phiQ[qq][j] * c[j];
-    const T f1 = g.F[(size_t)qq * Kp + k] * cq;
-    const T f2 = g.F[(size_t)(Q + qq) * Kp + k] * cq;
-#pragma unroll
-    for (int i = 0; i < N; ++i) rhs[i] += tb.g1[qq][i] * f1 + tb.g2[qq][i] * f2;
-  }
-  // upwind edge term
-  const int code = g.code[k];
-#pragma unroll
-  for (int n = 0; n < 3; ++n) {
-    const int nb = g.nbr[(size_t)n * Kp + k];
-    const int np = (code >> (2 * n)) & 3;
-    const bool outOk = (code >> (6 + n)) & 1;
-    T v[R];
-    bool anyIn = false;
-#pragma unroll
-    for (int r = 0; r < R; ++r) { v[r] = g.Vn[(size_t)(n * R + r) * Kp + k]; anyIn |= v[r] < T(0); }
-    T cn[N];
-    const bool gather = anyIn && nb >= 0;
-#pragma unroll
-    for (int j = 0; j < N; ++j) cn[j] = gather ? cin[(size_t)j * Kp + nb] : T(0);
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      T tr = T(0);
-      if (v[r] > T(0) && outOk) {
-#pragma unroll
-        for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r][j] * c[j];
-      } else if (v[r] < T(0) && nb >= 0) {
-#pragma unroll
-        for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r][j] * cn[j];
-      }
-      const T fl = v[r] * tr;
-#pragma unroll
-      for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r][i] * fl;
-    }
-  }
-  // mass solve
-  T cdot[N];
-  if (sizeof(T) == 8) {
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      T s = T(0);
-#pragma unroll
-      for (int j = 0; j < N; ++j) s += tb.hatMinv[i][j] * rhs[j];
-      cdot[i] = s;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < N; ++i) cdot[i] = rhs[i];
-  }
+  T qv[NQ];
+  int vid[3] = {0, 0, 0};
   bool bad = false;
-  if (MODE == 2) {
-    const Affine<T> af = load_affine(g, k);
-    T cT[N];
-    to_taylor<T, P>(cdot, af, cT);
+  if (active) {
+    T c[N], rhs[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cT[i]; bad |= !finite_(cT[i]); }
-    centroid_quantities<T, P>(cT, la.type, q, k, Kp);
-  } else {
-    const T w = T(sc.omega), tau = T(sc.tau);
-    T cnew[N];
+    for (int i = 0; i < N; ++i) { c[i] = cin[(size_t)i * Kp + k]; rhs[i] = T(0); }
+    if (RHS) {
+      for (int m = 0; m < g.nTerms; ++m) {
+        const T gm = T(sc.gco[m]);
 #pragma unroll
-    for (int i = 0; i < N; ++i) cnew[i] = w * c0[(size_t)i * Kp + k] + (T(1) - w) * (c[i] + tau * cdot[i]);
-    if (MODE == 0) {
+        for (int i = 0; i < N; ++i) rhs[i] += gm * g.rhs[((size_t)m * N + i) * Kp + k];
+      }
+    }
+    // volume term
 #pragma unroll
-      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+    for (int qq = 0; qq < Q; ++qq) {
+      T cq = T(0);
+#pragma unroll
+      for (int j = 0; j < N; ++j) cq += tb.phiQ[qq][j] * c[j];
+      const T f1 = g.F[(size_t)qq * Kp + k] * cq;
+      const T f2 = g.F[(size_t)(Q + qq) * Kp + k] * cq;
+#pragma unroll
+      for (int i = 0; i < N; ++i) rhs[i] += tb.g1[qq][i] * f1 + tb.g2[qq][i] * f2;
+    }
+    // upwind edge term
+    const int code = g.code[k];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      const int nb = g.nbr[(size_t)n * Kp + k];
+      const int np = (code >> (2 * n)) & 3;
+      const bool outOk = (code >> (6 + n)) & 1;
+      T v[R];
+      bool anyIn = false;
+#pragma unroll
+      for (int r = 0; r < R; ++r) { v[r] = g.Vn[(size_t)(n * R + r) * Kp + k]; anyIn |= v[r] < T(0); }
+      T cn[N];
+      const bool gather = anyIn && nb >= 0;
+#pragma unroll
+      for (int j = 0; j < N; ++j) cn[j] = gather ? cin[(size_t)j * Kp + nb] : T(0);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        T tr = T(0);
+        if (v[r] > T(0) && outOk) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r][j] * c[j];
+        } else if (v[r] < T(0) && nb >= 0) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r][j] * cn[j];
+        }
+        const T fl = v[r] * tr;
+#pragma unroll
+        for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r][i] * fl;
+      }
+    }
+    // mass solve
+    T cdot[N];
+    if (sizeof(T) == 8) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int j = 0; j < N; ++j) s += tb.hatMinv[i][j] * rhs[j];
+        cdot[i] = s;
+      }
     } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) cdot[i] = rhs[i];
+    }
+    if (MODE == 2) {
       const Affine<T> af = load_affine(g, k);
       T cT[N];
-      to_taylor<T, P>(cnew, af, cT);
+      to_taylor<T, P>(cdot, af, cT);
 #pragma unroll
       for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cT[i]; bad |= !finite_(cT[i]); }
-      centroid_quantities<T, P>(cT, la.type, q, k, Kp);
-    }
-  }
-  if (bad) atomicOr(sc.flag, 1);
-}
-
-// Vertex pass: min / max of every centroid quantity over the elements of each vertex patch
-// (CSR vertex -> elements), and the global min / max of each quantity for the shift.
-template <typename T>
-__global__ void __launch_bounds__(kBlock)
-k_vertex_minmax(const Geo<T> g, const T *__restrict__ q, int nc, T *__restrict__ vmm,
-                unsigned long long *gmm) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = v < g.numV;
-  int b = 0, e = 0;
-  if (active) { b = g.vptr[v]; e = g.vptr[v + 1]; }
-  for (int s = 0; s < nc; ++s) {
-    T mn = T(INFINITY), mx = T(-INFINITY);
-    const T *qs = q + (size_t)s * g.Kp;
-    for (int i = b; i < e; ++i) {
-      const T x = qs[g.vidx[i]];
-      mn = fmin(mn, x); mx = fmax(mx, x);
-    }
-    if (active) { vmm[(size_t)(2 * s) * g.Vp + v] = mn; vmm[(size_t)(2 * s + 1) * g.Vp + v] = mx; }
-    // block reduction for the global extremes
+      centroid_quantities<T, P>(cT, lo.type, qv);
+    } else {
+      const T w = T(sc.omega), tau = T(sc.tau);
+      T cnew[N];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      for (int i = 0; i < N; ++i) cnew[i] = w * c0[(size_t)i * Kp + k] + (T(1) - w) * (c[i] + tau * cdot[i]);
+      if (MODE == 0) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+      } else {
+        const Affine<T> af = load_affine(g, k);
+        T cT[N];
+        to_taylor<T, P>(cnew, af, cT);
+#pragma unroll
+        for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cT[i]; bad |= !finite_(cT[i]); }
+        centroid_quantities<T, P>(cT, lo.type, qv);
+      }
     }
-    if ((threadIdx.x & 31) == 0 && mn <= mx) {
-      atomicMin(&gmm[2 * s], okey(mn));
-      atomicMax(&gmm[2 * s + 1], okey(mx));
-    }
+    if (MODE != 0) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
   }
+  if (MODE != 0) scatter_quantities<T, NQ>(g, lo, qv, vid, active);
+  if (bad) atomicOr(sc.flag, 1);
 }
 
 // Time-derivative limiting and SSP update (advection/solveSubStep.m:69-83), then the Taylor
@@ -464,54 +513,56 @@ k_vertex_minmax(const Geo<T> g, const T *__restrict__ q, int nc, T *__restrict__
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
 k_limit_dot(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ tbuf,
-            T *__restrict__ q, const T *__restrict__ vmm, const LimArgs laDot, const LimArgs laSol,
-            const StageScalars sc) {
-  constexpr int N = Dims<P>::N, NMT = Dims<P>::NMT;
-  if (sc.gmm_reset && blockIdx.x == 0 && threadIdx.x < 2 * sc.nc_reset)
-    sc.gmm_reset[threadIdx.x] = (threadIdx.x & 1) ? 0ULL : key_max<T>();
+            const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= g.K) return;
+  reset_next<T>(g, lo, k);
+  const bool active = k < g.K;
   const int Kp = g.Kp;
-  const Affine<T> af = load_affine(g, k);
-  T cT[N], lim[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) { cT[i] = tbuf[(size_t)i * Kp + k]; lim[i] = cT[i]; }
-  const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
-  const int dmask = (g.code[k] >> 9) & 7;
-  const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
-  limit_taylor<T, P>(g, vmm, laDot, k, af, vid, dmask, nan3, lim);
-  // Taylor mass correction M_corr = diag(1/diag(M_T)) M_T applied to (cT - lim)
-  T d[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) d[i] = cT[i] - lim[i];
-  T cor[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    T s = T(0), dii = T(1);
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-      const int a = i < j ? i : j, b = i < j ? j : i;
-      const int idx = a * N - a * (a - 1) / 2 + (b - a);
-      const T m = g.MT[(size_t)idx * Kp + k];
-      s += m * d[j];
-      if (j == i) dii = m;
-    }
-    cor[i] = lim[i] + s / dii;
-  }
-  (void)NMT;
-  T cdot[N];
-  from_taylor<T, P>(cor, af, cdot);
-  const T w = T(sc.omega), tau = T(sc.tau);
-  T cnew[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i)
-    cnew[i] = w * c0[(size_t)i * Kp + k] + (T(1) - w) * (cin[(size_t)i * Kp + k] + tau * cdot[i]);
-  T cT2[N];
-  to_taylor<T, P>(cnew, af, cT2);
+  T qv[NQ];
+  int vid[3] = {0, 0, 0};
   bool bad = false;
+  if (active) {
+    const Affine<T> af = load_affine(g, k);
+    T cT[N], lim[N];
 #pragma unroll
-  for (int i = 0; i < N; ++i) { tbuf[(size_t)i * Kp + k] = cT2[i]; bad |= !finite_(cT2[i]); }
-  centroid_quantities<T, P>(cT2, laSol.type, q, k, Kp);
+    for (int i = 0; i < N; ++i) { cT[i] = tbuf[(size_t)i * Kp + k]; lim[i] = cT[i]; }
+    vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
+    const int dmask = (g.code[k] >> 9) & 7;
+    const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
+    limit_taylor<T, P>(g, li, af, vid, dmask, nan3, lim);
+    // Taylor mass correction M_corr = diag(1/diag(M_T)) M_T applied to (cT - lim)
+    T d[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = cT[i] - lim[i];
+    T cor[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T s = T(0), dii = T(1);
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const int a = i < j ? i : j, b = i < j ? j : i;
+        const int idx = a * N - a * (a - 1) / 2 + (b - a);
+        const T m = g.MT[(size_t)idx * Kp + k];
+        s += m * d[j];
+        if (j == i) dii = m;
+      }
+      cor[i] = lim[i] + s / dii;
+    }
+    T cdot[N];
+    from_taylor<T, P>(cor, af, cdot);
+    const T w = T(sc.omega), tau = T(sc.tau);
+    T cnew[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      cnew[i] = w * c0[(size_t)i * Kp + k] + (T(1) - w) * (cin[(size_t)i * Kp + k] + tau * cdot[i]);
+    T cT2[N];
+    to_taylor<T, P>(cnew, af, cT2);
+#pragma unroll
+    for (int i = 0; i < N; ++i) { tbuf[(size_t)i * Kp + k] = cT2[i]; bad |= !finite_(cT2[i]); }
+    centroid_quantities<T, P>(cT2, lo.type, qv);
+  }
+  scatter_quantities<T, NQ>(g, lo, qv, vid, active);
   if (bad) atomicOr(sc.flag, 1);
 }
 
@@ -519,8 +570,8 @@ k_limit_dot(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0,
 // (core/applySlopeLimiterDisc.m:77-86).
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const T *__restrict__ vmm,
-        const LimArgs la, const StageScalars sc) {
+k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const LimIn<T> li,
+        const StageScalars sc) {
   constexpr int N = Dims<P>::N;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= g.K) return;
@@ -539,7 +590,7 @@ k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const T
       for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
     }
   }
-  limit_taylor<T, P>(g, vmm, la, k, af, vid, dmask, data, cT);
+  limit_taylor<T, P>(g, li, af, vid, dmask, data, cT);
   T c[N];
   from_taylor<T, P>(cT, af, c);
   bool bad = false;
@@ -551,21 +602,25 @@ k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const T
 // Modal state -> Taylor form and centroid quantities (initial limiting).
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_to_taylor(const Geo<T> g, const T *__restrict__ c, T *__restrict__ tbuf, T *__restrict__ q,
-            const LimArgs la, const StageScalars sc) {
-  constexpr int N = Dims<P>::N;
-  if (sc.gmm_reset && blockIdx.x == 0 && threadIdx.x < 2 * sc.nc_reset)
-    sc.gmm_reset[threadIdx.x] = (threadIdx.x & 1) ? 0ULL : key_max<T>();
+k_to_taylor(const Geo<T> g, const T *__restrict__ c, T *__restrict__ tbuf, const LimOut<T> lo) {
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= g.K) return;
-  const Affine<T> af = load_affine(g, k);
-  T cc[N], cT[N];
+  reset_next<T>(g, lo, k);
+  const bool active = k < g.K;
+  T qv[NQ];
+  int vid[3] = {0, 0, 0};
+  if (active) {
+    const Affine<T> af = load_affine(g, k);
+    T cc[N], cT[N];
 #pragma unroll
-  for (int i = 0; i < N; ++i) cc[i] = c[(size_t)i * g.Kp + k];
-  to_taylor<T, P>(cc, af, cT);
+    for (int i = 0; i < N; ++i) cc[i] = c[(size_t)i * g.Kp + k];
+    to_taylor<T, P>(cc, af, cT);
 #pragma unroll
-  for (int i = 0; i < N; ++i) tbuf[(size_t)i * g.Kp + k] = cT[i];
-  centroid_quantities<T, P>(cT, la.type, q, k, g.Kp);
+    for (int i = 0; i < N; ++i) tbuf[(size_t)i * g.Kp + k] = cT[i];
+    centroid_quantities<T, P>(cT, lo.type, qv);
+    vid[0] = g.V0T[k]; vid[1] = g.V0T[g.Kp + k]; vid[2] = g.V0T[2 * g.Kp + k];
+  }
+  scatter_quantities<T, NQ>(g, lo, qv, vid, active);
 }
 
 // External (caller order, K x N column-major, FP64) <-> internal (SoA, stride Kp, precision T).
@@ -586,13 +641,6 @@ __global__ void k_gather_out(int K, int Kp, int N, const int *__restrict__ perm,
   for (int i = 0; i < N; ++i) ext[(size_t)i * K + e] = double(c[(size_t)i * Kp + k]);
 }
 
-// ---------------------------------------------------------------------------------------------
-// Host side.
-struct DevBuf {
-  void *p = nullptr;
-  size_t bytes = 0;
-};
-
 }  // namespace dgadv
 
 struct dgadv_handle {
@@ -605,8 +653,11 @@ struct dgadv_handle {
   // device arrays (element type depends on prec)
   void *F = nullptr, *Vn = nullptr, *Bm = nullptr, *MT = nullptr, *rhs = nullptr, *cDV0T = nullptr;
   int *nbr = nullptr, *code = nullptr, *V0T = nullptr, *vptr = nullptr, *vidx = nullptr, *perm = nullptr;
-  void *cn = nullptr, *cA = nullptr, *cB = nullptr, *tbuf = nullptr, *q = nullptr, *vmm = nullptr;
-  unsigned long long *gmm = nullptr;   // 2 sets x 2 x nc
+  void *cn = nullptr, *cA = nullptr, *cB = nullptr, *tbuf = nullptr;
+  void *vkeys = nullptr;               // 3 passes x nc x 2 x Vp vertex min / max keys
+  unsigned long long *gmm = nullptr;   // 3 passes x 2 x nc encoded global extremes
+  long long limPass = 0;               // limiter passes enqueued so far (selects q / slot set)
+  int passesPerStep = 0;
   int *flag = nullptr;
   double *stage_ext = nullptr;         // K x N staging for set/get state
   int nTerms = 0;
@@ -617,10 +668,13 @@ struct dgadv_handle {
   std::vector<uint8_t> markNotN;              // internal order, 3 per element
   std::vector<int> permv;                     // internal -> external element id
   dgadv::RefTables tables;
-  // CUDA graph of one step
-  cudaGraphExec_t graph = nullptr;
-  double graphTau = -1.0;
-  int graphSteps = 0;
+  // CUDA graphs of a chunk of steps, one per phase (limPass mod 3) at the chunk start
+  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+  bool profiling = false;
+  std::vector<cudaEvent_t> profEvents;
+  std::vector<int> profKinds;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double graphTau[3] = {-1.0, -1.0, -1.0};
   std::string err;
 };
 
@@ -683,18 +737,44 @@ static int rk_table(int ord, double omega[3], double cstage[3]) {
   return 3;
 }
 
+template <typename T>
+static LimOut<T> lim_out(dgadv_handle *h) {
+  using K_ = typename KeyOf<T>::type;
+  const int set = (int)(h->limPass % 3), next = (set + 1) % 3;
+  const size_t vset = (size_t)2 * h->nc * h->Vp;
+  LimOut<T> o;
+  o.vkeys = (K_ *)h->vkeys + set * vset;
+  o.vreset = (K_ *)h->vkeys + next * vset;
+  o.slots = h->gmm + (size_t)set * 2 * h->nc;
+  o.reset = h->gmm + (size_t)next * 2 * h->nc;
+  o.nc = h->nc; o.type = h->limType;
+  return o;
+}
+template <typename T>
+static LimIn<T> lim_in(const LimOut<T> &o, const dgadv_handle *h) {
+  LimIn<T> i;
+  i.vkeys = o.vkeys; i.slots = o.slots; i.nc = o.nc; i.type = o.type;
+  i.shift = (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1;
+  return i;
+}
+
+// Optional per-kernel timing with CUDA events on the handle's stream (dgadv_profile_kernels).
+static void prof_mark(dgadv_handle *h, int kind) {
+  if (!h->profiling) return;
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, h->stream);
+  h->profEvents.push_back(e);
+  h->profKinds.push_back(kind);
+}
+
 template <typename T, int P>
 static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
   const Geo<T> g = make_geo<T>(h);
-  const int grid = (h->K + kBlock - 1) / kBlock;
-  const int vgrid = (h->numV + kBlock - 1) / kBlock;
+  const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;   // producers also reset vertex keys
   double omega[3], cst[3];
   const int S = rk_table(h->ordRK, omega, cst);
-  T *cn = (T *)h->cn, *cA = (T *)h->cA, *cB = (T *)h->cB, *tb = (T *)h->tbuf, *q = (T *)h->q;
-  T *vmm = (T *)h->vmm;
-  unsigned long long *gmmDot = h->gmm, *gmmSol = h->gmm + 2 * h->nc;
-  LimArgs laDot{h->limType, h->nc, (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1, gmmDot};
-  LimArgs laSol{h->limType, h->nc, (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1, gmmSol};
+  T *cn = (T *)h->cn, *cA = (T *)h->cA, *cB = (T *)h->cB, *tb = (T *)h->tbuf;
   const bool rhs = h->nTerms > 0 && h->rhs;
   for (int s = 0; s < S; ++s) {
     T *in = (s == 0) ? cn : (s == 1 ? cA : cB);
@@ -703,29 +783,43 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     sc.omega = omega[s]; sc.tau = tau; sc.flag = h->flag;
     const double ts = t0 + cst[s] * tau;
     for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = time_factor(h->timeFn[m], ts);
+    LimOut<T> lo{};
     if (!h->lim) {
-      if (rhs) k_stage_op<T, P, 0, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, out, q, laSol, sc);
-      else k_stage_op<T, P, 0, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, out, q, laSol, sc);
+      prof_mark(h, 0);
+      if (rhs) k_stage_op<T, P, 0, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, out, lo, sc);
+      else k_stage_op<T, P, 0, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, out, lo, sc);
+      prof_mark(h, -1);
+      continue;
+    }
+    // limiter boundary data at tBC = t(s+1) or t(1) + tau (advection/solveSubStep.m:88)
+    const double tBC = (s + 1 < S) ? t0 + cst[s + 1] * tau : t0 + tau;
+    StageScalars scBC = sc;
+    for (int m = 0; m < h->nTerms; ++m) scBC.gco[m] = time_factor(h->timeFn[m], tBC);
+    if (h->limdot) {
+      const LimOut<T> lo1 = lim_out<T>(h);
+      ++h->limPass;
+      prof_mark(h, 0);
+      if (rhs) k_stage_op<T, P, 2, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lo1, sc);
+      else k_stage_op<T, P, 2, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lo1, sc);
+      prof_mark(h, -1);
+      const LimOut<T> lo2 = lim_out<T>(h);
+      ++h->limPass;
+      prof_mark(h, 1);
+      k_limit_dot<T, P><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
+      prof_mark(h, -1);
+      prof_mark(h, 2);
+      k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, tb, out, lim_in<T>(lo2, h), scBC);
+      prof_mark(h, -1);
     } else {
-      // limiter boundary data at tBC = t(s+1) or t(1) + tau (advection/solveSubStep.m:88)
-      const double tBC = (s + 1 < S) ? t0 + cst[s + 1] * tau : t0 + tau;
-      StageScalars scBC = sc;
-      for (int m = 0; m < h->nTerms; ++m) scBC.gco[m] = time_factor(h->timeFn[m], tBC);
-      scBC.gmm_reset = nullptr;
-      if (h->limdot) {
-        StageScalars s1 = sc; s1.gmm_reset = gmmDot; s1.nc_reset = h->nc;
-        if (rhs) k_stage_op<T, P, 2, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, laDot, s1);
-        else k_stage_op<T, P, 2, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, laDot, s1);
-        k_vertex_minmax<T><<<vgrid, kBlock, 0, h->stream>>>(g, q, h->nc, vmm, gmmDot);
-        StageScalars s2 = sc; s2.gmm_reset = gmmSol; s2.nc_reset = h->nc;
-        k_limit_dot<T, P><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, vmm, laDot, laSol, s2);
-      } else {
-        StageScalars s1 = sc; s1.gmm_reset = gmmSol; s1.nc_reset = h->nc;
-        if (rhs) k_stage_op<T, P, 1, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, laSol, s1);
-        else k_stage_op<T, P, 1, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, q, laSol, s1);
-      }
-      k_vertex_minmax<T><<<vgrid, kBlock, 0, h->stream>>>(g, q, h->nc, vmm, gmmSol);
-      k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, tb, out, vmm, laSol, scBC);
+      const LimOut<T> lo1 = lim_out<T>(h);
+      ++h->limPass;
+      prof_mark(h, 0);
+      if (rhs) k_stage_op<T, P, 1, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lo1, sc);
+      else k_stage_op<T, P, 1, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lo1, sc);
+      prof_mark(h, -1);
+      prof_mark(h, 2);
+      k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, tb, out, lim_in<T>(lo1, h), scBC);
+      prof_mark(h, -1);
     }
   }
   if (S == 1)
@@ -736,17 +830,14 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
 template <typename T, int P>
 static cudaError_t launch_limit_state(dgadv_handle *h, double t) {
   const Geo<T> g = make_geo<T>(h);
-  const int grid = (h->K + kBlock - 1) / kBlock;
-  const int vgrid = (h->numV + kBlock - 1) / kBlock;
-  unsigned long long *gmmSol = h->gmm + 2 * h->nc;
-  LimArgs la{h->limType, h->nc, (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1, gmmSol};
+  const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;   // producers also reset vertex keys
   StageScalars sc{};
   sc.flag = h->flag;
   for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = time_factor(h->timeFn[m], t);
-  StageScalars s1 = sc; s1.gmm_reset = gmmSol; s1.nc_reset = h->nc;
-  k_to_taylor<T, P><<<grid, kBlock, 0, h->stream>>>(g, (const T *)h->cn, (T *)h->tbuf, (T *)h->q, la, s1);
-  k_vertex_minmax<T><<<vgrid, kBlock, 0, h->stream>>>(g, (const T *)h->q, h->nc, (T *)h->vmm, gmmSol);
-  k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, (const T *)h->tbuf, (T *)h->cn, (const T *)h->vmm, la, sc);
+  const LimOut<T> lo = lim_out<T>(h);
+  ++h->limPass;
+  k_to_taylor<T, P><<<grid, kBlock, 0, h->stream>>>(g, (const T *)h->cn, (T *)h->tbuf, lo);
+  k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, (const T *)h->tbuf, (T *)h->cn, lim_in<T>(lo, h), sc);
   return cudaGetLastError();
 }
 
@@ -834,6 +925,7 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   h->lim = prm->isSlopeLim ? 1 : 0; h->limType = prm->typeSlopeLim; h->flags = prm->flags;
   h->limdot = h->lim && h->p > 1;
   h->nc = h->lim ? (h->limType == DGADV_LIM_LINEAR ? 1 : h->p * (h->p + 1) / 2) : 1;
+  h->passesPerStep = h->lim ? h->ordRK * (h->limdot ? 2 : 1) : 0;
   DG_CUDA(cudaSetDevice(h->device));
   DG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   // static grid data (core/generateGridData.m semantics)
@@ -942,9 +1034,8 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   if ((st = dev_alloc(h, &h->cA, (size_t)N * Kp * w))) return st;
   if ((st = dev_alloc(h, &h->cB, (size_t)N * Kp * w))) return st;
   if ((st = dev_alloc(h, &h->tbuf, (size_t)N * Kp * w))) return st;
-  if ((st = dev_alloc(h, &h->q, (size_t)nc * Kp * w))) return st;
-  if ((st = dev_alloc(h, &h->vmm, 2 * (size_t)nc * h->Vp * w))) return st;
-  if ((st = dev_alloc(h, (void **)&h->gmm, 4 * (size_t)nc * 8))) return st;
+  if ((st = dev_alloc(h, &h->vkeys, 3 * 2 * (size_t)nc * h->Vp * w))) return st;
+  if ((st = dev_alloc(h, (void **)&h->gmm, 6 * (size_t)nc * 8))) return st;
   if ((st = dev_alloc(h, (void **)&h->flag, 16))) return st;
   if ((st = dev_alloc(h, (void **)&h->stage_ext, (size_t)N * K * 8))) return st;
   DG_CUDA(cudaMemset(h->F, 0, 2 * (size_t)Q * Kp * w));
@@ -953,7 +1044,20 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   DG_CUDA(cudaMemset(h->cA, 0, (size_t)N * Kp * w));
   DG_CUDA(cudaMemset(h->cB, 0, (size_t)N * Kp * w));
   DG_CUDA(cudaMemset(h->tbuf, 0, (size_t)N * Kp * w));
-  DG_CUDA(cudaMemset(h->q, 0, (size_t)nc * Kp * w));
+  {
+    // vertex keys of every pass start reset (min = largest key, max = 0)
+    std::vector<unsigned char> vk(3 * 2 * (size_t)nc * h->Vp * w, 0);
+    for (size_t set = 0; set < 3 * (size_t)nc; ++set)
+      std::memset(vk.data() + set * 2 * h->Vp * w, 0xFF, (size_t)h->Vp * w);
+    if ((st = upload(h, h->vkeys, vk.data(), vk.size()))) return st;
+  }
+  {
+    // slots of pass 0 start reset; every later pass is reset by the previous producer
+    std::vector<unsigned long long> init(6 * (size_t)nc);
+    const unsigned long long kmax = h->prec == DGADV_FP64 ? ~0ULL : 0xFFFFFFFFULL;
+    for (size_t i = 0; i < init.size(); ++i) init[i] = (i & 1) ? 0ULL : kmax;
+    if ((st = upload(h, h->gmm, init.data(), init.size() * 8))) return st;
+  }
   DG_CUDA(cudaMemset(h->flag, 0, 16));
   if (h->prec == DGADV_FP64) { if ((st = upload_real<double>(h, h->Bm, Bsoa))) return st; }
   else { if ((st = upload_real<float>(h, h->Bm, Bsoa))) return st; }
@@ -1047,7 +1151,8 @@ extern "C" int dgadv_set_source_terms(dgadv_handle *h, int32_t nTerms, const int
     if (timeFn[m] != DGADV_TIME_CONST && timeFn[m] != DGADV_TIME_EXP_NEG) return DGADV_EINVAL;
   h->nTerms = nTerms;
   for (int m = 0; m < 4; ++m) h->timeFn[m] = m < nTerms ? timeFn[m] : 0;
-  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  for (int i = 0; i < 3; ++i)
+    if (h->graph[i]) { cudaGraphExecDestroy(h->graph[i]); h->graph[i] = nullptr; }
   if (nTerms == 0) return DGADV_OK;
   std::vector<double> r((size_t)nTerms * N * Kp, 0.0), d((size_t)nTerms * 3 * Kp, 0.0);
   for (int m = 0; m < nTerms; ++m)
@@ -1137,29 +1242,33 @@ extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, doubl
     }
     return DGADV_OK;
   }
-  // time-independent data: one captured graph of several steps, replayed
-  const int chunk = 10;
-  if (!h->graph || h->graphTau != tau) {
-    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
-    cudaGraph_t gph;
-    DG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaSuccess;
-    for (int s = 0; s < chunk && e == cudaSuccess; ++s)
-      e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, 0.0, tau) : dispatch_step<float>(h, 0.0, tau);
-    cudaError_t e2 = cudaStreamEndCapture(h->stream, &gph);
-    if (e != cudaSuccess || e2 != cudaSuccess) {
-      h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
-      return DGADV_ECUDA;
-    }
-    DG_CUDA(cudaGraphInstantiate(&h->graph, gph, 0));
-    cudaGraphDestroy(gph);
-    h->graphTau = tau;
-    h->graphSteps = chunk;
-  }
+  // time-independent data: a captured graph of a chunk of steps, replayed.  The chunk makes a
+  // multiple of three limiter passes, so the pass phase is the same before and after it.
+  const int chunk = 12;
   int done = 0;
-  while (nSteps - done >= h->graphSteps) {
-    DG_CUDA(cudaGraphLaunch(h->graph, h->stream));
-    done += h->graphSteps;
+  while (nSteps - done >= chunk) {
+    const int ph = (int)(h->limPass % 3);
+    if (!h->graph[ph] || h->graphTau[ph] != tau) {
+      if (h->graph[ph]) { cudaGraphExecDestroy(h->graph[ph]); h->graph[ph] = nullptr; }
+      const long long saved = h->limPass;
+      cudaGraph_t gph;
+      DG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = cudaSuccess;
+      for (int s = 0; s < chunk && e == cudaSuccess; ++s)
+        e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, 0.0, tau) : dispatch_step<float>(h, 0.0, tau);
+      cudaError_t e2 = cudaStreamEndCapture(h->stream, &gph);
+      h->limPass = saved;
+      if (e != cudaSuccess || e2 != cudaSuccess) {
+        h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+        return DGADV_ECUDA;
+      }
+      DG_CUDA(cudaGraphInstantiate(&h->graph[ph], gph, 0));
+      cudaGraphDestroy(gph);
+      h->graphTau[ph] = tau;
+    }
+    DG_CUDA(cudaGraphLaunch(h->graph[ph], h->stream));
+    h->limPass += (long long)chunk * h->passesPerStep;
+    done += chunk;
   }
   for (; done < nSteps; ++done) {
     cudaError_t e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, 0.0, tau) : dispatch_step<float>(h, 0.0, tau);
@@ -1168,12 +1277,58 @@ extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, doubl
   return DGADV_OK;
 }
 
+extern "C" int dgadv_time_steps(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau, double *ms) {
+  if (!h || !ms) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  if (!h->ev0) { DG_CUDA(cudaEventCreate(&h->ev0)); DG_CUDA(cudaEventCreate(&h->ev1)); }
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  DG_CUDA(cudaEventRecord(h->ev0, h->stream));
+  int st = dgadv_step(h, nSteps, nStep0, tau);
+  if (st) return st;
+  DG_CUDA(cudaEventRecord(h->ev1, h->stream));
+  DG_CUDA(cudaEventSynchronize(h->ev1));
+  float f = 0;
+  DG_CUDA(cudaEventElapsedTime(&f, h->ev0, h->ev1));
+  *ms = f;
+  return dgadv_sync(h);
+}
+
+extern "C" int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau,
+                                     double *msPerLaunch, int32_t *launches) {
+  if (!h || !msPerLaunch || !launches || nSteps < 1) return DGADV_EINVAL;
+  if (!h->hasVelocity) { h->err = "dgadv_set_velocity was not called"; return DGADV_EINVAL; }
+  DG_CUDA(cudaSetDevice(h->device));
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  h->profiling = true;
+  h->profEvents.clear(); h->profKinds.clear();
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < nSteps && e == cudaSuccess; ++s) {
+    const double t0 = (double)(nStep0 + s) * tau;
+    e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, t0, tau) : dispatch_step<float>(h, t0, tau);
+  }
+  h->profiling = false;
+  cudaError_t e2 = cudaStreamSynchronize(h->stream);
+  for (int k = 0; k < 4; ++k) { msPerLaunch[k] = 0; launches[k] = 0; }
+  for (size_t i = 0; i + 1 < h->profEvents.size(); i += 2) {
+    float f = 0;
+    if (e2 == cudaSuccess) cudaEventElapsedTime(&f, h->profEvents[i], h->profEvents[i + 1]);
+    const int kind = h->profKinds[i];
+    if (kind >= 0 && kind < 4) { msPerLaunch[kind] += f; launches[kind] += 1; }
+  }
+  for (cudaEvent_t ev : h->profEvents) cudaEventDestroy(ev);
+  h->profEvents.clear(); h->profKinds.clear();
+  for (int k = 0; k < 4; ++k)
+    if (launches[k]) msPerLaunch[k] /= launches[k];
+  if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
+  if (e2 != cudaSuccess) { h->err = cudaGetErrorString(e2); return DGADV_ECUDA; }
+  return dgadv_sync(h);
+}
+
 extern "C" int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count) {
   if (!h || !count) return DGADV_EINVAL;
-  const int S = h->ordRK;
   int perStage = 1;
-  if (h->lim) perStage = h->limdot ? 5 : 3;
-  *count = S * perStage + (S == 1 ? 0 : 0);
+  if (h->lim) perStage = h->limdot ? 3 : 2;
+  *count = h->ordRK * perStage;
   return DGADV_OK;
 }
 
@@ -1183,7 +1338,10 @@ extern "C" void dgadv_destroy(dgadv_handle *h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (int i = 0; i < 3; ++i)
+    if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
   for (void *p : h->allocs) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;

@@ -94,6 +94,21 @@ class DeviceSolver:
     def sync(self):
         self._c(self._lib.dgadv_sync(self._h))
 
+    def time_steps(self, nSteps, nStep0, tau):
+        """Device time (ms) of nSteps, from CUDA events on the library's stream."""
+        ms = ctypes.c_double()
+        self._c(self._lib.dgadv_time_steps(self._h, int(nSteps), int(nStep0), float(tau), ctypes.byref(ms)))
+        return ms.value
+
+    def profile_kernels(self, nSteps, nStep0, tau):
+        """Mean device ms per launch and launch counts of the kernel kinds
+        (stage operator, time-derivative limiter, solution limiter)."""
+        ms = np.zeros(4)
+        n = np.zeros(4, dtype=np.int32)
+        self._c(self._lib.dgadv_profile_kernels(self._h, int(nSteps), int(nStep0), float(tau),
+                                                L.ptr(ms), L.ptr(n, L._i32p)))
+        return ms[:3], n[:3]
+
     def kernels_per_step(self):
         n = ctypes.c_int32()
         self._c(self._lib.dgadv_kernels_per_step(self._h, ctypes.byref(n)))

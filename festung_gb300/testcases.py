@@ -92,7 +92,8 @@ def configure(pd):
     tc = pd['testcase']
     pd['fTerms'] = []
     pd['cDTerms'] = []
-    pd.setdefault('jitter', 0.0)
+    if pd.get('jitter') is None:
+        pd['jitter'] = 0.2 if tc == 'ensemble' else 0.0
     pd.setdefault('meshSeed', 0)
     if tc in ('solid_body', 'gauss_slot'):
         pd['isAnalytical'] = False
@@ -129,7 +130,6 @@ def configure(pd):
         pd['isAnalytical'] = False
         prm = ensemble_params(pd['instanceSeed'])
         pd['ensembleParams'] = prm
-        pd['jitter'] = pd.get('jitter') or 0.2
         pd['meshSeed'] = prm['mesh_seed']
         pd['u1Cont'], pd['u2Cont'] = streamfunction_velocity(prm['k'], prm['l'], prm['a'])
         cx, cy = prm['centre']; w2 = prm['width'] ** 2

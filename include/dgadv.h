@@ -112,7 +112,8 @@ typedef struct dgadv_params {
 typedef struct dgadv_handle dgadv_handle;
 
 /* Replaces the device-independent part of advection/preprocessProblem.m:48-112: grid, tables,
- * mass and Taylor data for one mesh; uploads everything once. */
+ * mass and Taylor data for one mesh; uploads everything once.  On failure *out may still hold a
+ * handle (so that dgadv_last_error can explain); release it with dgadv_destroy. */
 int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *params, dgadv_handle **out);
 
 /* Velocity data of advection/preprocessSubStep.m:72-79: u1Disc, u2Disc (K x N, projections of
@@ -143,6 +144,16 @@ int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau);
 
 /* Waits for enqueued work; reports DGADV_ENONFINITE if a kernel saw NaN/Inf. */
 int dgadv_sync(dgadv_handle *h);
+
+/* Runs dgadv_step between two CUDA events recorded on the handle's stream and waits; *ms is
+ * the device time of the enqueued steps. */
+int dgadv_time_steps(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau, double *ms);
+
+/* Runs nSteps with one launch per kernel and CUDA events around every launch; writes the mean
+ * device time per launch (ms) and the launch count for each kernel kind:
+ * [0] stage operator, [1] time-derivative limiter + SSP, [2] solution limiter, [3] unused. */
+int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau,
+                          double *msPerLaunch, int32_t *launches);
 
 /* Number of kernels one time step launches (for launch accounting). */
 int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count);
