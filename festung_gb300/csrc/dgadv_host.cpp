@@ -644,4 +644,65 @@ void taylor_mass_packed(const Grid &g, int p, std::vector<double> &out) {
   }
 }
 
+// Coefficients of (a + b z)^(D-m) (c + e z)^m in z^j (row m, column j).
+static void deriv_block_host(double a, double b, double c, double e, int D, std::vector<double> &S) {
+  S.assign((D + 1) * (D + 1), 0.0);
+  for (int m = 0; m <= D; ++m) {
+    std::vector<double> poly(D + 1, 0.0);
+    poly[0] = 1.0;
+    for (int r = 0; r < D; ++r) {
+      const bool first = r < D - m;
+      const double x0 = first ? a : c, x1 = first ? b : e;
+      for (int j = D; j >= 0; --j) poly[j] = poly[j] * x0 + (j > 0 ? poly[j - 1] * x1 : 0.0);
+    }
+    for (int j = 0; j <= D; ++j) S[m * (D + 1) + j] = poly[j];
+  }
+}
+
+void taylor_correction(const Grid &g, int p, const RefTables &t, std::vector<double> &out) {
+  const int N = N_of_p(p), P = N * (N + 1) / 2;
+  std::vector<double> mt;
+  taylor_mass_packed(g, p, mt);
+  out.assign((size_t)g.numT * N * (N - 1), 0.0);
+  std::vector<double> S(N * N), Si(N * N), M(N * N), W(N * N), blk;
+  for (int k = 0; k < g.numT; ++k) {
+    const double B11 = g.B[4 * (size_t)k], B12 = g.B[4 * (size_t)k + 1];
+    const double B21 = g.B[4 * (size_t)k + 2], B22 = g.B[4 * (size_t)k + 3];
+    const double det = B11 * B22 - B12 * B21;
+    const double A11 = B22 / det, A12 = -B12 / det, A21 = -B21 / det, A22 = B11 / det;
+    const double dX = 2 / std::sqrt(g.detJ0T[k]);
+    std::fill(S.begin(), S.end(), 0.0);
+    std::fill(Si.begin(), Si.end(), 0.0);
+    S[0] = 1.0; Si[0] = 1.0;
+    for (int d = 1; d <= p; ++d) {
+      const int off = d * (d + 1) / 2;
+      deriv_block_host(A11, A21, A12, A22, d, blk);
+      for (int m = 0; m <= d; ++m)
+        for (int j = 0; j <= d; ++j) S[(off + m) * N + off + j] = blk[m * (d + 1) + j] / std::pow(dX, d);
+      deriv_block_host(B11, B21, B12, B22, d, blk);
+      for (int m = 0; m <= d; ++m)
+        for (int j = 0; j <= d; ++j) Si[(off + m) * N + off + j] = blk[m * (d + 1) + j] * std::pow(dX, d);
+    }
+    // Mcorr from the packed Taylor mass block
+    const double *pk = &mt[(size_t)k * P];
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        const int a = std::min(i, j), b = std::max(i, j);
+        M[i * N + j] = pk[a * N - a * (a - 1) / 2 + (b - a)];
+      }
+    for (int i = 0; i < N; ++i) {
+      const double dii = M[i * N + i];
+      for (int j = 0; j < N; ++j) W[i * N + j] = M[i * N + j] / dii;
+    }
+    std::vector<double> T1, T2;
+    matmul(Si, W, N, T1);     // S^-1 Mcorr
+    matmul(T1, S, N, T2);     // S^-1 Mcorr S
+    for (int i = 0; i < N; ++i) T2[i * N + i] -= 1.0;
+    std::vector<double> Qk;
+    matmul(t.DMinv, T2, N, Qk);
+    for (int i = 0; i < N; ++i)
+      for (int j = 1; j < N; ++j) out[((size_t)k * N + i) * (N - 1) + (j - 1)] = Qk[i * N + j];
+  }
+}
+
 }  // namespace dgadv

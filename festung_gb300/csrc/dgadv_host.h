@@ -55,4 +55,10 @@ bool build_grid(int numV, const double *coordV_colmajor, int numT, const int32_t
 // triangle (i <= j) row by row, for every element.  Size numT x N(N+1)/2.
 void taylor_mass_packed(const Grid &g, int p, std::vector<double> &out);
 
+// Time-derivative limiting correction of the linear limiter in reference-derivative
+// coordinates: Q_k = DM^-1 (S_k^-1 Mcorr_k S_k - I), columns 1..N-1, for every element
+// (numT x N x (N-1), row-major per element).  S_k maps reference derivatives at the barycentre
+// to the element's Taylor coefficients; Mcorr_k = diag(1/diag(M_T)) M_T.
+void taylor_correction(const Grid &g, int p, const RefTables &t, std::vector<double> &out);
+
 }  // namespace dgadv

@@ -52,6 +52,7 @@ template <> __device__ __forceinline__ const Tab<float, 2> &tab<float, 2>() { re
 template <> __device__ __forceinline__ const Tab<float, 3> &tab<float, 3>() { return cTf3; }
 
 constexpr int kBlock = 128;
+constexpr int kSlotCopies = 32;   // copies of the global min / max slots (atomics spread over them)
 
 // ---------------------------------------------------------------------------------------------
 // Ordered integer keys: atomicMin/atomicMax on the key order like on the real numbers.
@@ -245,13 +246,13 @@ template <typename T> __host__ __device__ constexpr typename KeyOf<T>::type vkey
 template <typename T> struct LimOut {
   typename KeyOf<T>::type *vkeys;   // nc x 2 x Vp vertex min / max keys of this pass
   typename KeyOf<T>::type *vreset;  // the next pass's vertex keys, reset here
-  unsigned long long *slots;        // 2 x nc encoded global min / max (atomic)
+  unsigned long long *slots;        // kSlotCopies x 2 x nc encoded global min / max (atomic)
   unsigned long long *reset;        // slots of the next pass, reset by block 0
   int nc, type;
 };
 template <typename T> struct LimIn {
   const typename KeyOf<T>::type *vkeys;
-  const unsigned long long *slots;
+  const unsigned long long *slots;  // kSlotCopies x 2 x nc
   int nc, type, shift;
 };
 
@@ -271,18 +272,30 @@ __device__ __forceinline__ void scatter_quantities(const Geo<T> &g, const LimOut
       }
     }
   }
+  // global extremes: warp shuffles, then the block's four warps through shared memory, then one
+  // atomic per quantity and block into one of kSlotCopies copies (spreads same-address atomics)
+  __shared__ T red[kBlock / 32][2 * NQ];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int s = 0; s < NQ; ++s) {
-    if (s >= lo.nc) break;
-    T mn = active ? qv[s] : T(INFINITY), mx = active ? qv[s] : T(-INFINITY);
+    T mn = (active && s < lo.nc) ? qv[s] : T(INFINITY), mx = (active && s < lo.nc) ? qv[s] : T(-INFINITY);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
       mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     }
-    if ((threadIdx.x & 31) == 0 && mn <= mx) {
-      atomicMin(&lo.slots[2 * s], okey(mn));
-      atomicMax(&lo.slots[2 * s + 1], okey(mx));
+    if (lane == 0) { red[warp][2 * s] = mn; red[warp][2 * s + 1] = mx; }
+  }
+  __syncthreads();
+  if (threadIdx.x < lo.nc) {
+    const int s = threadIdx.x;
+    T mn = red[0][2 * s], mx = red[0][2 * s + 1];
+#pragma unroll
+    for (int w = 1; w < kBlock / 32; ++w) { mn = fmin(mn, red[w][2 * s]); mx = fmax(mx, red[w][2 * s + 1]); }
+    if (mn <= mx) {
+      unsigned long long *sl = lo.slots + (size_t)(blockIdx.x % kSlotCopies) * 2 * lo.nc;
+      atomicMin(&sl[2 * s], okey(mn));
+      atomicMax(&sl[2 * s + 1], okey(mx));
     }
   }
 }
@@ -295,8 +308,27 @@ __device__ __forceinline__ void reset_next(const Geo<T> &g, const LimOut<T> &lo,
       lo.vreset[(size_t)(2 * s) * g.Vp + t] = vkey_max<T>();
       lo.vreset[(size_t)(2 * s + 1) * g.Vp + t] = 0;
     }
-  if (blockIdx.x == 0 && threadIdx.x < 2 * lo.nc)
-    lo.reset[threadIdx.x] = (threadIdx.x & 1) ? 0ULL : key_max<T>();
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < kSlotCopies * 2 * lo.nc; i += blockDim.x)
+      lo.reset[i] = (i & 1) ? 0ULL : key_max<T>();
+}
+
+// Global extremes of every quantity from the kSlotCopies copies (warp 0), turned into the shift
+// values of core/computeMinMaxV0TElementPatch.m:75-78: sh[2s] = |min|+1, sh[2s+1] = |max|+1.
+template <typename T>
+__device__ __forceinline__ void load_shifts(const unsigned long long *slots, int nc, T *sh) {
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  for (int s = 0; s < nc; ++s) {
+    T mn = okey_inv<T>(slots[(size_t)lane * 2 * nc + 2 * s]);
+    T mx = okey_inv<T>(slots[(size_t)lane * 2 * nc + 2 * s + 1]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (lane == 0) { sh[2 * s] = fabs(mn) + T(1); sh[2 * s + 1] = fabs(mx) + T(1); }
+  }
 }
 
 // alpha of one computeVertexBasedLimiter call (core/computeVertexBasedLimiter.m:78-106)
@@ -315,23 +347,136 @@ __device__ __forceinline__ T vertex_alpha(T cbar, const T v[3], const T mn[3], c
   return alpha;
 }
 
-// Patch min / max of quantity s at the three vertices (read from the pass's vertex keys),
-// with the reference's global shift (min over the patch of (v - sNeg), then + sNeg; a monotone
-// shift commutes with min), then combined with the Dirichlet data (NaN = none; fmin / fmax
-// ignore NaN like Matlab's min / max).
+// ---------------------------------------------------------------------------------------------
+// Block staging: the rows of one block's elements (SoA rows, kBlock consecutive elements each)
+// are copied global -> shared by the TMA unit (cp.async.bulk, one elected thread) while the
+// threads load neighbour and vertex data directly.  The wait on the mbarrier is bounded in time;
+// on a timeout the kernel sets bit 1 of the error flag and leaves the element unprocessed.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for phase 0 of the block's barrier, at most ~2^31 SM cycles (about a second); after a
+// timeout it flags the error, gives the copies in flight the same time again, and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *flag) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, 0))
+    if (clock64() - t0 > (1LL << 31)) {
+      atomicOr(flag, 2);
+      const long long t1 = clock64();
+      while (!mbar_try_wait(bar, 0) && clock64() - t1 < (1LL << 31)) {
+      }
+      return false;
+    }
+  return true;
+}
+
+// Row copies into the staged layout (row index within the T rows / the int rows).
 template <typename T>
-__device__ __forceinline__ void patch_minmax(const Geo<T> &g, const LimIn<T> &li, int s, const int vid[3],
+__device__ __forceinline__ void stage_T(unsigned char *smem, int row, const T *base, int nrows, int Kp, int k0,
+                                        uint64_t *bar) {
+  for (int r = 0; r < nrows; ++r)
+    bulk_g2s(smem + (size_t)(row + r) * kBlock * sizeof(T), base + (size_t)r * Kp + k0, kBlock * sizeof(T), bar);
+}
+template <typename T>
+__device__ __forceinline__ void stage_I(unsigned char *smem, int nT, int row, const int *base, int nrows, int Kp,
+                                        int k0, uint64_t *bar) {
+  for (int r = 0; r < nrows; ++r)
+    bulk_g2s(smem + (size_t)nT * kBlock * sizeof(T) + (size_t)(row + r) * kBlock * sizeof(int),
+             base + (size_t)r * Kp + k0, kBlock * sizeof(int), bar);
+}
+template <typename T>
+__device__ __forceinline__ void stage_expect(uint64_t *bar, int nT, int nI) {
+  mbar_expect_tx(bar, nT * kBlock * (uint32_t)sizeof(T) + nI * kBlock * (uint32_t)sizeof(int));
+}
+
+// Programmatic dependent launch: the next kernel in the stream may start its prologue (static
+// data only) once every block of this one has started; pdl_wait() blocks until the previous
+// kernel has completed and its writes are visible.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename T> __device__ __forceinline__ const T *srow(const unsigned char *smem, int r) {
+  return (const T *)(smem + (size_t)r * kBlock * sizeof(T));
+}
+template <typename T> __device__ __forceinline__ const int *irow(const unsigned char *smem, int nT, int r) {
+  return (const int *)(smem + (size_t)nT * kBlock * sizeof(T) + (size_t)r * kBlock * sizeof(int));
+}
+
+template <typename T, int P> struct StageRows {
+  static constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NMT = Dims<P>::NMT;
+  // k_stage_op: c, [c0], F, Vn, [B] | code
+  __host__ __device__ static constexpr int op(int mode, bool lin) {
+    return N + (mode != 2 ? N : 0) + 2 * Q + 3 * R + (mode != 0 && !lin ? 4 : 0);
+  }
+  // k_limit_dot: tbuf, B, MT, c0, cin | code
+  __host__ __device__ static constexpr int limdot() { return N + 4 + NMT + 2 * N; }
+  // k_limit: tbuf, B | code
+  __host__ __device__ static constexpr int lim() { return N + 4; }
+  // k_limit_dot_lin: cDot, Q (N x (N-1)), c0, cin | code
+  __host__ __device__ static constexpr int limdot_lin() { return N + N * (N - 1) + 2 * N; }
+  // k_to_taylor: c, B
+  __host__ __device__ static constexpr int totaylor() { return N + 4; }
+  // rows first, then the block's mbarrier (8 bytes, 16 reserved)
+  __host__ __device__ static constexpr size_t bar_offset(int nT, int nI) {
+    return (size_t)nT * kBlock * sizeof(T) + (size_t)nI * kBlock * sizeof(int);
+  }
+  // + 16 for the mbarrier, + 2 x 6 shift values
+  __host__ __device__ static constexpr size_t bytes(int nT, int nI) { return bar_offset(nT, nI) + 16 + 12 * sizeof(T); }
+};
+
+// Prefetch of the three vertices' min / max keys of every sub-limiter quantity.
+template <typename T, int NQ> struct VKeys {
+  typename KeyOf<T>::type v[NQ][2][3];
+};
+template <typename T, int NQ>
+__device__ __forceinline__ void load_vkeys(const Geo<T> &g, const LimIn<T> &li, const int vid[3], VKeys<T, NQ> &kv) {
+#pragma unroll
+  for (int s = 0; s < NQ; ++s)
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+      for (int n = 0; n < 3; ++n)
+        kv.v[s][m][n] = (s < li.nc) ? li.vkeys[(size_t)(2 * s + m) * g.Vp + vid[n]] : 0;
+}
+
+// Patch min / max of quantity s at the three vertices (from the prefetched vertex keys), with
+// the reference's global shift (min over the patch of (v - sNeg), then + sNeg; a monotone shift
+// commutes with min), then combined with the Dirichlet data (NaN = none; fmin / fmax ignore NaN
+// like Matlab's min / max).
+template <typename T, int NQ>
+__device__ __forceinline__ void patch_minmax(const LimIn<T> &li, const VKeys<T, NQ> &kv, const T *sh, int s,
                                              const T valD[3], T mn[3], T mx[3]) {
   T sNeg = 0, sPos = 0;
-  if (li.shift) {
-    const T gmin = okey_inv<T>(li.slots[2 * s]), gmax = okey_inv<T>(li.slots[2 * s + 1]);
-    sPos = fabs(gmin) + T(1);
-    sNeg = fabs(gmax) + T(1);
-  }
+  if (li.shift) { sPos = sh[2 * s]; sNeg = sh[2 * s + 1]; }
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
-    T a = vkey_inv<T>(li.vkeys[(size_t)(2 * s) * g.Vp + vid[n]]);
-    T c = vkey_inv<T>(li.vkeys[(size_t)(2 * s + 1) * g.Vp + vid[n]]);
+    T a = vkey_inv<T>(kv.v[s][0][n]);
+    T c = vkey_inv<T>(kv.v[s][1][n]);
     if (li.shift) { a = (a - sNeg) + sNeg; c = (c + sPos) - sPos; }
     mn[n] = fmin(a, valD[n]);
     mx[n] = fmax(c, valD[n]);
@@ -340,9 +485,9 @@ __device__ __forceinline__ void patch_minmax(const Geo<T> &g, const LimIn<T> &li
 
 // Limit Taylor coefficients in place (linear / hierarchical vertex).  dataV0T: boundary values
 // at the three vertices for Dirichlet vertices (NaN means "no data").
-template <typename T, int P>
-__device__ __forceinline__ void limit_taylor(const Geo<T> &g, const LimIn<T> &li, const Affine<T> &af,
-                                             const int vid[3], int dmask, const T dataV0T[3], T *cT) {
+template <typename T, int P, int NQ>
+__device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, NQ> &kv, const T *sh,
+                                             const Affine<T> &af, int dmask, const T dataV0T[3], T *cT) {
   constexpr int N = Dims<P>::N;
   const T nan_ = T(NAN);
   T pt1[3], pt2[3];   // Taylor basis functions 2 and 3 at the vertices
@@ -355,7 +500,7 @@ __device__ __forceinline__ void limit_taylor(const Geo<T> &g, const LimIn<T> &li
       v[n] = (cT[0] * T(1) + cT[1] * pt1[n]) + cT[2] * pt2[n];
       valD[n] = ((dmask >> n) & 1) ? dataV0T[n] : nan_;
     }
-    patch_minmax(g, li, 0, vid, valD, mn, mx);
+    patch_minmax<T, NQ>(li, kv, sh, 0, valD, mn, mx);
     const T alpha = vertex_alpha(cT[0], v, mn, mx);
     cT[1] *= alpha; cT[2] *= alpha;
     const T keep = (alpha == T(1)) ? T(1) : T(0);
@@ -379,7 +524,7 @@ __device__ __forceinline__ void limit_taylor(const Geo<T> &g, const LimIn<T> &li
           v[n] = (orig[i0] * T(1) + orig[i1] * pt1[n]) + orig[i2] * pt2[n];
           valD[n] = ((dmask >> n) & 1) ? (ord > 1 ? v[n] : dataV0T[n]) : nan_;
         }
-        patch_minmax(g, li, s, vid, valD, mn, mx);
+        patch_minmax<T, NQ>(li, kv, sh, s, valD, mn, mx);
         aOrd = fmin(aOrd, vertex_alpha(orig[i0], v, mn, mx));
         ++s;
       }
@@ -390,32 +535,142 @@ __device__ __forceinline__ void limit_taylor(const Geo<T> &g, const LimIn<T> &li
   }
 }
 
+// Element geometry from staged rows of B.
+template <typename T> __device__ __forceinline__ Affine<T> affine_from(T B11, T B12, T B21, T B22) {
+  Affine<T> a;
+  a.B11 = B11; a.B12 = B12; a.B21 = B21; a.B22 = B22;
+  const T det = a.B11 * a.B22 - a.B12 * a.B21;
+  const T idet = T(1) / det;
+  a.A11 = a.B22 * idet; a.A12 = -a.B12 * idet; a.A21 = -a.B21 * idet; a.A22 = a.B11 * idet;
+  a.dX = T(2) / sqrt(det);
+  a.idX = T(1) / a.dX;
+  const T bx = -(a.B11 + a.B12) / T(3), by = -(a.B21 + a.B22) / T(3);
+  a.ox[0] = bx; a.oy[0] = by;
+  a.ox[1] = a.B11 + bx; a.oy[1] = a.B21 + by;
+  a.ox[2] = a.B12 + bx; a.oy[2] = a.B22 + by;
+  return a;
+}
+
 // ---------------------------------------------------------------------------------------------
-// Stage operator.  MODE 0: write c^(s);  MODE 1: write Taylor(c^(s)) and its centroid
-// quantities;  MODE 2: write Taylor(cDot) and its quantities (time-derivative limiting follows).
+// Linear limiter without element geometry.  The centroid value and the vertex values of the
+// linear Taylor reconstruction (core/applySlopeLimiterTaylorLinear.m:108-122) are
+//     cbar = u_0,   v_n = u_0 + u_1 (x^_n - c^)_1 + u_2 (x^_n - c^)_2,   u = DM c,
+// because grad u(b) . (x_n - b) is invariant under the affine map to the reference element
+// (x^_n the reference vertices, c^ = (1/3, 1/3)).  Scaling Taylor degree blocks commutes with
+// the block-diagonal map between reference derivatives and Taylor coefficients, so the limited
+// coefficients are c - DM^-1 du with du = (0, (1-a) u_1, (1-a) u_2, [a != 1] u_3, ...).
+template <typename T, int P>
+__device__ __forceinline__ void lin_u(const T *c, T *u) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    T s = T(0);
+#pragma unroll
+    for (int j = 0; j < N; ++j) s += tb.DM[i][j] * c[j];
+    u[i] = s;
+  }
+}
+template <typename T, int P> __device__ __forceinline__ T lin_mean(const T *c) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T s = T(0);
+#pragma unroll
+  for (int j = 0; j < N; ++j) s += tb.DM[0][j] * c[j];
+  return s;
+}
+// alpha of the linear limiter from u, and the removed part du (returns false if alpha == 1).
+template <typename T, int P, int NQ>
+__device__ __forceinline__ bool lin_alpha(const LimIn<T> &li, const VKeys<T, NQ> &kv, const T *sh, const T *u,
+                                          int dmask, const T dataV0T[3], T *du) {
+  constexpr int N = Dims<P>::N;
+  const T third = T(1) / T(3), two3 = T(2) / T(3);
+  const T hx[3] = {-third, two3, -third}, hy[3] = {-third, -third, two3};
+  T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    v[n] = (u[0] * T(1) + u[1] * hx[n]) + u[2] * hy[n];
+    valD[n] = ((dmask >> n) & 1) ? dataV0T[n] : T(NAN);
+  }
+  patch_minmax<T, NQ>(li, kv, sh, 0, valD, mn, mx);
+  const T alpha = vertex_alpha(u[0], v, mn, mx);
+  if (alpha == T(1)) return false;
+  du[0] = T(0);
+  du[1] = (T(1) - alpha) * u[1];
+  du[2] = (T(1) - alpha) * u[2];
+#pragma unroll
+  for (int i = 3; i < N; ++i) du[i] = u[i];
+  return true;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Stage operator.  MODE 0: write c^(s);  MODE 1: write Taylor(c^(s)) and scatter its centroid
+// quantities;  MODE 2: write Taylor(cDot) and scatter its quantities (time-derivative limiting
+// follows).
 struct StageScalars {
   double omega, tau;
   double gco[4];        // g_m(t) of the source terms / boundary data
-  int *flag;            // bit 0: non-finite value seen
+  int *flag;            // bit 0: non-finite value seen; bit 1: a bounded wait timed out
 };
 
-template <typename T, int P, int MODE, bool RHS>
+template <typename T, int P, int MODE, bool RHS, bool LIN>
 __global__ void __launch_bounds__(kBlock)
 k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ out,
            const LimOut<T> lo, const StageScalars sc) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
+  constexpr int NT = StageRows<T, P>::op(MODE, LIN);
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
   const Tab<T, P> &tb = tab<T, P>();
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (MODE != 0) reset_next<T>(g, lo, k);
-  const bool active = k < g.K;
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  pdl_trigger();
   const int Kp = g.Kp;
-  T qv[NQ];
+  const bool staged = k0 < g.K;                   // blocks beyond the elements only reset keys
+  constexpr int rC = 0, rC0 = N, rF = (MODE != 2) ? 2 * N : N, rV = rF + 2 * Q, rB = rV + 3 * R;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) {                                 // static rows before the dependency wait
+      stage_expect<T>(bar, NT, 1);
+      stage_T(smem, rF, g.F, 2 * Q, Kp, k0, bar);
+      stage_T(smem, rV, g.Vn, 3 * R, Kp, k0, bar);
+      if (MODE != 0 && !LIN) stage_T(smem, rB, g.Bm, 4, Kp, k0, bar);
+      stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+    }
+  }
+  const bool active = k < g.K;
+  int nb[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) nb[n] = active ? g.nbr[(size_t)n * Kp + k] : -1;
   int vid[3] = {0, 0, 0};
+  if (MODE != 0 && active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  if (MODE != 0) reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) {                                   // state rows after it
+    stage_T(smem, rC, cin, N, Kp, k0, bar);
+    if (MODE != 2) stage_T(smem, rC0, c0, N, Kp, k0, bar);
+  }
+  // neighbour coefficients: outside the block from global memory now, inside from shared later
+  T cn[3][N];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const bool outside = nb[n] >= 0 && (nb[n] < k0 || nb[n] >= k0 + kBlock);
+#pragma unroll
+    for (int j = 0; j < N; ++j) cn[n][j] = outside ? cin[(size_t)j * Kp + nb[n]] : T(0);
+  }
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T qv[NQ];
   bool bad = false;
-  if (active) {
+  if (active && ok) {
     T c[N], rhs[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) { c[i] = cin[(size_t)i * Kp + k]; rhs[i] = T(0); }
+    for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = T(0); }
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      if (nb[n] >= k0 && nb[n] < k0 + kBlock)
+#pragma unroll
+        for (int j = 0; j < N; ++j) cn[n][j] = srow<T>(smem, rC + j)[nb[n] - k0];
     if (RHS) {
       for (int m = 0; m < g.nTerms; ++m) {
         const T gm = T(sc.gco[m]);
@@ -429,39 +684,31 @@ k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, 
       T cq = T(0);
 #pragma unroll
       for (int j = 0; j < N; ++j) cq += tb.phiQ[qq][j] * c[j];
-      const T f1 = g.F[(size_t)qq * Kp + k] * cq;
-      const T f2 = g.F[(size_t)(Q + qq) * Kp + k] * cq;
+      const T f1 = srow<T>(smem, rF + qq)[t] * cq;
+      const T f2 = srow<T>(smem, rF + Q + qq)[t] * cq;
 #pragma unroll
       for (int i = 0; i < N; ++i) rhs[i] += tb.g1[qq][i] * f1 + tb.g2[qq][i] * f2;
     }
     // upwind edge term
-    const int code = g.code[k];
+    const int code = irow<T>(smem, NT, 0)[t];
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
-      const int nb = g.nbr[(size_t)n * Kp + k];
       const int np = (code >> (2 * n)) & 3;
       const bool outOk = (code >> (6 + n)) & 1;
-      T v[R];
-      bool anyIn = false;
 #pragma unroll
-      for (int r = 0; r < R; ++r) { v[r] = g.Vn[(size_t)(n * R + r) * Kp + k]; anyIn |= v[r] < T(0); }
-      T cn[N];
-      const bool gather = anyIn && nb >= 0;
-#pragma unroll
-      for (int j = 0; j < N; ++j) cn[j] = gather ? cin[(size_t)j * Kp + nb] : T(0);
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
+      for (int r2 = 0; r2 < R; ++r2) {
+        const T v = srow<T>(smem, rV + n * R + r2)[t];
         T tr = T(0);
-        if (v[r] > T(0) && outOk) {
+        if (v > T(0) && outOk) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r][j] * c[j];
-        } else if (v[r] < T(0) && nb >= 0) {
+          for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r2][j] * c[j];
+        } else if (v < T(0) && nb[n] >= 0) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r][j] * cn[j];
+          for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r2][j] * cn[n][j];
         }
-        const T fl = v[r] * tr;
+        const T fl = v * tr;
 #pragma unroll
-        for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r][i] * fl;
+        for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r2][i] * fl;
       }
     }
     // mass solve
@@ -478,8 +725,13 @@ k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, 
 #pragma unroll
       for (int i = 0; i < N; ++i) cdot[i] = rhs[i];
     }
-    if (MODE == 2) {
-      const Affine<T> af = load_affine(g, k);
+    if (MODE == 2 && LIN) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cdot[i]; bad |= !finite_(cdot[i]); }
+      qv[0] = lin_mean<T, P>(cdot);
+    } else if (MODE == 2) {
+      const Affine<T> af = affine_from<T>(srow<T>(smem, rB)[t], srow<T>(smem, rB + 1)[t],
+                                          srow<T>(smem, rB + 2)[t], srow<T>(smem, rB + 3)[t]);
       T cT[N];
       to_taylor<T, P>(cdot, af, cT);
 #pragma unroll
@@ -489,12 +741,14 @@ k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, 
       const T w = T(sc.omega), tau = T(sc.tau);
       T cnew[N];
 #pragma unroll
-      for (int i = 0; i < N; ++i) cnew[i] = w * c0[(size_t)i * Kp + k] + (T(1) - w) * (c[i] + tau * cdot[i]);
-      if (MODE == 0) {
+      for (int i = 0; i < N; ++i) cnew[i] = w * srow<T>(smem, rC0 + i)[t] + (T(1) - w) * (c[i] + tau * cdot[i]);
+      if (MODE == 0 || LIN) {
 #pragma unroll
         for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+        if (MODE == 1) qv[0] = lin_mean<T, P>(cnew);
       } else {
-        const Affine<T> af = load_affine(g, k);
+        const Affine<T> af = affine_from<T>(srow<T>(smem, rB)[t], srow<T>(smem, rB + 1)[t],
+                                            srow<T>(smem, rB + 2)[t], srow<T>(smem, rB + 3)[t]);
         T cT[N];
         to_taylor<T, P>(cnew, af, cT);
 #pragma unroll
@@ -502,35 +756,65 @@ k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, 
         centroid_quantities<T, P>(cT, lo.type, qv);
       }
     }
-    if (MODE != 0) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
   }
-  if (MODE != 0) scatter_quantities<T, NQ>(g, lo, qv, vid, active);
+  if (MODE != 0) scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok);
   if (bad) atomicOr(sc.flag, 1);
 }
 
 // Time-derivative limiting and SSP update (advection/solveSubStep.m:69-83), then the Taylor
-// form of the new stage value and its centroid quantities for the solution limiter.
+// form of the new stage value and the scatter of its centroid quantities for the solution
+// limiter.
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
 k_limit_dot(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ tbuf,
             const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
-  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  reset_next<T>(g, lo, k);
-  const bool active = k < g.K;
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value, NMT = Dims<P>::NMT;
+  constexpr int NT = StageRows<T, P>::limdot();
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  pdl_trigger();
   const int Kp = g.Kp;
-  T qv[NQ];
+  const bool staged = k0 < g.K;
+  constexpr int rT = 0, rB = N, rM = N + 4, rC0 = N + 4 + NMT, rC = rC0 + N;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) {
+      stage_expect<T>(bar, NT, 1);
+      stage_T(smem, rB, g.Bm, 4, Kp, k0, bar);
+      stage_T(smem, rM, g.MT, NMT, Kp, k0, bar);
+      stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+    }
+  }
+  const bool active = k < g.K;
   int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) {
+    stage_T(smem, rT, (const T *)tbuf, N, Kp, k0, bar);
+    stage_T(smem, rC0, c0, N, Kp, k0, bar);
+    stage_T(smem, rC, cin, N, Kp, k0, bar);
+  }
+  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T qv[NQ];
   bool bad = false;
-  if (active) {
-    const Affine<T> af = load_affine(g, k);
+  if (active && ok) {
+    const Affine<T> af = affine_from<T>(srow<T>(smem, rB)[t], srow<T>(smem, rB + 1)[t],
+                                        srow<T>(smem, rB + 2)[t], srow<T>(smem, rB + 3)[t]);
     T cT[N], lim[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) { cT[i] = tbuf[(size_t)i * Kp + k]; lim[i] = cT[i]; }
-    vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
-    const int dmask = (g.code[k] >> 9) & 7;
+    for (int i = 0; i < N; ++i) { cT[i] = srow<T>(smem, rT + i)[t]; lim[i] = cT[i]; }
+    const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
     const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
-    limit_taylor<T, P>(g, li, af, vid, dmask, nan3, lim);
+    limit_taylor<T, P, NQ>(li, kv, sh, af, dmask, nan3, lim);
     // Taylor mass correction M_corr = diag(1/diag(M_T)) M_T applied to (cT - lim)
     T d[N];
 #pragma unroll
@@ -543,7 +827,7 @@ k_limit_dot(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0,
       for (int j = 0; j < N; ++j) {
         const int a = i < j ? i : j, b = i < j ? j : i;
         const int idx = a * N - a * (a - 1) / 2 + (b - a);
-        const T m = g.MT[(size_t)idx * Kp + k];
+        const T m = srow<T>(smem, rM + idx)[t];
         s += m * d[j];
         if (j == i) dii = m;
       }
@@ -555,14 +839,14 @@ k_limit_dot(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0,
     T cnew[N];
 #pragma unroll
     for (int i = 0; i < N; ++i)
-      cnew[i] = w * c0[(size_t)i * Kp + k] + (T(1) - w) * (cin[(size_t)i * Kp + k] + tau * cdot[i]);
+      cnew[i] = w * srow<T>(smem, rC0 + i)[t] + (T(1) - w) * (srow<T>(smem, rC + i)[t] + tau * cdot[i]);
     T cT2[N];
     to_taylor<T, P>(cnew, af, cT2);
 #pragma unroll
     for (int i = 0; i < N; ++i) { tbuf[(size_t)i * Kp + k] = cT2[i]; bad |= !finite_(cT2[i]); }
     centroid_quantities<T, P>(cT2, lo.type, qv);
   }
-  scatter_quantities<T, NQ>(g, lo, qv, vid, active);
+  scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok);
   if (bad) atomicOr(sc.flag, 1);
 }
 
@@ -572,25 +856,48 @@ template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
 k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const LimIn<T> li,
         const StageScalars sc) {
-  constexpr int N = Dims<P>::N;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= g.K) return;
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
+  constexpr int NT = StageRows<T, P>::lim();
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  pdl_trigger();
+  if (k0 >= g.K) { pdl_wait(); return; }
   const int Kp = g.Kp;
-  const Affine<T> af = load_affine(g, k);
-  T cT[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) cT[i] = tbuf[(size_t)i * Kp + k];
-  const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
-  const int dmask = (g.code[k] >> 9) & 7;
+  if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+  __syncthreads();
+  if (t == 0) {
+    stage_expect<T>(bar, NT, 1);
+    stage_T(smem, N, g.Bm, 4, Kp, k0, bar);
+    stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+  }
+  const bool active = k < g.K;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  if (t == 0) stage_T(smem, 0, tbuf, N, Kp, k0, bar);
+  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
   T data[3] = {T(0), T(0), T(0)};
-  if (g.cDV0T) {
+  if (g.cDV0T && active) {
     for (int m = 0; m < g.nTerms; ++m) {
       const T gm = T(sc.gco[m]);
 #pragma unroll
       for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
     }
   }
-  limit_taylor<T, P>(g, li, af, vid, dmask, data, cT);
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  if (!active || !ok) return;
+  const Affine<T> af = affine_from<T>(srow<T>(smem, N)[t], srow<T>(smem, N + 1)[t],
+                                      srow<T>(smem, N + 2)[t], srow<T>(smem, N + 3)[t]);
+  T cT[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) cT[i] = srow<T>(smem, i)[t];
+  const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
+  limit_taylor<T, P, NQ>(li, kv, sh, af, dmask, data, cT);
   T c[N];
   from_taylor<T, P>(cT, af, c);
   bool bad = false;
@@ -599,28 +906,193 @@ k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const L
   if (bad) atomicOr(sc.flag, 1);
 }
 
-// Modal state -> Taylor form and centroid quantities (initial limiting).
+// Modal state -> Taylor form and scatter of its centroid quantities (initial limiting).
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_to_taylor(const Geo<T> g, const T *__restrict__ c, T *__restrict__ tbuf, const LimOut<T> lo) {
+k_to_taylor(const Geo<T> g, const T *__restrict__ c, T *__restrict__ tbuf, const LimOut<T> lo,
+            const StageScalars sc) {
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  reset_next<T>(g, lo, k);
+  constexpr int NT = StageRows<T, P>::totaylor();
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 0));
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  pdl_trigger();
+  const int Kp = g.Kp;
+  const bool staged = k0 < g.K;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) { stage_expect<T>(bar, NT, 0); stage_T(smem, N, g.Bm, 4, Kp, k0, bar); }
+  }
   const bool active = k < g.K;
-  T qv[NQ];
   int vid[3] = {0, 0, 0};
-  if (active) {
-    const Affine<T> af = load_affine(g, k);
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) stage_T(smem, 0, c, N, Kp, k0, bar);
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T qv[NQ];
+  if (active && ok) {
+    const Affine<T> af = affine_from<T>(srow<T>(smem, N)[t], srow<T>(smem, N + 1)[t],
+                                        srow<T>(smem, N + 2)[t], srow<T>(smem, N + 3)[t]);
     T cc[N], cT[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) cc[i] = c[(size_t)i * g.Kp + k];
+    for (int i = 0; i < N; ++i) cc[i] = srow<T>(smem, i)[t];
     to_taylor<T, P>(cc, af, cT);
 #pragma unroll
-    for (int i = 0; i < N; ++i) tbuf[(size_t)i * g.Kp + k] = cT[i];
+    for (int i = 0; i < N; ++i) tbuf[(size_t)i * Kp + k] = cT[i];
     centroid_quantities<T, P>(cT, lo.type, qv);
-    vid[0] = g.V0T[k]; vid[1] = g.V0T[g.Kp + k]; vid[2] = g.V0T[2 * g.Kp + k];
   }
-  scatter_quantities<T, NQ>(g, lo, qv, vid, active);
+  scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok);
+}
+
+// Time-derivative limiting and SSP update for the linear limiter: cDot += Q_k du with the
+// precomputed Q_k = DM^-1 (S_k^-1 Mcorr_k S_k - I) (advection/solveSubStep.m:69-83); the new
+// stage value is written in the modal basis and its mean scattered for the solution limiter.
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit_dot_lin(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ tbuf,
+                const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
+  constexpr int N = Dims<P>::N, NQ = 1;
+  constexpr int NT = StageRows<T, P>::limdot_lin();
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  pdl_trigger();
+  const int Kp = g.Kp;
+  const bool staged = k0 < g.K;
+  constexpr int rD = 0, rQ = N, rC0 = N + N * (N - 1), rC = rC0 + N;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) {
+      stage_expect<T>(bar, NT, 1);
+      stage_T(smem, rQ, g.MT, N * (N - 1), Kp, k0, bar);
+      stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+    }
+  }
+  const bool active = k < g.K;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) {
+    stage_T(smem, rD, (const T *)tbuf, N, Kp, k0, bar);
+    stage_T(smem, rC0, c0, N, Kp, k0, bar);
+    stage_T(smem, rC, cin, N, Kp, k0, bar);
+  }
+  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T q0 = T(0);
+  bool bad = false;
+  if (active && ok) {
+    T cd[N], u[N], du[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cd[i] = srow<T>(smem, rD + i)[t];
+    lin_u<T, P>(cd, u);
+    const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
+    const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
+    if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, nan3, du)) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int j = 1; j < N; ++j) s += srow<T>(smem, rQ + i * (N - 1) + (j - 1))[t] * du[j];
+        cd[i] += s;
+      }
+    }
+    const T w = T(sc.omega), tau = T(sc.tau);
+    T cnew[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      cnew[i] = w * srow<T>(smem, rC0 + i)[t] + (T(1) - w) * (srow<T>(smem, rC + i)[t] + tau * cd[i]);
+#pragma unroll
+    for (int i = 0; i < N; ++i) { tbuf[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+    q0 = lin_mean<T, P>(cnew);
+  }
+  scatter_quantities<T, NQ>(g, lo, &q0, vid, active && ok);
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Solution limiter for the linear limiter (core/applySlopeLimiterDisc.m:77-86 without the
+// Taylor round trip): c <- c - DM^-1 du.
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit_lin(const Geo<T> g, const T *__restrict__ cbuf, T *__restrict__ out, const LimIn<T> li,
+            const StageScalars sc) {
+  constexpr int N = Dims<P>::N, NQ = 1;
+  const Tab<T, P> &tb = tab<T, P>();
+  __shared__ T sh[2];
+  const int t = threadIdx.x, k = blockIdx.x * kBlock + t;
+  pdl_trigger();
+  const bool active = k < g.K;
+  const int Kp = g.Kp;
+  int vid[3] = {0, 0, 0}, dmask = 0;
+  if (active) {
+    vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
+    dmask = (g.code[k] >> 9) & 7;
+  }
+  T data[3] = {T(0), T(0), T(0)};
+  if (g.cDV0T && active) {
+    for (int m = 0; m < g.nTerms; ++m) {
+      const T gm = T(sc.gco[m]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
+    }
+  }
+  pdl_wait();
+  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  T c[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) c[i] = active ? cbuf[(size_t)i * Kp + k] : T(0);
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
+  if (!active) return;
+  T u[N], du[N];
+  lin_u<T, P>(c, u);
+  if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, data, du)) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T s = T(0);
+#pragma unroll
+      for (int j = 1; j < N; ++j) s += tb.DMinv[i][j] * du[j];
+      c[i] -= s;
+    }
+  }
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = c[i]; bad |= !finite_(c[i]); }
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Mean of the modal state scattered to the vertices (initial limiting, linear limiter).
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_mean_lin(const Geo<T> g, const T *__restrict__ c, const LimOut<T> lo) {
+  constexpr int N = Dims<P>::N;
+  const int t = threadIdx.x, k = blockIdx.x * kBlock + t;
+  pdl_trigger();
+  const bool active = k < g.K;
+  const int Kp = g.Kp;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  T q0 = T(0);
+  if (active) {
+    T cc[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cc[i] = c[(size_t)i * Kp + k];
+    q0 = lin_mean<T, P>(cc);
+  }
+  scatter_quantities<T, 1>(g, lo, &q0, vid, active);
 }
 
 // External (caller order, K x N column-major, FP64) <-> internal (SoA, stride Kp, precision T).
@@ -655,7 +1127,7 @@ struct dgadv_handle {
   int *nbr = nullptr, *code = nullptr, *V0T = nullptr, *vptr = nullptr, *vidx = nullptr, *perm = nullptr;
   void *cn = nullptr, *cA = nullptr, *cB = nullptr, *tbuf = nullptr;
   void *vkeys = nullptr;               // 3 passes x nc x 2 x Vp vertex min / max keys
-  unsigned long long *gmm = nullptr;   // 3 passes x 2 x nc encoded global extremes
+  unsigned long long *gmm = nullptr;   // 3 passes x kSlotCopies x 2 x nc encoded global extremes
   long long limPass = 0;               // limiter passes enqueued so far (selects q / slot set)
   int passesPerStep = 0;
   int *flag = nullptr;
@@ -745,8 +1217,8 @@ static LimOut<T> lim_out(dgadv_handle *h) {
   LimOut<T> o;
   o.vkeys = (K_ *)h->vkeys + set * vset;
   o.vreset = (K_ *)h->vkeys + next * vset;
-  o.slots = h->gmm + (size_t)set * 2 * h->nc;
-  o.reset = h->gmm + (size_t)next * 2 * h->nc;
+  o.slots = h->gmm + (size_t)set * kSlotCopies * 2 * h->nc;
+  o.reset = h->gmm + (size_t)next * kSlotCopies * 2 * h->nc;
   o.nc = h->nc; o.type = h->limType;
   return o;
 }
@@ -768,10 +1240,53 @@ static void prof_mark(dgadv_handle *h, int kind) {
   h->profKinds.push_back(kind);
 }
 
+// Kernel launch on the handle's stream, with programmatic dependent launch unless disabled.
+template <typename... KArgs, typename... Args>
+static void launch_k(const dgadv_handle *h, void (*kern)(KArgs...), int grid, size_t smem, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = (h->flags & DGADV_FLAG_NO_PDL) ? 0 : 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+// Opt-in shared memory sizes of the staged kernels of one (precision, degree).
+template <typename T, int P>
+static cudaError_t set_smem_attributes() {
+  using SR = StageRows<T, P>;
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void *f, size_t b) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b);
+  };
+  set((const void *)k_stage_op<T, P, 0, true, false>, SR::bytes(SR::op(0, false), 1));
+  set((const void *)k_stage_op<T, P, 0, false, false>, SR::bytes(SR::op(0, false), 1));
+  set((const void *)k_stage_op<T, P, 1, true, false>, SR::bytes(SR::op(1, false), 1));
+  set((const void *)k_stage_op<T, P, 1, false, false>, SR::bytes(SR::op(1, false), 1));
+  set((const void *)k_stage_op<T, P, 2, true, false>, SR::bytes(SR::op(2, false), 1));
+  set((const void *)k_stage_op<T, P, 2, false, false>, SR::bytes(SR::op(2, false), 1));
+  set((const void *)k_stage_op<T, P, 1, true, true>, SR::bytes(SR::op(1, true), 1));
+  set((const void *)k_stage_op<T, P, 1, false, true>, SR::bytes(SR::op(1, true), 1));
+  set((const void *)k_stage_op<T, P, 2, true, true>, SR::bytes(SR::op(2, true), 1));
+  set((const void *)k_stage_op<T, P, 2, false, true>, SR::bytes(SR::op(2, true), 1));
+  set((const void *)k_limit_dot_lin<T, P>, SR::bytes(SR::limdot_lin(), 1));
+  set((const void *)k_limit_dot<T, P>, SR::bytes(SR::limdot(), 1));
+  set((const void *)k_limit<T, P>, SR::bytes(SR::lim(), 1));
+  set((const void *)k_to_taylor<T, P>, SR::bytes(SR::totaylor(), 0));
+  return e;
+}
+
 template <typename T, int P>
 static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
+  using SR = StageRows<T, P>;
   const Geo<T> g = make_geo<T>(h);
   const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;   // producers also reset vertex keys
+  const int gridK = (h->K + kBlock - 1) / kBlock;
   double omega[3], cst[3];
   const int S = rk_table(h->ordRK, omega, cst);
   T *cn = (T *)h->cn, *cA = (T *)h->cA, *cB = (T *)h->cB, *tb = (T *)h->tbuf;
@@ -786,8 +1301,8 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     LimOut<T> lo{};
     if (!h->lim) {
       prof_mark(h, 0);
-      if (rhs) k_stage_op<T, P, 0, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, out, lo, sc);
-      else k_stage_op<T, P, 0, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, out, lo, sc);
+      if (rhs) launch_k(h, k_stage_op<T, P, 0, true, false>, grid, SR::bytes(SR::op(0, false), 1), g, in, cn, out, lo, sc);
+      else launch_k(h, k_stage_op<T, P, 0, false, false>, grid, SR::bytes(SR::op(0, false), 1), g, in, cn, out, lo, sc);
       prof_mark(h, -1);
       continue;
     }
@@ -795,32 +1310,43 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     const double tBC = (s + 1 < S) ? t0 + cst[s + 1] * tau : t0 + tau;
     StageScalars scBC = sc;
     for (int m = 0; m < h->nTerms; ++m) scBC.gco[m] = time_factor(h->timeFn[m], tBC);
-    if (h->limdot) {
-      const LimOut<T> lo1 = lim_out<T>(h);
-      ++h->limPass;
-      prof_mark(h, 0);
-      if (rhs) k_stage_op<T, P, 2, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lo1, sc);
-      else k_stage_op<T, P, 2, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lo1, sc);
-      prof_mark(h, -1);
+    const bool lin = h->limType == DGADV_LIM_LINEAR;
+    const LimOut<T> lo1 = lim_out<T>(h);
+    ++h->limPass;
+    const int mode = h->limdot ? 2 : 1;
+    prof_mark(h, 0);
+    if (mode == 2) {
+      if (lin) {
+        if (rhs) launch_k(h, k_stage_op<T, P, 2, true, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, tb, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 2, false, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, tb, lo1, sc);
+      } else {
+        if (rhs) launch_k(h, k_stage_op<T, P, 2, true, false>, grid, SR::bytes(SR::op(2, false), 1), g, in, cn, tb, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 2, false, false>, grid, SR::bytes(SR::op(2, false), 1), g, in, cn, tb, lo1, sc);
+      }
+    } else {
+      if (lin) {
+        if (rhs) launch_k(h, k_stage_op<T, P, 1, true, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, tb, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 1, false, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, tb, lo1, sc);
+      } else {
+        if (rhs) launch_k(h, k_stage_op<T, P, 1, true, false>, grid, SR::bytes(SR::op(1, false), 1), g, in, cn, tb, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 1, false, false>, grid, SR::bytes(SR::op(1, false), 1), g, in, cn, tb, lo1, sc);
+      }
+    }
+    prof_mark(h, -1);
+    LimOut<T> loS = lo1;
+    if (mode == 2) {
       const LimOut<T> lo2 = lim_out<T>(h);
       ++h->limPass;
       prof_mark(h, 1);
-      k_limit_dot<T, P><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
+      if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
+      else launch_k(h, k_limit_dot<T, P>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
       prof_mark(h, -1);
-      prof_mark(h, 2);
-      k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, tb, out, lim_in<T>(lo2, h), scBC);
-      prof_mark(h, -1);
-    } else {
-      const LimOut<T> lo1 = lim_out<T>(h);
-      ++h->limPass;
-      prof_mark(h, 0);
-      if (rhs) k_stage_op<T, P, 1, true><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lo1, sc);
-      else k_stage_op<T, P, 1, false><<<grid, kBlock, 0, h->stream>>>(g, in, cn, tb, lo1, sc);
-      prof_mark(h, -1);
-      prof_mark(h, 2);
-      k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, tb, out, lim_in<T>(lo1, h), scBC);
-      prof_mark(h, -1);
+      loS = lo2;
     }
+    prof_mark(h, 2);
+    if (lin) launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
+    else launch_k(h, k_limit<T, P>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
+    prof_mark(h, -1);
   }
   if (S == 1)
     cudaMemcpyAsync(cn, cA, (size_t)h->N * h->Kp * sizeof(T), cudaMemcpyDeviceToDevice, h->stream);
@@ -829,6 +1355,7 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
 
 template <typename T, int P>
 static cudaError_t launch_limit_state(dgadv_handle *h, double t) {
+  using SR = StageRows<T, P>;
   const Geo<T> g = make_geo<T>(h);
   const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;   // producers also reset vertex keys
   StageScalars sc{};
@@ -836,8 +1363,14 @@ static cudaError_t launch_limit_state(dgadv_handle *h, double t) {
   for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = time_factor(h->timeFn[m], t);
   const LimOut<T> lo = lim_out<T>(h);
   ++h->limPass;
-  k_to_taylor<T, P><<<grid, kBlock, 0, h->stream>>>(g, (const T *)h->cn, (T *)h->tbuf, lo);
-  k_limit<T, P><<<grid, kBlock, 0, h->stream>>>(g, (const T *)h->tbuf, (T *)h->cn, lim_in<T>(lo, h), sc);
+  if (h->limType == DGADV_LIM_LINEAR) {
+    const int gridK = (h->K + kBlock - 1) / kBlock;
+    launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)h->cn, lo);
+    launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)h->cn, (T *)h->cn, lim_in<T>(lo, h), sc);
+  } else {
+    launch_k(h, k_to_taylor<T, P>, grid, SR::bytes(SR::totaylor(), 0), g, (const T *)h->cn, (T *)h->tbuf, lo, sc);
+    launch_k(h, k_limit<T, P>, grid, SR::bytes(SR::lim(), 1), g, (const T *)h->tbuf, (T *)h->cn, lim_in<T>(lo, h), sc);
+  }
   return cudaGetLastError();
 }
 
@@ -933,7 +1466,7 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   if (!build_grid(mesh->numV, mesh->coordV, mesh->numT, mesh->V0T, gr, h->err)) return DGADV_EMESH;
   if (!build_ref_tables(h->p, h->tables, h->err)) return DGADV_EINVAL;
   const int K = gr.numT, N = h->N;
-  h->K = K; h->Kp = (K + 63) / 64 * 64; h->numV = gr.numV; h->Vp = (gr.numV + 63) / 64 * 64;
+  h->K = K; h->Kp = (K + kBlock - 1) / kBlock * kBlock;   // whole blocks of rows for the bulk copies h->numV = gr.numV; h->Vp = (gr.numV + 63) / 64 * 64;
   h->Q = h->tables.Q; h->R = h->tables.R;
   const int Kp = h->Kp;
   // element order on the device: Morton order of the barycentres
@@ -1035,7 +1568,7 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   if ((st = dev_alloc(h, &h->cB, (size_t)N * Kp * w))) return st;
   if ((st = dev_alloc(h, &h->tbuf, (size_t)N * Kp * w))) return st;
   if ((st = dev_alloc(h, &h->vkeys, 3 * 2 * (size_t)nc * h->Vp * w))) return st;
-  if ((st = dev_alloc(h, (void **)&h->gmm, 6 * (size_t)nc * 8))) return st;
+  if ((st = dev_alloc(h, (void **)&h->gmm, 3 * kSlotCopies * 2 * (size_t)nc * 8))) return st;
   if ((st = dev_alloc(h, (void **)&h->flag, 16))) return st;
   if ((st = dev_alloc(h, (void **)&h->stage_ext, (size_t)N * K * 8))) return st;
   DG_CUDA(cudaMemset(h->F, 0, 2 * (size_t)Q * Kp * w));
@@ -1053,7 +1586,7 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   }
   {
     // slots of pass 0 start reset; every later pass is reset by the previous producer
-    std::vector<unsigned long long> init(6 * (size_t)nc);
+    std::vector<unsigned long long> init(3 * kSlotCopies * 2 * (size_t)nc);
     const unsigned long long kmax = h->prec == DGADV_FP64 ? ~0ULL : 0xFFFFFFFFULL;
     for (size_t i = 0; i < init.size(); ++i) init[i] = (i & 1) ? 0ULL : kmax;
     if ((st = upload(h, h->gmm, init.data(), init.size() * 8))) return st;
@@ -1067,7 +1600,17 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   if ((st = upload(h, h->vptr, vptr.data(), vptr.size() * 4))) return st;
   if ((st = upload(h, h->vidx, vidx.data(), vidx.size() * 4))) return st;
   if ((st = upload(h, h->perm, perm.data(), perm.size() * 4))) return st;
-  if (h->limdot) {
+  if (h->limdot && h->limType == DGADV_LIM_LINEAR) {
+    std::vector<double> qk;
+    taylor_correction(gr, h->p, h->tables, qk);
+    const int NQk = N * (N - 1);
+    std::vector<double> soa((size_t)NQk * Kp, 0.0);
+    for (int k = 0; k < K; ++k)
+      for (int i = 0; i < NQk; ++i) soa[(size_t)i * Kp + k] = qk[(size_t)perm[k] * NQk + i];
+    if ((st = dev_alloc(h, &h->MT, soa.size() * w))) return st;
+    if (h->prec == DGADV_FP64) { if ((st = upload_real<double>(h, h->MT, soa))) return st; }
+    else { if ((st = upload_real<float>(h, h->MT, soa))) return st; }
+  } else if (h->limdot) {
     std::vector<double> mt;
     taylor_mass_packed(gr, h->p, mt);
     const int NMT = N * (N + 1) / 2;
@@ -1093,6 +1636,14 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
                         case 2: e = upload_tables<float, 2>(h->tables); break; default: e = upload_tables<float, 3>(h->tables); }
       }
       if (e != cudaSuccess) { h->err = std::string("table upload: ") + cudaGetErrorString(e); return DGADV_ECUDA; }
+      if (pi == 0) {
+        switch (h->p) { case 0: e = set_smem_attributes<double, 0>(); break; case 1: e = set_smem_attributes<double, 1>(); break;
+                        case 2: e = set_smem_attributes<double, 2>(); break; default: e = set_smem_attributes<double, 3>(); }
+      } else {
+        switch (h->p) { case 0: e = set_smem_attributes<float, 0>(); break; case 1: e = set_smem_attributes<float, 1>(); break;
+                        case 2: e = set_smem_attributes<float, 2>(); break; default: e = set_smem_attributes<float, 3>(); }
+      }
+      if (e != cudaSuccess) { h->err = std::string("kernel attributes: ") + cudaGetErrorString(e); return DGADV_ECUDA; }
       g_tab_loaded[h->device][pi][h->p] = true;
     }
   }
@@ -1197,6 +1748,7 @@ extern "C" int dgadv_sync(dgadv_handle *h) {
   DG_CUDA(cudaStreamSynchronize(h->stream));
   int flag = 0;
   DG_CUDA(cudaMemcpy(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag & 2) { h->err = "a bounded device wait timed out"; return DGADV_ETIMEOUT; }
   if (flag & 1) { h->err = "non-finite value in the state"; return DGADV_ENONFINITE; }
   return DGADV_OK;
 }

@@ -46,7 +46,8 @@ enum { DGADV_TIME_CONST = 0, DGADV_TIME_EXP_NEG = 1 };     /* g(t) = 1 or exp(-t
 enum {
   DGADV_FLAG_NO_REORDER = 1,   /* keep the caller's element order on the device            */
   DGADV_FLAG_NO_SHIFT = 2,     /* patch min/max without the reference's global shift       */
-  DGADV_FLAG_NO_GRAPH = 4      /* launch stage kernels one by one instead of a CUDA graph  */
+  DGADV_FLAG_NO_GRAPH = 4,     /* launch stage kernels one by one instead of a CUDA graph  */
+  DGADV_FLAG_NO_PDL = 8        /* no programmatic dependent launch between stage kernels   */
 };
 
 /* ---- host helpers: static data ------------------------------------------------------- */

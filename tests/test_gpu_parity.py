@@ -98,6 +98,14 @@ def test_graph_and_direct_launches_agree_bitwise(lib):
     assert np.array_equal(a.cDisc, b.cDisc)
 
 
+def test_dependent_launch_does_not_change_results(lib):
+    from festung_gb300 import _lib as L
+    kw = dict(testcase='gauss_slot', hmax=2 ** -4, p=2, tEnd=0.05, numSteps=25, isSlopeLim=True)
+    a = gpu_run(precision='fp32', **kw)
+    b = gpu_run(precision='fp32', gpuFlags=L.FLAG_NO_PDL | L.FLAG_NO_GRAPH, **kw)
+    assert np.array_equal(a.cDisc, b.cDisc)
+
+
 def test_repeatable_bitwise(lib):
     kw = dict(testcase='gauss_slot', hmax=2 ** -4, p=2, tEnd=0.05, numSteps=25, isSlopeLim=True)
     a = gpu_run(precision='fp32', **kw)
