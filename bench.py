@@ -38,6 +38,10 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     'cfg2': dict(testcase='gauss_slot', hmax=2 ** -8, p=2, numSteps=500, tEnd=500 * 1e-4,
                  isSlopeLim=True, typeSlopeLim='linear', ordRK=3),
+    # the same operator on a 16x larger mesh (2,097,152 triangles): inputs well beyond L2, used
+    # for the DRAM traffic capture of the stage kernels
+    'cfg2big': dict(testcase='gauss_slot', hmax=2 ** -10, p=2, numSteps=500, tEnd=500 * 1e-4,
+                    isSlopeLim=True, typeSlopeLim='linear', ordRK=3),
     'cfg1': dict(testcase='gauss_slot', hmax=2 ** -5, p=1, numSteps=500, tEnd=0.5,
                  isSlopeLim=True, typeSlopeLim='linear', ordRK=2),
     'cfg5': dict(testcase='gauss_slot', hmax=2 ** -10, p=3, numSteps=100, tEnd=100 * 2e-5,

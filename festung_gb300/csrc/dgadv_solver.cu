@@ -952,8 +952,8 @@ k_to_taylor(const Geo<T> g, const T *__restrict__ c, T *__restrict__ tbuf, const
 // stage value is written in the modal basis and its mean scattered for the solution limiter.
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_limit_dot_lin(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ tbuf,
-                const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
+k_limit_dot_lin(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, const T *__restrict__ tbuf,
+                T *__restrict__ out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
   constexpr int N = Dims<P>::N, NQ = 1;
   constexpr int NT = StageRows<T, P>::limdot_lin();
   extern __shared__ __align__(128) unsigned char smem[];
@@ -1013,7 +1013,7 @@ k_limit_dot_lin(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__
     for (int i = 0; i < N; ++i)
       cnew[i] = w * srow<T>(smem, rC0 + i)[t] + (T(1) - w) * (srow<T>(smem, rC + i)[t] + tau * cd[i]);
 #pragma unroll
-    for (int i = 0; i < N; ++i) { tbuf[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+    for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
     q0 = lin_mean<T, P>(cnew);
   }
   scatter_quantities<T, NQ>(g, lo, &q0, vid, active && ok);
@@ -1095,6 +1095,202 @@ k_mean_lin(const Geo<T> g, const T *__restrict__ c, const LimOut<T> lo) {
   scatter_quantities<T, 1>(g, lo, &q0, vid, active);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Stage operator fused with the previous pass's solution limiter (linear limiter, zero
+// Dirichlet data).  The input x is the unlimited stage value (limitIn = 1), or, in the first
+// stage of a call, the limited state itself (limitIn = 0).  Each element limits
+// its own coefficients and those of the three neighbours it gathers for the flux, each with its
+// own vertex patches (core/applySlopeLimiterDisc.m:77-86 applied where the value is used instead
+// of in a separate pass), then
+//   MODE 1: writes the new unlimited stage value (SSP update, advection/solveSubStep.m:83),
+//   MODE 2: writes cDot for the time-derivative limiter,
+// and scatters the mean of what it wrote for the next limiter pass.  xLout receives the limited
+// own input where later kernels need it (the limited c^n, or c^(s-1) for the SSP update).
+template <typename T, int P>
+__device__ __forceinline__ void lin_limit_inplace(const LimIn<T> &li, const VKeys<T, 1> &kv, const T *sh,
+                                                  int dmask, T *c) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T u[N], du[N];
+  lin_u<T, P>(c, u);
+  const T zero3[3] = {T(0), T(0), T(0)};
+  if (lin_alpha<T, P, 1>(li, kv, sh, u, dmask, zero3, du)) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T s = T(0);
+#pragma unroll
+      for (int j = 1; j < N; ++j) s += tb.DMinv[i][j] * du[j];
+      c[i] -= s;
+    }
+  }
+}
+
+template <typename T, int P, int MODE, bool RHS>
+__global__ void __launch_bounds__(kBlock)
+k_op_fused(const Geo<T> g, const T *__restrict__ x, int limitIn, T *__restrict__ xLout,
+           const T *__restrict__ c0L, int firstStage, T *__restrict__ out, const LimIn<T> li,
+           const LimOut<T> lo, const StageScalars sc) {
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
+  constexpr int NT = StageRows<T, P>::op(MODE, true);
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  const Tab<T, P> &tb = tab<T, P>();
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  pdl_trigger();
+  const int Kp = g.Kp;
+  const bool staged = k0 < g.K;
+  constexpr int rC = 0, rC0 = N, rF = (MODE != 2) ? 2 * N : N, rV = rF + 2 * Q;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) {
+      stage_expect<T>(bar, NT - ((MODE == 1 && firstStage) ? N : 0), 1);
+      stage_T(smem, rF, g.F, 2 * Q, Kp, k0, bar);
+      stage_T(smem, rV, g.Vn, 3 * R, Kp, k0, bar);
+      stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+    }
+  }
+  const bool active = k < g.K;
+  // static connectivity before the dependency wait: neighbours, their boundary bits and the
+  // vertex of each neighbour opposite the shared edge
+  int nb[3], nbc[3], v3[3];
+  int vid[3] = {0, 0, 0};
+  const int myCode = active ? g.code[k] : 0;
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    nb[n] = active ? g.nbr[(size_t)n * Kp + k] : -1;
+    const int np = (myCode >> (2 * n)) & 3;
+    nbc[n] = nb[n] >= 0 ? g.code[nb[n]] : 0;
+    v3[n] = nb[n] >= 0 ? g.V0T[(size_t)np * Kp + nb[n]] : 0;
+  }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) {
+    stage_T(smem, rC, x, N, Kp, k0, bar);
+    if (MODE == 1 && !firstStage) stage_T(smem, rC0, c0L, N, Kp, k0, bar);
+  }
+  // neighbour coefficients: outside the block from global memory now, inside from shared later
+  T cn[3][N];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const bool outside = nb[n] >= 0 && (nb[n] < k0 || nb[n] >= k0 + kBlock);
+#pragma unroll
+    for (int j = 0; j < N; ++j) cn[n][j] = outside ? x[(size_t)j * Kp + nb[n]] : T(0);
+  }
+  // vertex keys of the own element and of each neighbour (two vertices shared with the edge)
+  VKeys<T, 1> kvOwn, kvNb[3];
+  load_vkeys<T, 1>(g, li, vid, kvOwn);
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const int np = (myCode >> (2 * n)) & 3;
+    const typename KeyOf<T>::type k3min = li.vkeys[v3[n]], k3max = li.vkeys[(size_t)g.Vp + v3[n]];
+    // neighbour's local vertex np is opposite the shared edge; np+1 is our n+2, np+2 our n+1
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const int mm = (m + 3 - np) % 3;
+      const int ours = mm == 1 ? (n + 2) % 3 : (n + 1) % 3;
+      kvNb[n].v[0][0][m] = mm == 0 ? k3min : kvOwn.v[0][0][ours];
+      kvNb[n].v[0][1][m] = mm == 0 ? k3max : kvOwn.v[0][1][ours];
+    }
+  }
+  if (li.shift && limitIn) load_shifts<T>(li.slots, li.nc, sh);
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T q0 = T(0);
+  bool bad = false;
+  if (active && ok) {
+    T c[N], rhs[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = T(0); }
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      if (nb[n] >= k0 && nb[n] < k0 + kBlock)
+#pragma unroll
+        for (int j = 0; j < N; ++j) cn[n][j] = srow<T>(smem, rC + j)[nb[n] - k0];
+    if (limitIn) {
+      lin_limit_inplace<T, P>(li, kvOwn, sh, (myCode >> 9) & 7, c);
+#pragma unroll
+      for (int n = 0; n < 3; ++n)
+        if (nb[n] >= 0) lin_limit_inplace<T, P>(li, kvNb[n], sh, (nbc[n] >> 9) & 7, cn[n]);
+    }
+    if (xLout) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) xLout[(size_t)i * Kp + k] = c[i];
+    }
+    if (RHS) {
+      for (int m = 0; m < g.nTerms; ++m) {
+        const T gm = T(sc.gco[m]);
+#pragma unroll
+        for (int i = 0; i < N; ++i) rhs[i] += gm * g.rhs[((size_t)m * N + i) * Kp + k];
+      }
+    }
+#pragma unroll
+    for (int qq = 0; qq < Q; ++qq) {
+      T cq = T(0);
+#pragma unroll
+      for (int j = 0; j < N; ++j) cq += tb.phiQ[qq][j] * c[j];
+      const T f1 = srow<T>(smem, rF + qq)[t] * cq;
+      const T f2 = srow<T>(smem, rF + Q + qq)[t] * cq;
+#pragma unroll
+      for (int i = 0; i < N; ++i) rhs[i] += tb.g1[qq][i] * f1 + tb.g2[qq][i] * f2;
+    }
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      const int np = (myCode >> (2 * n)) & 3;
+      const bool outOk = (myCode >> (6 + n)) & 1;
+#pragma unroll
+      for (int r2 = 0; r2 < R; ++r2) {
+        const T v = srow<T>(smem, rV + n * R + r2)[t];
+        T tr = T(0);
+        if (v > T(0) && outOk) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r2][j] * c[j];
+        } else if (v < T(0) && nb[n] >= 0) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r2][j] * cn[n][j];
+        }
+        const T fl = v * tr;
+#pragma unroll
+        for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r2][i] * fl;
+      }
+    }
+    T cdot[N];
+    if (sizeof(T) == 8) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int j = 0; j < N; ++j) s += tb.hatMinv[i][j] * rhs[j];
+        cdot[i] = s;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) cdot[i] = rhs[i];
+    }
+    if (MODE == 2) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cdot[i]; bad |= !finite_(cdot[i]); }
+      q0 = lin_mean<T, P>(cdot);
+    } else {
+      const T w = T(sc.omega), tau = T(sc.tau);
+      T cnew[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const T c0v = firstStage ? c[i] : srow<T>(smem, rC0 + i)[t];
+        cnew[i] = w * c0v + (T(1) - w) * (c[i] + tau * cdot[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+      q0 = lin_mean<T, P>(cnew);
+    }
+  }
+  scatter_quantities<T, 1>(g, lo, &q0, vid, active && ok);
+  if (bad) atomicOr(sc.flag, 1);
+}
+
 // External (caller order, K x N column-major, FP64) <-> internal (SoA, stride Kp, precision T).
 template <typename T>
 __global__ void k_scatter_in(int K, int Kp, int N, const int *__restrict__ perm,
@@ -1126,9 +1322,10 @@ struct dgadv_handle {
   void *F = nullptr, *Vn = nullptr, *Bm = nullptr, *MT = nullptr, *rhs = nullptr, *cDV0T = nullptr;
   int *nbr = nullptr, *code = nullptr, *V0T = nullptr, *vptr = nullptr, *vidx = nullptr, *perm = nullptr;
   void *cn = nullptr, *cA = nullptr, *cB = nullptr, *tbuf = nullptr;
+  void *cR = nullptr, *cnL = nullptr, *cLx = nullptr;   // fused path: raw step output, limited c^n / c^(s-1)
   void *vkeys = nullptr;               // 3 passes x nc x 2 x Vp vertex min / max keys
   unsigned long long *gmm = nullptr;   // 3 passes x kSlotCopies x 2 x nc encoded global extremes
-  long long limPass = 0;               // limiter passes enqueued so far (selects q / slot set)
+  long long limPass = 1;               // limiter passes enqueued so far (selects key / slot set)
   int passesPerStep = 0;
   int *flag = nullptr;
   double *stage_ext = nullptr;         // K x N staging for set/get state
@@ -1223,6 +1420,18 @@ static LimOut<T> lim_out(dgadv_handle *h) {
   return o;
 }
 template <typename T>
+static LimIn<T> lim_in_pass(const dgadv_handle *h, long long pass) {
+  using K_ = typename KeyOf<T>::type;
+  const int set = (int)(((pass % 3) + 3) % 3);
+  LimIn<T> i;
+  i.vkeys = (const K_ *)h->vkeys + (size_t)set * 2 * h->nc * h->Vp;
+  i.slots = h->gmm + (size_t)set * kSlotCopies * 2 * h->nc;
+  i.nc = h->nc; i.type = h->limType;
+  i.shift = (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1;
+  return i;
+}
+
+template <typename T>
 static LimIn<T> lim_in(const LimOut<T> &o, const dgadv_handle *h) {
   LimIn<T> i;
   i.vkeys = o.vkeys; i.slots = o.slots; i.nc = o.nc; i.type = o.type;
@@ -1275,6 +1484,10 @@ static cudaError_t set_smem_attributes() {
   set((const void *)k_stage_op<T, P, 2, true, true>, SR::bytes(SR::op(2, true), 1));
   set((const void *)k_stage_op<T, P, 2, false, true>, SR::bytes(SR::op(2, true), 1));
   set((const void *)k_limit_dot_lin<T, P>, SR::bytes(SR::limdot_lin(), 1));
+  set((const void *)k_op_fused<T, P, 1, true>, SR::bytes(SR::op(1, true), 1));
+  set((const void *)k_op_fused<T, P, 1, false>, SR::bytes(SR::op(1, true), 1));
+  set((const void *)k_op_fused<T, P, 2, true>, SR::bytes(SR::op(2, true), 1));
+  set((const void *)k_op_fused<T, P, 2, false>, SR::bytes(SR::op(2, true), 1));
   set((const void *)k_limit_dot<T, P>, SR::bytes(SR::limdot(), 1));
   set((const void *)k_limit<T, P>, SR::bytes(SR::lim(), 1));
   set((const void *)k_to_taylor<T, P>, SR::bytes(SR::totaylor(), 0));
@@ -1338,7 +1551,7 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
       const LimOut<T> lo2 = lim_out<T>(h);
       ++h->limPass;
       prof_mark(h, 1);
-      if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
+      if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)in, (const T *)cn, (const T *)tb, tb, lim_in<T>(lo1, h), lo2, sc);
       else launch_k(h, k_limit_dot<T, P>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
       prof_mark(h, -1);
       loS = lo2;
@@ -1350,6 +1563,73 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
   }
   if (S == 1)
     cudaMemcpyAsync(cn, cA, (size_t)h->N * h->Kp * sizeof(T), cudaMemcpyDeviceToDevice, h->stream);
+  return cudaGetLastError();
+}
+
+// Fused path (linear limiter, zero Dirichlet data): per stage the operator kernel limits its
+// input on the fly; for p >= 2 the time-derivative limiter follows.  The state between calls
+// stays limited in cn; inside a call the step output R is unlimited, and finalize_fused limits
+// it back into cn at the end of the call.
+static bool use_fused(const dgadv_handle *h) {
+  return h->lim && h->limType == DGADV_LIM_LINEAR && !h->cDV0T && (h->flags & DGADV_FLAG_FUSE);
+}
+
+template <typename T, int P>
+static cudaError_t launch_step_fused(dgadv_handle *h, double t0, double tau, bool firstOfCall) {
+  using SR = StageRows<T, P>;
+  const Geo<T> g = make_geo<T>(h);
+  const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
+  double omega[3], cst[3];
+  const int S = rk_table(h->ordRK, omega, cst);
+  T *cn = (T *)h->cn, *R = (T *)h->cR, *rA = (T *)h->cA, *rB = (T *)h->cB;
+  T *cnL = (T *)h->cnL, *Lx = (T *)h->cLx, *tb = (T *)h->tbuf;
+  const bool rhs = h->nTerms > 0 && h->rhs;
+  for (int s = 0; s < S; ++s) {
+    const T *x = (s == 0) ? (firstOfCall ? cn : R) : (s == 1 ? rA : rB);
+    const int limitIn = (firstOfCall && s == 0) ? 0 : 1;
+    T *outRaw = (s == S - 1) ? R : (s == 0 ? rA : rB);
+    StageScalars sc{};
+    sc.omega = omega[s]; sc.tau = tau; sc.flag = h->flag;
+    const double ts = t0 + cst[s] * tau;
+    for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = time_factor(h->timeFn[m], ts);
+    const LimIn<T> li = lim_in_pass<T>(h, h->limPass - 1);
+    const LimOut<T> lo1 = lim_out<T>(h);
+    ++h->limPass;
+    prof_mark(h, 0);
+    if (!h->limdot) {
+      if (rhs) launch_k(h, k_op_fused<T, P, 1, true>, grid, SR::bytes(SR::op(1, true), 1), g, x, limitIn,
+                        s == 0 ? cnL : (T *)nullptr, (const T *)cnL, s == 0 ? 1 : 0, outRaw, li, lo1, sc);
+      else launch_k(h, k_op_fused<T, P, 1, false>, grid, SR::bytes(SR::op(1, true), 1), g, x, limitIn,
+                    s == 0 ? cnL : (T *)nullptr, (const T *)cnL, s == 0 ? 1 : 0, outRaw, li, lo1, sc);
+      prof_mark(h, -1);
+      continue;
+    }
+    T *xL = (s == 0) ? cnL : Lx;
+    if (rhs) launch_k(h, k_op_fused<T, P, 2, true>, grid, SR::bytes(SR::op(2, true), 1), g, x, limitIn, xL,
+                      (const T *)nullptr, s == 0 ? 1 : 0, tb, li, lo1, sc);
+    else launch_k(h, k_op_fused<T, P, 2, false>, grid, SR::bytes(SR::op(2, true), 1), g, x, limitIn, xL,
+                  (const T *)nullptr, s == 0 ? 1 : 0, tb, li, lo1, sc);
+    prof_mark(h, -1);
+    const LimOut<T> lo2 = lim_out<T>(h);
+    ++h->limPass;
+    prof_mark(h, 1);
+    launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)xL, (const T *)cnL,
+             (const T *)tb, outRaw, lim_in<T>(lo1, h), lo2, sc);
+    prof_mark(h, -1);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T, int P>
+static cudaError_t launch_finalize_fused(dgadv_handle *h) {
+  const Geo<T> g = make_geo<T>(h);
+  const int gridK = (h->K + kBlock - 1) / kBlock;
+  StageScalars sc{};
+  sc.flag = h->flag;
+  prof_mark(h, 2);
+  launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)h->cR, (T *)h->cn,
+           lim_in_pass<T>(h, h->limPass - 1), sc);
+  prof_mark(h, -1);
   return cudaGetLastError();
 }
 
@@ -1383,6 +1663,23 @@ static cudaError_t dispatch_step(dgadv_handle *h, double t0, double tau) {
     default: return launch_step<T, 3>(h, t0, tau);
   }
 }
+template <typename T>
+static cudaError_t dispatch_step_fused(dgadv_handle *h, double t0, double tau, bool first) {
+  switch (h->p) {
+    case 1: return launch_step_fused<T, 1>(h, t0, tau, first);
+    case 2: return launch_step_fused<T, 2>(h, t0, tau, first);
+    default: return launch_step_fused<T, 3>(h, t0, tau, first);
+  }
+}
+template <typename T>
+static cudaError_t dispatch_finalize_fused(dgadv_handle *h) {
+  switch (h->p) {
+    case 1: return launch_finalize_fused<T, 1>(h);
+    case 2: return launch_finalize_fused<T, 2>(h);
+    default: return launch_finalize_fused<T, 3>(h);
+  }
+}
+
 template <typename T>
 static cudaError_t dispatch_limit(dgadv_handle *h, double t) {
   switch (h->p) {
@@ -1567,6 +1864,9 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   if ((st = dev_alloc(h, &h->cA, (size_t)N * Kp * w))) return st;
   if ((st = dev_alloc(h, &h->cB, (size_t)N * Kp * w))) return st;
   if ((st = dev_alloc(h, &h->tbuf, (size_t)N * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->cR, (size_t)N * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->cnL, (size_t)N * Kp * w))) return st;
+  if ((st = dev_alloc(h, &h->cLx, (size_t)N * Kp * w))) return st;
   if ((st = dev_alloc(h, &h->vkeys, 3 * 2 * (size_t)nc * h->Vp * w))) return st;
   if ((st = dev_alloc(h, (void **)&h->gmm, 3 * kSlotCopies * 2 * (size_t)nc * 8))) return st;
   if ((st = dev_alloc(h, (void **)&h->flag, 16))) return st;
@@ -1577,6 +1877,9 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   DG_CUDA(cudaMemset(h->cA, 0, (size_t)N * Kp * w));
   DG_CUDA(cudaMemset(h->cB, 0, (size_t)N * Kp * w));
   DG_CUDA(cudaMemset(h->tbuf, 0, (size_t)N * Kp * w));
+  DG_CUDA(cudaMemset(h->cR, 0, (size_t)N * Kp * w));
+  DG_CUDA(cudaMemset(h->cnL, 0, (size_t)N * Kp * w));
+  DG_CUDA(cudaMemset(h->cLx, 0, (size_t)N * Kp * w));
   {
     // vertex keys of every pass start reset (min = largest key, max = 0)
     std::vector<unsigned char> vk(3 * 2 * (size_t)nc * h->Vp * w, 0);
@@ -1781,51 +2084,65 @@ static bool time_dependent(const dgadv_handle *h) {
   return false;
 }
 
+// One time step: fused or separate-pass pipeline.
+static cudaError_t one_step(dgadv_handle *h, double t0, double tau, bool firstOfCall) {
+  if (use_fused(h))
+    return h->prec == DGADV_FP64 ? dispatch_step_fused<double>(h, t0, tau, firstOfCall)
+                                 : dispatch_step_fused<float>(h, t0, tau, firstOfCall);
+  return h->prec == DGADV_FP64 ? dispatch_step<double>(h, t0, tau) : dispatch_step<float>(h, t0, tau);
+}
+static cudaError_t end_of_call(dgadv_handle *h) {
+  if (!use_fused(h)) return cudaSuccess;
+  return h->prec == DGADV_FP64 ? dispatch_finalize_fused<double>(h) : dispatch_finalize_fused<float>(h);
+}
+
 extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau) {
   if (!h || nSteps < 0 || !(tau > 0)) return DGADV_EINVAL;
   if (!h->hasVelocity) { if (h) h->err = "dgadv_set_velocity was not called"; return DGADV_EINVAL; }
   DG_CUDA(cudaSetDevice(h->device));
+  if (nSteps == 0) return DGADV_OK;
+  const bool fused = use_fused(h);
   const bool useGraph = !(h->flags & DGADV_FLAG_NO_GRAPH) && !time_dependent(h);
-  if (!useGraph) {
-    for (int s = 0; s < nSteps; ++s) {
-      const double t0 = (double)(nStep0 + s) * tau;   // (nStep - 1) * tau
-      cudaError_t e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, t0, tau) : dispatch_step<float>(h, t0, tau);
-      if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
-    }
-    return DGADV_OK;
-  }
-  // time-independent data: a captured graph of a chunk of steps, replayed.  The chunk makes a
-  // multiple of three limiter passes, so the pass phase is the same before and after it.
-  const int chunk = 12;
   int done = 0;
-  while (nSteps - done >= chunk) {
-    const int ph = (int)(h->limPass % 3);
-    if (!h->graph[ph] || h->graphTau[ph] != tau) {
-      if (h->graph[ph]) { cudaGraphExecDestroy(h->graph[ph]); h->graph[ph] = nullptr; }
-      const long long saved = h->limPass;
-      cudaGraph_t gph;
-      DG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-      cudaError_t e = cudaSuccess;
-      for (int s = 0; s < chunk && e == cudaSuccess; ++s)
-        e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, 0.0, tau) : dispatch_step<float>(h, 0.0, tau);
-      cudaError_t e2 = cudaStreamEndCapture(h->stream, &gph);
-      h->limPass = saved;
-      if (e != cudaSuccess || e2 != cudaSuccess) {
-        h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
-        return DGADV_ECUDA;
+  if (fused) {   // the first step of a call starts from the limited state
+    cudaError_t e = one_step(h, (double)nStep0 * tau, tau, true);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
+    done = 1;
+  }
+  if (useGraph) {
+    // time-independent data: a captured graph of a chunk of steps, replayed.  The chunk makes a
+    // multiple of three limiter passes, so the pass phase is the same before and after it.
+    const int chunk = 12;
+    while (nSteps - done >= chunk) {
+      const int ph = (int)(h->limPass % 3);
+      if (!h->graph[ph] || h->graphTau[ph] != tau) {
+        if (h->graph[ph]) { cudaGraphExecDestroy(h->graph[ph]); h->graph[ph] = nullptr; }
+        const long long saved = h->limPass;
+        cudaGraph_t gph;
+        DG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (int s = 0; s < chunk && e == cudaSuccess; ++s) e = one_step(h, 0.0, tau, false);
+        cudaError_t e2 = cudaStreamEndCapture(h->stream, &gph);
+        h->limPass = saved;
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+          h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+          return DGADV_ECUDA;
+        }
+        DG_CUDA(cudaGraphInstantiate(&h->graph[ph], gph, 0));
+        cudaGraphDestroy(gph);
+        h->graphTau[ph] = tau;
       }
-      DG_CUDA(cudaGraphInstantiate(&h->graph[ph], gph, 0));
-      cudaGraphDestroy(gph);
-      h->graphTau[ph] = tau;
+      DG_CUDA(cudaGraphLaunch(h->graph[ph], h->stream));
+      h->limPass += (long long)chunk * h->passesPerStep;
+      done += chunk;
     }
-    DG_CUDA(cudaGraphLaunch(h->graph[ph], h->stream));
-    h->limPass += (long long)chunk * h->passesPerStep;
-    done += chunk;
   }
   for (; done < nSteps; ++done) {
-    cudaError_t e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, 0.0, tau) : dispatch_step<float>(h, 0.0, tau);
+    cudaError_t e = one_step(h, (double)(nStep0 + done) * tau, tau, false);
     if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
   }
+  cudaError_t e = end_of_call(h);
+  if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
   return DGADV_OK;
 }
 
@@ -1854,10 +2171,8 @@ extern "C" int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nS
   h->profiling = true;
   h->profEvents.clear(); h->profKinds.clear();
   cudaError_t e = cudaSuccess;
-  for (int s = 0; s < nSteps && e == cudaSuccess; ++s) {
-    const double t0 = (double)(nStep0 + s) * tau;
-    e = h->prec == DGADV_FP64 ? dispatch_step<double>(h, t0, tau) : dispatch_step<float>(h, t0, tau);
-  }
+  for (int s = 0; s < nSteps && e == cudaSuccess; ++s) e = one_step(h, (double)(nStep0 + s) * tau, tau, s == 0);
+  if (e == cudaSuccess) e = end_of_call(h);
   h->profiling = false;
   cudaError_t e2 = cudaStreamSynchronize(h->stream);
   for (int k = 0; k < 4; ++k) { msPerLaunch[k] = 0; launches[k] = 0; }
@@ -1879,7 +2194,8 @@ extern "C" int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nS
 extern "C" int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count) {
   if (!h || !count) return DGADV_EINVAL;
   int perStage = 1;
-  if (h->lim) perStage = h->limdot ? 3 : 2;
+  if (use_fused(h)) perStage = h->limdot ? 2 : 1;
+  else if (h->lim) perStage = h->limdot ? 3 : 2;
   *count = h->ordRK * perStage;
   return DGADV_OK;
 }

@@ -47,7 +47,9 @@ enum {
   DGADV_FLAG_NO_REORDER = 1,   /* keep the caller's element order on the device            */
   DGADV_FLAG_NO_SHIFT = 2,     /* patch min/max without the reference's global shift       */
   DGADV_FLAG_NO_GRAPH = 4,     /* launch stage kernels one by one instead of a CUDA graph  */
-  DGADV_FLAG_NO_PDL = 8        /* no programmatic dependent launch between stage kernels   */
+  DGADV_FLAG_NO_PDL = 8,       /* no programmatic dependent launch between stage kernels   */
+  DGADV_FLAG_FUSE = 16         /* linear limiter with zero Dirichlet data: apply the solution
+                                  limiter inside the next stage's operator kernel            */
 };
 
 /* ---- host helpers: static data ------------------------------------------------------- */

@@ -106,6 +106,15 @@ def test_dependent_launch_does_not_change_results(lib):
     assert np.array_equal(a.cDisc, b.cDisc)
 
 
+@pytest.mark.parametrize('p', [1, 2, 3])
+def test_fused_limiter_pipeline_matches_separate_passes(lib, p):
+    from festung_gb300 import _lib as L
+    kw = dict(testcase='gauss_slot', hmax=2 ** -4, p=p, tEnd=0.03, numSteps=15, isSlopeLim=True)
+    a = gpu_run(precision='fp64', gpuFlags=L.FLAG_FUSE, **kw)
+    b = gpu_run(precision='fp64', **kw)
+    assert rel(a.cDisc, b.cDisc) <= 1e-13
+
+
 def test_repeatable_bitwise(lib):
     kw = dict(testcase='gauss_slot', hmax=2 ** -4, p=2, tEnd=0.05, numSteps=25, isSlopeLim=True)
     a = gpu_run(precision='fp32', **kw)
