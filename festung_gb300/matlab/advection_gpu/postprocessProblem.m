@@ -1,0 +1,13 @@
+% Final state and L2 error (advection/postprocessProblem.m:43-82); releases the device handle.
+function problemData = postprocessProblem(problemData)
+problemData.cDisc = dgadv_mex('get_state', problemData.gpu, problemData.K, problemData.N);
+dgadv_mex('destroy', problemData.gpu);
+if problemData.isAnalytical
+  problemData.error = computeL2Error(problemData.g, problemData.cDisc, ...
+    @(x1,x2) problemData.cCont(problemData.tEnd, x1, x2), problemData.qOrd, problemData.basesOnQuad);
+else
+  problemData.error = computeL2Error(problemData.g, problemData.cDisc, problemData.c0Cont, ...
+    problemData.qOrd, problemData.basesOnQuad);
+end % if
+fprintf('L2 error: %g\n', problemData.error);
+end % function

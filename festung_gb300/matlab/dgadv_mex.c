@@ -1,0 +1,145 @@
+/*
+ * dgadv_mex.c -- MEX / oct-file gateway over the C-ABI of libdgadv (include/dgadv.h).
+ *
+ * Build (Matlab):  mex -I<repo>/include dgadv_mex.c -L<repo>/festung_gb300 -ldgadv
+ * Build (Octave):  mkoctfile --mex -I<repo>/include dgadv_mex.c -L<repo>/festung_gb300 -ldgadv
+ *
+ * Usage from the advection_gpu problem folder:
+ *   h = dgadv_mex('create', coordV, V0T, idE0T, markE0TbdrD, markE0TbdrN, [p ordRK prec lim limType dev flags])
+ *   dgadv_mex('set_velocity', h, u1Disc, u2Disc, vNormalOnQuadEdge)
+ *   dgadv_mex('set_source_terms', h, timeFn, rhsTerms, cDV0T)
+ *   dgadv_mex('set_state', h, cDisc)
+ *   dgadv_mex('limit_state', h, t)
+ *   dgadv_mex('step', h, nSteps, nStep0, tau)
+ *   cDisc = dgadv_mex('get_state', h)
+ *   dgadv_mex('destroy', h)
+ * Arrays keep Matlab's layout (column-major), integer inputs are converted from 1-based doubles
+ * to 0-based int32 here.  Every non-zero status becomes a Matlab error with the library's
+ * message.  Handles are uint64 scalars; mexAtExit destroys the ones still open.
+ */
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "mex.h"
+#include "dgadv.h"
+
+#define MAX_HANDLES 64
+static dgadv_handle *g_open[MAX_HANDLES];
+
+static void cleanup(void) {
+  for (int i = 0; i < MAX_HANDLES; ++i)
+    if (g_open[i]) { dgadv_destroy(g_open[i]); g_open[i] = NULL; }
+}
+
+static void check(int st, dgadv_handle *h) {
+  if (st != DGADV_OK)
+    mexErrMsgIdAndTxt("dgadv:status", "%s: %s", dgadv_status_string(st), h ? dgadv_last_error(h) : "");
+}
+
+static dgadv_handle *get_handle(const mxArray *a) {
+  if (!mxIsUint64(a) || mxGetNumberOfElements(a) != 1) mexErrMsgIdAndTxt("dgadv:arg", "bad handle");
+  dgadv_handle *h = (dgadv_handle *)(uintptr_t)(*(uint64_t *)mxGetData(a));
+  for (int i = 0; i < MAX_HANDLES; ++i)
+    if (g_open[i] == h) return h;
+  mexErrMsgIdAndTxt("dgadv:arg", "unknown or destroyed handle");
+  return NULL;
+}
+
+static const double *dbl(const mxArray *a, size_t n, const char *what) {
+  if (!mxIsDouble(a) || mxIsComplex(a) || mxGetNumberOfElements(a) != n)
+    mexErrMsgIdAndTxt("dgadv:arg", "%s must be a real double array with %zu elements", what, n);
+  return mxGetPr(a);
+}
+
+/* 1-based double ids -> 0-based int32 (caller frees) */
+static int32_t *ids0(const mxArray *a, size_t n, const char *what) {
+  const double *d = dbl(a, n, what);
+  int32_t *o = (int32_t *)mxMalloc(n * sizeof(int32_t));
+  for (size_t i = 0; i < n; ++i) o[i] = (int32_t)d[i] - 1;
+  return o;
+}
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
+  static int registered = 0;
+  if (!registered) { mexAtExit(cleanup); registered = 1; }
+  if (nrhs < 1 || !mxIsChar(prhs[0])) mexErrMsgIdAndTxt("dgadv:arg", "first argument: command");
+  char cmd[32];
+  mxGetString(prhs[0], cmd, sizeof cmd);
+
+  if (!strcmp(cmd, "create")) {
+    if (nrhs != 7) mexErrMsgIdAndTxt("dgadv:arg", "create: 6 arguments");
+    const size_t numV = mxGetM(prhs[1]), numT = mxGetM(prhs[2]);
+    dgadv_mesh m;
+    memset(&m, 0, sizeof m);
+    m.numT = (int32_t)numT; m.numV = (int32_t)numV;
+    m.coordV = dbl(prhs[1], 2 * numV, "coordV");
+    int32_t *V0T = ids0(prhs[2], 3 * numT, "V0T");
+    m.V0T = V0T;
+    int32_t *idE0T = NULL; uint8_t *bD = NULL, *bN = NULL;
+    if (!mxIsEmpty(prhs[3])) {
+      const double *d = dbl(prhs[3], 3 * numT, "idE0T");
+      idE0T = (int32_t *)mxMalloc(3 * numT * sizeof(int32_t));
+      for (size_t i = 0; i < 3 * numT; ++i) idE0T[i] = (int32_t)d[i];
+      m.idE0T = idE0T;
+    }
+    if (!mxIsEmpty(prhs[4])) {
+      if (mxGetNumberOfElements(prhs[4]) != 3 * numT) mexErrMsgIdAndTxt("dgadv:arg", "markE0TbdrD size");
+      bD = (uint8_t *)mxMalloc(3 * numT);
+      for (size_t i = 0; i < 3 * numT; ++i) bD[i] = mxIsLogical(prhs[4]) ? mxGetLogicals(prhs[4])[i] : (mxGetPr(prhs[4])[i] != 0);
+      m.markE0TbdrD = bD;
+    }
+    if (!mxIsEmpty(prhs[5])) {
+      if (mxGetNumberOfElements(prhs[5]) != 3 * numT) mexErrMsgIdAndTxt("dgadv:arg", "markE0TbdrN size");
+      bN = (uint8_t *)mxMalloc(3 * numT);
+      for (size_t i = 0; i < 3 * numT; ++i) bN[i] = mxIsLogical(prhs[5]) ? mxGetLogicals(prhs[5])[i] : (mxGetPr(prhs[5])[i] != 0);
+      m.markE0TbdrN = bN;
+    }
+    const double *o = dbl(prhs[6], 7, "options");
+    dgadv_params prm = {(int32_t)o[0], (int32_t)o[1], (int32_t)o[2], (int32_t)o[3], (int32_t)o[4],
+                        (int32_t)o[5], (int32_t)o[6]};
+    dgadv_handle *h = NULL;
+    const int st = dgadv_create(&m, &prm, &h);
+    mxFree(V0T); if (idE0T) mxFree(idE0T); if (bD) mxFree(bD); if (bN) mxFree(bN);
+    if (st != DGADV_OK) {
+      char msg[512];
+      snprintf(msg, sizeof msg, "%s: %s", dgadv_status_string(st), h ? dgadv_last_error(h) : "");
+      dgadv_destroy(h);
+      mexErrMsgIdAndTxt("dgadv:status", "%s", msg);
+    }
+    int slot = -1;
+    for (int i = 0; i < MAX_HANDLES; ++i) if (!g_open[i]) { slot = i; break; }
+    if (slot < 0) { dgadv_destroy(h); mexErrMsgIdAndTxt("dgadv:arg", "too many open handles"); }
+    g_open[slot] = h;
+    plhs[0] = mxCreateNumericMatrix(1, 1, mxUINT64_CLASS, mxREAL);
+    *(uint64_t *)mxGetData(plhs[0]) = (uint64_t)(uintptr_t)h;
+    return;
+  }
+  if (nrhs < 2) mexErrMsgIdAndTxt("dgadv:arg", "%s: missing handle", cmd);
+  dgadv_handle *h = get_handle(prhs[1]);
+  if (!strcmp(cmd, "set_velocity")) {
+    check(dgadv_set_velocity(h, mxGetPr(prhs[2]), mxGetPr(prhs[3]), mxGetPr(prhs[4])), h);
+  } else if (!strcmp(cmd, "set_source_terms")) {
+    const size_t n = mxGetNumberOfElements(prhs[2]);
+    int32_t fn[4] = {0, 0, 0, 0};
+    for (size_t i = 0; i < n && i < 4; ++i) fn[i] = (int32_t)mxGetPr(prhs[2])[i];
+    check(dgadv_set_source_terms(h, (int32_t)n, fn, n ? mxGetPr(prhs[3]) : NULL,
+                                 (nrhs > 4 && !mxIsEmpty(prhs[4])) ? mxGetPr(prhs[4]) : NULL), h);
+  } else if (!strcmp(cmd, "set_state")) {
+    check(dgadv_set_state(h, mxGetPr(prhs[2])), h);
+  } else if (!strcmp(cmd, "limit_state")) {
+    check(dgadv_limit_state(h, mxGetScalar(prhs[2])), h);
+  } else if (!strcmp(cmd, "step")) {
+    check(dgadv_step(h, (int32_t)mxGetScalar(prhs[2]), (int32_t)mxGetScalar(prhs[3]), mxGetScalar(prhs[4])), h);
+  } else if (!strcmp(cmd, "get_state")) {
+    const mwSize K = (mwSize)mxGetScalar(prhs[2]), N = (mwSize)mxGetScalar(prhs[3]);
+    plhs[0] = mxCreateDoubleMatrix(K, N, mxREAL);
+    check(dgadv_get_state(h, mxGetPr(plhs[0])), h);
+  } else if (!strcmp(cmd, "destroy")) {
+    for (int i = 0; i < MAX_HANDLES; ++i) if (g_open[i] == h) g_open[i] = NULL;
+    dgadv_destroy(h);
+  } else {
+    mexErrMsgIdAndTxt("dgadv:arg", "unknown command %s", cmd);
+  }
+}
