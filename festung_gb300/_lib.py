@@ -71,7 +71,12 @@ SYMBOLS = {
     'dgadv_last_error': (ctypes.c_char_p, [ctypes.c_void_p]),
     'dgadv_status_string': (ctypes.c_char_p, [ctypes.c_int]),
     'dgadv_destroy': (None, [ctypes.c_void_p]),
+    'dgadv_limit_linear_noalloc': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
 }
+
+NOALLOC_MAX_VERTICES = 1 << 18
 
 _lib = None
 

@@ -165,6 +165,36 @@ const char *dgadv_last_error(const dgadv_handle *h);
 const char *dgadv_status_string(int status);
 void dgadv_destroy(dgadv_handle *h);
 
+/* Largest vertex count dgadv_limit_linear_noalloc accepts (its fixed scratch: 4 MB per GPU). */
+#define DGADV_NOALLOC_MAX_VERTICES (1 << 18)
+
+/* One pass of the linear vertex-based slope limiter on device arrays the caller owns, with no
+ * device allocation by this call or by the library on its behalf.  This entry point has no
+ * counterpart in the reference; it exists for callers that cannot call cudaMalloc, e.g. code
+ * whose device memory all comes from another framework's pool (an allocation outside the pool
+ * breaks its accounting), code held to a device-memory budget fixed in advance, or code that
+ * must not trigger the device-wide synchronisation an allocation can cause.
+ *
+ * Same result as one solution-limiter pass of a handle created with typeSlopeLim =
+ * DGADV_LIM_LINEAR and precision DGADV_FP64 (FP64 arithmetic, the reference's global shift).
+ * Device arrays, column-major in element order, 0-based ids:
+ *   V0T          numT x 3 int32 vertex ids, each < numV
+ *   markV0TbdrD  numT x 3 uint8, non-zero at Dirichlet vertices (NULL: none)
+ *   dataV0T      numT x 3 Dirichlet values at those vertices (NULL: zero)
+ *   cIn, cOut    numT x N modal coefficients, N = (p+1)(p+2)/2; cOut may equal cIn
+ * p is 1, 2 or 3.  numV above DGADV_NOALLOC_MAX_VERTICES returns DGADV_ENOMEM.  The scratch is
+ * a file-scope __device__ array that every GPU loading the library holds until the process
+ * exits.  The first call on a device (and the first per degree p) does a synchronous set-up
+ * with that device current: it looks up the array's device address and uploads the degree's
+ * constant tables; make that first call before any stream capture.  All calls on a device
+ * share the one array, which keeps the previous call's contents (each call clears what it
+ * needs at its start), so calls whose work overlaps on the GPU (different streams, or
+ * different host threads, without ordering between them) race and give wrong results.
+ * Enqueued on `stream` (a cudaStream_t, NULL = default stream); asynchronous. */
+int dgadv_limit_linear_noalloc(int32_t p, int32_t numT, int32_t numV, const int32_t *V0T,
+                               const uint8_t *markV0TbdrD, const double *dataV0T,
+                               const double *cIn, double *cOut, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
