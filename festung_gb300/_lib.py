@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, 'libdgadv.so')
 
 DGADV_OK, DGADV_EINVAL, DGADV_ECUDA, DGADV_ENOMEM, DGADV_EMESH = 0, 1, 2, 3, 4
 DGADV_ENONFINITE, DGADV_ETIMEOUT, DGADV_EUNSUPPORTED = 5, 6, 7
-FP64, FP32 = 0, 1
+FP64, FP32, DF32 = 0, 1, 2
 LIM_LINEAR, LIM_HIERARCH_VERT, LIM_STRICT = 0, 1, 2
 TIME_CONST, TIME_EXP_NEG = 0, 1
 FLAG_NO_REORDER, FLAG_NO_SHIFT, FLAG_NO_GRAPH, FLAG_NO_PDL, FLAG_FUSE = 1, 2, 4, 8, 16

@@ -1,7 +1,8 @@
 """Builds ``festung_gb300/libdgadv.so`` in-tree (host C++ + CUDA for sm_103a).
 
-Usage: ``python -m festung_gb300.build`` (or ``festung_gb300.build.build()``).  The three
-translation units compile in parallel; the result is git-ignored.  Host code uses
+Usage: ``python -m festung_gb300.build`` (or ``festung_gb300.build.build()``).  The translation
+units (host helpers, C-ABI, one unit of kernels per arithmetic type, the no-allocation limiter)
+compile in parallel; the result is git-ignored.  Host code uses
 ``-ffp-contract=off`` so that grid and table arithmetic rounds as written on x86-64 and aarch64.
 """
 import os
@@ -28,7 +29,10 @@ def _cuda_home():
 
 
 def sources():
-    return [os.path.join(CSRC, f) for f in ('dgadv_host.cpp', 'dgadv_capi.cpp', 'dgadv_solver.cu')]
+    return [os.path.join(CSRC, f) for f in ('dgadv_host.cpp', 'dgadv_capi.cpp', 'dgadv_solver.cu',
+                                            'dgadv_prec_fp64.cu', 'dgadv_prec_fp32.cu',
+                                            'dgadv_prec_df32_p01.cu', 'dgadv_prec_df32_p2.cu',
+                                            'dgadv_prec_df32_p3.cu', 'dgadv_noalloc.cu')]
 
 
 def _stale():

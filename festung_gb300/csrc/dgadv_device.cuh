@@ -1,0 +1,1325 @@
+// Device solver of the explicit DG advection step and its C-ABI entry points.
+//
+// Per-stage operator (advection/preprocessSubStep.m:56-99 + advection/solveSubStep.m:57-99),
+// matrix-free and element-centric:
+//   volume  (G1+G2)c |_{k,i} = sum_q c(x_q) [d1 phi_i (B22 u1 - B12 u2) + d2 phi_i (B11 u2 - B21 u1)] W_q
+//           (core/assembleMatElemDphiPhiFuncDisc.m:181-202; same rule of order 2p as hatG)
+//   flux    (R c)_{k,i} = sum_n |E_kn| sum_r w_r v_knr phi_i(g_n(q_r)) * (v>0 ? c_k : c_k+) traces
+//           (core/assembleMatEdgePhiPhiValUpwind.m:261-299: the upwind side is gathered through
+//           the neighbour map, so every element writes only its own rows: no atomics)
+//   mass    cDot = hatM^-1 rhs / detJ (FP64; the FP32 path uses hatM = I, |hatM - I| < 2e-14)
+//   SSP     c^(s) = w_s c^n + (1-w_s)(c^(s-1) + tau cDot)          advection/solveSubStep.m:83
+// Limiter: core/applySlopeLimiterTaylor*.m with patch min/max over CSR vertex patches
+// (core/computeMinMaxV0TElementPatch.m:66-112) and the Taylor transform in closed form
+// (Taylor coefficients = mean and scaled derivatives at the barycentre).
+//
+// This header holds every kernel, templated on the stored real type T (double, float or the
+// double-float df32).  A translation unit that includes it defines the constant tables of its
+// T and the tab<T, P>() accessors (DGADV_DEFINE_TABLES) before instantiating kernels, so that
+// the kernels of each arithmetic type compile in a unit of their own.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <type_traits>
+
+#include "dgadv_handle.h"
+#include "dgadv_kernels.cuh"
+#include "dgadv_df32.cuh"
+
+namespace dgadv {
+
+// Constant tables of one (type, degree): defined by the including unit.
+template <typename T, int P> __device__ __forceinline__ const Tab<T, P> &tab();
+namespace {
+template <typename T, int P> const void *tab_symbol();   // host address of the unit's table
+}  // namespace
+
+#define DGADV_DEFINE_TABLES(T, NAME)                                                            \
+  static __constant__ Tab<T, 0> NAME##0;                                                        \
+  static __constant__ Tab<T, 1> NAME##1;                                                        \
+  static __constant__ Tab<T, 2> NAME##2;                                                        \
+  static __constant__ Tab<T, 3> NAME##3;                                                        \
+  template <> __device__ __forceinline__ const Tab<T, 0> &tab<T, 0>() { return NAME##0; }       \
+  template <> __device__ __forceinline__ const Tab<T, 1> &tab<T, 1>() { return NAME##1; }       \
+  template <> __device__ __forceinline__ const Tab<T, 2> &tab<T, 2>() { return NAME##2; }       \
+  template <> __device__ __forceinline__ const Tab<T, 3> &tab<T, 3>() { return NAME##3; }       \
+  namespace {                                                                                   \
+  template <> [[maybe_unused]] const void *tab_symbol<T, 0>() { return (const void *)&NAME##0; }  \
+  template <> [[maybe_unused]] const void *tab_symbol<T, 1>() { return (const void *)&NAME##1; }  \
+  template <> [[maybe_unused]] const void *tab_symbol<T, 2>() { return (const void *)&NAME##2; }  \
+  template <> [[maybe_unused]] const void *tab_symbol<T, 3>() { return (const void *)&NAME##3; }  \
+  }
+
+// ---------------------------------------------------------------------------------------------
+// Ordered integer keys: atomicMin/atomicMax on the key order like on the real numbers.
+__device__ __forceinline__ unsigned long long okey(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ unsigned long long okey(float x) {
+  const unsigned int u = __float_as_uint(x);
+  return (unsigned long long)((u >> 31) ? ~u : (u | 0x80000000u));
+}
+template <typename T> __device__ __forceinline__ T okey_inv(unsigned long long k);
+template <> __device__ __forceinline__ double okey_inv<double>(unsigned long long k) {
+  const unsigned long long u = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFULL) : ~k;
+  return __longlong_as_double((long long)u);
+}
+template <> __device__ __forceinline__ float okey_inv<float>(unsigned long long k) {
+  const unsigned int kk = (unsigned int)k;
+  const unsigned int u = (kk >> 31) ? (kk & 0x7FFFFFFFu) : ~kk;
+  return __uint_as_float(u);
+}
+template <typename T> __host__ __device__ constexpr unsigned long long key_max();
+template <> __host__ __device__ constexpr unsigned long long key_max<double>() { return ~0ULL; }
+template <> __host__ __device__ constexpr unsigned long long key_max<float>() { return 0xFFFFFFFFULL; }
+
+__device__ __forceinline__ bool finite_(double x) { return isfinite(x); }
+__device__ __forceinline__ bool finite_(float x) { return isfinite(x); }
+
+// df32: the key of hi in the high half and the key of lo in the low half orders pairs like
+// their (hi, lo) lexicographic order, which is the order of the values for normalised pairs;
+// the key is exact and invertible.
+__device__ __forceinline__ unsigned long long okey(const df32 &x) {
+  return (okey(x.hi) << 32) | okey(x.lo);
+}
+template <> __device__ __forceinline__ df32 okey_inv<df32>(unsigned long long k) {
+  return df32(okey_inv<float>(k >> 32), okey_inv<float>(k & 0xFFFFFFFFULL));
+}
+template <> __host__ __device__ constexpr unsigned long long key_max<df32>() { return ~0ULL; }
+__device__ __forceinline__ bool finite_(const df32 &x) { return isfinite(x.hi) && isfinite(x.lo); }
+
+// ---------------------------------------------------------------------------------------------
+// Element geometry for the Taylor transform.
+template <typename T> struct Affine {
+  T B11, B12, B21, B22;   // B(:,m,n): m = coordinate, n = column
+  T A11, A12, A21, A22;   // A = B^-1
+  T dX, idX;              // dX = 2 / sqrt(detJ)
+  T ox[3], oy[3];         // vertex offsets from the barycentre
+};
+
+template <typename T> __device__ __forceinline__ Affine<T> load_affine(const Geo<T> &g, int k) {
+  Affine<T> a;
+  a.B11 = g.Bm[k]; a.B12 = g.Bm[g.Kp + k]; a.B21 = g.Bm[2 * g.Kp + k]; a.B22 = g.Bm[3 * g.Kp + k];
+  const T det = a.B11 * a.B22 - a.B12 * a.B21;
+  const T idet = T(1) / det;
+  a.A11 = a.B22 * idet; a.A12 = -a.B12 * idet; a.A21 = -a.B21 * idet; a.A22 = a.B11 * idet;
+  a.dX = T(2) / sqrt(det);
+  a.idX = T(1) / a.dX;
+  const T bx = -(a.B11 + a.B12) / T(3), by = -(a.B21 + a.B22) / T(3);
+  a.ox[0] = bx; a.oy[0] = by;
+  a.ox[1] = a.B11 + bx; a.oy[1] = a.B21 + by;
+  a.ox[2] = a.B12 + bx; a.oy[2] = a.B22 + by;
+  return a;
+}
+
+// Coefficients of (a + b z)^(D-m) (c + e z)^m in z^j, for m, j = 0..D.
+template <typename T, int D>
+__device__ __forceinline__ void deriv_block(T a, T b, T c, T e, T S[D + 1][D + 1]) {
+#pragma unroll
+  for (int m = 0; m <= D; ++m) {
+    T poly[D + 1];
+#pragma unroll
+    for (int j = 0; j <= D; ++j) poly[j] = (j == 0) ? T(1) : T(0);
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      const bool first = r < D - m;
+      const T x0 = first ? a : c, x1 = first ? b : e;
+#pragma unroll
+      for (int j = D; j >= 0; --j) poly[j] = poly[j] * x0 + (j > 0 ? poly[j - 1] * x1 : T(0));
+    }
+#pragma unroll
+    for (int j = 0; j <= D; ++j) S[m][j] = poly[j];
+  }
+}
+
+// modal c -> Taylor coefficients cT (core/projectDataDisc2DataTaylor.m:56-61 in closed form)
+template <typename T, int P>
+__device__ __forceinline__ void to_taylor(const T *c, const Affine<T> &af, T *cT) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T u[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    T s = T(0);
+#pragma unroll
+    for (int j = 0; j < N; ++j) s += tb.DM[i][j] * c[j];
+    u[i] = s;
+  }
+  cT[0] = u[0];
+  T sc = T(1);
+#pragma unroll
+  for (int d = 1; d <= P; ++d) {
+    sc *= af.idX;
+    const int off = d * (d + 1) / 2;
+    if (d == 1) {
+      T S[2][2]; deriv_block<T, 1>(af.A11, af.A21, af.A12, af.A22, S);
+#pragma unroll
+      for (int m = 0; m <= 1; ++m) { T s = T(0);
+#pragma unroll
+        for (int j = 0; j <= 1; ++j) s += S[m][j] * u[off + j]; cT[off + m] = s * sc; }
+    } else if (d == 2) {
+      T S[3][3]; deriv_block<T, 2>(af.A11, af.A21, af.A12, af.A22, S);
+#pragma unroll
+      for (int m = 0; m <= 2; ++m) { T s = T(0);
+#pragma unroll
+        for (int j = 0; j <= 2; ++j) s += S[m][j] * u[off + j]; cT[off + m] = s * sc; }
+    } else if (d == 3) {
+      T S[4][4]; deriv_block<T, 3>(af.A11, af.A21, af.A12, af.A22, S);
+#pragma unroll
+      for (int m = 0; m <= 3; ++m) { T s = T(0);
+#pragma unroll
+        for (int j = 0; j <= 3; ++j) s += S[m][j] * u[off + j]; cT[off + m] = s * sc; }
+    }
+  }
+}
+
+// Taylor coefficients -> modal (core/projectDataTaylor2DataDisc.m:56-61 in closed form)
+template <typename T, int P>
+__device__ __forceinline__ void from_taylor(const T *cT, const Affine<T> &af, T *c) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T w[N];
+  w[0] = cT[0];
+  T sc = T(1);
+#pragma unroll
+  for (int d = 1; d <= P; ++d) {
+    sc *= af.dX;
+    const int off = d * (d + 1) / 2;
+    if (d == 1) {
+      T S[2][2]; deriv_block<T, 1>(af.B11, af.B21, af.B12, af.B22, S);
+#pragma unroll
+      for (int m = 0; m <= 1; ++m) { T s = T(0);
+#pragma unroll
+        for (int j = 0; j <= 1; ++j) s += S[m][j] * cT[off + j]; w[off + m] = s * sc; }
+    } else if (d == 2) {
+      T S[3][3]; deriv_block<T, 2>(af.B11, af.B21, af.B12, af.B22, S);
+#pragma unroll
+      for (int m = 0; m <= 2; ++m) { T s = T(0);
+#pragma unroll
+        for (int j = 0; j <= 2; ++j) s += S[m][j] * cT[off + j]; w[off + m] = s * sc; }
+    } else if (d == 3) {
+      T S[4][4]; deriv_block<T, 3>(af.B11, af.B21, af.B12, af.B22, S);
+#pragma unroll
+      for (int m = 0; m <= 3; ++m) { T s = T(0);
+#pragma unroll
+        for (int j = 0; j <= 3; ++j) s += S[m][j] * cT[off + j]; w[off + m] = s * sc; }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    T s = T(0);
+#pragma unroll
+    for (int j = 0; j < N; ++j) s += tb.DMinv[i][j] * w[j];
+    c[i] = s;
+  }
+}
+
+// Index of the Taylor DOF with multi-index (a1, a2) (core/mult2ind.m:57-62, 0-based).
+__host__ __device__ constexpr int mind(int a1, int a2) { return (a1 + a2) * (a1 + a2 + 1) / 2 + a2; }
+
+template <int P> struct NCQ { static constexpr int value = P * (P + 1) / 2 > 1 ? P * (P + 1) / 2 : 1; };
+
+// Centroid quantities of the sub-limiters (one per computeVertexBasedLimiter call).
+template <typename T, int P>
+__device__ __forceinline__ void centroid_quantities(const T *cT, int type, T *qv) {
+  if (type == 0) {
+    qv[0] = cT[0];
+  } else {
+    int s = 0;
+#pragma unroll
+    for (int ord = P; ord >= 1; --ord)
+#pragma unroll
+      for (int i = 1; i <= ord; ++i) { qv[s] = cT[mind(ord - i, i - 1)]; ++s; }
+  }
+}
+
+// Limiter pass plumbing.  Pass j scatters its centroid quantities into per-vertex min / max
+// slots vkeys[j%3] with atomicMin / atomicMax on order-preserving integer keys (each element
+// updates its three vertices: the patch of a vertex is exactly the elements that update it,
+// core/computeMinMaxV0TElementPatch.m:99-111), and the global extremes (for the reference's
+// shift) into slots[j%3].  The producer of pass j resets the slots of pass j+1; three sets keep
+// the kernel that consumes pass j and produces pass j+1 clear of both.
+template <typename T> struct KeyOf { using type = unsigned int; };
+template <> struct KeyOf<double> { using type = unsigned long long; };
+template <> struct KeyOf<df32> { using type = unsigned long long; };
+
+__device__ __forceinline__ unsigned int okey32(float x) { return (unsigned int)okey(x); }
+__device__ __forceinline__ unsigned int vkey(float x) { return okey32(x); }
+__device__ __forceinline__ unsigned long long vkey(double x) { return okey(x); }
+__device__ __forceinline__ unsigned long long vkey(const df32 &x) { return okey(x); }
+template <typename T> __device__ __forceinline__ T vkey_inv(typename KeyOf<T>::type k) { return okey_inv<T>(k); }
+template <typename T> __host__ __device__ constexpr typename KeyOf<T>::type vkey_max() {
+  return (typename KeyOf<T>::type)key_max<T>();
+}
+
+template <typename T> struct LimOut {
+  typename KeyOf<T>::type *vkeys;   // nc x 2 x Vp vertex min / max keys of this pass
+  typename KeyOf<T>::type *vreset;  // the next pass's vertex keys, reset here
+  unsigned long long *slots;        // kSlotCopies x 2 x nc encoded global min / max (atomic)
+  unsigned long long *reset;        // slots of the next pass, reset by block 0
+  int nc, type;
+};
+template <typename T> struct LimIn {
+  const typename KeyOf<T>::type *vkeys;
+  const unsigned long long *slots;  // kSlotCopies x 2 x nc
+  int nc, type, shift;
+};
+
+// Scatter of the element's centroid quantities to its vertices and the block's global extremes.
+template <typename T, int NQ>
+__device__ __forceinline__ void scatter_quantities(const Geo<T> &g, const LimOut<T> &lo, const T *qv,
+                                                   const int vid[3], bool active) {
+  if (active) {
+#pragma unroll
+    for (int s = 0; s < NQ; ++s) {
+      if (s >= lo.nc) break;
+      const auto key = vkey(qv[s]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        atomicMin(&lo.vkeys[(size_t)(2 * s) * g.Vp + vid[n]], key);
+        atomicMax(&lo.vkeys[(size_t)(2 * s + 1) * g.Vp + vid[n]], key);
+      }
+    }
+  }
+  // global extremes: warp shuffles, then the block's four warps through shared memory, then one
+  // atomic per quantity and block into one of kSlotCopies copies (spreads same-address atomics)
+  __shared__ T red[kBlock / 32][2 * NQ];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < NQ; ++s) {
+    T mn = (active && s < lo.nc) ? qv[s] : T(INFINITY), mx = (active && s < lo.nc) ? qv[s] : T(-INFINITY);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (lane == 0) { red[warp][2 * s] = mn; red[warp][2 * s + 1] = mx; }
+  }
+  __syncthreads();
+  if (threadIdx.x < lo.nc) {
+    const int s = threadIdx.x;
+    T mn = red[0][2 * s], mx = red[0][2 * s + 1];
+#pragma unroll
+    for (int w = 1; w < kBlock / 32; ++w) { mn = fmin(mn, red[w][2 * s]); mx = fmax(mx, red[w][2 * s + 1]); }
+    if (mn <= mx) {
+      unsigned long long *sl = lo.slots + (size_t)(blockIdx.x % kSlotCopies) * 2 * lo.nc;
+      atomicMin(&sl[2 * s], okey(mn));
+      atomicMax(&sl[2 * s + 1], okey(mx));
+    }
+  }
+}
+
+// Reset of the next pass's vertex keys (thread t owns vertex t) and global slots (block 0).
+template <typename T>
+__device__ __forceinline__ void reset_next(const Geo<T> &g, const LimOut<T> &lo, int t) {
+  if (t < g.numV)
+    for (int s = 0; s < lo.nc; ++s) {
+      lo.vreset[(size_t)(2 * s) * g.Vp + t] = vkey_max<T>();
+      lo.vreset[(size_t)(2 * s + 1) * g.Vp + t] = 0;
+    }
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < kSlotCopies * 2 * lo.nc; i += blockDim.x)
+      lo.reset[i] = (i & 1) ? 0ULL : key_max<T>();
+}
+
+// Global extremes of every quantity from the kSlotCopies copies (warp 0), turned into the shift
+// values of core/computeMinMaxV0TElementPatch.m:75-78: sh[2s] = |min|+1, sh[2s+1] = |max|+1.
+template <typename T>
+__device__ __forceinline__ void load_shifts(const unsigned long long *slots, int nc, T *sh) {
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  for (int s = 0; s < nc; ++s) {
+    T mn = okey_inv<T>(slots[(size_t)lane * 2 * nc + 2 * s]);
+    T mx = okey_inv<T>(slots[(size_t)lane * 2 * nc + 2 * s + 1]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (lane == 0) { sh[2 * s] = fabs(mn) + T(1); sh[2 * s + 1] = fabs(mx) + T(1); }
+  }
+}
+
+// alpha of one computeVertexBasedLimiter call (core/computeVertexBasedLimiter.m:78-106)
+template <typename T>
+__device__ __forceinline__ T vertex_alpha(T cbar, const T v[3], const T mn[3], const T mx[3]) {
+  const T tol = T(1.e-8);
+  T alpha = T(1);
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const T dV = v[n] - cbar, dMin = mn[n] - cbar, dMax = mx[n] - cbar;
+    T a = T(1);
+    if (dV < dMin + tol) a = fmax(T(0), fmin(T(1), dMin / (dV - tol)));
+    if (dV > dMax - tol) a = fmax(T(0), fmin(T(1), dMax / (dV + tol)));
+    alpha = (n == 0) ? a : fmin(alpha, a);
+  }
+  return alpha;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Block staging: the rows of one block's elements (SoA rows, kBlock consecutive elements each)
+// are copied global -> shared by the TMA unit (cp.async.bulk, one elected thread) while the
+// threads load neighbour and vertex data directly.  The wait on the mbarrier is bounded in time;
+// on a timeout the kernel sets bit 1 of the error flag and leaves the element unprocessed.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for phase 0 of the block's barrier, at most ~2^31 SM cycles (about a second); after a
+// timeout it flags the error, gives the copies in flight the same time again, and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *flag) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, 0))
+    if (clock64() - t0 > (1LL << 31)) {
+      atomicOr(flag, 2);
+      const long long t1 = clock64();
+      while (!mbar_try_wait(bar, 0) && clock64() - t1 < (1LL << 31)) {
+      }
+      return false;
+    }
+  return true;
+}
+
+// Row copies into the staged layout (row index within the T rows / the int rows).
+template <typename T>
+__device__ __forceinline__ void stage_T(unsigned char *smem, int row, const T *base, int nrows, int Kp, int k0,
+                                        uint64_t *bar) {
+  for (int r = 0; r < nrows; ++r)
+    bulk_g2s(smem + (size_t)(row + r) * kBlock * sizeof(T), base + (size_t)r * Kp + k0, kBlock * sizeof(T), bar);
+}
+template <typename T>
+__device__ __forceinline__ void stage_I(unsigned char *smem, int nT, int row, const int *base, int nrows, int Kp,
+                                        int k0, uint64_t *bar) {
+  for (int r = 0; r < nrows; ++r)
+    bulk_g2s(smem + (size_t)nT * kBlock * sizeof(T) + (size_t)(row + r) * kBlock * sizeof(int),
+             base + (size_t)r * Kp + k0, kBlock * sizeof(int), bar);
+}
+template <typename T>
+__device__ __forceinline__ void stage_expect(uint64_t *bar, int nT, int nI) {
+  mbar_expect_tx(bar, nT * kBlock * (uint32_t)sizeof(T) + nI * kBlock * (uint32_t)sizeof(int));
+}
+
+// Programmatic dependent launch: the next kernel in the stream may start its prologue (static
+// data only) once every block of this one has started; pdl_wait() blocks until the previous
+// kernel has completed and its writes are visible.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename T> __device__ __forceinline__ const T *srow(const unsigned char *smem, int r) {
+  return (const T *)(smem + (size_t)r * kBlock * sizeof(T));
+}
+template <typename T> __device__ __forceinline__ const int *irow(const unsigned char *smem, int nT, int r) {
+  return (const int *)(smem + (size_t)nT * kBlock * sizeof(T) + (size_t)r * kBlock * sizeof(int));
+}
+
+template <typename T, int P> struct StageRows {
+  static constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NMT = Dims<P>::NMT;
+  // k_stage_op: c, [c0], F, Vn, [B] | code
+  __host__ __device__ static constexpr int op(int mode, bool lin) {
+    return N + (mode != 2 ? N : 0) + 2 * Q + 3 * R + (mode != 0 && !lin ? 4 : 0);
+  }
+  // k_limit_dot: tbuf, B, MT, c0, cin | code
+  __host__ __device__ static constexpr int limdot() { return N + 4 + NMT + 2 * N; }
+  // k_limit: tbuf, B | code
+  __host__ __device__ static constexpr int lim() { return N + 4; }
+  // k_limit_dot_lin: cDot, Q (N x (N-1)), c0, cin | code
+  __host__ __device__ static constexpr int limdot_lin() { return N + N * (N - 1) + 2 * N; }
+  // k_to_taylor: c, B
+  __host__ __device__ static constexpr int totaylor() { return N + 4; }
+  // rows first, then the block's mbarrier (8 bytes, 16 reserved)
+  __host__ __device__ static constexpr size_t bar_offset(int nT, int nI) {
+    return (size_t)nT * kBlock * sizeof(T) + (size_t)nI * kBlock * sizeof(int);
+  }
+  // + 16 for the mbarrier, + 2 x 6 shift values
+  __host__ __device__ static constexpr size_t bytes(int nT, int nI) { return bar_offset(nT, nI) + 16 + 12 * sizeof(T); }
+};
+
+// Prefetch of the three vertices' min / max keys of every sub-limiter quantity.
+template <typename T, int NQ> struct VKeys {
+  typename KeyOf<T>::type v[NQ][2][3];
+};
+template <typename T, int NQ>
+__device__ __forceinline__ void load_vkeys(const Geo<T> &g, const LimIn<T> &li, const int vid[3], VKeys<T, NQ> &kv) {
+#pragma unroll
+  for (int s = 0; s < NQ; ++s)
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+      for (int n = 0; n < 3; ++n)
+        kv.v[s][m][n] = (s < li.nc) ? li.vkeys[(size_t)(2 * s + m) * g.Vp + vid[n]] : 0;
+}
+
+// Patch min / max of quantity s at the three vertices (from the prefetched vertex keys), with
+// the reference's global shift (min over the patch of (v - sNeg), then + sNeg; a monotone shift
+// commutes with min), then combined with the Dirichlet data (NaN = none; fmin / fmax ignore NaN
+// like Matlab's min / max).
+template <typename T, int NQ>
+__device__ __forceinline__ void patch_minmax(const LimIn<T> &li, const VKeys<T, NQ> &kv, const T *sh, int s,
+                                             const T valD[3], T mn[3], T mx[3]) {
+  T sNeg = T(0), sPos = T(0);
+  if (li.shift) { sPos = sh[2 * s]; sNeg = sh[2 * s + 1]; }
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    T a = vkey_inv<T>(kv.v[s][0][n]);
+    T c = vkey_inv<T>(kv.v[s][1][n]);
+    if (li.shift) { a = (a - sNeg) + sNeg; c = (c + sPos) - sPos; }
+    mn[n] = fmin(a, valD[n]);
+    mx[n] = fmax(c, valD[n]);
+  }
+}
+
+// Limit Taylor coefficients in place (linear / hierarchical vertex).  dataV0T: boundary values
+// at the three vertices for Dirichlet vertices (NaN means "no data").
+template <typename T, int P, int NQ>
+__device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, NQ> &kv, const T *sh,
+                                             const Affine<T> &af, int dmask, const T dataV0T[3], T *cT) {
+  constexpr int N = Dims<P>::N;
+  const T nan_ = T(NAN);
+  T pt1[3], pt2[3];   // Taylor basis functions 2 and 3 at the vertices
+#pragma unroll
+  for (int n = 0; n < 3; ++n) { pt1[n] = af.ox[n] * af.dX; pt2[n] = af.oy[n] * af.dX; }
+  if (li.type == 0) {
+    T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      v[n] = (cT[0] * T(1) + cT[1] * pt1[n]) + cT[2] * pt2[n];
+      valD[n] = ((dmask >> n) & 1) ? dataV0T[n] : nan_;
+    }
+    patch_minmax<T, NQ>(li, kv, sh, 0, valD, mn, mx);
+    const T alpha = vertex_alpha(cT[0], v, mn, mx);
+    cT[1] *= alpha; cT[2] *= alpha;
+    const T keep = (alpha == T(1)) ? T(1) : T(0);
+#pragma unroll
+    for (int i = 3; i < N; ++i) cT[i] *= keep;
+  } else {
+    T orig[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) orig[i] = cT[i];
+    T alpha = T(0);
+    int s = 0;
+#pragma unroll
+    for (int ord = P; ord >= 1; --ord) {
+      T aOrd = T(1);
+#pragma unroll
+      for (int i = 1; i <= ord; ++i) {
+        const int i0 = mind(ord - i, i - 1), i1 = mind(ord - i + 1, i - 1), i2 = mind(ord - i, i);
+        T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+          v[n] = (orig[i0] * T(1) + orig[i1] * pt1[n]) + orig[i2] * pt2[n];
+          valD[n] = ((dmask >> n) & 1) ? (ord > 1 ? v[n] : dataV0T[n]) : nan_;
+        }
+        patch_minmax<T, NQ>(li, kv, sh, s, valD, mn, mx);
+        aOrd = fmin(aOrd, vertex_alpha(orig[i0], v, mn, mx));
+        ++s;
+      }
+      alpha = fmax(alpha, aOrd);
+#pragma unroll
+      for (int i = ord * (ord + 1) / 2; i < (ord + 1) * (ord + 2) / 2; ++i) cT[i] = alpha * orig[i];
+    }
+  }
+}
+
+// Element geometry from staged rows of B.
+template <typename T> __device__ __forceinline__ Affine<T> affine_from(T B11, T B12, T B21, T B22) {
+  Affine<T> a;
+  a.B11 = B11; a.B12 = B12; a.B21 = B21; a.B22 = B22;
+  const T det = a.B11 * a.B22 - a.B12 * a.B21;
+  const T idet = T(1) / det;
+  a.A11 = a.B22 * idet; a.A12 = -a.B12 * idet; a.A21 = -a.B21 * idet; a.A22 = a.B11 * idet;
+  a.dX = T(2) / sqrt(det);
+  a.idX = T(1) / a.dX;
+  const T bx = -(a.B11 + a.B12) / T(3), by = -(a.B21 + a.B22) / T(3);
+  a.ox[0] = bx; a.oy[0] = by;
+  a.ox[1] = a.B11 + bx; a.oy[1] = a.B21 + by;
+  a.ox[2] = a.B12 + bx; a.oy[2] = a.B22 + by;
+  return a;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Linear limiter without element geometry.  The centroid value and the vertex values of the
+// linear Taylor reconstruction (core/applySlopeLimiterTaylorLinear.m:108-122) are
+//     cbar = u_0,   v_n = u_0 + u_1 (x^_n - c^)_1 + u_2 (x^_n - c^)_2,   u = DM c,
+// because grad u(b) . (x_n - b) is invariant under the affine map to the reference element
+// (x^_n the reference vertices, c^ = (1/3, 1/3)).  Scaling Taylor degree blocks commutes with
+// the block-diagonal map between reference derivatives and Taylor coefficients, so the limited
+// coefficients are c - DM^-1 du with du = (0, (1-a) u_1, (1-a) u_2, [a != 1] u_3, ...).
+template <typename T, int P>
+__device__ __forceinline__ void lin_u(const T *c, T *u) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    T s = T(0);
+#pragma unroll
+    for (int j = 0; j < N; ++j) s += tb.DM[i][j] * c[j];
+    u[i] = s;
+  }
+}
+template <typename T, int P> __device__ __forceinline__ T lin_mean(const T *c) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T s = T(0);
+#pragma unroll
+  for (int j = 0; j < N; ++j) s += tb.DM[0][j] * c[j];
+  return s;
+}
+// alpha of the linear limiter from u, and the removed part du (returns false if alpha == 1).
+template <typename T, int P, int NQ>
+__device__ __forceinline__ bool lin_alpha(const LimIn<T> &li, const VKeys<T, NQ> &kv, const T *sh, const T *u,
+                                          int dmask, const T dataV0T[3], T *du) {
+  constexpr int N = Dims<P>::N;
+  const T third = T(1) / T(3), two3 = T(2) / T(3);
+  const T hx[3] = {-third, two3, -third}, hy[3] = {-third, -third, two3};
+  T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    v[n] = (u[0] * T(1) + u[1] * hx[n]) + u[2] * hy[n];
+    valD[n] = ((dmask >> n) & 1) ? dataV0T[n] : T(NAN);
+  }
+  patch_minmax<T, NQ>(li, kv, sh, 0, valD, mn, mx);
+  const T alpha = vertex_alpha(u[0], v, mn, mx);
+  if (alpha == T(1)) return false;
+  du[0] = T(0);
+  du[1] = (T(1) - alpha) * u[1];
+  du[2] = (T(1) - alpha) * u[2];
+#pragma unroll
+  for (int i = 3; i < N; ++i) du[i] = u[i];
+  return true;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Stage operator.  MODE 0: write c^(s);  MODE 1: write Taylor(c^(s)) and scatter its centroid
+// quantities;  MODE 2: write Taylor(cDot) and scatter its quantities (time-derivative limiting
+// follows).
+struct StageScalars {
+  double omega, tau;
+  double gco[4];        // g_m(t) of the source terms / boundary data
+  int *flag;            // bit 0: non-finite value seen; bit 1: a bounded wait timed out
+};
+
+template <typename T, int P, int MODE, bool RHS, bool LIN>
+__global__ void __launch_bounds__(kBlock)
+k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ out,
+           const LimOut<T> lo, const StageScalars sc) {
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
+  constexpr int NT = StageRows<T, P>::op(MODE, LIN);
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  const Tab<T, P> &tb = tab<T, P>();
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  pdl_trigger();
+  const int Kp = g.Kp;
+  const bool staged = k0 < g.K;                   // blocks beyond the elements only reset keys
+  constexpr int rC = 0, rC0 = N, rF = (MODE != 2) ? 2 * N : N, rV = rF + 2 * Q, rB = rV + 3 * R;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) {                                 // static rows before the dependency wait
+      stage_expect<T>(bar, NT, 1);
+      stage_T(smem, rF, g.F, 2 * Q, Kp, k0, bar);
+      stage_T(smem, rV, g.Vn, 3 * R, Kp, k0, bar);
+      if (MODE != 0 && !LIN) stage_T(smem, rB, g.Bm, 4, Kp, k0, bar);
+      stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+    }
+  }
+  const bool active = k < g.K;
+  int nb[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) nb[n] = active ? g.nbr[(size_t)n * Kp + k] : -1;
+  int vid[3] = {0, 0, 0};
+  if (MODE != 0 && active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  if (MODE != 0) reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) {                                   // state rows after it
+    stage_T(smem, rC, cin, N, Kp, k0, bar);
+    if (MODE != 2) stage_T(smem, rC0, c0, N, Kp, k0, bar);
+  }
+  // neighbour coefficients: outside the block from global memory now, inside from shared later
+  T cn[3][N];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const bool outside = nb[n] >= 0 && (nb[n] < k0 || nb[n] >= k0 + kBlock);
+#pragma unroll
+    for (int j = 0; j < N; ++j) cn[n][j] = outside ? cin[(size_t)j * Kp + nb[n]] : T(0);
+  }
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T qv[NQ];
+  bool bad = false;
+  if (active && ok) {
+    T c[N], rhs[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = T(0); }
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      if (nb[n] >= k0 && nb[n] < k0 + kBlock)
+#pragma unroll
+        for (int j = 0; j < N; ++j) cn[n][j] = srow<T>(smem, rC + j)[nb[n] - k0];
+    if (RHS) {
+      for (int m = 0; m < g.nTerms; ++m) {
+        const T gm = T(sc.gco[m]);
+#pragma unroll
+        for (int i = 0; i < N; ++i) rhs[i] += gm * g.rhs[((size_t)m * N + i) * Kp + k];
+      }
+    }
+    // volume term
+#pragma unroll
+    for (int qq = 0; qq < Q; ++qq) {
+      T cq = T(0);
+#pragma unroll
+      for (int j = 0; j < N; ++j) cq += tb.phiQ[qq][j] * c[j];
+      const T f1 = srow<T>(smem, rF + qq)[t] * cq;
+      const T f2 = srow<T>(smem, rF + Q + qq)[t] * cq;
+#pragma unroll
+      for (int i = 0; i < N; ++i) rhs[i] += tb.g1[qq][i] * f1 + tb.g2[qq][i] * f2;
+    }
+    // upwind edge term
+    const int code = irow<T>(smem, NT, 0)[t];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      const int np = (code >> (2 * n)) & 3;
+      const bool outOk = (code >> (6 + n)) & 1;
+#pragma unroll
+      for (int r2 = 0; r2 < R; ++r2) {
+        const T v = srow<T>(smem, rV + n * R + r2)[t];
+        T tr = T(0);
+        if (v > T(0) && outOk) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r2][j] * c[j];
+        } else if (v < T(0) && nb[n] >= 0) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r2][j] * cn[n][j];
+        }
+        const T fl = v * tr;
+#pragma unroll
+        for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r2][i] * fl;
+      }
+    }
+    // mass solve
+    T cdot[N];
+    if (sizeof(T) == 8) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int j = 0; j < N; ++j) s += tb.hatMinv[i][j] * rhs[j];
+        cdot[i] = s;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) cdot[i] = rhs[i];
+    }
+    if (MODE == 2 && LIN) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cdot[i]; bad |= !finite_(cdot[i]); }
+      qv[0] = lin_mean<T, P>(cdot);
+    } else if (MODE == 2) {
+      const Affine<T> af = affine_from<T>(srow<T>(smem, rB)[t], srow<T>(smem, rB + 1)[t],
+                                          srow<T>(smem, rB + 2)[t], srow<T>(smem, rB + 3)[t]);
+      T cT[N];
+      to_taylor<T, P>(cdot, af, cT);
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cT[i]; bad |= !finite_(cT[i]); }
+      centroid_quantities<T, P>(cT, lo.type, qv);
+    } else {
+      const T w = T(sc.omega), tau = T(sc.tau);
+      T cnew[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) cnew[i] = w * srow<T>(smem, rC0 + i)[t] + (T(1) - w) * (c[i] + tau * cdot[i]);
+      if (MODE == 0 || LIN) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+        if (MODE == 1) qv[0] = lin_mean<T, P>(cnew);
+      } else {
+        const Affine<T> af = affine_from<T>(srow<T>(smem, rB)[t], srow<T>(smem, rB + 1)[t],
+                                            srow<T>(smem, rB + 2)[t], srow<T>(smem, rB + 3)[t]);
+        T cT[N];
+        to_taylor<T, P>(cnew, af, cT);
+#pragma unroll
+        for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cT[i]; bad |= !finite_(cT[i]); }
+        centroid_quantities<T, P>(cT, lo.type, qv);
+      }
+    }
+  }
+  if (MODE != 0) scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok);
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Time-derivative limiting and SSP update (advection/solveSubStep.m:69-83), then the Taylor
+// form of the new stage value and the scatter of its centroid quantities for the solution
+// limiter.
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit_dot(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ tbuf,
+            const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value, NMT = Dims<P>::NMT;
+  constexpr int NT = StageRows<T, P>::limdot();
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  pdl_trigger();
+  const int Kp = g.Kp;
+  const bool staged = k0 < g.K;
+  constexpr int rT = 0, rB = N, rM = N + 4, rC0 = N + 4 + NMT, rC = rC0 + N;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) {
+      stage_expect<T>(bar, NT, 1);
+      stage_T(smem, rB, g.Bm, 4, Kp, k0, bar);
+      stage_T(smem, rM, g.MT, NMT, Kp, k0, bar);
+      stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+    }
+  }
+  const bool active = k < g.K;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) {
+    stage_T(smem, rT, (const T *)tbuf, N, Kp, k0, bar);
+    stage_T(smem, rC0, c0, N, Kp, k0, bar);
+    stage_T(smem, rC, cin, N, Kp, k0, bar);
+  }
+  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T qv[NQ];
+  bool bad = false;
+  if (active && ok) {
+    const Affine<T> af = affine_from<T>(srow<T>(smem, rB)[t], srow<T>(smem, rB + 1)[t],
+                                        srow<T>(smem, rB + 2)[t], srow<T>(smem, rB + 3)[t]);
+    T cT[N], lim[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) { cT[i] = srow<T>(smem, rT + i)[t]; lim[i] = cT[i]; }
+    const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
+    const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
+    limit_taylor<T, P, NQ>(li, kv, sh, af, dmask, nan3, lim);
+    // Taylor mass correction M_corr = diag(1/diag(M_T)) M_T applied to (cT - lim)
+    T d[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = cT[i] - lim[i];
+    T cor[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T s = T(0), dii = T(1);
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const int a = i < j ? i : j, b = i < j ? j : i;
+        const int idx = a * N - a * (a - 1) / 2 + (b - a);
+        const T m = srow<T>(smem, rM + idx)[t];
+        s += m * d[j];
+        if (j == i) dii = m;
+      }
+      cor[i] = lim[i] + s / dii;
+    }
+    T cdot[N];
+    from_taylor<T, P>(cor, af, cdot);
+    const T w = T(sc.omega), tau = T(sc.tau);
+    T cnew[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      cnew[i] = w * srow<T>(smem, rC0 + i)[t] + (T(1) - w) * (srow<T>(smem, rC + i)[t] + tau * cdot[i]);
+    T cT2[N];
+    to_taylor<T, P>(cnew, af, cT2);
+#pragma unroll
+    for (int i = 0; i < N; ++i) { tbuf[(size_t)i * Kp + k] = cT2[i]; bad |= !finite_(cT2[i]); }
+    centroid_quantities<T, P>(cT2, lo.type, qv);
+  }
+  scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok);
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Solution limiter: limited Taylor coefficients back to the modal basis
+// (core/applySlopeLimiterDisc.m:77-86).
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const LimIn<T> li,
+        const StageScalars sc) {
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
+  constexpr int NT = StageRows<T, P>::lim();
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  pdl_trigger();
+  if (k0 >= g.K) { pdl_wait(); return; }
+  const int Kp = g.Kp;
+  if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+  __syncthreads();
+  if (t == 0) {
+    stage_expect<T>(bar, NT, 1);
+    stage_T(smem, N, g.Bm, 4, Kp, k0, bar);
+    stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+  }
+  const bool active = k < g.K;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  if (t == 0) stage_T(smem, 0, tbuf, N, Kp, k0, bar);
+  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
+  T data[3] = {T(0), T(0), T(0)};
+  if (g.cDV0T && active) {
+    for (int m = 0; m < g.nTerms; ++m) {
+      const T gm = T(sc.gco[m]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
+    }
+  }
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  if (!active || !ok) return;
+  const Affine<T> af = affine_from<T>(srow<T>(smem, N)[t], srow<T>(smem, N + 1)[t],
+                                      srow<T>(smem, N + 2)[t], srow<T>(smem, N + 3)[t]);
+  T cT[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) cT[i] = srow<T>(smem, i)[t];
+  const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
+  limit_taylor<T, P, NQ>(li, kv, sh, af, dmask, data, cT);
+  T c[N];
+  from_taylor<T, P>(cT, af, c);
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = c[i]; bad |= !finite_(c[i]); }
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Modal state -> Taylor form and scatter of its centroid quantities (initial limiting).
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_to_taylor(const Geo<T> g, const T *__restrict__ c, T *__restrict__ tbuf, const LimOut<T> lo,
+            const StageScalars sc) {
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
+  constexpr int NT = StageRows<T, P>::totaylor();
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 0));
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  pdl_trigger();
+  const int Kp = g.Kp;
+  const bool staged = k0 < g.K;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) { stage_expect<T>(bar, NT, 0); stage_T(smem, N, g.Bm, 4, Kp, k0, bar); }
+  }
+  const bool active = k < g.K;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) stage_T(smem, 0, c, N, Kp, k0, bar);
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T qv[NQ];
+  if (active && ok) {
+    const Affine<T> af = affine_from<T>(srow<T>(smem, N)[t], srow<T>(smem, N + 1)[t],
+                                        srow<T>(smem, N + 2)[t], srow<T>(smem, N + 3)[t]);
+    T cc[N], cT[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cc[i] = srow<T>(smem, i)[t];
+    to_taylor<T, P>(cc, af, cT);
+#pragma unroll
+    for (int i = 0; i < N; ++i) tbuf[(size_t)i * Kp + k] = cT[i];
+    centroid_quantities<T, P>(cT, lo.type, qv);
+  }
+  scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok);
+}
+
+// Time-derivative limiting and SSP update for the linear limiter: cDot += Q_k du with the
+// precomputed Q_k = DM^-1 (S_k^-1 Mcorr_k S_k - I) (advection/solveSubStep.m:69-83); the new
+// stage value is written in the modal basis and its mean scattered for the solution limiter.
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit_dot_lin(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, const T *__restrict__ tbuf,
+                T *__restrict__ out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
+  constexpr int N = Dims<P>::N, NQ = 1;
+  constexpr int NT = StageRows<T, P>::limdot_lin();
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  pdl_trigger();
+  const int Kp = g.Kp;
+  const bool staged = k0 < g.K;
+  constexpr int rD = 0, rQ = N, rC0 = N + N * (N - 1), rC = rC0 + N;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) {
+      stage_expect<T>(bar, NT, 1);
+      stage_T(smem, rQ, g.MT, N * (N - 1), Kp, k0, bar);
+      stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+    }
+  }
+  const bool active = k < g.K;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) {
+    stage_T(smem, rD, (const T *)tbuf, N, Kp, k0, bar);
+    stage_T(smem, rC0, c0, N, Kp, k0, bar);
+    stage_T(smem, rC, cin, N, Kp, k0, bar);
+  }
+  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T q0 = T(0);
+  bool bad = false;
+  if (active && ok) {
+    T cd[N], u[N], du[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cd[i] = srow<T>(smem, rD + i)[t];
+    lin_u<T, P>(cd, u);
+    const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
+    const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
+    if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, nan3, du)) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int j = 1; j < N; ++j) s += srow<T>(smem, rQ + i * (N - 1) + (j - 1))[t] * du[j];
+        cd[i] += s;
+      }
+    }
+    const T w = T(sc.omega), tau = T(sc.tau);
+    T cnew[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      cnew[i] = w * srow<T>(smem, rC0 + i)[t] + (T(1) - w) * (srow<T>(smem, rC + i)[t] + tau * cd[i]);
+#pragma unroll
+    for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+    q0 = lin_mean<T, P>(cnew);
+  }
+  scatter_quantities<T, NQ>(g, lo, &q0, vid, active && ok);
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Solution limiter for the linear limiter (core/applySlopeLimiterDisc.m:77-86 without the
+// Taylor round trip): c <- c - DM^-1 du.
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit_lin(const Geo<T> g, const T *__restrict__ cbuf, T *__restrict__ out, const LimIn<T> li,
+            const StageScalars sc) {
+  constexpr int N = Dims<P>::N, NQ = 1;
+  const Tab<T, P> &tb = tab<T, P>();
+  __shared__ T sh[2];
+  const int t = threadIdx.x, k = blockIdx.x * kBlock + t;
+  pdl_trigger();
+  const bool active = k < g.K;
+  const int Kp = g.Kp;
+  int vid[3] = {0, 0, 0}, dmask = 0;
+  if (active) {
+    vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
+    dmask = (g.code[k] >> 9) & 7;
+  }
+  T data[3] = {T(0), T(0), T(0)};
+  if (g.cDV0T && active) {
+    for (int m = 0; m < g.nTerms; ++m) {
+      const T gm = T(sc.gco[m]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
+    }
+  }
+  pdl_wait();
+  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  T c[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) c[i] = active ? cbuf[(size_t)i * Kp + k] : T(0);
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
+  if (!active) return;
+  T u[N], du[N];
+  lin_u<T, P>(c, u);
+  if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, data, du)) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T s = T(0);
+#pragma unroll
+      for (int j = 1; j < N; ++j) s += tb.DMinv[i][j] * du[j];
+      c[i] -= s;
+    }
+  }
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = c[i]; bad |= !finite_(c[i]); }
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// Mean of the modal state scattered to the vertices (initial limiting, linear limiter).
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_mean_lin(const Geo<T> g, const T *__restrict__ c, const LimOut<T> lo) {
+  constexpr int N = Dims<P>::N;
+  const int t = threadIdx.x, k = blockIdx.x * kBlock + t;
+  pdl_trigger();
+  const bool active = k < g.K;
+  const int Kp = g.Kp;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  T q0 = T(0);
+  if (active) {
+    T cc[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cc[i] = c[(size_t)i * Kp + k];
+    q0 = lin_mean<T, P>(cc);
+  }
+  scatter_quantities<T, 1>(g, lo, &q0, vid, active);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Stage operator fused with the previous pass's solution limiter (linear limiter, zero
+// Dirichlet data).  The input x is the unlimited stage value (limitIn = 1), or, in the first
+// stage of a call, the limited state itself (limitIn = 0).  Each element limits
+// its own coefficients and those of the three neighbours it gathers for the flux, each with its
+// own vertex patches (core/applySlopeLimiterDisc.m:77-86 applied where the value is used instead
+// of in a separate pass), then
+//   MODE 1: writes the new unlimited stage value (SSP update, advection/solveSubStep.m:83),
+//   MODE 2: writes cDot for the time-derivative limiter,
+// and scatters the mean of what it wrote for the next limiter pass.  xLout receives the limited
+// own input where later kernels need it (the limited c^n, or c^(s-1) for the SSP update).
+template <typename T, int P>
+__device__ __forceinline__ void lin_limit_inplace(const LimIn<T> &li, const VKeys<T, 1> &kv, const T *sh,
+                                                  int dmask, T *c) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T u[N], du[N];
+  lin_u<T, P>(c, u);
+  const T zero3[3] = {T(0), T(0), T(0)};
+  if (lin_alpha<T, P, 1>(li, kv, sh, u, dmask, zero3, du)) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T s = T(0);
+#pragma unroll
+      for (int j = 1; j < N; ++j) s += tb.DMinv[i][j] * du[j];
+      c[i] -= s;
+    }
+  }
+}
+
+template <typename T, int P, int MODE, bool RHS>
+__global__ void __launch_bounds__(kBlock)
+k_op_fused(const Geo<T> g, const T *__restrict__ x, int limitIn, T *__restrict__ xLout,
+           const T *__restrict__ c0L, int firstStage, T *__restrict__ out, const LimIn<T> li,
+           const LimOut<T> lo, const StageScalars sc) {
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
+  constexpr int NT = StageRows<T, P>::op(MODE, true);
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  const Tab<T, P> &tb = tab<T, P>();
+  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  pdl_trigger();
+  const int Kp = g.Kp;
+  const bool staged = k0 < g.K;
+  constexpr int rC = 0, rC0 = N, rF = (MODE != 2) ? 2 * N : N, rV = rF + 2 * Q;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+    __syncthreads();
+    if (t == 0) {
+      stage_expect<T>(bar, NT - ((MODE == 1 && firstStage) ? N : 0), 1);
+      stage_T(smem, rF, g.F, 2 * Q, Kp, k0, bar);
+      stage_T(smem, rV, g.Vn, 3 * R, Kp, k0, bar);
+      stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+    }
+  }
+  const bool active = k < g.K;
+  // static connectivity before the dependency wait: neighbours, their boundary bits and the
+  // vertex of each neighbour opposite the shared edge
+  int nb[3], nbc[3], v3[3];
+  int vid[3] = {0, 0, 0};
+  const int myCode = active ? g.code[k] : 0;
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    nb[n] = active ? g.nbr[(size_t)n * Kp + k] : -1;
+    const int np = (myCode >> (2 * n)) & 3;
+    nbc[n] = nb[n] >= 0 ? g.code[nb[n]] : 0;
+    v3[n] = nb[n] >= 0 ? g.V0T[(size_t)np * Kp + nb[n]] : 0;
+  }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  if (!staged) return;
+  if (t == 0) {
+    stage_T(smem, rC, x, N, Kp, k0, bar);
+    if (MODE == 1 && !firstStage) stage_T(smem, rC0, c0L, N, Kp, k0, bar);
+  }
+  // neighbour coefficients: outside the block from global memory now, inside from shared later
+  T cn[3][N];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const bool outside = nb[n] >= 0 && (nb[n] < k0 || nb[n] >= k0 + kBlock);
+#pragma unroll
+    for (int j = 0; j < N; ++j) cn[n][j] = outside ? x[(size_t)j * Kp + nb[n]] : T(0);
+  }
+  // vertex keys of the own element and of each neighbour (two vertices shared with the edge)
+  VKeys<T, 1> kvOwn, kvNb[3];
+  load_vkeys<T, 1>(g, li, vid, kvOwn);
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const int np = (myCode >> (2 * n)) & 3;
+    const typename KeyOf<T>::type k3min = li.vkeys[v3[n]], k3max = li.vkeys[(size_t)g.Vp + v3[n]];
+    // neighbour's local vertex np is opposite the shared edge; np+1 is our n+2, np+2 our n+1
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const int mm = (m + 3 - np) % 3;
+      const int ours = mm == 1 ? (n + 2) % 3 : (n + 1) % 3;
+      kvNb[n].v[0][0][m] = mm == 0 ? k3min : kvOwn.v[0][0][ours];
+      kvNb[n].v[0][1][m] = mm == 0 ? k3max : kvOwn.v[0][1][ours];
+    }
+  }
+  if (li.shift && limitIn) load_shifts<T>(li.slots, li.nc, sh);
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(bar, sc.flag);
+  T q0 = T(0);
+  bool bad = false;
+  if (active && ok) {
+    T c[N], rhs[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = T(0); }
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      if (nb[n] >= k0 && nb[n] < k0 + kBlock)
+#pragma unroll
+        for (int j = 0; j < N; ++j) cn[n][j] = srow<T>(smem, rC + j)[nb[n] - k0];
+    if (limitIn) {
+      lin_limit_inplace<T, P>(li, kvOwn, sh, (myCode >> 9) & 7, c);
+#pragma unroll
+      for (int n = 0; n < 3; ++n)
+        if (nb[n] >= 0) lin_limit_inplace<T, P>(li, kvNb[n], sh, (nbc[n] >> 9) & 7, cn[n]);
+    }
+    if (xLout) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) xLout[(size_t)i * Kp + k] = c[i];
+    }
+    if (RHS) {
+      for (int m = 0; m < g.nTerms; ++m) {
+        const T gm = T(sc.gco[m]);
+#pragma unroll
+        for (int i = 0; i < N; ++i) rhs[i] += gm * g.rhs[((size_t)m * N + i) * Kp + k];
+      }
+    }
+#pragma unroll
+    for (int qq = 0; qq < Q; ++qq) {
+      T cq = T(0);
+#pragma unroll
+      for (int j = 0; j < N; ++j) cq += tb.phiQ[qq][j] * c[j];
+      const T f1 = srow<T>(smem, rF + qq)[t] * cq;
+      const T f2 = srow<T>(smem, rF + Q + qq)[t] * cq;
+#pragma unroll
+      for (int i = 0; i < N; ++i) rhs[i] += tb.g1[qq][i] * f1 + tb.g2[qq][i] * f2;
+    }
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      const int np = (myCode >> (2 * n)) & 3;
+      const bool outOk = (myCode >> (6 + n)) & 1;
+#pragma unroll
+      for (int r2 = 0; r2 < R; ++r2) {
+        const T v = srow<T>(smem, rV + n * R + r2)[t];
+        T tr = T(0);
+        if (v > T(0) && outOk) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r2][j] * c[j];
+        } else if (v < T(0) && nb[n] >= 0) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r2][j] * cn[n][j];
+        }
+        const T fl = v * tr;
+#pragma unroll
+        for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r2][i] * fl;
+      }
+    }
+    T cdot[N];
+    if (sizeof(T) == 8) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int j = 0; j < N; ++j) s += tb.hatMinv[i][j] * rhs[j];
+        cdot[i] = s;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) cdot[i] = rhs[i];
+    }
+    if (MODE == 2) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cdot[i]; bad |= !finite_(cdot[i]); }
+      q0 = lin_mean<T, P>(cdot);
+    } else {
+      const T w = T(sc.omega), tau = T(sc.tau);
+      T cnew[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const T c0v = firstStage ? c[i] : srow<T>(smem, rC0 + i)[t];
+        cnew[i] = w * c0v + (T(1) - w) * (c[i] + tau * cdot[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
+      q0 = lin_mean<T, P>(cnew);
+    }
+  }
+  scatter_quantities<T, 1>(g, lo, &q0, vid, active && ok);
+  if (bad) atomicOr(sc.flag, 1);
+}
+
+// External (caller order, K x N column-major, FP64) <-> internal (SoA, stride Kp, precision T).
+template <typename T>
+__global__ void k_scatter_in(int K, int Kp, int N, const int *__restrict__ perm,
+                             const double *__restrict__ ext, T *__restrict__ c) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  const int e = perm[k];
+  for (int i = 0; i < N; ++i) c[(size_t)i * Kp + k] = T(ext[(size_t)i * K + e]);
+}
+template <typename T>
+__global__ void k_gather_out(int K, int Kp, int N, const int *__restrict__ perm,
+                             const T *__restrict__ c, double *__restrict__ ext) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  const int e = perm[k];
+  for (int i = 0; i < N; ++i) ext[(size_t)i * K + e] = double(c[(size_t)i * Kp + k]);
+}
+
+}  // namespace dgadv

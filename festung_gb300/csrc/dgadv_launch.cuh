@@ -1,0 +1,409 @@
+// Host-side launch sequences of the stage pipeline, templated on the stored real type.
+// Included by each dgadv_prec_*.cu after dgadv_device.cuh.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <string>
+
+#include "dgadv_device.cuh"
+
+namespace dgadv {
+
+template <typename T, int P>
+static cudaError_t upload_tables(const RefTables &rt) {
+  Tab<T, P> t;
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
+  for (int q = 0; q < Q; ++q)
+    for (int i = 0; i < N; ++i) {
+      t.phiQ[q][i] = T(rt.phiQ[q * N + i]);
+      t.g1[q][i] = T(rt.gradQ[q * N + i]);
+      t.g2[q][i] = T(rt.gradQ[Q * N + q * N + i]);
+    }
+  for (int n = 0; n < 3; ++n)
+    for (int r = 0; r < R; ++r)
+      for (int i = 0; i < N; ++i) t.phi1D[n][r][i] = T(rt.phi1D[(n * R + r) * N + i]);
+  for (int nn = 0; nn < 3; ++nn)
+    for (int np = 0; np < 3; ++np)
+      for (int r = 0; r < R; ++r)
+        for (int i = 0; i < N; ++i) t.thetaPhi[nn][np][r][i] = T(rt.thetaPhi[((nn * 3 + np) * R + r) * N + i]);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      t.hatMinv[i][j] = T(rt.hatMinv[i * N + j]);
+      t.DM[i][j] = T(rt.DM[i * N + j]);
+      t.DMinv[i][j] = T(rt.DMinv[i * N + j]);
+    }
+  return cudaMemcpyToSymbol(tab_symbol<T, P>(), &t, sizeof(t));
+}
+
+template <typename T>
+static Geo<T> make_geo(const dgadv_handle *h) {
+  Geo<T> g;
+  g.K = h->K; g.Kp = h->Kp; g.numV = h->numV; g.Vp = h->Vp;
+  g.F = (const T *)h->F; g.Vn = (const T *)h->Vn; g.nbr = h->nbr; g.code = h->code;
+  g.Bm = (const T *)h->Bm; g.MT = (const T *)h->MT; g.V0T = h->V0T; g.vptr = h->vptr; g.vidx = h->vidx;
+  g.rhs = (const T *)h->rhs; g.cDV0T = (const T *)h->cDV0T; g.nTerms = h->nTerms;
+  for (int i = 0; i < 4; ++i) g.timeFn[i] = h->timeFn[i];
+  return g;
+}
+
+static double time_factor(int fn, double t) { return fn == DGADV_TIME_EXP_NEG ? std::exp(-t) : 1.0; }
+
+// SSP-RK tables (core/rungeKuttaExplicit.m:64-78)
+static int rk_table(int ord, double omega[3], double cstage[3]) {
+  if (ord == 1) { omega[0] = 0; cstage[0] = 0; return 1; }
+  if (ord == 2) { omega[0] = 0; omega[1] = 0.5; cstage[0] = 0; cstage[1] = 1; return 2; }
+  omega[0] = 0; omega[1] = 3.0 / 4.0; omega[2] = 1.0 / 3.0;
+  cstage[0] = 0; cstage[1] = 1; cstage[2] = 0.5;
+  return 3;
+}
+
+template <typename T>
+static LimOut<T> lim_out(dgadv_handle *h) {
+  using K_ = typename KeyOf<T>::type;
+  const int set = (int)(h->limPass % 3), next = (set + 1) % 3;
+  const size_t vset = (size_t)2 * h->nc * h->Vp;
+  LimOut<T> o;
+  o.vkeys = (K_ *)h->vkeys + set * vset;
+  o.vreset = (K_ *)h->vkeys + next * vset;
+  o.slots = h->gmm + (size_t)set * kSlotCopies * 2 * h->nc;
+  o.reset = h->gmm + (size_t)next * kSlotCopies * 2 * h->nc;
+  o.nc = h->nc; o.type = h->limType;
+  return o;
+}
+template <typename T>
+static LimIn<T> lim_in_pass(const dgadv_handle *h, long long pass) {
+  using K_ = typename KeyOf<T>::type;
+  const int set = (int)(((pass % 3) + 3) % 3);
+  LimIn<T> i;
+  i.vkeys = (const K_ *)h->vkeys + (size_t)set * 2 * h->nc * h->Vp;
+  i.slots = h->gmm + (size_t)set * kSlotCopies * 2 * h->nc;
+  i.nc = h->nc; i.type = h->limType;
+  i.shift = (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1;
+  return i;
+}
+
+template <typename T>
+static LimIn<T> lim_in(const LimOut<T> &o, const dgadv_handle *h) {
+  LimIn<T> i;
+  i.vkeys = o.vkeys; i.slots = o.slots; i.nc = o.nc; i.type = o.type;
+  i.shift = (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1;
+  return i;
+}
+
+// Optional per-kernel timing with CUDA events on the handle's stream (dgadv_profile_kernels).
+static void prof_mark(dgadv_handle *h, int kind) {
+  if (!h->profiling) return;
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, h->stream);
+  h->profEvents.push_back(e);
+  h->profKinds.push_back(kind);
+}
+
+// Kernel launch on the handle's stream, with programmatic dependent launch unless disabled.
+template <typename... KArgs, typename... Args>
+static void launch_k(const dgadv_handle *h, void (*kern)(KArgs...), int grid, size_t smem, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = (h->flags & DGADV_FLAG_NO_PDL) ? 0 : 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+// Opt-in shared memory sizes of the staged kernels of one (precision, degree).
+template <typename T, int P, bool FUSED>
+static cudaError_t set_smem_attributes() {
+  using SR = StageRows<T, P>;
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void *f, size_t b) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b);
+  };
+  set((const void *)k_stage_op<T, P, 0, true, false>, SR::bytes(SR::op(0, false), 1));
+  set((const void *)k_stage_op<T, P, 0, false, false>, SR::bytes(SR::op(0, false), 1));
+  set((const void *)k_stage_op<T, P, 1, true, false>, SR::bytes(SR::op(1, false), 1));
+  set((const void *)k_stage_op<T, P, 1, false, false>, SR::bytes(SR::op(1, false), 1));
+  set((const void *)k_stage_op<T, P, 2, true, false>, SR::bytes(SR::op(2, false), 1));
+  set((const void *)k_stage_op<T, P, 2, false, false>, SR::bytes(SR::op(2, false), 1));
+  set((const void *)k_stage_op<T, P, 1, true, true>, SR::bytes(SR::op(1, true), 1));
+  set((const void *)k_stage_op<T, P, 1, false, true>, SR::bytes(SR::op(1, true), 1));
+  set((const void *)k_stage_op<T, P, 2, true, true>, SR::bytes(SR::op(2, true), 1));
+  set((const void *)k_stage_op<T, P, 2, false, true>, SR::bytes(SR::op(2, true), 1));
+  set((const void *)k_limit_dot_lin<T, P>, SR::bytes(SR::limdot_lin(), 1));
+  if constexpr (FUSED) {
+    set((const void *)k_op_fused<T, P, 1, true>, SR::bytes(SR::op(1, true), 1));
+    set((const void *)k_op_fused<T, P, 1, false>, SR::bytes(SR::op(1, true), 1));
+    set((const void *)k_op_fused<T, P, 2, true>, SR::bytes(SR::op(2, true), 1));
+    set((const void *)k_op_fused<T, P, 2, false>, SR::bytes(SR::op(2, true), 1));
+  }
+  set((const void *)k_limit_dot<T, P>, SR::bytes(SR::limdot(), 1));
+  set((const void *)k_limit<T, P>, SR::bytes(SR::lim(), 1));
+  set((const void *)k_to_taylor<T, P>, SR::bytes(SR::totaylor(), 0));
+  return e;
+}
+
+template <typename T, int P>
+static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
+  using SR = StageRows<T, P>;
+  const Geo<T> g = make_geo<T>(h);
+  const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;   // producers also reset vertex keys
+  const int gridK = (h->K + kBlock - 1) / kBlock;
+  double omega[3], cst[3];
+  const int S = rk_table(h->ordRK, omega, cst);
+  T *cn = (T *)h->cn, *cA = (T *)h->cA, *cB = (T *)h->cB, *tb = (T *)h->tbuf;
+  const bool rhs = h->nTerms > 0 && h->rhs;
+  for (int s = 0; s < S; ++s) {
+    T *in = (s == 0) ? cn : (s == 1 ? cA : cB);
+    T *out = (s == S - 1) ? (S == 1 ? cA : cn) : (s == 0 ? cA : cB);
+    StageScalars sc{};
+    sc.omega = omega[s]; sc.tau = tau; sc.flag = h->flag;
+    const double ts = t0 + cst[s] * tau;
+    for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = time_factor(h->timeFn[m], ts);
+    LimOut<T> lo{};
+    if (!h->lim) {
+      prof_mark(h, 0);
+      if (rhs) launch_k(h, k_stage_op<T, P, 0, true, false>, grid, SR::bytes(SR::op(0, false), 1), g, in, cn, out, lo, sc);
+      else launch_k(h, k_stage_op<T, P, 0, false, false>, grid, SR::bytes(SR::op(0, false), 1), g, in, cn, out, lo, sc);
+      prof_mark(h, -1);
+      continue;
+    }
+    // limiter boundary data at tBC = t(s+1) or t(1) + tau (advection/solveSubStep.m:88)
+    const double tBC = (s + 1 < S) ? t0 + cst[s + 1] * tau : t0 + tau;
+    StageScalars scBC = sc;
+    for (int m = 0; m < h->nTerms; ++m) scBC.gco[m] = time_factor(h->timeFn[m], tBC);
+    const bool lin = h->limType == DGADV_LIM_LINEAR;
+    const LimOut<T> lo1 = lim_out<T>(h);
+    ++h->limPass;
+    const int mode = h->limdot ? 2 : 1;
+    prof_mark(h, 0);
+    if (mode == 2) {
+      if (lin) {
+        if (rhs) launch_k(h, k_stage_op<T, P, 2, true, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, tb, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 2, false, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, tb, lo1, sc);
+      } else {
+        if (rhs) launch_k(h, k_stage_op<T, P, 2, true, false>, grid, SR::bytes(SR::op(2, false), 1), g, in, cn, tb, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 2, false, false>, grid, SR::bytes(SR::op(2, false), 1), g, in, cn, tb, lo1, sc);
+      }
+    } else {
+      if (lin) {
+        if (rhs) launch_k(h, k_stage_op<T, P, 1, true, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, tb, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 1, false, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, tb, lo1, sc);
+      } else {
+        if (rhs) launch_k(h, k_stage_op<T, P, 1, true, false>, grid, SR::bytes(SR::op(1, false), 1), g, in, cn, tb, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 1, false, false>, grid, SR::bytes(SR::op(1, false), 1), g, in, cn, tb, lo1, sc);
+      }
+    }
+    prof_mark(h, -1);
+    LimOut<T> loS = lo1;
+    if (mode == 2) {
+      const LimOut<T> lo2 = lim_out<T>(h);
+      ++h->limPass;
+      prof_mark(h, 1);
+      if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)in, (const T *)cn, (const T *)tb, tb, lim_in<T>(lo1, h), lo2, sc);
+      else launch_k(h, k_limit_dot<T, P>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
+      prof_mark(h, -1);
+      loS = lo2;
+    }
+    prof_mark(h, 2);
+    if (lin) launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
+    else launch_k(h, k_limit<T, P>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
+    prof_mark(h, -1);
+  }
+  if (S == 1)
+    cudaMemcpyAsync(cn, cA, (size_t)h->N * h->Kp * sizeof(T), cudaMemcpyDeviceToDevice, h->stream);
+  return cudaGetLastError();
+}
+
+// Fused path (linear limiter, zero Dirichlet data): per stage the operator kernel limits its
+// input on the fly; for p >= 2 the time-derivative limiter follows.  The state between calls
+// stays limited in cn; inside a call the step output R is unlimited, and finalize_fused limits
+// it back into cn at the end of the call.
+
+template <typename T, int P>
+static cudaError_t launch_step_fused(dgadv_handle *h, double t0, double tau, bool firstOfCall) {
+  using SR = StageRows<T, P>;
+  const Geo<T> g = make_geo<T>(h);
+  const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
+  double omega[3], cst[3];
+  const int S = rk_table(h->ordRK, omega, cst);
+  T *cn = (T *)h->cn, *R = (T *)h->cR, *rA = (T *)h->cA, *rB = (T *)h->cB;
+  T *cnL = (T *)h->cnL, *Lx = (T *)h->cLx, *tb = (T *)h->tbuf;
+  const bool rhs = h->nTerms > 0 && h->rhs;
+  for (int s = 0; s < S; ++s) {
+    const T *x = (s == 0) ? (firstOfCall ? cn : R) : (s == 1 ? rA : rB);
+    const int limitIn = (firstOfCall && s == 0) ? 0 : 1;
+    T *outRaw = (s == S - 1) ? R : (s == 0 ? rA : rB);
+    StageScalars sc{};
+    sc.omega = omega[s]; sc.tau = tau; sc.flag = h->flag;
+    const double ts = t0 + cst[s] * tau;
+    for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = time_factor(h->timeFn[m], ts);
+    const LimIn<T> li = lim_in_pass<T>(h, h->limPass - 1);
+    const LimOut<T> lo1 = lim_out<T>(h);
+    ++h->limPass;
+    prof_mark(h, 0);
+    if (!h->limdot) {
+      if (rhs) launch_k(h, k_op_fused<T, P, 1, true>, grid, SR::bytes(SR::op(1, true), 1), g, x, limitIn,
+                        s == 0 ? cnL : (T *)nullptr, (const T *)cnL, s == 0 ? 1 : 0, outRaw, li, lo1, sc);
+      else launch_k(h, k_op_fused<T, P, 1, false>, grid, SR::bytes(SR::op(1, true), 1), g, x, limitIn,
+                    s == 0 ? cnL : (T *)nullptr, (const T *)cnL, s == 0 ? 1 : 0, outRaw, li, lo1, sc);
+      prof_mark(h, -1);
+      continue;
+    }
+    T *xL = (s == 0) ? cnL : Lx;
+    if (rhs) launch_k(h, k_op_fused<T, P, 2, true>, grid, SR::bytes(SR::op(2, true), 1), g, x, limitIn, xL,
+                      (const T *)nullptr, s == 0 ? 1 : 0, tb, li, lo1, sc);
+    else launch_k(h, k_op_fused<T, P, 2, false>, grid, SR::bytes(SR::op(2, true), 1), g, x, limitIn, xL,
+                  (const T *)nullptr, s == 0 ? 1 : 0, tb, li, lo1, sc);
+    prof_mark(h, -1);
+    const LimOut<T> lo2 = lim_out<T>(h);
+    ++h->limPass;
+    prof_mark(h, 1);
+    launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)xL, (const T *)cnL,
+             (const T *)tb, outRaw, lim_in<T>(lo1, h), lo2, sc);
+    prof_mark(h, -1);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T, int P>
+static cudaError_t launch_finalize_fused(dgadv_handle *h) {
+  const Geo<T> g = make_geo<T>(h);
+  const int gridK = (h->K + kBlock - 1) / kBlock;
+  StageScalars sc{};
+  sc.flag = h->flag;
+  prof_mark(h, 2);
+  launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)h->cR, (T *)h->cn,
+           lim_in_pass<T>(h, h->limPass - 1), sc);
+  prof_mark(h, -1);
+  return cudaGetLastError();
+}
+
+template <typename T, int P>
+static cudaError_t launch_limit_state(dgadv_handle *h, double t) {
+  using SR = StageRows<T, P>;
+  const Geo<T> g = make_geo<T>(h);
+  const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;   // producers also reset vertex keys
+  StageScalars sc{};
+  sc.flag = h->flag;
+  for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = time_factor(h->timeFn[m], t);
+  const LimOut<T> lo = lim_out<T>(h);
+  ++h->limPass;
+  if (h->limType == DGADV_LIM_LINEAR) {
+    const int gridK = (h->K + kBlock - 1) / kBlock;
+    launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)h->cn, lo);
+    launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)h->cn, (T *)h->cn, lim_in<T>(lo, h), sc);
+  } else {
+    launch_k(h, k_to_taylor<T, P>, grid, SR::bytes(SR::totaylor(), 0), g, (const T *)h->cn, (T *)h->tbuf, lo, sc);
+    launch_k(h, k_limit<T, P>, grid, SR::bytes(SR::lim(), 1), g, (const T *)h->tbuf, (T *)h->cn, lim_in<T>(lo, h), sc);
+  }
+  return cudaGetLastError();
+}
+
+// Dispatch on the degree over the degrees a unit instantiates: bit P of MASK set for degree P.
+// FUSED = false leaves the opt-in fused kernels out of a unit.
+template <typename T, int MASK>
+static cudaError_t dispatch_step(dgadv_handle *h, double t0, double tau) {
+  switch (h->p) {
+    case 0: if constexpr ((MASK & 1) != 0) return launch_step<T, 0>(h, t0, tau); break;
+    case 1: if constexpr ((MASK & 2) != 0) return launch_step<T, 1>(h, t0, tau); break;
+    case 2: if constexpr ((MASK & 4) != 0) return launch_step<T, 2>(h, t0, tau); break;
+    case 3: if constexpr ((MASK & 8) != 0) return launch_step<T, 3>(h, t0, tau); break;
+  }
+  return cudaErrorNotSupported;
+}
+template <typename T, int MASK, bool FUSED>
+static cudaError_t dispatch_step_fused(dgadv_handle *h, double t0, double tau, bool first) {
+  if constexpr (FUSED) {
+    switch (h->p) {
+      case 1: if constexpr ((MASK & 2) != 0) return launch_step_fused<T, 1>(h, t0, tau, first); break;
+      case 2: if constexpr ((MASK & 4) != 0) return launch_step_fused<T, 2>(h, t0, tau, first); break;
+      case 3: if constexpr ((MASK & 8) != 0) return launch_step_fused<T, 3>(h, t0, tau, first); break;
+    }
+  }
+  return cudaErrorNotSupported;
+}
+template <typename T, int MASK, bool FUSED>
+static cudaError_t dispatch_finalize_fused(dgadv_handle *h) {
+  if constexpr (FUSED) {
+    switch (h->p) {
+      case 1: if constexpr ((MASK & 2) != 0) return launch_finalize_fused<T, 1>(h); break;
+      case 2: if constexpr ((MASK & 4) != 0) return launch_finalize_fused<T, 2>(h); break;
+      case 3: if constexpr ((MASK & 8) != 0) return launch_finalize_fused<T, 3>(h); break;
+    }
+  }
+  return cudaErrorNotSupported;
+}
+template <typename T, int MASK>
+static cudaError_t dispatch_limit(dgadv_handle *h, double t) {
+  switch (h->p) {
+    case 1: if constexpr ((MASK & 2) != 0) return launch_limit_state<T, 1>(h, t); break;
+    case 2: if constexpr ((MASK & 4) != 0) return launch_limit_state<T, 2>(h, t); break;
+    case 3: if constexpr ((MASK & 8) != 0) return launch_limit_state<T, 3>(h, t); break;
+  }
+  return cudaErrorNotSupported;
+}
+
+template <typename T>
+static cudaError_t scatter_in(dgadv_handle *h) {
+  const int grid = (h->K + 255) / 256;
+  k_scatter_in<T><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, h->stage_ext, (T *)h->cn);
+  return cudaGetLastError();
+}
+template <typename T>
+static cudaError_t gather_out(dgadv_handle *h) {
+  const int grid = (h->K + 255) / 256;
+  k_gather_out<T><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, (const T *)h->cn, h->stage_ext);
+  return cudaGetLastError();
+}
+
+template <typename T, int MASK>
+static cudaError_t upload_tables_p(int p, const RefTables &rt) {
+  switch (p) {
+    case 0: if constexpr ((MASK & 1) != 0) return upload_tables<T, 0>(rt); break;
+    case 1: if constexpr ((MASK & 2) != 0) return upload_tables<T, 1>(rt); break;
+    case 2: if constexpr ((MASK & 4) != 0) return upload_tables<T, 2>(rt); break;
+    case 3: if constexpr ((MASK & 8) != 0) return upload_tables<T, 3>(rt); break;
+  }
+  return cudaErrorNotSupported;
+}
+template <typename T, int MASK, bool FUSED>
+static cudaError_t set_smem_p(int p) {
+  switch (p) {
+    case 0: if constexpr ((MASK & 1) != 0) return set_smem_attributes<T, 0, FUSED>(); break;
+    case 1: if constexpr ((MASK & 2) != 0) return set_smem_attributes<T, 1, FUSED>(); break;
+    case 2: if constexpr ((MASK & 4) != 0) return set_smem_attributes<T, 2, FUSED>(); break;
+    case 3: if constexpr ((MASK & 8) != 0) return set_smem_attributes<T, 3, FUSED>(); break;
+  }
+  return cudaErrorNotSupported;
+}
+template <typename T>
+static void to_real(const double *src, size_t n, void *dst) {
+  T *d = (T *)dst;
+  for (size_t i = 0; i < n; ++i) d[i] = T(src[i]);
+}
+
+template <typename T, int MASK, bool FUSED>
+static PrecOps make_ops() {
+  PrecOps o;
+  o.realBytes = sizeof(T);
+  o.keyBytes = sizeof(typename KeyOf<T>::type);
+  o.slotKeyMax = key_max<T>();
+  o.fused = FUSED;
+  o.to_real = to_real<T>;
+  o.upload_tables = upload_tables_p<T, MASK>;
+  o.set_smem = set_smem_p<T, MASK, FUSED>;
+  o.step = dispatch_step<T, MASK>;
+  o.step_fused = dispatch_step_fused<T, MASK, FUSED>;
+  o.finalize_fused = dispatch_finalize_fused<T, MASK, FUSED>;
+  o.limit = dispatch_limit<T, MASK>;
+  o.scatter_in = scatter_in<T>;
+  o.gather_out = gather_out<T>;
+  return o;
+}
+
+}  // namespace dgadv

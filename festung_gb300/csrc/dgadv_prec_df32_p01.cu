@@ -1,0 +1,17 @@
+// Kernels and launch sequences of the double-float path (stored reals: df32), degrees 0 and 1.
+// The df32 kernels are large (every operation expands to several FP32 instructions), so each
+// degree compiles in a unit of its own; the opt-in fused kernels are not built for df32.
+#include "dgadv_device.cuh"
+
+namespace dgadv {
+DGADV_DEFINE_TABLES(df32, cTw)
+}  // namespace dgadv
+
+#include "dgadv_launch.cuh"
+
+namespace dgadv {
+const PrecOps &ops_df32_p01() {
+  static const PrecOps ops = make_ops<df32, 0x3, false>();
+  return ops;
+}
+}  // namespace dgadv

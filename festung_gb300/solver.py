@@ -38,7 +38,7 @@ class DeviceSolver:
                 setattr(mesh, name, L.ptr(a, L._u8p))
         prm = L.Params()
         prm.p = p; prm.ordRK = ordRK
-        prm.precision = {'fp64': L.FP64, 'fp32': L.FP32}[precision]
+        prm.precision = {'fp64': L.FP64, 'fp32': L.FP32, 'df32': L.DF32}[precision]
         prm.isSlopeLim = 1 if isSlopeLim else 0
         prm.typeSlopeLim = L.LIMITER_TYPES[typeSlopeLim]
         prm.device = device; prm.flags = flags

@@ -38,7 +38,9 @@ enum {
   DGADV_EUNSUPPORTED = 7   /* option not supported by this build (e.g. p > 3 on the GPU)  */
 };
 
-enum { DGADV_FP64 = 0, DGADV_FP32 = 1 };
+/* Arithmetic of the stored state and of every kernel: FP64; FP32; or DF32, each real an
+ * unevaluated sum of two FP32 numbers (about 48 significant bits) computed on the FP32 units. */
+enum { DGADV_FP64 = 0, DGADV_FP32 = 1, DGADV_DF32 = 2 };
 enum { DGADV_LIM_LINEAR = 0, DGADV_LIM_HIERARCH_VERT = 1, DGADV_LIM_STRICT = 2 };
 enum { DGADV_TIME_CONST = 0, DGADV_TIME_EXP_NEG = 1 };     /* g(t) = 1 or exp(-t) */
 
@@ -105,7 +107,7 @@ typedef struct dgadv_mesh {
 typedef struct dgadv_params {
   int32_t p;             /* polynomial degree 0..3 (the reference allows 0..4)              */
   int32_t ordRK;         /* SSP-RK order 1..3 (core/rungeKuttaExplicit.m:64-78)             */
-  int32_t precision;     /* DGADV_FP64 or DGADV_FP32                                        */
+  int32_t precision;     /* DGADV_FP64, DGADV_FP32 or DGADV_DF32                            */
   int32_t isSlopeLim;    /* vertex-based Taylor limiter on/off                              */
   int32_t typeSlopeLim;  /* DGADV_LIM_*                                                     */
   int32_t device;        /* CUDA device ordinal                                             */

@@ -6,6 +6,7 @@ solver restated), where spread is the oracle's own roundoff sensitivity for that
 The spread is ~1e-15 for every configuration except the hierarchical limiter at p=3, whose
 second-derivative reconstructions cancel to ~1e-10 and make the limiter factor depend on
 roundoff at ~1e-9.  FP32 relative L2 <= 1e-5 against the FP64 results at these short horizons.
+DF32 (double-float on the FP32 units) meets the FP64 bar against the oracle.
 """
 import ast
 import os
@@ -88,6 +89,42 @@ def test_fp32_close_to_fp64(lib, kw, tol):
     a = gpu_run(precision='fp32', **kw)
     b = gpu_run(precision='fp64', **kw)
     assert rel(a.cDisc, b.cDisc) <= tol
+
+
+# Double-float (DF32): every real a pair of FP32 numbers, about 48 significant bits, computed on
+# the FP32 units.  Its unit roundoff per operation (2^-48) is 32x FP64's, which keeps it well
+# inside the FP64 bar of 1e-12 against the oracle at these horizons; the hierarchical limiter
+# keeps the same roundoff-spread allowance as FP64.
+DF32_CASES = [SMALL[i] for i in (0, 2, 4, 6, 7, 8, 10, 11, 12)]
+
+
+@pytest.mark.parametrize('kw', DF32_CASES, ids=lambda kw: '-'.join('%s=%s' % (k, v) for k, v in kw.items()
+                                                                     if k not in ('testcase',)))
+def test_df32_matches_oracle(lib, kw):
+    from oracle import matfree as MF
+    g = gpu_run(precision='df32', **kw)
+    o = oracle_run(**kw)
+    tol = FP64_TOL
+    if kw.get('typeSlopeLim') == 'hierarch_vert':
+        tol = max(FP64_TOL, 10 * MF.roundoff_spread(**kw))
+    assert rel(g.cDisc, o.cDisc) <= tol
+
+
+def test_df32_close_to_fp64_over_a_long_run(lib):
+    """300 limited steps on 8192 triangles: the accumulated DF32 error stays far below the 1e-6
+    accuracy bar that plain FP32 misses at this horizon."""
+    kw = dict(testcase='gauss_slot', hmax=2 ** -6, p=2, tEnd=0.03, numSteps=300, isSlopeLim=True)
+    a = gpu_run(precision='df32', **kw)
+    b = gpu_run(precision='fp64', **kw)
+    assert rel(a.cDisc, b.cDisc) <= 1e-10
+
+
+def test_df32_rejects_the_fused_pipeline(lib):
+    from festung_gb300 import _lib as L
+    with pytest.raises(L.DgadvError) as e:
+        gpu_run(precision='df32', gpuFlags=L.FLAG_FUSE, testcase='gauss_slot', hmax=2 ** -3, p=1, tEnd=0.01,
+                numSteps=2, isSlopeLim=True)
+    assert e.value.status == L.DGADV_EUNSUPPORTED
 
 
 def test_graph_and_direct_launches_agree_bitwise(lib):
