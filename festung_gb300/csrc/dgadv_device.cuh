@@ -93,6 +93,39 @@ template <> __host__ __device__ constexpr unsigned long long key_max<df32>() { r
 __device__ __forceinline__ bool finite_(const df32 &x) { return isfinite(x.hi) && isfinite(x.lo); }
 
 // ---------------------------------------------------------------------------------------------
+// Sum of products s = s0 + sum a_k b_k.  float / double: the plain multiply-add s += a b.  df32:
+// the running sum is an FP32 head, advanced by one exact two_sum per term, and an FP32 tail that
+// collects the head's rounding errors and the products' low parts; one two_sum normalises the
+// pair at the end.  That is about 13 FP32 instructions per term instead of a double-word
+// product plus a double-word addition (about 28), at an error of order n u^2 sum |a_k b_k|.
+template <typename T> struct Acc {
+  T s;
+  Acc() = default;
+  __device__ __forceinline__ explicit Acc(const T &s0) : s(s0) {}
+  __device__ __forceinline__ void fma(const T &a, const T &b) { s += a * b; }
+  __device__ __forceinline__ void fms(const T &a, const T &b) { s -= a * b; }
+  __device__ __forceinline__ T get() const { return s; }
+};
+template <> struct Acc<df32> {
+  float hi, lo;
+  Acc() = default;
+  __device__ __forceinline__ explicit Acc(const df32 &s0) : hi(s0.hi), lo(s0.lo) {}
+  __device__ __forceinline__ void fma(const df32 &a, const df32 &b) {
+    float p, e, t;
+    df::two_prod(a.hi, b.hi, p, e);
+    e = fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, e));
+    df::two_sum(hi, p, hi, t);
+    lo += t + e;
+  }
+  __device__ __forceinline__ void fms(const df32 &a, const df32 &b) { fma(-a, b); }
+  __device__ __forceinline__ df32 get() const {
+    float h, l;
+    df::two_sum(hi, lo, h, l);
+    return df32(h, l);
+  }
+};
+
+// ---------------------------------------------------------------------------------------------
 // Element geometry for the Taylor transform.
 template <typename T> struct Affine {
   T B11, B12, B21, B22;   // B(:,m,n): m = coordinate, n = column
@@ -144,10 +177,10 @@ __device__ __forceinline__ void to_taylor(const T *c, const Affine<T> &af, T *cT
   T u[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    T s = T(0);
+    Acc<T> s(T(0));
 #pragma unroll
-    for (int j = 0; j < N; ++j) s += tb.DM[i][j] * c[j];
-    u[i] = s;
+    for (int j = 0; j < N; ++j) s.fma(tb.DM[i][j], c[j]);
+    u[i] = s.get();
   }
   cT[0] = u[0];
   T sc = T(1);
@@ -211,10 +244,10 @@ __device__ __forceinline__ void from_taylor(const T *cT, const Affine<T> &af, T 
   }
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    T s = T(0);
+    Acc<T> s(T(0));
 #pragma unroll
-    for (int j = 0; j < N; ++j) s += tb.DMinv[i][j] * w[j];
-    c[i] = s;
+    for (int j = 0; j < N; ++j) s.fma(tb.DMinv[i][j], w[j]);
+    c[i] = s.get();
   }
 }
 
@@ -578,19 +611,19 @@ __device__ __forceinline__ void lin_u(const T *c, T *u) {
   const Tab<T, P> &tb = tab<T, P>();
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    T s = T(0);
+    Acc<T> s(T(0));
 #pragma unroll
-    for (int j = 0; j < N; ++j) s += tb.DM[i][j] * c[j];
-    u[i] = s;
+    for (int j = 0; j < N; ++j) s.fma(tb.DM[i][j], c[j]);
+    u[i] = s.get();
   }
 }
 template <typename T, int P> __device__ __forceinline__ T lin_mean(const T *c) {
   constexpr int N = Dims<P>::N;
   const Tab<T, P> &tb = tab<T, P>();
-  T s = T(0);
+  Acc<T> s(T(0));
 #pragma unroll
-  for (int j = 0; j < N; ++j) s += tb.DM[0][j] * c[j];
-  return s;
+  for (int j = 0; j < N; ++j) s.fma(tb.DM[0][j], c[j]);
+  return s.get();
 }
 // alpha of the linear limiter from u, and the removed part du (returns false if alpha == 1).
 template <typename T, int P, int NQ>
@@ -676,9 +709,10 @@ k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, 
   T qv[NQ];
   bool bad = false;
   if (active && ok) {
-    T c[N], rhs[N];
+    T c[N];
+    Acc<T> rhs[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = T(0); }
+    for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = Acc<T>(T(0)); }
 #pragma unroll
     for (int n = 0; n < 3; ++n)
       if (nb[n] >= k0 && nb[n] < k0 + kBlock)
@@ -688,19 +722,20 @@ k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, 
       for (int m = 0; m < g.nTerms; ++m) {
         const T gm = T(sc.gco[m]);
 #pragma unroll
-        for (int i = 0; i < N; ++i) rhs[i] += gm * g.rhs[((size_t)m * N + i) * Kp + k];
+        for (int i = 0; i < N; ++i) rhs[i].fma(gm, g.rhs[((size_t)m * N + i) * Kp + k]);
       }
     }
     // volume term
 #pragma unroll
     for (int qq = 0; qq < Q; ++qq) {
-      T cq = T(0);
+      Acc<T> cqa(T(0));
 #pragma unroll
-      for (int j = 0; j < N; ++j) cq += tb.phiQ[qq][j] * c[j];
+      for (int j = 0; j < N; ++j) cqa.fma(tb.phiQ[qq][j], c[j]);
+      const T cq = cqa.get();
       const T f1 = srow<T>(smem, rF + qq)[t] * cq;
       const T f2 = srow<T>(smem, rF + Q + qq)[t] * cq;
 #pragma unroll
-      for (int i = 0; i < N; ++i) rhs[i] += tb.g1[qq][i] * f1 + tb.g2[qq][i] * f2;
+      for (int i = 0; i < N; ++i) { rhs[i].fma(tb.g1[qq][i], f1); rhs[i].fma(tb.g2[qq][i], f2); }
     }
     // upwind edge term
     const int code = irow<T>(smem, NT, 0)[t];
@@ -711,32 +746,35 @@ k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, 
 #pragma unroll
       for (int r2 = 0; r2 < R; ++r2) {
         const T v = srow<T>(smem, rV + n * R + r2)[t];
-        T tr = T(0);
+        Acc<T> tr(T(0));
         if (v > T(0) && outOk) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r2][j] * c[j];
+          for (int j = 0; j < N; ++j) tr.fma(tb.phi1D[n][r2][j], c[j]);
         } else if (v < T(0) && nb[n] >= 0) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r2][j] * cn[n][j];
+          for (int j = 0; j < N; ++j) tr.fma(tb.thetaPhi[n][np][r2][j], cn[n][j]);
         }
-        const T fl = v * tr;
+        const T fl = v * tr.get();
 #pragma unroll
-        for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r2][i] * fl;
+        for (int i = 0; i < N; ++i) rhs[i].fms(tb.phi1D[n][r2][i], fl);
       }
     }
     // mass solve
     T cdot[N];
     if (sizeof(T) == 8) {
+      T r[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) r[j] = rhs[j].get();
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        T s = T(0);
+        Acc<T> s(T(0));
 #pragma unroll
-        for (int j = 0; j < N; ++j) s += tb.hatMinv[i][j] * rhs[j];
-        cdot[i] = s;
+        for (int j = 0; j < N; ++j) s.fma(tb.hatMinv[i][j], r[j]);
+        cdot[i] = s.get();
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < N; ++i) cdot[i] = rhs[i];
+      for (int i = 0; i < N; ++i) cdot[i] = rhs[i].get();
     }
     if (MODE == 2 && LIN) {
 #pragma unroll
@@ -1014,10 +1052,10 @@ k_limit_dot_lin(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__
     if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, nan3, du)) {
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        T s = T(0);
+        Acc<T> s(cd[i]);
 #pragma unroll
-        for (int j = 1; j < N; ++j) s += srow<T>(smem, rQ + i * (N - 1) + (j - 1))[t] * du[j];
-        cd[i] += s;
+        for (int j = 1; j < N; ++j) s.fma(srow<T>(smem, rQ + i * (N - 1) + (j - 1))[t], du[j]);
+        cd[i] = s.get();
       }
     }
     const T w = T(sc.omega), tau = T(sc.tau);
@@ -1073,10 +1111,10 @@ k_limit_lin(const Geo<T> g, const T *__restrict__ cbuf, T *__restrict__ out, con
   if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, data, du)) {
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      T s = T(0);
+      Acc<T> s(c[i]);
 #pragma unroll
-      for (int j = 1; j < N; ++j) s += tb.DMinv[i][j] * du[j];
-      c[i] -= s;
+      for (int j = 1; j < N; ++j) s.fms(tb.DMinv[i][j], du[j]);
+      c[i] = s.get();
     }
   }
   bool bad = false;
@@ -1130,10 +1168,10 @@ __device__ __forceinline__ void lin_limit_inplace(const LimIn<T> &li, const VKey
   if (lin_alpha<T, P, 1>(li, kv, sh, u, dmask, zero3, du)) {
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      T s = T(0);
+      Acc<T> s(c[i]);
 #pragma unroll
-      for (int j = 1; j < N; ++j) s += tb.DMinv[i][j] * du[j];
-      c[i] -= s;
+      for (int j = 1; j < N; ++j) s.fms(tb.DMinv[i][j], du[j]);
+      c[i] = s.get();
     }
   }
 }
@@ -1215,9 +1253,10 @@ k_op_fused(const Geo<T> g, const T *__restrict__ x, int limitIn, T *__restrict__
   T q0 = T(0);
   bool bad = false;
   if (active && ok) {
-    T c[N], rhs[N];
+    T c[N];
+    Acc<T> rhs[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = T(0); }
+    for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = Acc<T>(T(0)); }
 #pragma unroll
     for (int n = 0; n < 3; ++n)
       if (nb[n] >= k0 && nb[n] < k0 + kBlock)
@@ -1237,18 +1276,19 @@ k_op_fused(const Geo<T> g, const T *__restrict__ x, int limitIn, T *__restrict__
       for (int m = 0; m < g.nTerms; ++m) {
         const T gm = T(sc.gco[m]);
 #pragma unroll
-        for (int i = 0; i < N; ++i) rhs[i] += gm * g.rhs[((size_t)m * N + i) * Kp + k];
+        for (int i = 0; i < N; ++i) rhs[i].fma(gm, g.rhs[((size_t)m * N + i) * Kp + k]);
       }
     }
 #pragma unroll
     for (int qq = 0; qq < Q; ++qq) {
-      T cq = T(0);
+      Acc<T> cqa(T(0));
 #pragma unroll
-      for (int j = 0; j < N; ++j) cq += tb.phiQ[qq][j] * c[j];
+      for (int j = 0; j < N; ++j) cqa.fma(tb.phiQ[qq][j], c[j]);
+      const T cq = cqa.get();
       const T f1 = srow<T>(smem, rF + qq)[t] * cq;
       const T f2 = srow<T>(smem, rF + Q + qq)[t] * cq;
 #pragma unroll
-      for (int i = 0; i < N; ++i) rhs[i] += tb.g1[qq][i] * f1 + tb.g2[qq][i] * f2;
+      for (int i = 0; i < N; ++i) { rhs[i].fma(tb.g1[qq][i], f1); rhs[i].fma(tb.g2[qq][i], f2); }
     }
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
@@ -1257,31 +1297,34 @@ k_op_fused(const Geo<T> g, const T *__restrict__ x, int limitIn, T *__restrict__
 #pragma unroll
       for (int r2 = 0; r2 < R; ++r2) {
         const T v = srow<T>(smem, rV + n * R + r2)[t];
-        T tr = T(0);
+        Acc<T> tr(T(0));
         if (v > T(0) && outOk) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) tr += tb.phi1D[n][r2][j] * c[j];
+          for (int j = 0; j < N; ++j) tr.fma(tb.phi1D[n][r2][j], c[j]);
         } else if (v < T(0) && nb[n] >= 0) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) tr += tb.thetaPhi[n][np][r2][j] * cn[n][j];
+          for (int j = 0; j < N; ++j) tr.fma(tb.thetaPhi[n][np][r2][j], cn[n][j]);
         }
-        const T fl = v * tr;
+        const T fl = v * tr.get();
 #pragma unroll
-        for (int i = 0; i < N; ++i) rhs[i] -= tb.phi1D[n][r2][i] * fl;
+        for (int i = 0; i < N; ++i) rhs[i].fms(tb.phi1D[n][r2][i], fl);
       }
     }
     T cdot[N];
     if (sizeof(T) == 8) {
+      T r[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) r[j] = rhs[j].get();
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        T s = T(0);
+        Acc<T> s(T(0));
 #pragma unroll
-        for (int j = 0; j < N; ++j) s += tb.hatMinv[i][j] * rhs[j];
-        cdot[i] = s;
+        for (int j = 0; j < N; ++j) s.fma(tb.hatMinv[i][j], r[j]);
+        cdot[i] = s.get();
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < N; ++i) cdot[i] = rhs[i];
+      for (int i = 0; i < N; ++i) cdot[i] = rhs[i].get();
     }
     if (MODE == 2) {
 #pragma unroll

@@ -92,10 +92,13 @@ def test_fp32_close_to_fp64(lib, kw, tol):
 
 
 # Double-float (DF32): every real a pair of FP32 numbers, about 48 significant bits, computed on
-# the FP32 units.  Its unit roundoff per operation (2^-48) is 32x FP64's, which keeps it well
-# inside the FP64 bar of 1e-12 against the oracle at these horizons; the hierarchical limiter
-# keeps the same roundoff-spread allowance as FP64.
+# the FP32 units.  Its unit roundoff per operation (2^-48) is 32x FP64's (2^-53), which keeps it
+# inside the FP64 bar of 1e-12 against the oracle at these horizons.  Where the oracle's own
+# roundoff spread (measured at FP64's unit roundoff) sets the allowance, DF32 gets that spread
+# scaled by the ratio of the unit roundoffs: the hierarchical limiter at p=3 moves by ~1e-9
+# under FP64 re-rounding and by ~3e-8 in DF32.
 DF32_CASES = [SMALL[i] for i in (0, 2, 4, 6, 7, 8, 10, 11, 12)]
+DF32_UNIT_RATIO = 2.0 ** -48 / 2.0 ** -53
 
 
 @pytest.mark.parametrize('kw', DF32_CASES, ids=lambda kw: '-'.join('%s=%s' % (k, v) for k, v in kw.items()
@@ -106,7 +109,7 @@ def test_df32_matches_oracle(lib, kw):
     o = oracle_run(**kw)
     tol = FP64_TOL
     if kw.get('typeSlopeLim') == 'hierarch_vert':
-        tol = max(FP64_TOL, 10 * MF.roundoff_spread(**kw))
+        tol = max(FP64_TOL, 10 * DF32_UNIT_RATIO * MF.roundoff_spread(**kw))
     assert rel(g.cDisc, o.cDisc) <= tol
 
 
