@@ -71,6 +71,11 @@ SYMBOLS = {
     'dgadv_last_error': (ctypes.c_char_p, [ctypes.c_void_p]),
     'dgadv_status_string': (ctypes.c_char_p, [ctypes.c_int]),
     'dgadv_destroy': (None, [ctypes.c_void_p]),
+    'dgadv_set_velocity_modes': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp, _dp]),
+    'dgadv_set_velocity_theta': (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    'dgadv_forward_record': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_int32]),
+    'dgadv_backward': (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp]),
+    'dgadv_checkpoint_schedule': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i32p]),
     'dgadv_limit_linear_noalloc': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -142,6 +147,19 @@ def grid_build(coordV, V0T):
                coordV0T=arr(g.coordV0T, (T, 3, 2), np.float64), detJ0T=arr(g.detJ0T, (T,), np.float64))
     lib.dgadv_grid_free(out)
     return res
+
+
+def checkpoint_schedule(nSteps, nSnapshots):
+    """The adjoint's checkpointing actions as an (n, 2) array of (action, argument) and the index
+    of the first reverse-sweep action (actions: 0 restore slot, 1 advance, 2 store slot,
+    3 reverse step)."""
+    lib = load()
+    n = ctypes.c_int32(0)
+    b = ctypes.c_int32(0)
+    check(lib.dgadv_checkpoint_schedule(nSteps, nSnapshots, None, ctypes.byref(n), None))
+    a = np.zeros(2 * n.value, dtype=np.int32)
+    check(lib.dgadv_checkpoint_schedule(nSteps, nSnapshots, ptr(a, _i32p), ctypes.byref(n), ctypes.byref(b)))
+    return a.reshape(-1, 2), b.value
 
 
 def quad_rule_1d(qOrd):

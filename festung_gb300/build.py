@@ -32,7 +32,8 @@ def sources():
     return [os.path.join(CSRC, f) for f in ('dgadv_host.cpp', 'dgadv_capi.cpp', 'dgadv_solver.cu',
                                             'dgadv_prec_fp64.cu', 'dgadv_prec_fp32.cu',
                                             'dgadv_prec_df32_p01.cu', 'dgadv_prec_df32_p2.cu',
-                                            'dgadv_prec_df32_p3.cu', 'dgadv_noalloc.cu')]
+                                            'dgadv_prec_df32_p3.cu', 'dgadv_adjoint.cu',
+                                            'dgadv_noalloc.cu')]
 
 
 def _stale():

@@ -1,0 +1,432 @@
+// C-ABI of the discrete adjoint (include/dgadv.h): velocity modes, the recorded forward run with
+// binomial checkpointing, and the reverse sweep.
+//
+// Checkpointing.  Reversing T steps needs the state c^i at the start of every step i, in
+// reverse order.  With S snapshot slots (slot 0 holds c^0), the schedule is the binomial one
+// of Griewank (1992, "Achieving logarithmic growth of temporal and spatial complexity in reverse
+// automatic differentiation"): with s free slots and t steps, let r be the smallest integer with
+// beta(s, r) = C(s + r, s) >= t; advance to a split point m = a + max(1, t - beta(s - 1, r)),
+// store c^m, reverse [m, b) with s - 1 free slots, then [a, m) with s.  No step is recomputed
+// more than r times.  With as many slots as steps every state is stored once and nothing is
+// recomputed.  Each reversed step recomputes its own RK stages from c^i (one forward step)
+// before the adjoint stages run.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dgadv_handle.h"
+
+using namespace dgadv;
+
+namespace {
+
+enum { A_RESTORE = 0, A_ADVANCE = 1, A_STORE = 2, A_BACKWARD = 3 };
+
+double beta(int s, int r) {   // C(s + r, s), as a double (only compared with step counts)
+  double b = 1.0;
+  for (int i = 1; i <= s; ++i) b = b * (r + i) / i;
+  return b;
+}
+
+void push(std::vector<int> &o, int op, int arg) { o.push_back(op); o.push_back(arg); }
+
+// Reverse steps [a, b) given c^a in slot sa; slots top, top+1, ... are free (freeS of them).
+void reverse_steps(std::vector<int> &o, int a, int b, int sa, int top, int freeS) {
+  const int t = b - a;
+  if (t == 1) { push(o, A_RESTORE, sa); push(o, A_BACKWARD, a); return; }
+  if (freeS == 0) {
+    for (int i = b - 1; i >= a; --i) {
+      push(o, A_RESTORE, sa);
+      if (i > a) push(o, A_ADVANCE, i - a);
+      push(o, A_BACKWARD, i);
+    }
+    return;
+  }
+  int r = 1;
+  while (beta(freeS, r) < t) ++r;
+  const int m = a + (int)std::max(1.0, t - beta(freeS - 1, r));
+  push(o, A_RESTORE, sa);
+  push(o, A_ADVANCE, m - a);
+  push(o, A_STORE, top);
+  reverse_steps(o, m, b, top, top + 1, freeS - 1);
+  reverse_steps(o, a, m, sa, top, freeS);
+}
+
+void make_schedule(int nSteps, int nSlots, std::vector<int> &o) {
+  o.clear();
+  reverse_steps(o, 0, nSteps, 0, 1, nSlots - 1);
+}
+
+// First action of the reverse sweep: the last restore before the first backward step (the
+// forward phase runs the actions before it, then carries the state on to the final step).
+size_t backward_start(const std::vector<int> &o) {
+  size_t f = 0;
+  while (f < o.size() && o[f] != A_BACKWARD) f += 2;
+  while (f >= 2 && o[f] != A_RESTORE) f -= 2;
+  return f;
+}
+
+// dJ/dtheta_m partial sums: block b of mode m sums aF F_m + aV Vn_m over its elements.
+__global__ void k_theta_partial(int K, int Kp, int nF, int nV, const double *__restrict__ aF,
+                                const double *__restrict__ aV, const double *__restrict__ modeF,
+                                const double *__restrict__ modeV, double *__restrict__ part) {
+  __shared__ double red[256];
+  const int m = blockIdx.y;
+  double s = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
+    for (int c = 0; c < nF; ++c) s += aF[(size_t)c * Kp + k] * modeF[((size_t)m * nF + c) * Kp + k];
+    for (int c = 0; c < nV; ++c) s += aV[(size_t)c * Kp + k] * modeV[((size_t)m * nV + c) * Kp + k];
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[(size_t)m * gridDim.x + blockIdx.x] = red[0];
+}
+
+constexpr int kThetaBlocks = 304;   // 2 x 152 SMs
+
+// The cached reverse-sweep graph no longer fits the recorded run.
+void drop_sweep(dgadv_handle *h) {
+  if (h->adjExec) cudaGraphExecDestroy(h->adjExec);
+  h->adjExec = nullptr;
+  h->adjExecSteps = h->adjExecSlots = 0;
+  h->adjExecTau = 0.0;
+}
+
+void dev_release(dgadv_handle *h, void *&p) {
+  if (!p) return;
+  cudaFree(p);
+  h->allocs.erase(std::remove(h->allocs.begin(), h->allocs.end(), p), h->allocs.end());
+  p = nullptr;
+}
+
+// Cursor of a schedule run: the step the run stands at, where that state lives (a slot, or the
+// work buffer cn), and which step cn holds.
+struct Cursor {
+  int step = 0;     // state the schedule has reached
+  int slot = -1;    // slot holding that state (-1: only cn holds it)
+  int cnStep = 0;   // step held by cn (-1: none)
+};
+
+int rk_stages(const dgadv_handle *h, double omega[3]) {
+  omega[0] = omega[1] = omega[2] = 0.0;
+  if (h->ordRK == 2) { omega[1] = 0.5; return 2; }
+  if (h->ordRK == 3) { omega[1] = 0.75; omega[2] = 1.0 / 3.0; return 3; }
+  return 1;
+}
+
+// One forward step from cn (the cursor's state); with stage storage the step's stage states are
+// written straight into its stage slots.
+int forward_step(dgadv_handle *h, Cursor &w) {
+  const PrecOps &o = ops_of(h);
+  double omega[3];
+  const int S = rk_stages(h, omega);
+  const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
+  void *cA = h->cA, *cB = h->cB;
+  if (h->adjStages && S > 1) {
+    char *st = (char *)h->adjStages + (size_t)w.step * (S - 1) * bytes;
+    h->cA = st;
+    if (S > 2) h->cB = st + bytes;
+  }
+  const cudaError_t e = o.step(h, w.step * h->recTau, h->recTau);
+  h->cA = cA;
+  h->cB = cB;
+  DG_CUDA(e);
+  ++w.step;
+  w.cnStep = w.step;
+  w.slot = -1;
+  return DGADV_OK;
+}
+
+// Executes schedule actions [from, to) on the handle's stream.  Restores are lazy: a slot is
+// copied into cn only when a forward step has to start from it.  With stage storage (every
+// step's stage states kept by the recorded run) a reversed step reads its stages from there
+// and recomputes nothing.
+int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
+  const PrecOps &o = ops_of(h);
+  const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
+  const double tau = h->recTau;
+  double omega[3];
+  const int S = rk_stages(h, omega);
+  char *slots = (char *)h->adjSlots;
+  char *stages = (char *)h->adjStages;
+  auto stage_ptr = [&](int step, int s) { return stages + ((size_t)step * (S - 1) + (s - 1)) * bytes; };
+  auto materialize = [&]() -> int {
+    if (w.cnStep == w.step) return DGADV_OK;
+    if (w.slot < 0) { h->err = "checkpoint schedule lost its state"; return DGADV_EINVAL; }
+    DG_CUDA(o.copy(h, h->cn, slots + (size_t)w.slot * bytes, bytes));
+    w.cnStep = w.step;
+    return DGADV_OK;
+  };
+  int st;
+  for (size_t a = from; a < to; a += 2) {
+    const int op = h->schedule[a], arg = h->schedule[a + 1];
+    if (op == A_RESTORE) {
+      w.step = h->slotStep[arg];
+      w.slot = arg;
+    } else if (op == A_ADVANCE) {
+      if ((st = materialize())) return st;
+      for (int i = 0; i < arg; ++i)
+        if ((st = forward_step(h, w))) return st;
+    } else if (op == A_STORE) {
+      if ((st = materialize())) return st;
+      DG_CUDA(o.copy(h, slots + (size_t)arg * bytes, h->cn, bytes));
+      h->slotStep[arg] = w.step;
+      w.slot = arg;
+    } else {   // A_BACKWARD: the stage states of step arg (stored or recomputed), then reversed
+      if (w.step != arg) { h->err = "checkpoint schedule out of order"; return DGADV_EINVAL; }
+      const void *stageIn[3];
+      if (stages) {
+        if (w.slot < 0) { h->err = "checkpoint schedule lost its state"; return DGADV_EINVAL; }
+        stageIn[0] = slots + (size_t)w.slot * bytes;
+        for (int s = 1; s < S; ++s) stageIn[s] = stage_ptr(arg, s);
+      } else {
+        if ((st = materialize())) return st;
+        const void *c0 = h->cx;
+        if (w.slot >= 0) c0 = slots + (size_t)w.slot * bytes;   // c^i is that slot
+        else DG_CUDA(o.copy(h, h->cx, h->cn, bytes));
+        if ((st = forward_step(h, w))) return st;
+        stageIn[0] = c0;
+        stageIn[1] = h->cA;
+        stageIn[2] = h->cB;
+      }
+      void *mub[3] = {nullptr, h->mu1, h->mu2};
+      for (int s = S - 1; s >= 0; --s) {
+        AdjStageArgs x;
+        x.muIn = (s == S - 1) ? h->lam : mub[s + 1];
+        x.cs = stageIn[s];
+        x.muOut = s > 0 ? mub[s] : nullptr;
+        x.accn = h->accn;
+        x.omega = omega[s];
+        x.tau = tau;
+        x.init = s == S - 1;
+        x.last = s == 0;
+        DG_CUDA(o.adj_stage(h, x));
+      }
+      std::swap(h->lam, h->accn);
+      w.step = arg + 1;
+      w.slot = -1;
+    }
+  }
+  return DGADV_OK;
+}
+
+}  // namespace
+
+extern "C" int dgadv_set_velocity_modes(dgadv_handle *h, int32_t nModes, const double *u1Modes,
+                                        const double *u2Modes, const double *vNModes) {
+  if (!h || nModes < 0 || nModes > 1024) return DGADV_EINVAL;
+  if (nModes > 0 && (!u1Modes || !u2Modes || !vNModes)) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  void *pF = h->modeF, *pV = h->modeV;
+  dev_release(h, pF);
+  dev_release(h, pV);
+  h->modeF = h->modeV = nullptr;
+  h->nModes = 0;
+  if (nModes == 0) return DGADV_OK;
+  const size_t nF = 2 * (size_t)h->Q * h->Kp, nV = 3 * (size_t)h->R * h->Kp;
+  const size_t sU = (size_t)h->K * h->N, sV = (size_t)h->K * 3 * h->R;
+  std::vector<double> allF(nF * nModes), allV(nV * nModes), F, Vn;
+  for (int m = 0; m < nModes; ++m) {
+    velocity_factors(h, u1Modes + m * sU, u2Modes + m * sU, vNModes + m * sV, F, Vn);
+    std::copy(F.begin(), F.end(), allF.begin() + m * nF);
+    std::copy(Vn.begin(), Vn.end(), allV.begin() + m * nV);
+  }
+  int st;
+  if ((st = dev_alloc(h, (void **)&h->modeF, allF.size() * 8))) return st;
+  if ((st = dev_alloc(h, (void **)&h->modeV, allV.size() * 8))) return st;
+  if ((st = upload(h, h->modeF, allF.data(), allF.size() * 8))) return st;
+  if ((st = upload(h, h->modeV, allV.data(), allV.size() * 8))) return st;
+  h->nModes = nModes;
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_set_velocity_theta(dgadv_handle *h, const double *theta) {
+  if (!h || !theta) return DGADV_EINVAL;
+  if (h->nModes == 0) { h->err = "no velocity modes set"; return DGADV_EINVAL; }
+  DG_CUDA(cudaSetDevice(h->device));
+  const size_t nF = 2 * (size_t)h->Q * h->Kp, nV = 3 * (size_t)h->R * h->Kp;
+  std::vector<double> allF(nF * h->nModes), allV(nV * h->nModes);
+  DG_CUDA(cudaMemcpy(allF.data(), h->modeF, allF.size() * 8, cudaMemcpyDeviceToHost));
+  DG_CUDA(cudaMemcpy(allV.data(), h->modeV, allV.size() * 8, cudaMemcpyDeviceToHost));
+  std::vector<double> F(nF, 0.0), Vn(nV, 0.0);
+  for (int m = 0; m < h->nModes; ++m) {
+    for (size_t i = 0; i < nF; ++i) F[i] += theta[m] * allF[m * nF + i];
+    for (size_t i = 0; i < nV; ++i) Vn[i] += theta[m] * allV[m * nV + i];
+  }
+  int st;
+  if ((st = upload_real(h, h->F, F))) return st;
+  if ((st = upload_real(h, h->Vn, Vn))) return st;
+  h->hasVelocity = true;
+  h->recorded = false;
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau, int32_t nSnapshots) {
+  if (!h || nSteps < 1 || !(tau > 0.0)) return DGADV_EINVAL;
+  const PrecOps &o = ops_of(h);
+  if (!o.adj_stage) { h->err = "no adjoint kernels for this precision"; return DGADV_EUNSUPPORTED; }
+  if (h->lim) { h->err = "the adjoint covers the unlimited scheme only"; return DGADV_EUNSUPPORTED; }
+  DG_CUDA(cudaSetDevice(h->device));
+  const int nSlots = (nSnapshots <= 0 || nSnapshots >= nSteps) ? nSteps : nSnapshots;
+  const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
+  double omega[3];
+  const int S = rk_stages(h, omega);
+  const int stageSteps = (nSnapshots <= 0 && S > 1) ? nSteps : 0;   // keep every stage state
+  int st;
+  if (stageSteps != h->adjStageSteps) {
+    drop_sweep(h);
+    dev_release(h, h->adjStages);
+    h->adjStageSteps = 0;
+    if (stageSteps) {
+      if ((st = dev_alloc(h, &h->adjStages, (size_t)stageSteps * (S - 1) * bytes))) return st;
+      h->adjStageSteps = stageSteps;
+    }
+  }
+  if (nSlots != h->nSlots || nSteps != h->adjExecSteps || tau != h->adjExecTau) drop_sweep(h);
+  if (nSlots != h->nSlots) {
+    dev_release(h, h->adjSlots);
+    if ((st = dev_alloc(h, &h->adjSlots, (size_t)nSlots * bytes))) return st;
+    h->nSlots = nSlots;
+  }
+  if (!h->lam) {
+    if ((st = dev_alloc(h, &h->lam, bytes))) return st;
+    if ((st = dev_alloc(h, &h->mu1, bytes))) return st;
+    if ((st = dev_alloc(h, &h->mu2, bytes))) return st;
+    if ((st = dev_alloc(h, &h->accn, bytes))) return st;
+    h->adjBuf[0] = h->lam;
+    h->adjBuf[1] = h->accn;
+    if ((st = dev_alloc(h, &h->cx, bytes))) return st;
+    if ((st = dev_alloc(h, (void **)&h->aF, 2 * (size_t)h->Q * h->Kp * 8))) return st;
+    if ((st = dev_alloc(h, (void **)&h->aV, 3 * (size_t)h->R * h->Kp * 8))) return st;
+    if ((st = dev_alloc(h, (void **)&h->thetaPart, (size_t)kThetaBlocks * 1024 * 8))) return st;
+    DG_CUDA(cudaMemset(h->mu1, 0, bytes));
+    DG_CUDA(cudaMemset(h->mu2, 0, bytes));
+  }
+  h->slotStep.assign(nSlots, -1);
+  make_schedule(nSteps, nSlots, h->schedule);
+  h->schedBackward = backward_start(h->schedule);
+  h->recSteps = nSteps;
+  h->recTau = tau;
+  // c^0 is the current state
+  DG_CUDA(o.copy(h, h->adjSlots, h->cn, bytes));
+  h->slotStep[0] = 0;
+  Cursor w;
+  w.slot = 0;
+  if ((st = run_actions(h, 0, h->schedBackward, w))) return st;
+  if (w.cnStep != w.step) DG_CUDA(o.copy(h, h->cn, (char *)h->adjSlots + (size_t)w.slot * bytes, bytes));
+  w.cnStep = w.step;
+  while (w.step < nSteps)
+    if ((st = forward_step(h, w))) return st;
+  h->recorded = true;
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc0, double *dJdtheta) {
+  if (!h || !dJdcT) return DGADV_EINVAL;
+  if (!h->recorded) { h->err = "no recorded forward run"; return DGADV_EINVAL; }
+  const PrecOps &o = ops_of(h);
+  DG_CUDA(cudaSetDevice(h->device));
+  const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
+  // every sweep starts from the same buffer order, so that a cached graph stays valid
+  h->lam = h->adjBuf[0];
+  h->accn = h->adjBuf[1];
+  // memsets and copies first, then a plain kernel launch, so that the dependent-launch chain of
+  // the sweep starts after work that is complete
+  DG_CUDA(cudaMemsetAsync(h->lam, 0, bytes, h->stream));
+  DG_CUDA(cudaMemsetAsync(h->aF, 0, 2 * (size_t)h->Q * h->Kp * 8, h->stream));
+  DG_CUDA(cudaMemsetAsync(h->aV, 0, 3 * (size_t)h->R * h->Kp * 8, h->stream));
+  DG_CUDA(cudaMemcpyAsync(h->stage_ext, dJdcT, (size_t)h->N * h->K * 8, cudaMemcpyHostToDevice, h->stream));
+  DG_CUDA(o.scatter_in(h, h->lam));
+  // The reverse sweep (about 2S + 1 launches per step) runs as one CUDA graph, captured on the
+  // first backward of a run length / step / snapshot count and replayed afterwards.
+  int st = DGADV_OK;
+  const bool useGraph = !(h->flags & DGADV_FLAG_NO_GRAPH);
+  if (useGraph && !h->adjExec) {
+    Cursor w;
+    w.step = w.cnStep = h->recSteps;
+    cudaGraph_t graph = nullptr;
+    DG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    st = run_actions(h, h->schedBackward, h->schedule.size(), w);
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    if (st == DGADV_OK && e != cudaSuccess) {
+      h->err = std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e);
+      st = DGADV_ECUDA;
+    }
+    if (st == DGADV_OK) {
+      const cudaError_t e2 = cudaGraphInstantiate(&h->adjExec, graph, 0);
+      if (e2 != cudaSuccess) {
+        h->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e2);
+        h->adjExec = nullptr;
+        st = DGADV_ECUDA;
+      } else {
+        h->adjExecSteps = h->recSteps;
+        h->adjExecSlots = h->nSlots;
+        h->adjExecTau = h->recTau;
+      }
+    }
+    if (graph) cudaGraphDestroy(graph);
+  } else if (!useGraph) {
+    Cursor w;
+    w.step = w.cnStep = h->recSteps;
+    st = run_actions(h, h->schedBackward, h->schedule.size(), w);
+  }
+  if (st == DGADV_OK && useGraph) {
+    const cudaError_t e = cudaGraphLaunch(h->adjExec, h->stream);
+    if (e != cudaSuccess) { h->err = std::string("cudaGraphLaunch: ") + cudaGetErrorString(e); st = DGADV_ECUDA; }
+  }
+  // after recSteps swaps the result sits in adjBuf[recSteps % 2]
+  h->lam = h->adjBuf[h->recSteps % 2];
+  h->accn = h->adjBuf[1 - h->recSteps % 2];
+  if (st) return st;
+  h->recorded = false;
+  if (dJdc0) {
+    DG_CUDA(o.gather_out(h, h->lam));
+    DG_CUDA(cudaMemcpyAsync(dJdc0, h->stage_ext, (size_t)h->N * h->K * 8, cudaMemcpyDeviceToHost, h->stream));
+  }
+  if (dJdtheta && h->nModes > 0) {
+    const int nF = 2 * h->Q, nV = 3 * h->R;
+    const int gx = std::min(kThetaBlocks, (h->K + 255) / 256);
+    for (int m0 = 0; m0 < h->nModes; m0 += 1024) {
+      const int nm = std::min(1024, h->nModes - m0);
+      k_theta_partial<<<dim3(gx, nm), 256, 0, h->stream>>>(h->K, h->Kp, nF, nV, h->aF, h->aV,
+                                                          h->modeF + (size_t)m0 * nF * h->Kp,
+                                                          h->modeV + (size_t)m0 * nV * h->Kp, h->thetaPart);
+      DG_CUDA(cudaGetLastError());
+      std::vector<double> part((size_t)nm * gx);
+      DG_CUDA(cudaMemcpyAsync(part.data(), h->thetaPart, part.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+      DG_CUDA(cudaStreamSynchronize(h->stream));
+      for (int m = 0; m < nm; ++m) {
+        double s = 0.0;
+        for (int b = 0; b < gx; ++b) s += part[(size_t)m * gx + b];
+        dJdtheta[m0 + m] = s;
+      }
+    }
+  }
+  // leave c^0 as the handle's state
+  DG_CUDA(o.copy(h, h->cn, h->adjSlots, bytes));
+  return dgadv_sync(h);
+}
+
+extern "C" int dgadv_checkpoint_schedule(int32_t nSteps, int32_t nSnapshots, int32_t *actions, int32_t *count,
+                                         int32_t *backwardStart) {
+  if (nSteps < 1 || !count) return DGADV_EINVAL;
+  const int nSlots = (nSnapshots <= 0 || nSnapshots >= nSteps) ? nSteps : nSnapshots;
+  std::vector<int> o;
+  make_schedule(nSteps, nSlots, o);
+  const int n = (int)o.size() / 2;
+  if (actions) {
+    if (*count < n) { *count = n; return DGADV_EINVAL; }
+    std::memcpy(actions, o.data(), o.size() * sizeof(int));
+  }
+  *count = n;
+  if (backwardStart) *backwardStart = (int32_t)(backward_start(o) / 2);
+  return DGADV_OK;
+}

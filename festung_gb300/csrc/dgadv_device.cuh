@@ -465,6 +465,21 @@ __device__ __forceinline__ void stage_expect(uint64_t *bar, int nT, int nI) {
 // kernel has completed and its writes are visible.
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// A kernel in such a chain must not declare a buffer that earlier kernels of the chain write as
+// `const T *__restrict__`: the compiler may then take its loads for invariant over the whole
+// kernel and move them above griddepcontrol.wait.  Outputs that alias no input keep a
+// (non-const) __restrict__, which lets input loads move past their stores.
+
+// Device-to-device copy of n 16-byte words as a kernel of the launch chain.  A copy between two
+// kernels that use programmatic dependent launch has to be a kernel itself: the second kernel's
+// dependency wait covers the kernel launched before it, not a copy-engine transfer queued in
+// between, so a cudaMemcpyAsync there is not ordered against the kernel that follows.
+static __global__ void k_copy16(const uint4 *src, uint4 *__restrict__ dst, size_t n) {
+  pdl_trigger();
+  pdl_wait();
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
 
 template <typename T> __device__ __forceinline__ const T *srow(const unsigned char *smem, int r) {
   return (const T *)(smem + (size_t)r * kBlock * sizeof(T));
@@ -661,7 +676,7 @@ struct StageScalars {
 
 template <typename T, int P, int MODE, bool RHS, bool LIN>
 __global__ void __launch_bounds__(kBlock)
-k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ out,
+k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
            const LimOut<T> lo, const StageScalars sc) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::op(MODE, LIN);
@@ -817,7 +832,7 @@ k_stage_op(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, 
 // limiter.
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_limit_dot(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, T *__restrict__ tbuf,
+k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
             const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value, NMT = Dims<P>::NMT;
   constexpr int NT = StageRows<T, P>::limdot();
@@ -905,7 +920,7 @@ k_limit_dot(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0,
 // (core/applySlopeLimiterDisc.m:77-86).
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const LimIn<T> li,
+k_limit(const Geo<T> g, const T *tbuf, T *__restrict__ out, const LimIn<T> li,
         const StageScalars sc) {
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::lim();
@@ -960,7 +975,7 @@ k_limit(const Geo<T> g, const T *__restrict__ tbuf, T *__restrict__ out, const L
 // Modal state -> Taylor form and scatter of its centroid quantities (initial limiting).
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_to_taylor(const Geo<T> g, const T *__restrict__ c, T *__restrict__ tbuf, const LimOut<T> lo,
+k_to_taylor(const Geo<T> g, const T *c, T *__restrict__ tbuf, const LimOut<T> lo,
             const StageScalars sc) {
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::totaylor();
@@ -1003,8 +1018,8 @@ k_to_taylor(const Geo<T> g, const T *__restrict__ c, T *__restrict__ tbuf, const
 // stage value is written in the modal basis and its mean scattered for the solution limiter.
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_limit_dot_lin(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__ c0, const T *__restrict__ tbuf,
-                T *__restrict__ out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
+k_limit_dot_lin(const Geo<T> g, const T *cin, const T *c0, const T *tbuf,
+                T *out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
   constexpr int N = Dims<P>::N, NQ = 1;
   constexpr int NT = StageRows<T, P>::limdot_lin();
   extern __shared__ __align__(128) unsigned char smem[];
@@ -1075,7 +1090,7 @@ k_limit_dot_lin(const Geo<T> g, const T *__restrict__ cin, const T *__restrict__
 // Taylor round trip): c <- c - DM^-1 du.
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_limit_lin(const Geo<T> g, const T *__restrict__ cbuf, T *__restrict__ out, const LimIn<T> li,
+k_limit_lin(const Geo<T> g, const T *cbuf, T *out, const LimIn<T> li,
             const StageScalars sc) {
   constexpr int N = Dims<P>::N, NQ = 1;
   const Tab<T, P> &tb = tab<T, P>();
@@ -1126,7 +1141,7 @@ k_limit_lin(const Geo<T> g, const T *__restrict__ cbuf, T *__restrict__ out, con
 // Mean of the modal state scattered to the vertices (initial limiting, linear limiter).
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_mean_lin(const Geo<T> g, const T *__restrict__ c, const LimOut<T> lo) {
+k_mean_lin(const Geo<T> g, const T *c, const LimOut<T> lo) {
   constexpr int N = Dims<P>::N;
   const int t = threadIdx.x, k = blockIdx.x * kBlock + t;
   pdl_trigger();
@@ -1178,8 +1193,8 @@ __device__ __forceinline__ void lin_limit_inplace(const LimIn<T> &li, const VKey
 
 template <typename T, int P, int MODE, bool RHS>
 __global__ void __launch_bounds__(kBlock)
-k_op_fused(const Geo<T> g, const T *__restrict__ x, int limitIn, T *__restrict__ xLout,
-           const T *__restrict__ c0L, int firstStage, T *__restrict__ out, const LimIn<T> li,
+k_op_fused(const Geo<T> g, const T *x, int limitIn, T *xLout,
+           const T *c0L, int firstStage, T *out, const LimIn<T> li,
            const LimOut<T> lo, const StageScalars sc) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
   constexpr int NT = StageRows<T, P>::op(MODE, true);

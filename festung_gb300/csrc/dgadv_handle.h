@@ -51,10 +51,40 @@ struct dgadv_handle {
   std::vector<int> profKinds;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double graphTau[3] = {-1.0, -1.0, -1.0};
+  // discrete adjoint (dgadv_forward_record / dgadv_backward)
+  int nModes = 0;
+  double *modeF = nullptr, *modeV = nullptr;   // nModes x 2Q x Kp, nModes x 3R x Kp (FP64)
+  void *adjSlots = nullptr;                    // state snapshots, nSlots x N x Kp
+  void *adjStages = nullptr;                   // stage states c^(1..S-1) of every step (or null)
+  int adjStageSteps = 0;
+  int nSlots = 0;
+  std::vector<int> slotStep;                   // step index held by each slot (-1: none)
+  void *lam = nullptr, *mu1 = nullptr, *mu2 = nullptr, *accn = nullptr, *cx = nullptr;
+  void *adjBuf[2] = {nullptr, nullptr};        // lam / accn swap between these every step
+  cudaGraphExec_t adjExec = nullptr;           // reverse sweep of the recorded schedule
+  int adjExecSteps = 0, adjExecSlots = 0;      // ... and the run it was captured for
+  double adjExecTau = 0.0;
+  double *aF = nullptr, *aV = nullptr;         // velocity sensitivities, 2Q x Kp and 3R x Kp
+  double *thetaPart = nullptr;                 // per-block partial sums of the mode gradient
+  std::vector<int> schedule;                   // checkpointing actions of the recorded run
+  size_t schedBackward = 0;                    // first action of the reverse sweep
+  int recSteps = 0;
+  double recTau = 0.0;
+  bool recorded = false;
   std::string err;
 };
 
 namespace dgadv {
+
+// One reversed stage of the adjoint sweep (device pointers of the handle's real type).
+struct AdjStageArgs {
+  const void *muIn;    // dJ/dc^(s+1)
+  const void *cs;      // c^(s), the stage input of the forward step
+  void *muOut;         // dJ/dc^(s) (may be null when s = 0)
+  void *accn;          // dJ/dc^n, accumulated over the stages of the step
+  double omega, tau;
+  int init, last;
+};
 
 // Work of one arithmetic type, enqueued on the handle's stream.
 struct PrecOps {
@@ -70,8 +100,11 @@ struct PrecOps {
   cudaError_t (*step_fused)(dgadv_handle *h, double t0, double tau, bool firstOfCall);
   cudaError_t (*finalize_fused)(dgadv_handle *h);
   cudaError_t (*limit)(dgadv_handle *h, double t);
-  cudaError_t (*scatter_in)(dgadv_handle *h);   // stage_ext (caller order, FP64) -> cn
-  cudaError_t (*gather_out)(dgadv_handle *h);   // cn -> stage_ext
+  cudaError_t (*scatter_in)(dgadv_handle *h, void *dst);        // stage_ext (caller order, FP64) -> dst
+  cudaError_t (*gather_out)(dgadv_handle *h, const void *src);  // src -> stage_ext
+  cudaError_t (*adj_stage)(dgadv_handle *h, const AdjStageArgs &a);   // null: no adjoint kernels
+  // device copy of a state-sized buffer (bytes a multiple of 16) ordered with dependent launches
+  cudaError_t (*copy)(dgadv_handle *h, void *dst, const void *src, size_t bytes);
 };
 
 // Fused path (linear limiter, zero Dirichlet data, opted in): per stage the operator kernel
@@ -79,6 +112,26 @@ struct PrecOps {
 inline bool use_fused(const dgadv_handle *h) {
   return h->lim && h->limType == DGADV_LIM_LINEAR && !h->cDV0T && (h->flags & DGADV_FLAG_FUSE);
 }
+
+const PrecOps &ops_of(const dgadv_handle *h);
+
+// Status return of a failed CUDA call inside a C-ABI function holding `h`.
+#define DG_CUDA(call)                                                               \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);                  \
+      return DGADV_ECUDA;                                                           \
+    }                                                                               \
+  } while (0)
+
+// Shared host helpers of the C-ABI units (dgadv_solver.cu).
+int dev_alloc(dgadv_handle *h, void **p, size_t bytes);
+int upload(dgadv_handle *h, void *dst, const void *src, size_t bytes);
+int upload_real(dgadv_handle *h, void *dst, const std::vector<double> &src);
+// Volume factors F (2Q x Kp) and edge factors Vn (3R x Kp) of one velocity, internal order.
+void velocity_factors(const dgadv_handle *h, const double *u1, const double *u2, const double *vN,
+                      std::vector<double> &F, std::vector<double> &Vn);
 
 const PrecOps &ops_fp64();
 const PrecOps &ops_fp32();

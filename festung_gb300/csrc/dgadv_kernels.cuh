@@ -1,16 +1,13 @@
-// Device kernels of the DG advection stage.  One thread owns one element; all per-element
-// arrays are structure-of-arrays with leading dimension Kp (coalesced loads across a warp).
+// Shared types of the device kernels.  One thread owns one element; all per-element arrays are
+// structure-of-arrays with leading dimension Kp (coalesced loads across a warp).
 //
 // Stage pipeline (stage s of an SSP-RK step, advection/solveSubStep.m:57-99):
 //   limiter off:          k_stage_op  (volume + upwind flux + mass + SSP)            -> c^(s)
-//   limiter on, p = 1:    k_stage_op  -> Taylor(c^(s)), centroid values q
-//                         k_vertex_minmax (CSR vertex patches)  -> vertex min/max
-//                         k_limit     -> limited modal c^(s)
-//   limiter on, p >= 2:   k_stage_op  -> Taylor(cDot), q
-//                         k_vertex_minmax
-//                         k_limit_dot (limit cDot, Taylor mass correction, SSP) -> Taylor(c^(s)), q
-//                         k_vertex_minmax
-//                         k_limit     -> limited modal c^(s)
+//   linear limiter:       k_stage_op  -> c^(s) (p = 1) or cDot (p >= 2), element means scattered
+//                         to the vertex min / max keys with atomics
+//                         k_limit_dot_lin (p >= 2: limit cDot, Taylor mass correction, SSP)
+//                         k_limit_lin  -> limited modal c^(s)
+//   hierarchical limiter: the same passes on Taylor coefficients (k_limit_dot, k_limit)
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -35,6 +32,12 @@ template <typename T, int P> struct Tab {
   T hatMinv[N][N];
   T DM[N][N];         // modal -> reference derivatives at the barycentre (times hatM)
   T DMinv[N][N];
+  // adjoint: the transposed mass solve folded into the test-function tables,
+  // Hg1[q][j] = sum_i g1[q][i] hatMinv[i][j] (likewise Hg2, Hphi), or the tables themselves
+  // where the forward path uses hatM = I (FP32)
+  T Hg1[Q][N];
+  T Hg2[Q][N];
+  T Hphi[3][R][N];
 };
 
 // Static per-element data of one mesh (device pointers, SoA with stride Kp).

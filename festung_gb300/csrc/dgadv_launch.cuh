@@ -32,6 +32,22 @@ static cudaError_t upload_tables(const RefTables &rt) {
       t.DM[i][j] = T(rt.DM[i * N + j]);
       t.DMinv[i][j] = T(rt.DMinv[i * N + j]);
     }
+  // adjoint tables (the forward FP32 path takes hatM^-1 = I; so does its adjoint)
+  const bool massSolve = sizeof(T) == 8;
+  auto fold = [&](const double *row, int j) {
+    if (!massSolve) return row[j];
+    double a = 0.0;
+    for (int i = 0; i < N; ++i) a += row[i] * rt.hatMinv[i * N + j];
+    return a;
+  };
+  for (int q = 0; q < Q; ++q)
+    for (int j = 0; j < N; ++j) {
+      t.Hg1[q][j] = T(fold(&rt.gradQ[q * N], j));
+      t.Hg2[q][j] = T(fold(&rt.gradQ[Q * N + q * N], j));
+    }
+  for (int n = 0; n < 3; ++n)
+    for (int r = 0; r < R; ++r)
+      for (int j = 0; j < N; ++j) t.Hphi[n][r][j] = T(fold(&rt.phi1D[(n * R + r) * N], j));
   return cudaMemcpyToSymbol(tab_symbol<T, P>(), &t, sizeof(t));
 }
 
@@ -114,6 +130,14 @@ static void launch_k(const dgadv_handle *h, void (*kern)(KArgs...), int grid, si
   cfg.attrs = at;
   cfg.numAttrs = (h->flags & DGADV_FLAG_NO_PDL) ? 0 : 1;
   cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+// Copy of a state-sized buffer (a multiple of 16 bytes) in the dependent-launch chain.
+static cudaError_t copy_state(dgadv_handle *h, void *dst, const void *src, size_t bytes) {
+  const size_t n = bytes / 16;
+  const int grid = (int)std::min<size_t>((n + kBlock - 1) / kBlock, 4 * 152);
+  launch_k(h, k_copy16, std::max(grid, 1), (size_t)0, (const uint4 *)src, (uint4 *)dst, n);
+  return cudaGetLastError();
 }
 
 // Opt-in shared memory sizes of the staged kernels of one (precision, degree).
@@ -214,8 +238,7 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     else launch_k(h, k_limit<T, P>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
     prof_mark(h, -1);
   }
-  if (S == 1)
-    cudaMemcpyAsync(cn, cA, (size_t)h->N * h->Kp * sizeof(T), cudaMemcpyDeviceToDevice, h->stream);
+  if (S == 1) return copy_state(h, cn, cA, (size_t)h->N * h->Kp * sizeof(T));
   return cudaGetLastError();
 }
 
@@ -349,15 +372,15 @@ static cudaError_t dispatch_limit(dgadv_handle *h, double t) {
 }
 
 template <typename T>
-static cudaError_t scatter_in(dgadv_handle *h) {
+static cudaError_t scatter_in(dgadv_handle *h, void *dst) {
   const int grid = (h->K + 255) / 256;
-  k_scatter_in<T><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, h->stage_ext, (T *)h->cn);
+  k_scatter_in<T><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, h->stage_ext, (T *)dst);
   return cudaGetLastError();
 }
 template <typename T>
-static cudaError_t gather_out(dgadv_handle *h) {
+static cudaError_t gather_out(dgadv_handle *h, const void *src) {
   const int grid = (h->K + 255) / 256;
-  k_gather_out<T><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, (const T *)h->cn, h->stage_ext);
+  k_gather_out<T><<<grid, 256, 0, h->stream>>>(h->K, h->Kp, h->N, h->perm, (const T *)src, h->stage_ext);
   return cudaGetLastError();
 }
 
@@ -403,6 +426,8 @@ static PrecOps make_ops() {
   o.limit = dispatch_limit<T, MASK>;
   o.scatter_in = scatter_in<T>;
   o.gather_out = gather_out<T>;
+  o.adj_stage = nullptr;
+  o.copy = copy_state;
   return o;
 }
 

@@ -1,4 +1,4 @@
-// Kernels and launch sequences of the FP32 path (stored reals: float), every degree.
+// Kernels and launch sequences of the FP32 path (stored reals: float), every degree, with the adjoint kernels.
 #include "dgadv_device.cuh"
 
 namespace dgadv {
@@ -6,10 +6,11 @@ DGADV_DEFINE_TABLES(float, cTf)
 }  // namespace dgadv
 
 #include "dgadv_launch.cuh"
+#include "dgadv_adjoint.cuh"
 
 namespace dgadv {
 const PrecOps &ops_fp32() {
-  static const PrecOps ops = make_ops<float, 0xF, true>();
+  static const PrecOps ops = with_adjoint<float, 0xF>(make_ops<float, 0xF, true>());
   return ops;
 }
 }  // namespace dgadv

@@ -1,4 +1,4 @@
-// Kernels and launch sequences of the FP64 path (stored reals: double), every degree.
+// Kernels and launch sequences of the FP64 path (stored reals: double), every degree, with the adjoint kernels.
 #include "dgadv_device.cuh"
 
 namespace dgadv {
@@ -6,10 +6,11 @@ DGADV_DEFINE_TABLES(double, cTd)
 }  // namespace dgadv
 
 #include "dgadv_launch.cuh"
+#include "dgadv_adjoint.cuh"
 
 namespace dgadv {
 const PrecOps &ops_fp64() {
-  static const PrecOps ops = make_ops<double, 0xF, true>();
+  static const PrecOps ops = with_adjoint<double, 0xF>(make_ops<double, 0xF, true>());
   return ops;
 }
 }  // namespace dgadv

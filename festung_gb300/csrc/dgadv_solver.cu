@@ -25,16 +25,8 @@ static bool g_tab_loaded[64][3][kMaxP + 1];
 // C-ABI
 using namespace dgadv;
 
-#define DG_CUDA(call)                                                               \
-  do {                                                                              \
-    cudaError_t e_ = (call);                                                        \
-    if (e_ != cudaSuccess) {                                                        \
-      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);                  \
-      return DGADV_ECUDA;                                                           \
-    }                                                                               \
-  } while (0)
 
-static int dev_alloc(dgadv_handle *h, void **p, size_t bytes) {
+int dgadv::dev_alloc(dgadv_handle *h, void **p, size_t bytes) {
   if (bytes == 0) bytes = 16;
   cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) { h->err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return DGADV_ENOMEM; }
@@ -42,21 +34,24 @@ static int dev_alloc(dgadv_handle *h, void **p, size_t bytes) {
   return DGADV_OK;
 }
 
-static int upload(dgadv_handle *h, void *dst, const void *src, size_t bytes) {
+int dgadv::upload(dgadv_handle *h, void *dst, const void *src, size_t bytes) {
   DG_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
   return DGADV_OK;
 }
 
-static const PrecOps &ops(const dgadv_handle *h) {
+namespace dgadv {
+const PrecOps &ops_of(const dgadv_handle *h) {
   switch (h->prec) {
     case DGADV_FP64: return ops_fp64();
     case DGADV_FP32: return ops_fp32();
     default: return h->p <= 1 ? ops_df32_p01() : h->p == 2 ? ops_df32_p2() : ops_df32_p3();
   }
 }
+}  // namespace dgadv
+static const PrecOps &ops(const dgadv_handle *h) { return ops_of(h); }
 
 // Host FP64 values converted to the handle's stored reals and copied to the device.
-static int upload_real(dgadv_handle *h, void *dst, const std::vector<double> &src) {
+int dgadv::upload_real(dgadv_handle *h, void *dst, const std::vector<double> &src) {
   const PrecOps &o = ops(h);
   std::vector<unsigned char> tmp(src.size() * o.realBytes);
   o.to_real(src.data(), src.size(), tmp.data());
@@ -281,12 +276,12 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   return DGADV_OK;
 }
 
-extern "C" int dgadv_set_velocity(dgadv_handle *h, const double *u1, const double *u2, const double *vN) {
-  if (!h || !u1 || !u2 || !vN) return DGADV_EINVAL;
-  DG_CUDA(cudaSetDevice(h->device));
+void dgadv::velocity_factors(const dgadv_handle *h, const double *u1, const double *u2, const double *vN,
+                             std::vector<double> &F, std::vector<double> &Vn) {
   const int K = h->K, Kp = h->Kp, N = h->N, Q = h->Q, R = h->R;
   const RefTables &t = h->tables;
-  std::vector<double> F(2 * (size_t)Q * Kp, 0.0), Vn(3 * (size_t)R * Kp, 0.0);
+  F.assign(2 * (size_t)Q * Kp, 0.0);
+  Vn.assign(3 * (size_t)R * Kp, 0.0);
   for (int k = 0; k < K; ++k) {
     const int e = h->permv[k];
     const double B11 = h->Bhost[4 * (size_t)k], B12 = h->Bhost[4 * (size_t)k + 1];
@@ -308,6 +303,13 @@ extern "C" int dgadv_set_velocity(dgadv_handle *h, const double *u1, const doubl
             h->markNotN[3 * (size_t)k + n] ? h->areaE0T[3 * (size_t)k + n] * t.edge.W[r] * v / dj : 0.0;
       }
   }
+}
+
+extern "C" int dgadv_set_velocity(dgadv_handle *h, const double *u1, const double *u2, const double *vN) {
+  if (!h || !u1 || !u2 || !vN) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  std::vector<double> F, Vn;
+  velocity_factors(h, u1, u2, vN, F, Vn);
   int st;
   if ((st = upload_real(h, h->F, F))) return st;
   if ((st = upload_real(h, h->Vn, Vn))) return st;
@@ -329,6 +331,7 @@ extern "C" int dgadv_set_source_terms(dgadv_handle *h, int32_t nTerms, const int
   for (int m = 0; m < 4; ++m) h->timeFn[m] = m < nTerms ? timeFn[m] : 0;
   for (int i = 0; i < 3; ++i)
     if (h->graph[i]) { cudaGraphExecDestroy(h->graph[i]); h->graph[i] = nullptr; }
+  if (h->adjExec) { cudaGraphExecDestroy(h->adjExec); h->adjExec = nullptr; h->adjExecSteps = 0; }
   if (nTerms == 0) return DGADV_OK;
   std::vector<double> r((size_t)nTerms * N * Kp, 0.0), d((size_t)nTerms * 3 * Kp, 0.0);
   for (int m = 0; m < nTerms; ++m)
@@ -352,7 +355,7 @@ extern "C" int dgadv_set_state(dgadv_handle *h, const double *c) {
   if (!h || !c) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   DG_CUDA(cudaMemcpyAsync(h->stage_ext, c, (size_t)h->N * h->K * 8, cudaMemcpyHostToDevice, h->stream));
-  DG_CUDA(ops(h).scatter_in(h));
+  DG_CUDA(ops(h).scatter_in(h, h->cn));
   DG_CUDA(cudaStreamSynchronize(h->stream));
   return DGADV_OK;
 }
@@ -371,7 +374,7 @@ extern "C" int dgadv_sync(dgadv_handle *h) {
 extern "C" int dgadv_get_state(dgadv_handle *h, double *c) {
   if (!h || !c) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
-  DG_CUDA(ops(h).gather_out(h));
+  DG_CUDA(ops(h).gather_out(h, h->cn));
   DG_CUDA(cudaMemcpyAsync(c, h->stage_ext, (size_t)h->N * h->K * 8, cudaMemcpyDeviceToHost, h->stream));
   return dgadv_sync(h);
 }
@@ -514,6 +517,7 @@ extern "C" void dgadv_destroy(dgadv_handle *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (int i = 0; i < 3; ++i)
     if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+  if (h->adjExec) cudaGraphExecDestroy(h->adjExec);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (void *p : h->allocs) cudaFree(p);

@@ -114,6 +114,32 @@ class DeviceSolver:
         self._c(self._lib.dgadv_kernels_per_step(self._h, ctypes.byref(n)))
         return n.value
 
+    # ---- discrete adjoint -------------------------------------------------------------------
+    def set_velocity_modes(self, u1Modes, u2Modes, vNModes):
+        """Velocity modes u_m: u1Modes, u2Modes K x N x M, vNModes K x 3 x R x M."""
+        u1, u2, vn = L.f64(u1Modes), L.f64(u2Modes), L.f64(vNModes)
+        M = u1.shape[-1]
+        assert u1.shape == (self.K, self.N, M) and u2.shape == u1.shape and vn.shape[:2] == (self.K, 3)
+        self.nModes = M
+        self._c(self._lib.dgadv_set_velocity_modes(self._h, M, L.ptr(u1), L.ptr(u2), L.ptr(vn)))
+
+    def set_velocity_theta(self, theta):
+        th = L.f64(theta)
+        self._c(self._lib.dgadv_set_velocity_theta(self._h, L.ptr(th)))
+
+    def forward_record(self, nSteps, tau, nSnapshots=0):
+        self._c(self._lib.dgadv_forward_record(self._h, int(nSteps), float(tau), int(nSnapshots)))
+
+    def backward(self, dJdcT, want_theta=True):
+        """(dJ/dc0 K x N, dJ/dtheta) for the last recorded run."""
+        g = L.f64(dJdcT)
+        assert g.shape == (self.K, self.N)
+        g0 = np.zeros((self.K, self.N), order='F')
+        gt = np.zeros(getattr(self, 'nModes', 0)) if want_theta else None
+        self._c(self._lib.dgadv_backward(self._h, L.ptr(g), L.ptr(g0),
+                                         L.ptr(gt) if gt is not None and gt.size else None))
+        return g0, gt
+
     def close(self):
         if self._h:
             self._lib.dgadv_destroy(self._h)

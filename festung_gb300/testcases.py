@@ -87,6 +87,27 @@ def streamfunction_velocity(k, l, a):
     return u1, u2
 
 
+# Velocity modes of the adjoint workload: psi_m = sin(k_m pi x) sin(l_m pi y), (k_m, l_m) in
+# {1..4}^2 (u . n = 0 on the unit square's boundary).
+ADJOINT_MODES = [(k, l) for k in (1, 2, 3, 4) for l in (1, 2, 3, 4)]
+
+
+def adjoint_params(seed):
+    """Coefficients of the adjoint workload's streamfunction psi = sum_m theta_m psi_m: base
+    theta ~ N(0, 0.1^2); the target run adds N(0, 0.05^2) to 8 of the 16 modes (seeded)."""
+    rng = np.random.default_rng(seed)
+    theta = rng.normal(0.0, 0.1, size=len(ADJOINT_MODES))
+    idx = rng.choice(len(ADJOINT_MODES), size=8, replace=False)
+    dtheta = np.zeros(len(ADJOINT_MODES))
+    dtheta[idx] = rng.normal(0.0, 0.05, size=8)
+    return dict(theta=theta, dtheta=dtheta)
+
+
+def mode_velocity(m):
+    k, l = ADJOINT_MODES[m]
+    return streamfunction_velocity([k], [l], [1.0])
+
+
 def configure(pd):
     """Sets c0Cont, u1Cont, u2Cont (time-independent), fTerms, cDTerms, mesh parameters."""
     tc = pd['testcase']
@@ -134,6 +155,14 @@ def configure(pd):
         pd['u1Cont'], pd['u2Cont'] = streamfunction_velocity(prm['k'], prm['l'], prm['a'])
         cx, cy = prm['centre']; w2 = prm['width'] ** 2
         pd['c0Cont'] = lambda x1, x2: np.exp(-((x1 - cx) ** 2 + (x2 - cy) ** 2) / w2)
+    elif tc == 'adjoint':
+        pd['isAnalytical'] = False
+        prm = adjoint_params(pd.get('adjointSeed', 0))
+        theta = prm['theta'] + (prm['dtheta'] if pd.get('adjointTarget', False) else 0.0)
+        pd['theta'] = theta
+        pd['u1Cont'], pd['u2Cont'] = streamfunction_velocity([k for k, _ in ADJOINT_MODES],
+                                                             [l for _, l in ADJOINT_MODES], theta)
+        pd['c0Cont'] = lambda x1, x2: np.exp(-((x1 - 0.4) ** 2 + (x2 - 0.45) ** 2) / 0.01)
     else:
         raise ValueError('Invalid testcase "%s".' % tc)
     return pd

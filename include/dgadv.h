@@ -167,6 +167,37 @@ const char *dgadv_last_error(const dgadv_handle *h);
 const char *dgadv_status_string(int status);
 void dgadv_destroy(dgadv_handle *h);
 
+/* ---- discrete adjoint ------------------------------------------------------------------
+ * Gradients of a functional J(c(T)) of the final state of an unlimited run with respect to the
+ * initial coefficients and to the coefficients theta of a velocity u = sum_m theta_m u_m.  The
+ * reference has no adjoint; these follow the torch.autograd.Function contract (forward records,
+ * backward maps dJ/dc(T) to the input gradients).  The upwind choice is frozen at the recorded
+ * velocity (the flux is piecewise linear in u); right-hand-side vectors set with
+ * dgadv_set_source_terms are treated as independent of theta. */
+
+/* Velocity modes u_m, each given like dgadv_set_velocity: u1Modes, u2Modes K x N x nModes,
+ * vNModes K x 3 x R x nModes. */
+int dgadv_set_velocity_modes(dgadv_handle *h, int32_t nModes, const double *u1Modes,
+                             const double *u2Modes, const double *vNModes);
+/* Sets the velocity to sum_m theta[m] u_m (replaces dgadv_set_velocity). */
+int dgadv_set_velocity_theta(dgadv_handle *h, const double *theta);
+/* Runs nSteps steps from the current state (steps 1..nSteps, t0 = 0) and keeps what
+ * dgadv_backward needs: nSnapshots <= 0 keeps every step state and every RK stage state (no
+ * recomputation; nSteps x ordRK state-sized buffers); nSnapshots >= nSteps keeps every step
+ * state (each reversed step recomputes its stages); otherwise nSnapshots states are placed by
+ * binomial checkpointing.  The final state is then the handle's state (dgadv_get_state).
+ * DGADV_EUNSUPPORTED with the limiter on or in DF32. */
+int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau, int32_t nSnapshots);
+/* Reverse sweep of the last recorded run: dJdcT (K x N) in, dJdc0 (K x N, may be NULL) and
+ * dJdtheta (nModes, may be NULL) out.  Recomputes what was not stored; the handle's state is
+ * the initial state afterwards.  One backward per recorded run. */
+int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc0, double *dJdtheta);
+/* The checkpointing schedule as pairs (action, argument): 0 restore slot, 1 advance n steps,
+ * 2 store slot, 3 reverse step; *backwardStart = first action of the reverse sweep.  With
+ * actions == NULL only *count is written.  Host only. */
+int dgadv_checkpoint_schedule(int32_t nSteps, int32_t nSnapshots, int32_t *actions, int32_t *count,
+                              int32_t *backwardStart);
+
 /* Largest vertex count dgadv_limit_linear_noalloc accepts (its fixed scratch: 4 MB per GPU). */
 #define DGADV_NOALLOC_MAX_VERTICES (1 << 18)
 

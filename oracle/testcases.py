@@ -5,8 +5,9 @@ Test infrastructure: see ``oracle/__init__.py``.
 'solid_body' and 'transient' restate advection/configureProblem.m:106-133 (LeVeque's solid-body
 rotation; the analytical transient case used by advection/doConvergenceTest.m).  'gauss_slot' is
 the rotating Gaussian hump plus slotted cylinder of the benchmark configurations, and
-'ensemble' the seeded random instance (streamfunction of 8 Fourier modes, Gaussian hump); both
-are new cases defined by formulas.  Meshes come from domainSquare
+'ensemble' the seeded random instance (streamfunction of 8 Fourier modes, Gaussian hump), and
+'adjoint' the gradient workload (streamfunction of 16 seeded modes, Gaussian hump); these are
+new cases defined by formulas.  Meshes come from domainSquare
 (advection/configureProblem.m:139-146 without the PDE toolbox), optionally with seeded jitter of
 the interior nodes.
 
@@ -71,6 +72,26 @@ def streamfunction_velocity(k, l, a):
     return u1, u2
 
 
+# Adjoint workload (a new item with no counterpart in the reference): streamfunction modes
+# psi_m = sin(k_m pi x) sin(l_m pi y), (k_m, l_m) in {1..4}^2.
+ADJOINT_MODES = [(k, l) for k in (1, 2, 3, 4) for l in (1, 2, 3, 4)]
+
+
+def adjoint_params(seed):
+    """Base coefficients theta ~ N(0, 0.1^2); the target run adds N(0, 0.05^2) to 8 modes."""
+    rng = np.random.default_rng(seed)
+    theta = rng.normal(0.0, 0.1, size=len(ADJOINT_MODES))
+    idx = rng.choice(len(ADJOINT_MODES), size=8, replace=False)
+    dtheta = np.zeros(len(ADJOINT_MODES))
+    dtheta[idx] = rng.normal(0.0, 0.05, size=8)
+    return dict(theta=theta, dtheta=dtheta)
+
+
+def mode_velocity(m):
+    k, l = ADJOINT_MODES[m]
+    return streamfunction_velocity([k], [l], [1.0])
+
+
 def configure_testcase(pd):
     tc = pd.testcase
     zero = lambda t, x1, x2: np.zeros(np.broadcast(x1, x2).shape)
@@ -132,6 +153,19 @@ def configure_testcase(pd):
         pd.cDCont = zero
         pd.gNCont = zero
         pd.generateGridData = lambda h: jittered_square(h, pd.jitter, prm['mesh_seed'])
+    elif tc == 'adjoint':
+        pd.isAnalytical = False
+        prm = adjoint_params(pd.get('adjointSeed', 0))
+        theta = prm['theta'] + (prm['dtheta'] if pd.get('adjointTarget', False) else 0.0)
+        pd.theta = theta
+        u1, u2 = streamfunction_velocity([k for k, _ in ADJOINT_MODES], [l for _, l in ADJOINT_MODES], theta)
+        pd.c0Cont = lambda x1, x2: np.exp(-((x1 - 0.4) ** 2 + (x2 - 0.45) ** 2) / 0.01)
+        pd.fCont = zero
+        pd.u1Cont = u1
+        pd.u2Cont = u2
+        pd.cDCont = zero
+        pd.gNCont = zero
+        pd.generateGridData = domainSquare
     else:
         raise ValueError('Invalid testcase "%s".' % tc)
     return pd

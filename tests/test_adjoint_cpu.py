@@ -1,0 +1,98 @@
+"""CPU checks of the adjoint's oracle and of the checkpointing schedule (no GPU).
+
+The oracle's gradients (reverse sweep with the transposed assembled operators) must match
+central finite differences of its own forward run, and its forward run must be the reference
+restatement's run; the checkpointing schedule must reverse every step once, in order, within
+its slots, and recompute no step more often than the binomial bound allows.
+"""
+import math
+
+import numpy as np
+import pytest
+
+KW = dict(hmax=2 ** -3, p=2, numSteps=8, tEnd=8 * 2e-4)
+
+
+@pytest.fixture(scope='module')
+def oracle_case():
+    from oracle import adjoint as OA
+    o = OA.AdjointOracle(**KW)
+    o.set_modes(OA.mode_velocities())
+    tgt = OA.AdjointOracle(adjointTarget=True, **KW)
+    c0 = o.pd.cDisc
+    cstar = tgt.forward(c0, KW['numSteps'])
+    cT = o.forward(c0, KW['numSteps'])
+    g0, gth = o.backward(cT - cstar)
+    return o, c0, cstar, g0, gth
+
+
+def test_oracle_forward_is_the_reference_run(oracle_case):
+    from oracle import advection as adv
+    o, c0, *_ = oracle_case
+    ref = adv.main(testcase='adjoint', **KW)
+    assert np.array_equal(o.forward(c0, KW['numSteps']), ref.cDisc)
+
+
+def test_oracle_gradient_matches_finite_differences(oracle_case):
+    o, c0, cstar, g0, gth = oracle_case
+    rng = np.random.default_rng(3)
+    h = 1e-6
+    J = lambda c: 0.5 * float(np.sum((o.forward(c, KW['numSteps']) - cstar) ** 2))
+    for _ in range(2):
+        d = rng.standard_normal(c0.shape)
+        fd = (J(c0 + h * d) - J(c0 - h * d)) / (2 * h)
+        assert abs(fd - np.sum(g0 * d)) <= 1e-7 * abs(fd)
+    th0 = o.pd.theta.copy()
+    for _ in range(2):
+        d = rng.standard_normal(th0.size)
+        o.set_theta(th0 + h * d)
+        Jp = J(c0)
+        o.set_theta(th0 - h * d)
+        Jm = J(c0)
+        fd = (Jp - Jm) / (2 * h)
+        assert abs(fd - gth @ d) <= 1e-7 * abs(fd)
+    o.set_theta(th0)
+
+
+def simulate(actions, start, nSteps):
+    """Runs the action list: returns the reversed steps, slots used, steps advanced per step.
+    The forward phase runs actions[:start] and then carries the state on to the last step."""
+    slots = {0: 0}
+    reversed_steps, used, advanced = [], {0}, np.zeros(nSteps, dtype=int)
+    w = 0
+    for i, (op, arg) in enumerate(actions):
+        if i == start:
+            w = nSteps
+        if op == 0:
+            w = slots[arg]
+        elif op == 1:
+            advanced[w:w + arg] += 1
+            w += arg
+        elif op == 2:
+            slots[arg] = w
+            used.add(arg)
+        else:
+            assert i >= start
+            assert w == arg, 'reverse step %d with the state of step %d' % (arg, w)
+            reversed_steps.append(arg)
+            w = arg + 1
+    return reversed_steps, used, advanced
+
+
+@pytest.mark.parametrize('nSteps,nSnap', [(1, 0), (7, 0), (10, 3), (20, 4), (200, 20), (50, 1), (33, 2)])
+def test_checkpoint_schedule_reverses_every_step_within_its_slots(lib, nSteps, nSnap):
+    from festung_gb300 import _lib as L
+    actions, start = L.checkpoint_schedule(nSteps, nSnap)
+    rev, used, advanced = simulate(actions, start, nSteps)
+    assert rev == list(range(nSteps - 1, -1, -1))
+    slots = nSteps if nSnap <= 0 or nSnap >= nSteps else nSnap
+    assert max(used) < slots
+    # binomial bound: no step advanced more than r times, beta(s, r) = C(s + r, s) >= nSteps
+    s = slots - 1
+    r = 1
+    while s > 0 and math.comb(s + r, s) < nSteps:
+        r += 1
+    if s > 0:
+        assert advanced.max() <= r
+    if slots == nSteps:
+        assert advanced.max() <= 1      # every state stored once, nothing recomputed

@@ -1,0 +1,131 @@
+"""GPU adjoint: gradients through the C-ABI against the oracle's transposed assembled operators
+and against central finite differences of the GPU forward run.
+
+Bars: FP64 relative L2 <= 1e-11 against the oracle (dJ/dc0 and dJ/dtheta; the reduction orders
+differ); FP64 finite differences (h = 1e-6) within 1e-7 of the adjoint's directional derivative;
+the checkpointed and stage-recomputing sweeps bitwise equal to the fully stored one; FP32
+within 1e-3 of FP64.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+
+
+def oracle_gradient(kw):
+    from oracle import adjoint as OA
+    o = OA.AdjointOracle(**kw)
+    o.set_modes(OA.mode_velocities())
+    tgt = OA.AdjointOracle(adjointTarget=True, **kw)
+    c0 = o.pd.cDisc
+    cstar = tgt.forward(c0, kw['numSteps'])
+    cT = o.forward(c0, kw['numSteps'])
+    g0, gth = o.backward(cT - cstar)
+    return c0, cstar, 0.5 * float(np.sum((cT - cstar) ** 2)), g0, gth
+
+
+CASES = [dict(hmax=2 ** -3, p=2, numSteps=10, tEnd=10 * 2e-4),
+         dict(hmax=2 ** -3, p=1, numSteps=10, tEnd=10 * 4e-4),
+         dict(hmax=2 ** -4, p=3, numSteps=6, tEnd=6 * 1e-4)]
+
+
+@pytest.mark.parametrize('kw', CASES, ids=['p2', 'p1', 'p3'])
+def test_fp64_gradient_matches_oracle(lib, kw):
+    from festung_gb300 import adjoint as AD
+    c0, cstar, Jo, og0, ogth = oracle_gradient(kw)
+    pd = AD.setup(precision='fp64', **kw)
+    try:
+        J, g0, gth = AD.misfit_gradient(pd, c0, pd.theta, cstar)
+    finally:
+        pd.solver.close()
+    assert abs(J - Jo) <= 1e-12 * Jo
+    assert rel(g0, og0) <= 1e-11
+    assert rel(gth, ogth) <= 1e-11
+
+
+def test_checkpointed_sweep_equals_stored_sweep(lib):
+    from festung_gb300 import adjoint as AD
+    kw = dict(hmax=2 ** -4, p=2, numSteps=30, tEnd=30 * 2e-4)
+    c0, cstar, *_ = oracle_gradient(dict(kw, numSteps=1, tEnd=2e-4))
+    pd = AD.setup(precision='fp64', **kw)
+    try:
+        ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
+        for snaps in (1, 3, 7, kw['numSteps']):   # binomial, and every state without the stages
+            got = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=snaps)
+            assert got[0] == ref[0]
+            assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
+    finally:
+        pd.solver.close()
+
+
+def test_fp64_gradient_matches_finite_differences(lib):
+    from festung_gb300 import adjoint as AD
+    kw = dict(hmax=2 ** -5, p=2, numSteps=60, tEnd=60 * 2e-4)
+    tg = AD.setup(precision='fp64', adjointTarget=True, **kw)
+    tg.solver.step(kw['numSteps'], 0, tg.tau)
+    cstar = tg.solver.get_state()
+    tg.solver.close()
+    pd = AD.setup(precision='fp64', **kw)
+    try:
+        c0 = np.asfortranarray(pd._cDisc)
+        J, g0, gth = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=8)
+        rng = np.random.default_rng(7)
+        h = 1e-6
+        for _ in range(3):
+            d = rng.standard_normal(c0.shape)
+            fd = (AD.misfit(pd, c0 + h * d, pd.theta, cstar) - AD.misfit(pd, c0 - h * d, pd.theta, cstar)) / (2 * h)
+            assert abs(fd - np.sum(g0 * d)) <= 1e-7 * abs(fd)
+            dt = rng.standard_normal(gth.size)
+            fd = (AD.misfit(pd, c0, pd.theta + h * dt, cstar) - AD.misfit(pd, c0, pd.theta - h * dt, cstar)) / (2 * h)
+            assert abs(fd - gth @ dt) <= 1e-7 * abs(fd)
+    finally:
+        pd.solver.close()
+
+
+def test_fp32_gradient_close_to_fp64(lib):
+    from festung_gb300 import adjoint as AD
+    kw = dict(hmax=2 ** -4, p=2, numSteps=40, tEnd=40 * 2e-4)
+    c0, cstar, *_ = oracle_gradient(dict(kw, numSteps=1, tEnd=2e-4))
+    out = {}
+    for prec in ('fp64', 'fp32'):
+        pd = AD.setup(precision=prec, **kw)
+        try:
+            out[prec] = AD.misfit_gradient(pd, c0, pd.theta, cstar)
+        finally:
+            pd.solver.close()
+    assert rel(out['fp32'][1], out['fp64'][1]) <= 1e-3
+    assert rel(out['fp32'][2], out['fp64'][2]) <= 1e-3
+
+
+def test_autograd_function_gives_the_adjoint_gradient(lib):
+    torch = pytest.importorskip('torch')
+    from festung_gb300 import adjoint as AD
+    kw = dict(hmax=2 ** -3, p=2, numSteps=10, tEnd=10 * 2e-4)
+    c0, cstar, Jo, og0, ogth = oracle_gradient(kw)
+    pd = AD.setup(precision='fp64', **kw)
+    try:
+        x = torch.tensor(np.ascontiguousarray(c0), dtype=torch.float64, requires_grad=True)
+        th = torch.tensor(pd.theta, dtype=torch.float64, requires_grad=True)
+        cT = AD.AdvectionSolve.apply(x, th, pd.solver, kw['numSteps'], pd.tau, 0)
+        J = 0.5 * ((cT - torch.from_numpy(np.ascontiguousarray(cstar))) ** 2).sum()
+        J.backward()
+        assert rel(x.grad.numpy(), og0) <= 1e-11
+        assert rel(th.grad.numpy(), ogth) <= 1e-11
+    finally:
+        pd.solver.close()
+
+
+def test_limited_runs_have_no_adjoint(lib):
+    from festung_gb300 import _lib as L
+    from festung_gb300 import adjoint as AD
+    pd = AD.setup(precision='fp64', hmax=2 ** -3, p=1, numSteps=2, tEnd=4e-4, isSlopeLim=True)
+    try:
+        with pytest.raises(L.DgadvError) as e:
+            pd.solver.forward_record(2, pd.tau, 0)
+        assert e.value.status == L.DGADV_EUNSUPPORTED
+    finally:
+        pd.solver.close()
