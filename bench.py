@@ -324,6 +324,53 @@ def adjoint_block(reps=3, fd_dirs=4):
     return out
 
 
+def ensemble_block(rank, world, device, n=256, steps=200, reps=3):
+    """The ensemble workload: n seeded instances (2048 to 32768 triangles, p in {1, 2}, their own
+    velocity fields), 200 steps in FP32 with the linear limiter; each degree group is one stacked
+    handle (one launch per stage kernel for all its instances), autotuned first.  Instances are
+    sharded across ranks with no exchange; whole-job DOF-stage/s = all ranks' work / the slowest
+    rank's time."""
+    import torch
+    from festung_gb300 import ensemble as E
+    t = time.perf_counter()
+    ens = E.Ensemble(E.shard(n, rank, world), precision='fp32', device=device, numSteps=steps)
+    setup_s = time.perf_counter() - t
+    tuned = ens.tune()
+    flush = torch.empty(512 * 2 ** 20, dtype=torch.uint8, device='cuda')
+    ens.step(steps)
+    ens.sync()
+    times = []
+    for _ in range(reps):
+        ens.reset()
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ens.step(steps)
+        ens.sync()
+        times.append(time.perf_counter() - t)
+    dt = min(times)
+    units = ens.dof_stages(steps)
+    if world > 1:
+        x = torch.tensor([dt, float(units)], dtype=torch.float64, device='cuda')
+        mx = x.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.SUM)
+        dt, units = float(mx[0]), float(x[1])
+    launches = {int(p): ens.solvers[p].kernels_per_step() for p in ens.solvers}
+    out = {'workload': 'ensemble: %d seeded instances, hmax in {2^-5,2^-6,2^-7} with 0.2 h jitter, p in {1,2}, '
+                       '8-mode streamfunction velocity, Gaussian hump, %d steps of 5e-4, FP32, linear limiter'
+                       % (n, steps),
+           'instances_this_rank': len(ens.seeds), 'dofs_this_rank': ens.dofs,
+           'value': units / dt, 'unit': 'DOF-stage/s', 'ms_per_solve': 1e3 * dt,
+           'groups': {int(p): {'instances': len(m), 'elements': int(sum(ens.problems[i].K for i in m)),
+                               'kernels_per_step': launches[p], 'tuned': tuned[p]}
+                      for p, m in ens.groups.items()},
+           'host_setup_s': setup_s, 'timing': 'wall clock of 200 steps on both group streams, after an '
+                                              'L2 flush; initial data reset and limited before each'}
+    ens.close()
+    return out
+
+
 def workload_config(wl, K, N, S, steps):
     kw = WORKLOADS[wl]
     return {'workload': '%s: domainSquare hmax=2^%d, K=%d triangles, p=%d (N=%d), SSP-RK%d, '
@@ -461,6 +508,11 @@ def run_ours(args):
             'value': within[best][0] if best else None,
             'speedup_vs_fp64': within[best][0] / result['fp64']['value'] if best else None}
 
+    if not args.no_ensemble:
+        ens = ensemble_block(rank, world, device)
+        if rank == 0:
+            result['ensemble'] = ens
+
     if rank == 0 and not args.no_adjoint:
         result['adjoint'] = adjoint_block()
 
@@ -489,6 +541,7 @@ def main():
     ap.add_argument('--no-fp64', action='store_true')
     ap.add_argument('--no-df32', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
+    ap.add_argument('--no-ensemble', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-stages', type=int, default=1)
     ap.add_argument('--ref-stages-per-step', type=int, default=1)

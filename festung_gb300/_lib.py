@@ -16,6 +16,7 @@ FP64, FP32, DF32 = 0, 1, 2
 LIM_LINEAR, LIM_HIERARCH_VERT, LIM_STRICT = 0, 1, 2
 TIME_CONST, TIME_EXP_NEG = 0, 1
 FLAG_NO_REORDER, FLAG_NO_SHIFT, FLAG_NO_GRAPH, FLAG_NO_PDL, FLAG_FUSE = 1, 2, 4, 8, 16
+OPT_GRAPH_STEPS, OPT_FLAGS = 1, 2
 
 LIMITER_TYPES = {'linear': LIM_LINEAR, 'hierarch_vert': LIM_HIERARCH_VERT, 'strict': LIM_STRICT}
 
@@ -57,6 +58,8 @@ SYMBOLS = {
     'dgadv_basis_eval': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _dp, _dp, _dp, _dp]),
     'dgadv_create': (ctypes.c_int, [ctypes.POINTER(Mesh), ctypes.POINTER(Params),
                                     ctypes.POINTER(ctypes.c_void_p)]),
+    'dgadv_create_ensemble': (ctypes.c_int, [ctypes.POINTER(Mesh), ctypes.c_int32, ctypes.POINTER(Params),
+                                             ctypes.POINTER(ctypes.c_void_p)]),
     'dgadv_set_velocity': (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp]),
     'dgadv_set_source_terms': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _i32p, _dp, _dp]),
     'dgadv_set_state': (ctypes.c_int, [ctypes.c_void_p, _dp]),
@@ -64,6 +67,8 @@ SYMBOLS = {
     'dgadv_limit_state': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     'dgadv_step': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double]),
     'dgadv_sync': (ctypes.c_int, [ctypes.c_void_p]),
+    'dgadv_set_option': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+    'dgadv_get_option': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _i32p]),
     'dgadv_kernels_per_step': (ctypes.c_int, [ctypes.c_void_p, _i32p]),
     'dgadv_time_steps': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _dp]),
     'dgadv_profile_kernels': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,

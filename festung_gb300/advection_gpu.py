@@ -169,8 +169,10 @@ def configureProblem(pd):
     return pd
 
 
-def preprocessProblem(pd):
-    """advection/preprocessProblem.m:48-112: grid, markers, tables; device upload."""
+def host_preprocess(pd):
+    """The host part of advection/preprocessProblem.m:48-112: grid, markers, tables, velocity
+    data (advection/preprocessSubStep.m:72-79, time-independent) and the separable
+    right-hand-side terms; no device work."""
     coordV, V0T, dim, h = TC.square_coords(pd.hmax)
     coordV = TC.jitter_coords(coordV, h, pd.jitter, pd.meshSeed)
     g = L.grid_build(coordV, V0T)
@@ -190,16 +192,9 @@ def preprocessProblem(pd):
     _, _, W = tables.rule2(qv)
     P = tables.phi2D(qv)
     pd.hatM = (W[:, None] * P).T @ P
-    pd.solver = DeviceSolver(coordV, V0T, pd.p, pd.ordRK, precision=pd.precision,
-                             isSlopeLim=pd.isSlopeLim, typeSlopeLim=pd.typeSlopeLim,
-                             idE0T=g['idE0T'], markE0TbdrD=g['markE0TbdrD'],
-                             markE0TbdrN=g['markE0TbdrN'], device=pd.device, flags=pd.gpuFlags)
-    # velocity data of advection/preprocessSubStep.m:72-79 (time-independent)
-    u1Disc = project(g, tables, pd.u1Cont, 2 * pd.p, pd.hatM)
-    u2Disc = project(g, tables, pd.u2Cont, 2 * pd.p, pd.hatM)
-    vN = normal_velocity(g, tables, pd.u1Cont, pd.u2Cont, 2 * pd.p + 1)
-    pd.u1Disc, pd.u2Disc, pd.vNormalOnQuadEdge = u1Disc, u2Disc, vN
-    pd.solver.set_velocity(u1Disc, u2Disc, vN)
+    pd.u1Disc = project(g, tables, pd.u1Cont, 2 * pd.p, pd.hatM)
+    pd.u2Disc = project(g, tables, pd.u2Cont, 2 * pd.p, pd.hatM)
+    pd.vNormalOnQuadEdge = normal_velocity(g, tables, pd.u1Cont, pd.u2Cont, 2 * pd.p + 1)
     # separable right-hand-side terms rhs_m = M f_m - K_D,m  (K_N = 0: no Neumann data)
     terms = {}
     detJ = g['detJ0T']
@@ -209,12 +204,33 @@ def preprocessProblem(pd):
             detJ[:, None] * (fd @ pd.hatM.T)
     for fn, f in pd.cDTerms:
         e = terms.setdefault(fn, [np.zeros((pd.K, pd.N)), np.zeros((pd.K, 3))])
-        e[0][...] -= dirichlet_vector(g, tables, g['markE0TbdrD'], f, vN, pd.qOrd)
+        e[0][...] -= dirichlet_vector(g, tables, g['markE0TbdrD'], f, pd.vNormalOnQuadEdge, pd.qOrd)
         e[1][...] += vertex_values(g, f)
     codes = {'const': L.TIME_CONST, 'exp_neg': L.TIME_EXP_NEG}
     names = sorted(terms)
-    pd.solver.set_source_terms([codes[n] for n in names], [terms[n][0] for n in names],
-                               [terms[n][1] for n in names] if pd.cDTerms else None)
+    pd.srcTimeFn = [codes[n] for n in names]
+    pd.srcRhs = [terms[n][0] for n in names]
+    pd.srcCD = [terms[n][1] for n in names] if pd.cDTerms else None
+    return pd
+
+
+def instance_mesh(pd):
+    """The mesh of one problem as DeviceSolver takes it (also one instance of an ensemble)."""
+    g = pd.g
+    return dict(coordV=g['coordV'], V0T=g['V0T'], idE0T=g['idE0T'], markE0TbdrD=g['markE0TbdrD'],
+                markE0TbdrN=g['markE0TbdrN'])
+
+
+def preprocessProblem(pd):
+    """advection/preprocessProblem.m:48-112: grid, markers, tables; device upload."""
+    host_preprocess(pd)
+    m = instance_mesh(pd)
+    pd.solver = DeviceSolver(m['coordV'], m['V0T'], pd.p, pd.ordRK, precision=pd.precision,
+                             isSlopeLim=pd.isSlopeLim, typeSlopeLim=pd.typeSlopeLim,
+                             idE0T=m['idE0T'], markE0TbdrD=m['markE0TbdrD'],
+                             markE0TbdrN=m['markE0TbdrN'], device=pd.device, flags=pd.gpuFlags)
+    pd.solver.set_velocity(pd.u1Disc, pd.u2Disc, pd.vNormalOnQuadEdge)
+    pd.solver.set_source_terms(pd.srcTimeFn, pd.srcRhs, pd.srcCD)
     return pd
 
 

@@ -1,0 +1,72 @@
+"""Launch-configuration autotuner.
+
+For one handle (one mesh, or one degree group of an ensemble) it times the launch
+configurations this library has and keeps the fastest:
+- the limiter pipeline: separate passes, or the fused one (linear limiter, zero Dirichlet data);
+- programmatic dependent launch on or off;
+- the number of time steps per captured CUDA graph.
+Each candidate runs ``nSteps`` steps of the handle's own problem after one warm-up call, timed
+with CUDA events on the handle's stream; the state is restored afterwards.  The choice can be
+kept in a JSON file keyed by the problem's signature and the GPU name, and reused.
+
+Fixed by design and not tuned: 128 elements per CTA (the row unit of the TMA bulk copies and the
+padding of every per-element array) and one thread per element.
+"""
+import json
+import os
+
+from . import _lib as L
+
+GRAPH_STEPS = (4, 12, 24, 48)
+
+
+def candidates(solver, fused_ok):
+    out = []
+    for fuse in ((False, True) if fused_ok else (False,)):
+        for pdl in (True, False):
+            for gs in GRAPH_STEPS:
+                flags = (L.FLAG_FUSE if fuse else 0) | (0 if pdl else L.FLAG_NO_PDL)
+                out.append(dict(flags=flags, graphSteps=gs))
+    return out
+
+
+def signature(solver, tau, precision, extra=''):
+    import torch
+    name = torch.cuda.get_device_name(0) if torch.cuda.is_available() else 'cpu'
+    return '%s|K=%d|p=%d|%s|%s|tau=%g%s' % (name, solver.K, solver.p, precision, solver.limiter, tau, extra)
+
+
+def tune(solver, tau, nSteps=48, reps=3, fused_ok=False, cache=None, key=None):
+    """Times every candidate on `solver` and applies the fastest; returns (best, table).
+    `cache`: optional JSON path; with `key`, a stored choice is applied without timing."""
+    if cache and key and os.path.exists(cache):
+        with open(cache) as f:
+            stored = json.load(f)
+        if key in stored:
+            best = stored[key]['best']
+            solver.set_option(L.OPT_FLAGS, best['flags'])
+            solver.set_option(L.OPT_GRAPH_STEPS, best['graphSteps'])
+            return best, stored[key]['table']
+    state = solver.get_state()
+    table = []
+    for c in candidates(solver, fused_ok):
+        solver.set_option(L.OPT_FLAGS, c['flags'])
+        solver.set_option(L.OPT_GRAPH_STEPS, c['graphSteps'])
+        solver.set_state(state)
+        solver.time_steps(nSteps, 0, tau)                 # warm-up: graph capture, first launches
+        ms = min(solver.time_steps(nSteps, 0, tau) for _ in range(reps))
+        table.append(dict(c, ms_per_step=ms / nSteps))
+    best = min(table, key=lambda r: r['ms_per_step'])
+    best = dict(flags=best['flags'], graphSteps=best['graphSteps'], ms_per_step=best['ms_per_step'])
+    solver.set_option(L.OPT_FLAGS, best['flags'])
+    solver.set_option(L.OPT_GRAPH_STEPS, best['graphSteps'])
+    solver.set_state(state)
+    if cache and key:
+        stored = {}
+        if os.path.exists(cache):
+            with open(cache) as f:
+                stored = json.load(f)
+        stored[key] = dict(best=best, table=table)
+        with open(cache, 'w') as f:
+            json.dump(stored, f, indent=1)
+    return best, table

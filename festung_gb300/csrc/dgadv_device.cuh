@@ -292,15 +292,22 @@ template <typename T> __host__ __device__ constexpr typename KeyOf<T>::type vkey
 template <typename T> struct LimOut {
   typename KeyOf<T>::type *vkeys;   // nc x 2 x Vp vertex min / max keys of this pass
   typename KeyOf<T>::type *vreset;  // the next pass's vertex keys, reset here
-  unsigned long long *slots;        // kSlotCopies x 2 x nc encoded global min / max (atomic)
-  unsigned long long *reset;        // slots of the next pass, reset by block 0
+  unsigned long long *slots;        // nInst x kSlotCopies x 2 x nc encoded global min / max (atomic)
+  unsigned long long *reset;        // slots of the next pass, reset by the grid
   int nc, type;
 };
 template <typename T> struct LimIn {
   const typename KeyOf<T>::type *vkeys;
-  const unsigned long long *slots;  // kSlotCopies x 2 x nc
+  const unsigned long long *slots;  // nInst x kSlotCopies x 2 x nc
   int nc, type, shift;
 };
+
+// Offset of this block's instance in a slot set (each instance of an ensemble has its own
+// global extremes, as each reference problem has).
+template <typename T>
+__device__ __forceinline__ size_t slot_base(const Geo<T> &g, int nc) {
+  return g.instOf ? (size_t)g.instOf[blockIdx.x] * kSlotCopies * 2 * nc : 0;
+}
 
 // Scatter of the element's centroid quantities to its vertices and the block's global extremes.
 template <typename T, int NQ>
@@ -339,14 +346,14 @@ __device__ __forceinline__ void scatter_quantities(const Geo<T> &g, const LimOut
 #pragma unroll
     for (int w = 1; w < kBlock / 32; ++w) { mn = fmin(mn, red[w][2 * s]); mx = fmax(mx, red[w][2 * s + 1]); }
     if (mn <= mx) {
-      unsigned long long *sl = lo.slots + (size_t)(blockIdx.x % kSlotCopies) * 2 * lo.nc;
+      unsigned long long *sl = lo.slots + slot_base(g, lo.nc) + (size_t)(blockIdx.x % kSlotCopies) * 2 * lo.nc;
       atomicMin(&sl[2 * s], okey(mn));
       atomicMax(&sl[2 * s + 1], okey(mx));
     }
   }
 }
 
-// Reset of the next pass's vertex keys (thread t owns vertex t) and global slots (block 0).
+// Reset of the next pass's vertex keys (thread t owns vertex t) and global slots (grid-stride).
 template <typename T>
 __device__ __forceinline__ void reset_next(const Geo<T> &g, const LimOut<T> &lo, int t) {
   if (t < g.numV)
@@ -354,9 +361,9 @@ __device__ __forceinline__ void reset_next(const Geo<T> &g, const LimOut<T> &lo,
       lo.vreset[(size_t)(2 * s) * g.Vp + t] = vkey_max<T>();
       lo.vreset[(size_t)(2 * s + 1) * g.Vp + t] = 0;
     }
-  if (blockIdx.x == 0)
-    for (int i = threadIdx.x; i < kSlotCopies * 2 * lo.nc; i += blockDim.x)
-      lo.reset[i] = (i & 1) ? 0ULL : key_max<T>();
+  const int nSlots = (g.instOf ? g.nInst : 1) * kSlotCopies * 2 * lo.nc;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nSlots; i += gridDim.x * blockDim.x)
+    lo.reset[i] = (i & 1) ? 0ULL : key_max<T>();
 }
 
 // Global extremes of every quantity from the kSlotCopies copies (warp 0), turned into the shift
@@ -865,7 +872,7 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
     stage_T(smem, rC0, c0, N, Kp, k0, bar);
     stage_T(smem, rC, cin, N, Kp, k0, bar);
   }
-  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
   VKeys<T, NQ> kv;
   load_vkeys<T, NQ>(g, li, vid, kv);
   __syncthreads();
@@ -943,7 +950,7 @@ k_limit(const Geo<T> g, const T *tbuf, T *__restrict__ out, const LimIn<T> li,
   if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
   pdl_wait();
   if (t == 0) stage_T(smem, 0, tbuf, N, Kp, k0, bar);
-  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
   VKeys<T, NQ> kv;
   load_vkeys<T, NQ>(g, li, vid, kv);
   __syncthreads();
@@ -1050,7 +1057,7 @@ k_limit_dot_lin(const Geo<T> g, const T *cin, const T *c0, const T *tbuf,
     stage_T(smem, rC0, c0, N, Kp, k0, bar);
     stage_T(smem, rC, cin, N, Kp, k0, bar);
   }
-  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
   VKeys<T, NQ> kv;
   load_vkeys<T, NQ>(g, li, vid, kv);
   __syncthreads();
@@ -1113,7 +1120,7 @@ k_limit_lin(const Geo<T> g, const T *cbuf, T *out, const LimIn<T> li,
     }
   }
   pdl_wait();
-  if (li.shift) load_shifts<T>(li.slots, li.nc, sh);
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
   T c[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) c[i] = active ? cbuf[(size_t)i * Kp + k] : T(0);
@@ -1262,7 +1269,7 @@ k_op_fused(const Geo<T> g, const T *x, int limitIn, T *xLout,
       kvNb[n].v[0][1][m] = mm == 0 ? k3max : kvOwn.v[0][1][ours];
     }
   }
-  if (li.shift && limitIn) load_shifts<T>(li.slots, li.nc, sh);
+  if (li.shift && limitIn) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
   __syncthreads();
   const bool ok = mbar_wait_bounded(bar, sc.flag);
   T q0 = T(0);

@@ -28,11 +28,15 @@ struct dgadv_handle {
   // device arrays (element type depends on prec)
   void *F = nullptr, *Vn = nullptr, *Bm = nullptr, *MT = nullptr, *rhs = nullptr, *cDV0T = nullptr;
   int *nbr = nullptr, *code = nullptr, *V0T = nullptr, *vptr = nullptr, *vidx = nullptr, *perm = nullptr;
+  int nInst = 1;                       // ensembles: instances (each its own limiter extremes)
+  int *instOf = nullptr;               // ensembles: instance of each block of kBlock elements
+  std::vector<int> instStart;          // first element of each instance (caller order), + K
   void *cn = nullptr, *cA = nullptr, *cB = nullptr, *tbuf = nullptr;
   void *cR = nullptr, *cnL = nullptr, *cLx = nullptr;   // fused path: raw step output, limited c^n / c^(s-1)
   void *vkeys = nullptr;               // 3 passes x nc x 2 x Vp vertex min / max keys
   unsigned long long *gmm = nullptr;   // 3 passes x kSlotCopies x 2 x nc encoded global extremes
   long long limPass = 1;               // limiter passes enqueued so far (selects key / slot set)
+  int graphSteps = 12;                 // time steps per captured CUDA graph
   int passesPerStep = 0;
   int *flag = nullptr;
   double *stage_ext = nullptr;         // K x N staging for set/get state

@@ -57,6 +57,8 @@ template <typename T> struct Geo {
   const T *cDV0T;    // nTerms x 3 x Kp   boundary values at the vertices
   int nTerms;
   int timeFn[4];
+  const int *instOf; // ensembles: instance of each block of kBlock elements (null: one instance)
+  int nInst;         // instances; each has its own global-extreme slots
 };
 
 struct LimArgs {

@@ -59,6 +59,8 @@ static Geo<T> make_geo(const dgadv_handle *h) {
   g.Bm = (const T *)h->Bm; g.MT = (const T *)h->MT; g.V0T = h->V0T; g.vptr = h->vptr; g.vidx = h->vidx;
   g.rhs = (const T *)h->rhs; g.cDV0T = (const T *)h->cDV0T; g.nTerms = h->nTerms;
   for (int i = 0; i < 4; ++i) g.timeFn[i] = h->timeFn[i];
+  g.instOf = h->instOf;
+  g.nInst = h->nInst;
   return g;
 }
 
@@ -81,8 +83,8 @@ static LimOut<T> lim_out(dgadv_handle *h) {
   LimOut<T> o;
   o.vkeys = (K_ *)h->vkeys + set * vset;
   o.vreset = (K_ *)h->vkeys + next * vset;
-  o.slots = h->gmm + (size_t)set * kSlotCopies * 2 * h->nc;
-  o.reset = h->gmm + (size_t)next * kSlotCopies * 2 * h->nc;
+  o.slots = h->gmm + (size_t)set * h->nInst * kSlotCopies * 2 * h->nc;
+  o.reset = h->gmm + (size_t)next * h->nInst * kSlotCopies * 2 * h->nc;
   o.nc = h->nc; o.type = h->limType;
   return o;
 }
@@ -92,7 +94,7 @@ static LimIn<T> lim_in_pass(const dgadv_handle *h, long long pass) {
   const int set = (int)(((pass % 3) + 3) % 3);
   LimIn<T> i;
   i.vkeys = (const K_ *)h->vkeys + (size_t)set * 2 * h->nc * h->Vp;
-  i.slots = h->gmm + (size_t)set * kSlotCopies * 2 * h->nc;
+  i.slots = h->gmm + (size_t)set * h->nInst * kSlotCopies * 2 * h->nc;
   i.nc = h->nc; i.type = h->limType;
   i.shift = (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1;
   return i;

@@ -70,7 +70,10 @@ static uint32_t morton2(uint32_t x, uint32_t y) {
   return spread(x) | (spread(y) << 1);
 }
 
-extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dgadv_handle **out) {
+// One handle over one mesh, or over the disjoint union of an ensemble's meshes: instStart holds
+// the first element of every instance and the total element count (empty: one instance).
+static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const std::vector<int> &instStart,
+                       dgadv_handle **out) {
   if (!out) return DGADV_EINVAL;
   *out = nullptr;
   if (!mesh || !prm) return DGADV_EINVAL;
@@ -101,23 +104,35 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   if (!build_grid(mesh->numV, mesh->coordV, mesh->numT, mesh->V0T, gr, h->err)) return DGADV_EMESH;
   if (!build_ref_tables(h->p, h->tables, h->err)) return DGADV_EINVAL;
   const int K = gr.numT, N = h->N;
-  h->K = K; h->Kp = (K + kBlock - 1) / kBlock * kBlock;   // whole blocks of rows for the bulk copies h->numV = gr.numV; h->Vp = (gr.numV + 63) / 64 * 64;
+  h->K = K; h->Kp = (K + kBlock - 1) / kBlock * kBlock;   // whole blocks of rows for the bulk copies
   h->Q = h->tables.Q; h->R = h->tables.R;
   const int Kp = h->Kp;
-  // element order on the device: Morton order of the barycentres
+  // instances: contiguous element ranges, each a whole number of blocks
+  h->instStart = instStart.empty() ? std::vector<int>{0, K} : instStart;
+  h->nInst = (int)h->instStart.size() - 1;
+  if (h->instStart.back() != K) { h->err = "instance ranges do not cover the elements"; return DGADV_EINVAL; }
+  for (int i = 0; i < h->nInst; ++i)
+    if (h->nInst > 1 && (h->instStart[i + 1] - h->instStart[i]) % kBlock != 0) {
+      h->err = "every ensemble instance needs a multiple of 128 elements";
+      return DGADV_EINVAL;
+    }
+  // element order on the device: Morton order of the barycentres within each instance
   std::vector<int> perm(K);
   std::iota(perm.begin(), perm.end(), 0);
   if (!(h->flags & DGADV_FLAG_NO_REORDER)) {
-    double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
-    for (int t = 0; t < K; ++t) {
-      xmin = std::min(xmin, gr.baryT[2 * t]); xmax = std::max(xmax, gr.baryT[2 * t]);
-      ymin = std::min(ymin, gr.baryT[2 * t + 1]); ymax = std::max(ymax, gr.baryT[2 * t + 1]);
+    for (int i = 0; i < h->nInst; ++i) {
+      const int t0 = h->instStart[i], t1 = h->instStart[i + 1];
+      double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+      for (int t = t0; t < t1; ++t) {
+        xmin = std::min(xmin, gr.baryT[2 * t]); xmax = std::max(xmax, gr.baryT[2 * t]);
+        ymin = std::min(ymin, gr.baryT[2 * t + 1]); ymax = std::max(ymax, gr.baryT[2 * t + 1]);
+      }
+      const double sx = 65535.0 / std::max(xmax - xmin, 1e-300), sy = 65535.0 / std::max(ymax - ymin, 1e-300);
+      std::vector<uint32_t> key(K);
+      for (int t = t0; t < t1; ++t)
+        key[t] = morton2((uint32_t)((gr.baryT[2 * t] - xmin) * sx), (uint32_t)((gr.baryT[2 * t + 1] - ymin) * sy));
+      std::stable_sort(perm.begin() + t0, perm.begin() + t1, [&](int a, int b) { return key[a] < key[b]; });
     }
-    const double sx = 65535.0 / std::max(xmax - xmin, 1e-300), sy = 65535.0 / std::max(ymax - ymin, 1e-300);
-    std::vector<uint32_t> key(K);
-    for (int t = 0; t < K; ++t)
-      key[t] = morton2((uint32_t)((gr.baryT[2 * t] - xmin) * sx), (uint32_t)((gr.baryT[2 * t + 1] - ymin) * sy));
-    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return key[a] < key[b]; });
   }
   std::vector<int> inv(K);
   for (int k = 0; k < K; ++k) inv[perm[k]] = k;
@@ -206,7 +221,7 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   if ((st = dev_alloc(h, &h->cnL, (size_t)N * Kp * w))) return st;
   if ((st = dev_alloc(h, &h->cLx, (size_t)N * Kp * w))) return st;
   if ((st = dev_alloc(h, &h->vkeys, 3 * 2 * (size_t)nc * h->Vp * kw))) return st;
-  if ((st = dev_alloc(h, (void **)&h->gmm, 3 * kSlotCopies * 2 * (size_t)nc * 8))) return st;
+  if ((st = dev_alloc(h, (void **)&h->gmm, 3 * (size_t)h->nInst * kSlotCopies * 2 * (size_t)nc * 8))) return st;
   if ((st = dev_alloc(h, (void **)&h->flag, 16))) return st;
   if ((st = dev_alloc(h, (void **)&h->stage_ext, (size_t)N * K * 8))) return st;
   DG_CUDA(cudaMemset(h->F, 0, 2 * (size_t)Q * Kp * w));
@@ -227,7 +242,7 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   }
   {
     // slots of pass 0 start reset; every later pass is reset by the previous producer
-    std::vector<unsigned long long> init(3 * kSlotCopies * 2 * (size_t)nc);
+    std::vector<unsigned long long> init(3 * (size_t)h->nInst * kSlotCopies * 2 * (size_t)nc);
     const unsigned long long kmax = ops(h).slotKeyMax;
     for (size_t i = 0; i < init.size(); ++i) init[i] = (i & 1) ? 0ULL : kmax;
     if ((st = upload(h, h->gmm, init.data(), init.size() * 8))) return st;
@@ -240,6 +255,15 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   if ((st = upload(h, h->vptr, vptr.data(), vptr.size() * 4))) return st;
   if ((st = upload(h, h->vidx, vidx.data(), vidx.size() * 4))) return st;
   if ((st = upload(h, h->perm, perm.data(), perm.size() * 4))) return st;
+  if (h->nInst > 1) {
+    // instance of every block a kernel may launch (grids cover max(K, numV) elements)
+    const int nBlocks = (std::max(Kp, h->Vp) + kBlock - 1) / kBlock + 1;
+    std::vector<int> instOf(nBlocks, 0);
+    for (int i = 0; i < h->nInst; ++i)
+      for (int t = h->instStart[i]; t < h->instStart[i + 1]; t += kBlock) instOf[t / kBlock] = i;
+    if ((st = dev_alloc(h, (void **)&h->instOf, instOf.size() * 4))) return st;
+    if ((st = upload(h, h->instOf, instOf.data(), instOf.size() * 4))) return st;
+  }
   if (h->limdot && h->limType == DGADV_LIM_LINEAR) {
     std::vector<double> qk;
     taylor_correction(gr, h->p, h->tables, qk);
@@ -274,6 +298,56 @@ extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dga
   }
   DG_CUDA(cudaDeviceSynchronize());
   return DGADV_OK;
+}
+
+extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dgadv_handle **out) {
+  return create_impl(mesh, prm, std::vector<int>(), out);
+}
+
+extern "C" int dgadv_create_ensemble(const dgadv_mesh *meshes, int32_t nInst, const dgadv_params *prm,
+                                     dgadv_handle **out) {
+  if (!out) return DGADV_EINVAL;
+  *out = nullptr;
+  if (!meshes || !prm || nInst < 1) return DGADV_EINVAL;
+  // the disjoint union of the instance meshes, instances in order
+  int nT = 0, nV = 0;
+  const bool hasId = meshes[0].idE0T, hasD = meshes[0].markE0TbdrD, hasN = meshes[0].markE0TbdrN;
+  for (int i = 0; i < nInst; ++i) {
+    const dgadv_mesh &m = meshes[i];
+    if (m.numT <= 0 || m.numV <= 0 || !m.coordV || !m.V0T) return DGADV_EINVAL;
+    if ((bool)m.idE0T != hasId || (bool)m.markE0TbdrD != hasD || (bool)m.markE0TbdrN != hasN) return DGADV_EINVAL;
+    nT += m.numT;
+    nV += m.numV;
+  }
+  std::vector<double> coordV(2 * (size_t)nV);
+  std::vector<int32_t> V0T(3 * (size_t)nT), idE0T(hasId ? 3 * (size_t)nT : 0);
+  std::vector<uint8_t> mD(hasD ? 3 * (size_t)nT : 0), mN(hasN ? 3 * (size_t)nT : 0);
+  std::vector<int> instStart(1, 0);
+  int t0 = 0, v0 = 0;
+  for (int i = 0; i < nInst; ++i) {
+    const dgadv_mesh &m = meshes[i];
+    for (int v = 0; v < m.numV; ++v) {
+      coordV[v0 + v] = m.coordV[v];
+      coordV[(size_t)nV + v0 + v] = m.coordV[(size_t)m.numV + v];
+    }
+    for (int n = 0; n < 3; ++n)
+      for (int t = 0; t < m.numT; ++t) {
+        const size_t src = (size_t)n * m.numT + t, dst = (size_t)n * nT + t0 + t;
+        V0T[dst] = m.V0T[src] + v0;
+        if (hasId) idE0T[dst] = m.idE0T[src];
+        if (hasD) mD[dst] = m.markE0TbdrD[src];
+        if (hasN) mN[dst] = m.markE0TbdrN[src];
+      }
+    t0 += m.numT;
+    v0 += m.numV;
+    instStart.push_back(t0);
+  }
+  dgadv_mesh u;
+  u.numT = nT; u.numV = nV; u.coordV = coordV.data(); u.V0T = V0T.data();
+  u.idE0T = hasId ? idE0T.data() : nullptr;
+  u.markE0TbdrD = hasD ? mD.data() : nullptr;
+  u.markE0TbdrN = hasN ? mN.data() : nullptr;
+  return create_impl(&u, prm, instStart, out);
 }
 
 void dgadv::velocity_factors(const dgadv_handle *h, const double *u1, const double *u2, const double *vN,
@@ -419,9 +493,9 @@ extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, doubl
     done = 1;
   }
   if (useGraph) {
-    // time-independent data: a captured graph of a chunk of steps, replayed.  The chunk makes a
-    // multiple of three limiter passes, so the pass phase is the same before and after it.
-    const int chunk = 12;
+    // time-independent data: a captured graph of a chunk of steps, replayed.  Graphs are kept per
+    // limiter-pass phase (pass count mod 3) at the chunk start, the key / slot set they use.
+    const int chunk = h->graphSteps;
     while (nSteps - done >= chunk) {
       const int ph = (int)(h->limPass % 3);
       if (!h->graph[ph] || h->graphTau[ph] != tau) {
@@ -452,6 +526,39 @@ extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, doubl
   }
   cudaError_t e = end_of_call(h);
   if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
+  return DGADV_OK;
+}
+
+static void drop_graphs(dgadv_handle *h) {
+  for (int i = 0; i < 3; ++i)
+    if (h->graph[i]) { cudaGraphExecDestroy(h->graph[i]); h->graph[i] = nullptr; }
+  if (h->adjExec) { cudaGraphExecDestroy(h->adjExec); h->adjExec = nullptr; h->adjExecSteps = 0; }
+}
+
+extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) {
+  if (!h) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  if (option == DGADV_OPT_GRAPH_STEPS) {
+    if (value < 1 || value > 256) return DGADV_EINVAL;
+    h->graphSteps = value;
+  } else if (option == DGADV_OPT_FLAGS) {
+    const int runtime = DGADV_FLAG_NO_GRAPH | DGADV_FLAG_NO_PDL | DGADV_FLAG_FUSE;
+    if (value & ~runtime) { h->err = "only NO_GRAPH, NO_PDL and FUSE change after creation"; return DGADV_EINVAL; }
+    if ((value & DGADV_FLAG_FUSE) && !ops(h).fused) { h->err = "no fused pipeline for this precision"; return DGADV_EUNSUPPORTED; }
+    h->flags = (h->flags & ~runtime) | value;
+  } else {
+    return DGADV_EINVAL;
+  }
+  drop_graphs(h);
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *value) {
+  if (!h || !value) return DGADV_EINVAL;
+  if (option == DGADV_OPT_GRAPH_STEPS) *value = h->graphSteps;
+  else if (option == DGADV_OPT_FLAGS) *value = h->flags;
+  else return DGADV_EINVAL;
   return DGADV_OK;
 }
 

@@ -1,0 +1,116 @@
+"""Ensembles of independent advection problems on one GPU (and sharded across ranks).
+
+The ensemble workload: seeded instances of the 'ensemble' test case.
+- Each instance draws its mesh level hmax in {2^-5, 2^-6, 2^-7} (2048 / 8192 / 32768
+  triangles), with interior nodes jittered by +-0.2 h.
+- It draws its degree p in {1, 2}.
+- Its velocity comes from a streamfunction of 8 random Fourier modes.
+- Its initial data is a Gaussian hump.
+- Every instance runs SSP-RK of order p + 1 (the reference's default,
+  advection/configureProblem.m:80), 200 steps of 5e-4, with the linear vertex-based limiter.
+
+The instances of one degree are stacked into one handle (``dgadv_create_ensemble``): every
+stage kernel then covers all of them in one launch, each instance keeping its own limiter
+extremes. The degree groups run on their own handles.
+
+``shard(n, rank, world)`` splits instances across ranks with no data exchange: each rank runs
+its own instances (weak scaling); results stay on their rank.
+"""
+import numpy as np
+
+from . import advection_gpu as G
+from . import testcases as TC
+from .solver import DeviceSolver
+
+STEPS, TAU = 200, 5e-4
+
+
+def shard(n, rank, world):
+    """Instances of this rank: i = rank, rank + world, ... (a balanced mix of sizes)."""
+    return list(range(rank, n, world))
+
+
+def instance_problem(seed, numSteps=STEPS, tau=TAU, **overrides):
+    """configureProblem + the host part of preprocessProblem for instance `seed`."""
+    prm = TC.ensemble_params(seed)
+    kw = dict(testcase='ensemble', instanceSeed=seed, hmax=prm['hmax'], p=prm['p'], numSteps=numSteps,
+              tEnd=numSteps * tau, isSlopeLim=True, typeSlopeLim='linear')
+    kw.update(overrides)
+    pd = G.Struct(kw)
+    pd.problemName = 'advection_gpu'
+    G.configureProblem(pd)
+    G.host_preprocess(pd)
+    pd.c0 = G.project(pd.g, pd.tables, pd.c0Cont, pd.qOrd, pd.hatM)
+    return pd
+
+
+class Ensemble:
+    """Instances grouped by degree, one stacked handle per group."""
+
+    def __init__(self, seeds, precision='fp32', device=0, flags=0, numSteps=STEPS, tau=TAU, **overrides):
+        self.seeds = list(seeds)
+        self.problems = [instance_problem(s, numSteps, tau, **overrides) for s in self.seeds]
+        self.numSteps, self.tau = numSteps, tau
+        self.groups = {}
+        for i, pd in enumerate(self.problems):
+            self.groups.setdefault(pd.p, []).append(i)
+        self.solvers = {}
+        for p, members in sorted(self.groups.items()):
+            pds = [self.problems[i] for i in members]
+            pd0 = pds[0]
+            s = DeviceSolver(None, None, p, pd0.ordRK, precision=precision, isSlopeLim=pd0.isSlopeLim,
+                             typeSlopeLim=pd0.typeSlopeLim, device=device, flags=flags,
+                             instances=[G.instance_mesh(pd) for pd in pds])
+            s.set_velocity(np.concatenate([pd.u1Disc for pd in pds]), np.concatenate([pd.u2Disc for pd in pds]),
+                           np.concatenate([pd.vNormalOnQuadEdge for pd in pds]))
+            self.solvers[p] = s
+        self.reset()
+
+    @property
+    def dofs(self):
+        return sum(pd.K * pd.N for pd in self.problems)
+
+    def dof_stages(self, nSteps):
+        return sum(pd.K * pd.N * pd.ordRK for pd in self.problems) * nSteps
+
+    def reset(self):
+        """Initial data of every instance, limited (advection/initializeProblem.m:56-67)."""
+        for p, members in self.groups.items():
+            s = self.solvers[p]
+            s.set_state(np.concatenate([self.problems[i].c0 for i in members]))
+            if self.problems[members[0]].isSlopeLim:
+                s.limit_state(0.0)
+
+    def step(self, nSteps, nStep0=0):
+        """Enqueues steps on every group's stream (the groups run concurrently)."""
+        for s in self.solvers.values():
+            s.step(nSteps, nStep0, self.tau)
+
+    def sync(self):
+        for s in self.solvers.values():
+            s.sync()
+
+    def states(self):
+        """Per-instance coefficient arrays (K x N), in seed order."""
+        out = [None] * len(self.problems)
+        for p, members in self.groups.items():
+            parts = self.solvers[p].split(self.solvers[p].get_state())
+            for i, c in zip(members, parts):
+                out[i] = np.array(c)
+        return out
+
+    def tune(self, nSteps=48, reps=3, cache=None):
+        """Autotunes every group's launch configuration (festung_gb300.autotune)."""
+        from . import autotune as AT
+        out = {}
+        for p, s in self.solvers.items():
+            pd0 = self.problems[self.groups[p][0]]
+            fused_ok = pd0.isSlopeLim and pd0.typeSlopeLim == 'linear' and s.precision != 'df32' and not pd0.cDTerms
+            key = AT.signature(s, self.tau, s.precision, '|ensemble:%d' % len(self.groups[p])) if cache else None
+            out[p] = AT.tune(s, self.tau, nSteps, reps, fused_ok=fused_ok, cache=cache, key=key)[0]
+        return out
+
+    def close(self):
+        for s in self.solvers.values():
+            s.close()
+        self.solvers = {}

@@ -15,41 +15,61 @@ class DeviceSolver:
 
     def __init__(self, coordV, V0T, p, ordRK, precision='fp64', isSlopeLim=False,
                  typeSlopeLim='linear', idE0T=None, markE0TbdrD=None, markE0TbdrN=None,
-                 device=0, flags=0):
+                 device=0, flags=0, instances=None):
+        """One mesh (coordV, V0T, markers), or an ensemble: ``instances`` a list of dicts with
+        keys coordV, V0T and optionally idE0T, markE0TbdrD, markE0TbdrN (coordV / V0T ignored);
+        the handle's arrays are then the instances' arrays stacked in order."""
         self._lib = L.load()
         self._h = None
-        self.coordV = L.f64(coordV)
-        self.V0T = np.require(np.asarray(V0T, dtype=np.int32), requirements=['F', 'A'])
-        self.K = self.V0T.shape[0]
-        self.N = (p + 1) * (p + 2) // 2
         self.p = p
-        keep = [self.coordV, self.V0T]
-        mesh = L.Mesh()
-        mesh.numT = self.K
-        mesh.numV = self.coordV.shape[0]
-        mesh.coordV = L.ptr(self.coordV)
-        mesh.V0T = L.ptr(self.V0T, L._i32p)
-        if idE0T is not None:
-            a = np.require(np.asarray(idE0T, dtype=np.int32), requirements=['F', 'A']); keep.append(a)
-            mesh.idE0T = L.ptr(a, L._i32p)
-        for name, m in (('markE0TbdrD', markE0TbdrD), ('markE0TbdrN', markE0TbdrN)):
-            if m is not None:
-                a = np.require(np.asarray(m, dtype=np.uint8), requirements=['F', 'A']); keep.append(a)
-                setattr(mesh, name, L.ptr(a, L._u8p))
+        self.N = (p + 1) * (p + 2) // 2
+        self._keep = []
+        meshes = instances if instances is not None else [dict(coordV=coordV, V0T=V0T, idE0T=idE0T,
+                                                                markE0TbdrD=markE0TbdrD,
+                                                                markE0TbdrN=markE0TbdrN)]
+        arr = (L.Mesh * len(meshes))()
+        self.instK = []
+        for m, mesh in zip(meshes, arr):
+            cv = L.f64(m['coordV'])
+            vt = np.require(np.asarray(m['V0T'], dtype=np.int32), requirements=['F', 'A'])
+            self._keep += [cv, vt]
+            mesh.numT = vt.shape[0]
+            mesh.numV = cv.shape[0]
+            mesh.coordV = L.ptr(cv)
+            mesh.V0T = L.ptr(vt, L._i32p)
+            self.instK.append(vt.shape[0])
+            if m.get('idE0T') is not None:
+                a = np.require(np.asarray(m['idE0T'], dtype=np.int32), requirements=['F', 'A']); self._keep.append(a)
+                mesh.idE0T = L.ptr(a, L._i32p)
+            for name in ('markE0TbdrD', 'markE0TbdrN'):
+                if m.get(name) is not None:
+                    a = np.require(np.asarray(m[name], dtype=np.uint8), requirements=['F', 'A']); self._keep.append(a)
+                    setattr(mesh, name, L.ptr(a, L._u8p))
+        self.K = int(sum(self.instK))
+        self.instStart = np.concatenate([[0], np.cumsum(self.instK)]).astype(np.int64)
         prm = L.Params()
         prm.p = p; prm.ordRK = ordRK
         prm.precision = {'fp64': L.FP64, 'fp32': L.FP32, 'df32': L.DF32}[precision]
+        self.limiter = typeSlopeLim if isSlopeLim else 'none'
+        self.precision = precision
         prm.isSlopeLim = 1 if isSlopeLim else 0
         prm.typeSlopeLim = L.LIMITER_TYPES[typeSlopeLim]
         prm.device = device; prm.flags = flags
         h = ctypes.c_void_p()
-        st = self._lib.dgadv_create(ctypes.byref(mesh), ctypes.byref(prm), ctypes.byref(h))
+        if instances is None:
+            st = self._lib.dgadv_create(arr, ctypes.byref(prm), ctypes.byref(h))
+        else:
+            st = self._lib.dgadv_create_ensemble(arr, len(meshes), ctypes.byref(prm), ctypes.byref(h))
         self._h = h.value
         if st != L.DGADV_OK:
             try:
                 L.check(st, self._h)
             finally:
                 self.close()
+
+    def split(self, a):
+        """Per-instance views of a stacked K x ... array."""
+        return [a[self.instStart[i]:self.instStart[i + 1]] for i in range(len(self.instK))]
 
     # -------------------------------------------------------------------------------------
     def _c(self, st):
@@ -108,6 +128,14 @@ class DeviceSolver:
         self._c(self._lib.dgadv_profile_kernels(self._h, int(nSteps), int(nStep0), float(tau),
                                                 L.ptr(ms), L.ptr(n, L._i32p)))
         return ms[:3], n[:3]
+
+    def set_option(self, option, value):
+        self._c(self._lib.dgadv_set_option(self._h, int(option), int(value)))
+
+    def get_option(self, option):
+        v = ctypes.c_int32()
+        self._c(self._lib.dgadv_get_option(self._h, int(option), ctypes.byref(v)))
+        return v.value
 
     def kernels_per_step(self):
         n = ctypes.c_int32()

@@ -54,6 +54,13 @@ enum {
                                   limiter inside the next stage's operator kernel            */
 };
 
+/* options of dgadv_set_option (launch configuration: graph length and dependent launch leave
+ * results bitwise unchanged; the fused pipeline changes them at the roundoff level) */
+enum {
+  DGADV_OPT_GRAPH_STEPS = 1,   /* time steps per captured CUDA graph, 1..256 (default 12)        */
+  DGADV_OPT_FLAGS = 2          /* the runtime flags NO_GRAPH, NO_PDL, FUSE                       */
+};
+
 /* ---- host helpers: static data ------------------------------------------------------- */
 
 /* Output of generateGridData (core/generateGridData.m:130-198).  Allocated by
@@ -121,6 +128,14 @@ typedef struct dgadv_handle dgadv_handle;
  * handle (so that dgadv_last_error can explain); release it with dgadv_destroy. */
 int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *params, dgadv_handle **out);
 
+/* An ensemble: one handle over the disjoint union of nInst meshes, so that every stage kernel
+ * covers all instances in one launch.  Each instance needs a multiple of 128 triangles and
+ * keeps its own limiter extremes (the reference's global shift is per problem).  The handle's
+ * arrays (cDisc, velocity data, ...) are the instances' arrays stacked in instance order.  The
+ * reference runs one problem at a time; this has no counterpart there. */
+int dgadv_create_ensemble(const dgadv_mesh *meshes, int32_t nInst, const dgadv_params *params,
+                          dgadv_handle **out);
+
 /* Velocity data of advection/preprocessSubStep.m:72-79: u1Disc, u2Disc (K x N, projections of
  * order 2p) and vNormalOnQuadEdge (K x 3 x R, order 2p+1).  Held until replaced. */
 int dgadv_set_velocity(dgadv_handle *h, const double *u1Disc, const double *u2Disc,
@@ -159,6 +174,11 @@ int dgadv_time_steps(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau
  * [0] stage operator, [1] time-derivative limiter + SSP, [2] solution limiter, [3] unused. */
 int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau,
                           double *msPerLaunch, int32_t *launches);
+
+/* Launch configuration of a handle (DGADV_OPT_*), e.g. as chosen by an autotuner.  Changing it
+ * drops the handle's captured graphs; the state is kept.  No counterpart in the reference. */
+int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value);
+int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *value);
 
 /* Number of kernels one time step launches (for launch accounting). */
 int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count);

@@ -1,0 +1,127 @@
+"""GPU ensembles: instances stacked into one handle per degree (one launch per stage kernel for
+all of them) give each instance exactly its own single-problem result.
+
+Bars: bitwise equal to the single-instance handle (FP32 and FP64: the same per-element
+arithmetic, the same vertex patches, the instance's own limiter extremes); FP64 relative L2
+<= 1e-12 against the oracle.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def single(seed, precision, **kw):
+    from festung_gb300 import advection_gpu as G
+    from festung_gb300 import testcases as TC
+    prm = TC.ensemble_params(seed)
+    args = dict(testcase='ensemble', instanceSeed=seed, hmax=prm['hmax'], p=prm['p'], isSlopeLim=True,
+                precision=precision)
+    args.update(kw)
+    pd = G.main(**args)
+    pd.solver.close()
+    return pd.cDisc
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'fp64'])
+def test_stacked_instances_equal_single_runs_bitwise(lib, precision):
+    from festung_gb300 import ensemble as E
+    seeds = list(range(6))
+    kw = dict(hmax=2 ** -4)                       # 512 triangles each, both degrees
+    ens = E.Ensemble(seeds, precision=precision, numSteps=12, tau=5e-4, **kw)
+    try:
+        assert len(ens.groups) == 2
+        ens.step(12)
+        got = ens.states()
+    finally:
+        ens.close()
+    for s, c in zip(seeds, got):
+        ref = single(s, precision, numSteps=12, tEnd=12 * 5e-4, **kw)
+        assert np.array_equal(c, ref), 'instance %d' % s
+
+
+def test_uneven_instances_equal_single_runs_bitwise(lib):
+    from festung_gb300 import ensemble as E
+    seeds = [0, 1, 2, 3]                          # the workload's own levels: 2048 to 32768 triangles
+    ens = E.Ensemble(seeds, precision='fp32', numSteps=8)
+    try:
+        sizes = sorted({pd.K for pd in ens.problems})
+        assert len(sizes) >= 2
+        ens.step(8)
+        got = ens.states()
+    finally:
+        ens.close()
+    for s, c in zip(seeds, got):
+        assert np.array_equal(c, single(s, 'fp32', numSteps=8, tEnd=8 * 5e-4)), 'instance %d' % s
+
+
+def test_fp64_ensemble_matches_oracle(lib):
+    from festung_gb300 import ensemble as E
+    from oracle import matfree as MF
+    seeds = [3, 4]
+    kw = dict(hmax=2 ** -4)
+    ens = E.Ensemble(seeds, precision='fp64', numSteps=10, tau=5e-4, **kw)
+    try:
+        ens.step(10)
+        got = ens.states()
+    finally:
+        ens.close()
+    from festung_gb300 import testcases as TC
+    for s, c in zip(seeds, got):
+        o = MF.main_matfree(testcase='ensemble', instanceSeed=s, hmax=kw['hmax'], p=TC.ensemble_params(s)['p'],
+                            numSteps=10, tEnd=10 * 5e-4, isSlopeLim=True).cDisc
+        assert np.linalg.norm(c - o) <= 1e-12 * np.linalg.norm(o)
+
+
+def test_instances_must_fill_whole_blocks(lib):
+    from festung_gb300 import _lib as L
+    from festung_gb300 import ensemble as E
+    with pytest.raises(L.DgadvError) as e:
+        E.Ensemble([0, 1], precision='fp32', numSteps=2, hmax=0.1)   # 200 triangles each
+    assert e.value.status == L.DGADV_EINVAL
+
+
+def test_graph_length_and_dependent_launch_leave_results_unchanged(lib):
+    from festung_gb300 import _lib as L
+    from festung_gb300 import ensemble as E
+    ens = E.Ensemble([0, 1, 2], precision='fp32', numSteps=30, hmax=2 ** -4)
+    try:
+        ens.step(30)
+        ref = ens.states()
+        for flags, gs in ((0, 1), (0, 7), (L.FLAG_NO_PDL, 24), (L.FLAG_NO_GRAPH, 12)):
+            for s in ens.solvers.values():
+                s.set_option(L.OPT_FLAGS, flags)
+                s.set_option(L.OPT_GRAPH_STEPS, gs)
+            ens.reset()
+            ens.step(30)
+            for a, b in zip(ens.states(), ref):
+                assert np.array_equal(a, b), (flags, gs)
+    finally:
+        ens.close()
+
+
+def test_autotuner_picks_a_measured_configuration(lib, tmp_path):
+    from festung_gb300 import _lib as L
+    from festung_gb300 import ensemble as E
+    ens = E.Ensemble([0, 1, 2, 3], precision='fp64', numSteps=24, hmax=2 ** -4)
+    try:
+        cache = str(tmp_path / 'tune.json')
+        best = ens.tune(nSteps=12, reps=2, cache=cache)
+        for p, b in best.items():
+            s = ens.solvers[p]
+            assert s.get_option(L.OPT_GRAPH_STEPS) == b['graphSteps']
+            assert s.get_option(L.OPT_FLAGS) & (L.FLAG_FUSE | L.FLAG_NO_PDL) == b['flags']
+        ens.reset()
+        ens.step(24)
+        tuned = ens.states()
+        again = ens.tune(cache=cache)                  # read back from the cache, no timing
+        assert again == best
+    finally:
+        ens.close()
+    ref = E.Ensemble([0, 1, 2, 3], precision='fp64', numSteps=24, hmax=2 ** -4)
+    try:
+        ref.step(24)
+        for a, b in zip(tuned, ref.states()):
+            assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(b)   # the fused pipeline: roundoff
+    finally:
+        ref.close()
