@@ -553,6 +553,43 @@ __device__ __forceinline__ void patch_minmax(const LimIn<T> &li, const VKeys<T, 
 
 // Limit Taylor coefficients in place (linear / hierarchical vertex).  dataV0T: boundary values
 // at the three vertices for Dirichlet vertices (NaN means "no data").
+// Taylor basis functions of core/phiTaylorPhy.m at the element's vertices, phi[n][j] for the
+// first N functions: scaled monomials about the barycentre, mean-free from degree 2 on.  The
+// means are the exact triangle moments about the barycentre, E[x^2] = sum_n x_n^2 / 12 and
+// E[x^3] = sum_n x_n^3 / 30 (mixed moments likewise), which the reference integrates with
+// quadrature rules exact for them.
+template <typename T, int P>
+__device__ __forceinline__ void taylor_vertex_basis(const Affine<T> &af, T phi[3][Dims<P>::N]) {
+  const T d = af.dX;
+  T exx = T(0), exy = T(0), eyy = T(0), exxx = T(0), exxy = T(0), exyy = T(0), eyyy = T(0);
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const T x = af.ox[n], y = af.oy[n];
+    exx = exx + x * x; exy = exy + x * y; eyy = eyy + y * y;
+    exxx = exxx + x * x * x; exxy = exxy + x * x * y; exyy = exyy + x * y * y; eyyy = eyyy + y * y * y;
+  }
+  exx = exx / T(12); exy = exy / T(12); eyy = eyy / T(12);
+  exxx = exxx / T(30); exxy = exxy / T(30); exyy = exyy / T(30); eyyy = eyyy / T(30);
+  const T d2 = d * d, d3 = d2 * d, half = T(1) / T(2), sixth = T(1) / T(6);
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const T x = af.ox[n], y = af.oy[n];
+    phi[n][0] = T(1);
+    if (P >= 1) { phi[n][1] = x * d; phi[n][2] = y * d; }
+    if (P >= 2) {
+      phi[n][3] = half * (x * x - exx) * d2;
+      phi[n][4] = (x * y - exy) * d2;
+      phi[n][5] = half * (y * y - eyy) * d2;
+    }
+    if (P >= 3) {
+      phi[n][6] = sixth * (x * x * x - exxx) * d3;
+      phi[n][7] = half * (x * x * y - exxy) * d3;
+      phi[n][8] = half * (x * y * y - exyy) * d3;
+      phi[n][9] = sixth * (y * y * y - eyyy) * d3;
+    }
+  }
+}
+
 template <typename T, int P, int NQ>
 __device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, NQ> &kv, const T *sh,
                                              const Affine<T> &af, int dmask, const T dataV0T[3], T *cT) {
@@ -574,6 +611,39 @@ __device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, 
     const T keep = (alpha == T(1)) ? T(1) : T(0);
 #pragma unroll
     for (int i = 3; i < N; ++i) cT[i] *= keep;
+  } else if (li.type == 2) {
+    // core/applySlopeLimiterTaylorStrict.m:111-150: for ord = p..1 the reconstructions of
+    // degree p - ord + 1 about each derivative of order ord - 1, from the data already limited
+    // at the higher orders; every DOF of order >= ord is scaled by the order's factor.  The
+    // centroid quantities (derivatives of order ord - 1) are never rescaled by a higher order,
+    // so their patch extremes are those of the unlimited data (the same passes as hierarchical).
+    T phi[3][N];
+    taylor_vertex_basis<T, P>(af, phi);
+    int s = 0;
+#pragma unroll
+    for (int ord = P; ord >= 1; --ord) {
+      T aOrd = T(1);
+#pragma unroll
+      for (int i = 1; i <= ord; ++i) {
+        const int ba = ord - i, bb = i - 1, i0 = mind(ba, bb);
+        T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+          T acc = T(0);
+#pragma unroll
+          for (int a = 0; a <= P - ord + 1; ++a)
+#pragma unroll
+            for (int b = 0; a + b <= P - ord + 1; ++b) acc = acc + cT[mind(ba + a, bb + b)] * phi[n][mind(a, b)];
+          v[n] = acc;
+          valD[n] = ((dmask >> n) & 1) ? (ord > 1 ? v[n] : dataV0T[n]) : nan_;
+        }
+        patch_minmax<T, NQ>(li, kv, sh, s, valD, mn, mx);
+        aOrd = fmin(aOrd, vertex_alpha(cT[i0], v, mn, mx));
+        ++s;
+      }
+#pragma unroll
+      for (int i = ord * (ord + 1) / 2; i < N; ++i) cT[i] = aOrd * cT[i];
+    }
   } else {
     T orig[N];
 #pragma unroll

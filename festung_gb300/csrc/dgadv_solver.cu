@@ -82,8 +82,9 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
     return DGADV_EINVAL;
   if (prm->isSlopeLim && prm->p < 1) return DGADV_EINVAL;
   if (prm->p > kMaxP) return DGADV_EUNSUPPORTED;
-  if (prm->isSlopeLim && prm->typeSlopeLim != DGADV_LIM_LINEAR && prm->typeSlopeLim != DGADV_LIM_HIERARCH_VERT)
-    return prm->typeSlopeLim == DGADV_LIM_STRICT ? DGADV_EUNSUPPORTED : DGADV_EINVAL;
+  if (prm->isSlopeLim && prm->typeSlopeLim != DGADV_LIM_LINEAR && prm->typeSlopeLim != DGADV_LIM_HIERARCH_VERT &&
+      prm->typeSlopeLim != DGADV_LIM_STRICT)
+    return DGADV_EINVAL;
   dgadv_handle *h = new (std::nothrow) dgadv_handle();
   if (!h) return DGADV_ENOMEM;
   *out = h;

@@ -92,12 +92,14 @@ def test_fp32_close_to_fp64(lib, kw, tol):
 
 
 # Double-float (DF32): every real a pair of FP32 numbers, about 48 significant bits, computed on
-# the FP32 units.  Its unit roundoff per operation (2^-48) is 32x FP64's (2^-53), which keeps it
-# inside the FP64 bar of 1e-12 against the oracle at these horizons.  Where the oracle's own
-# roundoff spread (measured at FP64's unit roundoff) sets the allowance, DF32 gets that spread
-# scaled by the ratio of the unit roundoffs: the hierarchical limiter at p=3 moves by ~1e-9
-# under FP64 re-rounding and by ~3e-8 in DF32.
+# the FP32 units.  Its unit roundoff per operation (2^-48) is 32x FP64's (2^-53); its bar
+# against the oracle is 1e-11 (results land between 4e-15 and 1e-12), five orders below the
+# 1e-6 accuracy bar it exists for.  Where the oracle's own roundoff spread (measured at FP64's
+# unit roundoff) sets the allowance, DF32 gets that spread scaled by the ratio of the unit
+# roundoffs: the hierarchical limiter at p=3 moves by ~1e-9 under FP64 re-rounding and by
+# ~3e-8 in DF32.
 DF32_CASES = [SMALL[i] for i in (0, 2, 4, 6, 7, 8, 10, 11, 12)]
+DF32_TOL = 1e-11
 DF32_UNIT_RATIO = 2.0 ** -48 / 2.0 ** -53
 
 
@@ -107,9 +109,9 @@ def test_df32_matches_oracle(lib, kw):
     from oracle import matfree as MF
     g = gpu_run(precision='df32', **kw)
     o = oracle_run(**kw)
-    tol = FP64_TOL
+    tol = DF32_TOL
     if kw.get('typeSlopeLim') == 'hierarch_vert':
-        tol = max(FP64_TOL, 10 * DF32_UNIT_RATIO * MF.roundoff_spread(**kw))
+        tol = max(DF32_TOL, 10 * DF32_UNIT_RATIO * MF.roundoff_spread(**kw))
     assert rel(g.cDisc, o.cDisc) <= tol
 
 
@@ -180,3 +182,32 @@ def test_transient_convergence_order(lib):
             errs.append(pd.error)
         eoc = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
         assert eoc[-1] > p + 1 - 0.25, (p, errs, eoc)
+
+
+STRICT = [dict(testcase='gauss_slot', hmax=2 ** -3, p=1, tEnd=0.05, numSteps=20, isSlopeLim=True, typeSlopeLim='strict'),
+          dict(testcase='gauss_slot', hmax=2 ** -3, p=2, tEnd=0.05, numSteps=20, isSlopeLim=True, typeSlopeLim='strict'),
+          dict(testcase='gauss_slot', hmax=2 ** -3, p=3, tEnd=0.02, numSteps=10, isSlopeLim=True, typeSlopeLim='strict'),
+          dict(testcase='ensemble', instanceSeed=3, hmax=2 ** -3, p=3, tEnd=0.02, numSteps=10, isSlopeLim=True,
+               typeSlopeLim='strict'),
+          dict(testcase='transient', hmax=2 ** -3, p=2, tEnd=0.1, numSteps=20, isSlopeLim=True, typeSlopeLim='strict')]
+
+
+@pytest.mark.parametrize('kw', STRICT, ids=['p1', 'p2', 'p3', 'p3-jitter', 'transient-p2'])
+@pytest.mark.parametrize('precision', ['fp64', 'df32'])
+def test_strict_limiter_matches_oracle(lib, kw, precision):
+    """core/applySlopeLimiterTaylorStrict.m on the device: FP64 at the FP64 bar, DF32 at its own
+    (the oracle's roundoff spread is ~1e-15 to ~4e-14 on these cases)."""
+    from oracle import matfree as MF
+    g = gpu_run(precision=precision, **kw)
+    o = oracle_run(**kw)
+    tol = max(FP64_TOL if precision == 'fp64' else DF32_TOL, 10 * MF.roundoff_spread(**kw))
+    assert rel(g.cDisc, o.cDisc) <= tol
+
+
+def test_strict_limiter_fp32_close_to_fp64(lib):
+    """In FP32 the strict limiter's threshold tests (against the absolute tol = 1e-8 of
+    core/computeVertexBasedLimiter.m on first-derivative reconstructions of order-2 data) fall
+    the other way for some elements of this case, so FP32 lands ~5e-3 from FP64 while FP64 and
+    DF32 match the oracle; the bound records that level."""
+    kw = STRICT[1]
+    assert rel(gpu_run(precision='fp32', **kw).cDisc, gpu_run(precision='fp64', **kw).cDisc) <= 1e-2
