@@ -15,8 +15,8 @@ DGADV_ENONFINITE, DGADV_ETIMEOUT, DGADV_EUNSUPPORTED = 5, 6, 7
 FP64, FP32, DF32 = 0, 1, 2
 LIM_LINEAR, LIM_HIERARCH_VERT, LIM_STRICT = 0, 1, 2
 TIME_CONST, TIME_EXP_NEG = 0, 1
-FLAG_NO_REORDER, FLAG_NO_SHIFT, FLAG_NO_GRAPH, FLAG_NO_PDL, FLAG_FUSE = 1, 2, 4, 8, 16
-OPT_GRAPH_STEPS, OPT_FLAGS = 1, 2
+FLAG_NO_REORDER, FLAG_NO_SHIFT, FLAG_NO_GRAPH, FLAG_NO_PDL, FLAG_FUSE, FLAG_PERSIST = 1, 2, 4, 8, 16, 32
+OPT_GRAPH_STEPS, OPT_FLAGS, OPT_PERSIST_BLOCKS = 1, 2, 3
 
 LIMITER_TYPES = {'linear': LIM_LINEAR, 'hierarch_vert': LIM_HIERARCH_VERT, 'strict': LIM_STRICT}
 

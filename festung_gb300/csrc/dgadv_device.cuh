@@ -305,14 +305,16 @@ template <typename T> struct LimIn {
 // Offset of this block's instance in a slot set (each instance of an ensemble has its own
 // global extremes, as each reference problem has).
 template <typename T>
-__device__ __forceinline__ size_t slot_base(const Geo<T> &g, int nc) {
-  return g.instOf ? (size_t)g.instOf[blockIdx.x] * kSlotCopies * 2 * nc : 0;
+__device__ __forceinline__ size_t slot_base(const Geo<T> &g, int nc, int tile = -1) {
+  if (tile < 0) tile = blockIdx.x;
+  return g.instOf ? (size_t)g.instOf[tile] * kSlotCopies * 2 * nc : 0;
 }
 
 // Scatter of the element's centroid quantities to its vertices and the block's global extremes.
 template <typename T, int NQ>
 __device__ __forceinline__ void scatter_quantities(const Geo<T> &g, const LimOut<T> &lo, const T *qv,
-                                                   const int vid[3], bool active) {
+                                                   const int vid[3], bool active, int tile = -1) {
+  if (tile < 0) tile = blockIdx.x;
   if (active) {
 #pragma unroll
     for (int s = 0; s < NQ; ++s) {
@@ -346,7 +348,7 @@ __device__ __forceinline__ void scatter_quantities(const Geo<T> &g, const LimOut
 #pragma unroll
     for (int w = 1; w < kBlock / 32; ++w) { mn = fmin(mn, red[w][2 * s]); mx = fmax(mx, red[w][2 * s + 1]); }
     if (mn <= mx) {
-      unsigned long long *sl = lo.slots + slot_base(g, lo.nc) + (size_t)(blockIdx.x % kSlotCopies) * 2 * lo.nc;
+      unsigned long long *sl = lo.slots + slot_base(g, lo.nc, tile) + (size_t)(tile % kSlotCopies) * 2 * lo.nc;
       atomicMin(&sl[2 * s], okey(mn));
       atomicMax(&sl[2 * s + 1], okey(mx));
     }
@@ -752,15 +754,14 @@ struct StageScalars {
 };
 
 template <typename T, int P, int MODE, bool RHS, bool LIN>
-__global__ void __launch_bounds__(kBlock)
-k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
-           const LimOut<T> lo, const StageScalars sc) {
+__device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, const T *c0, T *out,
+           const LimOut<T> lo, const StageScalars sc, const int tile) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::op(MODE, LIN);
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
   const Tab<T, P> &tb = tab<T, P>();
-  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  const int t = threadIdx.x, k0 = tile * kBlock, k = k0 + t;
   pdl_trigger();
   const int Kp = g.Kp;
   const bool staged = k0 < g.K;                   // blocks beyond the elements only reset keys
@@ -900,8 +901,14 @@ k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
       }
     }
   }
-  if (MODE != 0) scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok);
+  if (MODE != 0) scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok, tile);
   if (bad) atomicOr(sc.flag, 1);
+}
+template <typename T, int P, int MODE, bool RHS, bool LIN>
+__global__ void __launch_bounds__(kBlock)
+k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
+           const LimOut<T> lo, const StageScalars sc) {
+  stage_op_tile<T, P, MODE, RHS, LIN>(g, cin, c0, out, lo, sc, blockIdx.x);
 }
 
 // Time-derivative limiting and SSP update (advection/solveSubStep.m:69-83), then the Taylor
@@ -1094,14 +1101,13 @@ k_to_taylor(const Geo<T> g, const T *c, T *__restrict__ tbuf, const LimOut<T> lo
 // precomputed Q_k = DM^-1 (S_k^-1 Mcorr_k S_k - I) (advection/solveSubStep.m:69-83); the new
 // stage value is written in the modal basis and its mean scattered for the solution limiter.
 template <typename T, int P>
-__global__ void __launch_bounds__(kBlock)
-k_limit_dot_lin(const Geo<T> g, const T *cin, const T *c0, const T *tbuf,
-                T *out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
+__device__ __forceinline__ void limit_dot_lin_tile(const Geo<T> g, const T *cin, const T *c0, const T *tbuf,
+                T *out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc, const int tile) {
   constexpr int N = Dims<P>::N, NQ = 1;
   constexpr int NT = StageRows<T, P>::limdot_lin();
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
-  const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
+  const int t = threadIdx.x, k0 = tile * kBlock, k = k0 + t;
   T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
   pdl_trigger();
   const int Kp = g.Kp;
@@ -1127,7 +1133,7 @@ k_limit_dot_lin(const Geo<T> g, const T *cin, const T *c0, const T *tbuf,
     stage_T(smem, rC0, c0, N, Kp, k0, bar);
     stage_T(smem, rC, cin, N, Kp, k0, bar);
   }
-  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc, tile), li.nc, sh);
   VKeys<T, NQ> kv;
   load_vkeys<T, NQ>(g, li, vid, kv);
   __syncthreads();
@@ -1159,20 +1165,25 @@ k_limit_dot_lin(const Geo<T> g, const T *cin, const T *c0, const T *tbuf,
     for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
     q0 = lin_mean<T, P>(cnew);
   }
-  scatter_quantities<T, NQ>(g, lo, &q0, vid, active && ok);
+  scatter_quantities<T, NQ>(g, lo, &q0, vid, active && ok, tile);
   if (bad) atomicOr(sc.flag, 1);
+}
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit_dot_lin(const Geo<T> g, const T *cin, const T *c0, const T *tbuf,
+                T *out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
+  limit_dot_lin_tile<T, P>(g, cin, c0, tbuf, out, li, lo, sc, blockIdx.x);
 }
 
 // Solution limiter for the linear limiter (core/applySlopeLimiterDisc.m:77-86 without the
 // Taylor round trip): c <- c - DM^-1 du.
 template <typename T, int P>
-__global__ void __launch_bounds__(kBlock)
-k_limit_lin(const Geo<T> g, const T *cbuf, T *out, const LimIn<T> li,
-            const StageScalars sc) {
+__device__ __forceinline__ void limit_lin_tile(const Geo<T> g, const T *cbuf, T *out, const LimIn<T> li,
+            const StageScalars sc, const int tile) {
   constexpr int N = Dims<P>::N, NQ = 1;
   const Tab<T, P> &tb = tab<T, P>();
   __shared__ T sh[2];
-  const int t = threadIdx.x, k = blockIdx.x * kBlock + t;
+  const int t = threadIdx.x, k = tile * kBlock + t;
   pdl_trigger();
   const bool active = k < g.K;
   const int Kp = g.Kp;
@@ -1190,7 +1201,7 @@ k_limit_lin(const Geo<T> g, const T *cbuf, T *out, const LimIn<T> li,
     }
   }
   pdl_wait();
-  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc, tile), li.nc, sh);
   T c[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) c[i] = active ? cbuf[(size_t)i * Kp + k] : T(0);
@@ -1213,6 +1224,12 @@ k_limit_lin(const Geo<T> g, const T *cbuf, T *out, const LimIn<T> li,
 #pragma unroll
   for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = c[i]; bad |= !finite_(c[i]); }
   if (bad) atomicOr(sc.flag, 1);
+}
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_limit_lin(const Geo<T> g, const T *cbuf, T *out, const LimIn<T> li,
+            const StageScalars sc) {
+  limit_lin_tile<T, P>(g, cbuf, out, li, sc, blockIdx.x);
 }
 
 // Mean of the modal state scattered to the vertices (initial limiting, linear limiter).

@@ -16,6 +16,7 @@
 namespace dgadv {
 constexpr int kBlock = 128;       // elements per CTA (one thread per element)
 constexpr int kSlotCopies = 32;   // copies of the global min / max slots (atomics spread over them)
+constexpr int kGridBarBytes = 8192;   // state of the persistent step's grid barrier
 }  // namespace dgadv
 
 struct dgadv_handle {
@@ -37,6 +38,9 @@ struct dgadv_handle {
   unsigned long long *gmm = nullptr;   // 3 passes x kSlotCopies x 2 x nc encoded global extremes
   long long limPass = 1;               // limiter passes enqueued so far (selects key / slot set)
   int graphSteps = 12;                 // time steps per captured CUDA graph
+  void *gridBar = nullptr;             // grid barrier state of the persistent step (zeroed)
+  int persistGrid = 0;                 // blocks of the persistent step (0: not yet sized)
+  int persistPerSM = 0;                // resident blocks per SM it may use (0: all that fit)
   int passesPerStep = 0;
   int *flag = nullptr;
   double *stage_ext = nullptr;         // K x N staging for set/get state
@@ -107,6 +111,8 @@ struct PrecOps {
   cudaError_t (*scatter_in)(dgadv_handle *h, void *dst);        // stage_ext (caller order, FP64) -> dst
   cudaError_t (*gather_out)(dgadv_handle *h, const void *src);  // src -> stage_ext
   cudaError_t (*adj_stage)(dgadv_handle *h, const AdjStageArgs &a);   // null: no adjoint kernels
+  cudaError_t (*step_persist)(dgadv_handle *h, double t0, double tau); // null: not built
+  cudaError_t (*persist_attributes)(int p);
   // device copy of a state-sized buffer (bytes a multiple of 16) ordered with dependent launches
   cudaError_t (*copy)(dgadv_handle *h, void *dst, const void *src, size_t bytes);
 };
@@ -115,6 +121,12 @@ struct PrecOps {
 // limits its input on the fly.
 inline bool use_fused(const dgadv_handle *h) {
   return h->lim && h->limType == DGADV_LIM_LINEAR && !h->cDV0T && (h->flags & DGADV_FLAG_FUSE);
+}
+// Persistent step (opted in): one cooperative launch per time step, linear limiter or none,
+// no source terms.
+inline bool use_persistent(const dgadv_handle *h) {
+  return (h->flags & DGADV_FLAG_PERSIST) && !(h->flags & DGADV_FLAG_FUSE) && h->p >= 1 &&
+         (!h->lim || h->limType == DGADV_LIM_LINEAR) && h->nTerms == 0;
 }
 
 const PrecOps &ops_of(const dgadv_handle *h);

@@ -429,6 +429,8 @@ static PrecOps make_ops() {
   o.scatter_in = scatter_in<T>;
   o.gather_out = gather_out<T>;
   o.adj_stage = nullptr;
+  o.step_persist = nullptr;
+  o.persist_attributes = nullptr;
   o.copy = copy_state;
   return o;
 }

@@ -1,4 +1,4 @@
-// Kernels and launch sequences of the FP32 path (stored reals: float), every degree, with the adjoint kernels.
+// Kernels and launch sequences of the FP32 path (stored reals: float), every degree, with the adjoint kernels and the persistent step.
 #include "dgadv_device.cuh"
 
 namespace dgadv {
@@ -7,10 +7,11 @@ DGADV_DEFINE_TABLES(float, cTf)
 
 #include "dgadv_launch.cuh"
 #include "dgadv_adjoint.cuh"
+#include "dgadv_persist.cuh"
 
 namespace dgadv {
 const PrecOps &ops_fp32() {
-  static const PrecOps ops = with_adjoint<float, 0xF>(make_ops<float, 0xF, true>());
+  static const PrecOps ops = with_persistent<float, 0xF>(with_adjoint<float, 0xF>(make_ops<float, 0xF, true>()));
   return ops;
 }
 }  // namespace dgadv

@@ -224,6 +224,7 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
   if ((st = dev_alloc(h, &h->vkeys, 3 * 2 * (size_t)nc * h->Vp * kw))) return st;
   if ((st = dev_alloc(h, (void **)&h->gmm, 3 * (size_t)h->nInst * kSlotCopies * 2 * (size_t)nc * 8))) return st;
   if ((st = dev_alloc(h, (void **)&h->flag, 16))) return st;
+  if ((st = dev_alloc(h, &h->gridBar, kGridBarBytes))) return st;
   if ((st = dev_alloc(h, (void **)&h->stage_ext, (size_t)N * K * 8))) return st;
   DG_CUDA(cudaMemset(h->F, 0, 2 * (size_t)Q * Kp * w));
   DG_CUDA(cudaMemset(h->Vn, 0, 3 * (size_t)R * Kp * w));
@@ -249,6 +250,7 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
     if ((st = upload(h, h->gmm, init.data(), init.size() * 8))) return st;
   }
   DG_CUDA(cudaMemset(h->flag, 0, 16));
+  DG_CUDA(cudaMemset(h->gridBar, 0, kGridBarBytes));
   if ((st = upload_real(h, h->Bm, Bsoa))) return st;
   if ((st = upload(h, h->nbr, nbr.data(), nbr.size() * 4))) return st;
   if ((st = upload(h, h->code, code.data(), code.size() * 4))) return st;
@@ -293,6 +295,7 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
       cudaError_t e = ops(h).upload_tables(h->p, h->tables);
       if (e != cudaSuccess) { h->err = std::string("table upload: ") + cudaGetErrorString(e); return DGADV_ECUDA; }
       e = ops(h).set_smem(h->p);
+      if (e == cudaSuccess && ops(h).persist_attributes) e = ops(h).persist_attributes(h->p);
       if (e != cudaSuccess) { h->err = std::string("kernel attributes: ") + cudaGetErrorString(e); return DGADV_ECUDA; }
       g_tab_loaded[h->device][pi][h->p] = true;
     }
@@ -441,7 +444,12 @@ extern "C" int dgadv_sync(dgadv_handle *h) {
   DG_CUDA(cudaStreamSynchronize(h->stream));
   int flag = 0;
   DG_CUDA(cudaMemcpy(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost));
-  if (flag & 2) { h->err = "a bounded device wait timed out"; return DGADV_ETIMEOUT; }
+  if (flag & 2) {
+    // a block gave up at a barrier: the barrier state is reset for the next launch
+    cudaMemset(h->gridBar, 0, kGridBarBytes);
+    h->err = "a bounded device wait timed out";
+    return DGADV_ETIMEOUT;
+  }
   if (flag & 1) { h->err = "non-finite value in the state"; return DGADV_ENONFINITE; }
   return DGADV_OK;
 }
@@ -471,6 +479,7 @@ static bool time_dependent(const dgadv_handle *h) {
 
 // One time step: fused or separate-pass pipeline.
 static cudaError_t one_step(dgadv_handle *h, double t0, double tau, bool firstOfCall) {
+  if (use_persistent(h) && ops(h).step_persist) return ops(h).step_persist(h, t0, tau);
   if (use_fused(h))
     return ops(h).step_fused(h, t0, tau, firstOfCall);
   return ops(h).step(h, t0, tau);
@@ -543,9 +552,14 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
   if (option == DGADV_OPT_GRAPH_STEPS) {
     if (value < 1 || value > 256) return DGADV_EINVAL;
     h->graphSteps = value;
+  } else if (option == DGADV_OPT_PERSIST_BLOCKS) {
+    if (value < 0 || value > 64) return DGADV_EINVAL;
+    h->persistPerSM = value;
+    h->persistGrid = 0;
   } else if (option == DGADV_OPT_FLAGS) {
-    const int runtime = DGADV_FLAG_NO_GRAPH | DGADV_FLAG_NO_PDL | DGADV_FLAG_FUSE;
-    if (value & ~runtime) { h->err = "only NO_GRAPH, NO_PDL and FUSE change after creation"; return DGADV_EINVAL; }
+    const int runtime = DGADV_FLAG_NO_GRAPH | DGADV_FLAG_NO_PDL | DGADV_FLAG_FUSE | DGADV_FLAG_PERSIST;
+    if (value & ~runtime) { h->err = "only NO_GRAPH, NO_PDL, FUSE and PERSIST change after creation"; return DGADV_EINVAL; }
+    if ((value & DGADV_FLAG_PERSIST) && !ops(h).step_persist) { h->err = "no persistent step for this precision"; return DGADV_EUNSUPPORTED; }
     if ((value & DGADV_FLAG_FUSE) && !ops(h).fused) { h->err = "no fused pipeline for this precision"; return DGADV_EUNSUPPORTED; }
     h->flags = (h->flags & ~runtime) | value;
   } else {
@@ -559,6 +573,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   if (!h || !value) return DGADV_EINVAL;
   if (option == DGADV_OPT_GRAPH_STEPS) *value = h->graphSteps;
   else if (option == DGADV_OPT_FLAGS) *value = h->flags;
+  else if (option == DGADV_OPT_PERSIST_BLOCKS) *value = h->persistPerSM;
   else return DGADV_EINVAL;
   return DGADV_OK;
 }
@@ -610,6 +625,7 @@ extern "C" int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nS
 
 extern "C" int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count) {
   if (!h || !count) return DGADV_EINVAL;
+  if (use_persistent(h) && ops_of(h).step_persist) { *count = 1; return DGADV_OK; }
   int perStage = 1;
   if (use_fused(h)) perStage = h->limdot ? 2 : 1;
   else if (h->lim) perStage = h->limdot ? 3 : 2;

@@ -50,15 +50,18 @@ enum {
   DGADV_FLAG_NO_SHIFT = 2,     /* patch min/max without the reference's global shift       */
   DGADV_FLAG_NO_GRAPH = 4,     /* launch stage kernels one by one instead of a CUDA graph  */
   DGADV_FLAG_NO_PDL = 8,       /* no programmatic dependent launch between stage kernels   */
-  DGADV_FLAG_FUSE = 16         /* linear limiter with zero Dirichlet data: apply the solution
+  DGADV_FLAG_FUSE = 16,        /* linear limiter with zero Dirichlet data: apply the solution
                                   limiter inside the next stage's operator kernel            */
+  DGADV_FLAG_PERSIST = 32      /* one cooperative launch per time step with grid barriers
+                                  (FP32 / FP64, linear limiter or none, no source terms)     */
 };
 
 /* options of dgadv_set_option (launch configuration: graph length and dependent launch leave
  * results bitwise unchanged; the fused pipeline changes them at the roundoff level) */
 enum {
   DGADV_OPT_GRAPH_STEPS = 1,   /* time steps per captured CUDA graph, 1..256 (default 12)        */
-  DGADV_OPT_FLAGS = 2          /* the runtime flags NO_GRAPH, NO_PDL, FUSE                       */
+  DGADV_OPT_FLAGS = 2,         /* the runtime flags NO_GRAPH, NO_PDL, FUSE, PERSIST              */
+  DGADV_OPT_PERSIST_BLOCKS = 3 /* blocks per SM of the persistent step (0: all that fit)        */
 };
 
 /* ---- host helpers: static data ------------------------------------------------------- */
