@@ -545,11 +545,20 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-stages', type=int, default=1)
     ap.add_argument('--ref-stages-per-step', type=int, default=1)
-    ap.add_argument('--ncu-case', default=None, choices=sorted(WORKLOADS),
+    ap.add_argument('--ncu-case', default=None, choices=sorted(WORKLOADS) + ['adjoint'],
                     help='profiling driver: set up the workload and run --ncu-steps steps, no timing')
     ap.add_argument('--ncu-steps', type=int, default=2)
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64', 'df32'])
     args = ap.parse_args()
+    if args.ncu_case == 'adjoint':
+        # one recorded run and its reverse sweep on 524288 triangles (p = 2), for profiling
+        from festung_gb300 import adjoint as AD
+        pd = AD.setup(precision=args.precision, hmax=2 ** -9, p=2, numSteps=args.ncu_steps,
+                      tEnd=args.ncu_steps * 2e-5)
+        c0 = np.asfortranarray(pd._cDisc)
+        AD.misfit_gradient(pd, c0, pd.theta, 0.9 * c0, nSnapshots=0)
+        pd.solver.close()
+        return 0
     if args.ncu_case:
         pd = setup_problem(args.ncu_case, args.precision, 0)
         pd.solver.step(args.ncu_steps, 0, pd.tau)
