@@ -404,6 +404,11 @@ def run_ours(args):
     units = K * N * S * steps
     c0 = np.asfortranarray(pd._cDisc)
     flush = torch.empty(512 * 2 ** 20, dtype=torch.uint8, device='cuda')
+    # launch configuration from the autotuner (graph length, dependent launch, pipeline)
+    from festung_gb300 import autotune as AT
+    tuned = AT.tune(s, pd.tau, nSteps=48, reps=3, fused_ok=(pd.typeSlopeLim == 'linear'))[0] \
+        if not args.no_tune else None
+    s.set_state(c0)
 
     for _ in range(args.warmup):
         s.step(steps, 0, pd.tau)
@@ -477,7 +482,7 @@ def run_ours(args):
         'value': value, 'unit': 'DOF-stage/s', 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-        'config': workload_config(wl, K, N, S, steps),
+        'config': dict(workload_config(wl, K, N, S, steps), launch=tuned),
         'clocks': sampler.summary(),
         'e2e': {'value': e2e_value, 'unit': 'DOF-stage/s', 'h2d_bytes_per_step': K * N * 8,
                 'd2h_bytes_per_step': K * N * 8},
@@ -542,6 +547,7 @@ def main():
     ap.add_argument('--no-df32', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--no-ensemble', action='store_true')
+    ap.add_argument('--no-tune', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-stages', type=int, default=1)
     ap.add_argument('--ref-stages-per-step', type=int, default=1)
