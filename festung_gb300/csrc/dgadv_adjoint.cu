@@ -135,9 +135,19 @@ int forward_step(dgadv_handle *h, Cursor &w) {
     h->cA = st;
     if (S > 2) h->cB = st + bytes;
   }
+  if (h->lim) {   // the limiter inputs of every stage: per step (stage storage) or scratch
+    for (int s = 0; s < S; ++s) {
+      h->recY[s] = h->adjRecY ? (char *)h->adjRecY + ((size_t)w.step * S + s) * bytes
+                              : (char *)h->adjScrY + (size_t)s * bytes;
+      if (h->limdot)
+        h->recCdot[s] = h->adjRecCdot ? (char *)h->adjRecCdot + ((size_t)w.step * S + s) * bytes
+                                      : (char *)h->adjScrCdot + (size_t)s * bytes;
+    }
+  }
   const cudaError_t e = o.step(h, w.step * h->recTau, h->recTau);
   h->cA = cA;
   h->cB = cB;
+  for (int s = 0; s < 3; ++s) h->recY[s] = h->recCdot[s] = nullptr;
   DG_CUDA(e);
   ++w.step;
   w.cnStep = w.step;
@@ -155,6 +165,7 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
   const double tau = h->recTau;
   double omega[3];
   const int S = rk_stages(h, omega);
+  const double cst[3] = {0.0, 1.0, 0.5};   // stage times (core/rungeKuttaExplicit.m:64-78)
   char *slots = (char *)h->adjSlots;
   char *stages = (char *)h->adjStages;
   auto stage_ptr = [&](int step, int s) { return stages + ((size_t)step * (S - 1) + (s - 1)) * bytes; };
@@ -199,8 +210,36 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
       }
       void *mub[3] = {nullptr, h->mu1, h->mu2};
       for (int s = S - 1; s >= 0; --s) {
+        const void *muNext = (s == S - 1) ? h->lam : mub[s + 1];
+        const void *muY = muNext, *mp = nullptr;
+        if (h->lim) {
+          // solution limiter, then (p >= 2) the time-derivative limiter, transposed
+          const char *Y = h->adjRecY ? (const char *)h->adjRecY + ((size_t)arg * S + s) * bytes
+                                     : (const char *)h->adjScrY + (size_t)s * bytes;
+          LimVjpArgs v;
+          std::memset(&v, 0, sizeof(v));
+          const double tBC = (s + 1 < S) ? (arg + cst[s + 1]) * tau : (arg + 1) * tau;
+          for (int m = 0; m < h->nTerms; ++m)
+            v.gco[m] = h->timeFn[m] == DGADV_TIME_EXP_NEG ? std::exp(-tBC) : 1.0;
+          DG_CUDA(o.vjp_scatter(h, Y, h->adjPass));
+          v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
+          DG_CUDA(o.lim_vjp(h, v));
+          muY = h->tmpY;
+          if (h->limdot) {
+            const char *Cd = h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
+                                           : (const char *)h->adjScrCdot + (size_t)s * bytes;
+            DG_CUDA(o.vjp_scatter(h, Cd, h->adjPass));
+            LimVjpArgs d;
+            std::memset(&d, 0, sizeof(d));
+            d.kind = 1; d.x = Cd; d.lamIn = h->tmpY; d.lamOut = h->tmpD; d.scale = (1.0 - omega[s]) * tau;
+            d.pass = h->adjPass++;
+            DG_CUDA(o.lim_vjp(h, d));
+            mp = h->tmpD;
+          }
+        }
         AdjStageArgs x;
-        x.muIn = (s == S - 1) ? h->lam : mub[s + 1];
+        x.muIn = muY;
+        x.mpIn = mp;
         x.cs = stageIn[s];
         x.muOut = s > 0 ? mub[s] : nullptr;
         x.accn = h->accn;
@@ -273,7 +312,10 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
   if (!h || nSteps < 1 || !(tau > 0.0)) return DGADV_EINVAL;
   const PrecOps &o = ops_of(h);
   if (!o.adj_stage) { h->err = "no adjoint kernels for this precision"; return DGADV_EUNSUPPORTED; }
-  if (h->lim) { h->err = "the adjoint covers the unlimited scheme only"; return DGADV_EUNSUPPORTED; }
+  if (h->lim && h->limType != DGADV_LIM_LINEAR) {
+    h->err = "the adjoint covers the unlimited scheme and the linear limiter";
+    return DGADV_EUNSUPPORTED;
+  }
   DG_CUDA(cudaSetDevice(h->device));
   const int nSlots = (nSnapshots <= 0 || nSnapshots >= nSteps) ? nSteps : nSnapshots;
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
@@ -310,6 +352,29 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
     DG_CUDA(cudaMemset(h->mu1, 0, bytes));
     DG_CUDA(cudaMemset(h->mu2, 0, bytes));
   }
+  if (h->lim) {
+    // limiter adjoint: recorded limiter inputs, its own vertex keys, per-element records
+    const size_t kb = o.keyBytes;
+    const bool perStep = stageSteps > 0;
+    if (!h->tmpY) {
+      if ((st = dev_alloc(h, &h->tmpY, bytes))) return st;
+      if ((st = dev_alloc(h, &h->tmpD, bytes))) return st;
+      if ((st = dev_alloc(h, (void **)&h->recTarget, (size_t)h->Kp * 4))) return st;
+      if ((st = dev_alloc(h, (void **)&h->recVertex, (size_t)h->Kp * 4))) return st;
+      if ((st = dev_alloc(h, &h->recW, (size_t)h->Kp * o.realBytes))) return st;
+      if ((st = dev_alloc(h, &h->vkeysA, 3 * 2 * (size_t)h->Vp * kb))) return st;
+      if ((st = dev_alloc(h, (void **)&h->gmmA, 3 * (size_t)h->nInst * kSlotCopies * 2 * 8))) return st;
+      if ((st = dev_alloc(h, &h->adjScrY, (size_t)S * bytes))) return st;
+      if ((st = dev_alloc(h, &h->adjScrCdot, (size_t)S * bytes))) return st;
+    }
+    dev_release(h, h->adjRecY);
+    dev_release(h, h->adjRecCdot);
+    if (perStep) {
+      if ((st = dev_alloc(h, &h->adjRecY, (size_t)nSteps * S * bytes))) return st;
+      if (h->limdot && (st = dev_alloc(h, &h->adjRecCdot, (size_t)nSteps * S * bytes))) return st;
+    }
+    drop_sweep(h);
+  }
   h->slotStep.assign(nSlots, -1);
   make_schedule(nSteps, nSlots, h->schedule);
   h->schedBackward = backward_start(h->schedule);
@@ -343,6 +408,19 @@ extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc
   DG_CUDA(cudaMemsetAsync(h->lam, 0, bytes, h->stream));
   DG_CUDA(cudaMemsetAsync(h->aF, 0, 2 * (size_t)h->Q * h->Kp * 8, h->stream));
   DG_CUDA(cudaMemsetAsync(h->aV, 0, 3 * (size_t)h->R * h->Kp * 8, h->stream));
+  if (h->lim) {
+    // every sweep starts with the limiter adjoint's key sets reset and its pass count at 0
+    const size_t kb = o.keyBytes, vset = 2 * (size_t)h->Vp * kb;
+    for (int set = 0; set < 3; ++set) {
+      DG_CUDA(cudaMemsetAsync((char *)h->vkeysA + set * vset, 0xFF, (size_t)h->Vp * kb, h->stream));
+      DG_CUDA(cudaMemsetAsync((char *)h->vkeysA + set * vset + (size_t)h->Vp * kb, 0, (size_t)h->Vp * kb, h->stream));
+    }
+    std::vector<unsigned long long> init(3 * (size_t)h->nInst * kSlotCopies * 2);
+    for (size_t i = 0; i < init.size(); ++i) init[i] = (i & 1) ? 0ULL : o.slotKeyMax;
+    DG_CUDA(cudaMemcpyAsync(h->gmmA, init.data(), init.size() * 8, cudaMemcpyHostToDevice, h->stream));
+    DG_CUDA(cudaStreamSynchronize(h->stream));
+    h->adjPass = 0;
+  }
   DG_CUDA(cudaMemcpyAsync(h->stage_ext, dJdcT, (size_t)h->N * h->K * 8, cudaMemcpyHostToDevice, h->stream));
   DG_CUDA(o.scatter_in(h, h->lam));
   // The reverse sweep (about 2S + 1 launches per step) runs as one CUDA graph, captured on the

@@ -28,8 +28,8 @@ struct AdjScalars {
 
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_adj_stage(const Geo<T> g, const T *muIn, const T *cs, T *__restrict__ muOut, T *__restrict__ accn,
-            double *__restrict__ aF, double *__restrict__ aV, const AdjScalars a) {
+k_adj_stage(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__restrict__ muOut,
+            T *__restrict__ accn, double *__restrict__ aF, double *__restrict__ aV, const AdjScalars a) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
   const Tab<T, P> &tb = tab<T, P>();
   const int k = blockIdx.x * kBlock + threadIdx.x;
@@ -68,7 +68,7 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *cs, T *__restrict__ muOut, T
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       cn[n][j] = nb[n] >= 0 ? cs[(size_t)j * Kp + nb[n]] : T(0);
-      mu2[n][j] = nb[n] >= 0 ? muIn[(size_t)j * Kp + nb[n]] : T(0);
+      mu2[n][j] = nb[n] >= 0 ? (mpIn ? mpIn[(size_t)j * Kp + nb[n]] : coef * muIn[(size_t)j * Kp + nb[n]]) : T(0);
     }
 #pragma unroll
   for (int i = 0; i < 2 * Q; ++i) sF[i] = aF[(size_t)i * Kp + k];
@@ -76,7 +76,7 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *cs, T *__restrict__ muOut, T
   for (int i = 0; i < 3 * R; ++i) sV[i] = aV[(size_t)i * Kp + k];
   T mp[N];
 #pragma unroll
-  for (int i = 0; i < N; ++i) mp[i] = coef * mu[i];   // dJ/dcDot of this stage
+  for (int i = 0; i < N; ++i) mp[i] = mpIn ? mpIn[(size_t)i * Kp + k] : coef * mu[i];   // dJ/dcDot
   Acc<T> grad[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) grad[i] = Acc<T>(T(0));
@@ -137,7 +137,7 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *cs, T *__restrict__ muOut, T
         Acc<T> eta(T(0));
 #pragma unroll
         for (int j = 0; j < N; ++j) eta.fma(tb.Hphi[nk[n]][r][j], mu2[n][j]);
-        const T ev = coef * eta.get() * v2;
+        const T ev = eta.get() * v2;
 #pragma unroll
         for (int j = 0; j < N; ++j) grad[j].fms(tb.thetaPhi[nk[n]][n][r][j], ev);
       }
@@ -158,14 +158,207 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *cs, T *__restrict__ muOut, T
   for (int i = 0; i < 3 * R; ++i) aV[(size_t)i * Kp + k] = sV[i];
 }
 
+// ---------------------------------------------------------------------------------------------
+// Adjoint of the linear limiter (core/computeVertexBasedLimiter.m:78-106 in the geometry-free form
+// of lin_alpha).  With its discrete choices frozen the limiter is rational in its input x:
+//   solution limiter (KIND 0):        out = x - DM^-1[:,1:] du(x)             (Dirichlet data)
+//   time-derivative limiter (KIND 1): out = x + Q_k du(x)                      (no data)
+// du = (0, (1-a) u1, (1-a) u2, u3, ...) for a < 1 (zero otherwise), u = DM x, a = dm / den at
+// the first vertex whose factor is the element's, den = dV -/+ tol on the branch taken.  With
+// r = M^T lambda (M = -DM^-1[:,1:] or Q_k):
+//   dJ/dx = lambda + sum_j r_j d du_j/dx
+//         = lambda + (1-a)(r1 DM1 + r2 DM2) + sum_{j>=3} r_j DMj - (r1 u1 + r2 u2) da/dx,
+// where da/dx covers x's own mean and vertex value, and da/dm = 1/den goes to the patch element
+// holding the extreme (its mean is DM0 . x): recorded here, gathered by k_lim_vjp_gather.  The
+// choices are recomputed from the recorded input x (the same keys, shift and comparisons as the
+// forward kernels); a tie for the extreme goes to the lowest element index of the caller's order,
+// Dirichlet data winning a tie with an element.
+template <typename T, int P, int KIND>
+__global__ void __launch_bounds__(kBlock)
+k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, const LimIn<T> li,
+          const StageScalars sc, double scale, int *__restrict__ recTarget, int *__restrict__ recVertex,
+          T *__restrict__ recW) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  __shared__ T sh[2];
+  const int k = blockIdx.x * kBlock + threadIdx.x;
+  pdl_trigger();
+  const bool active = k < g.K;
+  const int Kp = g.Kp;
+  int vid[3] = {0, 0, 0}, dmask = 0;
+  if (active) {
+    vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
+    if (KIND == 0) dmask = (g.code[k] >> 9) & 7;
+  }
+  T data[3] = {T(0), T(0), T(0)};
+  if (KIND == 0 && g.cDV0T && active)
+    for (int m = 0; m < g.nTerms; ++m) {
+      const T gm = T(sc.gco[m]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
+    }
+  pdl_wait();
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
+  T xv[N], lam[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    xv[i] = active ? x[(size_t)i * Kp + k] : T(0);
+    lam[i] = active ? T(scale) * lamIn[(size_t)i * Kp + k] : T(0);
+  }
+  VKeys<T, 1> kv;
+  load_vkeys<T, 1>(g, li, vid, kv);
+  __syncthreads();
+  if (!active) return;
+  T u[N];
+  lin_u<T, P>(xv, u);
+  // the forward's factor, vertex by vertex (vertex_alpha), with its branch and raw ratio
+  const T third = T(1) / T(3), two3 = T(2) / T(3), tol = T(1.e-8);
+  const T hx[3] = {-third, two3, -third}, hy[3] = {-third, -third, two3};
+  T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    v[n] = (u[0] * T(1) + u[1] * hx[n]) + u[2] * hy[n];
+    valD[n] = ((dmask >> n) & 1) ? data[n] : T(NAN);
+  }
+  patch_minmax<T, 1>(li, kv, sh, 0, valD, mn, mx);
+  T an[3];
+  int br[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const T dV = v[n] - u[0], dMin = mn[n] - u[0], dMax = mx[n] - u[0];
+    an[n] = T(1);
+    br[n] = 0;
+    if (dV < dMin + tol) { an[n] = fmax(T(0), fmin(T(1), dMin / (dV - tol))); br[n] = 1; }
+    if (dV > dMax - tol) { an[n] = fmax(T(0), fmin(T(1), dMax / (dV + tol))); br[n] = 2; }
+  }
+  const T alpha = fmin(fmin(an[0], an[1]), an[2]);
+  int ns = 0;
+  if (!(an[0] == alpha)) ns = (an[1] == alpha) ? 1 : 2;
+  T out[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) out[i] = lam[i];
+  int tgt = -1;
+  T w = T(0);
+  if (alpha < T(1)) {
+    T r[N];
+    r[0] = T(0);
+#pragma unroll
+    for (int j = 1; j < N; ++j) {
+      Acc<T> a(T(0));
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        if (KIND == 0) a.fms(tb.DMinv[i][j], lam[i]);
+        else a.fma(g.MT[(size_t)(i * (N - 1) + (j - 1)) * Kp + k], lam[i]);
+      }
+      r[j] = a.get();
+    }
+    T gu[N];   // dJ/du
+#pragma unroll
+    for (int j = 0; j < N; ++j) gu[j] = (j == 0) ? T(0) : (j <= 2 ? (T(1) - alpha) * r[j] : r[j]);
+    const T dV = v[ns] - u[0];
+    const bool isPos = br[ns] == 2;
+    const T den = isPos ? dV + tol : dV - tol;
+    const T dm = (isPos ? mx[ns] : mn[ns]) - u[0];
+    const T raw = dm / den;
+    if (br[ns] != 0 && raw > T(0) && raw < T(1)) {
+      const T sa = -(r[1] * u[1] + r[2] * u[2]);                  // dJ / d alpha
+      const T q = dm / (den * den);
+      gu[0] = gu[0] - sa / den;                                   // d dm / d u0 = -1
+      gu[1] = gu[1] - sa * q * hx[ns];
+      gu[2] = gu[2] - sa * q * hy[ns];
+      // the extreme's source: Dirichlet data, or the patch element with that mean
+      const T rawExt = vkey_inv<T>(kv.v[0][isPos ? 1 : 0][ns]);
+      const bool fromData = ((dmask >> ns) & 1) && (isPos ? !(data[ns] < rawExt) : !(data[ns] > rawExt));
+      if (!fromData) {
+        const auto key = kv.v[0][isPos ? 1 : 0][ns];
+        const int vv = vid[ns];
+        int best = -1, bestId = 0x7fffffff;
+        for (int i = g.vptr[vv]; i < g.vptr[vv + 1]; ++i) {
+          const int k2 = g.vidx[i];
+          T c2[N];
+#pragma unroll
+          for (int j = 0; j < N; ++j) c2[j] = x[(size_t)j * Kp + k2];
+          if (vkey(lin_mean<T, P>(c2)) == key && g.permv[k2] < bestId) { best = k2; bestId = g.permv[k2]; }
+        }
+        tgt = best;
+        w = sa / den;                                             // d alpha / d m = 1 / den
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      Acc<T> a(out[j]);
+#pragma unroll
+      for (int i = 0; i < N; ++i) a.fma(tb.DM[i][j], gu[i]);
+      out[j] = a.get();
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) lamOut[(size_t)i * Kp + k] = out[i];
+  recTarget[k] = tgt;
+  recVertex[k] = vid[ns];
+  recW[k] = w;
+}
+
+// Gathers the recorded extreme terms: element e adds w DM0 for every element of its vertex
+// patches whose limiter factor took its extreme from e at that vertex (CSR order: deterministic).
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_lim_vjp_gather(const Geo<T> g, T *lam, const int *recTarget, const int *recVertex, const T *recW) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  const int k = blockIdx.x * kBlock + threadIdx.x;
+  pdl_trigger();
+  if (k >= g.K) return;
+  const int Kp = g.Kp;
+  const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
+  pdl_wait();
+  T acc = T(0);
+  bool any = false;
+  for (int n = 0; n < 3; ++n)
+    for (int i = g.vptr[vid[n]]; i < g.vptr[vid[n] + 1]; ++i) {
+      const int k2 = g.vidx[i];
+      if (recTarget[k2] == k && recVertex[k2] == vid[n]) { acc = acc + recW[k2]; any = true; }
+    }
+  if (!any) return;
+#pragma unroll
+  for (int j = 0; j < N; ++j) lam[(size_t)j * Kp + k] = lam[(size_t)j * Kp + k] + acc * tb.DM[0][j];
+}
+
+template <typename T, int P>
+static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
+  const Geo<T> g = make_geo<T>(h);
+  const int gridK = (h->K + kBlock - 1) / kBlock;
+  StageScalars sc{};
+  sc.flag = h->flag;
+  for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = v.gco[m];
+  if (v.kind == 0)
+    launch_k(h, k_lim_vjp<T, P, 0>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn, (T *)v.lamOut,
+             lim_in_adj<T>(h, v.pass), sc, v.scale, h->recTarget, h->recVertex, (T *)h->recW);
+  else
+    launch_k(h, k_lim_vjp<T, P, 1>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn, (T *)v.lamOut,
+             lim_in_adj<T>(h, v.pass), sc, v.scale, h->recTarget, h->recVertex, (T *)h->recW);
+  launch_k(h, k_lim_vjp_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, (const int *)h->recTarget,
+           (const int *)h->recVertex, (const T *)h->recW);
+  return cudaGetLastError();
+}
+
+// Means of x scattered to the adjoint's own vertex keys (the limiter's patch extremes).
+template <typename T, int P>
+static cudaError_t launch_vjp_scatter(dgadv_handle *h, const void *x, long long pass) {
+  const Geo<T> g = make_geo<T>(h);
+  const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
+  launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)x, lim_out_adj<T>(h, pass));
+  return cudaGetLastError();
+}
+
 template <typename T, int P>
 static cudaError_t launch_adj_stage(dgadv_handle *h, const AdjStageArgs &s) {
   const Geo<T> g = make_geo<T>(h);
   const int grid = (h->K + kBlock - 1) / kBlock;
   AdjScalars a;
   a.omega = s.omega; a.tau = s.tau; a.init = s.init; a.last = s.last;
-  launch_k(h, k_adj_stage<T, P>, grid, (size_t)0, g, (const T *)s.muIn, (const T *)s.cs, (T *)s.muOut,
-           (T *)s.accn, h->aF, h->aV, a);
+  launch_k(h, k_adj_stage<T, P>, grid, (size_t)0, g, (const T *)s.muIn, (const T *)s.mpIn, (const T *)s.cs,
+           (T *)s.muOut, (T *)s.accn, h->aF, h->aV, a);
   return cudaGetLastError();
 }
 
@@ -180,10 +373,31 @@ static cudaError_t dispatch_adj_stage(dgadv_handle *h, const AdjStageArgs &s) {
   return cudaErrorNotSupported;
 }
 
+template <typename T, int MASK>
+static cudaError_t dispatch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
+  switch (h->p) {
+    case 1: if constexpr ((MASK & 2) != 0) return launch_lim_vjp<T, 1>(h, v); break;
+    case 2: if constexpr ((MASK & 4) != 0) return launch_lim_vjp<T, 2>(h, v); break;
+    case 3: if constexpr ((MASK & 8) != 0) return launch_lim_vjp<T, 3>(h, v); break;
+  }
+  return cudaErrorNotSupported;
+}
+template <typename T, int MASK>
+static cudaError_t dispatch_vjp_scatter(dgadv_handle *h, const void *x, long long pass) {
+  switch (h->p) {
+    case 1: if constexpr ((MASK & 2) != 0) return launch_vjp_scatter<T, 1>(h, x, pass); break;
+    case 2: if constexpr ((MASK & 4) != 0) return launch_vjp_scatter<T, 2>(h, x, pass); break;
+    case 3: if constexpr ((MASK & 8) != 0) return launch_vjp_scatter<T, 3>(h, x, pass); break;
+  }
+  return cudaErrorNotSupported;
+}
+
 // The operation table of a unit with the adjoint kernels added.
 template <typename T, int MASK>
 static PrecOps with_adjoint(PrecOps o) {
   o.adj_stage = dispatch_adj_stage<T, MASK>;
+  o.lim_vjp = dispatch_lim_vjp<T, MASK>;
+  o.vjp_scatter = dispatch_vjp_scatter<T, MASK>;
   return o;
 }
 

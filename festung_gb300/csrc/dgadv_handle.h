@@ -74,6 +74,17 @@ struct dgadv_handle {
   double adjExecTau = 0.0;
   double *aF = nullptr, *aV = nullptr;         // velocity sensitivities, 2Q x Kp and 3R x Kp
   double *thetaPart = nullptr;                 // per-block partial sums of the mode gradient
+  // adjoint of the linear limiter: the limiter inputs of every stage, recorded by the forward
+  // run (recY: the unlimited stage value; recCdot: cDot before time-derivative limiting)
+  void *recY[3] = {nullptr, nullptr, nullptr}, *recCdot[3] = {nullptr, nullptr, nullptr};
+  void *adjRecY = nullptr, *adjRecCdot = nullptr;   // per step and stage (stage storage mode)
+  void *adjScrY = nullptr, *adjScrCdot = nullptr;   // per stage (recomputing modes)
+  void *tmpY = nullptr, *tmpD = nullptr;            // dJ/dy and dJ/dcDot of a reversed stage
+  int *recTarget = nullptr, *recVertex = nullptr;   // extreme's element and vertex per element
+  void *recW = nullptr;                             // its weight
+  void *vkeysA = nullptr;                           // the adjoint's own vertex keys (3 sets)
+  unsigned long long *gmmA = nullptr;               // ... and global-extreme slots
+  long long adjPass = 0;
   std::vector<int> schedule;                   // checkpointing actions of the recorded run
   size_t schedBackward = 0;                    // first action of the reverse sweep
   int recSteps = 0;
@@ -86,12 +97,24 @@ namespace dgadv {
 
 // One reversed stage of the adjoint sweep (device pointers of the handle's real type).
 struct AdjStageArgs {
-  const void *muIn;    // dJ/dc^(s+1)
+  const void *muIn;    // dJ/dc^(s+1) (with the limiter: dJ/d of the unlimited stage value)
+  const void *mpIn;    // dJ/dcDot if precomputed (time-derivative limiter adjoint), else null
   const void *cs;      // c^(s), the stage input of the forward step
   void *muOut;         // dJ/dc^(s) (may be null when s = 0)
   void *accn;          // dJ/dc^n, accumulated over the stages of the step
   double omega, tau;
   int init, last;
+};
+
+// One limiter adjoint pass: lamOut = (d limiter / d x)^T (scale * lamIn).
+struct LimVjpArgs {
+  int kind;            // 0 solution limiter, 1 time-derivative limiter
+  const void *x;       // the limiter's recorded input
+  const void *lamIn;
+  void *lamOut;
+  double scale;
+  long long pass;      // adjoint key set (pass mod 3) holding x's patch extremes
+  double gco[4];       // time factors of the Dirichlet data (solution limiter)
 };
 
 // Work of one arithmetic type, enqueued on the handle's stream.
@@ -113,6 +136,8 @@ struct PrecOps {
   cudaError_t (*adj_stage)(dgadv_handle *h, const AdjStageArgs &a);   // null: no adjoint kernels
   cudaError_t (*step_persist)(dgadv_handle *h, double t0, double tau); // null: not built
   cudaError_t (*persist_attributes)(int p);
+  cudaError_t (*lim_vjp)(dgadv_handle *h, const LimVjpArgs &a);
+  cudaError_t (*vjp_scatter)(dgadv_handle *h, const void *x, long long pass);
   // device copy of a state-sized buffer (bytes a multiple of 16) ordered with dependent launches
   cudaError_t (*copy)(dgadv_handle *h, void *dst, const void *src, size_t bytes);
 };

@@ -58,6 +58,7 @@ template <typename T> struct Geo {
   int nTerms;
   int timeFn[4];
   const int *instOf; // ensembles: instance of each block of kBlock elements (null: one instance)
+  const int *permv;  // Kp       caller's index of each element (ties of the limiter adjoint)
   int nInst;         // instances; each has its own global-extreme slots
 };
 

@@ -61,6 +61,7 @@ static Geo<T> make_geo(const dgadv_handle *h) {
   for (int i = 0; i < 4; ++i) g.timeFn[i] = h->timeFn[i];
   g.instOf = h->instOf;
   g.nInst = h->nInst;
+  g.permv = h->perm;
   return g;
 }
 
@@ -96,6 +97,32 @@ static LimIn<T> lim_in_pass(const dgadv_handle *h, long long pass) {
   i.vkeys = (const K_ *)h->vkeys + (size_t)set * 2 * h->nc * h->Vp;
   i.slots = h->gmm + (size_t)set * h->nInst * kSlotCopies * 2 * h->nc;
   i.nc = h->nc; i.type = h->limType;
+  i.shift = (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1;
+  return i;
+}
+
+// The adjoint's own key sets (the limiter adjoint recomputes the forward's patch extremes).
+template <typename T>
+static LimOut<T> lim_out_adj(dgadv_handle *h, long long pass) {
+  using K_ = typename KeyOf<T>::type;
+  const int set = (int)(pass % 3), next = (set + 1) % 3;
+  const size_t vset = (size_t)2 * h->Vp;
+  LimOut<T> o;
+  o.vkeys = (K_ *)h->vkeysA + set * vset;
+  o.vreset = (K_ *)h->vkeysA + next * vset;
+  o.slots = h->gmmA + (size_t)set * h->nInst * kSlotCopies * 2;
+  o.reset = h->gmmA + (size_t)next * h->nInst * kSlotCopies * 2;
+  o.nc = 1; o.type = 0;
+  return o;
+}
+template <typename T>
+static LimIn<T> lim_in_adj(const dgadv_handle *h, long long pass) {
+  using K_ = typename KeyOf<T>::type;
+  const int set = (int)(pass % 3);
+  LimIn<T> i;
+  i.vkeys = (const K_ *)h->vkeysA + (size_t)set * 2 * h->Vp;
+  i.slots = h->gmmA + (size_t)set * h->nInst * kSlotCopies * 2;
+  i.nc = 1; i.type = 0;
   i.shift = (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1;
   return i;
 }
@@ -225,6 +252,10 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
       }
     }
     prof_mark(h, -1);
+    // recorded run of the adjoint: the limiter inputs of this stage
+    const size_t stBytes = (size_t)h->N * h->Kp * sizeof(T);
+    if (lin && mode == 2 && h->recCdot[s]) copy_state(h, h->recCdot[s], tb, stBytes);
+    if (lin && mode == 1 && h->recY[s]) copy_state(h, h->recY[s], tb, stBytes);
     LimOut<T> loS = lo1;
     if (mode == 2) {
       const LimOut<T> lo2 = lim_out<T>(h);
@@ -233,6 +264,7 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
       if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)in, (const T *)cn, (const T *)tb, tb, lim_in<T>(lo1, h), lo2, sc);
       else launch_k(h, k_limit_dot<T, P>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
       prof_mark(h, -1);
+      if (lin && h->recY[s]) copy_state(h, h->recY[s], tb, stBytes);
       loS = lo2;
     }
     prof_mark(h, 2);
@@ -429,6 +461,8 @@ static PrecOps make_ops() {
   o.scatter_in = scatter_in<T>;
   o.gather_out = gather_out<T>;
   o.adj_stage = nullptr;
+  o.lim_vjp = nullptr;
+  o.vjp_scatter = nullptr;
   o.step_persist = nullptr;
   o.persist_attributes = nullptr;
   o.copy = copy_state;

@@ -578,6 +578,35 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   return DGADV_OK;
 }
 
+// Self-test of the bounded device wait: one block waits on a device flag that nothing sets,
+// gives up after limitCycles SM cycles, and records the timeout in the handle's error flag.
+__global__ void k_wait_selftest(const int *never, int *flag, long long limitCycles) {
+  if (threadIdx.x != 0) return;
+  const volatile int *v = never;
+  const long long t0 = clock64();
+  while (*v == 0)
+    if (clock64() - t0 > limitCycles) {
+      atomicOr(flag, 2);
+      return;
+    }
+}
+
+extern "C" int dgadv_selftest_wait(dgadv_handle *h, double seconds) {
+  if (!h || !(seconds > 0.0) || seconds > 2.0) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  int khz = 0;
+  DG_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, h->device));
+  const long long limit = (long long)(seconds * khz * 1e3);
+  int *never = (int *)h->stage_ext;   // any device word that stays 0 for the test
+  DG_CUDA(cudaMemsetAsync(never, 0, sizeof(int), h->stream));
+  k_wait_selftest<<<1, 32, 0, h->stream>>>(never, h->flag, limit);
+  DG_CUDA(cudaGetLastError());
+  const int st = dgadv_sync(h);
+  // the handle stays usable: clear the recorded error
+  DG_CUDA(cudaMemset(h->flag, 0, 16));
+  return st;
+}
+
 extern "C" int dgadv_time_steps(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau, double *ms) {
   if (!h || !ms) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));

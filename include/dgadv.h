@@ -183,6 +183,12 @@ int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nStep0, doubl
 int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value);
 int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *value);
 
+/* Failure-detection self-test: a device wait on a flag that nothing sets gives up after
+ * `seconds` (at most 2) and the call returns DGADV_ETIMEOUT, as every bounded wait of the stage
+ * kernels does; the error is then cleared and the handle stays usable.  No counterpart in the
+ * reference. */
+int dgadv_selftest_wait(dgadv_handle *h, double seconds);
+
 /* Number of kernels one time step launches (for launch accounting). */
 int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count);
 

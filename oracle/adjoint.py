@@ -18,6 +18,7 @@ from scipy.sparse.linalg import splu
 
 from . import advection as adv
 from . import assembly as A
+from . import matfree as MF
 from . import testcases as TC
 
 
@@ -132,3 +133,211 @@ class AdjointOracle:
 
 def mode_velocities():
     return [TC.mode_velocity(m) for m in range(len(TC.ADJOINT_MODES))]
+
+
+# ---------------------------------------------------------------------------------------------
+# The limited scheme (linear vertex-based limiter): the limiter is piecewise rational in its
+# input; with its discrete choices frozen (the vertex whose factor is the element's alpha, the
+# branch of core/computeVertexBasedLimiter.m:78-106 taken there, the clip, and which element of
+# the vertex patch holds the extreme, or the Dirichlet data), it is differentiable.  Ties go to
+# the first vertex and to the lowest element index; Dirichlet data wins a tie with an element.
+# The vector-Jacobian product is written in the reference's Taylor basis
+# (core/applySlopeLimiterTaylorLinear.m:108-122 through core/projectDataDisc2DataTaylor.m and
+# core/projectDataTaylor2DataDisc.m): dJ/dx = P^T (dlimit/dcT)^T P^-T dJ/dout, P = MDT^-1 M.
+TOL = 1.e-8
+
+
+def patch_extremes(mf, val, markV0TbdrD, dataV0T):
+    """Per (element, local vertex): patch min / max as the forward computes them (with the
+    reference's shift) and their sources: the element index, or -1 for Dirichlet data."""
+    g = mf.pd.g
+    mn, mx = mf.patch_minmax(val, markV0TbdrD, dataV0T)
+    ptr, idx = mf.ptr, mf.idx
+    nV = len(ptr) - 1
+    amin = np.empty(nV, dtype=np.int64)
+    amax = np.empty(nV, dtype=np.int64)
+    for v in range(nV):
+        e = np.sort(idx[ptr[v]:ptr[v + 1]])
+        vv = val[e]
+        amin[v] = e[np.argmin(vv)]      # first (lowest index) attaining the extreme
+        amax[v] = e[np.argmax(vv)]
+    srcMin = amin[g.V0T].copy()
+    srcMax = amax[g.V0T].copy()
+    valD = np.full(g.V0T.shape, np.nan)
+    valD[markV0TbdrD] = dataV0T[markV0TbdrD]
+    hasD = ~np.isnan(valD)
+    srcMin[hasD & (valD <= val[amin[g.V0T]])] = -1
+    srcMax[hasD & (valD >= val[amax[g.V0T]])] = -1
+    return mn, mx, srcMin, srcMax
+
+
+def limiter_choices(mf, cT, markV0TbdrD, dataV0T):
+    """alpha and the frozen choices of the linear limiter on Taylor coefficients cT."""
+    phiV = mf.pd.basesOnQuad.phiTaylorV0T
+    K = cT.shape[0]
+    cbar = cT[:, 0]
+    v = cbar[:, None] + cT[:, 1:2] * phiV[:, :, 1] + cT[:, 2:3] * phiV[:, :, 2]
+    mn, mx, sMin, sMax = patch_extremes(mf, cbar, markV0TbdrD, dataV0T)
+    dV, dMin, dMax = v - cbar[:, None], mn - cbar[:, None], mx - cbar[:, None]
+    neg = dV < dMin + TOL
+    pos = dV > dMax - TOL
+    a = np.ones_like(dV)
+    raw = np.full_like(dV, np.nan)
+    with np.errstate(divide='ignore', invalid='ignore'):
+        raw[neg] = dMin[neg] / (dV[neg] - TOL)
+        raw[pos] = dMax[pos] / (dV[pos] + TOL)
+    m = neg | pos
+    a[m] = np.fmax(0, np.fmin(1, raw[m]))
+    alpha = np.fmin(np.fmin(a[:, 0], a[:, 1]), a[:, 2])
+    ns = np.argmax(a == alpha[:, None], axis=1)          # first vertex attaining alpha
+    r = np.arange(K)
+    isPos, isNeg = pos[r, ns], neg[r, ns] & ~pos[r, ns]
+    den = np.where(isPos, dV[r, ns] + TOL, dV[r, ns] - TOL)
+    dm = np.where(isPos, dMax[r, ns], dMin[r, ns])
+    src = np.where(isPos, sMax[r, ns], sMin[r, ns])
+    rr = raw[r, ns]
+    active = (isPos | isNeg) & (alpha < 1) & (rr > 0) & (rr < 1)   # alpha varies with the data here
+    mval = np.where(isPos, mx[r, ns], mn[r, ns])
+    return dict(alpha=alpha, ns=ns, den=den, dm=dm, src=src, active=active, isPos=isPos,
+                mval=mval, phi1=phiV[r, ns, 1], phi2=phiV[r, ns, 2])
+
+
+def limit_frozen(cT, ch):
+    """The linear limiter with the choices ch held fixed (a smooth function of cT): the
+    derivative that limiter_vjp_taylor transposes."""
+    alpha = ch['alpha'].copy()
+    act = ch['active']
+    m = np.where(ch['src'] >= 0, cT[np.maximum(ch['src'], 0), 0], ch['mval'])
+    dV = cT[:, 1] * ch['phi1'] + cT[:, 2] * ch['phi2']
+    den = np.where(ch['isPos'], dV + TOL, dV - TOL)
+    alpha[act] = ((m - cT[:, 0]) / den)[act]
+    out = cT.copy()
+    lim = ch['alpha'] < 1
+    out[lim, 1] = alpha[lim] * cT[lim, 1]
+    out[lim, 2] = alpha[lim] * cT[lim, 2]
+    out[lim, 3:] = 0.0
+    return out
+
+
+def limiter_vjp_taylor(cT, ch, lamL):
+    """(d limitTaylor / d cT)^T lamL for the linear limiter with frozen choices ch."""
+    alpha = ch['alpha']
+    lim = alpha < 1
+    g = lamL.copy()
+    g[lim, 1] = alpha[lim] * lamL[lim, 1]
+    g[lim, 2] = alpha[lim] * lamL[lim, 2]
+    g[lim, 3:] = 0.0
+    s = lamL[:, 1] * cT[:, 1] + lamL[:, 2] * cT[:, 2]        # dJ / d alpha
+    act = ch['active']
+    den, dm = ch['den'], ch['dm']
+    g[act, 0] -= s[act] / den[act]                            # d dm / d cbar = -1
+    g[act, 1] -= s[act] * dm[act] / den[act] ** 2 * ch['phi1'][act]
+    g[act, 2] -= s[act] * dm[act] / den[act] ** 2 * ch['phi2'][act]
+    nl = act & (ch['src'] >= 0)
+    np.add.at(g[:, 0], ch['src'][nl], s[nl] / den[nl])        # the extreme's element
+    return g
+
+
+class LimitedAdjointOracle:
+    """Forward run and reverse sweep of the scheme with the linear limiter (solution limiting,
+    and time-derivative limiting at p >= 2, advection/solveSubStep.m:69-98)."""
+
+    def __init__(self, **kw):
+        kw = dict(kw)
+        kw.setdefault('testcase', 'adjoint')
+        kw['isSlopeLim'] = True
+        kw['typeSlopeLim'] = 'linear'
+        self.op = AdjointOracle.__new__(AdjointOracle)
+        AdjointOracle.__init__(self.op, **dict(kw, isSlopeLim=False))
+        pd = adv.Struct(kw)
+        pd.problemName = 'advection'
+        for f in (adv.configureProblem, adv.preprocessProblem, adv.initializeProblem):
+            pd = f(pd)
+        self.pd = pd
+        self.mf = MF.MatFree(pd)
+        self.P = np.linalg.solve(self.mf.MDT, self.mf.M)        # Taylor = P modal
+        self.Pinv = np.linalg.solve(self.mf.M, self.mf.MDT)
+        self.omega = self.op.omega
+
+    def set_modes(self, velocities):
+        self.op.set_modes(velocities)
+
+    def T(self, c):
+        return np.einsum('kij,kj->ki', self.P, c)
+
+    def Tinv(self, cT):
+        return np.einsum('kij,kj->ki', self.Pinv, cT)
+
+    def forward(self, c0, nSteps, frozen=False):
+        """frozen=True replays the choices of the last unfrozen run (for finite differences of
+        the differentiable branch)."""
+        pd, g = self.pd, self.pd.g
+        K, N = pd.K, pd.N
+        tau = pd.tau
+        none = np.zeros((K, 3), dtype=bool)
+        cD = np.zeros((K, 3))                                   # the adjoint case: c_D = 0
+        c = np.asarray(c0, dtype=np.float64).reshape(K, N).copy()
+        if not frozen:
+            self.rec, self.choices = [], []
+        for n in range(nSteps):
+            cn = c
+            stages, chs = [], []
+            for s, w in enumerate(self.omega):
+                cdot = self.op.A(c.reshape(-1)).reshape(K, N)
+                cdotRaw = cdot
+                chd = None
+                if pd.p > 1:
+                    cT = self.T(cdot)
+                    if frozen:
+                        cTL = limit_frozen(cT, self.choices[n][s][0])
+                    else:
+                        chd = limiter_choices(self.mf, cT, none, np.full((K, 3), np.nan))
+                        cTL = self.mf.limit_taylor(cT, none, np.full((K, 3), np.nan), 'linear')
+                    cdot = self.Tinv(cTL + np.einsum('kij,kj->ki', self.mf.Mcorr, cT - cTL))
+                y = w * cn + (1 - w) * (c + tau * cdot)
+                if frozen:
+                    c = self.Tinv(limit_frozen(self.T(y), self.choices[n][s][1]))
+                else:
+                    stages.append((c, cdotRaw, y))
+                    chs.append((chd, limiter_choices(self.mf, self.T(y), g.markV0TbdrD, cD)))
+                    c = self.mf.limit_disc(y, g.markV0TbdrD, cD)
+            if not frozen:
+                self.rec.append(stages)
+                self.choices.append(chs)
+        return c
+
+    def backward(self, dJdcT):
+        pd, g = self.pd, self.pd.g
+        K, N = pd.K, pd.N
+        tau = pd.tau
+        none = np.zeros((K, 3), dtype=bool)
+        cD = np.zeros((K, 3))
+        lam = np.asarray(dJdcT, dtype=np.float64).reshape(K, N).copy()
+        gth = np.zeros(len(self.op.modes))
+        PinvT = lambda x: np.einsum('kji,kj->ki', self.Pinv, x)
+        PT = lambda x: np.einsum('kji,kj->ki', self.P, x)
+        for stages in reversed(self.rec):
+            mu, accn = lam, np.zeros_like(lam)
+            for s in reversed(range(len(self.omega))):
+                w = self.omega[s]
+                cs, cdotRaw, y = stages[s]
+                # solution limiter
+                yT = self.T(y)
+                ch = limiter_choices(self.mf, yT, g.markV0TbdrD, cD)
+                muY = PT(limiter_vjp_taylor(yT, ch, PinvT(mu)))
+                accn += w * muY
+                lamDot = (1 - w) * tau * muY
+                # time-derivative limiter with the Taylor mass correction
+                if pd.p > 1:
+                    dT = self.T(cdotRaw)
+                    chd = limiter_choices(self.mf, dT, none, np.full((K, 3), np.nan))
+                    lT = PinvT(lamDot)
+                    McT = np.einsum('kji,kj->ki', self.mf.Mcorr, lT)
+                    lamDot = PT(McT + limiter_vjp_taylor(dT, chd, lT - McT))
+                flat = lamDot.reshape(-1)
+                if self.op.modes:
+                    Mmu = self.op.lu.solve(flat)
+                    gth += np.array([Mmu @ (Bm @ cs.reshape(-1)) for Bm in self.op.modes])
+                mu = (1 - w) * muY + self.op.AT(flat).reshape(K, N)
+            lam = accn + mu
+        return lam, gth

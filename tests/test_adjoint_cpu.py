@@ -96,3 +96,45 @@ def test_checkpoint_schedule_reverses_every_step_within_its_slots(lib, nSteps, n
         assert advanced.max() <= r
     if slots == nSteps:
         assert advanced.max() <= 1      # every state stored once, nothing recomputed
+
+
+@pytest.mark.parametrize('p,steps', [(1, 6), (2, 6), (3, 3)])
+def test_limited_oracle_gradient_matches_finite_differences(p, steps):
+    """The scheme with the linear limiter.  The limiter is piecewise rational; directions scaled
+    by each coefficient's magnitude keep the near-zero elements (where the 1e-8 tolerance sets
+    the limiter factor) in their linear regime, and there the adjoint matches central
+    differences of the full run and of the run with the limiter's choices frozen."""
+    from oracle import adjoint as OA
+    kw = dict(hmax=2 ** -3, p=p, numSteps=steps, tEnd=steps * 2e-4)
+    o = OA.LimitedAdjointOracle(**kw)
+    o.set_modes(OA.mode_velocities())
+    c0 = o.pd.cDisc
+    cstar = OA.LimitedAdjointOracle(adjointTarget=True, **kw).forward(c0, steps)
+    cT = o.forward(c0, steps)
+    assert np.linalg.norm(o.forward(c0, steps, frozen=True) - cT) <= 1e-14 * np.linalg.norm(cT)
+    g0, gth = o.backward(cT - cstar)
+    h = 1e-5
+    rng = np.random.default_rng(5)
+    d = rng.standard_normal(c0.shape) * np.abs(c0)
+    J = lambda c, fr: 0.5 * float(np.sum((o.forward(c, steps, frozen=fr) - cstar) ** 2))
+    for fr in (True, False):
+        fd = (J(c0 + h * d, fr) - J(c0 - h * d, fr)) / (2 * h)
+        o.forward(c0, steps)                        # the base point's choices again
+        assert abs(fd - float(np.sum(g0 * d))) <= 1e-6 * abs(fd)
+    th0 = o.pd.theta.copy()
+    dt = rng.standard_normal(th0.size) * np.abs(th0)
+    o.op.set_theta(th0 + h * dt)
+    Jp = J(c0, False)
+    o.op.set_theta(th0 - h * dt)
+    Jm = J(c0, False)
+    o.op.set_theta(th0)
+    assert abs((Jp - Jm) / (2 * h) - float(gth @ dt)) <= 1e-6 * abs((Jp - Jm) / (2 * h))
+
+
+def test_limited_oracle_forward_is_the_reference_run():
+    from oracle import adjoint as OA
+    from oracle import advection as adv
+    kw = dict(hmax=2 ** -3, p=2, numSteps=5, tEnd=5 * 2e-4)
+    o = OA.LimitedAdjointOracle(**kw)
+    ref = adv.main(testcase='adjoint', isSlopeLim=True, typeSlopeLim='linear', **kw).cDisc
+    assert np.linalg.norm(o.forward(o.pd.cDisc, 5) - ref) <= 1e-14 * np.linalg.norm(ref)

@@ -1,5 +1,6 @@
 """GPU adjoint: gradients through the C-ABI against the oracle's transposed assembled operators
-and against central finite differences of the GPU forward run.
+(and, with the linear limiter, the oracle's limiter adjoint) and against central finite
+differences of the GPU forward run.
 
 Bars: FP64 relative L2 <= 1e-11 against the oracle (dJ/dc0 and dJ/dtheta; the reduction orders
 differ); FP64 finite differences (h = 1e-6) within 1e-7 of the adjoint's directional derivative;
@@ -119,10 +120,70 @@ def test_autograd_function_gives_the_adjoint_gradient(lib):
         pd.solver.close()
 
 
-def test_limited_runs_have_no_adjoint(lib):
+def limited_oracle_gradient(kw):
+    from oracle import adjoint as OA
+    o = OA.LimitedAdjointOracle(**kw)
+    o.set_modes(OA.mode_velocities())
+    c0 = o.pd.cDisc
+    cstar = OA.LimitedAdjointOracle(adjointTarget=True, **kw).forward(c0, kw['numSteps'])
+    cT = o.forward(c0, kw['numSteps'])
+    g0, gth = o.backward(cT - cstar)
+    return c0, cstar, 0.5 * float(np.sum((cT - cstar) ** 2)), g0, gth
+
+
+LIMITED = [dict(hmax=2 ** -3, p=2, numSteps=8, tEnd=8 * 2e-4),
+           dict(hmax=2 ** -3, p=1, numSteps=8, tEnd=8 * 2e-4),
+           dict(hmax=2 ** -3, p=3, numSteps=4, tEnd=4 * 2e-4)]
+
+
+@pytest.mark.parametrize('kw', LIMITED, ids=['p2', 'p1', 'p3'])
+@pytest.mark.parametrize('snaps', [0, 3])
+def test_limited_fp64_gradient_matches_oracle(lib, kw, snaps):
+    """The linear limiter's adjoint (frozen choices recomputed from the recorded limiter inputs)
+    against the oracle's, written in the reference's Taylor basis; both stage storage and
+    recomputing checkpoints."""
+    from festung_gb300 import adjoint as AD
+    c0, cstar, Jo, og0, ogth = limited_oracle_gradient(kw)
+    pd = AD.setup(precision='fp64', isSlopeLim=True, **kw)
+    try:
+        J, g0, gth = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=snaps)
+    finally:
+        pd.solver.close()
+    assert abs(J - Jo) <= 1e-12 * Jo
+    assert rel(g0, og0) <= 1e-11
+    assert rel(gth, ogth) <= 1e-11
+
+
+def test_limited_theta_gradient_matches_finite_differences(lib):
+    """Velocity perturbations move every element together and stay on one side of the
+    limiter's switches at h = 1e-6: the adjoint matches central differences.  (Random
+    perturbations of the initial coefficients cross a switch somewhere on a mesh this size;
+    the oracle test checks those directions on the run with frozen choices.)"""
+    from festung_gb300 import adjoint as AD
+    kw = dict(hmax=2 ** -6, p=2, numSteps=40, tEnd=40 * 2e-4)
+    tg = AD.setup(precision='fp64', adjointTarget=True, isSlopeLim=True, **kw)
+    tg.solver.step(kw['numSteps'], 0, tg.tau)
+    cstar = tg.solver.get_state()
+    tg.solver.close()
+    pd = AD.setup(precision='fp64', isSlopeLim=True, **kw)
+    try:
+        c0 = np.asfortranarray(pd._cDisc)
+        J, g0, gth = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
+        rng = np.random.default_rng(11)
+        h = 1e-6
+        for _ in range(2):
+            dt = rng.standard_normal(gth.size) * np.abs(pd.theta)
+            fd = (AD.misfit(pd, c0, pd.theta + h * dt, cstar) - AD.misfit(pd, c0, pd.theta - h * dt, cstar)) / (2 * h)
+            assert abs(fd - gth @ dt) <= 1e-7 * abs(fd)
+    finally:
+        pd.solver.close()
+
+
+def test_hierarchical_limiter_has_no_adjoint(lib):
     from festung_gb300 import _lib as L
     from festung_gb300 import adjoint as AD
-    pd = AD.setup(precision='fp64', hmax=2 ** -3, p=1, numSteps=2, tEnd=4e-4, isSlopeLim=True)
+    pd = AD.setup(precision='fp64', hmax=2 ** -3, p=2, numSteps=2, tEnd=4e-4, isSlopeLim=True,
+                  typeSlopeLim='hierarch_vert')
     try:
         with pytest.raises(L.DgadvError) as e:
             pd.solver.forward_record(2, pd.tau, 0)
