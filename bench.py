@@ -321,6 +321,42 @@ def adjoint_block(reps=3, fd_dirs=4):
     rel = lambda a, b: float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
     out['fp32_vs_fp64_grad_rel_l2'] = {'dJdc0': rel(grads['fp32'][0], grads['fp64'][0]),
                                        'dJdtheta': rel(grads['fp32'][1], grads['fp64'][1])}
+    # the same workload with the linear limiter on (its adjoint through the limiter's choices)
+    lim = {}
+    tg = AD.setup(precision='fp64', adjointTarget=True, isSlopeLim=True, **kw)
+    tg.solver.step(kw['numSteps'], 0, tg.tau)
+    cstarL = tg.solver.get_state()
+    tg.solver.close()
+    for prec in ('fp64', 'fp32'):
+        pd = AD.setup(precision=prec, isSlopeLim=True, **kw)
+        s = pd.solver
+        c0 = np.asfortranarray(pd._cDisc)
+        s.set_state(c0); s.step(kw['numSteps'], 0, pd.tau); s.sync()
+        tf = []
+        for _ in range(reps):
+            t = time.perf_counter(); s.set_state(c0); s.step(kw['numSteps'], 0, pd.tau); s.sync()
+            tf.append(time.perf_counter() - t)
+        row = {'forward_ms': 1e3 * min(tf)}
+        for name, snaps in (('stages_stored', 0), ('snapshots_20', 20)):
+            tb = []
+            for _ in range(reps + 1):
+                s.set_velocity_theta(pd.theta); s.set_state(c0)
+                s.forward_record(kw['numSteps'], pd.tau, snaps); s.sync()
+                r = s.get_state() - cstarL
+                t = time.perf_counter(); g0, gth = s.backward(r); tb.append(time.perf_counter() - t)
+            row[name] = {'backward_ms': 1e3 * min(tb[1:]), 'backward_over_forward': min(tb[1:]) / min(tf)}
+        if prec == 'fp64' and fd_dirs:
+            rng = np.random.default_rng(1)
+            h = 1e-6
+            errs = []
+            for _ in range(fd_dirs):
+                dt = rng.standard_normal(gth.size) * np.abs(pd.theta)
+                fd = (AD.misfit(pd, c0, pd.theta + h * dt, cstarL) - AD.misfit(pd, c0, pd.theta - h * dt, cstarL)) / (2 * h)
+                errs.append(abs(fd - float(gth @ dt)) / abs(fd))
+            row['fd_theta_max_rel_err'] = max(errs)
+        lim[prec] = row
+        s.close()
+    out['linear_limiter'] = lim
     return out
 
 
