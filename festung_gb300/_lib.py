@@ -11,12 +11,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libdgadv.so')
 
 DGADV_OK, DGADV_EINVAL, DGADV_ECUDA, DGADV_ENOMEM, DGADV_EMESH = 0, 1, 2, 3, 4
-DGADV_ENONFINITE, DGADV_ETIMEOUT, DGADV_EUNSUPPORTED = 5, 6, 7
+DGADV_ENONFINITE, DGADV_ETIMEOUT, DGADV_EUNSUPPORTED, DGADV_EIO = 5, 6, 7, 8
 FP64, FP32, DF32 = 0, 1, 2
 LIM_LINEAR, LIM_HIERARCH_VERT, LIM_STRICT = 0, 1, 2
 TIME_CONST, TIME_EXP_NEG = 0, 1
 FLAG_NO_REORDER, FLAG_NO_SHIFT, FLAG_NO_GRAPH, FLAG_NO_PDL, FLAG_FUSE, FLAG_PERSIST = 1, 2, 4, 8, 16, 32
 OPT_GRAPH_STEPS, OPT_FLAGS, OPT_PERSIST_BLOCKS = 1, 2, 3
+OUT_VTK, OUT_TEC = 1, 2
+OUTPUT_TYPES = {'vtk': OUT_VTK, 'tec': OUT_TEC}
 
 LIMITER_TYPES = {'linear': LIM_LINEAR, 'hierarch_vert': LIM_HIERARCH_VERT, 'strict': LIM_STRICT}
 
@@ -82,6 +84,12 @@ SYMBOLS = {
     'dgadv_forward_record': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_int32]),
     'dgadv_backward': (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp]),
     'dgadv_checkpoint_schedule': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i32p]),
+    'dgadv_get_lagrange': (ctypes.c_int, [ctypes.c_void_p, _dp, _i32p]),
+    'dgadv_output': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32,
+                                    ctypes.c_int32]),
+    'dgadv_output_wait': (ctypes.c_int, [ctypes.c_void_p]),
+    'dgadv_write_lagrange': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _dp, _i32p, ctypes.c_int32, _dp,
+                                            ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32]),
     'dgadv_limit_linear_noalloc': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -153,6 +161,29 @@ def grid_build(coordV, V0T):
                coordV0T=arr(g.coordV0T, (T, 3, 2), np.float64), detJ0T=arr(g.detJ0T, (T,), np.float64))
     lib.dgadv_grid_free(out)
     return res
+
+
+def output_types(types):
+    """'vtk' / 'tec' or a list of them (the reference's outputTypes) -> DGADV_OUT_* bits."""
+    if isinstance(types, str):
+        types = [types]
+    bits = 0
+    for t in types:
+        if t not in OUTPUT_TYPES:
+            raise ValueError('Unknown file type: %s' % t)
+        bits |= OUTPUT_TYPES[t]
+    return bits
+
+
+def write_lagrange(coordV, V0T, dataLagr, varName, fileName, tLvl, types='vtk'):
+    """Host-only writer (core/visualizeDataLagr.m): coordV numV x 2, V0T numT x 3 (0-based),
+    dataLagr numT x numP with numP in {1, 3, 6}."""
+    lib = load()
+    cV = f64(coordV)
+    V = np.require(np.asarray(V0T, dtype=np.int32), requirements=['F', 'A'])
+    d = f64(dataLagr)
+    check(lib.dgadv_write_lagrange(V.shape[0], cV.shape[0], ptr(cV), ptr(V, _i32p), d.shape[1], ptr(d),
+                                   varName.encode(), fileName.encode(), int(tLvl), output_types(types)))
 
 
 def checkpoint_schedule(nSteps, nSnapshots):

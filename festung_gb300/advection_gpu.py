@@ -155,7 +155,10 @@ def configureProblem(pd):
     setdefault(pd, 'tEnd', (pd.numSteps / (3142 * 1.5)) * 2 * np.pi)
     setdefault(pd, 'isSlopeLim', False)
     setdefault(pd, 'typeSlopeLim', 'linear')
-    setdefault(pd, 'isVisSol', False)
+    setdefault(pd, 'isVisSol', False)          # the reference defaults to true (writes files)
+    setdefault(pd, 'outputFrequency', 100)
+    setdefault(pd, 'outputBasename', 'output/advection_' + pd.typeSlopeLim)
+    setdefault(pd, 'outputTypes', ['vtk'])
     setdefault(pd, 'precision', 'fp64')
     setdefault(pd, 'device', 0)
     setdefault(pd, 'gpuFlags', 0)
@@ -245,6 +248,8 @@ def initializeProblem(pd):
     pd._cDisc = np.ascontiguousarray(c)
     pd._stale = False
     pd.initialError = l2_error(pd.g, pd.tables, pd._cDisc, pd.c0Cont, 2 * pd.p)
+    if pd.isVisSol:
+        pd.solver.output(pd.outputBasename, 0, pd.outputTypes)
     return pd
 
 
@@ -274,11 +279,19 @@ def postprocessStep(pd, nStep):
 
 
 def outputStep(pd, nStep):
+    """advection/outputStep.m:53-66: nodal values of u_h every outputFrequency steps, written to
+    <outputBasename>.<nStep>.vtu / .plt by the library's writer thread (the call only enqueues)."""
+    if pd.isVisSol and nStep % pd.outputFrequency == 0:
+        pd.solver.output(pd.outputBasename, nStep, pd.outputTypes)
     return pd
 
 
 def postprocessProblem(pd):
-    """advection/postprocessProblem.m:43-82 (error against the exact or the initial data)."""
+    """advection/postprocessProblem.m:43-82 (output, then the error against the exact or the
+    initial data)."""
+    if pd.isVisSol:
+        pd.solver.output(pd.outputBasename, pd.numSteps, pd.outputTypes)
+        pd.solver.output_wait()
     pd.cDisc = cDisc(pd)
     if pd.isAnalytical:
         f = lambda x1, x2: pd.cCont(pd.tEnd, x1, x2)

@@ -33,7 +33,7 @@ def sources():
                                             'dgadv_prec_fp64.cu', 'dgadv_prec_fp32.cu',
                                             'dgadv_prec_df32_p01.cu', 'dgadv_prec_df32_p2.cu',
                                             'dgadv_prec_df32_p3.cu', 'dgadv_adjoint.cu',
-                                            'dgadv_noalloc.cu')]
+                                            'dgadv_noalloc.cu', 'dgadv_vis.cpp', 'dgadv_output.cu')]
 
 
 def _stale():
@@ -62,7 +62,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
             cmd = [nvcc, '-O3', '-std=c++17', *ARCH, '-lineinfo', '-Xcompiler', '-fPIC,-ffp-contract=off',
                    *inc, *extra_nvcc, '-c', src, '-o', obj]
         else:
-            cmd = ['g++', '-O2', '-std=c++17', '-fPIC', '-ffp-contract=off', *inc, '-I',
+            cmd = ['g++', '-O2', '-std=c++17', '-fPIC', '-pthread', '-ffp-contract=off', *inc, '-I',
                    os.path.join(cuda, 'include'), '-c', src, '-o', obj]
         jobs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     failed = []
@@ -75,7 +75,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
     if failed:
         raise RuntimeError('build failed:\n' + '\n'.join(failed))
     tmp = OUT + '.tmp'
-    link = [nvcc, '-shared', *ARCH, '-o', tmp, *objs, '-lcudart']
+    link = [nvcc, '-shared', *ARCH, '-o', tmp, *objs, '-lcudart', '-Xcompiler', '-pthread']
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode:
         raise RuntimeError('link failed:\n' + r.stdout.decode(errors='replace'))

@@ -111,6 +111,7 @@ extern "C" const char *dgadv_status_string(int s) {
     case DGADV_ENONFINITE: return "non-finite value in the state";
     case DGADV_ETIMEOUT: return "bounded device wait timed out";
     case DGADV_EUNSUPPORTED: return "unsupported option";
+    case DGADV_EIO: return "output file could not be written";
   }
   return "unknown status";
 }

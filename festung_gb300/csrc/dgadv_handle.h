@@ -13,7 +13,10 @@
 #include "../../include/dgadv.h"
 #include "dgadv_host.h"
 
+struct dgadv_handle;
 namespace dgadv {
+struct OutputQueue;
+void output_release(dgadv_handle *h);   // joins the writer thread, frees the output buffers
 constexpr int kBlock = 128;       // elements per CTA (one thread per element)
 constexpr int kSlotCopies = 32;   // copies of the global min / max slots (atomics spread over them)
 constexpr int kGridBarBytes = 8192;   // state of the persistent step's grid barrier
@@ -51,6 +54,9 @@ struct dgadv_handle {
   std::vector<double> detJ, areaE0T, Bhost;   // internal order
   std::vector<uint8_t> markNotN;              // internal order, 3 per element
   std::vector<int> permv;                     // internal -> external element id
+  std::vector<double> visCoordV;              // caller's vertices, numV x 2 row-major (output files)
+  std::vector<int32_t> visV0T;                // caller's V0T, numT x 3 row-major
+  dgadv::OutputQueue *outq = nullptr;         // solution output (dgadv_output), made on first use
   dgadv::RefTables tables;
   // CUDA graphs of a chunk of steps, one per phase (limPass mod 3) at the chunk start
   cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};

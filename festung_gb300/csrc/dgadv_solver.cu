@@ -104,6 +104,8 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
   Grid gr;
   if (!build_grid(mesh->numV, mesh->coordV, mesh->numT, mesh->V0T, gr, h->err)) return DGADV_EMESH;
   if (!build_ref_tables(h->p, h->tables, h->err)) return DGADV_EINVAL;
+  h->visCoordV = gr.coordV;
+  h->visV0T = gr.V0T;
   const int K = gr.numT, N = h->N;
   h->K = K; h->Kp = (K + kBlock - 1) / kBlock * kBlock;   // whole blocks of rows for the bulk copies
   h->Q = h->tables.Q; h->R = h->tables.R;
@@ -668,6 +670,7 @@ extern "C" void dgadv_destroy(dgadv_handle *h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  output_release(h);
   for (int i = 0; i < 3; ++i)
     if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
   if (h->adjExec) cudaGraphExecDestroy(h->adjExec);

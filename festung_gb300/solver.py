@@ -108,6 +108,25 @@ class DeviceSolver:
     def limit_state(self, t):
         self._c(self._lib.dgadv_limit_state(self._h, float(t)))
 
+    def get_lagrange(self):
+        """projectDataDisc2DataLagr of the current state on the device: K x numP nodal values."""
+        numP = 1 if self.p == 0 else (3 if self.p == 1 else 6)
+        out = np.zeros((self.K, numP), order='F')
+        n = ctypes.c_int32()
+        self._c(self._lib.dgadv_get_lagrange(self._h, L.ptr(out), ctypes.byref(n)))
+        assert n.value == numP
+        return out
+
+    def output(self, fileName, tLvl, types='vtk', varName='u_h'):
+        """visualizeDataLagr(g, projectDataDisc2DataLagr(cDisc), varName, fileName, tLvl, types),
+        enqueued: the files are written by the library's writer thread while later steps run."""
+        self._c(self._lib.dgadv_output(self._h, varName.encode(), fileName.encode(), int(tLvl),
+                                       L.output_types(types)))
+
+    def output_wait(self):
+        """Waits for every output file; raises if one could not be written."""
+        self._c(self._lib.dgadv_output_wait(self._h))
+
     def step(self, nSteps, nStep0, tau):
         self._c(self._lib.dgadv_step(self._h, int(nSteps), int(nStep0), float(tau)))
 

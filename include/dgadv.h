@@ -35,7 +35,8 @@ enum {
   DGADV_EMESH = 4,         /* inconsistent mesh (non-manifold edge, bad vertex id, ...)     */
   DGADV_ENONFINITE = 5,    /* a kernel found NaN/Inf in the state                          */
   DGADV_ETIMEOUT = 6,      /* a bounded device-side wait gave up                           */
-  DGADV_EUNSUPPORTED = 7   /* option not supported by this build (e.g. p > 3 on the GPU)  */
+  DGADV_EUNSUPPORTED = 7,  /* option not supported by this build (e.g. p > 3 on the GPU)  */
+  DGADV_EIO = 8            /* an output file could not be written                          */
 };
 
 /* Arithmetic of the stored state and of every kernel: FP64; FP32; or DF32, each real an
@@ -188,6 +189,37 @@ int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *value);
  * kernels does; the error is then cleared and the handle stays usable.  No counterpart in the
  * reference. */
 int dgadv_selftest_wait(dgadv_handle *h, double seconds);
+
+/* ---- solution output ------------------------------------------------------------------
+ * The reference writes u_h at the Lagrange nodes of each triangle (projectDataDisc2DataLagr):
+ * numP = 1 value at the centroid (p = 0), 3 at the vertices (p = 1), or 6 at the vertices and
+ * edge midpoints (p >= 2), as VTK XML (.vtu) and / or Tecplot ASCII (.plt) files named
+ * <fileName>.<tLvl>.vtu / .plt (core/visualizeDataLagr.m:114-291, scalar data); missing
+ * directories of fileName are created. */
+enum { DGADV_OUT_VTK = 1, DGADV_OUT_TEC = 2 };
+
+/* Replaces core/projectDataDisc2DataLagr.m:43-57 on the current state: dataLagr is K x numP
+ * (*numP written if not NULL).  Synchronous. */
+int dgadv_get_lagrange(dgadv_handle *h, double *dataLagr, int32_t *numP);
+
+/* Replaces the output of advection/outputStep.m:53-66 (projectDataDisc2DataLagr +
+ * visualizeDataLagr): evaluates the nodal values on the device, copies them to a pinned host
+ * buffer on the handle's stream and returns; a writer thread of the handle writes the files
+ * when the copy has landed, while later steps run.  At most two outputs are in flight (a third
+ * call waits for the writer). */
+int dgadv_output(dgadv_handle *h, const char *varName, const char *fileName, int32_t tLvl,
+                 int32_t fileTypes);
+
+/* Waits until every output file of the handle is written; DGADV_EIO (message in
+ * dgadv_last_error) if one could not be.  dgadv_destroy also finishes pending files. */
+int dgadv_output_wait(dgadv_handle *h);
+
+/* Host-only writer, core/visualizeDataLagr.m:114-291 for one scalar variable: the mesh
+ * in the layout of dgadv_mesh: coordV numV x 2, V0T numT x 3, 0-based; dataLagr numT x numP with
+ * numP in {1, 3, 6}. */
+int dgadv_write_lagrange(int32_t numT, int32_t numV, const double *coordV, const int32_t *V0T,
+                         int32_t numP, const double *dataLagr, const char *varName,
+                         const char *fileName, int32_t tLvl, int32_t fileTypes);
 
 /* Number of kernels one time step launches (for launch accounting). */
 int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count);
