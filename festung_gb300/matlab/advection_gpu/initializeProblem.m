@@ -8,4 +8,8 @@ if problemData.isSlopeLim
   dgadv_mex('limit_state', problemData.gpu, 0);
   problemData.cDisc = dgadv_mex('get_state', problemData.gpu, problemData.K, problemData.N);
 end % if
+if problemData.isVisSol   % advection/initializeProblem.m:80-86
+  dgadv_mex('output', problemData.gpu, 'u_h', problemData.outputBasename, 0, ...
+            outputTypeBits(problemData.outputTypes));
+end % if
 end % function

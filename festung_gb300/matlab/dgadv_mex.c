@@ -136,6 +136,14 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     const mwSize K = (mwSize)mxGetScalar(prhs[2]), N = (mwSize)mxGetScalar(prhs[3]);
     plhs[0] = mxCreateDoubleMatrix(K, N, mxREAL);
     check(dgadv_get_state(h, mxGetPr(plhs[0])), h);
+  } else if (!strcmp(cmd, "output")) {
+    /* dgadv_mex('output', h, varName, fileName, tLvl, fileTypes): fileTypes 1 vtk, 2 tec, 3 both */
+    char var[256], file[4096];
+    if (nrhs < 6 || mxGetString(prhs[2], var, sizeof var) || mxGetString(prhs[3], file, sizeof file))
+      mexErrMsgIdAndTxt("dgadv:arg", "output: varName, fileName, tLvl, fileTypes expected");
+    check(dgadv_output(h, var, file, (int32_t)mxGetScalar(prhs[4]), (int32_t)mxGetScalar(prhs[5])), h);
+  } else if (!strcmp(cmd, "output_wait")) {
+    check(dgadv_output_wait(h), h);
   } else if (!strcmp(cmd, "destroy")) {
     for (int i = 0; i < MAX_HANDLES; ++i) if (g_open[i] == h) g_open[i] = NULL;
     dgadv_destroy(h);
