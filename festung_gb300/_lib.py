@@ -18,6 +18,9 @@ TIME_CONST, TIME_EXP_NEG = 0, 1
 FLAG_NO_REORDER, FLAG_NO_SHIFT, FLAG_NO_GRAPH, FLAG_NO_PDL, FLAG_FUSE, FLAG_PERSIST = 1, 2, 4, 8, 16, 32
 OPT_GRAPH_STEPS, OPT_FLAGS, OPT_PERSIST_BLOCKS = 1, 2, 3
 OUT_VTK, OUT_TEC = 1, 2
+FN_CONST, FN_POLY3, FN_SOLID_BODY, FN_GAUSS_SLOT, FN_GAUSS, FN_TRANSIENT = 0, 1, 2, 3, 4, 5
+VEL_ROTATION, VEL_TRANSIENT, VEL_STREAM = 16, 17, 18
+FN_MAX_PARAMS = 64
 OUTPUT_TYPES = {'vtk': OUT_VTK, 'tec': OUT_TEC}
 
 LIMITER_TYPES = {'linear': LIM_LINEAR, 'hierarch_vert': LIM_HIERARCH_VERT, 'strict': LIM_STRICT}
@@ -49,6 +52,24 @@ class Params(ctypes.Structure):
     _fields_ = [('p', ctypes.c_int32), ('ordRK', ctypes.c_int32), ('precision', ctypes.c_int32),
                 ('isSlopeLim', ctypes.c_int32), ('typeSlopeLim', ctypes.c_int32),
                 ('device', ctypes.c_int32), ('flags', ctypes.c_int32)]
+
+
+class Function(ctypes.Structure):
+    _fields_ = [('kind', ctypes.c_int32), ('nParams', ctypes.c_int32), ('params', _dp)]
+
+
+def functions(specs):
+    """(kind, params) pairs -> a ctypes array of dgadv_function (and the parameter arrays it
+    points into, which must stay alive during the call)."""
+    arr = (Function * len(specs))()
+    keep = []
+    for i, (kind, params) in enumerate(specs):
+        p = np.ascontiguousarray(np.asarray(params if params is not None else [], dtype=np.float64))
+        keep.append(p)
+        arr[i].kind = int(kind)
+        arr[i].nParams = p.size
+        arr[i].params = p.ctypes.data_as(_dp) if p.size else None
+    return arr, keep
 
 
 SYMBOLS = {
@@ -84,6 +105,11 @@ SYMBOLS = {
     'dgadv_forward_record': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_int32]),
     'dgadv_backward': (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp]),
     'dgadv_checkpoint_schedule': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i32p]),
+    'dgadv_project_state': (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Function), ctypes.c_int32,
+                                           ctypes.c_double, ctypes.c_int32]),
+    'dgadv_set_velocity_function': (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Function), ctypes.c_int32]),
+    'dgadv_l2_error': (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Function), ctypes.c_int32, ctypes.c_double,
+                                      ctypes.c_int32, _dp]),
     'dgadv_get_lagrange': (ctypes.c_int, [ctypes.c_void_p, _dp, _i32p]),
     'dgadv_output': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32,
                                     ctypes.c_int32]),

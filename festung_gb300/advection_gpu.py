@@ -162,6 +162,7 @@ def configureProblem(pd):
     setdefault(pd, 'precision', 'fp64')
     setdefault(pd, 'device', 0)
     setdefault(pd, 'gpuFlags', 0)
+    setdefault(pd, 'setupOnDevice', True)      # projections, velocity data, L2 errors on the GPU
     assert not pd.isQuadri, 'advection_gpu supports triangles only (isQuadri = false).'
     assert 0 <= pd.p <= 4, 'Polynomial order must be zero to four.'
     assert 1 <= pd.ordRK <= 3, 'Order of Runge Kutta must be zero to three.'
@@ -169,13 +170,14 @@ def configureProblem(pd):
     assert pd.numSteps > 0, 'Number of time steps must be positive.'
     assert (not pd.isSlopeLim) or pd.p > 0, 'Slope limiting only available for p > 0.'
     TC.configure(pd)
+    pd.deviceFns = TC.device_functions(pd) if pd.setupOnDevice else None
     return pd
 
 
 def host_preprocess(pd):
-    """The host part of advection/preprocessProblem.m:48-112: grid, markers, tables, velocity
-    data (advection/preprocessSubStep.m:72-79, time-independent) and the separable
-    right-hand-side terms; no device work."""
+    """The host part of advection/preprocessProblem.m:48-112: grid, markers, tables, the
+    separable right-hand-side terms, and (without device functions for the case) the velocity
+    data (advection/preprocessSubStep.m:72-79, time-independent); no device work."""
     coordV, V0T, dim, h = TC.square_coords(pd.hmax)
     coordV = TC.jitter_coords(coordV, h, pd.jitter, pd.meshSeed)
     g = L.grid_build(coordV, V0T)
@@ -195,9 +197,11 @@ def host_preprocess(pd):
     _, _, W = tables.rule2(qv)
     P = tables.phi2D(qv)
     pd.hatM = (W[:, None] * P).T @ P
-    pd.u1Disc = project(g, tables, pd.u1Cont, 2 * pd.p, pd.hatM)
-    pd.u2Disc = project(g, tables, pd.u2Cont, 2 * pd.p, pd.hatM)
-    pd.vNormalOnQuadEdge = normal_velocity(g, tables, pd.u1Cont, pd.u2Cont, 2 * pd.p + 1)
+    if not pd.get('deviceFns'):
+        pd.u1Disc = project(g, tables, pd.u1Cont, 2 * pd.p, pd.hatM)
+        pd.u2Disc = project(g, tables, pd.u2Cont, 2 * pd.p, pd.hatM)
+    if not pd.get('deviceFns') or pd.cDTerms:     # the Dirichlet vectors need it on the host
+        pd.vNormalOnQuadEdge = normal_velocity(g, tables, pd.u1Cont, pd.u2Cont, 2 * pd.p + 1)
     # separable right-hand-side terms rhs_m = M f_m - K_D,m  (K_N = 0: no Neumann data)
     terms = {}
     detJ = g['detJ0T']
@@ -232,7 +236,10 @@ def preprocessProblem(pd):
                              isSlopeLim=pd.isSlopeLim, typeSlopeLim=pd.typeSlopeLim,
                              idE0T=m['idE0T'], markE0TbdrD=m['markE0TbdrD'],
                              markE0TbdrN=m['markE0TbdrN'], device=pd.device, flags=pd.gpuFlags)
-    pd.solver.set_velocity(pd.u1Disc, pd.u2Disc, pd.vNormalOnQuadEdge)
+    if pd.deviceFns:
+        pd.solver.set_velocity_function(pd.deviceFns['u'])
+    else:
+        pd.solver.set_velocity(pd.u1Disc, pd.u2Disc, pd.vNormalOnQuadEdge)
     pd.solver.set_source_terms(pd.srcTimeFn, pd.srcRhs, pd.srcCD)
     return pd
 
@@ -240,14 +247,18 @@ def preprocessProblem(pd):
 def initializeProblem(pd):
     """advection/initializeProblem.m:46-86: L2 projection of c0, initial limiting, error."""
     pd.isFinished = False
-    c = project(pd.g, pd.tables, pd.c0Cont, pd.qOrd, pd.hatM)
-    pd.solver.set_state(c)
+    if pd.deviceFns:
+        pd.solver.project_state(pd.deviceFns['c0'], 0.0, pd.qOrd)
+    else:
+        pd.solver.set_state(project(pd.g, pd.tables, pd.c0Cont, pd.qOrd, pd.hatM))
     if pd.isSlopeLim:
         pd.solver.limit_state(0.0)
-        c = pd.solver.get_state()
-    pd._cDisc = np.ascontiguousarray(c)
+    pd._cDisc = np.ascontiguousarray(pd.solver.get_state())
     pd._stale = False
-    pd.initialError = l2_error(pd.g, pd.tables, pd._cDisc, pd.c0Cont, 2 * pd.p)
+    if pd.deviceFns:
+        pd.initialError = pd.solver.l2_error(pd.deviceFns['c0'], 0.0, 2 * pd.p)
+    else:
+        pd.initialError = l2_error(pd.g, pd.tables, pd._cDisc, pd.c0Cont, 2 * pd.p)
     if pd.isVisSol:
         pd.solver.output(pd.outputBasename, 0, pd.outputTypes)
     return pd
@@ -293,6 +304,12 @@ def postprocessProblem(pd):
         pd.solver.output(pd.outputBasename, pd.numSteps, pd.outputTypes)
         pd.solver.output_wait()
     pd.cDisc = cDisc(pd)
+    if pd.deviceFns:
+        if pd.isAnalytical:
+            pd.error = pd.solver.l2_error(pd.deviceFns['cCont'], pd.tEnd, pd.qOrd)
+        else:
+            pd.error = pd.solver.l2_error(pd.deviceFns['c0'], 0.0, pd.qOrd)
+        return pd
     if pd.isAnalytical:
         f = lambda x1, x2: pd.cCont(pd.tEnd, x1, x2)
     else:

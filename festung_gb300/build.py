@@ -33,7 +33,13 @@ def sources():
                                             'dgadv_prec_fp64.cu', 'dgadv_prec_fp32.cu',
                                             'dgadv_prec_df32_p01.cu', 'dgadv_prec_df32_p2.cu',
                                             'dgadv_prec_df32_p3.cu', 'dgadv_adjoint.cu',
-                                            'dgadv_noalloc.cu', 'dgadv_vis.cpp', 'dgadv_output.cu')]
+                                            'dgadv_noalloc.cu', 'dgadv_vis.cpp', 'dgadv_output.cu',
+                                            'dgadv_setup.cu')]
+
+
+# per-unit extra flags: the set-up unit evaluates quadrature points and indicator functions
+# with separate roundings, as the host expressions do
+EXTRA_FLAGS = {'dgadv_setup.cu': ['-fmad=false']}
 
 
 def _stale():
@@ -60,7 +66,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
         objs.append(obj)
         if src.endswith('.cu'):
             cmd = [nvcc, '-O3', '-std=c++17', *ARCH, '-lineinfo', '-Xcompiler', '-fPIC,-ffp-contract=off',
-                   *inc, *extra_nvcc, '-c', src, '-o', obj]
+                   *inc, *extra_nvcc, *EXTRA_FLAGS.get(os.path.basename(src), []), '-c', src, '-o', obj]
         else:
             cmd = ['g++', '-O2', '-std=c++17', '-fPIC', '-pthread', '-ffp-contract=off', *inc, '-I',
                    os.path.join(cuda, 'include'), '-c', src, '-o', obj]

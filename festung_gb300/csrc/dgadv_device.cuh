@@ -1474,4 +1474,10 @@ __global__ void k_gather_out(int K, int Kp, int N, const int *__restrict__ perm,
   for (int i = 0; i < N; ++i) ext[(size_t)i * K + e] = double(c[(size_t)i * Kp + k]);
 }
 
+template <typename T>
+__global__ void k_from_f64(size_t n, const double *__restrict__ src, T *__restrict__ dst) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = T(src[i]);
+}
+
 }  // namespace dgadv

@@ -53,6 +53,7 @@ struct dgadv_handle {
   // host copies needed later
   std::vector<double> detJ, areaE0T, Bhost;   // internal order
   std::vector<uint8_t> markNotN;              // internal order, 3 per element
+  std::vector<double> nuE0T, corner0;         // internal order: 3 x 2 normals, first corner
   std::vector<int> permv;                     // internal -> external element id
   std::vector<double> visCoordV;              // caller's vertices, numV x 2 row-major (output files)
   std::vector<int32_t> visV0T;                // caller's V0T, numT x 3 row-major
@@ -146,6 +147,8 @@ struct PrecOps {
   cudaError_t (*vjp_scatter)(dgadv_handle *h, const void *x, long long pass);
   // device copy of a state-sized buffer (bytes a multiple of 16) ordered with dependent launches
   cudaError_t (*copy)(dgadv_handle *h, void *dst, const void *src, size_t bytes);
+  // n FP64 values on the device -> stored reals
+  cudaError_t (*from_f64)(dgadv_handle *h, void *dst, const double *src, size_t n);
 };
 
 // Fused path (linear limiter, zero Dirichlet data, opted in): per stage the operator kernel

@@ -418,6 +418,14 @@ static cudaError_t gather_out(dgadv_handle *h, const void *src) {
   return cudaGetLastError();
 }
 
+template <typename T>
+static cudaError_t from_f64(dgadv_handle *h, void *dst, const double *src, size_t n) {
+  const int grid = (int)std::min<size_t>((n + 255) / 256, 4096);
+  if (n == 0) return cudaSuccess;
+  k_from_f64<T><<<grid, 256, 0, h->stream>>>(n, src, (T *)dst);
+  return cudaGetLastError();
+}
+
 template <typename T, int MASK>
 static cudaError_t upload_tables_p(int p, const RefTables &rt) {
   switch (p) {
@@ -466,6 +474,7 @@ static PrecOps make_ops() {
   o.step_persist = nullptr;
   o.persist_attributes = nullptr;
   o.copy = copy_state;
+  o.from_f64 = from_f64<T>;
   return o;
 }
 

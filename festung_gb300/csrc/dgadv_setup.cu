@@ -1,0 +1,445 @@
+// Set-up work on the device: the steps either side of the time loop.
+//
+//   dgadv_project_state          projectFuncCont2DataDisc of the initial data
+//                                (core/projectFuncCont2DataDisc.m:94-102,
+//                                advection/initializeProblem.m:53)
+//   dgadv_set_velocity_function  u1Disc, u2Disc (order 2p) and vNormalOnQuadEdge (order 2p+1)
+//                                (advection/preprocessSubStep.m:72-79), turned into the stage
+//                                kernels' velocity factors
+//   dgadv_l2_error               computeL2Error (core/computeL2Error.m:97-114)
+//
+// The reference passes closures (advection/configureProblem.m:106-133); here the built-in test
+// cases' functions are device functions selected by dgadv_function.kind.  One thread per
+// element, internal element order, FP64 throughout; this unit compiles without FMA contraction
+// so that physical quadrature points and the discontinuous indicator functions evaluate as the
+// host expressions do.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dgadv_handle.h"
+
+namespace dgadv {
+namespace {
+
+constexpr int kSetupMaxN = (kMaxP + 1) * (kMaxP + 2) / 2;
+
+struct FnDesc {
+  int kind, n;
+  double p[DGADV_FN_MAX_PARAMS];
+};
+
+// Per-element FP64 geometry, SoA rows of K values in internal order.
+enum { G_X0, G_Y0, G_B11, G_B12, G_B21, G_B22, G_DETJ, G_NU, G_AE = G_NU + 6, kGeoRows = G_AE + 3 };
+
+struct SetupArgs {
+  int K, Kp, N, nFn;
+  const int *perm;       // internal -> caller element
+  const int *instOf;     // instance of each block of kBlock elements (null: one instance)
+  const double *geo;     // kGeoRows x K
+  const FnDesc *fns;
+  double t;
+};
+
+__device__ __forceinline__ const FnDesc *fn_of(const SetupArgs &a, int k) {
+  return a.fns + (a.nFn == 1 ? 0 : a.instOf[k / kBlock]);
+}
+
+__device__ __forceinline__ double sq(double x) { return x * x; }
+
+// Slotted cylinder of radius 0.15 at (0.5, 0.75) (advection/configureProblem.m:110).
+__device__ __forceinline__ double slotted_cylinder(double x, double y) {
+  return (sq(x - 0.5) + sq(y - 0.75) <= 0.0225 && (x <= 0.475 || x >= 0.525 || y >= 0.85)) ? 1.0 : 0.0;
+}
+
+__device__ double fn_scalar(const FnDesc *f, double t, double x, double y) {
+  const double *p = f->p;
+  switch (f->kind) {
+    case DGADV_FN_CONST:
+      return p[0];
+    case DGADV_FN_POLY3:
+      return p[0] + p[1] * x + p[2] * y + p[3] * x * x + p[4] * x * y + p[5] * y * y + p[6] * x * x * x +
+             p[7] * x * x * y + p[8] * x * y * y + p[9] * y * y * y;
+    case DGADV_FN_SOLID_BODY: {   // advection/configureProblem.m:109-113
+      const double cone = (1.0 / 0.15) * sqrt(sq(x - 0.5) + sq(y - 0.25));
+      const double hump = (1.0 / 0.15) * sqrt(sq(x - 0.25) + sq(y - 0.5));
+      return slotted_cylinder(x, y) + (1 - cone) * (sq(x - 0.5) + sq(y - 0.25) <= 0.0225 ? 1.0 : 0.0) +
+             0.25 * (1 + cos(M_PI * hump)) * (sq(x - 0.25) + sq(y - 0.5) <= 0.0225 ? 1.0 : 0.0);
+    }
+    case DGADV_FN_GAUSS_SLOT:
+      return exp(-(sq(x - 0.25) + sq(y - 0.5)) / 0.01) + slotted_cylinder(x, y);
+    case DGADV_FN_GAUSS:
+      return exp(-(sq(x - p[0]) + sq(y - p[1])) / p[2]);
+    case DGADV_FN_TRANSIENT:   // advection/configureProblem.m:126
+      return cos(7 * x) * cos(7 * y) + exp(-t);
+  }
+  return 0.0;
+}
+
+__device__ void fn_velocity(const FnDesc *f, double x, double y, double &u1, double &u2) {
+  switch (f->kind) {
+    case DGADV_VEL_ROTATION:   // advection/configureProblem.m:115-116
+      u1 = 0.5 - y;
+      u2 = x - 0.5;
+      return;
+    case DGADV_VEL_TRANSIENT:   // advection/configureProblem.m:127-128
+      u1 = exp(0.5 * (x + y));
+      u2 = exp(0.5 * (x - y));
+      return;
+    case DGADV_VEL_STREAM: {   // u = (d psi / dy, -d psi / dx), modes in order
+      const int M = f->n / 3;
+      const double *k = f->p, *l = f->p + M, *a = f->p + 2 * M;
+      double s1 = 0.0, s2 = 0.0;
+      for (int m = 0; m < M; ++m) {
+        s1 = s1 + a[m] * (l[m] * M_PI) * sin(k[m] * M_PI * x) * cos(l[m] * M_PI * y);
+        s2 = s2 - a[m] * (k[m] * M_PI) * cos(k[m] * M_PI * x) * sin(l[m] * M_PI * y);
+      }
+      u1 = s1;
+      u2 = s2;
+      return;
+    }
+  }
+  u1 = u2 = 0.0;
+}
+
+// Physical point of reference point (X1, X2): (B X)_m + corner 0, summed as the reference's
+// (B(:,m,1) X1 + B(:,m,2) X2) + coordV0T(:,1,m) (core/projectFuncCont2DataDisc.m:99).
+__device__ __forceinline__ void map_point(const SetupArgs &a, int k, double X1, double X2, double &x, double &y) {
+  const size_t K = a.K;
+  x = (a.geo[G_B11 * K + k] * X1 + a.geo[G_B12 * K + k] * X2) + a.geo[G_X0 * K + k];
+  y = (a.geo[G_B21 * K + k] * X1 + a.geo[G_B22 * K + k] * X2) + a.geo[G_Y0 * K + k];
+}
+
+// rule: X1[nq], X2[nq], then nq x N values of W_q phi_i(X_q) (or phi_i(X_q) for the error).
+__global__ void k_project(const SetupArgs a, const double *__restrict__ rule, int nq,
+                          const double *__restrict__ hatMinv, double *__restrict__ ext) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const FnDesc *f = fn_of(a, k);
+  const int N = a.N;
+  const double *X1 = rule, *X2 = rule + nq, *Wphi = rule + 2 * nq;
+  double rhs[kSetupMaxN];
+  for (int i = 0; i < kSetupMaxN; ++i) rhs[i] = 0.0;
+  for (int q = 0; q < nq; ++q) {
+    double x, y;
+    map_point(a, k, X1[q], X2[q], x, y);
+    const double v = fn_scalar(f, a.t, x, y);
+    for (int i = 0; i < N; ++i) rhs[i] += v * Wphi[q * N + i];
+  }
+  const int e = a.perm[k];
+  for (int j = 0; j < N; ++j) {
+    double c = 0.0;
+    for (int i = 0; i < N; ++i) c += rhs[i] * hatMinv[i * N + j];
+    ext[(size_t)j * a.K + e] = c;
+  }
+}
+
+// Velocity factors of the stage kernels (the device form of velocity_factors in
+// dgadv_solver.cu): u1, u2 projected with the order-2p rule, evaluated at the volume points;
+// the normal velocity evaluated exactly at the order-(2p+1) edge points.
+//   vol:  Q x N phi values, then W[Q]
+//   edge: 3 x R reference points X1, then 3 x R X2, then W[R]
+__global__ void k_velocity(const SetupArgs a, const double *__restrict__ rule, int nq,
+                           const double *__restrict__ hatMinv, const double *__restrict__ vol, int Q,
+                           const double *__restrict__ edge, int R, double *__restrict__ F,
+                           double *__restrict__ Vn) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const FnDesc *f = fn_of(a, k);
+  const int N = a.N;
+  const size_t K = a.K, Kp = a.Kp;
+  const double *X1 = rule, *X2 = rule + nq, *Wphi = rule + 2 * nq;
+  double r1[kSetupMaxN], r2[kSetupMaxN];
+  for (int i = 0; i < kSetupMaxN; ++i) r1[i] = r2[i] = 0.0;
+  for (int q = 0; q < nq; ++q) {
+    double x, y, u1, u2;
+    map_point(a, k, X1[q], X2[q], x, y);
+    fn_velocity(f, x, y, u1, u2);
+    for (int i = 0; i < N; ++i) {
+      r1[i] += u1 * Wphi[q * N + i];
+      r2[i] += u2 * Wphi[q * N + i];
+    }
+  }
+  double c1[kSetupMaxN], c2[kSetupMaxN];
+  for (int j = 0; j < N; ++j) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int i = 0; i < N; ++i) {
+      s1 += r1[i] * hatMinv[i * N + j];
+      s2 += r2[i] * hatMinv[i * N + j];
+    }
+    c1[j] = s1;
+    c2[j] = s2;
+  }
+  const double B11 = a.geo[G_B11 * K + k], B12 = a.geo[G_B12 * K + k];
+  const double B21 = a.geo[G_B21 * K + k], B22 = a.geo[G_B22 * K + k];
+  const double dj = a.geo[G_DETJ * K + k];
+  const double *phiQ = vol, *W = vol + Q * N;
+  for (int q = 0; q < Q; ++q) {
+    double s = 0.0, t = 0.0;
+    for (int l = 0; l < N; ++l) {
+      s += phiQ[q * N + l] * c1[l];
+      t += phiQ[q * N + l] * c2[l];
+    }
+    F[q * Kp + k] = W[q] * (B22 * s - B12 * t) / dj;
+    F[(Q + q) * Kp + k] = W[q] * (B11 * t - B21 * s) / dj;
+  }
+  const double *E1 = edge, *E2 = edge + 3 * R, *W1 = edge + 6 * R;
+  for (int n = 0; n < 3; ++n) {
+    const double nu1 = a.geo[(G_NU + 2 * n) * K + k], nu2 = a.geo[(G_NU + 2 * n + 1) * K + k];
+    const double aE = a.geo[(G_AE + n) * K + k];
+    for (int r = 0; r < R; ++r) {
+      double x, y, u1, u2;
+      map_point(a, k, E1[n * R + r], E2[n * R + r], x, y);
+      fn_velocity(f, x, y, u1, u2);
+      const double v = nu1 * u1 + nu2 * u2;
+      Vn[(size_t)(n * R + r) * Kp + k] = aE * W1[r] * v / dj;
+    }
+  }
+}
+
+// Per-block sums of |T| sum_q W_q (u_h - f)^2 (core/computeL2Error.m:104-113).
+//   rule: X1[nq], X2[nq], W[nq], then nq x N phi values
+__global__ void __launch_bounds__(kBlock) k_l2_error(const SetupArgs a, const double *__restrict__ rule, int nq,
+                                                     const double *__restrict__ ext, double *__restrict__ partial) {
+  __shared__ double red[kBlock];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double s = 0.0;
+  if (k < a.K) {
+    const FnDesc *f = fn_of(a, k);
+    const int N = a.N, e = a.perm[k];
+    const double *X1 = rule, *X2 = rule + nq, *W = rule + 2 * nq, *phi = rule + 3 * nq;
+    double c[kSetupMaxN];
+    for (int i = 0; i < N; ++i) c[i] = ext[(size_t)i * a.K + e];
+    for (int q = 0; q < nq; ++q) {
+      double x, y;
+      map_point(a, k, X1[q], X2[q], x, y);
+      double u = 0.0;
+      for (int i = 0; i < N; ++i) u += c[i] * phi[q * N + i];
+      const double d = u - fn_scalar(f, a.t, x, y);
+      s += d * d * W[q];
+    }
+    s *= 0.5 * a.geo[G_DETJ * (size_t)a.K + k];   // areaT = detJ / 2
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = kBlock / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// Device buffers of one set-up call, released (after the stream has drained) on scope exit.
+struct Scratch {
+  dgadv_handle *h;
+  std::vector<void *> bufs;
+  explicit Scratch(dgadv_handle *hh) : h(hh) {}
+  ~Scratch() {
+    if (!bufs.empty()) cudaStreamSynchronize(h->stream);
+    for (void *p : bufs) cudaFree(p);
+  }
+  template <typename T>
+  int upload(const std::vector<T> &v, const T **out) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(v.size(), 1) * sizeof(T)) != cudaSuccess) {
+      h->err = "device allocation for set-up data failed";
+      return DGADV_ENOMEM;
+    }
+    bufs.push_back(p);
+    if (!v.empty() && cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream) != cudaSuccess) {
+      h->err = "upload of set-up data failed";
+      return DGADV_ECUDA;
+    }
+    *out = (const T *)p;
+    return DGADV_OK;
+  }
+  int alloc(size_t bytes, void **out) {
+    if (cudaMalloc(out, std::max<size_t>(bytes, 8)) != cudaSuccess) {
+      h->err = "device allocation for set-up data failed";
+      return DGADV_ENOMEM;
+    }
+    bufs.push_back(*out);
+    return DGADV_OK;
+  }
+};
+
+bool is_scalar_kind(int k) { return k >= DGADV_FN_CONST && k <= DGADV_FN_TRANSIENT; }
+bool is_velocity_kind(int k) { return k >= DGADV_VEL_ROTATION && k <= DGADV_VEL_STREAM; }
+
+// Checks and packs the functions (one, or one per instance).
+int pack_functions(dgadv_handle *h, const dgadv_function *f, int nFn, bool velocity, std::vector<FnDesc> &out) {
+  if (!f || (nFn != 1 && nFn != h->nInst)) {
+    h->err = "give one function, or one per instance";
+    return DGADV_EINVAL;
+  }
+  out.assign(nFn, FnDesc{});
+  for (int i = 0; i < nFn; ++i) {
+    const dgadv_function &g = f[i];
+    const bool kindOk = velocity ? is_velocity_kind(g.kind) : is_scalar_kind(g.kind);
+    int need = 0;
+    switch (g.kind) {
+      case DGADV_FN_CONST: need = 1; break;
+      case DGADV_FN_POLY3: need = 10; break;
+      case DGADV_FN_GAUSS: need = 3; break;
+      case DGADV_VEL_STREAM: need = g.nParams > 0 && g.nParams % 3 == 0 ? g.nParams : -1; break;
+      default: need = 0;
+    }
+    if (!kindOk || need < 0 || g.nParams != need || g.nParams > DGADV_FN_MAX_PARAMS || (need > 0 && !g.params)) {
+      h->err = "function " + std::to_string(i) + ": unknown kind or wrong parameter count";
+      return DGADV_EINVAL;
+    }
+    out[i].kind = g.kind;
+    out[i].n = g.nParams;
+    for (int j = 0; j < g.nParams; ++j) out[i].p[j] = g.params[j];
+  }
+  return DGADV_OK;
+}
+
+int common_args(dgadv_handle *h, Scratch &sc, const dgadv_function *f, int nFn, bool velocity, double t,
+                SetupArgs &a) {
+  std::vector<FnDesc> fns;
+  if (int st = pack_functions(h, f, nFn, velocity, fns)) return st;
+  const size_t K = h->K;
+  std::vector<double> geo(kGeoRows * K);
+  for (size_t k = 0; k < K; ++k) {
+    geo[G_X0 * K + k] = h->corner0[2 * k];
+    geo[G_Y0 * K + k] = h->corner0[2 * k + 1];
+    for (int i = 0; i < 4; ++i) geo[(G_B11 + i) * K + k] = h->Bhost[4 * k + i];
+    geo[G_DETJ * K + k] = h->detJ[k];
+    for (int i = 0; i < 6; ++i) geo[(G_NU + i) * K + k] = h->nuE0T[6 * k + i];
+    for (int n = 0; n < 3; ++n) geo[(G_AE + n) * K + k] = h->markNotN[3 * k + n] ? h->areaE0T[3 * k + n] : 0.0;
+  }
+  a = SetupArgs{};
+  a.K = h->K; a.Kp = h->Kp; a.N = h->N; a.nFn = nFn;
+  a.perm = h->perm;
+  a.instOf = h->instOf;
+  a.t = t;
+  if (int st = sc.upload(geo, &a.geo)) return st;
+  const FnDesc *df = nullptr;
+  if (int st = sc.upload(fns, &df)) return st;
+  a.fns = df;
+  return DGADV_OK;
+}
+
+// X1, X2 and W_q phi_i(X_q) of the 2D rule of order qOrd (weighted = false: phi without W, and
+// W stored after X2).
+int rule_table(dgadv_handle *h, int qOrd, bool weighted, std::vector<double> &out, int &nq) {
+  Rule2D r;
+  if (qOrd < 1 || qOrd > 20 || !quad_rule_2d(qOrd, r)) {
+    h->err = "quadrature order out of range (1..20)";
+    return DGADV_EINVAL;
+  }
+  nq = (int)r.W.size();
+  const int N = h->N;
+  out.clear();
+  out.insert(out.end(), r.Q1.begin(), r.Q1.end());
+  out.insert(out.end(), r.Q2.begin(), r.Q2.end());
+  if (!weighted) out.insert(out.end(), r.W.begin(), r.W.end());
+  for (int q = 0; q < nq; ++q)
+    for (int i = 0; i < N; ++i) {
+      const double v = phi(i, r.Q1[q], r.Q2[q]);
+      out.push_back(weighted ? r.W[q] * v : v);
+    }
+  return DGADV_OK;
+}
+
+}  // namespace
+}  // namespace dgadv
+
+using namespace dgadv;
+
+extern "C" int dgadv_project_state(dgadv_handle *h, const dgadv_function *c0, int32_t nFn, double t, int32_t qOrd) {
+  if (!h) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  Scratch sc(h);
+  SetupArgs a;
+  if (int st = common_args(h, sc, c0, nFn, false, t, a)) return st;
+  std::vector<double> rule;
+  int nq = 0;
+  if (int st = rule_table(h, std::max(qOrd, 1), true, rule, nq)) return st;
+  const double *dRule = nullptr, *dMinv = nullptr;
+  if (int st = sc.upload(rule, &dRule)) return st;
+  if (int st = sc.upload(h->tables.hatMinv, &dMinv)) return st;
+  k_project<<<(h->K + kBlock - 1) / kBlock, kBlock, 0, h->stream>>>(a, dRule, nq, dMinv, h->stage_ext);
+  DG_CUDA(cudaGetLastError());
+  DG_CUDA(ops_of(h).scatter_in(h, h->cn));
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_set_velocity_function(dgadv_handle *h, const dgadv_function *u, int32_t nFn) {
+  if (!h) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  Scratch sc(h);
+  SetupArgs a;
+  if (int st = common_args(h, sc, u, nFn, true, 0.0, a)) return st;
+  const RefTables &t = h->tables;
+  std::vector<double> rule, vol(t.phiQ), edge;
+  int nq = 0;
+  if (int st = rule_table(h, std::max(2 * h->p, 1), true, rule, nq)) return st;
+  vol.insert(vol.end(), t.vol.W.begin(), t.vol.W.end());
+  // edge points gammaMap(n, s) (core/gammaMap.m:50-57): (1-s, s), (0, 1-s), (s, 0)
+  const int R = h->R;
+  edge.assign(6 * (size_t)R + R, 0.0);
+  for (int r = 0; r < R; ++r) {
+    const double s = t.edge.Q[r];
+    edge[0 * R + r] = 1 - s; edge[3 * R + 0 * R + r] = s;
+    edge[1 * R + r] = 0.0;   edge[3 * R + 1 * R + r] = 1 - s;
+    edge[2 * R + r] = s;     edge[3 * R + 2 * R + r] = 0.0;
+    edge[6 * R + r] = t.edge.W[r];
+  }
+  const double *dRule = nullptr, *dMinv = nullptr, *dVol = nullptr, *dEdge = nullptr;
+  if (int st = sc.upload(rule, &dRule)) return st;
+  if (int st = sc.upload(t.hatMinv, &dMinv)) return st;
+  if (int st = sc.upload(vol, &dVol)) return st;
+  if (int st = sc.upload(edge, &dEdge)) return st;
+  const size_t nF = 2 * (size_t)h->Q * h->Kp, nV = 3 * (size_t)R * h->Kp;
+  void *F = nullptr, *Vn = nullptr;
+  if (int st = sc.alloc(nF * 8, &F)) return st;
+  if (int st = sc.alloc(nV * 8, &Vn)) return st;
+  DG_CUDA(cudaMemsetAsync(F, 0, nF * 8, h->stream));
+  DG_CUDA(cudaMemsetAsync(Vn, 0, nV * 8, h->stream));
+  k_velocity<<<(h->K + kBlock - 1) / kBlock, kBlock, 0, h->stream>>>(a, dRule, nq, dMinv, dVol, h->Q, dEdge, R,
+                                                                      (double *)F, (double *)Vn);
+  DG_CUDA(cudaGetLastError());
+  DG_CUDA(ops_of(h).from_f64(h, h->F, (const double *)F, nF));
+  DG_CUDA(ops_of(h).from_f64(h, h->Vn, (const double *)Vn, nV));
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  h->hasVelocity = true;
+  return DGADV_OK;
+}
+
+extern "C" int dgadv_l2_error(dgadv_handle *h, const dgadv_function *f, int32_t nFn, double t, int32_t qOrd,
+                              double *err) {
+  if (!h || !err) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  Scratch sc(h);
+  SetupArgs a;
+  if (int st = common_args(h, sc, f, nFn, false, t, a)) return st;
+  std::vector<double> rule;
+  int nq = 0;
+  if (int st = rule_table(h, std::max(qOrd, 1), false, rule, nq)) return st;
+  const double *dRule = nullptr;
+  if (int st = sc.upload(rule, &dRule)) return st;
+  const int nBlocks = (h->K + kBlock - 1) / kBlock;
+  void *part = nullptr;
+  if (int st = sc.alloc((size_t)nBlocks * 8, &part)) return st;
+  DG_CUDA(ops_of(h).gather_out(h, h->cn));
+  k_l2_error<<<nBlocks, kBlock, 0, h->stream>>>(a, dRule, nq, h->stage_ext, (double *)part);
+  DG_CUDA(cudaGetLastError());
+  std::vector<double> hp(nBlocks);
+  DG_CUDA(cudaMemcpyAsync(hp.data(), part, (size_t)nBlocks * 8, cudaMemcpyDeviceToHost, h->stream));
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  // sum the blocks of each instance in order (an ensemble's instances start at whole blocks)
+  const int nOut = nFn == 1 ? 1 : h->nInst;
+  for (int i = 0; i < nOut; ++i) {
+    const int b0 = nOut == 1 ? 0 : h->instStart[i] / kBlock;
+    const int b1 = nOut == 1 ? nBlocks : (h->instStart[i + 1] + kBlock - 1) / kBlock;
+    double s = 0.0;
+    for (int b = b0; b < b1; ++b) s += hp[b];
+    err[i] = std::sqrt(2.0 * s);
+  }
+  return DGADV_OK;
+}

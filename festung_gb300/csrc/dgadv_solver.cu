@@ -173,6 +173,7 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
   std::vector<int> nbr(3 * (size_t)Kp, -1), code(Kp, 0), V0T(3 * (size_t)Kp, 0);
   h->detJ.assign(K, 0); h->areaE0T.assign(3 * (size_t)K, 0); h->Bhost.assign(4 * (size_t)K, 0);
   h->markNotN.assign(3 * (size_t)K, 0);
+  h->nuE0T.assign(6 * (size_t)K, 0); h->corner0.assign(2 * (size_t)K, 0);
   std::vector<double> Bsoa(4 * (size_t)Kp, 0.0);
   for (int k = 0; k < K; ++k) {
     const int t = perm[k];
@@ -189,7 +190,10 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
       V0T[(size_t)n * Kp + k] = vnew[gr.V0T[3 * (size_t)t + n]];
       h->areaE0T[3 * (size_t)k + n] = gr.areaE0T[3 * (size_t)t + n];
       h->markNotN[3 * (size_t)k + n] = bdrN[3 * (size_t)t + n] ? 0 : 1;
+      for (int m = 0; m < 2; ++m) h->nuE0T[6 * (size_t)k + 2 * n + m] = gr.nuE0T[6 * (size_t)t + 2 * n + m];
     }
+    h->corner0[2 * (size_t)k] = gr.coordV0T[6 * (size_t)t];
+    h->corner0[2 * (size_t)k + 1] = gr.coordV0T[6 * (size_t)t + 1];
     code[k] = cd;
     h->detJ[k] = gr.detJ0T[t];
     for (int i = 0; i < 4; ++i) { Bsoa[(size_t)i * Kp + k] = gr.B[4 * (size_t)t + i]; h->Bhost[4 * (size_t)k + i] = gr.B[4 * (size_t)t + i]; }

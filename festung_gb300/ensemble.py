@@ -31,7 +31,9 @@ def shard(n, rank, world):
 
 
 def instance_problem(seed, numSteps=STEPS, tau=TAU, **overrides):
-    """configureProblem + the host part of preprocessProblem for instance `seed`."""
+    """configureProblem + the host part of preprocessProblem for instance `seed`.  With
+    setupOnDevice (the default) the velocity and the initial data stay device functions
+    (``pd.deviceFns``); otherwise they are projected on the host (pd.u1Disc, ..., pd.c0)."""
     prm = TC.ensemble_params(seed)
     kw = dict(testcase='ensemble', instanceSeed=seed, hmax=prm['hmax'], p=prm['p'], numSteps=numSteps,
               tEnd=numSteps * tau, isSlopeLim=True, typeSlopeLim='linear')
@@ -40,7 +42,8 @@ def instance_problem(seed, numSteps=STEPS, tau=TAU, **overrides):
     pd.problemName = 'advection_gpu'
     G.configureProblem(pd)
     G.host_preprocess(pd)
-    pd.c0 = G.project(pd.g, pd.tables, pd.c0Cont, pd.qOrd, pd.hatM)
+    if not pd.deviceFns:
+        pd.c0 = G.project(pd.g, pd.tables, pd.c0Cont, pd.qOrd, pd.hatM)
     return pd
 
 
@@ -61,8 +64,12 @@ class Ensemble:
             s = DeviceSolver(None, None, p, pd0.ordRK, precision=precision, isSlopeLim=pd0.isSlopeLim,
                              typeSlopeLim=pd0.typeSlopeLim, device=device, flags=flags,
                              instances=[G.instance_mesh(pd) for pd in pds])
-            s.set_velocity(np.concatenate([pd.u1Disc for pd in pds]), np.concatenate([pd.u2Disc for pd in pds]),
-                           np.concatenate([pd.vNormalOnQuadEdge for pd in pds]))
+            if pd0.deviceFns:
+                s.set_velocity_function([pd.deviceFns['u'] for pd in pds])
+            else:
+                s.set_velocity(np.concatenate([pd.u1Disc for pd in pds]),
+                               np.concatenate([pd.u2Disc for pd in pds]),
+                               np.concatenate([pd.vNormalOnQuadEdge for pd in pds]))
             self.solvers[p] = s
         self.reset()
 
@@ -77,8 +84,12 @@ class Ensemble:
         """Initial data of every instance, limited (advection/initializeProblem.m:56-67)."""
         for p, members in self.groups.items():
             s = self.solvers[p]
-            s.set_state(np.concatenate([self.problems[i].c0 for i in members]))
-            if self.problems[members[0]].isSlopeLim:
+            pds = [self.problems[i] for i in members]
+            if pds[0].deviceFns:
+                s.project_state([pd.deviceFns['c0'] for pd in pds], 0.0, pds[0].qOrd)
+            else:
+                s.set_state(np.concatenate([pd.c0 for pd in pds]))
+            if pds[0].isSlopeLim:
                 s.limit_state(0.0)
 
     def step(self, nSteps, nStep0=0):

@@ -108,6 +108,27 @@ class DeviceSolver:
     def limit_state(self, t):
         self._c(self._lib.dgadv_limit_state(self._h, float(t)))
 
+    # ---- set-up on the device (functions of the built-in test cases) ----------------------
+    def project_state(self, fns, t=0.0, qOrd=1):
+        """projectFuncCont2DataDisc of f(t, x) into the state; fns: one (kind, params) pair or
+        one per instance."""
+        arr, keep = L.functions(_fn_list(fns))
+        self._c(self._lib.dgadv_project_state(self._h, arr, len(arr), float(t), int(qOrd)))
+
+    def set_velocity_function(self, fns):
+        """Velocity data of u(x) computed on the device (replaces set_velocity's host arrays)."""
+        arr, keep = L.functions(_fn_list(fns))
+        self._c(self._lib.dgadv_set_velocity_function(self._h, arr, len(arr)))
+
+    def l2_error(self, fns, t=0.0, qOrd=1):
+        """computeL2Error of the state against f(t, x): a float, or one per instance when one
+        function per instance is given."""
+        specs = _fn_list(fns)
+        arr, keep = L.functions(specs)
+        out = np.zeros(len(specs))
+        self._c(self._lib.dgadv_l2_error(self._h, arr, len(arr), float(t), int(qOrd), L.ptr(out)))
+        return float(out[0]) if len(specs) == 1 else out
+
     def get_lagrange(self):
         """projectDataDisc2DataLagr of the current state on the device: K x numP nodal values."""
         numP = 1 if self.p == 0 else (3 if self.p == 1 else 6)
@@ -197,3 +218,10 @@ class DeviceSolver:
             self.close()
         except Exception:
             pass
+
+
+def _fn_list(fns):
+    """A (kind, params) pair or a list of them."""
+    if isinstance(fns, tuple) and len(fns) == 2 and not isinstance(fns[0], tuple):
+        return [fns]
+    return list(fns)

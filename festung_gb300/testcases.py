@@ -166,3 +166,28 @@ def configure(pd):
     else:
         raise ValueError('Invalid testcase "%s".' % tc)
     return pd
+
+
+def device_functions(pd):
+    """The configured problem's data as device functions (kind, params) of ``dgadv_function``:
+    'c0' (initial data), 'u' (velocity) and, for analytical cases, 'cCont' (exact solution,
+    evaluated at a time t).  The parameters reproduce the host closures above."""
+    from . import _lib as L
+    tc = pd['testcase']
+    if tc == 'solid_body':
+        return dict(c0=(L.FN_SOLID_BODY, []), u=(L.VEL_ROTATION, []))
+    if tc == 'gauss_slot':
+        return dict(c0=(L.FN_GAUSS_SLOT, []), u=(L.VEL_ROTATION, []))
+    if tc == 'transient':
+        return dict(c0=(L.FN_TRANSIENT, []), u=(L.VEL_TRANSIENT, []), cCont=(L.FN_TRANSIENT, []))
+    if tc == 'ensemble':
+        prm = pd['ensembleParams']
+        cx, cy = prm['centre']
+        return dict(c0=(L.FN_GAUSS, [cx, cy, prm['width'] ** 2]),
+                    u=(L.VEL_STREAM, np.concatenate([prm['k'], prm['l'], prm['a']]).astype(np.float64)))
+    if tc == 'adjoint':
+        k = [km for km, _ in ADJOINT_MODES]
+        l = [lm for _, lm in ADJOINT_MODES]
+        return dict(c0=(L.FN_GAUSS, [0.4, 0.45, 0.01]),
+                    u=(L.VEL_STREAM, np.concatenate([k, l, pd['theta']]).astype(np.float64)))
+    return None

@@ -190,6 +190,48 @@ int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *value);
  * reference. */
 int dgadv_selftest_wait(dgadv_handle *h, double seconds);
 
+/* ---- set-up on the device ------------------------------------------------------------
+ * The reference hands its data to the solver as closures (advection/configureProblem.m:106-133)
+ * and evaluates them on the host.  Here the built-in test cases' functions are device
+ * functions, selected by kind with their parameters, so the steps either side of the time loop
+ * (projections, velocity data, L2 errors) run on the GPU.  An ensemble handle takes one
+ * function for every instance (nFn = 1) or one per instance (nFn = number of instances). */
+#define DGADV_FN_MAX_PARAMS 64
+enum {
+  DGADV_FN_CONST = 0,        /* params[0]                                                      */
+  DGADV_FN_POLY3 = 1,        /* params . (1, x, y, x^2, xy, y^2, x^3, x^2 y, x y^2, y^3)         */
+  DGADV_FN_SOLID_BODY = 2,   /* c0 of 'solid_body': slotted cylinder, cone, hump (:109-113)     */
+  DGADV_FN_GAUSS_SLOT = 3,   /* exp(-((x-0.25)^2 + (y-0.5)^2) / 0.01) + the slotted cylinder     */
+  DGADV_FN_GAUSS = 4,        /* exp(-((x-p0)^2 + (y-p1)^2) / p2), p2 the squared width          */
+  DGADV_FN_TRANSIENT = 5,    /* cCont of 'transient': cos(7x) cos(7y) + exp(-t) (:126)          */
+  DGADV_VEL_ROTATION = 16,   /* u = (0.5 - y, x - 0.5) ('solid_body', :115-116)                 */
+  DGADV_VEL_TRANSIENT = 17,  /* u = (exp((x+y)/2), exp((x-y)/2)) ('transient', :127-128)        */
+  DGADV_VEL_STREAM = 18      /* u = (dpsi/dy, -dpsi/dx), psi = sum_m a_m sin(k_m pi x) sin(l_m pi y),
+                                params k[M], l[M], a[M] (nParams = 3M)                          */
+};
+typedef struct dgadv_function {
+  int32_t kind;              /* DGADV_FN_* or DGADV_VEL_*                                       */
+  int32_t nParams;           /* at most DGADV_FN_MAX_PARAMS                                     */
+  const double *params;
+} dgadv_function;
+
+/* Replaces projectFuncCont2DataDisc of the initial data (core/projectFuncCont2DataDisc.m:94-102,
+ * advection/initializeProblem.m:53): the state becomes the L2 projection of f(t, x) with the
+ * 2D rule of order max(qOrd, 1) (at most 20).  Synchronous. */
+int dgadv_project_state(dgadv_handle *h, const dgadv_function *f, int32_t nFn, double t,
+                        int32_t qOrd);
+
+/* Replaces the host velocity data of dgadv_set_velocity (advection/preprocessSubStep.m:72-79):
+ * u1Disc, u2Disc projected with order 2p and the normal velocity at the order-(2p+1) edge
+ * points, evaluated on the device.  Synchronous. */
+int dgadv_set_velocity_function(dgadv_handle *h, const dgadv_function *u, int32_t nFn);
+
+/* Replaces computeL2Error (core/computeL2Error.m:97-114) for the current state against f(t, x)
+ * with the rule of order max(qOrd, 1): err[0], or err[i] for each instance when nFn is the
+ * number of instances.  Synchronous. */
+int dgadv_l2_error(dgadv_handle *h, const dgadv_function *f, int32_t nFn, double t, int32_t qOrd,
+                   double *err);
+
 /* ---- solution output ------------------------------------------------------------------
  * The reference writes u_h at the Lagrange nodes of each triangle (projectDataDisc2DataLagr):
  * numP = 1 value at the centroid (p = 0), 3 at the vertices (p = 1), or 6 at the vertices and

@@ -10,11 +10,13 @@ def test_instances_follow_their_seeds():
     from festung_gb300 import ensemble as E
     from festung_gb300 import testcases as TC
     for seed in (0, 5):
-        pd = E.instance_problem(seed, numSteps=4)
+        pd = E.instance_problem(seed, numSteps=4, setupOnDevice=False)
         prm = TC.ensemble_params(seed)
         assert pd.p == prm['p'] and pd.hmax == prm['hmax']
         assert pd.K % 128 == 0 and pd.K in (2048, 8192, 32768)
         assert pd.c0.shape == (pd.K, pd.N) and pd.u1Disc.shape == (pd.K, pd.N)
+        dev = E.instance_problem(seed, numSteps=4)
+        assert dev.deviceFns['c0'][1][2] == prm['width'] ** 2 and 'u1Disc' not in dev
 
 
 def test_shard_partitions_instances():
