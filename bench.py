@@ -389,6 +389,60 @@ def limited_sensitivity(AD, pd, c0, cstar, steps, h=1e-14):
             'max_abs_cT': float(np.abs(ca).max())}
 
 
+def setup_block(wl, device, reps=2):
+    """The steps either side of the time loop on the headline workload (FP32 handle): velocity
+    data, projection of the initial data and the L2 error, with the test case's device functions
+    (dgadv_set_velocity_function, dgadv_project_state, dgadv_l2_error) and with the host set-up
+    (numpy projections, dgadv_set_velocity / dgadv_set_state, numpy L2 error).  Wall time of
+    each (best of `reps`), and the whole configure + preprocess + initialize both ways."""
+    from festung_gb300 import advection_gpu as G
+    out = {'workload': wl, 'precision': 'fp32'}
+    whole = {}
+    for dev in (True, False):
+        ts = []
+        for _ in range(reps):
+            t = time.perf_counter()
+            pd = G.Struct(dict(WORKLOADS[wl], precision='fp32', device=device, setupOnDevice=dev))
+            pd.problemName = 'advection_gpu'
+            for f in G.PRE:
+                pd = f(pd)
+            ts.append(time.perf_counter() - t)
+            if dev:
+                pdDev = pd
+            else:
+                pdHost = pd
+        whole['device' if dev else 'host'] = min(ts)
+    out['pre_s'] = whole
+    s, fns = pdDev.solver, pdDev.deviceFns
+
+    def best(fn):
+        ts = []
+        for _ in range(reps + 1):
+            t = time.perf_counter(); fn(); ts.append(time.perf_counter() - t)
+        return 1e3 * min(ts[1:])
+    g, tb, ph = pdHost.g, pdHost.tables, pdHost
+    out['device_ms'] = {
+        'velocity': best(lambda: s.set_velocity_function(fns['u'])),
+        'initial_data': best(lambda: s.project_state(fns['c0'], 0.0, pdDev.qOrd)),
+        'l2_error': best(lambda: s.l2_error(fns['c0'], 0.0, pdDev.qOrd))}
+
+    def host_velocity():
+        u1 = G.project(g, tb, ph.u1Cont, 2 * ph.p, ph.hatM)
+        u2 = G.project(g, tb, ph.u2Cont, 2 * ph.p, ph.hatM)
+        vn = G.normal_velocity(g, tb, ph.u1Cont, ph.u2Cont, 2 * ph.p + 1)
+        ph.solver.set_velocity(u1, u2, vn)
+    out['host_ms'] = {
+        'velocity': best(host_velocity),
+        'initial_data': best(lambda: ph.solver.set_state(G.project(g, tb, ph.c0Cont, ph.qOrd, ph.hatM))),
+        'l2_error': best(lambda: G.l2_error(g, tb, ph.solver.get_state(), ph.c0Cont, ph.qOrd))}
+    out['l2_error_device_vs_host_rel'] = abs(s.l2_error(fns['c0'], 0.0, ph.qOrd) -
+                                             G.l2_error(g, tb, s.get_state(), ph.c0Cont, ph.qOrd)) / \
+        G.l2_error(g, tb, s.get_state(), ph.c0Cont, ph.qOrd)
+    pdDev.solver.close()
+    pdHost.solver.close()
+    return out
+
+
 def ensemble_block(rank, world, device, n=256, steps=200, reps=3):
     """The ensemble workload: n seeded instances (2048 to 32768 triangles, p in {1, 2}, their own
     velocity fields), 200 steps in FP32 with the linear limiter; each degree group is one stacked
@@ -578,6 +632,9 @@ def run_ours(args):
             'value': within[best][0] if best else None,
             'speedup_vs_fp64': within[best][0] / result['fp64']['value'] if best else None}
 
+    if rank == 0 and not args.no_setup:
+        result['setup'] = setup_block(wl, device)
+
     if not args.no_ensemble:
         ens = ensemble_block(rank, world, device)
         if rank == 0:
@@ -613,6 +670,7 @@ def main():
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--no-ensemble', action='store_true')
     ap.add_argument('--no-tune', action='store_true')
+    ap.add_argument('--no-setup', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-stages', type=int, default=1)
     ap.add_argument('--ref-stages-per-step', type=int, default=1)
