@@ -12,14 +12,16 @@ LIB_PATH = os.path.join(HERE, 'libdgadv.so')
 
 DGADV_OK, DGADV_EINVAL, DGADV_ECUDA, DGADV_ENOMEM, DGADV_EMESH = 0, 1, 2, 3, 4
 DGADV_ENONFINITE, DGADV_ETIMEOUT, DGADV_EUNSUPPORTED, DGADV_EIO = 5, 6, 7, 8
+DGADV_ENOCONV = 9
 FP64, FP32, DF32 = 0, 1, 2
 LIM_LINEAR, LIM_HIERARCH_VERT, LIM_STRICT = 0, 1, 2
 TIME_CONST, TIME_EXP_NEG = 0, 1
 FLAG_NO_REORDER, FLAG_NO_SHIFT, FLAG_NO_GRAPH, FLAG_NO_PDL, FLAG_FUSE, FLAG_PERSIST = 1, 2, 4, 8, 16, 32
 OPT_GRAPH_STEPS, OPT_FLAGS, OPT_PERSIST_BLOCKS = 1, 2, 3
 OUT_VTK, OUT_TEC = 1, 2
-FN_CONST, FN_POLY3, FN_SOLID_BODY, FN_GAUSS_SLOT, FN_GAUSS, FN_TRANSIENT = 0, 1, 2, 3, 4, 5
-VEL_ROTATION, VEL_TRANSIENT, VEL_STREAM = 16, 17, 18
+FN_CONST, FN_POLY3, FN_SOLID_BODY, FN_GAUSS_SLOT, FN_GAUSS, FN_TRANSIENT, FN_COS7 = 0, 1, 2, 3, 4, 5, 6
+VEL_ROTATION, VEL_TRANSIENT, VEL_STREAM, VEL_CONST = 16, 17, 18, 19
+FLAG_IMPLICIT = 64
 FN_MAX_PARAMS = 64
 OUTPUT_TYPES = {'vtk': OUT_VTK, 'tec': OUT_TEC}
 
@@ -52,6 +54,10 @@ class Params(ctypes.Structure):
     _fields_ = [('p', ctypes.c_int32), ('ordRK', ctypes.c_int32), ('precision', ctypes.c_int32),
                 ('isSlopeLim', ctypes.c_int32), ('typeSlopeLim', ctypes.c_int32),
                 ('device', ctypes.c_int32), ('flags', ctypes.c_int32)]
+
+
+class Krylov(ctypes.Structure):
+    _fields_ = [('tol', ctypes.c_double), ('maxIter', ctypes.c_int32), ('restart', ctypes.c_int32)]
 
 
 class Function(ctypes.Structure):
@@ -105,6 +111,9 @@ SYMBOLS = {
     'dgadv_forward_record': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_int32]),
     'dgadv_backward': (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp]),
     'dgadv_checkpoint_schedule': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i32p]),
+    'dgadv_step_implicit': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                           ctypes.c_int32, ctypes.POINTER(Krylov), _i32p, _dp]),
+    'dgadv_solve_stationary': (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Krylov), _i32p, _dp]),
     'dgadv_project_state': (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Function), ctypes.c_int32,
                                            ctypes.c_double, ctypes.c_int32]),
     'dgadv_set_velocity_function': (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Function), ctypes.c_int32]),

@@ -312,6 +312,7 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
   if (!h || nSteps < 1 || !(tau > 0.0)) return DGADV_EINVAL;
   const PrecOps &o = ops_of(h);
   if (!o.adj_stage) { h->err = "no adjoint kernels for this precision"; return DGADV_EUNSUPPORTED; }
+  if (h->flags & DGADV_FLAG_IMPLICIT) { h->err = "the adjoint covers the explicit scheme"; return DGADV_EUNSUPPORTED; }
   if (h->lim && h->limType != DGADV_LIM_LINEAR) {
     h->err = "the adjoint covers the unlimited scheme and the linear limiter";
     return DGADV_EUNSUPPORTED;

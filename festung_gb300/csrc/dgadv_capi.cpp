@@ -112,6 +112,7 @@ extern "C" const char *dgadv_status_string(int s) {
     case DGADV_ETIMEOUT: return "bounded device wait timed out";
     case DGADV_EUNSUPPORTED: return "unsupported option";
     case DGADV_EIO: return "output file could not be written";
+    case DGADV_ENOCONV: return "iterative solve did not converge";
   }
   return "unknown status";
 }

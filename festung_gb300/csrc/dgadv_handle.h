@@ -17,6 +17,8 @@ struct dgadv_handle;
 namespace dgadv {
 struct OutputQueue;
 void output_release(dgadv_handle *h);   // joins the writer thread, frees the output buffers
+struct ImplicitState;
+void implicit_release(dgadv_handle *h); // frees the implicit solver's host state
 constexpr int kBlock = 128;       // elements per CTA (one thread per element)
 constexpr int kSlotCopies = 32;   // copies of the global min / max slots (atomics spread over them)
 constexpr int kGridBarBytes = 8192;   // state of the persistent step's grid barrier
@@ -58,6 +60,8 @@ struct dgadv_handle {
   std::vector<double> visCoordV;              // caller's vertices, numV x 2 row-major (output files)
   std::vector<int32_t> visV0T;                // caller's V0T, numT x 3 row-major
   dgadv::OutputQueue *outq = nullptr;         // solution output (dgadv_output), made on first use
+  dgadv::ImplicitState *impl = nullptr;       // implicit solver (dgadv_step_implicit), on first use
+  int velOrder = 1;                           // order of the velocity projections (2p or 2p+1)
   dgadv::RefTables tables;
   // CUDA graphs of a chunk of steps, one per phase (limPass mod 3) at the chunk start
   cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};

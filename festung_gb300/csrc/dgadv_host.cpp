@@ -408,11 +408,11 @@ static double taylor_eval(int j, double dx, double dy, const TaylorElem &te) {
 }
 
 // ---------------------------------------------------------------------------------------------
-bool build_ref_tables(int p, RefTables &t, std::string &err) {
+bool build_ref_tables(int p, RefTables &t, std::string &err, int volOrder) {
   if (p < 0 || p > kMaxPHost) { err = "p must be in 0..4"; return false; }
   const int N = N_of_p(p);
   t.p = p; t.N = N;
-  const int qv = std::max(2 * p, 1);
+  const int qv = volOrder > 0 ? volOrder : std::max(2 * p, 1);
   quad_rule_2d(qv, t.vol);
   quad_rule_1d(2 * p + 1, t.edge);
   t.Q = (int)t.vol.W.size();

@@ -34,7 +34,9 @@ struct RefTables {
   std::vector<double> DM;          // N x N   Taylor-derivative map times hatM
   std::vector<double> DMinv;       // N x N   its inverse
 };
-bool build_ref_tables(int p, RefTables &t, std::string &err);
+// volOrder: order of the volume rule (0: max(2p, 1), the explicit problem's; the implicit
+// problem integrates with 2p + 1, advection_implicit/preprocessProblem.m)
+bool build_ref_tables(int p, RefTables &t, std::string &err, int volOrder = 0);
 
 // Grid data with generateGridData semantics (row-major per element / edge, 0-based ids).
 struct Grid {

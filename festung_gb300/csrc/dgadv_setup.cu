@@ -74,6 +74,8 @@ __device__ double fn_scalar(const FnDesc *f, double t, double x, double y) {
       return exp(-(sq(x - p[0]) + sq(y - p[1])) / p[2]);
     case DGADV_FN_TRANSIENT:   // advection/configureProblem.m:126
       return cos(7 * x) * cos(7 * y) + exp(-t);
+    case DGADV_FN_COS7:        // advection_implicit/getTestcase.m ('stationary')
+      return cos(7 * x) * cos(7 * y);
   }
   return 0.0;
 }
@@ -100,6 +102,10 @@ __device__ void fn_velocity(const FnDesc *f, double x, double y, double &u1, dou
       u2 = s2;
       return;
     }
+    case DGADV_VEL_CONST:
+      u1 = f->p[0];
+      u2 = f->p[1];
+      return;
   }
   u1 = u2 = 0.0;
 }
@@ -265,8 +271,8 @@ struct Scratch {
   }
 };
 
-bool is_scalar_kind(int k) { return k >= DGADV_FN_CONST && k <= DGADV_FN_TRANSIENT; }
-bool is_velocity_kind(int k) { return k >= DGADV_VEL_ROTATION && k <= DGADV_VEL_STREAM; }
+bool is_scalar_kind(int k) { return k >= DGADV_FN_CONST && k <= DGADV_FN_COS7; }
+bool is_velocity_kind(int k) { return k >= DGADV_VEL_ROTATION && k <= DGADV_VEL_CONST; }
 
 // Checks and packs the functions (one, or one per instance).
 int pack_functions(dgadv_handle *h, const dgadv_function *f, int nFn, bool velocity, std::vector<FnDesc> &out) {
@@ -284,6 +290,7 @@ int pack_functions(dgadv_handle *h, const dgadv_function *f, int nFn, bool veloc
       case DGADV_FN_POLY3: need = 10; break;
       case DGADV_FN_GAUSS: need = 3; break;
       case DGADV_VEL_STREAM: need = g.nParams > 0 && g.nParams % 3 == 0 ? g.nParams : -1; break;
+      case DGADV_VEL_CONST: need = 2; break;
       default: need = 0;
     }
     if (!kindOk || need < 0 || g.nParams != need || g.nParams > DGADV_FN_MAX_PARAMS || (need > 0 && !g.params)) {
@@ -378,7 +385,7 @@ extern "C" int dgadv_set_velocity_function(dgadv_handle *h, const dgadv_function
   const RefTables &t = h->tables;
   std::vector<double> rule, vol(t.phiQ), edge;
   int nq = 0;
-  if (int st = rule_table(h, std::max(2 * h->p, 1), true, rule, nq)) return st;
+  if (int st = rule_table(h, h->velOrder, true, rule, nq)) return st;
   vol.insert(vol.end(), t.vol.W.begin(), t.vol.W.end());
   // edge points gammaMap(n, s) (core/gammaMap.m:50-57): (1-s, s), (0, 1-s), (s, 0)
   const int R = h->R;

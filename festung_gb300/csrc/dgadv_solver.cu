@@ -103,7 +103,10 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
   // static grid data (core/generateGridData.m semantics)
   Grid gr;
   if (!build_grid(mesh->numV, mesh->coordV, mesh->numT, mesh->V0T, gr, h->err)) return DGADV_EMESH;
-  if (!build_ref_tables(h->p, h->tables, h->err)) return DGADV_EINVAL;
+  const bool implicit = (h->flags & DGADV_FLAG_IMPLICIT) != 0;
+  if (implicit && h->lim) { h->err = "the implicit problem has no limiter"; return DGADV_EINVAL; }
+  if (!build_ref_tables(h->p, h->tables, h->err, implicit ? 2 * h->p + 1 : 0)) return DGADV_EINVAL;
+  h->velOrder = implicit ? 2 * h->p + 1 : std::max(2 * h->p, 1);
   h->visCoordV = gr.coordV;
   h->visV0T = gr.V0T;
   const int K = gr.numT, N = h->N;
@@ -297,7 +300,7 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
     std::lock_guard<std::mutex> lk(g_tab_mutex);
     const int pi = h->prec;
     if (h->device < 0 || h->device >= 64) { h->err = "device ordinal out of range"; return DGADV_EINVAL; }
-    if (!g_tab_loaded[h->device][pi][h->p]) {
+    if (!implicit && !g_tab_loaded[h->device][pi][h->p]) {   // implicit handles use their own tables
       cudaError_t e = ops(h).upload_tables(h->p, h->tables);
       if (e != cudaSuccess) { h->err = std::string("table upload: ") + cudaGetErrorString(e); return DGADV_ECUDA; }
       e = ops(h).set_smem(h->p);
@@ -497,6 +500,10 @@ static cudaError_t end_of_call(dgadv_handle *h) {
 
 extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau) {
   if (!h || nSteps < 0 || !(tau > 0)) return DGADV_EINVAL;
+  if (h->flags & DGADV_FLAG_IMPLICIT) {
+    h->err = "explicit steps need a handle without DGADV_FLAG_IMPLICIT";
+    return DGADV_EUNSUPPORTED;
+  }
   if (!h->hasVelocity) { if (h) h->err = "dgadv_set_velocity was not called"; return DGADV_EINVAL; }
   DG_CUDA(cudaSetDevice(h->device));
   if (nSteps == 0) return DGADV_OK;
@@ -633,6 +640,7 @@ extern "C" int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nS
                                      double *msPerLaunch, int32_t *launches) {
   if (!h || !msPerLaunch || !launches || nSteps < 1) return DGADV_EINVAL;
   if (!h->hasVelocity) { h->err = "dgadv_set_velocity was not called"; return DGADV_EINVAL; }
+  if (h->flags & DGADV_FLAG_IMPLICIT) { h->err = "explicit steps need a handle without DGADV_FLAG_IMPLICIT"; return DGADV_EUNSUPPORTED; }
   DG_CUDA(cudaSetDevice(h->device));
   DG_CUDA(cudaStreamSynchronize(h->stream));
   h->profiling = true;
@@ -675,6 +683,7 @@ extern "C" void dgadv_destroy(dgadv_handle *h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   output_release(h);
+  implicit_release(h);
   for (int i = 0; i < 3; ++i)
     if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
   if (h->adjExec) cudaGraphExecDestroy(h->adjExec);

@@ -129,6 +129,23 @@ class DeviceSolver:
         self._c(self._lib.dgadv_l2_error(self._h, arr, len(arr), float(t), int(qOrd), L.ptr(out)))
         return float(out[0]) if len(specs) == 1 else out
 
+    # ---- implicit time stepping (handles created with flags=FLAG_IMPLICIT) -----------------
+    def step_implicit(self, nSteps, nStep0, tau, ordRK, tol=1e-12, maxIter=2000, restart=50):
+        """DIRK steps nStep0+1 .. nStep0+nSteps (GMRES per stage); returns (iterations, largest
+        final relative residual)."""
+        kr = L.Krylov(float(tol), int(maxIter), int(restart))
+        it, rr = ctypes.c_int32(), ctypes.c_double()
+        self._c(self._lib.dgadv_step_implicit(self._h, int(nSteps), int(nStep0), float(tau), int(ordRK),
+                                              ctypes.byref(kr), ctypes.byref(it), ctypes.byref(rr)))
+        return it.value, rr.value
+
+    def solve_stationary(self, tol=1e-12, maxIter=2000, restart=50):
+        """A c = sysV(0) from the current state; returns (iterations, final relative residual)."""
+        kr = L.Krylov(float(tol), int(maxIter), int(restart))
+        it, rr = ctypes.c_int32(), ctypes.c_double()
+        self._c(self._lib.dgadv_solve_stationary(self._h, ctypes.byref(kr), ctypes.byref(it), ctypes.byref(rr)))
+        return it.value, rr.value
+
     def get_lagrange(self):
         """projectDataDisc2DataLagr of the current state on the device: K x numP nodal values."""
         numP = 1 if self.p == 0 else (3 if self.p == 1 else 6)

@@ -191,3 +191,55 @@ def device_functions(pd):
         return dict(c0=(L.FN_GAUSS, [0.4, 0.45, 0.01]),
                     u=(L.VEL_STREAM, np.concatenate([k, l, pd['theta']]).astype(np.float64)))
     return None
+
+
+# ---------------------------------------------------------------------------------------------
+# Test cases of the implicit problem (advection_implicit/getTestcase.m).  Source and Dirichlet
+# data as time-separable terms, as above; 'stationary' has no Neumann edge (its id -1 marks
+# none), so every boundary edge is Dirichlet.
+IMPLICIT_CASES = ('solid_body', 'stationary', 'transient_ode', 'transient')
+
+
+def configure_implicit(pd):
+    """Sets isStationary, isAnalytical, numSteps, tEnd, c0Cont, u1Cont, u2Cont, cCont, fTerms,
+    cDTerms and the device functions ('c0', 'u', 'cCont' at a time t) of an implicit case."""
+    from . import _lib as L
+    tc = pd['testcase']
+    cos7 = lambda x1, x2: np.cos(7 * x1) * np.cos(7 * x2)
+    u1e = lambda x1, x2: np.exp(0.5 * (x1 + x2))
+    u2e = lambda x1, x2: np.exp(0.5 * (x1 - x2))
+    adv = lambda x1, x2: (-7 * u1e(x1, x2) * np.sin(7 * x1) * np.cos(7 * x2)
+                          - 7 * u2e(x1, x2) * np.cos(7 * x1) * np.sin(7 * x2)
+                          + 0.5 * (u1e(x1, x2) - u2e(x1, x2)) * cos7(x1, x2))
+    ones = lambda x1, x2: np.ones(np.broadcast(x1, x2).shape)
+    if tc == 'solid_body':
+        d = dict(isStationary=False, isAnalytical=False, numSteps=320, tEnd=2 * np.pi,
+                 u1Cont=lambda x1, x2: 0.5 - x2, u2Cont=lambda x1, x2: x1 - 0.5, fTerms=[], cDTerms=[])
+        d['c0Cont'] = configure(dict(testcase='solid_body', jitter=0.0))['c0Cont']   # the explicit case's c0
+        fns = dict(c0=(L.FN_SOLID_BODY, []), u=(L.VEL_ROTATION, []))
+    elif tc == 'stationary':
+        d = dict(isStationary=True, isAnalytical=True, numSteps=1, tEnd=10, u1Cont=u1e, u2Cont=u2e,
+                 cCont=lambda t, x1, x2: cos7(x1, x2), c0Cont=cos7,
+                 fTerms=[('const', adv)], cDTerms=[('const', cos7)])
+        fns = dict(c0=(L.FN_COS7, []), u=(L.VEL_TRANSIENT, []), cCont=(L.FN_COS7, []))
+    elif tc == 'transient_ode':
+        zero = lambda x1, x2: np.zeros(np.broadcast(x1, x2).shape)
+        d = dict(isStationary=False, isAnalytical=True, numSteps=4, tEnd=2, u1Cont=zero, u2Cont=zero,
+                 cCont=lambda t, x1, x2: np.exp(-t) * ones(x1, x2), c0Cont=ones,
+                 fTerms=[('exp_neg', lambda x1, x2: -ones(x1, x2))], cDTerms=[('exp_neg', ones)])
+        fns = dict(c0=(L.FN_CONST, [1.0]), u=(L.VEL_CONST, [0.0, 0.0]))
+    elif tc == 'transient':
+        d = dict(isStationary=False, isAnalytical=True, numSteps=10, tEnd=2, u1Cont=u1e, u2Cont=u2e,
+                 cCont=lambda t, x1, x2: cos7(x1, x2) + np.exp(-t),
+                 c0Cont=lambda x1, x2: cos7(x1, x2) + 1.0,
+                 fTerms=[('const', adv), ('exp_neg', lambda x1, x2: -1 + 0.5 * (u1e(x1, x2) - u2e(x1, x2)))],
+                 cDTerms=[('const', cos7), ('exp_neg', ones)])
+        fns = dict(c0=(L.FN_TRANSIENT, []), u=(L.VEL_TRANSIENT, []), cCont=(L.FN_TRANSIENT, []))
+    else:
+        raise ValueError('Invalid testcase "%s".' % tc)
+    for k, v in d.items():
+        pd.setdefault(k, v)
+    pd['jitter'] = pd.get('jitter') or 0.0
+    pd.setdefault('meshSeed', 0)
+    pd['implicitFns'] = fns
+    return pd

@@ -36,7 +36,8 @@ enum {
   DGADV_ENONFINITE = 5,    /* a kernel found NaN/Inf in the state                          */
   DGADV_ETIMEOUT = 6,      /* a bounded device-side wait gave up                           */
   DGADV_EUNSUPPORTED = 7,  /* option not supported by this build (e.g. p > 3 on the GPU)  */
-  DGADV_EIO = 8            /* an output file could not be written                          */
+  DGADV_EIO = 8,           /* an output file could not be written                          */
+  DGADV_ENOCONV = 9        /* an iterative solve stopped before its tolerance               */
 };
 
 /* Arithmetic of the stored state and of every kernel: FP64; FP32; or DF32, each real an
@@ -53,8 +54,11 @@ enum {
   DGADV_FLAG_NO_PDL = 8,       /* no programmatic dependent launch between stage kernels   */
   DGADV_FLAG_FUSE = 16,        /* linear limiter with zero Dirichlet data: apply the solution
                                   limiter inside the next stage's operator kernel            */
-  DGADV_FLAG_PERSIST = 32      /* one cooperative launch per time step with grid barriers
+  DGADV_FLAG_PERSIST = 32,     /* one cooperative launch per time step with grid barriers
                                   (FP32 / FP64, linear limiter or none, no source terms)     */
+  DGADV_FLAG_IMPLICIT = 64     /* the advection_implicit problem: volume integrals and velocity
+                                  projections with the rule of order 2p+1; only implicit steps
+                                  (dgadv_step_implicit, dgadv_solve_stationary), no limiter     */
 };
 
 /* options of dgadv_set_option (launch configuration: graph length and dependent launch leave
@@ -190,6 +194,29 @@ int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *value);
  * reference. */
 int dgadv_selftest_wait(dgadv_handle *h, double seconds);
 
+/* ---- implicit time stepping (advection_implicit) ----------------------------------------
+ * Each stage of the diagonally implicit Runge-Kutta method of core/rungeKuttaImplicit.m solves
+ * (M + tau a_ii A) x_i = tau a_ii sysV(t_i) + M c^n + sum_j tau a_ij rhs_j
+ * (advection_implicit/solveSubStep.m).  The reference uses a sparse direct solver; here the
+ * system, multiplied by M^-1, is solved matrix-free by restarted GMRES with a block-Jacobi
+ * preconditioner (the inverse of each element's diagonal block), to a relative residual tol. */
+typedef struct dgadv_krylov {
+  double tol;          /* relative residual of every solve (default 1e-12)                     */
+  int32_t maxIter;     /* iterations per solve (default 2000)                                  */
+  int32_t restart;     /* Krylov vectors before a restart, 1..256 (default 50)                 */
+} dgadv_krylov;
+
+/* Replaces advection_implicit/solveStep.m and its sub-steps: steps nStep0+1 .. nStep0+nSteps
+ * of order ordRK (1..4) with step size tau, source terms at the stage times.  kr may be NULL
+ * (defaults).  iters receives the GMRES iterations, relres the largest final relative residual
+ * (either may be NULL).  DGADV_ENOCONV if a solve stopped at maxIter.  Synchronous. */
+int dgadv_step_implicit(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau, int32_t ordRK,
+                        const dgadv_krylov *kr, int32_t *iters, double *relres);
+
+/* The stationary problem A c = sysV(0) (advection_implicit/solveSubStep.m, isStationary), with
+ * the current state as the initial guess; the solution becomes the state. */
+int dgadv_solve_stationary(dgadv_handle *h, const dgadv_krylov *kr, int32_t *iters, double *relres);
+
 /* ---- set-up on the device ------------------------------------------------------------
  * The reference hands its data to the solver as closures (advection/configureProblem.m:106-133)
  * and evaluates them on the host.  Here the built-in test cases' functions are device
@@ -204,10 +231,12 @@ enum {
   DGADV_FN_GAUSS_SLOT = 3,   /* exp(-((x-0.25)^2 + (y-0.5)^2) / 0.01) + the slotted cylinder     */
   DGADV_FN_GAUSS = 4,        /* exp(-((x-p0)^2 + (y-p1)^2) / p2), p2 the squared width          */
   DGADV_FN_TRANSIENT = 5,    /* cCont of 'transient': cos(7x) cos(7y) + exp(-t) (:126)          */
+  DGADV_FN_COS7 = 6,         /* cos(7x) cos(7y) ('stationary' of advection_implicit/getTestcase.m) */
   DGADV_VEL_ROTATION = 16,   /* u = (0.5 - y, x - 0.5) ('solid_body', :115-116)                 */
   DGADV_VEL_TRANSIENT = 17,  /* u = (exp((x+y)/2), exp((x-y)/2)) ('transient', :127-128)        */
-  DGADV_VEL_STREAM = 18      /* u = (dpsi/dy, -dpsi/dx), psi = sum_m a_m sin(k_m pi x) sin(l_m pi y),
+  DGADV_VEL_STREAM = 18,     /* u = (dpsi/dy, -dpsi/dx), psi = sum_m a_m sin(k_m pi x) sin(l_m pi y),
                                 params k[M], l[M], a[M] (nParams = 3M)                          */
+  DGADV_VEL_CONST = 19       /* u = (params[0], params[1])                                        */
 };
 typedef struct dgadv_function {
   int32_t kind;              /* DGADV_FN_* or DGADV_VEL_*                                       */
