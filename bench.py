@@ -443,6 +443,60 @@ def setup_block(wl, device, reps=2):
     return out
 
 
+IMPLICIT_WORKLOAD = dict(testcase='solid_body', p=2, ordRK=3, hmax=2 ** -6, numSteps=320, tEnd=2 * np.pi)
+
+
+def implicit_block(device, steps=20, reps=2, with_cpu=True):
+    """The implicit problem's default configuration (advection_implicit/configureProblem.m:
+    solid body rotation, p = 2, 3-stage DIRK, hmax = 2^-6, 320 steps to 2 pi): wall time per
+    step of dgadv_step_implicit (every stage a block-Jacobi GMRES solve to a relative residual
+    of 1e-12 in FP64, 1e-6 in FP32), GMRES iterations per stage, and one step of the oracle's
+    sparse direct solves (scipy, host) on the same mesh with its difference to the GPU step."""
+    from festung_gb300 import advection_implicit_gpu as AI
+    from oracle import implicit as I
+    out = {'workload': 'advection_implicit defaults: solid_body, hmax=2^-6 (8192 triangles), p=2, '
+                       'DIRK3, tau=2pi/320'}
+    S = IMPLICIT_WORKLOAD['ordRK']
+    first = {}
+    for prec in ('fp64', 'fp32'):
+        pd = AI.Struct(dict(IMPLICIT_WORKLOAD, precision=prec, device=device))
+        pd.problemName = 'advection_implicit_gpu'
+        for f in AI.PRE:
+            pd = f(pd)
+        s = pd.solver
+        c0 = np.asfortranarray(s.get_state())
+        it1, _ = s.step_implicit(1, 0, pd.tau, pd.ordRK, pd.krylovTol, pd.krylovMaxIter, pd.krylovRestart)
+        first[prec] = s.get_state()
+        ts, its = [], []
+        for _ in range(reps):
+            s.set_state(c0)
+            t = time.perf_counter()
+            it, rr = s.step_implicit(steps, 0, pd.tau, pd.ordRK, pd.krylovTol, pd.krylovMaxIter, pd.krylovRestart)
+            ts.append(time.perf_counter() - t)
+            its.append(it)
+        dt = min(ts)
+        out[prec] = {'ms_per_step': 1e3 * dt / steps, 'gmres_iterations_per_stage': its[0] / (steps * S),
+                     'value': pd.K * pd.N * S * steps / dt, 'unit': 'DOF-stage/s', 'final_relres': rr,
+                     'tol': pd.krylovTol}
+        s.close()
+    if not with_cpu:
+        return out
+    # CPU baseline and checker: one step of the oracle restatement (sparse LU per stage)
+    o = I.Struct(dict(IMPLICIT_WORKLOAD))
+    o.problemName = 'advection_implicit'
+    for f in (I.configureProblem, I.preprocessProblem, I.initializeProblem):
+        o = f(o)
+    t = time.perf_counter()
+    I.solveStep(o, 1)
+    out['cpu_baseline'] = {'ms_per_step': 1e3 * (time.perf_counter() - t), 'kind': 'port', 'cores': 1,
+                           'sample': 'one step of the oracle restatement: assembly and scipy sparse LU '
+                                     'per stage, host'}
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    out['fp64_vs_oracle_rel_l2_1step'] = rel(first['fp64'], o.cDisc)
+    out['fp32_vs_oracle_rel_l2_1step'] = rel(first['fp32'], o.cDisc)
+    return out
+
+
 def ensemble_block(rank, world, device, n=256, steps=200, reps=3):
     """The ensemble workload: n seeded instances (2048 to 32768 triangles, p in {1, 2}, their own
     velocity fields), 200 steps in FP32 with the linear limiter; each degree group is one stacked
@@ -643,6 +697,9 @@ def run_ours(args):
     if rank == 0 and not args.no_adjoint:
         result['adjoint'] = adjoint_block()
 
+    if rank == 0 and not args.no_implicit:
+        result['implicit'] = implicit_block(device, with_cpu=not args.no_cpu)
+
     if rank == 0 and not args.no_cpu:
         n = thread_count()
         v, dt, _ = cpu_baseline(wl, args.cpu_stages)
@@ -671,6 +728,7 @@ def main():
     ap.add_argument('--no-ensemble', action='store_true')
     ap.add_argument('--no-tune', action='store_true')
     ap.add_argument('--no-setup', action='store_true')
+    ap.add_argument('--no-implicit', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-stages', type=int, default=1)
     ap.add_argument('--ref-stages-per-step', type=int, default=1)
