@@ -23,6 +23,8 @@ from . import advection_gpu as AG
 from . import testcases as TC
 from .solver import DeviceSolver
 
+Struct = AG.Struct
+
 
 def configureProblem(pd):
     AG.setdefault(pd, 'testcase', 'solid_body')
