@@ -136,6 +136,26 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     const mwSize K = (mwSize)mxGetScalar(prhs[2]), N = (mwSize)mxGetScalar(prhs[3]);
     plhs[0] = mxCreateDoubleMatrix(K, N, mxREAL);
     check(dgadv_get_state(h, mxGetPr(plhs[0])), h);
+  } else if (!strcmp(cmd, "step_implicit") || !strcmp(cmd, "solve_stationary")) {
+    /* [iters, relres] = dgadv_mex('step_implicit', h, nSteps, nStep0, tau, ordRK, [tol maxIter restart])
+     * [iters, relres] = dgadv_mex('solve_stationary', h, [tol maxIter restart])
+     * (handles created with flags DGADV_FLAG_IMPLICIT in the options' last entry) */
+    const int stat = !strcmp(cmd, "solve_stationary");
+    const int ko = stat ? 2 : 6;
+    dgadv_krylov kr = {1e-12, 2000, 50};
+    if (nrhs > ko && !mxIsEmpty(prhs[ko])) {
+      const double *k = dbl(prhs[ko], 3, "krylov options");
+      kr.tol = k[0]; kr.maxIter = (int32_t)k[1]; kr.restart = (int32_t)k[2];
+    }
+    int32_t it = 0;
+    double rr = 0.0;
+    if (stat)
+      check(dgadv_solve_stationary(h, &kr, &it, &rr), h);
+    else
+      check(dgadv_step_implicit(h, (int32_t)mxGetScalar(prhs[2]), (int32_t)mxGetScalar(prhs[3]), mxGetScalar(prhs[4]),
+                                (int32_t)mxGetScalar(prhs[5]), &kr, &it, &rr), h);
+    plhs[0] = mxCreateDoubleScalar((double)it);
+    if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(rr);
   } else if (!strcmp(cmd, "output")) {
     /* dgadv_mex('output', h, varName, fileName, tLvl, fileTypes): fileTypes 1 vtk, 2 tec, 3 both */
     char var[256], file[4096];
