@@ -265,6 +265,54 @@ def solve_path(wl, precision, device, c0, flush):
     return ms, c
 
 
+def large_block(device, flush):
+    """BASELINE's large single mesh (cfg5): 2,097,152 jittered triangles, p = 3, the hierarchical
+    vertex limiter, 100 SSP-RK3 steps.  One full solve from the projected initial data in FP32
+    and in FP64 after an L2 flush (the working set, >1 GB, is far beyond L2), the FP32 kernels'
+    launch times and the dominant kernel's HBM roofline, and FP32's distance to FP64."""
+    import torch
+    out = {'workload': 'cfg5: domainSquare hmax=2^-10 with 10% node jitter (2,097,152 triangles), p=3 '
+                       '(N=10), hierarchical vertex limiter, 100 SSP-RK3 steps, tau=2e-5, gauss_slot'}
+    states = {}
+    for prec in ('fp32', 'fp64'):
+        pd = setup_problem('cfg5', prec, device)
+        s = pd.solver
+        c0 = np.asfortranarray(pd._cDisc)
+        s.step(5, 0, pd.tau)                        # warm-up (graph capture, first launches)
+        s.sync()
+        s.set_state(c0)
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms = s.time_steps(pd.numSteps, 0, pd.tau)
+        states[prec] = s.get_state()
+        K, N, S = pd.K, pd.N, pd.ordRK
+        row = {'value': K * N * S * pd.numSteps / (ms / 1e3), 'unit': 'DOF-stage/s', 'ms_per_solve': ms,
+               'K': K}
+        if prec == 'fp32':
+            kpl, nl = s.profile_kernels(4, 0, pd.tau)
+            w, Q, R, nc = 4, 12, pd.p + 1, pd.p * (pd.p + 1) // 2
+            kinds = ['op2', 'limdot', 'lim']
+            names = ['k_stage_op', 'k_limit_dot', 'k_limit']
+            shares = [kpl[i] * nl[i] for i in range(3)]
+            dom = int(np.argmax(shares))
+            peak, peak_kind = measured_peaks()
+            kern = {}
+            for i in range(3):
+                b = algorithmic_bytes(kinds[i], w, N, Q, R, nc) * K
+                kern[names[i]] = {'ms_per_launch': kpl[i], 'launches': int(nl[i]),
+                                  'share': shares[i] / max(sum(shares), 1e-30),
+                                  'algorithmic_bytes_per_launch': b, 'achieved_GBps': b / (kpl[i] * 1e-3) / 1e9}
+            a = kern[names[dom]]['achieved_GBps']
+            row['kernels'] = kern
+            row['roofline'] = {'bound': 'hbm', 'kernel': names[dom], 'achieved': a, 'peak': peak, 'unit': 'GB/s',
+                               'frac': a / peak, 'peak_source': peak_kind}
+        out[prec] = row
+        s.close()
+    out['fp32_vs_fp64_rel_l2'] = float(np.linalg.norm(states['fp32'] - states['fp64']) /
+                                       np.linalg.norm(states['fp64']))
+    return out
+
+
 ADJOINT_WORKLOAD = dict(hmax=2 ** -7, p=2, numSteps=200, tEnd=200 * 2e-4)
 
 
@@ -689,6 +737,10 @@ def run_ours(args):
     if rank == 0 and not args.no_setup:
         result['setup'] = setup_block(wl, device)
 
+    if rank == 0 and not args.no_large:
+        flush = torch.empty(512 * 2 ** 20, dtype=torch.uint8, device='cuda')
+        result['large'] = large_block(device, flush)
+
     if not args.no_ensemble:
         ens = ensemble_block(rank, world, device)
         if rank == 0:
@@ -729,6 +781,7 @@ def main():
     ap.add_argument('--no-tune', action='store_true')
     ap.add_argument('--no-setup', action='store_true')
     ap.add_argument('--no-implicit', action='store_true')
+    ap.add_argument('--no-large', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-stages', type=int, default=1)
     ap.add_argument('--ref-stages-per-step', type=int, default=1)

@@ -184,7 +184,9 @@ def grid_build(coordV, V0T):
 
     def arr(p, shape, dt):
         n = int(np.prod(shape))
-        a = np.ctypeslib.as_array(p, shape=(n,)).astype(dt, copy=True)
+        ct = p._type_                                # c_double or c_int32
+        buf = (ct * n).from_address(ctypes.addressof(p.contents))
+        a = np.frombuffer(buf, dtype=np.dtype(ct), count=n).astype(dt, copy=True)
         return a.reshape(shape, order='F')
     res = dict(numT=T, numV=g.numV, numE=E,
                V0E=arr(g.V0E, (E, 2), np.int64), T0E=arr(g.T0E, (E, 2), np.int64),
