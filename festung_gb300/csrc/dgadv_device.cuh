@@ -503,8 +503,8 @@ template <typename T, int P> struct StageRows {
   __host__ __device__ static constexpr int op(int mode, bool lin) {
     return N + (mode != 2 ? N : 0) + 2 * Q + 3 * R + (mode != 0 && !lin ? 4 : 0);
   }
-  // k_limit_dot: tbuf, B, MT, c0, cin | code
-  __host__ __device__ static constexpr int limdot() { return N + 4 + NMT + 2 * N; }
+  // k_limit_dot: tbuf, B, c0, cin | code (the packed Taylor mass rows stream from global memory)
+  __host__ __device__ static constexpr int limdot() { return N + 4 + 2 * N; }
   // k_limit: tbuf, B | code
   __host__ __device__ static constexpr int lim() { return N + 4; }
   // k_limit_dot_lin: cDot, Q (N x (N-1)), c0, cin | code
@@ -914,11 +914,16 @@ k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
 // Time-derivative limiting and SSP update (advection/solveSubStep.m:69-83), then the Taylor
 // form of the new stage value and the scatter of its centroid quantities for the solution
 // limiter.
+// Resident blocks per SM asked of k_limit_dot: five in FP32 (the register cap costs a few
+// spills at p = 3 and lifts the occupancy from four blocks); no bound for the wider types.
+template <typename T> struct LimDotBlocks { static constexpr int value = 1; };
+template <> struct LimDotBlocks<float> { static constexpr int value = 5; };
+
 template <typename T, int P>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, LimDotBlocks<T>::value)
 k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
             const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
-  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value, NMT = Dims<P>::NMT;
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::limdot();
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
@@ -927,14 +932,13 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
   pdl_trigger();
   const int Kp = g.Kp;
   const bool staged = k0 < g.K;
-  constexpr int rT = 0, rB = N, rM = N + 4, rC0 = N + 4 + NMT, rC = rC0 + N;
+  constexpr int rT = 0, rB = N, rC0 = N + 4, rC = rC0 + N;
   if (staged) {
     if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
     __syncthreads();
     if (t == 0) {
       stage_expect<T>(bar, NT, 1);
       stage_T(smem, rB, g.Bm, 4, Kp, k0, bar);
-      stage_T(smem, rM, g.MT, NMT, Kp, k0, bar);
       stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
     }
   }
@@ -965,24 +969,32 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
     const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
     const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
     limit_taylor<T, P, NQ>(li, kv, sh, af, dmask, nan3, lim);
-    // Taylor mass correction M_corr = diag(1/diag(M_T)) M_T applied to (cT - lim)
+    // Taylor mass correction M_corr = diag(1/diag(M_T)) M_T applied to (cT - lim); the packed
+    // upper triangle is read once, row by row, and every row i of the product still sums its
+    // terms in the order j = 0..N-1
     T d[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) d[i] = cT[i] - lim[i];
+    T acc[N], dii[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) { acc[i] = T(0); dii[i] = T(1); }
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+      for (int b = a; b < N; ++b) {
+        const int idx = a * N - a * (a - 1) / 2 + (b - a);
+        const T m = g.MT[(size_t)idx * Kp + k];
+        if (a == b) {
+          acc[a] += m * d[a];
+          dii[a] = m;
+        } else {
+          acc[a] += m * d[b];
+          acc[b] += m * d[a];
+        }
+      }
     T cor[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      T s = T(0), dii = T(1);
-#pragma unroll
-      for (int j = 0; j < N; ++j) {
-        const int a = i < j ? i : j, b = i < j ? j : i;
-        const int idx = a * N - a * (a - 1) / 2 + (b - a);
-        const T m = srow<T>(smem, rM + idx)[t];
-        s += m * d[j];
-        if (j == i) dii = m;
-      }
-      cor[i] = lim[i] + s / dii;
-    }
+    for (int i = 0; i < N; ++i) cor[i] = lim[i] + acc[i] / dii[i];
     T cdot[N];
     from_taylor<T, P>(cor, af, cdot);
     const T w = T(sc.omega), tau = T(sc.tau);
