@@ -918,6 +918,9 @@ k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
 // spills at p = 3 and lifts the occupancy from four blocks); no bound for the wider types.
 template <typename T> struct LimDotBlocks { static constexpr int value = 1; };
 template <> struct LimDotBlocks<float> { static constexpr int value = 5; };
+// ... and of k_limit
+template <typename T> struct LimBlocks { static constexpr int value = 1; };
+template <> struct LimBlocks<float> { static constexpr int value = 5; };
 
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock, LimDotBlocks<T>::value)
@@ -1015,7 +1018,7 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
 // Solution limiter: limited Taylor coefficients back to the modal basis
 // (core/applySlopeLimiterDisc.m:77-86).
 template <typename T, int P>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, LimBlocks<T>::value)
 k_limit(const Geo<T> g, const T *tbuf, T *__restrict__ out, const LimIn<T> li,
         const StageScalars sc) {
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
