@@ -744,18 +744,6 @@ __device__ __forceinline__ bool lin_alpha(const LimIn<T> &li, const VKeys<T, NQ>
 }
 
 // ---------------------------------------------------------------------------------------------
-// Resident blocks per SM asked of k_limit_dot: five in FP32 (the register cap costs a few
-// spills at p = 3 and lifts the occupancy from four blocks); no bound for the wider types.
-template <typename T> struct LimDotBlocks { static constexpr int value = 1; };
-template <> struct LimDotBlocks<float> { static constexpr int value = 5; };
-// ... and of k_limit
-template <typename T> struct LimBlocks { static constexpr int value = 1; };
-template <> struct LimBlocks<float> { static constexpr int value = 5; };
-// ... and of the operator feeding the hierarchical limiters at p = 3 (FP32)
-template <typename T, int P, int MODE, bool LIN> struct OpBlocks { static constexpr int value = 1; };
-template <> struct OpBlocks<float, 3, 2, false> { static constexpr int value = 7; };
-template <> struct OpBlocks<float, 3, 1, false> { static constexpr int value = 7; };
-
 // Stage operator.  MODE 0: write c^(s);  MODE 1: write Taylor(c^(s)) and scatter its centroid
 // quantities;  MODE 2: write Taylor(cDot) and scatter its quantities (time-derivative limiting
 // follows).
@@ -917,7 +905,7 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
   if (bad) atomicOr(sc.flag, 1);
 }
 template <typename T, int P, int MODE, bool RHS, bool LIN>
-__global__ void __launch_bounds__(kBlock, OpBlocks<T, P, MODE, LIN>::value)
+__global__ void __launch_bounds__(kBlock)
 k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
            const LimOut<T> lo, const StageScalars sc) {
   stage_op_tile<T, P, MODE, RHS, LIN>(g, cin, c0, out, lo, sc, blockIdx.x);
@@ -926,6 +914,13 @@ k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
 // Time-derivative limiting and SSP update (advection/solveSubStep.m:69-83), then the Taylor
 // form of the new stage value and the scatter of its centroid quantities for the solution
 // limiter.
+// Resident blocks per SM asked of k_limit_dot: five in FP32 (the register cap costs a few
+// spills at p = 3 and lifts the occupancy from four blocks); no bound for the wider types.
+template <typename T> struct LimDotBlocks { static constexpr int value = 1; };
+template <> struct LimDotBlocks<float> { static constexpr int value = 5; };
+// ... and of k_limit
+template <typename T> struct LimBlocks { static constexpr int value = 1; };
+template <> struct LimBlocks<float> { static constexpr int value = 5; };
 
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock, LimDotBlocks<T>::value)
