@@ -244,26 +244,6 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   return s;
 }
 
-// partial[v * gridDim.x + b] = block b's share of <V_v, w>, v < nv <= kChunk
-template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_mdot(const T *__restrict__ V, size_t ldv, int nv,
-                                                      const T *__restrict__ w, size_t n, double *__restrict__ partial) {
-  __shared__ double sh[kVecThreads / 32];
-  double acc[kChunk];
-#pragma unroll
-  for (int v = 0; v < kChunk; ++v) acc[v] = 0.0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double wi = (double)w[i];
-#pragma unroll
-    for (int v = 0; v < kChunk; ++v)
-      if (v < nv) acc[v] += (double)V[v * ldv + i] * wi;
-  }
-  for (int v = 0; v < nv; ++v) {
-    const double s = block_sum(acc[v], sh);
-    if (threadIdx.x == 0) partial[v * gridDim.x + blockIdx.x] = s;
-  }
-}
-
 // out[v] = sum of nb partials of vector v (one block per vector, fixed order)
 __global__ void __launch_bounds__(kVecThreads) k_dot_final(const double *__restrict__ partial, int nb,
                                                            double *__restrict__ out) {
@@ -272,23 +252,6 @@ __global__ void __launch_bounds__(kVecThreads) k_dot_final(const double *__restr
   for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partial[blockIdx.x * nb + i];
   s = block_sum(s, sh);
   if (threadIdx.x == 0) out[blockIdx.x] = s;
-}
-
-// y = ay y + sgn sum_v coef[v] V_v, coefficients in device memory
-template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_vcomb(T *__restrict__ y, double ay, const T *__restrict__ V,
-                                                       size_t ldv, int nv, const double *__restrict__ coef,
-                                                       double sgn, size_t n) {
-  double c[kChunk];
-#pragma unroll
-  for (int v = 0; v < kChunk; ++v) c[v] = v < nv ? sgn * coef[v] : 0.0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    double s = ay == 0.0 ? 0.0 : ay * (double)y[i];
-#pragma unroll
-    for (int v = 0; v < kChunk; ++v)
-      if (v < nv) s += c[v] * (double)V[v * ldv + i];
-    y[i] = T(s);
-  }
 }
 
 // y = sum_v c_v x_v (host coefficients, up to kChunk vectors; y may alias an input)
@@ -315,6 +278,89 @@ __global__ void __launch_bounds__(kVecThreads) k_unit(T *__restrict__ v, const T
   const double s = nrm2[0] > 0.0 ? 1.0 / sqrt(nrm2[0]) : 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     v[i] = T((double)w[i] * s);
+}
+
+// partial[v * gridDim.x + b] = block b's share of <V_v, w> for every v < nv, kChunk vectors per
+// pass over w
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_mdot_n(const T *__restrict__ V, size_t ldv, int nv,
+                                                        const T *__restrict__ w, size_t n, double *__restrict__ partial) {
+  __shared__ double sh[kVecThreads / 32];
+  for (int v0 = 0; v0 < nv; v0 += kChunk) {
+    const int c = min(kChunk, nv - v0);
+    double acc[kChunk];
+#pragma unroll
+    for (int v = 0; v < kChunk; ++v) acc[v] = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      const double wi = (double)w[i];
+#pragma unroll
+      for (int v = 0; v < kChunk; ++v)
+        if (v < c) acc[v] += (double)V[(size_t)(v0 + v) * ldv + i] * wi;
+    }
+    for (int v = 0; v < c; ++v) {
+      const double s = block_sum(acc[v], sh);
+      if (threadIdx.x == 0) partial[(size_t)(v0 + v) * gridDim.x + blockIdx.x] = s;
+    }
+  }
+}
+
+// y = ay y + sgn sum_{v < nv} coef[v] V_v (coefficients in device memory)
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_vcomb_n(T *__restrict__ y, double ay, const T *__restrict__ V,
+                                                         size_t ldv, int nv, const double *__restrict__ coef,
+                                                         double sgn, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double s = ay == 0.0 ? 0.0 : ay * (double)y[i];
+    for (int v = 0; v < nv; ++v) s += sgn * coef[v] * (double)V[(size_t)v * ldv + i];
+    y[i] = T(s);
+  }
+}
+
+// The small dense part of GMRES, one thread: Hessenberg column j from the two Gram-Schmidt
+// passes and |w|^2, the earlier Givens rotations, a new one, and the residual estimate.
+// status: [0] |g_{j+1}|, [1] columns in use, [2] breakdown seen (later columns are ignored).
+struct GmresDense {
+  double *H, *cs, *sn, *g, *y, *status;   // H: (m + 1) x m, column-major
+};
+__global__ void k_gmres_start(GmresDense d, const double *__restrict__ nrm2, int m) {
+  d.g[0] = sqrt(fmax(nrm2[0], 0.0));
+  for (int i = 1; i <= m; ++i) d.g[i] = 0.0;
+  d.status[0] = d.g[0];
+  d.status[1] = 0.0;
+  d.status[2] = 0.0;
+}
+__global__ void k_gmres_column(GmresDense d, const double *__restrict__ h1, const double *__restrict__ h2,
+                               const double *__restrict__ nrm2, int j, int m) {
+  if (d.status[2] != 0.0) return;
+  double *col = d.H + (size_t)j * (m + 1);
+  for (int i = 0; i <= j; ++i) col[i] = h1[i] + h2[i];
+  col[j + 1] = sqrt(fmax(nrm2[0], 0.0));
+  for (int i = 0; i < j; ++i) {
+    const double t0 = d.cs[i] * col[i] + d.sn[i] * col[i + 1];
+    col[i + 1] = -d.sn[i] * col[i] + d.cs[i] * col[i + 1];
+    col[i] = t0;
+  }
+  const double r = hypot(col[j], col[j + 1]);
+  d.cs[j] = r > 0.0 ? col[j] / r : 1.0;
+  d.sn[j] = r > 0.0 ? col[j + 1] / r : 0.0;
+  col[j] = r;
+  col[j + 1] = 0.0;
+  d.g[j + 1] = -d.sn[j] * d.g[j];
+  d.g[j] = d.cs[j] * d.g[j];
+  d.status[0] = fabs(d.g[j + 1]);
+  d.status[1] = (double)(j + 1);
+  if (r == 0.0) d.status[2] = 1.0;
+}
+// y = H^-1 g over the columns in use (upper triangular), zero beyond them.
+__global__ void k_gmres_solve(GmresDense d, int m) {
+  const int je = (int)d.status[1];
+  for (int i = m - 1; i >= je; --i) d.y[i] = 0.0;
+  for (int i = je - 1; i >= 0; --i) {
+    double s = d.g[i];
+    for (int l = i + 1; l < je; ++l) s -= d.H[(size_t)l * (m + 1) + i] * d.y[l];
+    const double diag = d.H[(size_t)i * (m + 1) + i];
+    d.y[i] = diag != 0.0 ? s / diag : 0.0;
+  }
 }
 
 double time_factor_of(int fn, double t) { return fn == DGADV_TIME_EXP_NEG ? std::exp(-t) : 1.0; }
@@ -368,6 +414,7 @@ struct ImplicitState {
   double *partial = nullptr;      // kChunk x kMaxDotBlocks
   double *dres = nullptr;         // 3 x (m + 2): h1, h2, |w|^2
   double *dcoef = nullptr;        // m + 1 coefficients
+  double *dense = nullptr;        // H ((m + 1) x m), cs, sn, g, y, status
   double *hres = nullptr;         // pinned mirror of dres
   bool tablesLoaded = false;
 };
@@ -446,19 +493,12 @@ struct Solver {
   }
   // dres[off + v] = <V_v, w> for v < nv (V: nv vectors of stride n)
   void mdot(const T *V, int nv, const T *w, int off) {
-    for (int v0 = 0; v0 < nv; v0 += kChunk) {
-      const int c = std::min(kChunk, nv - v0);
-      k_mdot<T><<<nbD, kVecThreads, 0, h->stream>>>(V + (size_t)v0 * n, n, c, w, n, st->partial);
-      k_dot_final<<<c, kVecThreads, 0, h->stream>>>(st->partial, nbD, st->dres + off + v0);
-    }
+    k_mdot_n<T><<<nbD, kVecThreads, 0, h->stream>>>(V, n, nv, w, n, st->partial);
+    k_dot_final<<<nv, kVecThreads, 0, h->stream>>>(st->partial, nbD, st->dres + off);
   }
   // y = ay y + sgn V coef (coef in device memory)
   void vcomb(T *y, double ay, const T *V, int nv, const double *coef, double sgn) {
-    for (int v0 = 0; v0 < nv; v0 += kChunk) {
-      const int c = std::min(kChunk, nv - v0);
-      k_vcomb<T><<<gridV, kVecThreads, 0, h->stream>>>(y, v0 == 0 ? ay : 1.0, V + (size_t)v0 * n, n, c,
-                                                       coef + v0, sgn, n);
-    }
+    if (nv > 0) k_vcomb_n<T><<<gridV, kVecThreads, 0, h->stream>>>(y, ay, V, n, nv, coef, sgn, n);
   }
   void comb(T *y, std::initializer_list<std::pair<const T *, double>> terms) {
     Comb<T> cb{};
@@ -475,8 +515,12 @@ struct Solver {
   }
 
   // Solves (ca I + cb cDot0) x = b, x holding the initial guess; right block-Jacobi
-  // preconditioning.  Returns DGADV_OK or DGADV_ENOCONV; iters accumulates iterations.
+  // preconditioning.  The Hessenberg column, the Givens rotations and the small triangular
+  // solve run on the device; the host reads the residual estimate every kCheck iterations
+  // (a few iterations past convergence only improve the iterate).  Returns DGADV_OK or
+  // DGADV_ENOCONV; iters accumulates iterations.
   int gmres(const T *b, T *x, double ca, double cb, double tol, int maxIter, int &iters, double &relres) {
+    constexpr int kCheck = 4;
     const int m = st->m;
     build_prec(ca, cb);
     T *w = vec(st->w), *z = vec(st->z), *r = vec(st->r);
@@ -486,66 +530,50 @@ struct Solver {
       relres = 0.0;
       return DGADV_OK;
     }
-    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+    GmresDense d;
+    d.H = st->dense;
+    d.cs = d.H + (size_t)(m + 1) * m;
+    d.sn = d.cs + m;
+    d.g = d.sn + m;
+    d.y = d.g + (m + 1);
+    d.status = d.y + m;
+    double *h1 = st->dres, *h2 = st->dres + (m + 1), *nw = st->dres + 2 * (m + 1);
     int used = 0;
     for (;;) {
       op(x, w, ca, cb, false, 0.0);
       comb(r, {{b, 1.0}, {w, -1.0}});
-      const double beta2 = norm2(r);
-      const double beta = std::sqrt(beta2);
+      const double beta = std::sqrt(norm2(r));
       relres = beta / bnorm;
       if (relres <= tol) return DGADV_OK;
       if (used >= maxIter) return DGADV_ENOCONV;
       k_unit<T><<<gridV, kVecThreads, 0, h->stream>>>(basis(0), r, st->dres, n);
-      std::fill(g.begin(), g.end(), 0.0);
-      g[0] = beta;
+      k_gmres_start<<<1, 1, 0, h->stream>>>(d, st->dres, m);
       int j = 0;
-      bool done = false;
-      for (; j < m && used < maxIter; ++j) {
+      while (j < m && used < maxIter) {
         ++used;
         ++iters;
         prec(basis(j), z);
         op(z, w, ca, cb, false, 0.0);
-        // classical Gram-Schmidt, twice
-        mdot(basis(0), j + 1, w, 0);
-        vcomb(w, 1.0, basis(0), j + 1, st->dres, -1.0);
+        mdot(basis(0), j + 1, w, 0);                  // classical Gram-Schmidt, twice
+        vcomb(w, 1.0, basis(0), j + 1, h1, -1.0);
         mdot(basis(0), j + 1, w, m + 1);
-        vcomb(w, 1.0, basis(0), j + 1, st->dres + m + 1, -1.0);
+        vcomb(w, 1.0, basis(0), j + 1, h2, -1.0);
         mdot(w, 1, w, 2 * (m + 1));
-        k_unit<T><<<gridV, kVecThreads, 0, h->stream>>>(basis(j + 1), w, st->dres + 2 * (m + 1), n);
-        cudaMemcpyAsync(st->hres, st->dres, 3 * (m + 1) * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
-        if (cudaStreamSynchronize(h->stream) != cudaSuccess) return DGADV_ECUDA;
-        double *col = &H[(size_t)j * (m + 1)];
-        for (int i = 0; i <= j; ++i) col[i] = st->hres[i] + st->hres[m + 1 + i];
-        col[j + 1] = std::sqrt(std::max(st->hres[2 * (m + 1)], 0.0));
-        for (int i = 0; i < j; ++i) {   // earlier rotations
-          const double t0 = cs[i] * col[i] + sn[i] * col[i + 1];
-          col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
-          col[i] = t0;
+        k_unit<T><<<gridV, kVecThreads, 0, h->stream>>>(basis(j + 1), w, nw, n);
+        k_gmres_column<<<1, 1, 0, h->stream>>>(d, h1, h2, nw, j, m);
+        ++j;
+        if (j % kCheck == 0 || j == m || used >= maxIter) {
+          cudaMemcpyAsync(st->hres, d.status, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+          if (cudaStreamSynchronize(h->stream) != cudaSuccess) return DGADV_ECUDA;
+          relres = st->hres[0] / bnorm;
+          if (relres <= tol || st->hres[2] != 0.0) break;
         }
-        const double d = std::hypot(col[j], col[j + 1]);
-        cs[j] = d > 0 ? col[j] / d : 1.0;
-        sn[j] = d > 0 ? col[j + 1] / d : 0.0;
-        col[j] = d;
-        col[j + 1] = 0.0;
-        g[j + 1] = -sn[j] * g[j];
-        g[j] = cs[j] * g[j];
-        relres = std::fabs(g[j + 1]) / bnorm;
-        if (relres <= tol || d == 0.0) { ++j; done = true; break; }
       }
-      // x += P^-1 V y, y = H^-1 g (upper triangular j x j)
-      for (int i = j - 1; i >= 0; --i) {
-        double s = g[i];
-        for (int l = i + 1; l < j; ++l) s -= H[(size_t)l * (m + 1) + i] * y[l];
-        const double diag = H[(size_t)i * (m + 1) + i];
-        y[i] = diag != 0.0 ? s / diag : 0.0;
-      }
-      cudaMemcpyAsync(st->dcoef, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, h->stream);
-      vcomb(r, 0.0, basis(0), j, st->dcoef, 1.0);
+      // x += P^-1 V y with y = H^-1 g over the columns in use
+      k_gmres_solve<<<1, 1, 0, h->stream>>>(d, m);
+      vcomb(r, 0.0, basis(0), j, d.y, 1.0);
       prec(r, z);
       comb(x, {{x, 1.0}, {z, 1.0}});
-      if (cudaStreamSynchronize(h->stream) != cudaSuccess) return DGADV_ECUDA;   // y stays alive until here
-      (void)done;
     }
   }
 
@@ -611,9 +639,10 @@ int ensure_state(dgadv_handle *h, int restart) {
     if ((e = dev_alloc(h, b, vb))) return e;
   if ((e = dev_alloc(h, &st->kst, 4 * vb))) return e;
   if ((e = dev_alloc(h, &st->Pinv, (size_t)h->N * h->N * h->Kp * rb))) return e;
-  if ((e = dev_alloc(h, (void **)&st->partial, (size_t)kChunk * kMaxDotBlocks * 8))) return e;
+  if ((e = dev_alloc(h, (void **)&st->partial, (size_t)(restart + 2) * kMaxDotBlocks * 8))) return e;
   if ((e = dev_alloc(h, (void **)&st->dres, (size_t)3 * (restart + 1) * 8))) return e;
   if ((e = dev_alloc(h, (void **)&st->dcoef, (size_t)(restart + 1) * 8))) return e;
+  if ((e = dev_alloc(h, (void **)&st->dense, ((size_t)(restart + 1) * restart + 4 * (size_t)restart + 8) * 8))) return e;
   DG_CUDA(cudaMallocHost((void **)&st->hres, (size_t)3 * (restart + 1) * 8));
   DG_CUDA(cudaMemsetAsync(st->V, 0, (size_t)(restart + 1) * vb, h->stream));
   for (void **b : bufs) DG_CUDA(cudaMemsetAsync(*b, 0, vb, h->stream));
