@@ -304,6 +304,7 @@ extern "C" int dgadv_set_velocity_theta(dgadv_handle *h, const double *theta) {
   if ((st = upload_real(h, h->F, F))) return st;
   if ((st = upload_real(h, h->Vn, Vn))) return st;
   h->hasVelocity = true;
+  ++h->velVersion;
   h->recorded = false;
   return DGADV_OK;
 }

@@ -62,6 +62,7 @@ struct dgadv_handle {
   dgadv::OutputQueue *outq = nullptr;         // solution output (dgadv_output), made on first use
   dgadv::ImplicitState *impl = nullptr;       // implicit solver (dgadv_step_implicit), on first use
   int velOrder = 1;                           // order of the velocity projections (2p or 2p+1)
+  int velVersion = 0;                         // bumped whenever the velocity factors change
   dgadv::RefTables tables;
   // CUDA graphs of a chunk of steps, one per phase (limPass mod 3) at the chunk start
   cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};

@@ -410,11 +410,13 @@ struct ImplicitState {
   void *kst = nullptr;            // 4 x n stage derivatives
   void *Pinv = nullptr;           // N^2 x Kp
   double pinvA = 0.0, pinvB = 0.0;
-  bool pinvValid = false;
+  int pinvVersion = -1;           // velocity version the blocks were built for
   double *partial = nullptr;      // kChunk x kMaxDotBlocks
   double *dres = nullptr;         // 3 x (m + 2): h1, h2, |w|^2
   double *dcoef = nullptr;        // m + 1 coefficients
   double *dense = nullptr;        // H ((m + 1) x m), cs, sn, g, y, status
+  std::vector<cudaGraphExec_t> arnoldi;   // Arnoldi step j as a CUDA graph, for (graphA, graphB)
+  double graphA = 0.0, graphB = 0.0;
   double *hres = nullptr;         // pinned mirror of dres
   bool tablesLoaded = false;
 };
@@ -422,6 +424,8 @@ struct ImplicitState {
 void implicit_release(dgadv_handle *h) {
   ImplicitState *st = h->impl;
   if (!st) return;
+  for (cudaGraphExec_t g : st->arnoldi)
+    if (g) cudaGraphExecDestroy(g);
   if (st->hres) cudaFreeHost(st->hres);
   delete st;   // device buffers belong to h->allocs
   h->impl = nullptr;
@@ -487,9 +491,9 @@ struct Solver {
     k_impl_prec<T, P><<<gridK, kImplBlock, 0, h->stream>>>(h->K, h->Kp, (const T *)st->Pinv, r, z);
   }
   void build_prec(double ca, double cb) {
-    if (st->pinvValid && st->pinvA == ca && st->pinvB == cb) return;
+    if (st->pinvVersion == h->velVersion && st->pinvA == ca && st->pinvB == cb) return;
     k_impl_block<T, P><<<gridK, kImplBlock, 0, h->stream>>>(args, ca, cb, (T *)st->Pinv);
-    st->pinvA = ca; st->pinvB = cb; st->pinvValid = true;
+    st->pinvA = ca; st->pinvB = cb; st->pinvVersion = h->velVersion;
   }
   // dres[off + v] = <V_v, w> for v < nv (V: nv vectors of stride n)
   void mdot(const T *V, int nv, const T *w, int off) {
@@ -512,6 +516,48 @@ struct Solver {
     cudaMemcpyAsync(st->hres, st->dres, sizeof(double), cudaMemcpyDeviceToHost, h->stream);
     cudaStreamSynchronize(h->stream);
     return st->hres[0];
+  }
+
+  // Arnoldi step j: w = A P^-1 v_j, orthogonalised against v_0..v_j (classical Gram-Schmidt,
+  // twice), v_{j+1} = w / |w|, and the dense update of column j.
+  void arnoldi_enqueue(int j, double ca, double cb, const GmresDense &d) {
+    const int m = st->m;
+    T *w = vec(st->w), *z = vec(st->z);
+    double *h1 = st->dres, *h2 = st->dres + (m + 1), *nw = st->dres + 2 * (m + 1);
+    prec(basis(j), z);
+    op(z, w, ca, cb, false, 0.0);
+    mdot(basis(0), j + 1, w, 0);
+    vcomb(w, 1.0, basis(0), j + 1, h1, -1.0);
+    mdot(basis(0), j + 1, w, m + 1);
+    vcomb(w, 1.0, basis(0), j + 1, h2, -1.0);
+    mdot(w, 1, w, 2 * (m + 1));
+    k_unit<T><<<gridV, kVecThreads, 0, h->stream>>>(basis(j + 1), w, nw, n);
+    k_gmres_column<<<1, 1, 0, h->stream>>>(d, h1, h2, nw, j, m);
+  }
+  // The step as a CUDA graph, captured once per j and operator (all its buffers are the
+  // handle's own; the operator's coefficients are baked in).
+  int arnoldi_step(int j, double ca, double cb, const GmresDense &d) {
+    if (h->flags & DGADV_FLAG_NO_GRAPH) {
+      arnoldi_enqueue(j, ca, cb, d);
+      return DGADV_OK;
+    }
+    if (st->graphA != ca || st->graphB != cb || (int)st->arnoldi.size() != st->m) {
+      for (cudaGraphExec_t g : st->arnoldi)
+        if (g) cudaGraphExecDestroy(g);
+      st->arnoldi.assign(st->m, nullptr);
+      st->graphA = ca;
+      st->graphB = cb;
+    }
+    if (!st->arnoldi[j]) {
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return DGADV_ECUDA;
+      arnoldi_enqueue(j, ca, cb, d);
+      if (cudaStreamEndCapture(h->stream, &g) != cudaSuccess) return DGADV_ECUDA;
+      const cudaError_t e = cudaGraphInstantiate(&st->arnoldi[j], g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return DGADV_ECUDA;
+    }
+    return cudaGraphLaunch(st->arnoldi[j], h->stream) == cudaSuccess ? DGADV_OK : DGADV_ECUDA;
   }
 
   // Solves (ca I + cb cDot0) x = b, x holding the initial guess; right block-Jacobi
@@ -537,7 +583,6 @@ struct Solver {
     d.g = d.sn + m;
     d.y = d.g + (m + 1);
     d.status = d.y + m;
-    double *h1 = st->dres, *h2 = st->dres + (m + 1), *nw = st->dres + 2 * (m + 1);
     int used = 0;
     for (;;) {
       op(x, w, ca, cb, false, 0.0);
@@ -552,15 +597,7 @@ struct Solver {
       while (j < m && used < maxIter) {
         ++used;
         ++iters;
-        prec(basis(j), z);
-        op(z, w, ca, cb, false, 0.0);
-        mdot(basis(0), j + 1, w, 0);                  // classical Gram-Schmidt, twice
-        vcomb(w, 1.0, basis(0), j + 1, h1, -1.0);
-        mdot(basis(0), j + 1, w, m + 1);
-        vcomb(w, 1.0, basis(0), j + 1, h2, -1.0);
-        mdot(w, 1, w, 2 * (m + 1));
-        k_unit<T><<<gridV, kVecThreads, 0, h->stream>>>(basis(j + 1), w, nw, n);
-        k_gmres_column<<<1, 1, 0, h->stream>>>(d, h1, h2, nw, j, m);
+        if (int e = arnoldi_step(j, ca, cb, d)) return e;
         ++j;
         if (j % kCheck == 0 || j == m || used >= maxIter) {
           cudaMemcpyAsync(st->hres, d.status, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream);

@@ -415,6 +415,7 @@ extern "C" int dgadv_set_velocity_function(dgadv_handle *h, const dgadv_function
   DG_CUDA(ops_of(h).from_f64(h, h->Vn, (const double *)Vn, nV));
   DG_CUDA(cudaStreamSynchronize(h->stream));
   h->hasVelocity = true;
+  ++h->velVersion;
   return DGADV_OK;
 }
 

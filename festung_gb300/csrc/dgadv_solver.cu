@@ -401,6 +401,7 @@ extern "C" int dgadv_set_velocity(dgadv_handle *h, const double *u1, const doubl
   if ((st = upload_real(h, h->F, F))) return st;
   if ((st = upload_real(h, h->Vn, Vn))) return st;
   h->hasVelocity = true;
+  ++h->velVersion;
   return DGADV_OK;
 }
 
