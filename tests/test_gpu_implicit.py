@@ -92,3 +92,23 @@ def test_implicit_handle_refuses_explicit_steps(lib):
         assert e.value.status == L.DGADV_EINVAL
     finally:
         s.close()
+
+
+def test_graph_and_eager_arnoldi_steps_agree_bitwise(lib):
+    """The Arnoldi steps replayed as CUDA graphs give the eager launches' results bit for bit."""
+    from festung_gb300 import _lib as L
+    from festung_gb300 import advection_implicit_gpu as AI
+    out = []
+    for flags in (0, L.FLAG_NO_GRAPH):
+        pd = AI.Struct(dict(testcase='transient', p=2, ordRK=3, hmax=1 / 4, numSteps=3, tEnd=0.3,
+                            precision='fp64'))
+        pd.problemName = 'advection_implicit_gpu'
+        for f in AI.PRE:
+            pd = f(pd)
+        try:
+            pd.solver.set_option(L.OPT_FLAGS, flags)
+            it, rr = pd.solver.step_implicit(3, 0, pd.tau, 3, 1e-13)
+            out.append((pd.solver.get_state(), it))
+        finally:
+            pd.solver.close()
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
