@@ -294,18 +294,23 @@ def large_block(device, flush):
             kinds = ['op2', 'limdot', 'lim']
             names = ['k_stage_op', 'k_limit_dot', 'k_limit']
             shares = [kpl[i] * nl[i] for i in range(3)]
+            tot = max(sum(shares), 1e-30)
             dom = int(np.argmax(shares))
             peak, peak_kind = measured_peaks()
             kern = {}
             for i in range(3):
                 b = algorithmic_bytes(kinds[i], w, N, Q, R, nc) * K
-                kern[names[i]] = {'ms_per_launch': kpl[i], 'launches': int(nl[i]),
-                                  'share': shares[i] / max(sum(shares), 1e-30),
-                                  'algorithmic_bytes_per_launch': b, 'achieved_GBps': b / (kpl[i] * 1e-3) / 1e9}
-            a = kern[names[dom]]['achieved_GBps']
+                live = ms * shares[i] / tot / (nl[i] / 4.0 * pd.numSteps)
+                kern[names[i]] = {'ms_per_launch_isolated': kpl[i], 'ms_per_launch_live': live,
+                                  'share': shares[i] / tot, 'algorithmic_bytes_per_launch': b,
+                                  'achieved_GBps_live': b / (live * 1e-3) / 1e9,
+                                  'achieved_GBps_isolated': b / (kpl[i] * 1e-3) / 1e9}
+            a = kern[names[dom]]['achieved_GBps_live']
+            ai = kern[names[dom]]['achieved_GBps_isolated']
             row['kernels'] = kern
             row['roofline'] = {'bound': 'hbm', 'kernel': names[dom], 'achieved': a, 'peak': peak, 'unit': 'GB/s',
-                               'frac': a / peak, 'peak_source': peak_kind}
+                               'frac': a / peak, 'peak_source': peak_kind, 'achieved_isolated': ai,
+                               'frac_isolated': ai / peak}
         out[prec] = row
         s.close()
     out['fp32_vs_fp64_rel_l2'] = float(np.linalg.norm(states['fp32'] - states['fp64']) /
@@ -664,16 +669,23 @@ def run_ours(args):
     names = {'op0': 'k_stage_op', 'op1': 'k_stage_op', 'op2': 'k_stage_op', 'limdot': 'k_limit_dot',
              'lim': 'k_limit'}
     shares = [kpl[i] * nlaunch[i] for i in range(3)]
+    tot = max(sum(shares), 1e-30)
     dom = int(np.argmax(shares))
     peak, peak_kind = measured_peaks()
     bytes_launch = algorithmic_bytes(kinds[dom], w, N, Q, R, nc) * K
-    achieved = bytes_launch / (kpl[dom] * 1e-3) / 1e9
-    kernel_profile = {names[kinds[i]] + ('' if i else ''): {'ms_per_launch': kpl[i], 'launches': int(nlaunch[i]),
-                      'share': shares[i] / max(sum(shares), 1e-30),
+    # live launch time in the timed region: the timed solve split over the kernels by their
+    # share of the event-timed launches (the chained kernels overlap, so no launch can be timed
+    # alone inside the solve); the isolated launch time is reported beside it
+    per_solve = [nlaunch[i] / 20.0 * steps for i in range(3)]
+    live_ms = [ms_per_step * shares[i] / tot / per_solve[i] if nlaunch[i] else None for i in range(3)]
+    achieved = bytes_launch / (live_ms[dom] * 1e-3) / 1e9
+    achieved_iso = bytes_launch / (kpl[dom] * 1e-3) / 1e9
+    kernel_profile = {names[kinds[i]]: {'ms_per_launch_isolated': kpl[i], 'ms_per_launch_live': live_ms[i],
+                      'launches_per_solve': int(per_solve[i]), 'share': shares[i] / tot,
                       'algorithmic_bytes_per_launch': algorithmic_bytes(kinds[i], w, N, Q, R, nc) * K,
-                      'achieved_GBps': algorithmic_bytes(kinds[i], w, N, Q, R, nc) * K / (kpl[i] * 1e-3) / 1e9
-                      if kpl[i] > 0 else None}
-                      for i in range(3) if nlaunch[i]}
+                      'achieved_GBps_live': algorithmic_bytes(kinds[i], w, N, Q, R, nc) * K / (live_ms[i] * 1e-3) / 1e9,
+                      'achieved_GBps_isolated': algorithmic_bytes(kinds[i], w, N, Q, R, nc) * K / (kpl[i] * 1e-3) / 1e9}
+                      for i in range(3) if nlaunch[i] and kpl[i] > 0}
 
     # end to end through the C-ABI with pinned host buffers
     hin = torch.empty((N, K), dtype=torch.float64, pin_memory=True)
@@ -711,7 +723,10 @@ def run_ours(args):
         'roofline': {'bound': 'hbm', 'kernel': names[kinds[dom]], 'achieved': achieved,
                      'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
                      'peak_source': peak_kind,
-                     'traffic': MEASURED_TRAFFIC.get((wl, names[kinds[dom]]))},
+                     'traffic': MEASURED_TRAFFIC.get((wl, names[kinds[dom]])),
+                     'method': 'live: timed solve x kernel share (CUDA events around every launch of a '
+                               'profiling pass) / launches per solve',
+                     'achieved_isolated': achieved_iso, 'frac_isolated': achieved_iso / peak},
         'kernels': kernel_profile,
     }
     s.close()
