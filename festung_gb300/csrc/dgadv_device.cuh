@@ -818,8 +818,8 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
         for (int i = 0; i < N; ++i) rhs[i].fma(gm, g.rhs[((size_t)m * N + i) * Kp + k]);
       }
     }
-    // volume term
-#pragma unroll
+    // volume term (at p = 3, 12 points: unrolled by 3 to keep the body in the instruction cache)
+#pragma unroll(P >= 3 ? 3 : Q)
     for (int qq = 0; qq < Q; ++qq) {
       Acc<T> cqa(T(0));
 #pragma unroll
