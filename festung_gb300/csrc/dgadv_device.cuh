@@ -836,7 +836,7 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
     for (int n = 0; n < 3; ++n) {
       const int np = (code >> (2 * n)) & 3;
       const bool outOk = (code >> (6 + n)) & 1;
-#pragma unroll(P >= 3 ? 2 : R)
+#pragma unroll
       for (int r2 = 0; r2 < R; ++r2) {
         const T v = srow<T>(smem, rV + n * R + r2)[t];
         Acc<T> tr(T(0));
