@@ -592,7 +592,9 @@ __device__ __forceinline__ void taylor_vertex_basis(const Affine<T> &af, T phi[3
   }
 }
 
-template <typename T, int P, int NQ>
+// LT: the limiter type (0 linear, 1 hierarchical vertex, 2 strict), fixed per kernel so that
+// each kernel carries the code of one limiter only.
+template <typename T, int P, int NQ, int LT>
 __device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, NQ> &kv, const T *sh,
                                              const Affine<T> &af, int dmask, const T dataV0T[3], T *cT) {
   constexpr int N = Dims<P>::N;
@@ -600,7 +602,7 @@ __device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, 
   T pt1[3], pt2[3];   // Taylor basis functions 2 and 3 at the vertices
 #pragma unroll
   for (int n = 0; n < 3; ++n) { pt1[n] = af.ox[n] * af.dX; pt2[n] = af.oy[n] * af.dX; }
-  if (li.type == 0) {
+  if constexpr (LT == 0) {
     T v[3], valD[3], mn[3], mx[3];
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
@@ -613,7 +615,7 @@ __device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, 
     const T keep = (alpha == T(1)) ? T(1) : T(0);
 #pragma unroll
     for (int i = 3; i < N; ++i) cT[i] *= keep;
-  } else if (li.type == 2) {
+  } else if constexpr (LT == 2) {
     // core/applySlopeLimiterTaylorStrict.m:111-150: for ord = p..1 the reconstructions of
     // degree p - ord + 1 about each derivative of order ord - 1, from the data already limited
     // at the higher orders; every DOF of order >= ord is scaled by the order's factor.  The
@@ -922,7 +924,7 @@ template <> struct LimDotBlocks<float> { static constexpr int value = 5; };
 template <typename T> struct LimBlocks { static constexpr int value = 1; };
 template <> struct LimBlocks<float> { static constexpr int value = 5; };
 
-template <typename T, int P>
+template <typename T, int P, int LT>
 __global__ void __launch_bounds__(kBlock, LimDotBlocks<T>::value)
 k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
             const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
@@ -971,7 +973,7 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
     for (int i = 0; i < N; ++i) { cT[i] = srow<T>(smem, rT + i)[t]; lim[i] = cT[i]; }
     const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
     const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
-    limit_taylor<T, P, NQ>(li, kv, sh, af, dmask, nan3, lim);
+    limit_taylor<T, P, NQ, LT>(li, kv, sh, af, dmask, nan3, lim);
     // Taylor mass correction M_corr = diag(1/diag(M_T)) M_T applied to (cT - lim); the packed
     // upper triangle is read once, row by row, and every row i of the product still sums its
     // terms in the order j = 0..N-1
@@ -1017,7 +1019,7 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
 
 // Solution limiter: limited Taylor coefficients back to the modal basis
 // (core/applySlopeLimiterDisc.m:77-86).
-template <typename T, int P>
+template <typename T, int P, int LT>
 __global__ void __launch_bounds__(kBlock, LimBlocks<T>::value)
 k_limit(const Geo<T> g, const T *tbuf, T *__restrict__ out, const LimIn<T> li,
         const StageScalars sc) {
@@ -1062,7 +1064,7 @@ k_limit(const Geo<T> g, const T *tbuf, T *__restrict__ out, const LimIn<T> li,
 #pragma unroll
   for (int i = 0; i < N; ++i) cT[i] = srow<T>(smem, i)[t];
   const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
-  limit_taylor<T, P, NQ>(li, kv, sh, af, dmask, data, cT);
+  limit_taylor<T, P, NQ, LT>(li, kv, sh, af, dmask, data, cT);
   T c[N];
   from_taylor<T, P>(cT, af, c);
   bool bad = false;

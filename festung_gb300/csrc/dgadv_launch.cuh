@@ -194,8 +194,10 @@ static cudaError_t set_smem_attributes() {
     set((const void *)k_op_fused<T, P, 2, true>, SR::bytes(SR::op(2, true), 1));
     set((const void *)k_op_fused<T, P, 2, false>, SR::bytes(SR::op(2, true), 1));
   }
-  set((const void *)k_limit_dot<T, P>, SR::bytes(SR::limdot(), 1));
-  set((const void *)k_limit<T, P>, SR::bytes(SR::lim(), 1));
+  set((const void *)k_limit_dot<T, P, 1>, SR::bytes(SR::limdot(), 1));
+  set((const void *)k_limit_dot<T, P, 2>, SR::bytes(SR::limdot(), 1));
+  set((const void *)k_limit<T, P, 1>, SR::bytes(SR::lim(), 1));
+  set((const void *)k_limit<T, P, 2>, SR::bytes(SR::lim(), 1));
   set((const void *)k_to_taylor<T, P>, SR::bytes(SR::totaylor(), 0));
   return e;
 }
@@ -262,14 +264,20 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
       ++h->limPass;
       prof_mark(h, 1);
       if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)in, (const T *)cn, (const T *)tb, tb, lim_in<T>(lo1, h), lo2, sc);
-      else launch_k(h, k_limit_dot<T, P>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
+      else if (h->limType == DGADV_LIM_STRICT)
+        launch_k(h, k_limit_dot<T, P, 2>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
+      else
+        launch_k(h, k_limit_dot<T, P, 1>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
       prof_mark(h, -1);
       if (lin && h->recY[s]) copy_state(h, h->recY[s], tb, stBytes);
       loS = lo2;
     }
     prof_mark(h, 2);
     if (lin) launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
-    else launch_k(h, k_limit<T, P>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
+    else if (h->limType == DGADV_LIM_STRICT)
+      launch_k(h, k_limit<T, P, 2>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
+    else
+      launch_k(h, k_limit<T, P, 1>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
     prof_mark(h, -1);
   }
   if (S == 1) return copy_state(h, cn, cA, (size_t)h->N * h->Kp * sizeof(T));
@@ -356,7 +364,10 @@ static cudaError_t launch_limit_state(dgadv_handle *h, double t) {
     launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)h->cn, (T *)h->cn, lim_in<T>(lo, h), sc);
   } else {
     launch_k(h, k_to_taylor<T, P>, grid, SR::bytes(SR::totaylor(), 0), g, (const T *)h->cn, (T *)h->tbuf, lo, sc);
-    launch_k(h, k_limit<T, P>, grid, SR::bytes(SR::lim(), 1), g, (const T *)h->tbuf, (T *)h->cn, lim_in<T>(lo, h), sc);
+    if (h->limType == DGADV_LIM_STRICT)
+      launch_k(h, k_limit<T, P, 2>, grid, SR::bytes(SR::lim(), 1), g, (const T *)h->tbuf, (T *)h->cn, lim_in<T>(lo, h), sc);
+    else
+      launch_k(h, k_limit<T, P, 1>, grid, SR::bytes(SR::lim(), 1), g, (const T *)h->tbuf, (T *)h->cn, lim_in<T>(lo, h), sc);
   }
   return cudaGetLastError();
 }
