@@ -114,6 +114,10 @@ SYMBOLS = {
     'dgadv_step_implicit': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                            ctypes.c_int32, ctypes.POINTER(Krylov), _i32p, _dp]),
     'dgadv_solve_stationary': (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Krylov), _i32p, _dp]),
+    'dgadv_transport_init': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp, ctypes.c_double,
+                                            ctypes.c_int32]),
+    'dgadv_transport_step': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double]),
+    'dgadv_transport_get': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp, _u8p]),
     'dgadv_project_state': (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Function), ctypes.c_int32,
                                            ctypes.c_double, ctypes.c_int32]),
     'dgadv_set_velocity_function': (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Function), ctypes.c_int32]),

@@ -34,7 +34,7 @@ def sources():
                                             'dgadv_prec_df32_p01.cu', 'dgadv_prec_df32_p2.cu',
                                             'dgadv_prec_df32_p3.cu', 'dgadv_adjoint.cu',
                                             'dgadv_noalloc.cu', 'dgadv_vis.cpp', 'dgadv_output.cu',
-                                            'dgadv_setup.cu', 'dgadv_implicit.cu')]
+                                            'dgadv_setup.cu', 'dgadv_implicit.cu', 'dgadv_transport.cu')]
 
 
 # per-unit extra flags: the set-up unit evaluates quadrature points and indicator functions

@@ -19,6 +19,8 @@ struct OutputQueue;
 void output_release(dgadv_handle *h);   // joins the writer thread, frees the output buffers
 struct ImplicitState;
 void implicit_release(dgadv_handle *h); // frees the implicit solver's host state
+struct TransportState;
+void transport_release(dgadv_handle *h);
 constexpr int kBlock = 128;       // elements per CTA (one thread per element)
 constexpr int kSlotCopies = 32;   // copies of the global min / max slots (atomics spread over them)
 constexpr int kGridBarBytes = 8192;   // state of the persistent step's grid barrier
@@ -61,6 +63,7 @@ struct dgadv_handle {
   std::vector<int32_t> visV0T;                // caller's V0T, numT x 3 row-major
   dgadv::OutputQueue *outq = nullptr;         // solution output (dgadv_output), made on first use
   dgadv::ImplicitState *impl = nullptr;       // implicit solver (dgadv_step_implicit), on first use
+  dgadv::TransportState *trans = nullptr;     // transported species (dgadv_transport_init)
   int velOrder = 1;                           // order of the velocity projections (2p or 2p+1)
   int velVersion = 0;                         // bumped whenever the velocity factors change
   dgadv::RefTables tables;
@@ -129,6 +132,15 @@ struct LimVjpArgs {
   double gco[4];       // time factors of the Dirichlet data (solution limiter)
 };
 
+// One stage of one transported species (dgadv_transport.cu): c h out from c h in, the
+// step's c h, the species' concentration and mask.
+struct TrStageArgs {
+  const void *conc, *cHin, *cH0;
+  void *cHout;
+  const uint8_t *mask;
+  double omega, tau;
+};
+
 // Work of one arithmetic type, enqueued on the handle's stream.
 struct PrecOps {
   size_t realBytes;                    // bytes of one stored real
@@ -154,6 +166,10 @@ struct PrecOps {
   cudaError_t (*copy)(dgadv_handle *h, void *dst, const void *src, size_t bytes);
   // n FP64 values on the device -> stored reals
   cudaError_t (*from_f64)(dgadv_handle *h, void *dst, const double *src, size_t n);
+  // transport problem (null: not built for this type)
+  cudaError_t (*tr_stage)(dgadv_handle *h, const TrStageArgs &a);
+  cudaError_t (*tr_convert)(dgadv_handle *h, const void *in, void *out, const void *hQ, int toConc);
+  cudaError_t (*tr_mask)(dgadv_handle *h, long long pass, double tol, uint8_t *mask);
 };
 
 // Fused path (linear limiter, zero Dirichlet data, opted in): per stage the operator kernel

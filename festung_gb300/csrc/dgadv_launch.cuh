@@ -486,6 +486,9 @@ static PrecOps make_ops() {
   o.persist_attributes = nullptr;
   o.copy = copy_state;
   o.from_f64 = from_f64<T>;
+  o.tr_stage = nullptr;
+  o.tr_convert = nullptr;
+  o.tr_mask = nullptr;
   return o;
 }
 

@@ -1,4 +1,4 @@
-// Kernels and launch sequences of the FP32 path (stored reals: float), every degree, with the adjoint kernels and the persistent step.
+// Kernels and launch sequences of the FP32 path (stored reals: float), every degree, with the adjoint kernels, the persistent step and the transport kernels.
 #include "dgadv_device.cuh"
 
 namespace dgadv {
@@ -8,10 +8,12 @@ DGADV_DEFINE_TABLES(float, cTf)
 #include "dgadv_launch.cuh"
 #include "dgadv_adjoint.cuh"
 #include "dgadv_persist.cuh"
+#include "dgadv_transport.cuh"
 
 namespace dgadv {
 const PrecOps &ops_fp32() {
-  static const PrecOps ops = with_persistent<float, 0xF>(with_adjoint<float, 0xF>(make_ops<float, 0xF, true>()));
+  static const PrecOps ops =
+      with_transport<float, 0xF>(with_persistent<float, 0xF>(with_adjoint<float, 0xF>(make_ops<float, 0xF, true>())));
   return ops;
 }
 }  // namespace dgadv

@@ -685,6 +685,7 @@ extern "C" void dgadv_destroy(dgadv_handle *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   output_release(h);
   implicit_release(h);
+  transport_release(h);
   for (int i = 0; i < 3; ++i)
     if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
   if (h->adjExec) cudaGraphExecDestroy(h->adjExec);

@@ -129,6 +129,27 @@ class DeviceSolver:
         self._c(self._lib.dgadv_l2_error(self._h, arr, len(arr), float(t), int(qOrd), L.ptr(out)))
         return float(out[0]) if len(specs) == 1 else out
 
+    # ---- transported species (transport problem) ------------------------------------------
+    def transport_init(self, hDisc, cH0, maskTol=1e-6, isMask=True):
+        """hDisc K x N depth; cH0 K x N x nSpecies (c h at t = 0)."""
+        hd = L.f64(hDisc)
+        c = L.f64(cH0)
+        assert hd.shape == (self.K, self.N) and c.shape[:2] == (self.K, self.N)
+        self.nSpecies = c.shape[2]
+        self._c(self._lib.dgadv_transport_init(self._h, self.nSpecies, L.ptr(hd), L.ptr(c), float(maskTol),
+                                               1 if isMask else 0))
+
+    def transport_step(self, nSteps, nStep0, tau):
+        self._c(self._lib.dgadv_transport_step(self._h, int(nSteps), int(nStep0), float(tau)))
+
+    def transport_get(self, species):
+        """(c h, c, mask) of one species."""
+        cH = np.zeros((self.K, self.N), order='F')
+        conc = np.zeros((self.K, self.N), order='F')
+        mask = np.zeros(self.K, dtype=np.uint8)
+        self._c(self._lib.dgadv_transport_get(self._h, int(species), L.ptr(cH), L.ptr(conc), L.ptr(mask, L._u8p)))
+        return cH, conc, mask.astype(bool)
+
     # ---- implicit time stepping (handles created with flags=FLAG_IMPLICIT) -----------------
     def step_implicit(self, nSteps, nStep0, tau, ordRK, tol=1e-12, maxIter=2000, restart=50):
         """DIRK steps nStep0+1 .. nStep0+nSteps (GMRES per stage); returns (iterations, largest

@@ -217,6 +217,28 @@ int dgadv_step_implicit(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double 
  * the current state as the initial guess; the solution becomes the state. */
 int dgadv_solve_stationary(dgadv_handle *h, const dgadv_krylov *kr, int32_t *iters, double *relres);
 
+/* ---- transport of several species (transport/) -----------------------------------------
+ * The transport problem without coupling to a flow model: species advected as depth-integrated
+ * concentrations c h with the depth-integrated velocity (u h, v h), which the handle holds
+ * (dgadv_set_velocity with the projections of u h, v h).  Each species is advected only over
+ * its active elements (its mask, recomputed after every step from the limiter's patch extremes,
+ * core/computeMask.m 'vertex-based'), and its concentration c = Pi(c h / h) is limited with the
+ * handle's linear vertex limiter (zero Dirichlet data).  The handle must be explicit, with the
+ * linear limiter and p >= 1, in FP64 or FP32. */
+
+/* Replaces transport/initializeProblem.m: hDisc (K x N) the depth, cH0 (K x N x nSpecies) the
+ * projections of c h at t = 0; each species' concentration is formed, limited, and its mask
+ * computed (isMask = 0: every element stays active). */
+int dgadv_transport_init(dgadv_handle *h, int32_t nSpecies, const double *hDisc, const double *cH0,
+                         double maskTol, int32_t isMask);
+
+/* Replaces transport/solveStep.m with its sub-steps and transport/postprocessStep.m: steps
+ * nStep0+1 .. nStep0+nSteps of the handle's SSP-RK order. */
+int dgadv_transport_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau);
+
+/* Species s: c h and c (K x N each) and the mask (K, 1 = active); any output may be NULL. */
+int dgadv_transport_get(dgadv_handle *h, int32_t species, double *cH, double *conc, uint8_t *mask);
+
 /* ---- set-up on the device ------------------------------------------------------------
  * The reference hands its data to the solver as closures (advection/configureProblem.m:106-133)
  * and evaluates them on the host.  Here the built-in test cases' functions are device
