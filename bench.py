@@ -550,6 +550,46 @@ def implicit_block(device, steps=20, reps=2, with_cpu=True):
     return out
 
 
+def transport_block(device, steps=200, with_cpu=True):
+    """The transport problem's 'rotation' configuration (transport/configureProblem.m: 8192
+    triangles, p = 1, SSP-RK2, masks on), with 1 and 4 species: wall time per step of
+    dgadv_transport_step (FP64), the active fraction of the elements, and one step of the
+    oracle restatement on the host with its difference to the GPU step."""
+    from festung_gb300 import transport_gpu as TG
+    from oracle import transport as TR
+    out = {'workload': 'transport rotation: domainSquare hmax=2^-6 (8192 triangles), p=1, SSP-RK2, '
+                       'tau=2pi/3142, vertex-based masks (tol 1e-6), FP64'}
+    kw = dict(hmax=2 ** -6, numSteps=3124, tEnd=(3124 / 3142) * 2 * np.pi)
+    for ns in (1, 4):
+        pd = TG.Struct(dict(kw, numSpecies=ns, precision='fp64', device=device))
+        pd.problemName = 'transport_gpu'
+        for f in TG.PRE:
+            pd = f(pd)
+        s = pd.solver
+        s.transport_step(1, 0, pd.tau)
+        first = [s.transport_get(i) for i in range(ns)]
+        t = time.perf_counter()
+        s.transport_step(steps, 1, pd.tau)
+        dt = time.perf_counter() - t
+        act = np.mean([s.transport_get(i)[2].mean() for i in range(ns)])
+        out['species_%d' % ns] = {'ms_per_step': 1e3 * dt / steps, 'active_fraction': float(act),
+                                  'value': ns * pd.K * pd.N * pd.ordRK * steps / dt, 'unit': 'DOF-stage/s'}
+        s.close()
+        if ns == 1 and with_cpu:
+            o = TR.Struct(dict(kw, numSpecies=1))
+            o.problemName = 'transport'
+            for f in (TR.configureProblem, TR.preprocessProblem, TR.initializeProblem):
+                o = f(o)
+            t = time.perf_counter()
+            TR.solveStep(o, 1)
+            out['cpu_baseline'] = {'ms_per_step': 1e3 * (time.perf_counter() - t), 'kind': 'port', 'cores': 1,
+                                   'sample': 'one step of the oracle restatement (masked sparse assembly, host)'}
+            out['fp64_vs_oracle_rel_l2_1step'] = float(np.linalg.norm(first[0][0] - o.cDisc[0]) /
+                                                       np.linalg.norm(o.cDisc[0]))
+            out['mask_equal_1step'] = bool(np.array_equal(first[0][2], o.mask[0]))
+    return out
+
+
 def ensemble_block(rank, world, device, n=256, steps=200, reps=3):
     """The ensemble workload: n seeded instances (2048 to 32768 triangles, p in {1, 2}, their own
     velocity fields), 200 steps in FP32 with the linear limiter; each degree group is one stacked
@@ -767,6 +807,9 @@ def run_ours(args):
     if rank == 0 and not args.no_implicit:
         result['implicit'] = implicit_block(device, with_cpu=not args.no_cpu)
 
+    if rank == 0 and not args.no_transport:
+        result['transport'] = transport_block(device, with_cpu=not args.no_cpu)
+
     if rank == 0 and not args.no_cpu:
         n = thread_count()
         v, dt, _ = cpu_baseline(wl, args.cpu_stages)
@@ -797,6 +840,7 @@ def main():
     ap.add_argument('--no-setup', action='store_true')
     ap.add_argument('--no-implicit', action='store_true')
     ap.add_argument('--no-large', action='store_true')
+    ap.add_argument('--no-transport', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-stages', type=int, default=1)
     ap.add_argument('--ref-stages-per-step', type=int, default=1)
