@@ -261,6 +261,7 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
 
 extern "C" int dgadv_set_velocity_modes(dgadv_handle *h, int32_t nModes, const double *u1Modes,
                                         const double *u2Modes, const double *vNModes) {
+  return guarded(h, [&]() -> int {
   if (!h || nModes < 0 || nModes > 1024) return DGADV_EINVAL;
   if (nModes > 0 && (!u1Modes || !u2Modes || !vNModes)) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
@@ -285,9 +286,11 @@ extern "C" int dgadv_set_velocity_modes(dgadv_handle *h, int32_t nModes, const d
   if ((st = upload(h, h->modeV, allV.data(), allV.size() * 8))) return st;
   h->nModes = nModes;
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_set_velocity_theta(dgadv_handle *h, const double *theta) {
+  return guarded(h, [&]() -> int {
   if (!h || !theta) return DGADV_EINVAL;
   if (h->nModes == 0) { h->err = "no velocity modes set"; return DGADV_EINVAL; }
   DG_CUDA(cudaSetDevice(h->device));
@@ -307,9 +310,11 @@ extern "C" int dgadv_set_velocity_theta(dgadv_handle *h, const double *theta) {
   ++h->velVersion;
   h->recorded = false;
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau, int32_t nSnapshots) {
+  return guarded(h, [&]() -> int {
   if (!h || nSteps < 1 || !(tau > 0.0)) return DGADV_EINVAL;
   const PrecOps &o = ops_of(h);
   if (!o.adj_stage) { h->err = "no adjoint kernels for this precision"; return DGADV_EUNSUPPORTED; }
@@ -394,9 +399,11 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
     if ((st = forward_step(h, w))) return st;
   h->recorded = true;
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc0, double *dJdtheta) {
+  return guarded(h, [&]() -> int {
   if (!h || !dJdcT) return DGADV_EINVAL;
   if (!h->recorded) { h->err = "no recorded forward run"; return DGADV_EINVAL; }
   const PrecOps &o = ops_of(h);
@@ -493,10 +500,12 @@ extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc
   // leave c^0 as the handle's state
   DG_CUDA(o.copy(h, h->cn, h->adjSlots, bytes));
   return dgadv_sync(h);
+  });
 }
 
 extern "C" int dgadv_checkpoint_schedule(int32_t nSteps, int32_t nSnapshots, int32_t *actions, int32_t *count,
                                          int32_t *backwardStart) {
+  return guarded(nullptr, [&]() -> int {
   if (nSteps < 1 || !count) return DGADV_EINVAL;
   const int nSlots = (nSnapshots <= 0 || nSnapshots >= nSteps) ? nSteps : nSnapshots;
   std::vector<int> o;
@@ -509,4 +518,5 @@ extern "C" int dgadv_checkpoint_schedule(int32_t nSteps, int32_t nSnapshots, int
   *count = n;
   if (backwardStart) *backwardStart = (int32_t)(backward_start(o) / 2);
   return DGADV_OK;
+  });
 }

@@ -4,6 +4,7 @@
 #include <new>
 #include <string>
 
+#include "dgadv_guard.h"
 #include "../../include/dgadv.h"
 #include "dgadv_host.h"
 
@@ -11,6 +12,7 @@ using namespace dgadv;
 
 extern "C" int dgadv_grid_build(int32_t numV, const double *coordV, int32_t numT, const int32_t *V0T,
                                 dgadv_grid **out) {
+  return guarded(nullptr, [&]() -> int {
   if (!out || !coordV || !V0T || numV <= 0 || numT <= 0) return DGADV_EINVAL;
   *out = nullptr;
   Grid g;
@@ -57,6 +59,7 @@ extern "C" int dgadv_grid_build(int32_t numV, const double *coordV, int32_t numT
   }
   *out = r;
   return DGADV_OK;
+  });
 }
 
 extern "C" void dgadv_grid_free(dgadv_grid *g) {
@@ -68,6 +71,7 @@ extern "C" void dgadv_grid_free(dgadv_grid *g) {
 }
 
 extern "C" int dgadv_quad_rule_1d(int32_t qOrd, int32_t *R, double *Q, double *W) {
+  return guarded(nullptr, [&]() -> int {
   if (!R) return DGADV_EINVAL;
   Rule1D r;
   if (!quad_rule_1d(qOrd, r)) return DGADV_EINVAL;
@@ -75,9 +79,11 @@ extern "C" int dgadv_quad_rule_1d(int32_t qOrd, int32_t *R, double *Q, double *W
   if (Q && W)
     for (size_t i = 0; i < r.W.size(); ++i) { Q[i] = r.Q[i]; W[i] = r.W[i]; }
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_quad_rule_2d(int32_t qOrd, int32_t *R, double *Q1, double *Q2, double *W) {
+  return guarded(nullptr, [&]() -> int {
   if (!R) return DGADV_EINVAL;
   Rule2D r;
   if (!quad_rule_2d(qOrd, r)) return DGADV_EINVAL;
@@ -85,10 +91,12 @@ extern "C" int dgadv_quad_rule_2d(int32_t qOrd, int32_t *R, double *Q1, double *
   if (Q1 && Q2 && W)
     for (size_t i = 0; i < r.W.size(); ++i) { Q1[i] = r.Q1[i]; Q2[i] = r.Q2[i]; W[i] = r.W[i]; }
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_basis_eval(int32_t N, int32_t nPts, const double *X1, const double *X2, double *phiOut,
                                 double *gradOut) {
+  return guarded(nullptr, [&]() -> int {
   if (N < 1 || N > 15 || nPts < 0 || !X1 || !X2 || !phiOut) return DGADV_EINVAL;
   for (int q = 0; q < nPts; ++q)
     for (int i = 0; i < N; ++i) {
@@ -99,6 +107,7 @@ extern "C" int dgadv_basis_eval(int32_t N, int32_t nPts, const double *X1, const
       }
     }
   return DGADV_OK;
+  });
 }
 
 extern "C" const char *dgadv_status_string(int s) {

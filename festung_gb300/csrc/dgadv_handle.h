@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/dgadv.h"
+#include "dgadv_guard.h"
 #include "dgadv_host.h"
 
 struct dgadv_handle;

@@ -755,16 +755,20 @@ using namespace dgadv;
 
 extern "C" int dgadv_step_implicit(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau, int32_t ordRK,
                                    const dgadv_krylov *kr, int32_t *iters, double *relres) {
+  return guarded(h, [&]() -> int {
   if (!h || nSteps < 0 || !(tau > 0.0) || ordRK < 1 || ordRK > 4) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   const dgadv_krylov d = kr ? *kr : dgadv_krylov{1e-12, 2000, 50};
   if (nSteps == 0) return DGADV_OK;
   return dispatch(h, 0, nSteps, nStep0, tau, ordRK, d.tol, d.maxIter, d.restart, iters, relres);
+  });
 }
 
 extern "C" int dgadv_solve_stationary(dgadv_handle *h, const dgadv_krylov *kr, int32_t *iters, double *relres) {
+  return guarded(h, [&]() -> int {
   if (!h) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   const dgadv_krylov d = kr ? *kr : dgadv_krylov{1e-12, 2000, 50};
   return dispatch(h, 1, 0, 0, 1.0, 1, d.tol, d.maxIter, d.restart, iters, relres);
+  });
 }

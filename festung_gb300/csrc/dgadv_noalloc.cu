@@ -124,6 +124,7 @@ using namespace dgadv;
 extern "C" int dgadv_limit_linear_noalloc(int32_t p, int32_t numT, int32_t numV, const int32_t *V0T,
                                           const uint8_t *markV0TbdrD, const double *dataV0T,
                                           const double *cIn, double *cOut, void *stream) {
+  return guarded(nullptr, [&]() -> int {
   if (p < 1 || p > 3 || numT <= 0 || numV <= 0 || !V0T || !cIn || !cOut) return DGADV_EINVAL;
   if (numV > kNoAllocMaxVertices) return DGADV_ENOMEM;   // more vertices than the fixed scratch holds
   int dev = 0;
@@ -155,4 +156,5 @@ extern "C" int dgadv_limit_linear_noalloc(int32_t p, int32_t numT, int32_t numV,
                       : p == 2 ? na_launch<2>(numT, numV, V0T, markV0TbdrD, dataV0T, cIn, cOut, s, st)
                                : na_launch<3>(numT, numV, V0T, markV0TbdrD, dataV0T, cIn, cOut, s, st);
   return e == cudaSuccess ? DGADV_OK : DGADV_ECUDA;
+  });
 }

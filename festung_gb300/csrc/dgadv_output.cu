@@ -156,6 +156,7 @@ static int output_init(dgadv_handle *h) {
 using namespace dgadv;
 
 extern "C" int dgadv_get_lagrange(dgadv_handle *h, double *dataLagr, int32_t *numP) {
+  return guarded(h, [&]() -> int {
   if (!h || !dataLagr) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   const int st = output_init(h);
@@ -167,10 +168,12 @@ extern "C" int dgadv_get_lagrange(dgadv_handle *h, double *dataLagr, int32_t *nu
   DG_CUDA(cudaMemcpyAsync(dataLagr, h->outq->dev, (size_t)h->K * n * sizeof(double), cudaMemcpyDeviceToHost,
                           h->stream));
   return dgadv_sync(h);
+  });
 }
 
 extern "C" int dgadv_output(dgadv_handle *h, const char *varName, const char *fileName, int32_t tLvl,
                             int32_t fileTypes) {
+  return guarded(h, [&]() -> int {
   if (!h || !varName || !fileName || !fileTypes || (fileTypes & ~(DGADV_OUT_VTK | DGADV_OUT_TEC)))
     return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
@@ -201,9 +204,11 @@ extern "C" int dgadv_output(dgadv_handle *h, const char *varName, const char *fi
   }
   q->cv.notify_all();
   return e;
+  });
 }
 
 extern "C" int dgadv_output_wait(dgadv_handle *h) {
+  return guarded(h, [&]() -> int {
   if (!h) return DGADV_EINVAL;
   OutputQueue *q = h->outq;
   if (!q) return DGADV_OK;
@@ -215,4 +220,5 @@ extern "C" int dgadv_output_wait(dgadv_handle *h) {
     return DGADV_EIO;
   }
   return DGADV_OK;
+  });
 }

@@ -358,6 +358,7 @@ int rule_table(dgadv_handle *h, int qOrd, bool weighted, std::vector<double> &ou
 using namespace dgadv;
 
 extern "C" int dgadv_project_state(dgadv_handle *h, const dgadv_function *c0, int32_t nFn, double t, int32_t qOrd) {
+  return guarded(h, [&]() -> int {
   if (!h) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   Scratch sc(h);
@@ -374,9 +375,11 @@ extern "C" int dgadv_project_state(dgadv_handle *h, const dgadv_function *c0, in
   DG_CUDA(ops_of(h).scatter_in(h, h->cn));
   DG_CUDA(cudaStreamSynchronize(h->stream));
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_set_velocity_function(dgadv_handle *h, const dgadv_function *u, int32_t nFn) {
+  return guarded(h, [&]() -> int {
   if (!h) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   Scratch sc(h);
@@ -417,10 +420,12 @@ extern "C" int dgadv_set_velocity_function(dgadv_handle *h, const dgadv_function
   h->hasVelocity = true;
   ++h->velVersion;
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_l2_error(dgadv_handle *h, const dgadv_function *f, int32_t nFn, double t, int32_t qOrd,
                               double *err) {
+  return guarded(h, [&]() -> int {
   if (!h || !err) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   Scratch sc(h);
@@ -450,4 +455,5 @@ extern "C" int dgadv_l2_error(dgadv_handle *h, const dgadv_function *f, int32_t 
     err[i] = std::sqrt(2.0 * s);
   }
   return DGADV_OK;
+  });
 }

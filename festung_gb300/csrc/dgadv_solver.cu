@@ -26,6 +26,10 @@ static bool g_tab_loaded[64][3][kMaxP + 1];
 using namespace dgadv;
 
 
+void dgadv::set_error(const dgadv_handle *h, const char *msg) {
+  if (h) const_cast<dgadv_handle *>(h)->err = msg;
+}
+
 int dgadv::dev_alloc(dgadv_handle *h, void **p, size_t bytes) {
   if (bytes == 0) bytes = 16;
   cudaError_t e = cudaMalloc(p, bytes);
@@ -314,11 +318,14 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
 }
 
 extern "C" int dgadv_create(const dgadv_mesh *mesh, const dgadv_params *prm, dgadv_handle **out) {
+  return guarded(nullptr, [&]() -> int {
   return create_impl(mesh, prm, std::vector<int>(), out);
+  });
 }
 
 extern "C" int dgadv_create_ensemble(const dgadv_mesh *meshes, int32_t nInst, const dgadv_params *prm,
                                      dgadv_handle **out) {
+  return guarded(nullptr, [&]() -> int {
   if (!out) return DGADV_EINVAL;
   *out = nullptr;
   if (!meshes || !prm || nInst < 1) return DGADV_EINVAL;
@@ -361,6 +368,7 @@ extern "C" int dgadv_create_ensemble(const dgadv_mesh *meshes, int32_t nInst, co
   u.markE0TbdrD = hasD ? mD.data() : nullptr;
   u.markE0TbdrN = hasN ? mN.data() : nullptr;
   return create_impl(&u, prm, instStart, out);
+  });
 }
 
 void dgadv::velocity_factors(const dgadv_handle *h, const double *u1, const double *u2, const double *vN,
@@ -393,6 +401,7 @@ void dgadv::velocity_factors(const dgadv_handle *h, const double *u1, const doub
 }
 
 extern "C" int dgadv_set_velocity(dgadv_handle *h, const double *u1, const double *u2, const double *vN) {
+  return guarded(h, [&]() -> int {
   if (!h || !u1 || !u2 || !vN) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   std::vector<double> F, Vn;
@@ -403,10 +412,12 @@ extern "C" int dgadv_set_velocity(dgadv_handle *h, const double *u1, const doubl
   h->hasVelocity = true;
   ++h->velVersion;
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_set_source_terms(dgadv_handle *h, int32_t nTerms, const int32_t *timeFn,
                                       const double *rhsTerms, const double *cDV0T) {
+  return guarded(h, [&]() -> int {
   if (!h || nTerms < 0 || nTerms > 4) return DGADV_EINVAL;
   if (nTerms > 0 && (!timeFn || !rhsTerms)) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
@@ -437,18 +448,22 @@ extern "C" int dgadv_set_source_terms(dgadv_handle *h, int32_t nTerms, const int
   if (cDV0T && (st = upload_real(h, h->cDV0T, d))) return st;
   if (!cDV0T && h->cDV0T) DG_CUDA(cudaMemset(h->cDV0T, 0, 4 * (size_t)3 * Kp * w));
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_set_state(dgadv_handle *h, const double *c) {
+  return guarded(h, [&]() -> int {
   if (!h || !c) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   DG_CUDA(cudaMemcpyAsync(h->stage_ext, c, (size_t)h->N * h->K * 8, cudaMemcpyHostToDevice, h->stream));
   DG_CUDA(ops(h).scatter_in(h, h->cn));
   DG_CUDA(cudaStreamSynchronize(h->stream));
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_sync(dgadv_handle *h) {
+  return guarded(h, [&]() -> int {
   if (!h) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   DG_CUDA(cudaStreamSynchronize(h->stream));
@@ -462,23 +477,28 @@ extern "C" int dgadv_sync(dgadv_handle *h) {
   }
   if (flag & 1) { h->err = "non-finite value in the state"; return DGADV_ENONFINITE; }
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_get_state(dgadv_handle *h, double *c) {
+  return guarded(h, [&]() -> int {
   if (!h || !c) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   DG_CUDA(ops(h).gather_out(h, h->cn));
   DG_CUDA(cudaMemcpyAsync(c, h->stage_ext, (size_t)h->N * h->K * 8, cudaMemcpyDeviceToHost, h->stream));
   return dgadv_sync(h);
+  });
 }
 
 extern "C" int dgadv_limit_state(dgadv_handle *h, double t) {
+  return guarded(h, [&]() -> int {
   if (!h) return DGADV_EINVAL;
   if (!h->lim) { h->err = "limiter is off for this handle"; return DGADV_EINVAL; }
   DG_CUDA(cudaSetDevice(h->device));
   cudaError_t e = ops(h).limit(h, t);
   if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
   return dgadv_sync(h);
+  });
 }
 
 static bool time_dependent(const dgadv_handle *h) {
@@ -500,6 +520,7 @@ static cudaError_t end_of_call(dgadv_handle *h) {
 }
 
 extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau) {
+  return guarded(h, [&]() -> int {
   if (!h || nSteps < 0 || !(tau > 0)) return DGADV_EINVAL;
   if (h->flags & DGADV_FLAG_IMPLICIT) {
     h->err = "explicit steps need a handle without DGADV_FLAG_IMPLICIT";
@@ -551,6 +572,7 @@ extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, doubl
   cudaError_t e = end_of_call(h);
   if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
   return DGADV_OK;
+  });
 }
 
 static void drop_graphs(dgadv_handle *h) {
@@ -560,6 +582,7 @@ static void drop_graphs(dgadv_handle *h) {
 }
 
 extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) {
+  return guarded(h, [&]() -> int {
   if (!h) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   DG_CUDA(cudaStreamSynchronize(h->stream));
@@ -581,15 +604,18 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
   }
   drop_graphs(h);
   return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *value) {
+  return guarded(h, [&]() -> int {
   if (!h || !value) return DGADV_EINVAL;
   if (option == DGADV_OPT_GRAPH_STEPS) *value = h->graphSteps;
   else if (option == DGADV_OPT_FLAGS) *value = h->flags;
   else if (option == DGADV_OPT_PERSIST_BLOCKS) *value = h->persistPerSM;
   else return DGADV_EINVAL;
   return DGADV_OK;
+  });
 }
 
 // Self-test of the bounded device wait: one block waits on a device flag that nothing sets,
@@ -606,6 +632,7 @@ __global__ void k_wait_selftest(const int *never, int *flag, long long limitCycl
 }
 
 extern "C" int dgadv_selftest_wait(dgadv_handle *h, double seconds) {
+  return guarded(h, [&]() -> int {
   if (!h || !(seconds > 0.0) || seconds > 2.0) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   int khz = 0;
@@ -619,9 +646,11 @@ extern "C" int dgadv_selftest_wait(dgadv_handle *h, double seconds) {
   // the handle stays usable: clear the recorded error
   DG_CUDA(cudaMemset(h->flag, 0, 16));
   return st;
+  });
 }
 
 extern "C" int dgadv_time_steps(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau, double *ms) {
+  return guarded(h, [&]() -> int {
   if (!h || !ms) return DGADV_EINVAL;
   DG_CUDA(cudaSetDevice(h->device));
   if (!h->ev0) { DG_CUDA(cudaEventCreate(&h->ev0)); DG_CUDA(cudaEventCreate(&h->ev1)); }
@@ -635,10 +664,12 @@ extern "C" int dgadv_time_steps(dgadv_handle *h, int32_t nSteps, int32_t nStep0,
   DG_CUDA(cudaEventElapsedTime(&f, h->ev0, h->ev1));
   *ms = f;
   return dgadv_sync(h);
+  });
 }
 
 extern "C" int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau,
                                      double *msPerLaunch, int32_t *launches) {
+  return guarded(h, [&]() -> int {
   if (!h || !msPerLaunch || !launches || nSteps < 1) return DGADV_EINVAL;
   if (!h->hasVelocity) { h->err = "dgadv_set_velocity was not called"; return DGADV_EINVAL; }
   if (h->flags & DGADV_FLAG_IMPLICIT) { h->err = "explicit steps need a handle without DGADV_FLAG_IMPLICIT"; return DGADV_EUNSUPPORTED; }
@@ -665,9 +696,11 @@ extern "C" int dgadv_profile_kernels(dgadv_handle *h, int32_t nSteps, int32_t nS
   if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
   if (e2 != cudaSuccess) { h->err = cudaGetErrorString(e2); return DGADV_ECUDA; }
   return dgadv_sync(h);
+  });
 }
 
 extern "C" int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count) {
+  return guarded(h, [&]() -> int {
   if (!h || !count) return DGADV_EINVAL;
   if (use_persistent(h) && ops_of(h).step_persist) { *count = 1; return DGADV_OK; }
   int perStage = 1;
@@ -675,6 +708,7 @@ extern "C" int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count) {
   else if (h->lim) perStage = h->limdot ? 3 : 2;
   *count = h->ordRK * perStage;
   return DGADV_OK;
+  });
 }
 
 extern "C" const char *dgadv_last_error(const dgadv_handle *h) { return h ? h->err.c_str() : "null handle"; }
@@ -683,7 +717,10 @@ extern "C" void dgadv_destroy(dgadv_handle *h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  output_release(h);
+  try {
+    output_release(h);   // joins the writer thread
+  } catch (...) {
+  }
   implicit_release(h);
   transport_release(h);
   for (int i = 0; i < 3; ++i)

@@ -70,6 +70,7 @@ int limit_species(dgadv_handle *h, int s, double t, bool updateMask) {
 
 extern "C" int dgadv_transport_init(dgadv_handle *h, int32_t nSpecies, const double *hDisc, const double *cH0,
                                     double maskTol, int32_t isMask) {
+  return guarded(h, [&]() -> int {
   if (!h || nSpecies < 1 || nSpecies > 64 || !hDisc || !cH0 || !(maskTol >= 0.0)) return DGADV_EINVAL;
   const PrecOps &o = ops_of(h);
   if (!o.tr_stage) { h->err = "the transport kernels are built for FP32 and FP64"; return DGADV_EUNSUPPORTED; }
@@ -120,9 +121,11 @@ extern "C" int dgadv_transport_init(dgadv_handle *h, int32_t nSpecies, const dou
   }
   DG_CUDA(cudaStreamSynchronize(h->stream));
   return dgadv_sync(h);
+  });
 }
 
 extern "C" int dgadv_transport_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau) {
+  return guarded(h, [&]() -> int {
   if (!h || nSteps < 0 || !(tau > 0.0)) return DGADV_EINVAL;
   if (int e = check(h)) return e;
   DG_CUDA(cudaSetDevice(h->device));
@@ -149,9 +152,11 @@ extern "C" int dgadv_transport_step(dgadv_handle *h, int32_t nSteps, int32_t nSt
     }
   }
   return dgadv_sync(h);
+  });
 }
 
 extern "C" int dgadv_transport_get(dgadv_handle *h, int32_t species, double *cH, double *conc, uint8_t *mask) {
+  return guarded(h, [&]() -> int {
   if (!h) return DGADV_EINVAL;
   if (int e = check(h)) return e;
   TransportState *st = h->trans;
@@ -176,4 +181,5 @@ extern "C" int dgadv_transport_get(dgadv_handle *h, int32_t species, double *cH,
     for (int k = 0; k < h->K; ++k) mask[h->permv[k]] = m[k];
   }
   return dgadv_sync(h);
+  });
 }

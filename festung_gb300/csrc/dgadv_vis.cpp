@@ -1,5 +1,6 @@
 // Solution output files (core/visualizeDataLagr.m:114-291, scalar data): text formatted in
 // parallel on the host cores, geometry text cached per mesh.
+#include "dgadv_guard.h"
 #include "dgadv_vis.h"
 
 #include <sys/stat.h>
@@ -276,6 +277,7 @@ bool VisMesh::write(const double *dataLagr, int numP, const char *varName, const
 extern "C" int dgadv_write_lagrange(int32_t numT, int32_t numV, const double *coordV, const int32_t *V0T,
                                     int32_t numP, const double *dataLagr, const char *varName,
                                     const char *fileName, int32_t tLvl, int32_t fileTypes) {
+  return dgadv::guarded(nullptr, [&]() -> int {
   if (numT <= 0 || numV <= 0 || !coordV || !V0T || !dataLagr || !varName || !fileName ||
       (numP != 1 && numP != 3 && numP != 6) || !fileTypes || (fileTypes & ~(DGADV_OUT_VTK | DGADV_OUT_TEC)))
     return DGADV_EINVAL;
@@ -288,4 +290,5 @@ extern "C" int dgadv_write_lagrange(int32_t numT, int32_t numV, const double *co
   std::string err;
   if (!mesh.init(numT, numV, xy.data(), t.data(), err)) return DGADV_EMESH;
   return mesh.write(dataLagr, numP, varName, fileName, tLvl, fileTypes, err) ? DGADV_OK : DGADV_EIO;
+  });
 }
