@@ -844,7 +844,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-stages', type=int, default=1)
     ap.add_argument('--ref-stages-per-step', type=int, default=1)
-    ap.add_argument('--ncu-case', default=None, choices=sorted(WORKLOADS) + ['adjoint'],
+    ap.add_argument('--ncu-case', default=None, choices=sorted(WORKLOADS) + ['adjoint', 'implicit', 'transport'],
                     help='profiling driver: set up the workload and run --ncu-steps steps, no timing')
     ap.add_argument('--ncu-steps', type=int, default=2)
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64', 'df32'])
@@ -856,6 +856,27 @@ def main():
                       tEnd=args.ncu_steps * 2e-5)
         c0 = np.asfortranarray(pd._cDisc)
         AD.misfit_gradient(pd, c0, pd.theta, 0.9 * c0, nSnapshots=0)
+        pd.solver.close()
+        return 0
+    if args.ncu_case == 'implicit':
+        # the implicit problem's default configuration, --ncu-steps DIRK steps
+        from festung_gb300 import advection_implicit_gpu as AI
+        pd = AI.Struct(dict(IMPLICIT_WORKLOAD, precision='fp64' if args.precision == 'df32' else args.precision))
+        pd.problemName = 'advection_implicit_gpu'
+        for f in AI.PRE:
+            pd = f(pd)
+        pd.solver.step_implicit(args.ncu_steps, 0, pd.tau, pd.ordRK, pd.krylovTol)
+        pd.solver.close()
+        return 0
+    if args.ncu_case == 'transport':
+        # the transport problem's 'rotation' configuration with 4 species, --ncu-steps steps
+        from festung_gb300 import transport_gpu as TG
+        pd = TG.Struct(dict(hmax=2 ** -6, numSteps=3124, tEnd=(3124 / 3142) * 2 * np.pi, numSpecies=4,
+                            precision='fp64' if args.precision == 'df32' else args.precision))
+        pd.problemName = 'transport_gpu'
+        for f in TG.PRE:
+            pd = f(pd)
+        pd.solver.transport_step(args.ncu_steps, 0, pd.tau)
         pd.solver.close()
         return 0
     if args.ncu_case:
