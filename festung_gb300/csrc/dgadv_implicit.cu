@@ -27,6 +27,7 @@ namespace dgadv {
 namespace {
 
 constexpr int kImplBlock = 128;
+constexpr int kElemThreads = 32;      // element kernels: one warp per block spreads a small mesh over every SM
 constexpr int kVecThreads = 256;
 constexpr int kMaxDotBlocks = 512;
 constexpr int kChunk = 8;             // vectors per multi-dot / update launch
@@ -472,7 +473,7 @@ struct Solver {
     args.K = h->K; args.Kp = h->Kp; args.nTerms = h->nTerms;
     args.F = (const T *)h->F; args.Vn = (const T *)h->Vn; args.rhs = (const T *)h->rhs;
     args.nbr = h->nbr; args.code = h->code;
-    gridK = (h->K + kImplBlock - 1) / kImplBlock;
+    gridK = (h->K + kElemThreads - 1) / kElemThreads;
     gridV = (int)std::min<size_t>((n + kVecThreads - 1) / kVecThreads, 4 * 152);
     nbD = (int)std::min<size_t>((n + kVecThreads - 1) / kVecThreads, kMaxDotBlocks);
   }
@@ -484,15 +485,15 @@ struct Solver {
     ImplArgs<T> a = args;
     const bool rhs = withRhs && h->nTerms > 0 && h->rhs;
     for (int m = 0; m < h->nTerms; ++m) a.gco[m] = time_factor_of(h->timeFn[m], t);
-    if (rhs) k_impl_op<T, P, true><<<gridK, kImplBlock, 0, h->stream>>>(a, x, y, ca, cb);
-    else k_impl_op<T, P, false><<<gridK, kImplBlock, 0, h->stream>>>(a, x, y, ca, cb);
+    if (rhs) k_impl_op<T, P, true><<<gridK, kElemThreads, 0, h->stream>>>(a, x, y, ca, cb);
+    else k_impl_op<T, P, false><<<gridK, kElemThreads, 0, h->stream>>>(a, x, y, ca, cb);
   }
   void prec(const T *r, T *z) {
-    k_impl_prec<T, P><<<gridK, kImplBlock, 0, h->stream>>>(h->K, h->Kp, (const T *)st->Pinv, r, z);
+    k_impl_prec<T, P><<<gridK, kElemThreads, 0, h->stream>>>(h->K, h->Kp, (const T *)st->Pinv, r, z);
   }
   void build_prec(double ca, double cb) {
     if (st->pinvVersion == h->velVersion && st->pinvA == ca && st->pinvB == cb) return;
-    k_impl_block<T, P><<<gridK, kImplBlock, 0, h->stream>>>(args, ca, cb, (T *)st->Pinv);
+    k_impl_block<T, P><<<gridK, kElemThreads, 0, h->stream>>>(args, ca, cb, (T *)st->Pinv);
     st->pinvA = ca; st->pinvB = cb; st->pinvVersion = h->velVersion;
   }
   // dres[off + v] = <V_v, w> for v < nv (V: nv vectors of stride n)

@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(kBlock) k_tr_stage(const Geo<T> g, const T *co
                                                      T *cHout, const uint8_t *__restrict__ mask, double omega,
                                                      double tau) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
-  const int k = blockIdx.x * kBlock + threadIdx.x;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= g.K) return;
   const Tab<T, P> &tb = tab<T, P>();
   const size_t Kp = g.Kp;
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kBlock) k_tr_convert(int K, int Kp, const T *_
                                                        T *__restrict__ out, const T *__restrict__ hQ, int toConc,
                                                        const VolWeights wq) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q;
-  const int k = blockIdx.x * kBlock + threadIdx.x;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= K) return;
   const Tab<T, P> &tb = tab<T, P>();
   T a[N], s[N];
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(kBlock) k_tr_mask(const Geo<T> g, const LimIn<
 template <typename T, int P>
 static cudaError_t tr_stage(dgadv_handle *h, const TrStageArgs &a) {
   const Geo<T> g = make_geo<T>(h);
-  k_tr_stage<T, P><<<(h->K + kBlock - 1) / kBlock, kBlock, 0, h->stream>>>(
+  k_tr_stage<T, P><<<(h->K + 31) / 32, 32, 0, h->stream>>>(
       g, (const T *)a.conc, (const T *)a.cHin, (const T *)a.cH0, (T *)a.cHout, a.mask, a.omega, a.tau);
   return cudaGetLastError();
 }
@@ -141,7 +141,7 @@ template <typename T, int P>
 static cudaError_t tr_convert(dgadv_handle *h, const void *in, void *out, const void *hQ, int toConc) {
   VolWeights wq{};
   for (int q = 0; q < Dims<P>::Q && q < 12; ++q) wq.w[q] = h->tables.vol.W[q];
-  k_tr_convert<T, P><<<(h->K + kBlock - 1) / kBlock, kBlock, 0, h->stream>>>(h->K, h->Kp, (const T *)in, (T *)out,
+  k_tr_convert<T, P><<<(h->K + 31) / 32, 32, 0, h->stream>>>(h->K, h->Kp, (const T *)in, (T *)out,
                                                                              (const T *)hQ, toConc, wq);
   return cudaGetLastError();
 }
