@@ -919,7 +919,7 @@ k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
 // Resident blocks per SM asked of k_limit_dot: five in FP32 (the register cap costs a few
 // spills at p = 3 and lifts the occupancy from four blocks); no bound for the wider types.
 template <typename T> struct LimDotBlocks { static constexpr int value = 1; };
-template <> struct LimDotBlocks<float> { static constexpr int value = 5; };
+template <> struct LimDotBlocks<float> { static constexpr int value = 6; };
 // ... and of k_limit
 template <typename T> struct LimBlocks { static constexpr int value = 1; };
 template <> struct LimBlocks<float> { static constexpr int value = 5; };
