@@ -916,16 +916,18 @@ k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
 // Time-derivative limiting and SSP update (advection/solveSubStep.m:69-83), then the Taylor
 // form of the new stage value and the scatter of its centroid quantities for the solution
 // limiter.
-// Resident blocks per SM asked of k_limit_dot: five in FP32 (the register cap costs a few
-// spills at p = 3 and lifts the occupancy from four blocks); no bound for the wider types.
-template <typename T> struct LimDotBlocks { static constexpr int value = 1; };
-template <> struct LimDotBlocks<float> { static constexpr int value = 6; };
+// Resident blocks per SM asked of k_limit_dot in FP32: six for the hierarchical limiter (80
+// registers), five for the strict one, whose larger body would spill at six; no bound for the
+// wider types.
+template <typename T, int LT> struct LimDotBlocks { static constexpr int value = 1; };
+template <> struct LimDotBlocks<float, 1> { static constexpr int value = 6; };
+template <> struct LimDotBlocks<float, 2> { static constexpr int value = 5; };
 // ... and of k_limit
 template <typename T> struct LimBlocks { static constexpr int value = 1; };
 template <> struct LimBlocks<float> { static constexpr int value = 5; };
 
 template <typename T, int P, int LT>
-__global__ void __launch_bounds__(kBlock, LimDotBlocks<T>::value)
+__global__ void __launch_bounds__(kBlock, LimDotBlocks<T, LT>::value)
 k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
             const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
