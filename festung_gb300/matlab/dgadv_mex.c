@@ -156,6 +156,25 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
                                 (int32_t)mxGetScalar(prhs[5]), &kr, &it, &rr), h);
     plhs[0] = mxCreateDoubleScalar((double)it);
     if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(rr);
+  } else if (!strcmp(cmd, "transport_init")) {
+    /* dgadv_mex('transport_init', h, hDisc, cH0, maskTol, isMask): cH0 is K x N x nSpecies */
+    const mwSize nd = mxGetNumberOfDimensions(prhs[3]);
+    const int32_t ns = nd > 2 ? (int32_t)mxGetDimensions(prhs[3])[2] : 1;
+    check(dgadv_transport_init(h, ns, mxGetPr(prhs[2]), mxGetPr(prhs[3]), mxGetScalar(prhs[4]),
+                               (int32_t)mxGetScalar(prhs[5])), h);
+  } else if (!strcmp(cmd, "transport_step")) {
+    check(dgadv_transport_step(h, (int32_t)mxGetScalar(prhs[2]), (int32_t)mxGetScalar(prhs[3]),
+                               mxGetScalar(prhs[4])), h);
+  } else if (!strcmp(cmd, "transport_get")) {
+    /* [cH, c, mask] = dgadv_mex('transport_get', h, species (1-based), K, N) */
+    const mwSize K = (mwSize)mxGetScalar(prhs[3]), N = (mwSize)mxGetScalar(prhs[4]);
+    plhs[0] = mxCreateDoubleMatrix(K, N, mxREAL);
+    mxArray *c = mxCreateDoubleMatrix(K, N, mxREAL);
+    mxArray *m = mxCreateNumericMatrix(K, 1, mxUINT8_CLASS, mxREAL);
+    check(dgadv_transport_get(h, (int32_t)mxGetScalar(prhs[2]) - 1, mxGetPr(plhs[0]), mxGetPr(c),
+                              (uint8_t *)mxGetData(m)), h);
+    if (nlhs > 1) plhs[1] = c; else mxDestroyArray(c);
+    if (nlhs > 2) plhs[2] = m; else mxDestroyArray(m);
   } else if (!strcmp(cmd, "output")) {
     /* dgadv_mex('output', h, varName, fileName, tLvl, fileTypes): fileTypes 1 vtk, 2 tec, 3 both */
     char var[256], file[4096];
