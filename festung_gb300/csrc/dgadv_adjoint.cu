@@ -70,16 +70,25 @@ size_t backward_start(const std::vector<int> &o) {
   return f;
 }
 
-// dJ/dtheta_m partial sums: block b of mode m sums aF F_m + aV Vn_m over its elements.
-__global__ void k_theta_partial(int K, int Kp, int nF, int nV, const double *__restrict__ aF,
+// One entry of aF / aV: FP64, or (pairs) the float pair hi + lo of the FP32 stage kernel.
+__device__ __forceinline__ double sens_entry(const double *a, size_t i, int pairs) {
+  if (!pairs) return a[i];
+  const float2 q = reinterpret_cast<const float2 *>(a)[i];
+  return (double)q.x + (double)q.y;
+}
+
+// dJ/dtheta_m partial sums in FP64: block b of mode m sums aF F_m + aV Vn_m over its elements.
+__global__ void k_theta_partial(int K, int Kp, int nF, int nV, int pairs, const double *__restrict__ aF,
                                 const double *__restrict__ aV, const double *__restrict__ modeF,
                                 const double *__restrict__ modeV, double *__restrict__ part) {
   __shared__ double red[256];
   const int m = blockIdx.y;
   double s = 0.0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
-    for (int c = 0; c < nF; ++c) s += aF[(size_t)c * Kp + k] * modeF[((size_t)m * nF + c) * Kp + k];
-    for (int c = 0; c < nV; ++c) s += aV[(size_t)c * Kp + k] * modeV[((size_t)m * nV + c) * Kp + k];
+    for (int c = 0; c < nF; ++c)
+      s += sens_entry(aF, (size_t)c * Kp + k, pairs) * modeF[((size_t)m * nF + c) * Kp + k];
+    for (int c = 0; c < nV; ++c)
+      s += sens_entry(aV, (size_t)c * Kp + k, pairs) * modeV[((size_t)m * nV + c) * Kp + k];
   }
   red[threadIdx.x] = s;
   __syncthreads();
@@ -122,13 +131,17 @@ int rk_stages(const dgadv_handle *h, double omega[3]) {
   return 1;
 }
 
-// One forward step from cn (the cursor's state); with stage storage the step's stage states are
-// written straight into its stage slots.
-int forward_step(dgadv_handle *h, Cursor &w) {
+// One forward step from c^step, read from `src` (cn or a slot), written to `dst` (cn or a slot);
+// with stage storage the step's stage states are written straight into its stage slots.  With
+// nStages < S only the first nStages stages run: their outputs (cA, cB) are what the reverse
+// stages of the unlimited scheme read, and c^(step+1) is neither needed nor written.
+int forward_step(dgadv_handle *h, Cursor &w, const void *src, void *dst, int nStages) {
   const PrecOps &o = ops_of(h);
   double omega[3];
   const int S = rk_stages(h, omega);
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
+  const bool partial = nStages < S;
+  if (partial && nStages <= 0) return DGADV_OK;   // one stage: its input c^step is all it needs
   void *cA = h->cA, *cB = h->cB;
   if (h->adjStages && S > 1) {
     char *st = (char *)h->adjStages + (size_t)w.step * (S - 1) * bytes;
@@ -144,21 +157,31 @@ int forward_step(dgadv_handle *h, Cursor &w) {
                                       : (char *)h->adjScrCdot + (size_t)s * bytes;
     }
   }
+  h->stepSrc = src == h->cn ? nullptr : src;
+  h->stepDst = dst == h->cn ? nullptr : dst;
+  h->stepStages = partial ? nStages : 0;
   const cudaError_t e = o.step(h, w.step * h->recTau, h->recTau);
   h->cA = cA;
   h->cB = cB;
+  h->stepSrc = nullptr;
+  h->stepDst = nullptr;
+  h->stepStages = 0;
   for (int s = 0; s < 3; ++s) h->recY[s] = h->recCdot[s] = nullptr;
   DG_CUDA(e);
+  if (partial) return DGADV_OK;
   ++w.step;
-  w.cnStep = w.step;
-  w.slot = -1;
+  if (dst == h->cn) {
+    w.cnStep = w.step;
+    w.slot = -1;
+  }
   return DGADV_OK;
 }
 
-// Executes schedule actions [from, to) on the handle's stream.  Restores are lazy: a slot is
-// copied into cn only when a forward step has to start from it.  With stage storage (every
-// step's stage states kept by the recorded run) a reversed step reads its stages from there
-// and recomputes nothing.
+// Executes schedule actions [from, to) on the handle's stream.  Restores cost nothing: a step
+// reads c^i from the slot that holds it, and an advance whose next action stores its result
+// writes that result straight into the slot.  With stage storage (every step's stage states kept
+// by the recorded run) a reversed step reads its stages from there and recomputes nothing;
+// without it, the unlimited scheme recomputes only the stages whose inputs it needs.
 int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
   const PrecOps &o = ops_of(h);
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
@@ -169,11 +192,12 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
   char *slots = (char *)h->adjSlots;
   char *stages = (char *)h->adjStages;
   auto stage_ptr = [&](int step, int s) { return stages + ((size_t)step * (S - 1) + (s - 1)) * bytes; };
-  auto materialize = [&]() -> int {
-    if (w.cnStep == w.step) return DGADV_OK;
-    if (w.slot < 0) { h->err = "checkpoint schedule lost its state"; return DGADV_EINVAL; }
-    DG_CUDA(o.copy(h, h->cn, slots + (size_t)w.slot * bytes, bytes));
-    w.cnStep = w.step;
+  auto slot_ptr = [&](int slot) { return slots + (size_t)slot * bytes; };
+  // where c^(w.step) can be read
+  auto current = [&](const void *&src) -> int {
+    if (w.cnStep == w.step) src = h->cn;
+    else if (w.slot >= 0 && h->slotStep[w.slot] == w.step) src = slot_ptr(w.slot);
+    else { h->err = "checkpoint schedule lost its state"; return DGADV_EINVAL; }
     return DGADV_OK;
   };
   int st;
@@ -183,27 +207,48 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
       w.step = h->slotStep[arg];
       w.slot = arg;
     } else if (op == A_ADVANCE) {
-      if ((st = materialize())) return st;
-      for (int i = 0; i < arg; ++i)
-        if ((st = forward_step(h, w))) return st;
+      const bool storeNext = a + 2 < to && h->schedule[a + 2] == A_STORE;
+      for (int i = 0; i < arg; ++i) {
+        const void *src;
+        if ((st = current(src))) return st;
+        void *dst = h->cn;
+        const int target = storeNext && i == arg - 1 ? h->schedule[a + 3] : -1;
+        if (target >= 0 && slot_ptr(target) != src) dst = slot_ptr(target);
+        if ((st = forward_step(h, w, src, dst, S))) return st;
+        if (dst != h->cn) {   // the result already sits in the slot the next action stores to
+          h->slotStep[target] = w.step;
+          w.slot = target;
+        }
+      }
     } else if (op == A_STORE) {
-      if ((st = materialize())) return st;
-      DG_CUDA(o.copy(h, slots + (size_t)arg * bytes, h->cn, bytes));
-      h->slotStep[arg] = w.step;
-      w.slot = arg;
+      if (!(w.slot == arg && h->slotStep[arg] == w.step)) {
+        const void *src;
+        if ((st = current(src))) return st;
+        DG_CUDA(o.copy(h, slot_ptr(arg), src, bytes));
+        h->slotStep[arg] = w.step;
+        w.slot = arg;
+      }
     } else {   // A_BACKWARD: the stage states of step arg (stored or recomputed), then reversed
       if (w.step != arg) { h->err = "checkpoint schedule out of order"; return DGADV_EINVAL; }
       const void *stageIn[3];
       if (stages) {
         if (w.slot < 0) { h->err = "checkpoint schedule lost its state"; return DGADV_EINVAL; }
-        stageIn[0] = slots + (size_t)w.slot * bytes;
+        stageIn[0] = slot_ptr(w.slot);
         for (int s = 1; s < S; ++s) stageIn[s] = stage_ptr(arg, s);
       } else {
-        if ((st = materialize())) return st;
-        const void *c0 = h->cx;
-        if (w.slot >= 0) c0 = slots + (size_t)w.slot * bytes;   // c^i is that slot
-        else DG_CUDA(o.copy(h, h->cx, h->cn, bytes));
-        if ((st = forward_step(h, w))) return st;
+        const void *c0;
+        if ((st = current(c0))) return st;
+        if (h->lim) {
+          // the limiter adjoint reads every stage's limiter inputs, so the whole step runs and
+          // its result goes to cn: c^arg read from cn moves to cx first
+          if (c0 == h->cn) {
+            DG_CUDA(o.copy(h, h->cx, h->cn, bytes));
+            c0 = h->cx;
+          }
+          if ((st = forward_step(h, w, c0, h->cn, S))) return st;
+        } else if ((st = forward_step(h, w, c0, h->cn, S - 1))) {
+          return st;
+        }
         stageIn[0] = c0;
         stageIn[1] = h->cA;
         stageIn[2] = h->cB;
@@ -393,10 +438,16 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
   Cursor w;
   w.slot = 0;
   if ((st = run_actions(h, 0, h->schedBackward, w))) return st;
+  // on to c^nSteps in cn; the state reached may sit in a slot only
+  if (w.cnStep != w.step && (w.slot < 0 || h->slotStep[w.slot] != w.step)) {
+    h->err = "checkpoint schedule lost its state";
+    return DGADV_EINVAL;
+  }
+  while (w.step < nSteps) {
+    const void *src = w.cnStep == w.step ? h->cn : (const void *)((char *)h->adjSlots + (size_t)w.slot * bytes);
+    if ((st = forward_step(h, w, src, h->cn, S))) return st;
+  }
   if (w.cnStep != w.step) DG_CUDA(o.copy(h, h->cn, (char *)h->adjSlots + (size_t)w.slot * bytes, bytes));
-  w.cnStep = w.step;
-  while (w.step < nSteps)
-    if ((st = forward_step(h, w))) return st;
   h->recorded = true;
   return DGADV_OK;
   });
@@ -483,7 +534,7 @@ extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc
     const int gx = std::min(kThetaBlocks, (h->K + 255) / 256);
     for (int m0 = 0; m0 < h->nModes; m0 += 1024) {
       const int nm = std::min(1024, h->nModes - m0);
-      k_theta_partial<<<dim3(gx, nm), 256, 0, h->stream>>>(h->K, h->Kp, nF, nV, h->aF, h->aV,
+      k_theta_partial<<<dim3(gx, nm), 256, 0, h->stream>>>(h->K, h->Kp, nF, nV, o.realBytes == 4, h->aF, h->aV,
                                                           h->modeF + (size_t)m0 * nF * h->Kp,
                                                           h->modeV + (size_t)m0 * nV * h->Kp, h->thetaPart);
       DG_CUDA(cudaGetLastError());

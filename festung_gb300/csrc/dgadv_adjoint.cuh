@@ -12,9 +12,10 @@
 //
 // The velocity enters linearly through F (volume factors at the quadrature points) and Vn
 // (normal velocities at the edge points), with the upwind choice frozen at the base velocity.
-// Each stage adds dJ/dF and dJ/dVn per element into FP64 arrays (aF: 2Q x Kp, aV: 3R x Kp);
-// the gradient of a velocity parameter theta_m is then sum aF F_m + aV Vn_m over elements, with
-// F_m, Vn_m the factors of velocity mode m.
+// Each stage adds dJ/dF and dJ/dVn per element into 8-byte entries (aF: 2Q x Kp, aV: 3R x Kp;
+// FP64, or float pairs on the FP32 path, see SensAcc); the gradient of a velocity parameter
+// theta_m is then sum aF F_m + aV Vn_m over elements, with F_m, Vn_m the factors of velocity
+// mode m.
 #pragma once
 #include "dgadv_device.cuh"
 
@@ -24,6 +25,34 @@ struct AdjScalars {
   double omega, tau;
   int init;   // accn starts at zero (first reversed stage of a step)
   int last;   // stage 0: its input is c^n itself, so dJ/dc^(0) joins accn
+};
+
+// One entry of the per-element velocity sensitivities aF / aV (8 bytes each).  The FP64 path adds
+// in FP64.  The FP32 path keeps the entry as an unevaluated pair hi + lo of floats in the same 8
+// bytes and adds with two_sum + fast_two_sum (Knuth; Dekker 1971), about 48 bits: GB300 issues
+// FP64 arithmetic at 1/64 of the FP32 rate, and the 2Q + 3R FP64 conversions and adds per element
+// were the busiest pipe of the FP32 stage.  k_theta_partial reads the pair as (double)hi + lo.
+template <typename T>
+struct SensAcc {
+  double v;
+  __device__ __forceinline__ void load(const double *p) { v = *p; }
+  __device__ __forceinline__ void add(T x) { v += double(x); }
+  __device__ __forceinline__ void store(double *p) const { *p = v; }
+};
+template <>
+struct SensAcc<float> {
+  float hi, lo;
+  __device__ __forceinline__ void load(const double *p) {
+    const float2 q = *reinterpret_cast<const float2 *>(p);
+    hi = q.x;
+    lo = q.y;
+  }
+  __device__ __forceinline__ void add(float x) {
+    float s, e;
+    df::two_sum(hi, x, s, e);
+    df::fast_two_sum(s, e + lo, hi, lo);
+  }
+  __device__ __forceinline__ void store(double *p) const { *reinterpret_cast<float2 *>(p) = make_float2(hi, lo); }
 };
 
 template <typename T, int P>
@@ -57,7 +86,7 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__rest
   pdl_wait();
   // every load of the stage's data up front: the kernel is latency-bound otherwise
   T mu[N], c[N], cn[3][N], mu2[3][N];
-  double sF[2 * Q], sV[3 * R];
+  SensAcc<T> sF[2 * Q], sV[3 * R];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
     mu[i] = muIn[(size_t)i * Kp + k];
@@ -71,9 +100,9 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__rest
       mu2[n][j] = nb[n] >= 0 ? (mpIn ? mpIn[(size_t)j * Kp + nb[n]] : coef * muIn[(size_t)j * Kp + nb[n]]) : T(0);
     }
 #pragma unroll
-  for (int i = 0; i < 2 * Q; ++i) sF[i] = aF[(size_t)i * Kp + k];
+  for (int i = 0; i < 2 * Q; ++i) sF[i].load(aF + (size_t)i * Kp + k);
 #pragma unroll
-  for (int i = 0; i < 3 * R; ++i) sV[i] = aV[(size_t)i * Kp + k];
+  for (int i = 0; i < 3 * R; ++i) sV[i].load(aV + (size_t)i * Kp + k);
   T mp[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) mp[i] = mpIn ? mpIn[(size_t)i * Kp + k] : coef * mu[i];   // dJ/dcDot
@@ -91,8 +120,8 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__rest
       s2a.fma(tb.Hg2[q][j], mp[j]);
     }
     const T cq = cqa.get(), s1 = s1a.get(), s2 = s2a.get();
-    sF[q] += double(s1 * cq);
-    sF[Q + q] += double(s2 * cq);
+    sF[q].add(s1 * cq);
+    sF[Q + q].add(s2 * cq);
     const T wq = s1 * F[q] + s2 * F[Q + q];
 #pragma unroll
     for (int j = 0; j < N; ++j) grad[j].fma(tb.phiQ[q][j], wq);
@@ -123,7 +152,7 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__rest
         for (int j = 0; j < N; ++j) tr.fma(tb.thetaPhi[n][nk[n]][r][j], cn[n][j]);
         sens = -(e * tr.get());
       }
-      sV[n * R + r] += double(sens);
+      sV[n * R + r].add(sens);
     }
   }
   // upwind flux of the neighbours that take this element's trace (their v < 0 on the shared edge)
@@ -153,9 +182,9 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__rest
     accn[(size_t)i * Kp + k] = acc;
   }
 #pragma unroll
-  for (int i = 0; i < 2 * Q; ++i) aF[(size_t)i * Kp + k] = sF[i];
+  for (int i = 0; i < 2 * Q; ++i) sF[i].store(aF + (size_t)i * Kp + k);
 #pragma unroll
-  for (int i = 0; i < 3 * R; ++i) aV[(size_t)i * Kp + k] = sV[i];
+  for (int i = 0; i < 3 * R; ++i) sV[i].store(aV + (size_t)i * Kp + k);
 }
 
 // ---------------------------------------------------------------------------------------------

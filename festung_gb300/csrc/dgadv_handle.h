@@ -41,6 +41,11 @@ struct dgadv_handle {
   int *instOf = nullptr;               // ensembles: instance of each block of kBlock elements
   std::vector<int> instStart;          // first element of each instance (caller order), + K
   void *cn = nullptr, *cA = nullptr, *cB = nullptr, *tbuf = nullptr;
+  // one call of the staged step (the adjoint's recomputation): c^n read from stepSrc and c^(n+1)
+  // written to stepDst instead of cn, and only the first stepStages stages run (0: all)
+  const void *stepSrc = nullptr;
+  void *stepDst = nullptr;
+  int stepStages = 0;
   void *cR = nullptr, *cnL = nullptr, *cLx = nullptr;   // fused path: raw step output, limited c^n / c^(s-1)
   void *vkeys = nullptr;               // 3 passes x nc x 2 x Vp vertex min / max keys
   unsigned long long *gmm = nullptr;   // 3 passes x kSlotCopies x 2 x nc encoded global extremes

@@ -210,11 +210,17 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
   const int gridK = (h->K + kBlock - 1) / kBlock;
   double omega[3], cst[3];
   const int S = rk_table(h->ordRK, omega, cst);
-  T *cn = (T *)h->cn, *cA = (T *)h->cA, *cB = (T *)h->cB, *tb = (T *)h->tbuf;
+  T *cA = (T *)h->cA, *cB = (T *)h->cB, *tb = (T *)h->tbuf;
+  // c^n and c^(n+1): cn, unless the caller redirects them (stepSrc / stepDst)
+  const T *cn = h->stepSrc ? (const T *)h->stepSrc : (const T *)h->cn;
+  T *dst = h->stepDst ? (T *)h->stepDst : (T *)h->cn;
+  const int nRun = (h->stepStages > 0 && h->stepStages < S) ? h->stepStages : S;
   const bool rhs = h->nTerms > 0 && h->rhs;
-  for (int s = 0; s < S; ++s) {
-    T *in = (s == 0) ? cn : (s == 1 ? cA : cB);
-    T *out = (s == S - 1) ? (S == 1 ? cA : cn) : (s == 0 ? cA : cB);
+  for (int s = 0; s < nRun; ++s) {
+    const T *in = (s == 0) ? cn : (s == 1 ? cA : cB);
+    // the last stage may write c^(n+1) over c^n (it reads c^n of its own element only), but not
+    // over its input, whose neighbour values it reads: with one stage it goes through cA
+    T *out = (s == S - 1) ? ((S == 1 && (const T *)dst == cn) ? cA : dst) : (s == 0 ? cA : cB);
     StageScalars sc{};
     sc.omega = omega[s]; sc.tau = tau; sc.flag = h->flag;
     const double ts = t0 + cst[s] * tau;
@@ -280,7 +286,7 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
       launch_k(h, k_limit<T, P, 1>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
     prof_mark(h, -1);
   }
-  if (S == 1) return copy_state(h, cn, cA, (size_t)h->N * h->Kp * sizeof(T));
+  if (S == 1 && nRun == 1 && (const T *)dst == cn) return copy_state(h, dst, cA, (size_t)h->N * h->Kp * sizeof(T));
   return cudaGetLastError();
 }
 
