@@ -187,6 +187,192 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__rest
   for (int i = 0; i < 3 * R; ++i) sV[i].store(aV + (size_t)i * Kp + k);
 }
 
+// The same stage with the work of an element split over four warps by role: warp n < 3 takes
+// edge n (the outflow terms of the element's own edge n and the terms of the neighbour across it)
+// and warp 3 the volume points, for the CTA's 32 elements; the partial gradients meet in shared
+// memory.  Each warp reads its tables at one entry at a time (the role is fixed per warp, the
+// edge index a template argument), so the table operands stay constant-bank broadcasts.  With one
+// thread per element a 32768-triangle mesh gives under two warps per scheduler and the stage
+// waits on its own instruction chain; the split gives four times the warps and a quarter of the
+// chain.  Sums in a fixed order: results are deterministic.
+constexpr int kAdjElems = kBlock / 4;   // elements per CTA of k_adj_stage_split
+
+template <typename T, int P>
+struct AdjSplitIn {
+  const T *muIn, *mpIn, *cs;
+  double *aF, *aV;
+  T coef;
+  int k, e, Kp;
+};
+
+template <typename T, int P, int n>
+__device__ __forceinline__ void adj_edge_role(const Geo<T> &g, const AdjSplitIn<T, P> &x, Acc<T> *grad) {
+  constexpr int N = Dims<P>::N, R = Dims<P>::R;
+  const Tab<T, P> &tb = tab<T, P>();
+  const int e = x.e, Kp = x.Kp;
+  const int code = g.code[e];
+  const int nb = g.nbr[(size_t)n * Kp + e];
+  const int nk = (code >> (2 * n)) & 3;   // the neighbour's local index of the shared edge
+  const bool outOk = (code >> (6 + n)) & 1;
+  T V[R], V2[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    V[r] = g.Vn[(size_t)(n * R + r) * Kp + e];
+    V2[r] = nb >= 0 ? g.Vn[(size_t)(nk * R + r) * Kp + nb] : T(0);
+  }
+  pdl_wait();
+  T c[N], mp[N], cn[N], mu2[N];
+  SensAcc<T> sV[R];
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    c[j] = x.cs[(size_t)j * Kp + e];
+    mp[j] = x.mpIn ? x.mpIn[(size_t)j * Kp + e] : x.coef * x.muIn[(size_t)j * Kp + e];
+    cn[j] = nb >= 0 ? x.cs[(size_t)j * Kp + nb] : T(0);
+    mu2[j] = nb >= 0 ? (x.mpIn ? x.mpIn[(size_t)j * Kp + nb] : x.coef * x.muIn[(size_t)j * Kp + nb]) : T(0);
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) sV[r].load(x.aV + (size_t)(n * R + r) * Kp + e);
+  // upwind flux of the element's own edge n
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const T v = V[r];
+    Acc<T> eta(T(0));
+#pragma unroll
+    for (int j = 0; j < N; ++j) eta.fma(tb.Hphi[n][r][j], mp[j]);
+    const T et = eta.get();
+    T sens = T(0);
+    if (v > T(0) && outOk) {
+      Acc<T> tr(T(0));
+#pragma unroll
+      for (int j = 0; j < N; ++j) tr.fma(tb.phi1D[n][r][j], c[j]);
+      sens = -(et * tr.get());
+      const T ev = et * v;
+#pragma unroll
+      for (int j = 0; j < N; ++j) grad[j].fms(tb.phi1D[n][r][j], ev);
+    } else if (v < T(0) && nb >= 0) {
+      Acc<T> tr(T(0));
+#pragma unroll
+      for (int j = 0; j < N; ++j) tr.fma(tb.thetaPhi[n][nk][r][j], cn[j]);
+      sens = -(et * tr.get());
+    }
+    sV[r].add(sens);
+  }
+  // upwind flux of the neighbour across edge n where it takes this element's trace (v < 0 there)
+  if (nb >= 0) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const T v2 = V2[r];
+      if (v2 < T(0)) {
+        Acc<T> eta(T(0));
+#pragma unroll
+        for (int j = 0; j < N; ++j) eta.fma(tb.Hphi[nk][r][j], mu2[j]);
+        const T ev = eta.get() * v2;
+#pragma unroll
+        for (int j = 0; j < N; ++j) grad[j].fms(tb.thetaPhi[nk][n][r][j], ev);
+      }
+    }
+  }
+  if (x.k >= 0) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) sV[r].store(x.aV + (size_t)(n * R + r) * Kp + x.k);
+  }
+}
+
+template <typename T, int P>
+__device__ __forceinline__ void adj_volume_role(const Geo<T> &g, const AdjSplitIn<T, P> &x, Acc<T> *grad) {
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q;
+  const Tab<T, P> &tb = tab<T, P>();
+  const int e = x.e, Kp = x.Kp;
+  T F[2 * Q];
+#pragma unroll
+  for (int i = 0; i < 2 * Q; ++i) F[i] = g.F[(size_t)i * Kp + e];
+  pdl_wait();
+  T c[N], mp[N];
+  SensAcc<T> sF[2 * Q];
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    c[j] = x.cs[(size_t)j * Kp + e];
+    mp[j] = x.mpIn ? x.mpIn[(size_t)j * Kp + e] : x.coef * x.muIn[(size_t)j * Kp + e];
+  }
+#pragma unroll
+  for (int i = 0; i < 2 * Q; ++i) sF[i].load(x.aF + (size_t)i * Kp + e);
+  // volume term: d/dc of sum_i nu_i sum_q (g1 F1 + g2 F2)_qi c_q, nu = hatM^-1 mp
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    Acc<T> cqa(T(0)), s1a(T(0)), s2a(T(0));
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      cqa.fma(tb.phiQ[q][j], c[j]);
+      s1a.fma(tb.Hg1[q][j], mp[j]);
+      s2a.fma(tb.Hg2[q][j], mp[j]);
+    }
+    const T cq = cqa.get(), s1 = s1a.get(), s2 = s2a.get();
+    sF[q].add(s1 * cq);
+    sF[Q + q].add(s2 * cq);
+    const T wq = s1 * F[q] + s2 * F[Q + q];
+#pragma unroll
+    for (int j = 0; j < N; ++j) grad[j].fma(tb.phiQ[q][j], wq);
+  }
+  if (x.k >= 0) {
+#pragma unroll
+    for (int i = 0; i < 2 * Q; ++i) sF[i].store(x.aF + (size_t)i * Kp + x.k);
+  }
+}
+
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_adj_stage_split(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__restrict__ muOut,
+                  T *__restrict__ accn, double *__restrict__ aF, double *__restrict__ aV, const AdjScalars a) {
+  constexpr int N = Dims<P>::N;
+  constexpr int NL = (N + 3) / 4;   // coefficients each role stores, at most
+  __shared__ T part[4][N][kAdjElems];
+  pdl_trigger();
+  const int role = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int k = blockIdx.x * kAdjElems + lane;
+  const bool active = k < g.K;
+  AdjSplitIn<T, P> x;
+  x.muIn = muIn; x.mpIn = mpIn; x.cs = cs; x.aF = aF; x.aV = aV;
+  x.coef = T((1.0 - a.omega) * a.tau);
+  x.e = active ? k : 0;   // lanes past the end read element 0 and store nothing
+  x.k = active ? k : -1;
+  x.Kp = g.Kp;
+  Acc<T> grad[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) grad[i] = Acc<T>(T(0));
+  switch (role) {   // uniform per warp
+    case 0: adj_edge_role<T, P, 0>(g, x, grad); break;
+    case 1: adj_edge_role<T, P, 1>(g, x, grad); break;
+    case 2: adj_edge_role<T, P, 2>(g, x, grad); break;
+    default: adj_volume_role<T, P>(g, x, grad); break;
+  }
+  // this role's coefficients of the update, read while the partials meet
+  const T w = T(a.omega);
+  T muL[NL], acL[NL];
+#pragma unroll
+  for (int t = 0; t < NL; ++t) {
+    const int i = role + 4 * t;
+    muL[t] = i < N ? muIn[(size_t)i * x.Kp + x.e] : T(0);
+    acL[t] = (i < N && !a.init) ? accn[(size_t)i * x.Kp + x.e] : T(0);
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) part[role][i][lane] = grad[i].get();
+  __syncthreads();
+  if (!active) return;
+  // reverse SSP update and the stores: role r stores coefficients r, r + 4, ...
+#pragma unroll
+  for (int t = 0; t < NL; ++t) {
+    const int i = role + 4 * t;
+    if (i < N) {
+      const T gi = ((part[3][i][lane] + part[0][i][lane]) + part[1][i][lane]) + part[2][i][lane];
+      const T mo = (T(1) - w) * muL[t] + gi;
+      if (muOut) muOut[(size_t)i * x.Kp + k] = mo;
+      T acc = a.init ? w * muL[t] : acL[t] + w * muL[t];
+      if (a.last) acc = acc + mo;
+      accn[(size_t)i * x.Kp + k] = acc;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Adjoint of the linear limiter (core/computeVertexBasedLimiter.m:78-106 in the geometry-free form
 // of lin_alpha).  With its discrete choices frozen the limiter is rational in its input x:
@@ -383,11 +569,19 @@ static cudaError_t launch_vjp_scatter(dgadv_handle *h, const void *x, long long 
 template <typename T, int P>
 static cudaError_t launch_adj_stage(dgadv_handle *h, const AdjStageArgs &s) {
   const Geo<T> g = make_geo<T>(h);
-  const int grid = (h->K + kBlock - 1) / kBlock;
   AdjScalars a;
   a.omega = s.omega; a.tau = s.tau; a.init = s.init; a.last = s.last;
-  launch_k(h, k_adj_stage<T, P>, grid, (size_t)0, g, (const T *)s.muIn, (const T *)s.mpIn, (const T *)s.cs,
-           (T *)s.muOut, (T *)s.accn, h->aF, h->aV, a);
+  if (std::is_same<T, float>::value) {
+    // FP32: the warp-role split (the FP64 stage is bound by the FP64 rate, where one thread per
+    // element issues fewer operations)
+    const int grid = (h->K + kAdjElems - 1) / kAdjElems;
+    launch_k(h, k_adj_stage_split<T, P>, grid, (size_t)0, g, (const T *)s.muIn, (const T *)s.mpIn,
+             (const T *)s.cs, (T *)s.muOut, (T *)s.accn, h->aF, h->aV, a);
+  } else {
+    const int grid = (h->K + kBlock - 1) / kBlock;
+    launch_k(h, k_adj_stage<T, P>, grid, (size_t)0, g, (const T *)s.muIn, (const T *)s.mpIn, (const T *)s.cs,
+             (T *)s.muOut, (T *)s.accn, h->aF, h->aV, a);
+  }
   return cudaGetLastError();
 }
 
