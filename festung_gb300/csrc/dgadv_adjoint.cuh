@@ -189,14 +189,13 @@ k_adj_stage(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__rest
 
 // The same stage with the work of an element split over four warps by role: warp n < 3 takes
 // edge n (the outflow terms of the element's own edge n and the terms of the neighbour across it)
-// and warp 3 the volume points, for the CTA's 32 elements; the partial gradients meet in shared
-// memory.  Each warp reads its tables at one entry at a time (the role is fixed per warp, the
-// edge index a template argument), so the table operands stay constant-bank broadcasts.  With one
-// thread per element a 32768-triangle mesh gives under two warps per scheduler and the stage
-// waits on its own instruction chain; the split gives four times the warps and a quarter of the
-// chain.  Sums in a fixed order: results are deterministic.
-constexpr int kAdjElems = kBlock / 4;   // elements per CTA of k_adj_stage_split
-
+// and warp 3 the volume points; the partial gradients meet in shared memory.  Each warp reads its
+// tables at one entry at a time (the role is fixed per warp, the edge index a template argument),
+// so the table operands stay constant-bank broadcasts.  With one thread per element a
+// 32768-triangle mesh gives under two warps per scheduler and the stage waits on its own
+// instruction chain; the split gives four times the warps and a quarter of the chain.  A CTA
+// covers 32 W elements with W warps per role (DGADV_OPT_ADJ_WARPS).  Sums in a fixed order:
+// results are deterministic and do not depend on W.
 template <typename T, int P>
 struct AdjSplitIn {
   const T *muIn, *mpIn, *cs;
@@ -319,16 +318,17 @@ __device__ __forceinline__ void adj_volume_role(const Geo<T> &g, const AdjSplitI
   }
 }
 
-template <typename T, int P>
-__global__ void __launch_bounds__(kBlock)
+template <typename T, int P, int W>
+__global__ void __launch_bounds__(128 * W)
 k_adj_stage_split(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__restrict__ muOut,
                   T *__restrict__ accn, double *__restrict__ aF, double *__restrict__ aV, const AdjScalars a) {
   constexpr int N = Dims<P>::N;
   constexpr int NL = (N + 3) / 4;   // coefficients each role stores, at most
-  __shared__ T part[4][N][kAdjElems];
+  __shared__ T part[4][N][32 * W];
   pdl_trigger();
-  const int role = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int k = blockIdx.x * kAdjElems + lane;
+  const int warp = threadIdx.x / 32, role = warp / W;
+  const int lane = (warp % W) * 32 + threadIdx.x % 32;   // element of the CTA
+  const int k = blockIdx.x * (32 * W) + lane;
   const bool active = k < g.K;
   AdjSplitIn<T, P> x;
   x.muIn = muIn; x.mpIn = mpIn; x.cs = cs; x.aF = aF; x.aV = aV;
@@ -574,9 +574,10 @@ static cudaError_t launch_adj_stage(dgadv_handle *h, const AdjStageArgs &s) {
   if (std::is_same<T, float>::value) {
     // FP32: the warp-role split (the FP64 stage is bound by the FP64 rate, where one thread per
     // element issues fewer operations)
-    const int grid = (h->K + kAdjElems - 1) / kAdjElems;
-    launch_k(h, k_adj_stage_split<T, P>, grid, (size_t)0, g, (const T *)s.muIn, (const T *)s.mpIn,
-             (const T *)s.cs, (T *)s.muOut, (T *)s.accn, h->aF, h->aV, a);
+    const int W = h->adjWarps, grid = (h->K + 32 * W - 1) / (32 * W);
+    auto kern = W == 4 ? k_adj_stage_split<T, P, 4> : (W == 2 ? k_adj_stage_split<T, P, 2> : k_adj_stage_split<T, P, 1>);
+    launch_kb(h, kern, grid, 128 * W, (size_t)0, g, (const T *)s.muIn, (const T *)s.mpIn, (const T *)s.cs,
+              (T *)s.muOut, (T *)s.accn, h->aF, h->aV, a);
   } else {
     const int grid = (h->K + kBlock - 1) / kBlock;
     launch_k(h, k_adj_stage<T, P>, grid, (size_t)0, g, (const T *)s.muIn, (const T *)s.mpIn, (const T *)s.cs,

@@ -145,12 +145,13 @@ static void prof_mark(dgadv_handle *h, int kind) {
   h->profKinds.push_back(kind);
 }
 
-// Kernel launch on the handle's stream, with programmatic dependent launch unless disabled.
+// Kernel launch on the handle's stream, with programmatic dependent launch unless disabled;
+// `block` threads per CTA (launch_k: kBlock).
 template <typename... KArgs, typename... Args>
-static void launch_k(const dgadv_handle *h, void (*kern)(KArgs...), int grid, size_t smem, Args... args) {
+static void launch_kb(const dgadv_handle *h, void (*kern)(KArgs...), int grid, int block, size_t smem, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(kBlock);
+  cfg.blockDim = dim3(block);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = h->stream;
   cudaLaunchAttribute at[1];
@@ -159,6 +160,10 @@ static void launch_k(const dgadv_handle *h, void (*kern)(KArgs...), int grid, si
   cfg.attrs = at;
   cfg.numAttrs = (h->flags & DGADV_FLAG_NO_PDL) ? 0 : 1;
   cudaLaunchKernelEx(&cfg, kern, args...);
+}
+template <typename... KArgs, typename... Args>
+static void launch_k(const dgadv_handle *h, void (*kern)(KArgs...), int grid, size_t smem, Args... args) {
+  launch_kb(h, kern, grid, kBlock, smem, args...);
 }
 
 // Copy of a state-sized buffer (a multiple of 16 bytes) in the dependent-launch chain.

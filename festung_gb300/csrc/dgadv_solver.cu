@@ -593,6 +593,9 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
     if (value < 0 || value > 64) return DGADV_EINVAL;
     h->persistPerSM = value;
     h->persistGrid = 0;
+  } else if (option == DGADV_OPT_ADJ_WARPS) {
+    if (value != 1 && value != 2 && value != 4) return DGADV_EINVAL;
+    h->adjWarps = value;
   } else if (option == DGADV_OPT_FLAGS) {
     const int runtime = DGADV_FLAG_NO_GRAPH | DGADV_FLAG_NO_PDL | DGADV_FLAG_FUSE | DGADV_FLAG_PERSIST;
     if (value & ~runtime) { h->err = "only NO_GRAPH, NO_PDL, FUSE and PERSIST change after creation"; return DGADV_EINVAL; }
@@ -613,6 +616,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   if (option == DGADV_OPT_GRAPH_STEPS) *value = h->graphSteps;
   else if (option == DGADV_OPT_FLAGS) *value = h->flags;
   else if (option == DGADV_OPT_PERSIST_BLOCKS) *value = h->persistPerSM;
+  else if (option == DGADV_OPT_ADJ_WARPS) *value = h->adjWarps;
   else return DGADV_EINVAL;
   return DGADV_OK;
   });

@@ -63,6 +63,28 @@ def test_checkpointed_sweep_equals_stored_sweep(lib):
         pd.solver.close()
 
 
+@pytest.mark.parametrize('p', [1, 2, 3])
+def test_fp32_sweeps_agree_bitwise_across_checkpoints_and_split_widths(lib, p):
+    """FP32: binomial and stage-recomputing sweeps equal the stored one bit for bit, and the
+    warp-role split of the stage kernel gives the same bits at 1, 2 and 4 warps per role."""
+    from festung_gb300 import _lib as L
+    from festung_gb300 import adjoint as AD
+    kw = dict(hmax=2 ** -4, p=p, numSteps=12, tEnd=12 * 1e-4)
+    c0, cstar, *_ = oracle_gradient(dict(kw, numSteps=1, tEnd=1e-4))
+    pd = AD.setup(precision='fp32', **kw)
+    try:
+        assert pd.solver.get_option(L.OPT_ADJ_WARPS) == 1
+        ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
+        for warps in (1, 2, 4):
+            pd.solver.set_option(L.OPT_ADJ_WARPS, warps)
+            for snaps in (0, 1, 4, kw['numSteps']):
+                got = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=snaps)
+                assert got[0] == ref[0]
+                assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2]), (warps, snaps)
+    finally:
+        pd.solver.close()
+
+
 def test_fp64_gradient_matches_finite_differences(lib):
     from festung_gb300 import adjoint as AD
     kw = dict(hmax=2 ** -5, p=2, numSteps=60, tEnd=60 * 2e-4)
