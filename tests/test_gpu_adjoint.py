@@ -73,7 +73,7 @@ def test_fp32_sweeps_agree_bitwise_across_checkpoints_and_split_widths(lib, p):
     c0, cstar, *_ = oracle_gradient(dict(kw, numSteps=1, tEnd=1e-4))
     pd = AD.setup(precision='fp32', **kw)
     try:
-        assert pd.solver.get_option(L.OPT_ADJ_WARPS) == 1
+        assert pd.solver.get_option(L.OPT_ADJ_WARPS) == 2
         ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
         for warps in (1, 2, 4):
             pd.solver.set_option(L.OPT_ADJ_WARPS, warps)
