@@ -9,11 +9,15 @@ Each candidate runs ``nSteps`` steps of the handle's own problem after one warm-
 with CUDA events on the handle's stream; the state is restored afterwards.  The choice can be
 kept in a JSON file keyed by the problem's signature and the GPU name, and reused.
 
+``tune_adjoint`` does the same for the FP32 adjoint stage kernel: warps per role, i.e. 32, 64 or
+128 elements per CTA with four warp roles (three edges, the volume points) per element.
+
 Fixed by design and not tuned: 128 elements per CTA (the row unit of the TMA bulk copies and the
-padding of every per-element array) and one thread per element.
+padding of every per-element array) and one thread per element in the forward kernels.
 """
 import json
 import os
+import time
 
 from . import _lib as L
 
@@ -69,4 +73,31 @@ def tune(solver, tau, nSteps=48, reps=3, fused_ok=False, cache=None, key=None):
         stored[key] = dict(best=best, table=table)
         with open(cache, 'w') as f:
             json.dump(stored, f, indent=1)
+    return best, table
+
+
+ADJ_WARPS = (1, 2, 4)
+
+
+def tune_adjoint(solver, tau, nSteps=20, nSnapshots=0, reps=3):
+    """Times a recorded run of `nSteps` steps and its reverse sweep at every warps-per-role
+    setting of the FP32 adjoint stage (wall time of dgadv_backward, which synchronises) and
+    applies the fastest; returns (best, table).  The gradients do not depend on the setting.
+    The handle's state is restored."""
+    state = solver.get_state()
+    table = []
+    for w in ADJ_WARPS:
+        solver.set_option(L.OPT_ADJ_WARPS, w)
+        times = []
+        for _ in range(reps + 1):   # the first backward captures the sweep's graph
+            solver.set_state(state)
+            solver.forward_record(nSteps, tau, nSnapshots)
+            g = solver.get_state()
+            t = time.perf_counter()
+            solver.backward(g)
+            times.append(time.perf_counter() - t)
+        table.append(dict(adjWarps=w, ms_backward=1e3 * min(times[1:])))
+    best = min(table, key=lambda r: r['ms_backward'])
+    solver.set_option(L.OPT_ADJ_WARPS, best['adjWarps'])
+    solver.set_state(state)
     return best, table

@@ -85,6 +85,24 @@ def test_fp32_sweeps_agree_bitwise_across_checkpoints_and_split_widths(lib, p):
         pd.solver.close()
 
 
+def test_adjoint_autotuner_applies_a_width_and_keeps_the_gradient(lib):
+    from festung_gb300 import _lib as L
+    from festung_gb300 import adjoint as AD
+    from festung_gb300 import autotune as AT
+    kw = dict(hmax=2 ** -4, p=2, numSteps=10, tEnd=10 * 1e-4)
+    c0, cstar, *_ = oracle_gradient(dict(kw, numSteps=1, tEnd=1e-4))
+    pd = AD.setup(precision='fp32', **kw)
+    try:
+        ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=3)
+        best, table = AT.tune_adjoint(pd.solver, pd.tau, nSteps=6, nSnapshots=3, reps=1)
+        assert [r['adjWarps'] for r in table] == [1, 2, 4]
+        assert pd.solver.get_option(L.OPT_ADJ_WARPS) == best['adjWarps']
+        got = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=3)
+        assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
+    finally:
+        pd.solver.close()
+
+
 def test_fp64_gradient_matches_finite_differences(lib):
     from festung_gb300 import adjoint as AD
     kw = dict(hmax=2 ** -5, p=2, numSteps=60, tEnd=60 * 2e-4)
