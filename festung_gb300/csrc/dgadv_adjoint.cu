@@ -414,6 +414,7 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
       if ((st = dev_alloc(h, (void **)&h->recTarget, (size_t)h->Kp * 4))) return st;
       if ((st = dev_alloc(h, (void **)&h->recVertex, (size_t)h->Kp * 4))) return st;
       if ((st = dev_alloc(h, &h->recW, (size_t)h->Kp * o.realBytes))) return st;
+      if ((st = dev_alloc(h, &h->adjMean, (size_t)h->Kp * o.realBytes))) return st;
       if ((st = dev_alloc(h, &h->vkeysA, 3 * 2 * (size_t)h->Vp * kb))) return st;
       if ((st = dev_alloc(h, (void **)&h->gmmA, 3 * (size_t)h->nInst * kSlotCopies * 2 * 8))) return st;
       if ((st = dev_alloc(h, &h->adjScrY, (size_t)S * bytes))) return st;

@@ -391,8 +391,8 @@ k_adj_stage_split(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *
 template <typename T, int P, int KIND>
 __global__ void __launch_bounds__(kBlock)
 k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, const LimIn<T> li,
-          const StageScalars sc, double scale, int *__restrict__ recTarget, int *__restrict__ recVertex,
-          T *__restrict__ recW) {
+          const StageScalars sc, double scale, const T *__restrict__ meanX, int *__restrict__ recTarget,
+          int *__restrict__ recVertex, T *__restrict__ recW) {
   constexpr int N = Dims<P>::N;
   const Tab<T, P> &tb = tab<T, P>();
   __shared__ T sh[2];
@@ -488,12 +488,11 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
         const auto key = kv.v[0][isPos ? 1 : 0][ns];
         const int vv = vid[ns];
         int best = -1, bestId = 0x7fffffff;
-        for (int i = g.vptr[vv]; i < g.vptr[vv + 1]; ++i) {
+        const int i0 = g.vptr[vv], i1 = g.vptr[vv + 1];
+#pragma unroll 4
+        for (int i = i0; i < i1; ++i) {   // the means k_mean_lin stored for this pass
           const int k2 = g.vidx[i];
-          T c2[N];
-#pragma unroll
-          for (int j = 0; j < N; ++j) c2[j] = x[(size_t)j * Kp + k2];
-          if (vkey(lin_mean<T, P>(c2)) == key && g.permv[k2] < bestId) { best = k2; bestId = g.permv[k2]; }
+          if (vkey(meanX[k2]) == key && g.permv[k2] < bestId) { best = k2; bestId = g.permv[k2]; }
         }
         tgt = best;
         w = sa / den;                                             // d alpha / d m = 1 / den
@@ -529,11 +528,20 @@ k_lim_vjp_gather(const Geo<T> g, T *lam, const int *recTarget, const int *recVer
   pdl_wait();
   T acc = T(0);
   bool any = false;
-  for (int n = 0; n < 3; ++n)
-    for (int i = g.vptr[vid[n]]; i < g.vptr[vid[n] + 1]; ++i) {
+  int i0[3], i1[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    i0[n] = g.vptr[vid[n]];
+    i1[n] = g.vptr[vid[n] + 1];
+  }
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+#pragma unroll 4
+    for (int i = i0[n]; i < i1[n]; ++i) {
       const int k2 = g.vidx[i];
       if (recTarget[k2] == k && recVertex[k2] == vid[n]) { acc = acc + recW[k2]; any = true; }
     }
+  }
   if (!any) return;
 #pragma unroll
   for (int j = 0; j < N; ++j) lam[(size_t)j * Kp + k] = lam[(size_t)j * Kp + k] + acc * tb.DM[0][j];
@@ -548,10 +556,12 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = v.gco[m];
   if (v.kind == 0)
     launch_k(h, k_lim_vjp<T, P, 0>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn, (T *)v.lamOut,
-             lim_in_adj<T>(h, v.pass), sc, v.scale, h->recTarget, h->recVertex, (T *)h->recW);
+             lim_in_adj<T>(h, v.pass), sc, v.scale, (const T *)h->adjMean, h->recTarget, h->recVertex,
+             (T *)h->recW);
   else
     launch_k(h, k_lim_vjp<T, P, 1>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn, (T *)v.lamOut,
-             lim_in_adj<T>(h, v.pass), sc, v.scale, h->recTarget, h->recVertex, (T *)h->recW);
+             lim_in_adj<T>(h, v.pass), sc, v.scale, (const T *)h->adjMean, h->recTarget, h->recVertex,
+             (T *)h->recW);
   launch_k(h, k_lim_vjp_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, (const int *)h->recTarget,
            (const int *)h->recVertex, (const T *)h->recW);
   return cudaGetLastError();
@@ -562,7 +572,7 @@ template <typename T, int P>
 static cudaError_t launch_vjp_scatter(dgadv_handle *h, const void *x, long long pass) {
   const Geo<T> g = make_geo<T>(h);
   const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
-  launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)x, lim_out_adj<T>(h, pass));
+  launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)x, lim_out_adj<T>(h, pass), (T *)h->adjMean);
   return cudaGetLastError();
 }
 

@@ -1251,10 +1251,11 @@ k_limit_lin(const Geo<T> g, const T *cbuf, T *out, const LimIn<T> li,
   limit_lin_tile<T, P>(g, cbuf, out, li, sc, blockIdx.x);
 }
 
-// Mean of the modal state scattered to the vertices (initial limiting, linear limiter).
+// Mean of the modal state scattered to the vertices (initial limiting, linear limiter); with
+// meanOut the means are also stored per element (the limiter adjoint looks up extremes there).
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_mean_lin(const Geo<T> g, const T *c, const LimOut<T> lo) {
+k_mean_lin(const Geo<T> g, const T *c, const LimOut<T> lo, T *__restrict__ meanOut) {
   constexpr int N = Dims<P>::N;
   const int t = threadIdx.x, k = blockIdx.x * kBlock + t;
   pdl_trigger();
@@ -1270,6 +1271,7 @@ k_mean_lin(const Geo<T> g, const T *c, const LimOut<T> lo) {
 #pragma unroll
     for (int i = 0; i < N; ++i) cc[i] = c[(size_t)i * Kp + k];
     q0 = lin_mean<T, P>(cc);
+    if (meanOut) meanOut[k] = q0;
   }
   scatter_quantities<T, 1>(g, lo, &q0, vid, active);
 }

@@ -104,6 +104,7 @@ struct dgadv_handle {
   void *tmpY = nullptr, *tmpD = nullptr;            // dJ/dy and dJ/dcDot of a reversed stage
   int *recTarget = nullptr, *recVertex = nullptr;   // extreme's element and vertex per element
   void *recW = nullptr;                             // its weight
+  void *adjMean = nullptr;                          // element means of the current limiter input
   void *vkeysA = nullptr;                           // the adjoint's own vertex keys (3 sets)
   unsigned long long *gmmA = nullptr;               // ... and global-extreme slots
   long long adjPass = 0;

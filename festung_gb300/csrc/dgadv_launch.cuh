@@ -371,7 +371,7 @@ static cudaError_t launch_limit_state(dgadv_handle *h, double t) {
   ++h->limPass;
   if (h->limType == DGADV_LIM_LINEAR) {
     const int gridK = (h->K + kBlock - 1) / kBlock;
-    launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)h->cn, lo);
+    launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)h->cn, lo, (T *)nullptr);
     launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)h->cn, (T *)h->cn, lim_in<T>(lo, h), sc);
   } else {
     launch_k(h, k_to_taylor<T, P>, grid, SR::bytes(SR::totaylor(), 0), g, (const T *)h->cn, (T *)h->tbuf, lo, sc);
