@@ -266,18 +266,26 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
           const double tBC = (s + 1 < S) ? (arg + cst[s + 1]) * tau : (arg + 1) * tau;
           for (int m = 0; m < h->nTerms; ++m)
             v.gco[m] = h->timeFn[m] == DGADV_TIME_EXP_NEG ? std::exp(-tBC) : 1.0;
+          // p >= 2: the solution limiter's kernel also scatters the time-derivative limiter's
+          // means, and the time-derivative limiter's kernel gathers the solution limiter's
+          // extreme terms first (5 launches per stage instead of 7)
+          const char *Cd = nullptr;
+          if (h->limdot)
+            Cd = h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
+                               : (const char *)h->adjScrCdot + (size_t)s * bytes;
           DG_CUDA(o.vjp_scatter(h, Y, h->adjPass));
           v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
+          v.nextX = Cd;
+          v.gatherOut = Cd ? 0 : 1;
           DG_CUDA(o.lim_vjp(h, v));
           muY = h->tmpY;
           if (h->limdot) {
-            const char *Cd = h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
-                                           : (const char *)h->adjScrCdot + (size_t)s * bytes;
-            DG_CUDA(o.vjp_scatter(h, Cd, h->adjPass));
             LimVjpArgs d;
             std::memset(&d, 0, sizeof(d));
             d.kind = 1; d.x = Cd; d.lamIn = h->tmpY; d.lamOut = h->tmpD; d.scale = (1.0 - omega[s]) * tau;
             d.pass = h->adjPass++;
+            d.gatherIn = 1;
+            d.gatherOut = 1;
             DG_CUDA(o.lim_vjp(h, d));
             mp = h->tmpD;
           }
@@ -415,6 +423,10 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
       if ((st = dev_alloc(h, (void **)&h->recVertex, (size_t)h->Kp * 4))) return st;
       if ((st = dev_alloc(h, &h->recW, (size_t)h->Kp * o.realBytes))) return st;
       if ((st = dev_alloc(h, &h->adjMean, (size_t)h->Kp * o.realBytes))) return st;
+      if ((st = dev_alloc(h, &h->adjMeanB, (size_t)h->Kp * o.realBytes))) return st;
+      if ((st = dev_alloc(h, (void **)&h->recTargetB, (size_t)h->Kp * 4))) return st;
+      if ((st = dev_alloc(h, (void **)&h->recVertexB, (size_t)h->Kp * 4))) return st;
+      if ((st = dev_alloc(h, &h->recWB, (size_t)h->Kp * o.realBytes))) return st;
       if ((st = dev_alloc(h, &h->vkeysA, 3 * 2 * (size_t)h->Vp * kb))) return st;
       if ((st = dev_alloc(h, (void **)&h->gmmA, 3 * (size_t)h->nInst * kSlotCopies * 2 * 8))) return st;
       if ((st = dev_alloc(h, &h->adjScrY, (size_t)S * bytes))) return st;

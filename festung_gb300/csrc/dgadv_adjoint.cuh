@@ -388,11 +388,23 @@ k_adj_stage_split(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *
 // choices are recomputed from the recorded input x (the same keys, shift and comparisons as the
 // forward kernels); a tie for the extreme goes to the lowest element index of the caller's order,
 // Dirichlet data winning a tie with an element.
-template <typename T, int P, int KIND>
+//
+// Two passes of a stage with the time-derivative limiter share launches:
+//   SNEXT (solution limiter): after the dependency wait the kernel also scatters the means of the
+//     time-derivative limiter's input `nextX` to the key set of the next pass (`loNext`, which
+//     resets the set after that) and stores them in `meanNext`; the grid covers max(K, numV);
+//   GIN (time-derivative limiter): each element first adds the solution limiter's extreme terms
+//     (records pTarget / pVertex / pW) into its lamIn and writes lamIn back, which is what
+//     k_lim_vjp_gather would have done in a launch of its own.
+// The key set written by SNEXT was reset by the previous pass's scatter and is read only by the
+// next kernel; the set it resets was last read two passes ago.
+template <typename T, int P, int KIND, bool GIN, bool SNEXT>
 __global__ void __launch_bounds__(kBlock)
 k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, const LimIn<T> li,
           const StageScalars sc, double scale, const T *__restrict__ meanX, int *__restrict__ recTarget,
-          int *__restrict__ recVertex, T *__restrict__ recW) {
+          int *__restrict__ recVertex, T *__restrict__ recW, T *lamInW, const int *__restrict__ pTarget,
+          const int *__restrict__ pVertex, const T *__restrict__ pW, const T *__restrict__ nextX,
+          const LimOut<T> loNext, T *__restrict__ meanNext) {
   constexpr int N = Dims<P>::N;
   const Tab<T, P> &tb = tab<T, P>();
   __shared__ T sh[2];
@@ -413,13 +425,54 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
       for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
     }
   pdl_wait();
+  if constexpr (SNEXT) {
+    reset_next<T>(g, loNext, k);
+    T q0 = T(0);
+    if (active) {
+      T cc[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) cc[i] = nextX[(size_t)i * Kp + k];
+      q0 = lin_mean<T, P>(cc);
+      meanNext[k] = q0;
+    }
+    scatter_quantities<T, 1>(g, loNext, &q0, vid, active);
+  }
   if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
   T xv[N], lam[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
     xv[i] = active ? x[(size_t)i * Kp + k] : T(0);
-    lam[i] = active ? T(scale) * lamIn[(size_t)i * Kp + k] : T(0);
+    lam[i] = active ? lamIn[(size_t)i * Kp + k] : T(0);
   }
+  if constexpr (GIN) {
+    if (active) {
+      int i0[3], i1[3];
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        i0[n] = g.vptr[vid[n]];
+        i1[n] = g.vptr[vid[n] + 1];
+      }
+      T acc = T(0);
+      bool any = false;
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+#pragma unroll 4
+        for (int i = i0[n]; i < i1[n]; ++i) {
+          const int k2 = g.vidx[i];
+          if (pTarget[k2] == k && pVertex[k2] == vid[n]) { acc = acc + pW[k2]; any = true; }
+        }
+      }
+      if (any) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+          lam[j] = lam[j] + acc * tb.DM[0][j];
+          lamInW[(size_t)j * Kp + k] = lam[j];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) lam[i] = T(scale) * lam[i];
   VKeys<T, 1> kv;
   load_vkeys<T, 1>(g, li, vid, kv);
   __syncthreads();
@@ -547,6 +600,8 @@ k_lim_vjp_gather(const Geo<T> g, T *lam, const int *recTarget, const int *recVer
   for (int j = 0; j < N; ++j) lam[(size_t)j * Kp + k] = lam[(size_t)j * Kp + k] + acc * tb.DM[0][j];
 }
 
+// The solution limiter's pass uses the first record set and the means of vjp_scatter; the
+// time-derivative limiter's pass the second record set and the means its predecessor scattered.
 template <typename T, int P>
 static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   const Geo<T> g = make_geo<T>(h);
@@ -554,16 +609,31 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   StageScalars sc{};
   sc.flag = h->flag;
   for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = v.gco[m];
-  if (v.kind == 0)
-    launch_k(h, k_lim_vjp<T, P, 0>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn, (T *)v.lamOut,
-             lim_in_adj<T>(h, v.pass), sc, v.scale, (const T *)h->adjMean, h->recTarget, h->recVertex,
-             (T *)h->recW);
-  else
-    launch_k(h, k_lim_vjp<T, P, 1>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn, (T *)v.lamOut,
-             lim_in_adj<T>(h, v.pass), sc, v.scale, (const T *)h->adjMean, h->recTarget, h->recVertex,
-             (T *)h->recW);
-  launch_k(h, k_lim_vjp_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, (const int *)h->recTarget,
-           (const int *)h->recVertex, (const T *)h->recW);
+  int *rT = v.kind == 0 ? h->recTarget : h->recTargetB, *rV = v.kind == 0 ? h->recVertex : h->recVertexB;
+  T *rW = (T *)(v.kind == 0 ? h->recW : h->recWB);
+  const T *meanX = (const T *)(v.kind == 0 ? h->adjMean : h->adjMeanB);
+  const LimOut<T> loNext = lim_out_adj<T>(h, v.pass + 1);
+  const T *lamIn = (const T *)v.lamIn;
+  T *lamInW = (T *)v.lamIn;
+  if (v.kind == 0 && v.nextX) {
+    const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
+    launch_k(h, k_lim_vjp<T, P, 0, false, true>, grid, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut,
+             lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, rT, rV, rW, lamInW, (const int *)nullptr,
+             (const int *)nullptr, (const T *)nullptr, (const T *)v.nextX, loNext, (T *)h->adjMeanB);
+  } else if (v.kind == 0) {
+    launch_k(h, k_lim_vjp<T, P, 0, false, false>, gridK, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut,
+             lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, rT, rV, rW, lamInW, (const int *)nullptr,
+             (const int *)nullptr, (const T *)nullptr, (const T *)nullptr, loNext, (T *)nullptr);
+  } else if (v.gatherIn) {
+    launch_k(h, k_lim_vjp<T, P, 1, true, false>, gridK, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut,
+             lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, rT, rV, rW, lamInW, (const int *)h->recTarget,
+             (const int *)h->recVertex, (const T *)h->recW, (const T *)nullptr, loNext, (T *)nullptr);
+  } else {
+    return cudaErrorInvalidValue;   // the time-derivative pass follows a solution pass with nextX
+  }
+  if (v.gatherOut)
+    launch_k(h, k_lim_vjp_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, (const int *)rT, (const int *)rV,
+             (const T *)rW);
   return cudaGetLastError();
 }
 

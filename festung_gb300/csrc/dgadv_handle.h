@@ -104,7 +104,9 @@ struct dgadv_handle {
   void *tmpY = nullptr, *tmpD = nullptr;            // dJ/dy and dJ/dcDot of a reversed stage
   int *recTarget = nullptr, *recVertex = nullptr;   // extreme's element and vertex per element
   void *recW = nullptr;                             // its weight
-  void *adjMean = nullptr;                          // element means of the current limiter input
+  void *adjMean = nullptr, *adjMeanB = nullptr;     // element means of the limiter inputs (per kind)
+  int *recTargetB = nullptr, *recVertexB = nullptr; // the time-derivative limiter's records
+  void *recWB = nullptr;
   void *vkeysA = nullptr;                           // the adjoint's own vertex keys (3 sets)
   unsigned long long *gmmA = nullptr;               // ... and global-extreme slots
   long long adjPass = 0;
@@ -138,6 +140,11 @@ struct LimVjpArgs {
   double scale;
   long long pass;      // adjoint key set (pass mod 3) holding x's patch extremes
   double gco[4];       // time factors of the Dirichlet data (solution limiter)
+  const void *nextX;   // solution limiter: the time-derivative limiter's input, whose means this
+                       // pass scatters to the key set of pass + 1 (null: none)
+  int gatherIn;        // time-derivative limiter: first add the solution limiter's extreme
+                       // terms into lamIn (written back), in place of their own gather launch
+  int gatherOut;       // launch the gather of this pass's extreme terms into lamOut
 };
 
 // One stage of one transported species (dgadv_transport.cu): c h out from c h in, the
