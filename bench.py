@@ -321,7 +321,7 @@ def large_block(device, flush):
 ADJOINT_WORKLOAD = dict(hmax=2 ** -7, p=2, numSteps=200, tEnd=200 * 2e-4)
 
 
-def adjoint_block(reps=3, fd_dirs=4):
+def adjoint_block(reps=3, fd_dirs=16):
     """Adjoint cost on the gradient workload (32768 triangles, p = 2, 200 SSP-RK3 steps): wall
     time of dgadv_backward over the wall time of the same run forward (dgadv_set_state +
     dgadv_step + sync), with every stage state stored and with 20 binomial snapshots; FP64

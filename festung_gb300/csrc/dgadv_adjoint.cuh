@@ -425,6 +425,9 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
       for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
     }
   pdl_wait();
+  // blocks past the last element tile (SNEXT grids cover the vertices) use the last tile's
+  // instance for the global extremes
+  const int tile = min((int)blockIdx.x, (g.K - 1) / kBlock);
   if constexpr (SNEXT) {
     reset_next<T>(g, loNext, k);
     T q0 = T(0);
@@ -435,9 +438,9 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
       q0 = lin_mean<T, P>(cc);
       meanNext[k] = q0;
     }
-    scatter_quantities<T, 1>(g, loNext, &q0, vid, active);
+    scatter_quantities<T, 1>(g, loNext, &q0, vid, active, tile);
   }
-  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc, tile), li.nc, sh);
   T xv[N], lam[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
