@@ -101,6 +101,21 @@ __global__ void k_theta_partial(int K, int Kp, int nF, int nV, int pairs, const 
 
 constexpr int kThetaBlocks = 304;   // 2 x 152 SMs
 
+// Position of each element in the CSR vertex patches of its three vertices (pos[n][k]: index i
+// with vidx[i] == k in patch V0T[n][k]).
+__global__ void k_csr_pos(int K, int Kp, const int *__restrict__ V0T, const int *__restrict__ vptr,
+                          const int *__restrict__ vidx, int *__restrict__ pos) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  for (int n = 0; n < 3; ++n) {
+    const int v = V0T[(size_t)n * Kp + k];
+    int at = -1;
+    for (int i = vptr[v]; i < vptr[v + 1]; ++i)
+      if (vidx[i] == k) at = i;
+    pos[(size_t)n * Kp + k] = at;
+  }
+}
+
 // The cached reverse-sweep graph no longer fits the recorded run.
 void drop_sweep(dgadv_handle *h) {
   if (h->adjExec) cudaGraphExecDestroy(h->adjExec);
@@ -419,14 +434,15 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
     if (!h->tmpY) {
       if ((st = dev_alloc(h, &h->tmpY, bytes))) return st;
       if ((st = dev_alloc(h, &h->tmpD, bytes))) return st;
-      if ((st = dev_alloc(h, (void **)&h->recTarget, (size_t)h->Kp * 4))) return st;
-      if ((st = dev_alloc(h, (void **)&h->recVertex, (size_t)h->Kp * 4))) return st;
-      if ((st = dev_alloc(h, &h->recW, (size_t)h->Kp * o.realBytes))) return st;
+      for (int r = 0; r < 2; ++r) {
+        if ((st = dev_alloc(h, (void **)&h->recSlotT[r], 3 * (size_t)h->K * 4))) return st;
+        if ((st = dev_alloc(h, &h->recSlotW[r], 3 * (size_t)h->K * o.realBytes))) return st;
+      }
+      if ((st = dev_alloc(h, (void **)&h->csrPos, 3 * (size_t)h->Kp * 4))) return st;
+      k_csr_pos<<<(h->K + 127) / 128, 128, 0, h->stream>>>(h->K, h->Kp, h->V0T, h->vptr, h->vidx, h->csrPos);
+      DG_CUDA(cudaGetLastError());
       if ((st = dev_alloc(h, &h->adjMean, (size_t)h->Kp * o.realBytes))) return st;
       if ((st = dev_alloc(h, &h->adjMeanB, (size_t)h->Kp * o.realBytes))) return st;
-      if ((st = dev_alloc(h, (void **)&h->recTargetB, (size_t)h->Kp * 4))) return st;
-      if ((st = dev_alloc(h, (void **)&h->recVertexB, (size_t)h->Kp * 4))) return st;
-      if ((st = dev_alloc(h, &h->recWB, (size_t)h->Kp * o.realBytes))) return st;
       if ((st = dev_alloc(h, &h->vkeysA, 3 * 2 * (size_t)h->Vp * kb))) return st;
       if ((st = dev_alloc(h, (void **)&h->gmmA, 3 * (size_t)h->nInst * kSlotCopies * 2 * 8))) return st;
       if ((st = dev_alloc(h, &h->adjScrY, (size_t)S * bytes))) return st;

@@ -394,17 +394,19 @@ k_adj_stage_split(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *
 //     time-derivative limiter's input `nextX` to the key set of the next pass (`loNext`, which
 //     resets the set after that) and stores them in `meanNext`; the grid covers max(K, numV);
 //   GIN (time-derivative limiter): each element first adds the solution limiter's extreme terms
-//     (records pTarget / pVertex / pW) into its lamIn and writes lamIn back, which is what
-//     k_lim_vjp_gather would have done in a launch of its own.
+//     (the first record set, pSlotT / pSlotW) into its lamIn and writes lamIn back, which is
+//     what k_lim_vjp_gather would have done in a launch of its own.
+// Records are kept by CSR position (csrPos): the element at position i of patch v writes slot i,
+// so a gather reads the slots of its patches directly instead of each patch element's record.
 // The key set written by SNEXT was reset by the previous pass's scatter and is read only by the
 // next kernel; the set it resets was last read two passes ago.
 template <typename T, int P, int KIND, bool GIN, bool SNEXT>
 __global__ void __launch_bounds__(kBlock)
 k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, const LimIn<T> li,
-          const StageScalars sc, double scale, const T *__restrict__ meanX, int *__restrict__ recTarget,
-          int *__restrict__ recVertex, T *__restrict__ recW, T *lamInW, const int *__restrict__ pTarget,
-          const int *__restrict__ pVertex, const T *__restrict__ pW, const T *__restrict__ nextX,
-          const LimOut<T> loNext, T *__restrict__ meanNext) {
+          const StageScalars sc, double scale, const T *__restrict__ meanX, const int *__restrict__ csrPos,
+          int *__restrict__ slotT, T *__restrict__ slotW, T *lamInW, const int *__restrict__ pSlotT,
+          const T *__restrict__ pSlotW, const T *__restrict__ nextX, const LimOut<T> loNext,
+          T *__restrict__ meanNext) {
   constexpr int N = Dims<P>::N;
   const Tab<T, P> &tb = tab<T, P>();
   __shared__ T sh[2];
@@ -412,9 +414,10 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
   pdl_trigger();
   const bool active = k < g.K;
   const int Kp = g.Kp;
-  int vid[3] = {0, 0, 0}, dmask = 0;
+  int vid[3] = {0, 0, 0}, pos[3] = {0, 0, 0}, dmask = 0;
   if (active) {
     vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
+    pos[0] = csrPos[k]; pos[1] = csrPos[Kp + k]; pos[2] = csrPos[2 * Kp + k];
     if (KIND == 0) dmask = (g.code[k] >> 9) & 7;
   }
   T data[3] = {T(0), T(0), T(0)};
@@ -460,10 +463,8 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
 #pragma unroll
       for (int n = 0; n < 3; ++n) {
 #pragma unroll 4
-        for (int i = i0[n]; i < i1[n]; ++i) {
-          const int k2 = g.vidx[i];
-          if (pTarget[k2] == k && pVertex[k2] == vid[n]) { acc = acc + pW[k2]; any = true; }
-        }
+        for (int i = i0[n]; i < i1[n]; ++i)
+          if (pSlotT[i] == k) { acc = acc + pSlotW[i]; any = true; }
       }
       if (any) {
 #pragma unroll
@@ -564,16 +565,17 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
   }
 #pragma unroll
   for (int i = 0; i < N; ++i) lamOut[(size_t)i * Kp + k] = out[i];
-  recTarget[k] = tgt;
-  recVertex[k] = vid[ns];
-  recW[k] = w;
+#pragma unroll
+  for (int n = 0; n < 3; ++n)
+    if (pos[n] >= 0) slotT[pos[n]] = n == ns ? tgt : -1;
+  if (pos[ns] >= 0) slotW[pos[ns]] = w;
 }
 
 // Gathers the recorded extreme terms: element e adds w DM0 for every element of its vertex
 // patches whose limiter factor took its extreme from e at that vertex (CSR order: deterministic).
 template <typename T, int P>
 __global__ void __launch_bounds__(kBlock)
-k_lim_vjp_gather(const Geo<T> g, T *lam, const int *recTarget, const int *recVertex, const T *recW) {
+k_lim_vjp_gather(const Geo<T> g, T *lam, const int *slotT, const T *slotW) {
   constexpr int N = Dims<P>::N;
   const Tab<T, P> &tb = tab<T, P>();
   const int k = blockIdx.x * kBlock + threadIdx.x;
@@ -594,8 +596,7 @@ k_lim_vjp_gather(const Geo<T> g, T *lam, const int *recTarget, const int *recVer
   for (int n = 0; n < 3; ++n) {
 #pragma unroll 4
     for (int i = i0[n]; i < i1[n]; ++i) {
-      const int k2 = g.vidx[i];
-      if (recTarget[k2] == k && recVertex[k2] == vid[n]) { acc = acc + recW[k2]; any = true; }
+      if (slotT[i] == k) { acc = acc + slotW[i]; any = true; }
     }
   }
   if (!any) return;
@@ -612,8 +613,9 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   StageScalars sc{};
   sc.flag = h->flag;
   for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = v.gco[m];
-  int *rT = v.kind == 0 ? h->recTarget : h->recTargetB, *rV = v.kind == 0 ? h->recVertex : h->recVertexB;
-  T *rW = (T *)(v.kind == 0 ? h->recW : h->recWB);
+  int *rT = h->recSlotT[v.kind];
+  T *rW = (T *)h->recSlotW[v.kind];
+  const int *cp = h->csrPos;
   const T *meanX = (const T *)(v.kind == 0 ? h->adjMean : h->adjMeanB);
   const LimOut<T> loNext = lim_out_adj<T>(h, v.pass + 1);
   const T *lamIn = (const T *)v.lamIn;
@@ -621,22 +623,21 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   if (v.kind == 0 && v.nextX) {
     const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
     launch_k(h, k_lim_vjp<T, P, 0, false, true>, grid, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut,
-             lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, rT, rV, rW, lamInW, (const int *)nullptr,
-             (const int *)nullptr, (const T *)nullptr, (const T *)v.nextX, loNext, (T *)h->adjMeanB);
+             lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, cp, rT, rW, lamInW, (const int *)nullptr,
+             (const T *)nullptr, (const T *)v.nextX, loNext, (T *)h->adjMeanB);
   } else if (v.kind == 0) {
     launch_k(h, k_lim_vjp<T, P, 0, false, false>, gridK, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut,
-             lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, rT, rV, rW, lamInW, (const int *)nullptr,
-             (const int *)nullptr, (const T *)nullptr, (const T *)nullptr, loNext, (T *)nullptr);
+             lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, cp, rT, rW, lamInW, (const int *)nullptr,
+             (const T *)nullptr, (const T *)nullptr, loNext, (T *)nullptr);
   } else if (v.gatherIn) {
     launch_k(h, k_lim_vjp<T, P, 1, true, false>, gridK, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut,
-             lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, rT, rV, rW, lamInW, (const int *)h->recTarget,
-             (const int *)h->recVertex, (const T *)h->recW, (const T *)nullptr, loNext, (T *)nullptr);
+             lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, cp, rT, rW, lamInW, (const int *)h->recSlotT[0],
+             (const T *)h->recSlotW[0], (const T *)nullptr, loNext, (T *)nullptr);
   } else {
     return cudaErrorInvalidValue;   // the time-derivative pass follows a solution pass with nextX
   }
   if (v.gatherOut)
-    launch_k(h, k_lim_vjp_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, (const int *)rT, (const int *)rV,
-             (const T *)rW);
+    launch_k(h, k_lim_vjp_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, (const int *)rT, (const T *)rW);
   return cudaGetLastError();
 }
 

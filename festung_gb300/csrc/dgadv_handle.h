@@ -102,11 +102,13 @@ struct dgadv_handle {
   void *adjRecY = nullptr, *adjRecCdot = nullptr;   // per step and stage (stage storage mode)
   void *adjScrY = nullptr, *adjScrCdot = nullptr;   // per stage (recomputing modes)
   void *tmpY = nullptr, *tmpD = nullptr;            // dJ/dy and dJ/dcDot of a reversed stage
-  int *recTarget = nullptr, *recVertex = nullptr;   // extreme's element and vertex per element
-  void *recW = nullptr;                             // its weight
+  // extreme terms of the limiter adjoint, one record set per limiter kind, stored by position in
+  // the vertex-patch CSR (vidx): the element at position i of patch v writes there the element
+  // holding its extreme at v (or -1) and the term's weight
+  int *recSlotT[2] = {nullptr, nullptr};
+  void *recSlotW[2] = {nullptr, nullptr};
+  int *csrPos = nullptr;                            // 3 x Kp: position of element k in patch V0T[n][k]
   void *adjMean = nullptr, *adjMeanB = nullptr;     // element means of the limiter inputs (per kind)
-  int *recTargetB = nullptr, *recVertexB = nullptr; // the time-derivative limiter's records
-  void *recWB = nullptr;
   void *vkeysA = nullptr;                           // the adjoint's own vertex keys (3 sets)
   unsigned long long *gmmA = nullptr;               // ... and global-extreme slots
   long long adjPass = 0;
