@@ -38,16 +38,19 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    'cfg2': dict(testcase='gauss_slot', hmax=2 ** -8, p=2, numSteps=500, tEnd=500 * 1e-4,
-                 isSlopeLim=True, typeSlopeLim='linear', ordRK=3),
+    # Gaussian hump and slotted cylinder in the rotating velocity, linear limiter
+    'gauss_slot_131k_p2': dict(testcase='gauss_slot', hmax=2 ** -8, p=2, numSteps=500, tEnd=500 * 1e-4,
+                               isSlopeLim=True, typeSlopeLim='linear', ordRK=3),
     # the same operator on a 16x larger mesh (2,097,152 triangles): inputs well beyond L2, used
     # for the DRAM traffic capture of the stage kernels
-    'cfg2big': dict(testcase='gauss_slot', hmax=2 ** -10, p=2, numSteps=500, tEnd=500 * 1e-4,
-                    isSlopeLim=True, typeSlopeLim='linear', ordRK=3),
-    'cfg1': dict(testcase='gauss_slot', hmax=2 ** -5, p=1, numSteps=500, tEnd=0.5,
-                 isSlopeLim=True, typeSlopeLim='linear', ordRK=2),
-    'cfg5': dict(testcase='gauss_slot', hmax=2 ** -10, p=3, numSteps=100, tEnd=100 * 2e-5,
-                 isSlopeLim=True, typeSlopeLim='hierarch_vert', ordRK=3, jitter=0.1, meshSeed=5),
+    'gauss_slot_2M_p2': dict(testcase='gauss_slot', hmax=2 ** -10, p=2, numSteps=500, tEnd=500 * 1e-4,
+                             isSlopeLim=True, typeSlopeLim='linear', ordRK=3),
+    'gauss_slot_2048_p1': dict(testcase='gauss_slot', hmax=2 ** -5, p=1, numSteps=500, tEnd=0.5,
+                               isSlopeLim=True, typeSlopeLim='linear', ordRK=2),
+    # 2,097,152 triangles with 10% node jitter, p = 3, hierarchical vertex limiter
+    'gauss_slot_2M_p3_hier': dict(testcase='gauss_slot', hmax=2 ** -10, p=3, numSteps=100, tEnd=100 * 2e-5,
+                                  isSlopeLim=True, typeSlopeLim='hierarch_vert', ordRK=3, jitter=0.1,
+                                  meshSeed=5),
 }
 
 
@@ -243,10 +246,12 @@ def run_reference(args):
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the stage kernels on
-# the 131072-triangle workload in FP32, from one ncu capture of `bench.py --ncu-case cfg2
-# --ncu-steps 2` (cold L2 under ncu; writes stay in L2 at this size).
-MEASURED_TRAFFIC = {('cfg2', 'k_stage_op'): 18.4e6, ('cfg2', 'k_limit_dot'): 28.4e6,
-                    ('cfg2', 'k_limit'): 5.8e6}
+# the 131072-triangle workload in FP32, from one ncu capture of
+# `bench.py --ncu-case gauss_slot_131k_p2 --ncu-steps 2` (cold L2 under ncu; writes stay in L2 at
+# this size).
+MEASURED_TRAFFIC = {('gauss_slot_131k_p2', 'k_stage_op'): 18.4e6,
+                    ('gauss_slot_131k_p2', 'k_limit_dot'): 28.4e6,
+                    ('gauss_slot_131k_p2', 'k_limit'): 5.8e6}
 
 
 def solve_path(wl, precision, device, c0, flush):
@@ -266,16 +271,17 @@ def solve_path(wl, precision, device, c0, flush):
 
 
 def large_block(device, flush):
-    """BASELINE's large single mesh (cfg5): 2,097,152 jittered triangles, p = 3, the hierarchical
+    """The large single mesh: 2,097,152 jittered triangles, p = 3, the hierarchical
     vertex limiter, 100 SSP-RK3 steps.  One full solve from the projected initial data in FP32
     and in FP64 after an L2 flush (the working set, >1 GB, is far beyond L2), the FP32 kernels'
     launch times and the dominant kernel's HBM roofline, and FP32's distance to FP64."""
     import torch
-    out = {'workload': 'cfg5: domainSquare hmax=2^-10 with 10% node jitter (2,097,152 triangles), p=3 '
-                       '(N=10), hierarchical vertex limiter, 100 SSP-RK3 steps, tau=2e-5, gauss_slot'}
+    out = {'workload': 'gauss_slot_2M_p3_hier: domainSquare hmax=2^-10 with 10% node jitter '
+                       '(2,097,152 triangles), p=3 (N=10), hierarchical vertex limiter, 100 SSP-RK3 '
+                       'steps, tau=2e-5, gauss_slot'}
     states = {}
     for prec in ('fp32', 'fp64'):
-        pd = setup_problem('cfg5', prec, device)
+        pd = setup_problem('gauss_slot_2M_p3_hier', prec, device)
         s = pd.solver
         c0 = np.asfortranarray(pd._cDisc)
         s.step(5, 0, pd.tau)                        # warm-up (graph capture, first launches)
@@ -831,7 +837,7 @@ def main():
     ap.add_argument('--steps', type=int, default=5)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--workload', default='cfg2', choices=sorted(WORKLOADS))
+    ap.add_argument('--workload', default='gauss_slot_131k_p2', choices=sorted(WORKLOADS))
     ap.add_argument('--no-fp64', action='store_true')
     ap.add_argument('--no-df32', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')

@@ -19,8 +19,8 @@ from oracle import matfree as MF  # noqa: E402
 
 CASES = {
     # the 2048-triangle benchmark case: p=1, RK2, tau=1e-3, 500 steps, linear limiter
-    'cfg1_p1_lim': dict(testcase='gauss_slot', hmax=2 ** -5, p=1, tEnd=0.5, numSteps=500,
-                        isSlopeLim=True, typeSlopeLim='linear'),
+    'gauss_slot_2048_p1_lim': dict(testcase='gauss_slot', hmax=2 ** -5, p=1, tEnd=0.5, numSteps=500,
+                                   isSlopeLim=True, typeSlopeLim='linear'),
     # p=2 with time-derivative limiting on a smaller mesh
     'p2_lim_h4': dict(testcase='gauss_slot', hmax=2 ** -4, p=2, tEnd=0.05, numSteps=100,
                       isSlopeLim=True, typeSlopeLim='linear'),

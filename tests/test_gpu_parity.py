@@ -70,7 +70,7 @@ def test_fp64_matches_oracle(lib, kw):
     assert abs(g.error - o.error) <= tol * max(1.0, o.error)
 
 
-@pytest.mark.parametrize('name', ['cfg1_p1_lim', 'p2_lim_h4', 'p3_hier_jit', 'transient_p2'])
+@pytest.mark.parametrize('name', ['gauss_slot_2048_p1_lim', 'p2_lim_h4', 'p3_hier_jit', 'transient_p2'])
 def test_fp64_matches_golden(lib, name):
     d = np.load(os.path.join(GOLD, name + '.npz'))
     kw = ast.literal_eval(str(d['params']))
