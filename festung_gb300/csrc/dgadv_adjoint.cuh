@@ -427,6 +427,23 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
 #pragma unroll
       for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
     }
+  // static data read before the dependency wait: the patch ranges of the three vertices and, for
+  // the time-derivative limiter up to p = 2, the element's packed Taylor mass block (used where
+  // the clip is active; loading it here takes a dependent round trip off that path)
+  int vp0[3] = {0, 0, 0}, vp1[3] = {0, 0, 0};
+  if (active) {
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      vp0[n] = g.vptr[vid[n]];
+      vp1[n] = g.vptr[vid[n] + 1];
+    }
+  }
+  constexpr bool kPrefetchMT = KIND == 1 && N <= 6;
+  T mtv[kPrefetchMT ? N * (N - 1) : 1];
+  if constexpr (kPrefetchMT) {
+#pragma unroll
+    for (int i = 0; i < N * (N - 1); ++i) mtv[i] = active ? g.MT[(size_t)i * Kp + k] : T(0);
+  }
   pdl_wait();
   // blocks past the last element tile (SNEXT grids cover the vertices) use the last tile's
   // instance for the global extremes
@@ -452,18 +469,12 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
   }
   if constexpr (GIN) {
     if (active) {
-      int i0[3], i1[3];
-#pragma unroll
-      for (int n = 0; n < 3; ++n) {
-        i0[n] = g.vptr[vid[n]];
-        i1[n] = g.vptr[vid[n] + 1];
-      }
       T acc = T(0);
       bool any = false;
 #pragma unroll
       for (int n = 0; n < 3; ++n) {
 #pragma unroll 4
-        for (int i = i0[n]; i < i1[n]; ++i)
+        for (int i = vp0[n]; i < vp1[n]; ++i)
           if (pSlotT[i] == k) { acc = acc + pSlotW[i]; any = true; }
       }
       if (any) {
@@ -520,6 +531,7 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         if (KIND == 0) a.fms(tb.DMinv[i][j], lam[i]);
+        else if constexpr (kPrefetchMT) a.fma(mtv[i * (N - 1) + (j - 1)], lam[i]);
         else a.fma(g.MT[(size_t)(i * (N - 1) + (j - 1)) * Kp + k], lam[i]);
       }
       r[j] = a.get();
@@ -543,9 +555,9 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
       const bool fromData = ((dmask >> ns) & 1) && (isPos ? !(data[ns] < rawExt) : !(data[ns] > rawExt));
       if (!fromData) {
         const auto key = kv.v[0][isPos ? 1 : 0][ns];
-        const int vv = vid[ns];
         int best = -1, bestId = 0x7fffffff;
-        const int i0 = g.vptr[vv], i1 = g.vptr[vv + 1];
+        const int i0 = ns == 0 ? vp0[0] : (ns == 1 ? vp0[1] : vp0[2]);
+        const int i1 = ns == 0 ? vp1[0] : (ns == 1 ? vp1[1] : vp1[2]);
 #pragma unroll 4
         for (int i = i0; i < i1; ++i) {   // the means k_mean_lin stored for this pass
           const int k2 = g.vidx[i];
