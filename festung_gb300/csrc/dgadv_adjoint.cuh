@@ -595,15 +595,15 @@ k_lim_vjp_gather(const Geo<T> g, T *lam, const int *slotT, const T *slotW) {
   if (k >= g.K) return;
   const int Kp = g.Kp;
   const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
-  pdl_wait();
-  T acc = T(0);
-  bool any = false;
-  int i0[3], i1[3];
+  int i0[3], i1[3];   // static: read before the dependency wait
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
     i0[n] = g.vptr[vid[n]];
     i1[n] = g.vptr[vid[n] + 1];
   }
+  pdl_wait();
+  T acc = T(0);
+  bool any = false;
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
 #pragma unroll 4
