@@ -28,6 +28,24 @@ def test_library_exports_every_declared_symbol(lib):
         assert n in L.SYMBOLS, 'binding missing for ' + n
 
 
+def declared_constants():
+    """NAME -> value of every `DGADV_NAME = value` enumerator in include/dgadv.h."""
+    src = open(os.path.join(ROOT, 'include', 'dgadv.h')).read()
+    return {m.group(1): int(m.group(2), 0) for m in re.finditer(r'\b(DGADV_[A-Z0-9_]+)\s*=\s*(-?(?:0x[0-9a-fA-F]+|\d+))', src)}
+
+
+def test_python_constants_match_the_header():
+    consts = declared_constants()
+    assert len(consts) >= 20 and consts['DGADV_OPT_ADJ_WARPS'] == 4
+    checked = 0
+    for name, value in consts.items():
+        for attr in (name, name[len('DGADV_'):]):
+            if hasattr(L, attr):
+                assert getattr(L, attr) == value, (attr, getattr(L, attr), value)
+                checked += 1
+    assert checked >= 15
+
+
 def test_status_strings(lib):
     assert lib.dgadv_status_string(0) == b'ok'
     assert lib.dgadv_status_string(L.DGADV_EMESH) == b'inconsistent mesh'
