@@ -246,45 +246,44 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     const LimOut<T> lo1 = lim_out<T>(h);
     ++h->limPass;
     const int mode = h->limdot ? 2 : 1;
+    // buffers of the limiter inputs: tb, or in a recorded run of the adjoint this stage's record
+    // slots, written directly (cDot before time-derivative limiting; the unlimited stage value)
+    T *cdB = (lin && mode == 2 && h->recCdot[s]) ? (T *)h->recCdot[s] : tb;
+    T *yB = (lin && h->recY[s]) ? (T *)h->recY[s] : tb;
     prof_mark(h, 0);
     if (mode == 2) {
       if (lin) {
-        if (rhs) launch_k(h, k_stage_op<T, P, 2, true, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, tb, lo1, sc);
-        else launch_k(h, k_stage_op<T, P, 2, false, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, tb, lo1, sc);
+        if (rhs) launch_k(h, k_stage_op<T, P, 2, true, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, cdB, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 2, false, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, cdB, lo1, sc);
       } else {
         if (rhs) launch_k(h, k_stage_op<T, P, 2, true, false>, grid, SR::bytes(SR::op(2, false), 1), g, in, cn, tb, lo1, sc);
         else launch_k(h, k_stage_op<T, P, 2, false, false>, grid, SR::bytes(SR::op(2, false), 1), g, in, cn, tb, lo1, sc);
       }
     } else {
       if (lin) {
-        if (rhs) launch_k(h, k_stage_op<T, P, 1, true, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, tb, lo1, sc);
-        else launch_k(h, k_stage_op<T, P, 1, false, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, tb, lo1, sc);
+        if (rhs) launch_k(h, k_stage_op<T, P, 1, true, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, yB, lo1, sc);
+        else launch_k(h, k_stage_op<T, P, 1, false, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, yB, lo1, sc);
       } else {
         if (rhs) launch_k(h, k_stage_op<T, P, 1, true, false>, grid, SR::bytes(SR::op(1, false), 1), g, in, cn, tb, lo1, sc);
         else launch_k(h, k_stage_op<T, P, 1, false, false>, grid, SR::bytes(SR::op(1, false), 1), g, in, cn, tb, lo1, sc);
       }
     }
     prof_mark(h, -1);
-    // recorded run of the adjoint: the limiter inputs of this stage
-    const size_t stBytes = (size_t)h->N * h->Kp * sizeof(T);
-    if (lin && mode == 2 && h->recCdot[s]) copy_state(h, h->recCdot[s], tb, stBytes);
-    if (lin && mode == 1 && h->recY[s]) copy_state(h, h->recY[s], tb, stBytes);
     LimOut<T> loS = lo1;
     if (mode == 2) {
       const LimOut<T> lo2 = lim_out<T>(h);
       ++h->limPass;
       prof_mark(h, 1);
-      if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)in, (const T *)cn, (const T *)tb, tb, lim_in<T>(lo1, h), lo2, sc);
+      if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)in, (const T *)cn, (const T *)cdB, yB, lim_in<T>(lo1, h), lo2, sc);
       else if (h->limType == DGADV_LIM_STRICT)
         launch_k(h, k_limit_dot<T, P, 2>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
       else
         launch_k(h, k_limit_dot<T, P, 1>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
       prof_mark(h, -1);
-      if (lin && h->recY[s]) copy_state(h, h->recY[s], tb, stBytes);
       loS = lo2;
     }
     prof_mark(h, 2);
-    if (lin) launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
+    if (lin) launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)yB, out, lim_in<T>(loS, h), scBC);
     else if (h->limType == DGADV_LIM_STRICT)
       launch_k(h, k_limit<T, P, 2>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
     else
