@@ -1,0 +1,87 @@
+"""The autotuners' host logic on a fake solver (no GPU): every candidate is timed, the fastest is
+applied, the state is restored, and a stored choice is reused without timing."""
+import json
+
+import numpy as np
+
+from festung_gb300 import _lib as L
+from festung_gb300 import autotune as AT
+
+
+class FakeSolver:
+    """Records the calls the tuners make; a launch option's cost comes from `cost`."""
+
+    K, p, limiter = 128, 2, 'linear'
+
+    def __init__(self, cost):
+        self.cost = cost
+        self.options = {L.OPT_FLAGS: 0, L.OPT_GRAPH_STEPS: 12, L.OPT_ADJ_WARPS: 2}
+        self.state = np.arange(12.0).reshape(4, 3)
+        self.calls = []
+
+    def set_option(self, option, value):
+        self.options[option] = value
+
+    def get_option(self, option):
+        return self.options[option]
+
+    def get_state(self):
+        return self.state.copy()
+
+    def set_state(self, c):
+        self.state = np.array(c, copy=True)
+
+    def time_steps(self, nSteps, nStep0, tau):
+        self.calls.append(('steps', self.options[L.OPT_FLAGS], self.options[L.OPT_GRAPH_STEPS]))
+        self.state = self.state + 1.0   # the tuner must put the state back
+        return nSteps * self.cost(self.options)
+
+    def forward_record(self, nSteps, tau, nSnapshots):
+        self.calls.append(('record', self.options[L.OPT_ADJ_WARPS], nSnapshots))
+        self.state = self.state + 1.0
+
+    def backward(self, g):
+        self.calls.append(('backward', self.options[L.OPT_ADJ_WARPS]))
+        _now[0] += 1e-3 * self.cost(self.options)   # the tuner's (fake) wall clock sees the cost
+        return np.zeros_like(g), None
+
+
+_now = [0.0]
+
+
+def test_tune_adjoint_times_every_width_and_applies_the_fastest(monkeypatch):
+    _now[0] = 0.0
+    monkeypatch.setattr(AT.time, 'perf_counter', lambda: _now[0])
+    costs = {1: 3.0, 2: 1.0, 4: 5.0}
+    s = FakeSolver(lambda o: costs[o[L.OPT_ADJ_WARPS]])
+    before = s.get_state()
+    best, table = AT.tune_adjoint(s, 1e-3, nSteps=4, nSnapshots=2, reps=2)
+    assert [r['adjWarps'] for r in table] == [1, 2, 4]
+    assert best['adjWarps'] == 2 and s.get_option(L.OPT_ADJ_WARPS) == 2
+    assert np.array_equal(s.get_state(), before)
+    # every width: reps + 1 recorded runs (the first captures the sweep's graph), each with the
+    # requested snapshots, and a backward after each
+    for w in (1, 2, 4):
+        assert s.calls.count(('record', w, 2)) == 3
+        assert s.calls.count(('backward', w)) == 3
+
+
+def test_tune_picks_the_fastest_launch_configuration_and_caches_it(tmp_path):
+    def cost(o):
+        return 1.0 + (0.5 if o[L.OPT_FLAGS] & L.FLAG_NO_PDL else 0.0) + abs(o[L.OPT_GRAPH_STEPS] - 24) / 100
+
+    s = FakeSolver(cost)
+    before = s.get_state()
+    cache = str(tmp_path / 'tune.json')
+    best, table = AT.tune(s, 1e-3, nSteps=8, reps=2, fused_ok=True, cache=cache, key='k')
+    assert len(table) == 2 * 2 * len(AT.GRAPH_STEPS)
+    assert best['graphSteps'] == 24 and not best['flags'] & L.FLAG_NO_PDL
+    assert s.get_option(L.OPT_GRAPH_STEPS) == 24
+    assert np.array_equal(s.get_state(), before)
+    stored = json.load(open(cache))
+    assert stored['k']['best']['graphSteps'] == 24
+    # a second call with the same key applies the stored choice without timing anything
+    s2 = FakeSolver(cost)
+    best2, _ = AT.tune(s2, 1e-3, cache=cache, key='k')
+    assert best2 == stored['k']['best'] and s2.calls == []
+    assert s2.get_option(L.OPT_GRAPH_STEPS) == 24
