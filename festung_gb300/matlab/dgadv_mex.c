@@ -13,6 +13,12 @@
  *   dgadv_mex('step', h, nSteps, nStep0, tau)
  *   cDisc = dgadv_mex('get_state', h)
  *   dgadv_mex('destroy', h)
+ * Launch options and the discrete adjoint (no counterpart in the reference):
+ *   dgadv_mex('set_option', h, option, value);  value = dgadv_mex('get_option', h, option)
+ *   dgadv_mex('set_velocity_modes', h, u1Modes, u2Modes, vNModes)   % K x N x M, K x N x M, K x 3R x M
+ *   dgadv_mex('set_velocity_theta', h, theta)                       % M coefficients
+ *   dgadv_mex('forward_record', h, nSteps, tau, nSnapshots)         % 0: every stage stored
+ *   [dJdc0, dJdtheta] = dgadv_mex('backward', h, dJdcT)             % dJdcT: K x N
  * Arrays keep Matlab's layout (column-major), integer inputs are converted from 1-based doubles
  * to 0-based int32 here.  Every non-zero status becomes a Matlab error with the library's
  * message.  Handles are uint64 scalars; mexAtExit destroys the ones still open.
@@ -27,6 +33,13 @@
 
 #define MAX_HANDLES 64
 static dgadv_handle *g_open[MAX_HANDLES];
+static int32_t g_nmodes[MAX_HANDLES];   /* velocity modes set on each open handle */
+
+static int slot_of(const dgadv_handle *h) {
+  for (int i = 0; i < MAX_HANDLES; ++i)
+    if (g_open[i] == h) return i;
+  return -1;
+}
 
 static void cleanup(void) {
   for (int i = 0; i < MAX_HANDLES; ++i)
@@ -112,6 +125,7 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     for (int i = 0; i < MAX_HANDLES; ++i) if (!g_open[i]) { slot = i; break; }
     if (slot < 0) { dgadv_destroy(h); mexErrMsgIdAndTxt("dgadv:arg", "too many open handles"); }
     g_open[slot] = h;
+    g_nmodes[slot] = 0;
     plhs[0] = mxCreateNumericMatrix(1, 1, mxUINT64_CLASS, mxREAL);
     *(uint64_t *)mxGetData(plhs[0]) = (uint64_t)(uintptr_t)h;
     return;
@@ -183,8 +197,33 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     check(dgadv_output(h, var, file, (int32_t)mxGetScalar(prhs[4]), (int32_t)mxGetScalar(prhs[5])), h);
   } else if (!strcmp(cmd, "output_wait")) {
     check(dgadv_output_wait(h), h);
+  } else if (!strcmp(cmd, "set_option")) {
+    check(dgadv_set_option(h, (int32_t)mxGetScalar(prhs[2]), (int32_t)mxGetScalar(prhs[3])), h);
+  } else if (!strcmp(cmd, "get_option")) {
+    int32_t v = 0;
+    check(dgadv_get_option(h, (int32_t)mxGetScalar(prhs[2]), &v), h);
+    plhs[0] = mxCreateDoubleScalar((double)v);
+  } else if (!strcmp(cmd, "set_velocity_modes")) {
+    /* the modes run along the third dimension of each array */
+    const mwSize nd = mxGetNumberOfDimensions(prhs[2]);
+    const int32_t nm = nd > 2 ? (int32_t)mxGetDimensions(prhs[2])[2] : 1;
+    check(dgadv_set_velocity_modes(h, nm, mxGetPr(prhs[2]), mxGetPr(prhs[3]), mxGetPr(prhs[4])), h);
+    g_nmodes[slot_of(h)] = nm;
+  } else if (!strcmp(cmd, "set_velocity_theta")) {
+    check(dgadv_set_velocity_theta(h, mxGetPr(prhs[2])), h);
+  } else if (!strcmp(cmd, "forward_record")) {
+    check(dgadv_forward_record(h, (int32_t)mxGetScalar(prhs[2]), mxGetScalar(prhs[3]),
+                               (int32_t)mxGetScalar(prhs[4])), h);
+  } else if (!strcmp(cmd, "backward")) {
+    /* dJdc0 has dJdcT's shape; dJdtheta one entry per velocity mode (empty without modes) */
+    const mwSize K = (mwSize)mxGetM(prhs[2]), N = (mwSize)(mxGetNumberOfElements(prhs[2]) / (K ? K : 1));
+    const int32_t nm = g_nmodes[slot_of(h)];
+    plhs[0] = mxCreateDoubleMatrix(K, N, mxREAL);
+    mxArray *g = mxCreateDoubleMatrix((mwSize)nm, nm ? 1 : 0, mxREAL);
+    check(dgadv_backward(h, dbl(prhs[2], (size_t)K * N, "dJdcT"), mxGetPr(plhs[0]), nm ? mxGetPr(g) : NULL), h);
+    if (nlhs > 1) plhs[1] = g; else mxDestroyArray(g);
   } else if (!strcmp(cmd, "destroy")) {
-    for (int i = 0; i < MAX_HANDLES; ++i) if (g_open[i] == h) g_open[i] = NULL;
+    for (int i = 0; i < MAX_HANDLES; ++i) if (g_open[i] == h) { g_open[i] = NULL; g_nmodes[i] = 0; }
     dgadv_destroy(h);
   } else {
     mexErrMsgIdAndTxt("dgadv:arg", "unknown command %s", cmd);
