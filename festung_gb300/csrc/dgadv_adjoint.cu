@@ -7,9 +7,11 @@
 // automatic differentiation"): with s free slots and t steps, let r be the smallest integer with
 // beta(s, r) = C(s + r, s) >= t; advance to a split point m = a + max(1, t - beta(s - 1, r)),
 // store c^m, reverse [m, b) with s - 1 free slots, then [a, m) with s.  No step is recomputed
-// more than r times.  With as many slots as steps every state is stored once and nothing is
-// recomputed.  Each reversed step recomputes its own RK stages from c^i (one forward step)
-// before the adjoint stages run.
+// more than r times.  With as many slots as steps every state is stored once; unless the
+// record also kept every stage state, each reversed step then recomputes, from c^i, the stages
+// its reverse stages read (the first S - 1 stages; with the limiter the whole step, whose
+// limiter inputs the limiter adjoint reads).  Checkpoints are read and written in place: no
+// state is copied into or out of a slot.
 #include <cuda_runtime.h>
 
 #include <algorithm>
