@@ -98,6 +98,21 @@ def test_checkpoint_schedule_reverses_every_step_within_its_slots(lib, nSteps, n
         assert advanced.max() <= 1      # every state stored once, nothing recomputed
 
 
+def test_gradient_workload_schedule_recomputes_what_the_cost_model_says(lib):
+    """200 steps with 20 slots: the record's checkpointing actions advance 199 steps (the last
+    step follows them), and the reverse sweep advances 180 steps, stores 180 checkpoints and
+    reverses 200 steps (each of which recomputes two of its three SSP-RK3 stages in the
+    unlimited scheme)."""
+    from festung_gb300 import _lib as L
+    actions, start = L.checkpoint_schedule(200, 20)
+    a = np.asarray(actions).reshape(-1, 2)
+    fwd, bwd = a[:start], a[start:]
+    assert fwd[fwd[:, 0] == 1, 1].sum() == 199
+    assert bwd[bwd[:, 0] == 1, 1].sum() == 180
+    assert (bwd[:, 0] == 3).sum() == 200
+    assert (bwd[:, 0] == 2).sum() == 180
+
+
 @pytest.mark.parametrize('p,steps', [(1, 6), (2, 6), (3, 3)])
 def test_limited_oracle_gradient_matches_finite_differences(p, steps):
     """The scheme with the linear limiter.  The limiter is piecewise rational; directions scaled
