@@ -41,20 +41,32 @@ __global__ void k_na_reset(unsigned long long *s, int numV) {
 
 // Element means (the centroid values) scattered to the three vertices' keys and to the
 // global extremes (core/computeMinMaxV0TElementPatch.m).
+// The three vertex ids of element k, and whether all lie in [0, numV) (numV never exceeds the
+// scratch array's vertex slots).  Elements with an id outside that range take no part in any
+// patch and are not limited: their output is NaN, so that the caller sees the bad input.
+__device__ __forceinline__ bool na_vertices(const int *V0T, int K, int numV, int k, int vid[3]) {
+  bool ok = true;
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    vid[n] = V0T[(size_t)n * K + k];
+    ok &= (unsigned)vid[n] < (unsigned)numV;
+  }
+  return ok;
+}
+
 template <int P>
 __global__ void __launch_bounds__(kBlock)
-k_na_scatter(int K, const int *__restrict__ V0T, const double *__restrict__ c, unsigned long long *s) {
+k_na_scatter(int K, int numV, const int *__restrict__ V0T, const double *__restrict__ c, unsigned long long *s) {
   constexpr int N = Dims<P>::N;
   const int k = blockIdx.x * kBlock + threadIdx.x;
-  const bool active = k < K;
   Geo<double> g{};
   g.Vp = kNoAllocMaxVertices;
   LimOut<double> lo{};
   lo.vkeys = s; lo.slots = s + 2 * kNoAllocMaxVertices; lo.nc = 1; lo.type = 0;
   int vid[3] = {0, 0, 0};
+  const bool active = k < K && na_vertices(V0T, K, numV, k, vid);
   double q0 = 0.0;
   if (active) {
-    vid[0] = V0T[k]; vid[1] = V0T[K + k]; vid[2] = V0T[2 * K + k];
     double cc[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) cc[i] = c[(size_t)i * K + k];
@@ -67,21 +79,25 @@ k_na_scatter(int K, const int *__restrict__ V0T, const double *__restrict__ c, u
 // core/computeVertexBasedLimiter.m): c <- c - DM^-1 du, Dirichlet data where markD is set.
 template <int P>
 __global__ void __launch_bounds__(kBlock)
-k_na_limit(int K, const int *__restrict__ V0T, const uint8_t *__restrict__ markD,
+k_na_limit(int K, int numV, const int *__restrict__ V0T, const uint8_t *__restrict__ markD,
            const double *__restrict__ dataD, const double *cin, double *cout, const unsigned long long *s) {
   constexpr int N = Dims<P>::N;
   const Tab<double, P> &tb = tab<double, P>();
   __shared__ double sh[2];
   const int k = blockIdx.x * kBlock + threadIdx.x;
-  const bool active = k < K;
   Geo<double> g{};
   g.Vp = kNoAllocMaxVertices;
   LimIn<double> li{};
   li.vkeys = s; li.slots = s + 2 * kNoAllocMaxVertices; li.nc = 1; li.type = 0; li.shift = 1;
   load_shifts<double>(li.slots, 1, sh);
   __syncthreads();
-  if (!active) return;
-  const int vid[3] = {V0T[k], V0T[K + k], V0T[2 * K + k]};
+  if (k >= K) return;
+  int vid[3];
+  if (!na_vertices(V0T, K, numV, k, vid)) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) cout[(size_t)i * K + k] = __longlong_as_double(0x7FF8000000000000LL);
+    return;
+  }
   int dmask = 0;
   double data[3] = {0.0, 0.0, 0.0};
   if (markD)
@@ -112,8 +128,8 @@ static cudaError_t na_launch(int K, int numV, const int *V0T, const uint8_t *mar
                              const double *cin, double *cout, unsigned long long *s, cudaStream_t st) {
   k_na_reset<<<(numV + 255) / 256, 256, 0, st>>>(s, numV);
   const int grid = (K + kBlock - 1) / kBlock;
-  k_na_scatter<P><<<grid, kBlock, 0, st>>>(K, V0T, cin, s);
-  k_na_limit<P><<<grid, kBlock, 0, st>>>(K, V0T, markD, dataD, cin, cout, s);
+  k_na_scatter<P><<<grid, kBlock, 0, st>>>(K, numV, V0T, cin, s);
+  k_na_limit<P><<<grid, kBlock, 0, st>>>(K, numV, V0T, markD, dataD, cin, cout, s);
   return cudaGetLastError();
 }
 

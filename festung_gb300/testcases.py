@@ -108,6 +108,11 @@ def mode_velocity(m):
     return streamfunction_velocity([k], [l], [1.0])
 
 
+# The explicit problem's test cases (configure below; the Matlab folder's configureProblem.m
+# defines the same names).
+TESTCASES = ('solid_body', 'transient', 'gauss_slot', 'ensemble', 'adjoint')
+
+
 def configure(pd):
     """Sets c0Cont, u1Cont, u2Cont (time-independent), fTerms, cDTerms, mesh parameters."""
     tc = pd['testcase']

@@ -366,7 +366,9 @@ int dgadv_checkpoint_schedule(int32_t nSteps, int32_t nSnapshots, int32_t *actio
  * Same result as one solution-limiter pass of a handle created with typeSlopeLim =
  * DGADV_LIM_LINEAR and precision DGADV_FP64 (FP64 arithmetic, the reference's global shift).
  * Device arrays, column-major in element order, 0-based ids:
- *   V0T          numT x 3 int32 vertex ids, each < numV
+ *   V0T          numT x 3 int32 vertex ids, each in [0, numV); the kernels check this, and an
+ *                element with an id outside that range enters no vertex patch and gets NaN in
+ *                every coefficient of cOut (no memory outside the arrays is touched)
  *   markV0TbdrD  numT x 3 uint8, non-zero at Dirichlet vertices (NULL: none)
  *   dataV0T      numT x 3 Dirichlet values at those vertices (NULL: zero)
  *   cIn, cOut    numT x N modal coefficients, N = (p+1)(p+2)/2; cOut may equal cIn

@@ -56,3 +56,19 @@ def test_gateway_compiles_against_the_header(tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 
+
+
+def test_matlab_problem_folder_is_complete():
+    """The advection_gpu folder holds every step function main.m and iterateSubSteps look up
+    (core/getStepLists.m) and configures every test case of the Python mirror."""
+    from festung_gb300.testcases import TESTCASES
+    d = os.path.join(ROOT, 'festung_gb300', 'matlab', 'advection_gpu')
+    steps = ('configureProblem', 'preprocessProblem', 'initializeProblem', 'preprocessStep', 'solveStep',
+             'postprocessStep', 'outputStep', 'postprocessProblem', 'preprocessSubStep', 'solveSubStep',
+             'postprocessSubStep')
+    for f in steps:
+        src = open(os.path.join(d, f + '.m')).read()
+        assert 'function problemData = %s(' % f in src, f
+    conf = open(os.path.join(d, 'configureProblem.m')).read()
+    for tc in TESTCASES:
+        assert "'%s'" % tc in conf, tc

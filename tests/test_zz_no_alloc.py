@@ -55,18 +55,20 @@ def _with_handle(cs):
         s.close()
 
 
-def _no_alloc(cs):
-    """Device arrays are made by the test (the caller); the entry point itself allocates none."""
+def _no_alloc(cs, in_place=False, V0T=None):
+    """Device arrays are made by the test (the caller); the entry point itself allocates none.
+    in_place: cOut is cIn.  V0T: vertex ids to pass instead of the case's own."""
     import torch
     from festung_gb300 import _lib as L
     lib = L.load()
     dev = torch.device('cuda:0')
     K, N = cs['c'].shape
-    V0T = torch.from_numpy(np.asfortranarray(cs['V0T'], dtype=np.int32).T.copy()).to(dev)   # 3 x K
+    ids = cs['V0T'] if V0T is None else V0T
+    V0T = torch.from_numpy(np.asfortranarray(ids, dtype=np.int32).T.copy()).to(dev)          # 3 x K
     mark = torch.from_numpy(cs['markV0TbdrD'].T.copy()).to(dev)
     data = torch.from_numpy(cs['data'].T.copy()).to(dev) if cs['data'] is not None else None
     cin = torch.from_numpy(cs['c'].T.copy()).to(dev)                                          # N x K
-    cout = torch.full_like(cin, float('nan'))
+    cout = cin if in_place else torch.full_like(cin, float('nan'))
     stream = torch.cuda.current_stream(dev)
     st = lib.dgadv_limit_linear_noalloc(cs['p'], K, cs['coordV'].shape[0], V0T.data_ptr(), mark.data_ptr(),
                                         data.data_ptr() if data is not None else None,
@@ -88,6 +90,37 @@ def test_no_alloc_matches_handle_two_calls():
         assert np.all(np.isfinite(got))
         assert not np.array_equal(ref, cs['c']), 'the limiter changed nothing: the case checks nothing'
         assert rel(got, ref) <= FP64_TOL, rel(got, ref)
+
+
+def test_no_alloc_in_place():
+    """cOut may be cIn: each element reads only its own coefficients after the patch pass."""
+    torch = pytest.importorskip('torch')
+    if not torch.cuda.is_available():
+        pytest.skip('no GPU')
+    cs = _case(2 ** -5, p=2, seed=11, jitter=0.2, with_data=True)
+    got = _no_alloc(cs, in_place=True)
+    ref = _with_handle(cs)
+    assert rel(got, ref) <= FP64_TOL, rel(got, ref)
+
+
+def test_no_alloc_skips_out_of_range_vertex():
+    """A vertex id outside [0, numV) is checked by the kernels: that element enters no patch and
+    its output is NaN; the other elements stay finite, and the next call is unaffected."""
+    torch = pytest.importorskip('torch')
+    if not torch.cuda.is_available():
+        pytest.skip('no GPU')
+    from festung_gb300 import _lib as L
+    cs = _case(2 ** -4, p=1, seed=12, jitter=0.1, with_data=False)
+    numV = cs['coordV'].shape[0]
+    bad = np.array(cs['V0T'], dtype=np.int64)
+    bad[5, 1] = L.NOALLOC_MAX_VERTICES + 7       # beyond the scratch array's vertex slots
+    bad[9, 2] = numV                              # one past the last vertex
+    got = _no_alloc(cs, V0T=bad)
+    assert np.all(np.isnan(got[[5, 9]]))
+    others = np.setdiff1d(np.arange(got.shape[0]), [5, 9])
+    assert np.all(np.isfinite(got[others]))
+    good = _no_alloc(cs)
+    assert rel(good, _with_handle(cs)) <= FP64_TOL
 
 
 def test_no_alloc_rejects_oversize():
