@@ -236,6 +236,8 @@ def preprocessProblem(pd):
                              isSlopeLim=pd.isSlopeLim, typeSlopeLim=pd.typeSlopeLim,
                              idE0T=m['idE0T'], markE0TbdrD=m['markE0TbdrD'],
                              markE0TbdrN=m['markE0TbdrN'], device=pd.device, flags=pd.gpuFlags)
+    for opt, val in (pd.get('gpuOptions') or {}).items():     # {DGADV_OPT_*: value}
+        pd.solver.set_option(opt, val)
     if pd.deviceFns:
         pd.solver.set_velocity_function(pd.deviceFns['u'])
     else:

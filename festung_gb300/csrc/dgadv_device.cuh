@@ -251,6 +251,81 @@ __device__ __forceinline__ void from_taylor(const T *cT, const Affine<T> &af, T 
   }
 }
 
+// Blocks of S^-1 (Taylor coefficients -> reference derivatives at the barycentre) per degree d:
+// Si[d][m][j] = dX^d times the coefficient of z^j in (B11 + B21 z)^(d-m) (B12 + B22 z)^m, the
+// map from_taylor applies (block 0 is 1).
+template <typename T, int P> struct SinvBlocks {
+  T b[P + 1][P + 1][P + 1];
+};
+template <typename T, int P>
+__device__ __forceinline__ void sinv_blocks(const Affine<T> &af, SinvBlocks<T, P> &si) {
+  si.b[0][0][0] = T(1);
+  T sc = T(1);
+#pragma unroll
+  for (int d = 1; d <= P; ++d) {
+    sc *= af.dX;
+    if (d == 1) {
+      T S[2][2]; deriv_block<T, 1>(af.B11, af.B21, af.B12, af.B22, S);
+#pragma unroll
+      for (int m = 0; m <= 1; ++m)
+#pragma unroll
+        for (int j = 0; j <= 1; ++j) si.b[1][m][j] = S[m][j] * sc;
+    } else if (d == 2) {
+      T S[3][3]; deriv_block<T, 2>(af.B11, af.B21, af.B12, af.B22, S);
+#pragma unroll
+      for (int m = 0; m <= 2; ++m)
+#pragma unroll
+        for (int j = 0; j <= 2; ++j) si.b[2][m][j] = S[m][j] * sc;
+    } else if (d == 3) {
+      T S[4][4]; deriv_block<T, 3>(af.B11, af.B21, af.B12, af.B22, S);
+#pragma unroll
+      for (int m = 0; m <= 3; ++m)
+#pragma unroll
+        for (int j = 0; j <= 3; ++j) si.b[3][m][j] = S[m][j] * sc;
+    }
+  }
+}
+
+// Taylor mass correction without a stored mass block (advection/solveSubStep.m:69-80 with
+// Mcorr = diag(1/diag(M_T)) M_T, advection/preprocessProblem.m:107-111).  With u = DM c the
+// reference derivatives and S the map u -> Taylor coefficients, an element's Taylor mass block
+// is M_T = 2|T| S^-T Gr S^-1 (Gr = DM^-T hatM DM^-1, a constant table).  For a Taylor-space
+// difference d given as y = S^-1 d (y_0 = 0), this returns
+//     m = Mcorr d = diag(D)^-1 S^-T Gr y,   D_i = (S^-T Gr S^-1)_ii,
+// the factor 2|T| cancelling.  S^-1 is block diagonal per degree, so D_i involves only the
+// diagonal block of Gr of its degree.
+template <typename T, int P>
+__device__ __forceinline__ void taylor_mcorr(const SinvBlocks<T, P> &si, const T *y, T *m) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T gy[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    Acc<T> s(T(0));
+#pragma unroll
+    for (int j = 1; j < N; ++j) s.fma(tb.Gr[i][j], y[j]);
+    gy[i] = s.get();
+  }
+  m[0] = gy[0] / tb.Gr[0][0];
+#pragma unroll
+  for (int d = 1; d <= P; ++d) {
+    const int off = d * (d + 1) / 2;
+#pragma unroll
+    for (int j = 0; j <= d; ++j) {
+      Acc<T> t(T(0)), D(T(0));
+#pragma unroll
+      for (int a = 0; a <= d; ++a) {
+        t.fma(si.b[d][a][j], gy[off + a]);
+        Acc<T> r(T(0));
+#pragma unroll
+        for (int b = 0; b <= d; ++b) r.fma(tb.Gr[off + a][off + b], si.b[d][b][j]);
+        D.fma(si.b[d][a][j], r.get());
+      }
+      m[off + j] = t.get() / D.get();
+    }
+  }
+}
+
 // Index of the Taylor DOF with multi-index (a1, a2) (core/mult2ind.m:57-62, 0-based).
 __host__ __device__ constexpr int mind(int a1, int a2) { return (a1 + a2) * (a1 + a2 + 1) / 2 + a2; }
 
@@ -507,8 +582,9 @@ template <typename T, int P> struct StageRows {
   __host__ __device__ static constexpr int limdot() { return N + 4 + 2 * N; }
   // k_limit: tbuf, B | code
   __host__ __device__ static constexpr int lim() { return N + 4; }
-  // k_limit_dot_lin: cDot, Q (N x (N-1)), c0, cin | code
-  __host__ __device__ static constexpr int limdot_lin() { return N + N * (N - 1) + 2 * N; }
+  // k_limit_dot_lin: cDot, Q (N x (N-1)) or B (4), c0, cin | code
+  __host__ __device__ static constexpr int limdot_lin_rows(bool fly) { return 3 * N + (fly ? 4 : N * (N - 1)); }
+  __host__ __device__ static constexpr int limdot_lin() { return limdot_lin_rows(N * (N - 1) < 4); }
   // k_to_taylor: c, B
   __host__ __device__ static constexpr int totaylor() { return N + 4; }
   // rows first, then the block's mbarrier (8 bytes, 16 reserved)
@@ -982,26 +1058,48 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
     T d[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) d[i] = cT[i] - lim[i];
-    T acc[N], dii[N];
+    T cor[N];
+    if (g.mtOnTheFly) {
+      // Mcorr d from B and the constant Gram table: y = S^-1 d, then taylor_mcorr
+      SinvBlocks<T, P> si;
+      sinv_blocks<T, P>(af, si);
+      T y[N], m[N];
+      y[0] = d[0];
 #pragma unroll
-    for (int i = 0; i < N; ++i) { acc[i] = T(0); dii[i] = T(1); }
+      for (int dd = 1; dd <= P; ++dd) {
+        const int off = dd * (dd + 1) / 2;
 #pragma unroll
-    for (int a = 0; a < N; ++a)
+        for (int a = 0; a <= dd; ++a) {
+          Acc<T> sy(T(0));
 #pragma unroll
-      for (int b = a; b < N; ++b) {
-        const int idx = a * N - a * (a - 1) / 2 + (b - a);
-        const T m = g.MT[(size_t)idx * Kp + k];
-        if (a == b) {
-          acc[a] += m * d[a];
-          dii[a] = m;
-        } else {
-          acc[a] += m * d[b];
-          acc[b] += m * d[a];
+          for (int j = 0; j <= dd; ++j) sy.fma(si.b[dd][a][j], d[off + j]);
+          y[off + a] = sy.get();
         }
       }
-    T cor[N];
+      taylor_mcorr<T, P>(si, y, m);
 #pragma unroll
-    for (int i = 0; i < N; ++i) cor[i] = lim[i] + acc[i] / dii[i];
+      for (int i = 0; i < N; ++i) cor[i] = lim[i] + m[i];
+    } else {
+      T acc[N], dii[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) { acc[i] = T(0); dii[i] = T(1); }
+#pragma unroll
+      for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int b = a; b < N; ++b) {
+          const int idx = a * N - a * (a - 1) / 2 + (b - a);
+          const T m = g.MT[(size_t)idx * Kp + k];
+          if (a == b) {
+            acc[a] += m * d[a];
+            dii[a] = m;
+          } else {
+            acc[a] += m * d[b];
+            acc[b] += m * d[a];
+          }
+        }
+#pragma unroll
+      for (int i = 0; i < N; ++i) cor[i] = lim[i] + acc[i] / dii[i];
+    }
     T cdot[N];
     from_taylor<T, P>(cor, af, cdot);
     const T w = T(sc.omega), tau = T(sc.tau);
@@ -1116,14 +1214,18 @@ k_to_taylor(const Geo<T> g, const T *c, T *__restrict__ tbuf, const LimOut<T> lo
   scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok);
 }
 
-// Time-derivative limiting and SSP update for the linear limiter: cDot += Q_k du with the
-// precomputed Q_k = DM^-1 (S_k^-1 Mcorr_k S_k - I) (advection/solveSubStep.m:69-83); the new
-// stage value is written in the modal basis and its mean scattered for the solution limiter.
+// Time-derivative limiting and SSP update for the linear limiter: cDot += Q_k du with
+// Q_k = DM^-1 (S_k^-1 Mcorr_k S_k - I) (advection/solveSubStep.m:69-83), either read as
+// precomputed rows or, with g.mtOnTheFly, applied from the element's B and the constant Gram
+// table (taylor_mcorr; 4 staged rows instead of N(N-1)); the new stage value is written in the
+// modal basis and its mean scattered for the solution limiter.
 template <typename T, int P>
 __device__ __forceinline__ void limit_dot_lin_tile(const Geo<T> g, const T *cin, const T *c0, const T *tbuf,
                 T *out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc, const int tile) {
   constexpr int N = Dims<P>::N, NQ = 1;
-  constexpr int NT = StageRows<T, P>::limdot_lin();
+  // staged rows: cDot, then N(N-1) rows of Q_k or the 4 rows of B, then c^n and c^(s-1)
+  const bool fly = g.mtOnTheFly != 0;
+  const int NT = StageRows<T, P>::limdot_lin_rows(fly);
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
   const int t = threadIdx.x, k0 = tile * kBlock, k = k0 + t;
@@ -1131,13 +1233,14 @@ __device__ __forceinline__ void limit_dot_lin_tile(const Geo<T> g, const T *cin,
   pdl_trigger();
   const int Kp = g.Kp;
   const bool staged = k0 < g.K;
-  constexpr int rD = 0, rQ = N, rC0 = N + N * (N - 1), rC = rC0 + N;
+  const int rD = 0, rQ = N, rC0 = NT - 2 * N, rC = rC0 + N;
   if (staged) {
     if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
     __syncthreads();
     if (t == 0) {
       stage_expect<T>(bar, NT, 1);
-      stage_T(smem, rQ, g.MT, N * (N - 1), Kp, k0, bar);
+      if (fly) stage_T(smem, rQ, g.Bm, 4, Kp, k0, bar);
+      else stage_T(smem, rQ, g.MT, N * (N - 1), Kp, k0, bar);
       stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
     }
   }
@@ -1167,12 +1270,41 @@ __device__ __forceinline__ void limit_dot_lin_tile(const Geo<T> g, const T *cin,
     const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
     const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
     if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, nan3, du)) {
+      if (fly) {
+        const Affine<T> af = affine_from<T>(srow<T>(smem, rQ)[t], srow<T>(smem, rQ + 1)[t],
+                                            srow<T>(smem, rQ + 2)[t], srow<T>(smem, rQ + 3)[t]);
+        SinvBlocks<T, P> si;
+        sinv_blocks<T, P>(af, si);
+        T m[N], z[N];
+        taylor_mcorr<T, P>(si, du, m);               // Mcorr S du, Taylor coordinates
+        z[0] = m[0] - du[0];                         // S^-1 Mcorr S du - du
 #pragma unroll
-      for (int i = 0; i < N; ++i) {
-        Acc<T> s(cd[i]);
+        for (int dd = 1; dd <= P; ++dd) {
+          const int off = dd * (dd + 1) / 2;
 #pragma unroll
-        for (int j = 1; j < N; ++j) s.fma(srow<T>(smem, rQ + i * (N - 1) + (j - 1))[t], du[j]);
-        cd[i] = s.get();
+          for (int a = 0; a <= dd; ++a) {
+            Acc<T> sz(T(0));
+#pragma unroll
+            for (int j = 0; j <= dd; ++j) sz.fma(si.b[dd][a][j], m[off + j]);
+            z[off + a] = sz.get() - du[off + a];
+          }
+        }
+        const Tab<T, P> &tbl = tab<T, P>();
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          Acc<T> s(cd[i]);
+#pragma unroll
+          for (int j = 0; j < N; ++j) s.fma(tbl.DMinv[i][j], z[j]);
+          cd[i] = s.get();
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          Acc<T> s(cd[i]);
+#pragma unroll
+          for (int j = 1; j < N; ++j) s.fma(srow<T>(smem, rQ + i * (N - 1) + (j - 1))[t], du[j]);
+          cd[i] = s.get();
+        }
       }
     }
     const T w = T(sc.omega), tau = T(sc.tau);

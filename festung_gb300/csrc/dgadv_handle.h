@@ -47,6 +47,7 @@ struct dgadv_handle {
   void *stepDst = nullptr;
   int stepStages = 0;
   int adjWarps = 2;                    // warps per role of the FP32 adjoint stage (1, 2 or 4)
+  bool mtOnTheFly = false;             // Taylor mass correction rebuilt from B (DGADV_OPT_TAYLOR_MASS)
   void *cR = nullptr, *cnL = nullptr, *cLx = nullptr;   // fused path: raw step output, limited c^n / c^(s-1)
   void *vkeys = nullptr;               // 3 passes x nc x 2 x Vp vertex min / max keys
   unsigned long long *gmm = nullptr;   // 3 passes x kSlotCopies x 2 x nc encoded global extremes

@@ -32,6 +32,8 @@ template <typename T, int P> struct Tab {
   T hatMinv[N][N];
   T DM[N][N];         // modal -> reference derivatives at the barycentre (times hatM)
   T DMinv[N][N];
+  T Gr[N][N];         // Gram matrix of the reference-derivative basis, DM^-T hatM DM^-1 (the
+                      // Taylor mass block of an element is 2|T| S^-T Gr S^-1)
   // adjoint: the transposed mass solve folded into the test-function tables,
   // Hg1[q][j] = sum_i g1[q][i] hatMinv[i][j] (likewise Hg2, Hphi), or the tables themselves
   // where the forward path uses hatM = I (FP32)
@@ -49,7 +51,10 @@ template <typename T> struct Geo {
   const int *code;   // Kp       bits 2n..2n+1: neighbour's local edge; bit 6+n: outflow counted;
                      //          bit 9+n: local vertex n lies on a Dirichlet edge
   const T *Bm;       // 4 x Kp   B11, B12, B21, B22
-  const T *MT;       // NMT x Kp packed Taylor mass blocks (time-derivative limiting)
+  const T *MT;       // time-derivative limiting: NMT x Kp packed Taylor mass blocks
+                     // (hierarchical / strict) or N(N-1) x Kp rows of Q_k (linear)
+  int mtOnTheFly;    // forward kernels rebuild the Taylor mass correction from B and Gr instead
+                     // of reading MT (the limiter adjoint still reads MT)
   const int *V0T;    // 3 x Kp   vertex ids
   const int *vptr;   // numV+1   CSR vertex -> elements
   const int *vidx;

@@ -32,6 +32,17 @@ static cudaError_t upload_tables(const RefTables &rt) {
       t.DM[i][j] = T(rt.DM[i * N + j]);
       t.DMinv[i][j] = T(rt.DMinv[i * N + j]);
     }
+  // Gr = DM^-T hatM DM^-1 in FP64, then rounded
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      double s = 0.0;
+      for (int a = 0; a < N; ++a) {
+        double r = 0.0;
+        for (int b = 0; b < N; ++b) r += rt.hatM[a * N + b] * rt.DMinv[b * N + j];
+        s += rt.DMinv[a * N + i] * r;
+      }
+      t.Gr[i][j] = T(s);
+    }
   // adjoint tables (the forward FP32 path takes hatM^-1 = I; so does its adjoint)
   const bool massSolve = sizeof(T) == 8;
   auto fold = [&](const double *row, int j) {
@@ -61,6 +72,7 @@ static Geo<T> make_geo(const dgadv_handle *h) {
   for (int i = 0; i < 4; ++i) g.timeFn[i] = h->timeFn[i];
   g.instOf = h->instOf;
   g.nInst = h->nInst;
+  g.mtOnTheFly = h->mtOnTheFly ? 1 : 0;
   g.permv = h->perm;
   return g;
 }
@@ -274,7 +286,7 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
       const LimOut<T> lo2 = lim_out<T>(h);
       ++h->limPass;
       prof_mark(h, 1);
-      if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)in, (const T *)cn, (const T *)cdB, yB, lim_in<T>(lo1, h), lo2, sc);
+      if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin_rows(h->mtOnTheFly), 1), g, (const T *)in, (const T *)cn, (const T *)cdB, yB, lim_in<T>(lo1, h), lo2, sc);
       else if (h->limType == DGADV_LIM_STRICT)
         launch_k(h, k_limit_dot<T, P, 2>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
       else
@@ -338,7 +350,7 @@ static cudaError_t launch_step_fused(dgadv_handle *h, double t0, double tau, boo
     const LimOut<T> lo2 = lim_out<T>(h);
     ++h->limPass;
     prof_mark(h, 1);
-    launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin(), 1), g, (const T *)xL, (const T *)cnL,
+    launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin_rows(h->mtOnTheFly), 1), g, (const T *)xL, (const T *)cnL,
              (const T *)tb, outRaw, lim_in<T>(lo1, h), lo2, sc);
     prof_mark(h, -1);
   }

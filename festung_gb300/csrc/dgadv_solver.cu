@@ -96,6 +96,7 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
   h->p = prm->p; h->N = N_of_p(prm->p); h->ordRK = prm->ordRK; h->prec = prm->precision;
   h->lim = prm->isSlopeLim ? 1 : 0; h->limType = prm->typeSlopeLim; h->flags = prm->flags;
   h->limdot = h->lim && h->p > 1;
+  h->mtOnTheFly = h->prec == DGADV_FP32;   // FP32 kernels are bandwidth-bound, the others are not
   h->nc = h->lim ? (h->limType == DGADV_LIM_LINEAR ? 1 : h->p * (h->p + 1) / 2) : 1;
   h->passesPerStep = h->lim ? h->ordRK * (h->limdot ? 2 : 1) : 0;
   if ((h->flags & DGADV_FLAG_FUSE) && !ops(h).fused) {
@@ -596,6 +597,9 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
   } else if (option == DGADV_OPT_ADJ_WARPS) {
     if (value != 1 && value != 2 && value != 4) return DGADV_EINVAL;
     h->adjWarps = value;
+  } else if (option == DGADV_OPT_TAYLOR_MASS) {
+    if (value != 0 && value != 1) return DGADV_EINVAL;
+    h->mtOnTheFly = value == 1;
   } else if (option == DGADV_OPT_FLAGS) {
     const int runtime = DGADV_FLAG_NO_GRAPH | DGADV_FLAG_NO_PDL | DGADV_FLAG_FUSE | DGADV_FLAG_PERSIST;
     if (value & ~runtime) { h->err = "only NO_GRAPH, NO_PDL, FUSE and PERSIST change after creation"; return DGADV_EINVAL; }
@@ -617,6 +621,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   else if (option == DGADV_OPT_FLAGS) *value = h->flags;
   else if (option == DGADV_OPT_PERSIST_BLOCKS) *value = h->persistPerSM;
   else if (option == DGADV_OPT_ADJ_WARPS) *value = h->adjWarps;
+  else if (option == DGADV_OPT_TAYLOR_MASS) *value = h->mtOnTheFly ? 1 : 0;
   else return DGADV_EINVAL;
   return DGADV_OK;
   });

@@ -211,3 +211,42 @@ def test_strict_limiter_fp32_close_to_fp64(lib):
     DF32 match the oracle; the bound records that level."""
     kw = STRICT[1]
     assert rel(gpu_run(precision='fp32', **kw).cDisc, gpu_run(precision='fp64', **kw).cDisc) <= 1e-2
+
+
+# The time-derivative limiter's Taylor mass correction rebuilt from B and the constant Gram
+# table (DGADV_OPT_TAYLOR_MASS = 1, the FP32 default) instead of the stored blocks: in FP64 it
+# must meet the same bar against the oracle.
+MASS_ON_THE_FLY = [
+    dict(testcase='gauss_slot', hmax=2 ** -3, p=2, tEnd=0.05, numSteps=20, isSlopeLim=True),
+    dict(testcase='gauss_slot', hmax=2 ** -3, p=3, tEnd=0.02, numSteps=10, isSlopeLim=True),
+    dict(testcase='gauss_slot', hmax=2 ** -3, p=2, tEnd=0.05, numSteps=20, isSlopeLim=True,
+         typeSlopeLim='hierarch_vert'),
+    dict(testcase='gauss_slot', hmax=2 ** -3, p=3, tEnd=0.02, numSteps=10, isSlopeLim=True,
+         typeSlopeLim='hierarch_vert', jitter=0.1, meshSeed=7),
+    dict(testcase='gauss_slot', hmax=2 ** -3, p=3, tEnd=0.02, numSteps=10, isSlopeLim=True,
+         typeSlopeLim='strict'),
+    dict(testcase='transient', hmax=2 ** -3, p=2, tEnd=0.1, numSteps=20, isSlopeLim=True),
+]
+
+
+@pytest.mark.parametrize('kw', MASS_ON_THE_FLY, ids=lambda kw: '-'.join('%s=%s' % (k, v) for k, v in kw.items()
+                                                                         if k not in ('testcase',)))
+def test_fp64_taylor_mass_on_the_fly_matches_oracle(lib, kw):
+    from festung_gb300 import _lib as L
+    from oracle import matfree as MF
+    g = gpu_run(precision='fp64', gpuOptions={L.OPT_TAYLOR_MASS: 1}, **kw)
+    o = oracle_run(**kw)
+    tol = FP64_TOL
+    if kw.get('typeSlopeLim') in ('hierarch_vert', 'strict') and kw['p'] == 3:
+        tol = max(FP64_TOL, 10 * MF.roundoff_spread(**kw))
+    assert rel(g.cDisc, o.cDisc) <= tol
+
+
+def test_fp32_taylor_mass_variants_agree(lib):
+    """FP32 with the rebuilt correction (default) and with the stored blocks: same scheme,
+    results within FP32 roundoff of each other on a limited p = 2 run."""
+    from festung_gb300 import _lib as L
+    kw = dict(testcase='gauss_slot', hmax=2 ** -4, p=2, tEnd=0.05, numSteps=20, isSlopeLim=True)
+    a = gpu_run(precision='fp32', **kw)
+    b = gpu_run(precision='fp32', gpuOptions={L.OPT_TAYLOR_MASS: 0}, **kw)
+    assert rel(a.cDisc, b.cDisc) <= 1e-5
