@@ -100,6 +100,7 @@ SYMBOLS = {
     'dgadv_get_option': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _i32p]),
     'dgadv_selftest_wait': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     'dgadv_kernels_per_step': (ctypes.c_int, [ctypes.c_void_p, _i32p]),
+    'dgadv_link': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     'dgadv_time_steps': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _dp]),
     'dgadv_profile_kernels': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                              _dp, _i32p]),

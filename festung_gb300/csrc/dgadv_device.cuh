@@ -430,16 +430,20 @@ __device__ __forceinline__ void scatter_quantities(const Geo<T> &g, const LimOut
   }
 }
 
-// Reset of the next pass's vertex keys (thread t owns vertex t) and global slots (grid-stride).
+// Reset of the next pass's vertex keys (thread t owns vertex t) and global slots (stride over
+// the tiles of the mesh: tile / nTiles, by default this block in its grid).
 template <typename T>
-__device__ __forceinline__ void reset_next(const Geo<T> &g, const LimOut<T> &lo, int t) {
+__device__ __forceinline__ void reset_next(const Geo<T> &g, const LimOut<T> &lo, int t, int tile = -1,
+                                           int nTiles = -1) {
+  if (tile < 0) tile = blockIdx.x;
+  if (nTiles < 0) nTiles = gridDim.x;
   if (t < g.numV)
     for (int s = 0; s < lo.nc; ++s) {
       lo.vreset[(size_t)(2 * s) * g.Vp + t] = vkey_max<T>();
       lo.vreset[(size_t)(2 * s + 1) * g.Vp + t] = 0;
     }
   const int nSlots = (g.instOf ? g.nInst : 1) * kSlotCopies * 2 * lo.nc;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nSlots; i += gridDim.x * blockDim.x)
+  for (int i = tile * blockDim.x + threadIdx.x; i < nSlots; i += nTiles * blockDim.x)
     lo.reset[i] = (i & 1) ? 0ULL : key_max<T>();
 }
 
@@ -833,7 +837,7 @@ struct StageScalars {
 
 template <typename T, int P, int MODE, bool RHS, bool LIN>
 __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, const T *c0, T *out,
-           const LimOut<T> lo, const StageScalars sc, const int tile) {
+           const LimOut<T> lo, const StageScalars sc, const int tile, const int nTiles = -1) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::op(MODE, LIN);
   extern __shared__ __align__(128) unsigned char smem[];
@@ -862,7 +866,7 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
   int vid[3] = {0, 0, 0};
   if (MODE != 0 && active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
   pdl_wait();
-  if (MODE != 0) reset_next<T>(g, lo, k);
+  if (MODE != 0) reset_next<T>(g, lo, k, nTiles < 0 ? -1 : tile, nTiles);
   if (!staged) return;
   if (t == 0) {                                   // state rows after it
     stage_T(smem, rC, cin, N, Kp, k0, bar);
@@ -1221,7 +1225,8 @@ k_to_taylor(const Geo<T> g, const T *c, T *__restrict__ tbuf, const LimOut<T> lo
 // modal basis and its mean scattered for the solution limiter.
 template <typename T, int P>
 __device__ __forceinline__ void limit_dot_lin_tile(const Geo<T> g, const T *cin, const T *c0, const T *tbuf,
-                T *out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc, const int tile) {
+                T *out, const LimIn<T> li, const LimOut<T> lo, const StageScalars sc, const int tile,
+                const int nTiles = -1) {
   constexpr int N = Dims<P>::N, NQ = 1;
   // staged rows: cDot, then N(N-1) rows of Q_k or the 4 rows of B, then c^n and c^(s-1)
   const bool fly = g.mtOnTheFly != 0;
@@ -1248,7 +1253,7 @@ __device__ __forceinline__ void limit_dot_lin_tile(const Geo<T> g, const T *cin,
   int vid[3] = {0, 0, 0};
   if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
   pdl_wait();
-  reset_next<T>(g, lo, k);
+  reset_next<T>(g, lo, k, nTiles < 0 ? -1 : tile, nTiles);
   if (!staged) return;
   if (t == 0) {
     stage_T(smem, rD, (const T *)tbuf, N, Kp, k0, bar);

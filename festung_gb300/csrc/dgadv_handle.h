@@ -8,6 +8,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/dgadv.h"
@@ -25,6 +26,7 @@ void transport_release(dgadv_handle *h);
 constexpr int kBlock = 128;       // elements per CTA (one thread per element)
 constexpr int kSlotCopies = 32;   // copies of the global min / max slots (atomics spread over them)
 constexpr int kGridBarBytes = 8192;   // state of the persistent step's grid barrier
+constexpr int kMaxLinkedParts = 4;    // handles in one linked step (a primary and three more)
 }  // namespace dgadv
 
 struct dgadv_handle {
@@ -48,6 +50,13 @@ struct dgadv_handle {
   int stepStages = 0;
   int adjWarps = 2;                    // warps per role of the FP32 adjoint stage (1, 2 or 4)
   bool mtOnTheFly = false;             // Taylor mass correction rebuilt from B (DGADV_OPT_TAYLOR_MASS)
+  // linked stepping (dgadv_link): this handle steps the handles in `linked` together with itself,
+  // one launch per stage kernel; a handle in another's list has that handle as linkedTo
+  std::vector<dgadv_handle *> linked;
+  dgadv_handle *linkedTo = nullptr;
+  std::vector<std::pair<long long, cudaGraphExec_t>> linkGraphs;   // key: phases of every part
+  double linkGraphTau = -1.0;
+  cudaEvent_t linkEv = nullptr;        // orders this handle's stream with the linked ones
   void *cR = nullptr, *cnL = nullptr, *cLx = nullptr;   // fused path: raw step output, limited c^n / c^(s-1)
   void *vkeys = nullptr;               // 3 passes x nc x 2 x Vp vertex min / max keys
   unsigned long long *gmm = nullptr;   // 3 passes x kSlotCopies x 2 x nc encoded global extremes
@@ -177,6 +186,8 @@ struct PrecOps {
   cudaError_t (*gather_out)(dgadv_handle *h, const void *src);  // src -> stage_ext
   cudaError_t (*adj_stage)(dgadv_handle *h, const AdjStageArgs &a);   // null: no adjoint kernels
   cudaError_t (*step_persist)(dgadv_handle *h, double t0, double tau); // null: not built
+  // one step of hs[0] and the handles linked to it, one launch per stage kernel (null: not built)
+  cudaError_t (*step_linked)(dgadv_handle **hs, int n, double t0, double tau);
   cudaError_t (*persist_attributes)(int p);
   cudaError_t (*lim_vjp)(dgadv_handle *h, const LimVjpArgs &a);
   cudaError_t (*vjp_scatter)(dgadv_handle *h, const void *x, long long pass);

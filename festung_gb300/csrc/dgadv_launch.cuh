@@ -505,6 +505,7 @@ static PrecOps make_ops() {
   o.lim_vjp = nullptr;
   o.vjp_scatter = nullptr;
   o.step_persist = nullptr;
+  o.step_linked = nullptr;
   o.persist_attributes = nullptr;
   o.copy = copy_state;
   o.from_f64 = from_f64<T>;

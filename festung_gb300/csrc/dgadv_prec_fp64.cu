@@ -1,4 +1,4 @@
-// Kernels and launch sequences of the FP64 path (stored reals: double), every degree, with the adjoint kernels, the persistent step and the transport kernels.
+// Kernels and launch sequences of the FP64 path (stored reals: double), every degree, with the adjoint kernels, the persistent step, the transport kernels and the linked step.
 #include "dgadv_device.cuh"
 
 namespace dgadv {
@@ -9,11 +9,12 @@ DGADV_DEFINE_TABLES(double, cTd)
 #include "dgadv_adjoint.cuh"
 #include "dgadv_persist.cuh"
 #include "dgadv_transport.cuh"
+#include "dgadv_linked.cuh"
 
 namespace dgadv {
 const PrecOps &ops_fp64() {
   static const PrecOps ops =
-      with_transport<double, 0xF>(with_persistent<double, 0xF>(with_adjoint<double, 0xF>(make_ops<double, 0xF, true>())));
+      with_linked<double, 0xE>(with_transport<double, 0xF>(with_persistent<double, 0xF>(with_adjoint<double, 0xF>(make_ops<double, 0xF, true>()))));
   return ops;
 }
 }  // namespace dgadv

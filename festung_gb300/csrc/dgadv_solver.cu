@@ -470,6 +470,11 @@ extern "C" int dgadv_sync(dgadv_handle *h) {
   DG_CUDA(cudaStreamSynchronize(h->stream));
   int flag = 0;
   DG_CUDA(cudaMemcpy(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost));
+  for (const dgadv_handle *o : h->linked) {   // the linked step's kernels flag in each part's word
+    int f = 0;
+    DG_CUDA(cudaMemcpy(&f, o->flag, sizeof(int), cudaMemcpyDeviceToHost));
+    flag |= f;
+  }
   if (flag & 2) {
     // a block gave up at a barrier: the barrier state is reset for the next launch
     cudaMemset(h->gridBar, 0, kGridBarBytes);
@@ -508,8 +513,21 @@ static bool time_dependent(const dgadv_handle *h) {
   return false;
 }
 
-// One time step: fused or separate-pass pipeline.
+// The parts of a linked step: h, then the handles linked to it.
+static int linked_parts(dgadv_handle *h, dgadv_handle **hs) {
+  int n = 0;
+  hs[n++] = h;
+  for (dgadv_handle *o : h->linked) hs[n++] = o;
+  return n;
+}
+
+// One time step: fused or separate-pass pipeline, or the linked step of h and its linked handles.
 static cudaError_t one_step(dgadv_handle *h, double t0, double tau, bool firstOfCall) {
+  if (!h->linked.empty()) {
+    dgadv_handle *hs[kMaxLinkedParts];
+    const int n = linked_parts(h, hs);
+    return ops(h).step_linked(hs, n, t0, tau);
+  }
   if (use_persistent(h) && ops(h).step_persist) return ops(h).step_persist(h, t0, tau);
   if (use_fused(h))
     return ops(h).step_fused(h, t0, tau, firstOfCall);
@@ -520,6 +538,76 @@ static cudaError_t end_of_call(dgadv_handle *h) {
   return ops(h).finalize_fused(h);
 }
 
+// Why a handle cannot take part in a linked step (nullptr: it can).
+static const char *link_refusal(const dgadv_handle *h) {
+  if (h->flags & DGADV_FLAG_IMPLICIT) return "implicit handles are not linked";
+  if (h->p < 1 || h->p > 3) return "linked steps cover degrees 1..3";
+  if (h->lim && h->limType != DGADV_LIM_LINEAR) return "linked steps take the linear limiter or none";
+  if (h->nTerms > 0 || h->rhs || h->cDV0T) return "linked steps take no source or boundary terms";
+  if (h->flags & (DGADV_FLAG_FUSE | DGADV_FLAG_PERSIST)) return "linked steps use the separate-pass pipeline";
+  if (h->stepSrc || h->stepDst || h->stepStages) return "a recorded adjoint run is in progress";
+  if (!h->hasVelocity) return "dgadv_set_velocity was not called";
+  return nullptr;
+}
+
+// Linked step of h and its linked handles: the others' work queued before waits for h's
+// stream first, and theirs waits for the step afterwards.
+static int linked_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau) {
+  dgadv_handle *hs[kMaxLinkedParts];
+  const int n = linked_parts(h, hs);
+  for (int i = 0; i < n; ++i)
+    if (const char *why = link_refusal(hs[i])) { h->err = std::string("linked step: ") + why; return DGADV_EUNSUPPORTED; }
+  for (int i = 1; i < n; ++i) {
+    if (!hs[i]->linkEv) DG_CUDA(cudaEventCreateWithFlags(&hs[i]->linkEv, cudaEventDisableTiming));
+    DG_CUDA(cudaEventRecord(hs[i]->linkEv, hs[i]->stream));
+    DG_CUDA(cudaStreamWaitEvent(h->stream, hs[i]->linkEv, 0));
+  }
+  int done = 0;
+  if (!(h->flags & DGADV_FLAG_NO_GRAPH)) {
+    const int chunk = h->graphSteps;
+    if (h->linkGraphTau != tau) {
+      for (auto &kv : h->linkGraphs) cudaGraphExecDestroy(kv.second);
+      h->linkGraphs.clear();
+      h->linkGraphTau = tau;
+    }
+    while (nSteps - done >= chunk) {
+      long long key = 0;
+      for (int i = n - 1; i >= 0; --i) key = 3 * key + hs[i]->limPass % 3;
+      cudaGraphExec_t ex = nullptr;
+      for (auto &kv : h->linkGraphs)
+        if (kv.first == key) ex = kv.second;
+      if (!ex) {
+        long long saved[kMaxLinkedParts];
+        for (int i = 0; i < n; ++i) saved[i] = hs[i]->limPass;
+        cudaGraph_t gph;
+        DG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (int s = 0; s < chunk && e == cudaSuccess; ++s) e = ops(h).step_linked(hs, n, 0.0, tau);
+        cudaError_t e2 = cudaStreamEndCapture(h->stream, &gph);
+        for (int i = 0; i < n; ++i) hs[i]->limPass = saved[i];
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+          h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+          return DGADV_ECUDA;
+        }
+        DG_CUDA(cudaGraphInstantiate(&ex, gph, 0));
+        cudaGraphDestroy(gph);
+        h->linkGraphs.emplace_back(key, ex);
+      }
+      DG_CUDA(cudaGraphLaunch(ex, h->stream));
+      for (int i = 0; i < n; ++i) hs[i]->limPass += (long long)chunk * hs[i]->passesPerStep;
+      done += chunk;
+    }
+  }
+  for (; done < nSteps; ++done) {
+    cudaError_t e = ops(h).step_linked(hs, n, (double)(nStep0 + done) * tau, tau);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return DGADV_ECUDA; }
+  }
+  if (!h->linkEv) DG_CUDA(cudaEventCreateWithFlags(&h->linkEv, cudaEventDisableTiming));
+  DG_CUDA(cudaEventRecord(h->linkEv, h->stream));
+  for (int i = 1; i < n; ++i) DG_CUDA(cudaStreamWaitEvent(hs[i]->stream, h->linkEv, 0));
+  return DGADV_OK;
+}
+
 extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, double tau) {
   return guarded(h, [&]() -> int {
   if (!h || nSteps < 0 || !(tau > 0)) return DGADV_EINVAL;
@@ -528,8 +616,10 @@ extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, doubl
     return DGADV_EUNSUPPORTED;
   }
   if (!h->hasVelocity) { if (h) h->err = "dgadv_set_velocity was not called"; return DGADV_EINVAL; }
+  if (h->linkedTo) { h->err = "this handle is stepped by the handle it is linked to"; return DGADV_EUNSUPPORTED; }
   DG_CUDA(cudaSetDevice(h->device));
   if (nSteps == 0) return DGADV_OK;
+  if (!h->linked.empty()) return linked_step(h, nSteps, nStep0, tau);
   const bool fused = use_fused(h);
   const bool useGraph = !(h->flags & DGADV_FLAG_NO_GRAPH) && !time_dependent(h);
   int done = 0;
@@ -580,6 +670,49 @@ static void drop_graphs(dgadv_handle *h) {
   for (int i = 0; i < 3; ++i)
     if (h->graph[i]) { cudaGraphExecDestroy(h->graph[i]); h->graph[i] = nullptr; }
   if (h->adjExec) { cudaGraphExecDestroy(h->adjExec); h->adjExec = nullptr; h->adjExecSteps = 0; }
+  for (auto &kv : h->linkGraphs) cudaGraphExecDestroy(kv.second);
+  h->linkGraphs.clear();
+  if (h->linkedTo) drop_graphs(h->linkedTo);   // the linked step's graphs hold this handle's launches
+}
+
+// Removes `o` from its primary's linked handles.
+static void unlink_one(dgadv_handle *o) {
+  dgadv_handle *h = o->linkedTo;
+  if (!h) return;
+  cudaStreamSynchronize(h->stream);
+  drop_graphs(h);
+  for (size_t i = 0; i < h->linked.size(); ++i)
+    if (h->linked[i] == o) { h->linked.erase(h->linked.begin() + i); break; }
+  o->linkedTo = nullptr;
+}
+
+extern "C" int dgadv_link(dgadv_handle *h, dgadv_handle *other) {
+  return guarded(h, [&]() -> int {
+  if (!h) return DGADV_EINVAL;
+  DG_CUDA(cudaSetDevice(h->device));
+  DG_CUDA(cudaStreamSynchronize(h->stream));
+  if (!other) {   // unlink every handle linked to h
+    while (!h->linked.empty()) unlink_one(h->linked.back());
+    return DGADV_OK;
+  }
+  if (other == h || other->device != h->device || other->prec != h->prec) {
+    h->err = "link: another handle of the same device and precision is needed";
+    return DGADV_EINVAL;
+  }
+  if (!ops(h).step_linked) { h->err = "link: no linked step for this precision"; return DGADV_EUNSUPPORTED; }
+  if (h->linkedTo || other->linkedTo || !other->linked.empty()) {
+    h->err = "link: a handle is linked into one primary at most, and a primary is linked into none";
+    return DGADV_EINVAL;
+  }
+  if ((int)h->linked.size() + 1 >= kMaxLinkedParts) { h->err = "link: too many linked handles"; return DGADV_EINVAL; }
+  for (const dgadv_handle *x : {(const dgadv_handle *)h, (const dgadv_handle *)other})
+    if (const char *why = link_refusal(x)) { h->err = std::string("link: ") + why; return DGADV_EUNSUPPORTED; }
+  DG_CUDA(cudaStreamSynchronize(other->stream));
+  h->linked.push_back(other);
+  other->linkedTo = h;
+  drop_graphs(h);
+  return DGADV_OK;
+  });
 }
 
 extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) {
@@ -712,6 +845,19 @@ extern "C" int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count) {
   return guarded(h, [&]() -> int {
   if (!h || !count) return DGADV_EINVAL;
   if (use_persistent(h) && ops_of(h).step_persist) { *count = 1; return DGADV_OK; }
+  if (!h->linked.empty()) {   // per stage: the operator, the cDot limiter if any part has it, the limiter
+    std::vector<const dgadv_handle *> hs{h};
+    for (const dgadv_handle *o : h->linked) hs.push_back(o);
+    int c = 0;
+    for (int s = 0; s < 3; ++s) {
+      bool op = false, ld = false, lm = false;
+      for (const dgadv_handle *x : hs)
+        if (s < x->ordRK) { op = true; ld |= x->limdot; lm |= x->lim != 0; }
+      c += (int)op + (int)ld + (int)lm;
+    }
+    *count = c;
+    return DGADV_OK;
+  }
   int perStage = 1;
   if (use_fused(h)) perStage = h->limdot ? 2 : 1;
   else if (h->lim) perStage = h->limdot ? 3 : 2;
@@ -726,6 +872,9 @@ extern "C" void dgadv_destroy(dgadv_handle *h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  unlink_one(h);
+  while (!h->linked.empty()) unlink_one(h->linked.back());
+  if (h->linkEv) cudaEventDestroy(h->linkEv);
   try {
     output_release(h);   // joins the writer thread
   } catch (...) {

@@ -9,9 +9,11 @@ The ensemble workload: seeded instances of the 'ensemble' test case.
 - Every instance runs SSP-RK of order p + 1 (the reference's default,
   advection/configureProblem.m:80), 200 steps of 5e-4, with the linear vertex-based limiter.
 
-The instances of one degree are stacked into one handle (``dgadv_create_ensemble``): every
-stage kernel then covers all of them in one launch, each instance keeping its own limiter
-extremes. The degree groups run on their own handles.
+The instances of one degree are stacked into one handle (``dgadv_create_ensemble``), each
+instance keeping its own limiter extremes.  The degree groups' handles are linked
+(``dgadv_link``): one step then launches each stage kernel once for every instance of every
+degree, the blocks of each group running that group's kernel code (``linked=False`` steps the
+groups on their own streams instead).
 
 ``shard(n, rank, world)`` splits instances across ranks with no data exchange: each rank runs
 its own instances (weak scaling); results stay on their rank.
@@ -50,7 +52,8 @@ def instance_problem(seed, numSteps=STEPS, tau=TAU, **overrides):
 class Ensemble:
     """Instances grouped by degree, one stacked handle per group."""
 
-    def __init__(self, seeds, precision='fp32', device=0, flags=0, numSteps=STEPS, tau=TAU, **overrides):
+    def __init__(self, seeds, precision='fp32', device=0, flags=0, numSteps=STEPS, tau=TAU, linked=True,
+                 **overrides):
         self.seeds = list(seeds)
         self.problems = [instance_problem(s, numSteps, tau, **overrides) for s in self.seeds]
         self.numSteps, self.tau = numSteps, tau
@@ -71,6 +74,13 @@ class Ensemble:
                                np.concatenate([pd.u2Disc for pd in pds]),
                                np.concatenate([pd.vNormalOnQuadEdge for pd in pds]))
             self.solvers[p] = s
+        # link the groups: the largest group's handle steps all of them
+        self.primary = None
+        if linked and len(self.solvers) > 1 and precision in ('fp32', 'fp64'):
+            order = sorted(self.solvers, key=lambda p: -sum(self.problems[i].K for i in self.groups[p]))
+            self.primary = self.solvers[order[0]]
+            for p in order[1:]:
+                self.primary.link(self.solvers[p])
         self.reset()
 
     @property
@@ -93,9 +103,18 @@ class Ensemble:
                 s.limit_state(0.0)
 
     def step(self, nSteps, nStep0=0):
-        """Enqueues steps on every group's stream (the groups run concurrently)."""
+        """Enqueues steps: one linked step for all groups, or each group on its own stream."""
+        if self.primary is not None:
+            self.primary.step(nSteps, nStep0, self.tau)
+            return
         for s in self.solvers.values():
             s.step(nSteps, nStep0, self.tau)
+
+    def kernels_per_step(self):
+        """Launches per time step: of the linked step, or per group."""
+        if self.primary is not None:
+            return {'linked': self.primary.kernels_per_step()}
+        return {int(p): s.kernels_per_step() for p, s in self.solvers.items()}
 
     def sync(self):
         for s in self.solvers.values():
@@ -114,6 +133,11 @@ class Ensemble:
         """Autotunes every group's launch configuration (festung_gb300.autotune)."""
         from . import autotune as AT
         out = {}
+        if self.primary is not None:   # the linked step: the primary's launch configuration
+            s = self.primary
+            key = AT.signature(s, self.tau, s.precision, '|ensemble-linked:%d' % len(self.problems)) if cache else None
+            out['linked'] = AT.tune(s, self.tau, nSteps, reps, fused_ok=False, cache=cache, key=key)[0]
+            return out
         for p, s in self.solvers.items():
             pd0 = self.problems[self.groups[p][0]]
             fused_ok = pd0.isSlopeLim and pd0.typeSlopeLim == 'linear' and s.precision != 'df32' and not pd0.cDTerms

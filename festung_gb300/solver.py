@@ -215,6 +215,10 @@ class DeviceSolver:
         self._c(self._lib.dgadv_get_option(self._h, int(option), ctypes.byref(v)))
         return v.value
 
+    def link(self, other):
+        """Steps `other` together with this handle from now on (dgadv_link); None unlinks all."""
+        self._c(self._lib.dgadv_link(self._h, other._h if other is not None else None))
+
     def kernels_per_step(self):
         n = ctypes.c_int32()
         self._c(self._lib.dgadv_kernels_per_step(self._h, ctypes.byref(n)))

@@ -319,8 +319,22 @@ int dgadv_write_lagrange(int32_t numT, int32_t numV, const double *coordV, const
                          int32_t numP, const double *dataLagr, const char *varName,
                          const char *fileName, int32_t tLvl, int32_t fileTypes);
 
-/* Number of kernels one time step launches (for launch accounting). */
+/* Number of kernels one time step launches (for launch accounting; for a handle with linked
+ * handles, the launches of the linked step). */
 int dgadv_kernels_per_step(const dgadv_handle *h, int32_t *count);
+
+/* Linked stepping (the batched launch of an ensemble whose instances differ in degree; no
+ * counterpart in the reference, whose problems run one at a time through main.m): links
+ * `other` to `h`, after which dgadv_step / dgadv_time_steps on h advance h and every handle
+ * linked to it with one launch per stage kernel covering all their elements, on h's stream.
+ * Each handle keeps its own state, tables, limiter extremes and RK order (a handle with fewer
+ * stages sits out the later stages of a step); results are bitwise those of stepping each
+ * handle alone.  Same device and precision (FP64 or FP32), degrees 1..3, the linear limiter or
+ * none, no source or boundary terms, the separate-pass pipeline; at most 3 handles linked to
+ * one.  A linked handle is not stepped on its own (DGADV_EUNSUPPORTED) until unlinked;
+ * dgadv_sync(h) reports the linked handles' non-finite flags too.  other == NULL unlinks every
+ * handle linked to h; destroying either handle unlinks it. */
+int dgadv_link(dgadv_handle *h, dgadv_handle *other);
 
 const char *dgadv_last_error(const dgadv_handle *h);
 const char *dgadv_status_string(int status);

@@ -1,5 +1,6 @@
-"""GPU ensembles: instances stacked into one handle per degree (one launch per stage kernel for
-all of them) give each instance exactly its own single-problem result.
+"""GPU ensembles: instances stacked into one handle per degree, the degree groups linked into one
+launch per stage kernel for all of them, give each instance exactly its own single-problem
+result.
 
 Bars: bitwise equal to the single-instance handle (FP32 and FP64: the same per-element
 arithmetic, the same vertex patches, the instance's own limiter extremes); FP64 relative L2
@@ -108,7 +109,7 @@ def test_autotuner_picks_a_measured_configuration(lib, tmp_path):
         cache = str(tmp_path / 'tune.json')
         best = ens.tune(nSteps=12, reps=2, cache=cache)
         for p, b in best.items():
-            s = ens.solvers[p]
+            s = ens.primary if p == 'linked' else ens.solvers[p]
             assert s.get_option(L.OPT_GRAPH_STEPS) == b['graphSteps']
             assert s.get_option(L.OPT_FLAGS) & (L.FLAG_FUSE | L.FLAG_NO_PDL) == b['flags']
         ens.reset()
@@ -125,3 +126,52 @@ def test_autotuner_picks_a_measured_configuration(lib, tmp_path):
             assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(b)   # the fused pipeline: roundoff
     finally:
         ref.close()
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'fp64'])
+def test_linked_groups_equal_separate_groups_bitwise(lib, precision):
+    """dgadv_link: one launch per stage kernel for both degrees (p = 1 with SSP-RK2, p = 2 with
+    SSP-RK3) gives bitwise the states of the groups stepped on their own, in fewer launches."""
+    from festung_gb300 import ensemble as E
+    seeds = list(range(8))
+    kw = dict(hmax=2 ** -4)
+    runs = {}
+    for linked in (True, False):
+        ens = E.Ensemble(seeds, precision=precision, numSteps=20, tau=5e-4, linked=linked, **kw)
+        try:
+            assert len(ens.groups) == 2
+            assert (ens.primary is not None) == linked
+            ens.step(7)                                   # not a multiple of the graph length
+            ens.step(13)
+            runs[linked] = (ens.states(), ens.kernels_per_step())
+        finally:
+            ens.close()
+    for a, b in zip(runs[True][0], runs[False][0]):
+        assert np.array_equal(a, b)
+    assert runs[True][1] == {'linked': 9}                # 3 stages x (operator, cDot limiter, limiter)
+    assert sum(runs[False][1].values()) == 6 + 9
+
+
+def test_link_refuses_what_it_does_not_cover(lib):
+    from festung_gb300 import _lib as L
+    from festung_gb300 import ensemble as E
+    ens = E.Ensemble([0, 1, 2, 3], precision='fp32', numSteps=4, hmax=2 ** -4)
+    try:
+        other = [s for s in ens.solvers.values() if s is not ens.primary][0]
+        with pytest.raises(L.DgadvError) as e:
+            other.step(1, 0, ens.tau)                     # stepped by its primary only
+        assert e.value.status == L.DGADV_EUNSUPPORTED
+        ens.primary.link(None)                            # unlinked: steps on its own again
+        other.step(1, 0, ens.tau)
+        other.sync()
+    finally:
+        ens.close()
+    hier = E.Ensemble([0, 1, 2, 3], precision='fp32', numSteps=4, hmax=2 ** -4, linked=False,
+                      typeSlopeLim='hierarch_vert')
+    try:
+        a, b = list(hier.solvers.values())
+        with pytest.raises(L.DgadvError) as e:
+            a.link(b)
+        assert e.value.status == L.DGADV_EUNSUPPORTED
+    finally:
+        hier.close()
