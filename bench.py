@@ -269,10 +269,13 @@ def large_block(device, flush):
     out = {'workload': 'gauss_slot_2M_p3_hier: domainSquare hmax=2^-10 with 10% node jitter '
                        '(2,097,152 triangles), p=3 (N=10), hierarchical vertex limiter, 100 SSP-RK3 '
                        'steps, tau=2e-5, gauss_slot'}
+    from festung_gb300 import _lib as L
     states = {}
-    for prec in ('fp32', 'fp64'):
-        pd = setup_problem('gauss_slot_2M_p3_hier', prec, device)
+    for prec in ('fp32', 'fp32_volume_mma', 'fp64'):
+        pd = setup_problem('gauss_slot_2M_p3_hier', prec.split('_')[0], device)
         s = pd.solver
+        if prec == 'fp32_volume_mma':                # the volume term on the tensor cores
+            s.set_option(L.OPT_VOLUME_MMA, 1)
         c0 = np.asfortranarray(pd._cDisc)
         s.step(5, 0, pd.tau)                        # warm-up (graph capture, first launches)
         s.sync()
@@ -284,7 +287,7 @@ def large_block(device, flush):
         K, N, S = pd.K, pd.N, pd.ordRK
         row = {'value': K * N * S * pd.numSteps / (ms / 1e3), 'unit': 'DOF-stage/s', 'ms_per_solve': ms,
                'K': K}
-        if prec == 'fp32':
+        if prec.startswith('fp32'):
             kpl, nl = s.profile_kernels(4, 0, pd.tau)
             w, Q, R, nc = 4, 12, pd.p + 1, pd.p * (pd.p + 1) // 2
             kinds = ['op2', 'limdot', 'lim']
@@ -309,8 +312,11 @@ def large_block(device, flush):
                                'frac_isolated': ai / peak}
         out[prec] = row
         s.close()
-    out['fp32_vs_fp64_rel_l2'] = float(np.linalg.norm(states['fp32'] - states['fp64']) /
-                                       np.linalg.norm(states['fp64']))
+    rel = lambda a, b: float(np.linalg.norm(states[a] - states[b]) / np.linalg.norm(states[b]))
+    out['fp32_vs_fp64_rel_l2'] = rel('fp32', 'fp64')
+    out['fp32_volume_mma']['rel_l2_vs_fp64'] = rel('fp32_volume_mma', 'fp64')
+    out['fp32_volume_mma']['rel_l2_vs_fp32'] = rel('fp32_volume_mma', 'fp32')
+    out['fp32_volume_mma']['speedup_vs_fp32'] = out['fp32']['ms_per_solve'] / out['fp32_volume_mma']['ms_per_solve']
     return out
 
 

@@ -558,6 +558,10 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 // kernel and move them above griddepcontrol.wait.  Outputs that alias no input keep a
 // (non-const) __restrict__, which lets input loads move past their stores.
 
+}  // namespace dgadv
+#include "dgadv_mma.cuh"
+namespace dgadv {
+
 // Device-to-device copy of n 16-byte words as a kernel of the launch chain.  A copy between two
 // kernels that use programmatic dependent launch has to be a kernel itself: the second kernel's
 // dependency wait covers the kernel launched before it, not a copy-engine transfer queued in
@@ -991,6 +995,179 @@ __global__ void __launch_bounds__(kBlock)
 k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
            const LimOut<T> lo, const StageScalars sc) {
   stage_op_tile<T, P, MODE, RHS, LIN>(g, cin, c0, out, lo, sc, blockIdx.x);
+}
+
+// The stage operator with the volume term on the tensor cores (dgadv_mma.cuh): FP32, p >= 2,
+// MODE 2 (cDot out, time-derivative limiting follows), no source terms.  The rest of the stage
+// (the upwind flux, the output, the scatter of centroid quantities) is stage_op_tile's; the
+// flux is computed while the first contraction runs.  Shared memory: the staged rows, then the
+// MMA area at the next 1024-byte boundary.
+template <int P> struct MmaSmem {
+  __host__ __device__ static constexpr size_t rows(bool lin) {
+    return StageRows<float, P>::bytes(StageRows<float, P>::op(2, lin), 1);
+  }
+  __host__ __device__ static constexpr size_t area(bool lin) { return (rows(lin) + 1023) / 1024 * 1024; }
+  __host__ __device__ static constexpr size_t bytes(bool lin) { return area(lin) + vmma::kBytes; }
+};
+
+template <int P, bool LIN>
+__device__ __forceinline__ void stage_op_tile_mma(const Geo<float> g, const float *cin, float *out,
+                                                  const LimOut<float> lo, const StageScalars sc, const int tile) {
+  using T = float;
+  constexpr int MODE = 2;
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
+  static_assert(N <= 16 && 2 * Q <= 32, "one 16-column accumulator per contraction");
+  constexpr int NT = StageRows<T, P>::op(MODE, LIN);
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  unsigned char *mm = smem + MmaSmem<P>::area(LIN);
+  uint64_t *mbar = (uint64_t *)(mm + vmma::oBar);
+  uint32_t *tslot = (uint32_t *)(mm + vmma::oTmem);
+  const Tab<T, P> &tb = tab<T, P>();
+  const int t = threadIdx.x, k0 = tile * kBlock, k = k0 + t;
+  pdl_trigger();
+  const int Kp = g.Kp;
+  const bool staged = k0 < g.K;
+  constexpr int rC = 0, rF = N, rV = rF + 2 * Q, rB = rV + 3 * R;
+  if (staged) {
+    if (t == 0) { mbar_init(bar, 1); mbar_init(mbar, 1); mbar_fence_init(); }
+    if (t < 32) vmma::alloc(tslot);
+    vmma::fill_tables<P>(mm);
+    vmma::fence_before();
+    __syncthreads();
+    vmma::fence_after();
+    if (t == 0) {
+      stage_expect<T>(bar, NT, 1);
+      stage_T(smem, rF, g.F, 2 * Q, Kp, k0, bar);
+      stage_T(smem, rV, g.Vn, 3 * R, Kp, k0, bar);
+      if (!LIN) stage_T(smem, rB, g.Bm, 4, Kp, k0, bar);
+      stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
+    }
+  }
+  const bool active = k < g.K;
+  int nb[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) nb[n] = active ? g.nbr[(size_t)n * Kp + k] : -1;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  if (!staged) return;
+  const uint32_t tbase = *tslot;
+  if (t == 0) stage_T(smem, rC, cin, N, Kp, k0, bar);
+  T cn[3][N];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const bool outside = nb[n] >= 0 && (nb[n] < k0 || nb[n] >= k0 + kBlock);
+#pragma unroll
+    for (int j = 0; j < N; ++j) cn[n][j] = outside ? cin[(size_t)j * Kp + nb[n]] : T(0);
+  }
+  const bool okAll = __syncthreads_and(mbar_wait_bounded(bar, sc.flag) ? 1 : 0) != 0;
+  T c[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) c[i] = (active && okAll) ? srow<T>(smem, rC + i)[t] : T(0);
+  // first contraction: A1 = this block's coefficients (row t), c_q into D1
+#pragma unroll
+  for (int j = 0; j < 16; ++j) vmma::put_split(mm, vmma::oA1h, vmma::oA1l, vmma::koff(t, j, 16), j < N ? c[j] : 0.f);
+  vmma::sync_for_mma();
+  const uint32_t mmBase = smem_u32(mm);
+  if (t == 0 && okAll)
+    vmma::issue(tbase, mmBase + vmma::oA1h, mmBase + vmma::oA1l, mmBase + vmma::oB1h, mmBase + vmma::oB1l, 16, mbar);
+  // the upwind flux meanwhile
+  Acc<T> rhs[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) rhs[i] = Acc<T>(T(0));
+  if (active && okAll) {
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      if (nb[n] >= k0 && nb[n] < k0 + kBlock)
+#pragma unroll
+        for (int j = 0; j < N; ++j) cn[n][j] = srow<T>(smem, rC + j)[nb[n] - k0];
+    const int code = irow<T>(smem, NT, 0)[t];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      const int np = (code >> (2 * n)) & 3;
+      const bool outOk = (code >> (6 + n)) & 1;
+#pragma unroll
+      for (int r2 = 0; r2 < R; ++r2) {
+        const T v = srow<T>(smem, rV + n * R + r2)[t];
+        Acc<T> tr(T(0));
+        if (v > T(0) && outOk) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr.fma(tb.phi1D[n][r2][j], c[j]);
+        } else if (v < T(0) && nb[n] >= 0) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tr.fma(tb.thetaPhi[n][np][r2][j], cn[n][j]);
+        }
+        const T fl = v * tr.get();
+#pragma unroll
+        for (int i = 0; i < N; ++i) rhs[i].fms(tb.phi1D[n][r2][i], fl);
+      }
+    }
+  }
+  // second contraction: A2 = (F1_q c_q, F2_q c_q), vol_i into D2
+  bool okM = okAll;
+  if (okAll) okM = vmma::wait_bounded(mbar, 0, sc.flag);
+  okM = __syncthreads_and(okM ? 1 : 0) != 0;
+  float cq[16];
+  if (okM) {
+    vmma::fence_after();
+    vmma::ld16(tbase + ((uint32_t)(32 * (t >> 5)) << 16), cq);
+  }
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const bool use = okM && active && q < Q;
+    const float f1 = use ? srow<T>(smem, rF + (q < Q ? q : 0))[t] * cq[q] : 0.f;
+    const float f2 = use ? srow<T>(smem, rF + Q + (q < Q ? q : 0))[t] * cq[q] : 0.f;
+    if (q < Q) {
+      vmma::put_split(mm, vmma::oA2h, vmma::oA2l, vmma::koff(t, q, 32), f1);
+      vmma::put_split(mm, vmma::oA2h, vmma::oA2l, vmma::koff(t, Q + q, 32), f2);
+    }
+  }
+#pragma unroll
+  for (int kk = 2 * Q; kk < 32; ++kk) vmma::put_split(mm, vmma::oA2h, vmma::oA2l, vmma::koff(t, kk, 32), 0.f);
+  vmma::sync_for_mma();
+  if (t == 0 && okM)
+    vmma::issue(tbase + 16, mmBase + vmma::oA2h, mmBase + vmma::oA2l, mmBase + vmma::oB2h, mmBase + vmma::oB2l, 32, mbar);
+  bool okV = okM;
+  if (okM) okV = vmma::wait_bounded(mbar, 1, sc.flag);
+  okV = __syncthreads_and(okV ? 1 : 0) != 0;
+  float vol[16];
+  if (okV) {
+    vmma::fence_after();
+    vmma::ld16(tbase + 16 + ((uint32_t)(32 * (t >> 5)) << 16), vol);
+  }
+  vmma::fence_before();
+  __syncthreads();
+  if (t < 32) vmma::dealloc(tbase);
+  T qv[NQ];
+  bool bad = false;
+  const bool done = active && okV;
+  if (done) {
+    T cdot[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cdot[i] = rhs[i].get() + vol[i];
+    if (LIN) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cdot[i]; bad |= !finite_(cdot[i]); }
+      qv[0] = lin_mean<T, P>(cdot);
+    } else {
+      const Affine<T> af = affine_from<T>(srow<T>(smem, rB)[t], srow<T>(smem, rB + 1)[t],
+                                          srow<T>(smem, rB + 2)[t], srow<T>(smem, rB + 3)[t]);
+      T cT[N];
+      to_taylor<T, P>(cdot, af, cT);
+#pragma unroll
+      for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cT[i]; bad |= !finite_(cT[i]); }
+      centroid_quantities<T, P>(cT, lo.type, qv);
+    }
+  }
+  scatter_quantities<T, NQ>(g, lo, qv, vid, done, tile);
+  if (bad) atomicOr(sc.flag, 1);
+}
+template <int P, bool LIN>
+__global__ void __launch_bounds__(kBlock)
+k_stage_op_mma(const Geo<float> g, const float *cin, float *out, const LimOut<float> lo, const StageScalars sc) {
+  stage_op_tile_mma<P, LIN>(g, cin, out, lo, sc, blockIdx.x);
 }
 
 // Time-derivative limiting and SSP update (advection/solveSubStep.m:69-83), then the Taylor

@@ -216,6 +216,10 @@ static cudaError_t set_smem_attributes() {
   set((const void *)k_limit<T, P, 1>, SR::bytes(SR::lim(), 1));
   set((const void *)k_limit<T, P, 2>, SR::bytes(SR::lim(), 1));
   set((const void *)k_to_taylor<T, P>, SR::bytes(SR::totaylor(), 0));
+  if constexpr (std::is_same_v<T, float> && P >= 2) {
+    set((const void *)k_stage_op_mma<P, true>, MmaSmem<P>::bytes(true));
+    set((const void *)k_stage_op_mma<P, false>, MmaSmem<P>::bytes(false));
+  }
   return e;
 }
 
@@ -263,7 +267,16 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     T *cdB = (lin && mode == 2 && h->recCdot[s]) ? (T *)h->recCdot[s] : tb;
     T *yB = (lin && h->recY[s]) ? (T *)h->recY[s] : tb;
     prof_mark(h, 0);
-    if (mode == 2) {
+    bool viaMma = false;
+    if constexpr (std::is_same_v<T, float> && P >= 2) {
+      if (mode == 2 && h->volumeMma && !rhs) {   // the volume term on the tensor cores
+        if (lin) launch_k(h, k_stage_op_mma<P, true>, grid, MmaSmem<P>::bytes(true), g, (const T *)in, cdB, lo1, sc);
+        else launch_k(h, k_stage_op_mma<P, false>, grid, MmaSmem<P>::bytes(false), g, (const T *)in, tb, lo1, sc);
+        viaMma = true;
+      }
+    }
+    if (viaMma) {
+    } else if (mode == 2) {
       if (lin) {
         if (rhs) launch_k(h, k_stage_op<T, P, 2, true, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, cdB, lo1, sc);
         else launch_k(h, k_stage_op<T, P, 2, false, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, cdB, lo1, sc);

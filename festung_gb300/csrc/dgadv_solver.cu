@@ -733,6 +733,13 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
   } else if (option == DGADV_OPT_TAYLOR_MASS) {
     if (value != 0 && value != 1) return DGADV_EINVAL;
     h->mtOnTheFly = value == 1;
+  } else if (option == DGADV_OPT_VOLUME_MMA) {
+    if (value != 0 && value != 1) return DGADV_EINVAL;
+    if (value && (h->prec != DGADV_FP32 || h->p < 2)) {
+      h->err = "the tensor-core volume term is built for FP32 at p >= 2";
+      return DGADV_EUNSUPPORTED;
+    }
+    h->volumeMma = value == 1;
   } else if (option == DGADV_OPT_FLAGS) {
     const int runtime = DGADV_FLAG_NO_GRAPH | DGADV_FLAG_NO_PDL | DGADV_FLAG_FUSE | DGADV_FLAG_PERSIST;
     if (value & ~runtime) { h->err = "only NO_GRAPH, NO_PDL, FUSE and PERSIST change after creation"; return DGADV_EINVAL; }
@@ -755,6 +762,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   else if (option == DGADV_OPT_PERSIST_BLOCKS) *value = h->persistPerSM;
   else if (option == DGADV_OPT_ADJ_WARPS) *value = h->adjWarps;
   else if (option == DGADV_OPT_TAYLOR_MASS) *value = h->mtOnTheFly ? 1 : 0;
+  else if (option == DGADV_OPT_VOLUME_MMA) *value = h->volumeMma ? 1 : 0;
   else return DGADV_EINVAL;
   return DGADV_OK;
   });

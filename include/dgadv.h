@@ -68,10 +68,14 @@ enum {
   DGADV_OPT_FLAGS = 2,         /* the runtime flags NO_GRAPH, NO_PDL, FUSE, PERSIST              */
   DGADV_OPT_PERSIST_BLOCKS = 3, /* blocks per SM of the persistent step (0: all that fit)       */
   DGADV_OPT_ADJ_WARPS = 4,      /* warps per role of the FP32 adjoint stage kernel: 1, 2 or 4    */
-  DGADV_OPT_TAYLOR_MASS = 5     /* time-derivative limiting's Taylor mass correction: 0 reads a
+  DGADV_OPT_TAYLOR_MASS = 5,    /* time-derivative limiting's Taylor mass correction: 0 reads a
                                    stored per-element block, 1 rebuilds it from the element's B
                                    and a constant table (default: 1 in FP32, 0 otherwise); the
                                    results agree to roundoff                                   */
+  DGADV_OPT_VOLUME_MMA = 6      /* 1: the volume term's two contractions on the tensor cores
+                                   (tcgen05, split TF32 with FP32 accumulation; FP32 handles,
+                                   p >= 2, time-derivative limiting, no source terms); 0 (the
+                                   default): FP32 multiply-adds                                */
 };
 
 /* ---- host helpers: static data ------------------------------------------------------- */

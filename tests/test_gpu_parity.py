@@ -250,3 +250,31 @@ def test_fp32_taylor_mass_variants_agree(lib):
     a = gpu_run(precision='fp32', **kw)
     b = gpu_run(precision='fp32', gpuOptions={L.OPT_TAYLOR_MASS: 0}, **kw)
     assert rel(a.cDisc, b.cDisc) <= 1e-5
+
+
+# The volume term on the tensor cores (DGADV_OPT_VOLUME_MMA, tcgen05 split-TF32 with FP32
+# accumulation) against the FP32 multiply-add path: same scheme, FP32-level differences.
+VOLUME_MMA = [
+    dict(testcase='gauss_slot', hmax=2 ** -4, p=2, tEnd=0.05, numSteps=20, isSlopeLim=True),
+    dict(testcase='gauss_slot', hmax=2 ** -4, p=3, tEnd=0.02, numSteps=10, isSlopeLim=True,
+         typeSlopeLim='hierarch_vert', jitter=0.1, meshSeed=7),
+    dict(testcase='ensemble', instanceSeed=3, hmax=2 ** -4, p=3, tEnd=0.02, numSteps=10, isSlopeLim=True),
+]
+
+
+@pytest.mark.parametrize('kw', VOLUME_MMA, ids=['p2-linear', 'p3-hier-jitter', 'p3-ensemble'])
+def test_fp32_volume_on_tensor_cores_matches_fma_path(lib, kw):
+    from festung_gb300 import _lib as L
+    a = gpu_run(precision='fp32', gpuOptions={L.OPT_VOLUME_MMA: 1}, **kw)
+    b = gpu_run(precision='fp32', **kw)
+    c = gpu_run(precision='fp64', **kw)
+    assert rel(a.cDisc, b.cDisc) <= 1e-5
+    assert rel(a.cDisc, c.cDisc) <= 2 * max(rel(b.cDisc, c.cDisc), 1e-6)
+
+
+def test_volume_mma_refused_outside_fp32(lib):
+    from festung_gb300 import _lib as L
+    kw = dict(testcase='gauss_slot', hmax=2 ** -3, p=2, tEnd=0.01, numSteps=2, isSlopeLim=True)
+    with pytest.raises(L.DgadvError) as e:
+        gpu_run(precision='fp64', gpuOptions={L.OPT_VOLUME_MMA: 1}, **kw)
+    assert e.value.status == L.DGADV_EUNSUPPORTED
