@@ -594,47 +594,65 @@ def transport_block(device, steps=200, with_cpu=True):
 
 def ensemble_block(rank, world, device, n=256, steps=200, reps=3):
     """The ensemble workload: n seeded instances (2048 to 32768 triangles, p in {1, 2}, their own
-    velocity fields), 200 steps in FP32 with the linear limiter; each degree group is one stacked
-    handle (one launch per stage kernel for all its instances), autotuned first.  Instances are
-    sharded across ranks with no exchange; whole-job DOF-stage/s = all ranks' work / the slowest
-    rank's time."""
+    velocity fields), 200 steps in FP32 with the linear limiter.  Each degree group is one
+    stacked handle and the groups are linked (one launch per stage kernel for all instances),
+    autotuned first; for comparison the groups are then unlinked, tuned and timed on their own
+    streams.  Instances are sharded across ranks with no exchange; whole-job DOF-stage/s = all
+    ranks' work / the slowest rank's time."""
     import torch
     from festung_gb300 import ensemble as E
     t = time.perf_counter()
     ens = E.Ensemble(E.shard(n, rank, world), precision='fp32', device=device, numSteps=steps)
     setup_s = time.perf_counter() - t
-    tuned = ens.tune()
     flush = torch.empty(512 * 2 ** 20, dtype=torch.uint8, device='cuda')
-    ens.step(steps)
-    ens.sync()
-    times = []
-    for _ in range(reps):
-        ens.reset()
-        flush.zero_()
-        torch.cuda.synchronize()
-        t = time.perf_counter()
+    units = ens.dof_stages(steps)
+
+    def timed():
         ens.step(steps)
         ens.sync()
-        times.append(time.perf_counter() - t)
-    dt = min(times)
-    units = ens.dof_stages(steps)
-    if world > 1:
-        x = torch.tensor([dt, float(units)], dtype=torch.float64, device='cuda')
-        mx = x.clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.SUM)
-        dt, units = float(mx[0]), float(x[1])
-    launches = {int(p): ens.solvers[p].kernels_per_step() for p in ens.solvers}
+        times = []
+        for _ in range(reps):
+            ens.reset()
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ens.step(steps)
+            ens.sync()
+            times.append(time.perf_counter() - t0)
+        dt = min(times)
+        u = float(units)
+        if world > 1:
+            x = torch.tensor([dt, u], dtype=torch.float64, device='cuda')
+            mx = x.clone()
+            torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+            torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.SUM)
+            dt, u = float(mx[0]), float(x[1])
+        return dt, u
+
+    tuned = ens.tune()
+    launches = ens.kernels_per_step()
+    linked = ens.primary is not None
+    dt, u = timed()
+    sep = None
+    if linked:
+        ens.unlink()
+        tunedSep = ens.tune()
+        dts, us = timed()
+        sep = {'value': us / dts, 'ms_per_solve': 1e3 * dts, 'kernels_per_step': ens.kernels_per_step(),
+               'tuned': tunedSep}
     out = {'workload': 'ensemble: %d seeded instances, hmax in {2^-5,2^-6,2^-7} with 0.2 h jitter, p in {1,2}, '
                        '8-mode streamfunction velocity, Gaussian hump, %d steps of 5e-4, FP32, linear limiter'
                        % (n, steps),
            'instances_this_rank': len(ens.seeds), 'dofs_this_rank': ens.dofs,
-           'value': units / dt, 'unit': 'DOF-stage/s', 'ms_per_solve': 1e3 * dt,
-           'groups': {int(p): {'instances': len(m), 'elements': int(sum(ens.problems[i].K for i in m)),
-                               'kernels_per_step': launches[p], 'tuned': tuned[p]}
+           'value': u / dt, 'unit': 'DOF-stage/s', 'ms_per_solve': 1e3 * dt,
+           'groups': {int(p): {'instances': len(m), 'elements': int(sum(ens.problems[i].K for i in m))}
                       for p, m in ens.groups.items()},
-           'host_setup_s': setup_s, 'timing': 'wall clock of 200 steps on both group streams, after an '
-                                              'L2 flush; initial data reset and limited before each'}
+           'linked': linked, 'kernels_per_step': launches, 'tuned': tuned,
+           'separate_groups': sep,
+           'host_setup_s': setup_s,
+           'timing': 'wall clock of 200 steps after an L2 flush, initial data reset and limited before each; '
+                     'linked: every degree group in one launch per stage kernel; separate_groups: one '
+                     'handle per degree on its own stream'}
     ens.close()
     return out
 

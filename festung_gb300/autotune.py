@@ -4,7 +4,9 @@ For one handle (one mesh, or one degree group of an ensemble) it times the launc
 configurations this library has and keeps the fastest:
 - the limiter pipeline: separate passes, or the fused one (linear limiter, zero Dirichlet data);
 - programmatic dependent launch on or off;
-- the number of time steps per captured CUDA graph.
+- the number of time steps per captured CUDA graph;
+- the stage operator's elements per CTA, 64 or 128 (one thread per element; separate-pass
+  pipeline, and the linked step of an ensemble's degree groups).
 Each candidate runs ``nSteps`` steps of the handle's own problem after one warm-up call, timed
 with CUDA events on the handle's stream; the state is restored afterwards.  The choice can be
 kept in a JSON file keyed by the problem's signature and the GPU name, and reused.
@@ -12,8 +14,7 @@ kept in a JSON file keyed by the problem's signature and the GPU name, and reuse
 ``tune_adjoint`` does the same for the FP32 adjoint stage kernel: warps per role, i.e. 32, 64 or
 128 elements per CTA with four warp roles (three edges, the volume points) per element.
 
-Fixed by design and not tuned: 128 elements per CTA (the row unit of the TMA bulk copies and the
-padding of every per-element array) and one thread per element in the forward kernels.
+The limiter kernels keep 128 elements per CTA (the padding unit of every per-element array).
 """
 import json
 import os
@@ -24,13 +25,19 @@ from . import _lib as L
 GRAPH_STEPS = (4, 12, 24, 48)
 
 
+OP_BLOCKS = (128, 64)
+
+
 def candidates(solver, fused_ok):
+    """Launch configurations: pipeline, dependent launch, steps per graph and, for the
+    separate-pass pipeline, the stage operator's elements per CTA (one thread per element)."""
     out = []
     for fuse in ((False, True) if fused_ok else (False,)):
         for pdl in (True, False):
             for gs in GRAPH_STEPS:
                 flags = (L.FLAG_FUSE if fuse else 0) | (0 if pdl else L.FLAG_NO_PDL)
-                out.append(dict(flags=flags, graphSteps=gs))
+                for eb in (OP_BLOCKS if not fuse else OP_BLOCKS[:1]):
+                    out.append(dict(flags=flags, graphSteps=gs, opBlock=eb))
     return out
 
 
@@ -50,20 +57,24 @@ def tune(solver, tau, nSteps=48, reps=3, fused_ok=False, cache=None, key=None):
             best = stored[key]['best']
             solver.set_option(L.OPT_FLAGS, best['flags'])
             solver.set_option(L.OPT_GRAPH_STEPS, best['graphSteps'])
+            solver.set_option(L.OPT_OP_BLOCK, best.get('opBlock', 128))
             return best, stored[key]['table']
     state = solver.get_state()
     table = []
     for c in candidates(solver, fused_ok):
         solver.set_option(L.OPT_FLAGS, c['flags'])
         solver.set_option(L.OPT_GRAPH_STEPS, c['graphSteps'])
+        solver.set_option(L.OPT_OP_BLOCK, c['opBlock'])
         solver.set_state(state)
         solver.time_steps(nSteps, 0, tau)                 # warm-up: graph capture, first launches
         ms = min(solver.time_steps(nSteps, 0, tau) for _ in range(reps))
         table.append(dict(c, ms_per_step=ms / nSteps))
     best = min(table, key=lambda r: r['ms_per_step'])
-    best = dict(flags=best['flags'], graphSteps=best['graphSteps'], ms_per_step=best['ms_per_step'])
+    best = dict(flags=best['flags'], graphSteps=best['graphSteps'], opBlock=best['opBlock'],
+                ms_per_step=best['ms_per_step'])
     solver.set_option(L.OPT_FLAGS, best['flags'])
     solver.set_option(L.OPT_GRAPH_STEPS, best['graphSteps'])
+    solver.set_option(L.OPT_OP_BLOCK, best['opBlock'])
     solver.set_state(state)
     if cache and key:
         stored = {}

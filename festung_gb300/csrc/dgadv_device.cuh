@@ -382,7 +382,7 @@ template <typename T> struct LimIn {
 template <typename T>
 __device__ __forceinline__ size_t slot_base(const Geo<T> &g, int nc, int tile = -1) {
   if (tile < 0) tile = blockIdx.x;
-  return g.instOf ? (size_t)g.instOf[tile] * kSlotCopies * 2 * nc : 0;
+  return g.instOf ? (size_t)g.instOf[(tile * (int)blockDim.x) / kBlock] * kSlotCopies * 2 * nc : 0;
 }
 
 // Scatter of the element's centroid quantities to its vertices and the block's global extremes.
@@ -421,7 +421,7 @@ __device__ __forceinline__ void scatter_quantities(const Geo<T> &g, const LimOut
     const int s = threadIdx.x;
     T mn = red[0][2 * s], mx = red[0][2 * s + 1];
 #pragma unroll
-    for (int w = 1; w < kBlock / 32; ++w) { mn = fmin(mn, red[w][2 * s]); mx = fmax(mx, red[w][2 * s + 1]); }
+    for (int w = 1; w < (int)(blockDim.x / 32); ++w) { mn = fmin(mn, red[w][2 * s]); mx = fmax(mx, red[w][2 * s + 1]); }
     if (mn <= mx) {
       unsigned long long *sl = lo.slots + slot_base(g, lo.nc, tile) + (size_t)(tile % kSlotCopies) * 2 * lo.nc;
       atomicMin(&sl[2 * s], okey(mn));
@@ -534,18 +534,18 @@ template <typename T>
 __device__ __forceinline__ void stage_T(unsigned char *smem, int row, const T *base, int nrows, int Kp, int k0,
                                         uint64_t *bar) {
   for (int r = 0; r < nrows; ++r)
-    bulk_g2s(smem + (size_t)(row + r) * kBlock * sizeof(T), base + (size_t)r * Kp + k0, kBlock * sizeof(T), bar);
+    bulk_g2s(smem + (size_t)(row + r) * blockDim.x * sizeof(T), base + (size_t)r * Kp + k0, blockDim.x * sizeof(T), bar);
 }
 template <typename T>
 __device__ __forceinline__ void stage_I(unsigned char *smem, int nT, int row, const int *base, int nrows, int Kp,
                                         int k0, uint64_t *bar) {
   for (int r = 0; r < nrows; ++r)
-    bulk_g2s(smem + (size_t)nT * kBlock * sizeof(T) + (size_t)(row + r) * kBlock * sizeof(int),
-             base + (size_t)r * Kp + k0, kBlock * sizeof(int), bar);
+    bulk_g2s(smem + (size_t)nT * blockDim.x * sizeof(T) + (size_t)(row + r) * blockDim.x * sizeof(int),
+             base + (size_t)r * Kp + k0, blockDim.x * sizeof(int), bar);
 }
 template <typename T>
 __device__ __forceinline__ void stage_expect(uint64_t *bar, int nT, int nI) {
-  mbar_expect_tx(bar, nT * kBlock * (uint32_t)sizeof(T) + nI * kBlock * (uint32_t)sizeof(int));
+  mbar_expect_tx(bar, nT * blockDim.x * (uint32_t)sizeof(T) + nI * blockDim.x * (uint32_t)sizeof(int));
 }
 
 // Programmatic dependent launch: the next kernel in the stream may start its prologue (static
@@ -574,10 +574,10 @@ static __global__ void k_copy16(const uint4 *src, uint4 *__restrict__ dst, size_
 }
 
 template <typename T> __device__ __forceinline__ const T *srow(const unsigned char *smem, int r) {
-  return (const T *)(smem + (size_t)r * kBlock * sizeof(T));
+  return (const T *)(smem + (size_t)r * blockDim.x * sizeof(T));
 }
 template <typename T> __device__ __forceinline__ const int *irow(const unsigned char *smem, int nT, int r) {
-  return (const int *)(smem + (size_t)nT * kBlock * sizeof(T) + (size_t)r * kBlock * sizeof(int));
+  return (const int *)(smem + (size_t)nT * blockDim.x * sizeof(T) + (size_t)r * blockDim.x * sizeof(int));
 }
 
 template <typename T, int P> struct StageRows {
@@ -595,12 +595,14 @@ template <typename T, int P> struct StageRows {
   __host__ __device__ static constexpr int limdot_lin() { return limdot_lin_rows(N * (N - 1) < 4); }
   // k_to_taylor: c, B
   __host__ __device__ static constexpr int totaylor() { return N + 4; }
-  // rows first, then the block's mbarrier (8 bytes, 16 reserved)
-  __host__ __device__ static constexpr size_t bar_offset(int nT, int nI) {
-    return (size_t)nT * kBlock * sizeof(T) + (size_t)nI * kBlock * sizeof(int);
+  // rows of eb elements first, then the block's mbarrier (8 bytes, 16 reserved)
+  __host__ __device__ static constexpr size_t bar_offset(int nT, int nI, int eb = kBlock) {
+    return (size_t)nT * eb * sizeof(T) + (size_t)nI * eb * sizeof(int);
   }
   // + 16 for the mbarrier, + 2 x 6 shift values
-  __host__ __device__ static constexpr size_t bytes(int nT, int nI) { return bar_offset(nT, nI) + 16 + 12 * sizeof(T); }
+  __host__ __device__ static constexpr size_t bytes(int nT, int nI, int eb = kBlock) {
+    return bar_offset(nT, nI, eb) + 16 + 12 * sizeof(T);
+  }
 };
 
 // Prefetch of the three vertices' min / max keys of every sub-limiter quantity.
@@ -845,9 +847,9 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::op(MODE, LIN);
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x));
   const Tab<T, P> &tb = tab<T, P>();
-  const int t = threadIdx.x, k0 = tile * kBlock, k = k0 + t;
+  const int t = threadIdx.x, eb = blockDim.x, k0 = tile * eb, k = k0 + t;
   pdl_trigger();
   const int Kp = g.Kp;
   const bool staged = k0 < g.K;                   // blocks beyond the elements only reset keys
@@ -880,7 +882,7 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
   T cn[3][N];
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
-    const bool outside = nb[n] >= 0 && (nb[n] < k0 || nb[n] >= k0 + kBlock);
+    const bool outside = nb[n] >= 0 && (nb[n] < k0 || nb[n] >= k0 + eb);
 #pragma unroll
     for (int j = 0; j < N; ++j) cn[n][j] = outside ? cin[(size_t)j * Kp + nb[n]] : T(0);
   }
@@ -894,7 +896,7 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
     for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = Acc<T>(T(0)); }
 #pragma unroll
     for (int n = 0; n < 3; ++n)
-      if (nb[n] >= k0 && nb[n] < k0 + kBlock)
+      if (nb[n] >= k0 && nb[n] < k0 + eb)
 #pragma unroll
         for (int j = 0; j < N; ++j) cn[n][j] = srow<T>(smem, rC + j)[nb[n] - k0];
     if (RHS) {
@@ -1019,7 +1021,7 @@ __device__ __forceinline__ void stage_op_tile_mma(const Geo<float> g, const floa
   static_assert(N <= 16 && 2 * Q <= 32, "one 16-column accumulator per contraction");
   constexpr int NT = StageRows<T, P>::op(MODE, LIN);
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x));
   unsigned char *mm = smem + MmaSmem<P>::area(LIN);
   uint64_t *mbar = (uint64_t *)(mm + vmma::oBar);
   uint32_t *tslot = (uint32_t *)(mm + vmma::oTmem);
@@ -1190,9 +1192,9 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::limdot();
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x));
   const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
-  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x) + 16);
   pdl_trigger();
   const int Kp = g.Kp;
   const bool staged = k0 < g.K;
@@ -1307,9 +1309,9 @@ k_limit(const Geo<T> g, const T *tbuf, T *__restrict__ out, const LimIn<T> li,
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::lim();
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x));
   const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
-  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x) + 16);
   pdl_trigger();
   if (k0 >= g.K) { pdl_wait(); return; }
   const int Kp = g.Kp;
@@ -1362,7 +1364,7 @@ k_to_taylor(const Geo<T> g, const T *c, T *__restrict__ tbuf, const LimOut<T> lo
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::totaylor();
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 0));
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 0, blockDim.x));
   const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
   pdl_trigger();
   const int Kp = g.Kp;
@@ -1409,9 +1411,9 @@ __device__ __forceinline__ void limit_dot_lin_tile(const Geo<T> g, const T *cin,
   const bool fly = g.mtOnTheFly != 0;
   const int NT = StageRows<T, P>::limdot_lin_rows(fly);
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x));
   const int t = threadIdx.x, k0 = tile * kBlock, k = k0 + t;
-  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x) + 16);
   pdl_trigger();
   const int Kp = g.Kp;
   const bool staged = k0 < g.K;
@@ -1628,8 +1630,8 @@ k_op_fused(const Geo<T> g, const T *x, int limitIn, T *xLout,
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
   constexpr int NT = StageRows<T, P>::op(MODE, true);
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1));
-  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1) + 16);
+  uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x));
+  T *sh = (T *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x) + 16);
   const Tab<T, P> &tb = tab<T, P>();
   const int t = threadIdx.x, k0 = blockIdx.x * kBlock, k = k0 + t;
   pdl_trigger();

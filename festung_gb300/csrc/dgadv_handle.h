@@ -51,6 +51,7 @@ struct dgadv_handle {
   int adjWarps = 2;                    // warps per role of the FP32 adjoint stage (1, 2 or 4)
   bool mtOnTheFly = false;             // Taylor mass correction rebuilt from B (DGADV_OPT_TAYLOR_MASS)
   bool volumeMma = false;              // volume term on the tensor cores (DGADV_OPT_VOLUME_MMA)
+  int opBlock = 128;                   // elements per block of the stage operator (DGADV_OPT_OP_BLOCK)
   // linked stepping (dgadv_link): this handle steps the handles in `linked` together with itself,
   // one launch per stage kernel; a handle in another's list has that handle as linkedTo
   std::vector<dgadv_handle *> linked;

@@ -229,6 +229,8 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
   const Geo<T> g = make_geo<T>(h);
   const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;   // producers also reset vertex keys
   const int gridK = (h->K + kBlock - 1) / kBlock;
+  // the stage operator's elements per block (DGADV_OPT_OP_BLOCK; one thread per element)
+  const int eb = h->opBlock, gridOp = (std::max(h->K, h->numV) + eb - 1) / eb;
   double omega[3], cst[3];
   const int S = rk_table(h->ordRK, omega, cst);
   T *cA = (T *)h->cA, *cB = (T *)h->cB, *tb = (T *)h->tbuf;
@@ -249,8 +251,8 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     LimOut<T> lo{};
     if (!h->lim) {
       prof_mark(h, 0);
-      if (rhs) launch_k(h, k_stage_op<T, P, 0, true, false>, grid, SR::bytes(SR::op(0, false), 1), g, in, cn, out, lo, sc);
-      else launch_k(h, k_stage_op<T, P, 0, false, false>, grid, SR::bytes(SR::op(0, false), 1), g, in, cn, out, lo, sc);
+      if (rhs) launch_kb(h, k_stage_op<T, P, 0, true, false>, gridOp, eb, SR::bytes(SR::op(0, false), 1, eb), g, in, cn, out, lo, sc);
+      else launch_kb(h, k_stage_op<T, P, 0, false, false>, gridOp, eb, SR::bytes(SR::op(0, false), 1, eb), g, in, cn, out, lo, sc);
       prof_mark(h, -1);
       continue;
     }
@@ -278,19 +280,19 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     if (viaMma) {
     } else if (mode == 2) {
       if (lin) {
-        if (rhs) launch_k(h, k_stage_op<T, P, 2, true, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, cdB, lo1, sc);
-        else launch_k(h, k_stage_op<T, P, 2, false, true>, grid, SR::bytes(SR::op(2, true), 1), g, in, cn, cdB, lo1, sc);
+        if (rhs) launch_kb(h, k_stage_op<T, P, 2, true, true>, gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
+        else launch_kb(h, k_stage_op<T, P, 2, false, true>, gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
       } else {
-        if (rhs) launch_k(h, k_stage_op<T, P, 2, true, false>, grid, SR::bytes(SR::op(2, false), 1), g, in, cn, tb, lo1, sc);
-        else launch_k(h, k_stage_op<T, P, 2, false, false>, grid, SR::bytes(SR::op(2, false), 1), g, in, cn, tb, lo1, sc);
+        if (rhs) launch_kb(h, k_stage_op<T, P, 2, true, false>, gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, tb, lo1, sc);
+        else launch_kb(h, k_stage_op<T, P, 2, false, false>, gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, tb, lo1, sc);
       }
     } else {
       if (lin) {
-        if (rhs) launch_k(h, k_stage_op<T, P, 1, true, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, yB, lo1, sc);
-        else launch_k(h, k_stage_op<T, P, 1, false, true>, grid, SR::bytes(SR::op(1, true), 1), g, in, cn, yB, lo1, sc);
+        if (rhs) launch_kb(h, k_stage_op<T, P, 1, true, true>, gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
+        else launch_kb(h, k_stage_op<T, P, 1, false, true>, gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
       } else {
-        if (rhs) launch_k(h, k_stage_op<T, P, 1, true, false>, grid, SR::bytes(SR::op(1, false), 1), g, in, cn, tb, lo1, sc);
-        else launch_k(h, k_stage_op<T, P, 1, false, false>, grid, SR::bytes(SR::op(1, false), 1), g, in, cn, tb, lo1, sc);
+        if (rhs) launch_kb(h, k_stage_op<T, P, 1, true, false>, gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, tb, lo1, sc);
+        else launch_kb(h, k_stage_op<T, P, 1, false, false>, gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, tb, lo1, sc);
       }
     }
     prof_mark(h, -1);

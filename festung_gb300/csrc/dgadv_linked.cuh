@@ -116,6 +116,7 @@ static cudaError_t launch_linked_step(dgadv_handle **hs, int n, double /*t0: no 
     e = cudaFuncSetAttribute((const void *)k_link_limdot<T, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smemLd);
   if (e != cudaSuccess) return e;
+  const int eb = h0->opBlock;                           // the operator's elements per block
   int S[kMaxLinked];
   double omega[kMaxLinked][3], cst[kMaxLinked][3];
   int Smax = 0;
@@ -131,6 +132,7 @@ static cudaError_t launch_linked_step(dgadv_handle **hs, int n, double /*t0: no 
       if (s >= S[i]) continue;
       const Geo<T> g = make_geo<T>(h);
       const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
+      const int gridE = (std::max(h->K, h->numV) + eb - 1) / eb;
       const int gridK = (h->K + kBlock - 1) / kBlock;
       T *cA = (T *)h->cA, *cB = (T *)h->cB, *tb = (T *)h->tbuf, *cn = (T *)h->cn;
       const T *in = (s == 0) ? cn : (s == 1 ? cA : cB);
@@ -138,9 +140,9 @@ static cudaError_t launch_linked_step(dgadv_handle **hs, int n, double /*t0: no 
       StageScalars sc{};
       sc.omega = omega[i][s]; sc.tau = tau; sc.flag = h->flag;
       LinkPart<T> &q = op.part[op.n++];
-      q.p = h->p; q.g = g; q.block0 = gOp; q.nBlocks = grid; q.sc = sc;
+      q.p = h->p; q.g = g; q.block0 = gOp; q.nBlocks = gridE; q.sc = sc;
       q.a = in; q.b = cn;
-      gOp += grid;
+      gOp += gridE;
       if (!h->lim) {
         q.mode = 0; q.out = out;
         continue;
@@ -167,7 +169,7 @@ static cudaError_t launch_linked_step(dgadv_handle **hs, int n, double /*t0: no 
       l.a = tb; l.out = out; l.li = lim_in<T>(loS, h);
       gLm += gridK;
     }
-    if (op.n) { prof_mark(h0, 0); launch_k(h0, k_link_op<T, MASK>, gOp, smemOp, op); prof_mark(h0, -1); }
+    if (op.n) { prof_mark(h0, 0); launch_kb(h0, k_link_op<T, MASK>, gOp, eb, smemOp, op); prof_mark(h0, -1); }
     if (ld.n) { prof_mark(h0, 1); launch_k(h0, k_link_limdot<T, MASK>, gLd, smemLd, ld); prof_mark(h0, -1); }
     if (lm.n) { prof_mark(h0, 2); launch_k(h0, k_link_lim<T, MASK>, gLm, (size_t)0, lm); prof_mark(h0, -1); }
   }

@@ -733,6 +733,9 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
   } else if (option == DGADV_OPT_TAYLOR_MASS) {
     if (value != 0 && value != 1) return DGADV_EINVAL;
     h->mtOnTheFly = value == 1;
+  } else if (option == DGADV_OPT_OP_BLOCK) {
+    if (value != 64 && value != 128) return DGADV_EINVAL;
+    h->opBlock = value;
   } else if (option == DGADV_OPT_VOLUME_MMA) {
     if (value != 0 && value != 1) return DGADV_EINVAL;
     if (value && (h->prec != DGADV_FP32 || h->p < 2)) {
@@ -763,6 +766,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   else if (option == DGADV_OPT_ADJ_WARPS) *value = h->adjWarps;
   else if (option == DGADV_OPT_TAYLOR_MASS) *value = h->mtOnTheFly ? 1 : 0;
   else if (option == DGADV_OPT_VOLUME_MMA) *value = h->volumeMma ? 1 : 0;
+  else if (option == DGADV_OPT_OP_BLOCK) *value = h->opBlock;
   else return DGADV_EINVAL;
   return DGADV_OK;
   });

@@ -110,6 +110,12 @@ class Ensemble:
         for s in self.solvers.values():
             s.step(nSteps, nStep0, self.tau)
 
+    def unlink(self):
+        """Back to one handle per degree group, each on its own stream."""
+        if self.primary is not None:
+            self.primary.link(None)
+            self.primary = None
+
     def kernels_per_step(self):
         """Launches per time step: of the linked step, or per group."""
         if self.primary is not None:

@@ -72,10 +72,12 @@ enum {
                                    stored per-element block, 1 rebuilds it from the element's B
                                    and a constant table (default: 1 in FP32, 0 otherwise); the
                                    results agree to roundoff                                   */
-  DGADV_OPT_VOLUME_MMA = 6      /* 1: the volume term's two contractions on the tensor cores
+  DGADV_OPT_VOLUME_MMA = 6,     /* 1: the volume term's two contractions on the tensor cores
                                    (tcgen05, split TF32 with FP32 accumulation; FP32 handles,
                                    p >= 2, time-derivative limiting, no source terms); 0 (the
                                    default): FP32 multiply-adds                                */
+  DGADV_OPT_OP_BLOCK = 7        /* elements per thread block of the stage operator, one thread
+                                   per element: 64 or 128 (default); results unchanged        */
 };
 
 /* ---- host helpers: static data ------------------------------------------------------- */

@@ -149,7 +149,7 @@ def test_linked_groups_equal_separate_groups_bitwise(lib, precision):
     for a, b in zip(runs[True][0], runs[False][0]):
         assert np.array_equal(a, b)
     assert runs[True][1] == {'linked': 9}                # 3 stages x (operator, cDot limiter, limiter)
-    assert sum(runs[False][1].values()) == 6 + 9
+    assert runs[False][1] == {1: 2 * 2, 2: 3 * 3}        # p = 1: 2 stages x (operator, limiter)
 
 
 def test_link_refuses_what_it_does_not_cover(lib):
@@ -175,3 +175,19 @@ def test_link_refuses_what_it_does_not_cover(lib):
         assert e.value.status == L.DGADV_EUNSUPPORTED
     finally:
         hier.close()
+
+
+def test_linked_operator_block_size_leaves_results_unchanged(lib):
+    from festung_gb300 import _lib as L
+    from festung_gb300 import ensemble as E
+    out = []
+    for eb in (128, 64):
+        ens = E.Ensemble(list(range(6)), precision='fp32', numSteps=12, hmax=2 ** -4)
+        try:
+            ens.primary.set_option(L.OPT_OP_BLOCK, eb)
+            ens.step(12)
+            out.append(ens.states())
+        finally:
+            ens.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)

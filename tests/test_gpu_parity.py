@@ -278,3 +278,16 @@ def test_volume_mma_refused_outside_fp32(lib):
     with pytest.raises(L.DgadvError) as e:
         gpu_run(precision='fp64', gpuOptions={L.OPT_VOLUME_MMA: 1}, **kw)
     assert e.value.status == L.DGADV_EUNSUPPORTED
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'fp64'])
+@pytest.mark.parametrize('lim', ['linear', 'hierarch_vert'])
+def test_operator_block_size_leaves_results_unchanged(lib, precision, lim):
+    """DGADV_OPT_OP_BLOCK = 64: the stage operator's tiles of 64 elements give bitwise the
+    results of 128-element tiles (the same per-element arithmetic and vertex patches)."""
+    from festung_gb300 import _lib as L
+    kw = dict(testcase='gauss_slot', hmax=2 ** -4, p=2, tEnd=0.05, numSteps=20, isSlopeLim=True, typeSlopeLim=lim,
+              jitter=0.1, meshSeed=3)
+    a = gpu_run(precision=precision, gpuOptions={L.OPT_OP_BLOCK: 64}, **kw)
+    b = gpu_run(precision=precision, **kw)
+    assert np.array_equal(a.cDisc, b.cDisc)
