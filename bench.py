@@ -761,11 +761,13 @@ def hbm_block(device, flush, reps=2):
     return out
 
 
-def side_path(wl, precision, device, c0, flush, reps):
+def side_path(wl, precision, device, c0, flush, reps, options=None):
     """One precision on the headline workload: `reps` solves from c0 (each after an L2 flush),
     the mean device time and the last final state, with its kernel table."""
     pd = setup_problem(wl, precision, device)
     s = pd.solver
+    for o, v in (options or {}).items():
+        s.set_option(o, v)
     s.step(pd.numSteps, 0, pd.tau)             # warm-up solve (graph capture, first launches)
     s.sync()
     ts, c = time_solves(s, c0, pd.numSteps, pd.tau, reps, flush)
@@ -880,12 +882,18 @@ def run_ours(args):
     s.close()
 
     if rank == 0 and not args.no_fp64:
+        from festung_gb300 import _lib as L
         paths = {'fp64': (value, 0.0)}
-        for prec in ('fp32',) + (() if args.no_df32 else ('df32',)):
-            row, c = side_path(wl, prec, device, c0, flush, reps=3)
+        # fp32: everything FP32; df32: everything double-float (~48 bits on the FP32 units);
+        # df32_operator_fp32: double-float state, SSP update and limiter, the operator in FP32
+        variants = [('fp32', 'fp32', None)]
+        if not args.no_df32:
+            variants += [('df32', 'df32', None), ('df32_operator_fp32', 'df32', {L.OPT_OPERATOR_FP32: 1})]
+        for name, prec, opts in variants:
+            row, c = side_path(wl, prec, device, c0, flush, reps=3, options=opts)
             row['rel_l2_vs_fp64'] = float(np.linalg.norm(c - c64) / np.linalg.norm(c64))
-            result[prec] = row
-            paths[prec] = (row['value'], row['rel_l2_vs_fp64'])
+            result[name] = row
+            paths[name] = (row['value'], row['rel_l2_vs_fp64'])
         result['fp32']['roofline']['note'] = ('L2-resident: the FP32 working set (~31 MB) stays in '
                                               'the 129 MB L2 within a solve; see hbm_case')
         result['fp32']['roofline']['traffic'] = MEASURED_TRAFFIC.get((wl, 'fp32', result['fp32']['roofline']['kernel']))

@@ -92,6 +92,13 @@ template <> __device__ __forceinline__ df32 okey_inv<df32>(unsigned long long k)
 template <> __host__ __device__ constexpr unsigned long long key_max<df32>() { return ~0ULL; }
 __device__ __forceinline__ bool finite_(const df32 &x) { return isfinite(x.hi) && isfinite(x.lo); }
 
+// A stored real in an arithmetic type A: itself, or a double-float's head in FP32 (|lo| is at
+// most half an FP32 unit of hi).
+template <typename A, typename T> __device__ __forceinline__ A as_arith(const T &x) {
+  if constexpr (std::is_same_v<A, T>) return x;
+  else return x.hi;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Sum of products s = s0 + sum a_k b_k.  float / double: the plain multiply-add s += a b.  df32:
 // the running sum is an FP32 head, advanced by one exact two_sum per term, and an FP32 tail that
@@ -841,10 +848,13 @@ struct StageScalars {
   int *flag;            // bit 0: non-finite value seen; bit 1: a bounded wait timed out
 };
 
-template <typename T, int P, int MODE, bool RHS, bool LIN>
+template <typename T, int P, int MODE, bool RHS, bool LIN, bool OPF = false>
 __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, const T *c0, T *out,
            const LimOut<T> lo, const StageScalars sc, const int tile, const int nTiles = -1) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
+  // OPF (double-float state only): the operator (volume, flux, hatM^-1 = I) in FP32 arithmetic;
+  // the SSP update, the outputs and the limiter's quantities stay in the stored type
+  using A = std::conditional_t<OPF, float, T>;
   constexpr int NT = StageRows<T, P>::op(MODE, LIN);
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x));
@@ -879,44 +889,44 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
     if (MODE != 2) stage_T(smem, rC0, c0, N, Kp, k0, bar);
   }
   // neighbour coefficients: outside the block from global memory now, inside from shared later
-  T cn[3][N];
+  A cn[3][N];
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
     const bool outside = nb[n] >= 0 && (nb[n] < k0 || nb[n] >= k0 + eb);
 #pragma unroll
-    for (int j = 0; j < N; ++j) cn[n][j] = outside ? cin[(size_t)j * Kp + nb[n]] : T(0);
+    for (int j = 0; j < N; ++j) cn[n][j] = outside ? as_arith<A>(cin[(size_t)j * Kp + nb[n]]) : A(0);
   }
   const bool ok = mbar_wait_bounded(bar, sc.flag);
   T qv[NQ];
   bool bad = false;
   if (active && ok) {
-    T c[N];
-    Acc<T> rhs[N];
+    A c[N];
+    Acc<A> rhs[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) { c[i] = srow<T>(smem, rC + i)[t]; rhs[i] = Acc<T>(T(0)); }
+    for (int i = 0; i < N; ++i) { c[i] = as_arith<A>(srow<T>(smem, rC + i)[t]); rhs[i] = Acc<A>(A(0)); }
 #pragma unroll
     for (int n = 0; n < 3; ++n)
       if (nb[n] >= k0 && nb[n] < k0 + eb)
 #pragma unroll
-        for (int j = 0; j < N; ++j) cn[n][j] = srow<T>(smem, rC + j)[nb[n] - k0];
+        for (int j = 0; j < N; ++j) cn[n][j] = as_arith<A>(srow<T>(smem, rC + j)[nb[n] - k0]);
     if (RHS) {
       for (int m = 0; m < g.nTerms; ++m) {
-        const T gm = T(sc.gco[m]);
+        const A gm = A(sc.gco[m]);
 #pragma unroll
-        for (int i = 0; i < N; ++i) rhs[i].fma(gm, g.rhs[((size_t)m * N + i) * Kp + k]);
+        for (int i = 0; i < N; ++i) rhs[i].fma(gm, as_arith<A>(g.rhs[((size_t)m * N + i) * Kp + k]));
       }
     }
     // volume term (at p = 3, 12 points: unrolled by 3 to keep the body in the instruction cache)
 #pragma unroll(P >= 3 ? 3 : Q)
     for (int qq = 0; qq < Q; ++qq) {
-      Acc<T> cqa(T(0));
+      Acc<A> cqa(A(0));
 #pragma unroll
-      for (int j = 0; j < N; ++j) cqa.fma(tb.phiQ[qq][j], c[j]);
-      const T cq = cqa.get();
-      const T f1 = srow<T>(smem, rF + qq)[t] * cq;
-      const T f2 = srow<T>(smem, rF + Q + qq)[t] * cq;
+      for (int j = 0; j < N; ++j) cqa.fma(as_arith<A>(tb.phiQ[qq][j]), c[j]);
+      const A cq = cqa.get();
+      const A f1 = as_arith<A>(srow<T>(smem, rF + qq)[t]) * cq;
+      const A f2 = as_arith<A>(srow<T>(smem, rF + Q + qq)[t]) * cq;
 #pragma unroll
-      for (int i = 0; i < N; ++i) { rhs[i].fma(tb.g1[qq][i], f1); rhs[i].fma(tb.g2[qq][i], f2); }
+      for (int i = 0; i < N; ++i) { rhs[i].fma(as_arith<A>(tb.g1[qq][i]), f1); rhs[i].fma(as_arith<A>(tb.g2[qq][i]), f2); }
     }
     // upwind edge term
     const int code = irow<T>(smem, NT, 0)[t];
@@ -926,36 +936,36 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
       const bool outOk = (code >> (6 + n)) & 1;
 #pragma unroll
       for (int r2 = 0; r2 < R; ++r2) {
-        const T v = srow<T>(smem, rV + n * R + r2)[t];
-        Acc<T> tr(T(0));
-        if (v > T(0) && outOk) {
+        const A v = as_arith<A>(srow<T>(smem, rV + n * R + r2)[t]);
+        Acc<A> tr(A(0));
+        if (v > A(0) && outOk) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) tr.fma(tb.phi1D[n][r2][j], c[j]);
-        } else if (v < T(0) && nb[n] >= 0) {
+          for (int j = 0; j < N; ++j) tr.fma(as_arith<A>(tb.phi1D[n][r2][j]), c[j]);
+        } else if (v < A(0) && nb[n] >= 0) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) tr.fma(tb.thetaPhi[n][np][r2][j], cn[n][j]);
+          for (int j = 0; j < N; ++j) tr.fma(as_arith<A>(tb.thetaPhi[n][np][r2][j]), cn[n][j]);
         }
-        const T fl = v * tr.get();
+        const A fl = v * tr.get();
 #pragma unroll
-        for (int i = 0; i < N; ++i) rhs[i].fms(tb.phi1D[n][r2][i], fl);
+        for (int i = 0; i < N; ++i) rhs[i].fms(as_arith<A>(tb.phi1D[n][r2][i]), fl);
       }
     }
     // mass solve
     T cdot[N];
-    if (sizeof(T) == 8) {
-      T r[N];
+    if constexpr (sizeof(A) == 8) {
+      A r[N];
 #pragma unroll
       for (int j = 0; j < N; ++j) r[j] = rhs[j].get();
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        Acc<T> s(T(0));
+        Acc<A> s(A(0));
 #pragma unroll
         for (int j = 0; j < N; ++j) s.fma(tb.hatMinv[i][j], r[j]);
         cdot[i] = s.get();
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < N; ++i) cdot[i] = rhs[i].get();
+      for (int i = 0; i < N; ++i) cdot[i] = T(rhs[i].get());
     }
     if (MODE == 2 && LIN) {
 #pragma unroll
@@ -973,7 +983,8 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
       const T w = T(sc.omega), tau = T(sc.tau);
       T cnew[N];
 #pragma unroll
-      for (int i = 0; i < N; ++i) cnew[i] = w * srow<T>(smem, rC0 + i)[t] + (T(1) - w) * (c[i] + tau * cdot[i]);
+      for (int i = 0; i < N; ++i)
+        cnew[i] = w * srow<T>(smem, rC0 + i)[t] + (T(1) - w) * (srow<T>(smem, rC + i)[t] + tau * cdot[i]);
       if (MODE == 0 || LIN) {
 #pragma unroll
         for (int i = 0; i < N; ++i) { out[(size_t)i * Kp + k] = cnew[i]; bad |= !finite_(cnew[i]); }
@@ -992,11 +1003,11 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
   if (MODE != 0) scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok, tile);
   if (bad) atomicOr(sc.flag, 1);
 }
-template <typename T, int P, int MODE, bool RHS, bool LIN>
+template <typename T, int P, int MODE, bool RHS, bool LIN, bool OPF = false>
 __global__ void __launch_bounds__(kBlock)
 k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
            const LimOut<T> lo, const StageScalars sc) {
-  stage_op_tile<T, P, MODE, RHS, LIN>(g, cin, c0, out, lo, sc, blockIdx.x);
+  stage_op_tile<T, P, MODE, RHS, LIN, OPF>(g, cin, c0, out, lo, sc, blockIdx.x);
 }
 
 // The stage operator with the volume term on the tensor cores (dgadv_mma.cuh): FP32, p >= 2,

@@ -52,6 +52,7 @@ struct dgadv_handle {
   bool mtOnTheFly = false;             // Taylor mass correction rebuilt from B (DGADV_OPT_TAYLOR_MASS)
   bool volumeMma = false;              // volume term on the tensor cores (DGADV_OPT_VOLUME_MMA)
   int opBlock = 128;                   // elements per block of the stage operator (DGADV_OPT_OP_BLOCK)
+  bool opFp32 = false;                 // double-float handle, FP32 operator (DGADV_OPT_OPERATOR_FP32)
   // linked stepping (dgadv_link): this handle steps the handles in `linked` together with itself,
   // one launch per stage kernel; a handle in another's list has that handle as linkedTo
   std::vector<dgadv_handle *> linked;

@@ -205,6 +205,18 @@ static cudaError_t set_smem_attributes() {
   set((const void *)k_stage_op<T, P, 2, true, true>, SR::bytes(SR::op(2, true), 1));
   set((const void *)k_stage_op<T, P, 2, false, true>, SR::bytes(SR::op(2, true), 1));
   set((const void *)k_limit_dot_lin<T, P>, SR::bytes(SR::limdot_lin(), 1));
+  if constexpr (std::is_same_v<T, df32>) {   // the FP32-operator variants (DGADV_OPT_OPERATOR_FP32)
+    set((const void *)k_stage_op<T, P, 0, true, false, true>, SR::bytes(SR::op(0, false), 1));
+    set((const void *)k_stage_op<T, P, 0, false, false, true>, SR::bytes(SR::op(0, false), 1));
+    set((const void *)k_stage_op<T, P, 1, true, false, true>, SR::bytes(SR::op(1, false), 1));
+    set((const void *)k_stage_op<T, P, 1, false, false, true>, SR::bytes(SR::op(1, false), 1));
+    set((const void *)k_stage_op<T, P, 2, true, false, true>, SR::bytes(SR::op(2, false), 1));
+    set((const void *)k_stage_op<T, P, 2, false, false, true>, SR::bytes(SR::op(2, false), 1));
+    set((const void *)k_stage_op<T, P, 1, true, true, true>, SR::bytes(SR::op(1, true), 1));
+    set((const void *)k_stage_op<T, P, 1, false, true, true>, SR::bytes(SR::op(1, true), 1));
+    set((const void *)k_stage_op<T, P, 2, true, true, true>, SR::bytes(SR::op(2, true), 1));
+    set((const void *)k_stage_op<T, P, 2, false, true, true>, SR::bytes(SR::op(2, true), 1));
+  }
   if constexpr (FUSED) {
     set((const void *)k_op_fused<T, P, 1, true>, SR::bytes(SR::op(1, true), 1));
     set((const void *)k_op_fused<T, P, 1, false>, SR::bytes(SR::op(1, true), 1));
@@ -221,6 +233,15 @@ static cudaError_t set_smem_attributes() {
     set((const void *)k_stage_op_mma<P, false>, MmaSmem<P>::bytes(false));
   }
   return e;
+}
+
+// The stage operator kernel of a handle: with DGADV_OPT_OPERATOR_FP32 on a double-float handle,
+// the variant whose operator arithmetic is FP32 (state, SSP update and limiter in double-float).
+template <typename T, int P, int MODE, bool RHS, bool LIN>
+static auto stage_kernel(const dgadv_handle *h) -> decltype(&k_stage_op<T, P, MODE, RHS, LIN, false>) {
+  if constexpr (std::is_same_v<T, df32>)
+    if (h->opFp32) return &k_stage_op<T, P, MODE, RHS, LIN, true>;
+  return &k_stage_op<T, P, MODE, RHS, LIN, false>;
 }
 
 template <typename T, int P>
@@ -251,8 +272,8 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     LimOut<T> lo{};
     if (!h->lim) {
       prof_mark(h, 0);
-      if (rhs) launch_kb(h, k_stage_op<T, P, 0, true, false>, gridOp, eb, SR::bytes(SR::op(0, false), 1, eb), g, in, cn, out, lo, sc);
-      else launch_kb(h, k_stage_op<T, P, 0, false, false>, gridOp, eb, SR::bytes(SR::op(0, false), 1, eb), g, in, cn, out, lo, sc);
+      if (rhs) launch_kb(h, stage_kernel<T, P, 0, true, false>(h), gridOp, eb, SR::bytes(SR::op(0, false), 1, eb), g, in, cn, out, lo, sc);
+      else launch_kb(h, stage_kernel<T, P, 0, false, false>(h), gridOp, eb, SR::bytes(SR::op(0, false), 1, eb), g, in, cn, out, lo, sc);
       prof_mark(h, -1);
       continue;
     }
@@ -280,19 +301,19 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     if (viaMma) {
     } else if (mode == 2) {
       if (lin) {
-        if (rhs) launch_kb(h, k_stage_op<T, P, 2, true, true>, gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
-        else launch_kb(h, k_stage_op<T, P, 2, false, true>, gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 2, true, true>(h), gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 2, false, true>(h), gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
       } else {
-        if (rhs) launch_kb(h, k_stage_op<T, P, 2, true, false>, gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, tb, lo1, sc);
-        else launch_kb(h, k_stage_op<T, P, 2, false, false>, gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, tb, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 2, true, false>(h), gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, tb, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 2, false, false>(h), gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, tb, lo1, sc);
       }
     } else {
       if (lin) {
-        if (rhs) launch_kb(h, k_stage_op<T, P, 1, true, true>, gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
-        else launch_kb(h, k_stage_op<T, P, 1, false, true>, gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 1, true, true>(h), gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 1, false, true>(h), gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
       } else {
-        if (rhs) launch_kb(h, k_stage_op<T, P, 1, true, false>, gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, tb, lo1, sc);
-        else launch_kb(h, k_stage_op<T, P, 1, false, false>, gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, tb, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 1, true, false>(h), gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, tb, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 1, false, false>(h), gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, tb, lo1, sc);
       }
     }
     prof_mark(h, -1);

@@ -733,6 +733,10 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
   } else if (option == DGADV_OPT_TAYLOR_MASS) {
     if (value != 0 && value != 1) return DGADV_EINVAL;
     h->mtOnTheFly = value == 1;
+  } else if (option == DGADV_OPT_OPERATOR_FP32) {
+    if (value != 0 && value != 1) return DGADV_EINVAL;
+    if (value && h->prec != DGADV_DF32) { h->err = "the FP32 operator is an option of double-float handles"; return DGADV_EUNSUPPORTED; }
+    h->opFp32 = value == 1;
   } else if (option == DGADV_OPT_OP_BLOCK) {
     if (value != 64 && value != 128) return DGADV_EINVAL;
     h->opBlock = value;
@@ -767,6 +771,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   else if (option == DGADV_OPT_TAYLOR_MASS) *value = h->mtOnTheFly ? 1 : 0;
   else if (option == DGADV_OPT_VOLUME_MMA) *value = h->volumeMma ? 1 : 0;
   else if (option == DGADV_OPT_OP_BLOCK) *value = h->opBlock;
+  else if (option == DGADV_OPT_OPERATOR_FP32) *value = h->opFp32 ? 1 : 0;
   else return DGADV_EINVAL;
   return DGADV_OK;
   });

@@ -76,8 +76,12 @@ enum {
                                    (tcgen05, split TF32 with FP32 accumulation; FP32 handles,
                                    p >= 2, time-derivative limiting, no source terms); 0 (the
                                    default): FP32 multiply-adds                                */
-  DGADV_OPT_OP_BLOCK = 7        /* elements per thread block of the stage operator, one thread
+  DGADV_OPT_OP_BLOCK = 7,       /* elements per thread block of the stage operator, one thread
                                    per element: 64 or 128 (default); results unchanged        */
+  DGADV_OPT_OPERATOR_FP32 = 8   /* double-float handles: 1 computes the stage operator (volume,
+                                   flux, mass) in FP32 arithmetic while the state, the SSP
+                                   update and the limiter stay double-float; 0 (default): all
+                                   double-float                                              */
 };
 
 /* ---- host helpers: static data ------------------------------------------------------- */

@@ -291,3 +291,19 @@ def test_operator_block_size_leaves_results_unchanged(lib, precision, lim):
     a = gpu_run(precision=precision, gpuOptions={L.OPT_OP_BLOCK: 64}, **kw)
     b = gpu_run(precision=precision, **kw)
     assert np.array_equal(a.cDisc, b.cDisc)
+
+
+@pytest.mark.parametrize('kw', [dict(testcase='gauss_slot', hmax=2 ** -4, p=2, tEnd=0.05, numSteps=20, isSlopeLim=True),
+                                dict(testcase='gauss_slot', hmax=2 ** -4, p=3, tEnd=0.02, numSteps=10, isSlopeLim=True,
+                                     typeSlopeLim='hierarch_vert', jitter=0.1, meshSeed=7),
+                                dict(testcase='transient', hmax=2 ** -3, p=2, tEnd=0.1, numSteps=20)],
+                         ids=['p2-linear', 'p3-hier-jitter', 'transient-p2'])
+def test_fp32_operator_on_double_float_state(lib, kw):
+    """DGADV_OPT_OPERATOR_FP32 on a double-float handle: the operator's FP32 rounding enters the
+    state scaled by tau, so the run lands far closer to FP64 than the all-FP32 path."""
+    from festung_gb300 import _lib as L
+    m = gpu_run(precision='df32', gpuOptions={L.OPT_OPERATOR_FP32: 1}, **kw)
+    d = gpu_run(precision='fp64', **kw)
+    f = gpu_run(precision='fp32', **kw)
+    em, ef = rel(m.cDisc, d.cDisc), rel(f.cDisc, d.cDisc)
+    assert em <= 1e-6 and em < ef, (em, ef)
