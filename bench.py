@@ -50,6 +50,11 @@ WORKLOADS = {
     'gauss_slot_2048_p1': dict(testcase='gauss_slot', hmax=2 ** -5, p=1, numSteps=500, tEnd=0.5,
                                isSlopeLim=True, typeSlopeLim='linear', ordRK=2),
     # 2,097,152 triangles with 10% node jitter, p = 3, hierarchical vertex limiter
+    # p = 3 with the hierarchical limiter on the 131072-triangle mesh (profiling captures of the
+    # p = 3 stage kernels at a size a full capture handles)
+    'gauss_slot_131k_p3_hier': dict(testcase='gauss_slot', hmax=2 ** -8, p=3, numSteps=100, tEnd=100 * 2e-5,
+                                    isSlopeLim=True, typeSlopeLim='hierarch_vert', ordRK=3, jitter=0.1,
+                                    meshSeed=5),
     'gauss_slot_2M_p3_hier': dict(testcase='gauss_slot', hmax=2 ** -10, p=3, numSteps=100, tEnd=100 * 2e-5,
                                   isSlopeLim=True, typeSlopeLim='hierarch_vert', ordRK=3, jitter=0.1,
                                   meshSeed=5),
@@ -64,10 +69,12 @@ def dist_env():
 
 
 # ---------------------------------------------------------------------------------------------
-def algorithmic_bytes(kind, w, N, Q, R, nc):
+def algorithmic_bytes(kind, w, N, Q, R, nc, mtRows=0):
     """Unique bytes per element a launch of each kernel kind must move (its own element's
     inputs and outputs plus the static per-element data; neighbour gathers re-read the same
-    arrays and count once)."""
+    arrays and count once).  mtRows: the per-element rows of the time-derivative limiter's Taylor
+    mass correction (N(N-1) of Q_k for the linear limiter, N(N+1)/2 packed M_T and the 4 of B
+    for the hierarchical one, or the 4 of B when it is rebuilt from B)."""
     csr = 14                                    # vertex CSR (vptr ~ 2 B, vidx 12 B per element)
     if kind == 'op0':                           # stage operator, limiter off: c, c^n, F, Vn, ints, out
         return w * (3 * N + 2 * Q + 3 * R) + 16
@@ -75,8 +82,8 @@ def algorithmic_bytes(kind, w, N, Q, R, nc):
         return w * (3 * N + 2 * Q + 3 * R + 4 + nc) + 16
     if kind == 'op2':                           # c, F, Vn, B, ints; Taylor(cDot) and q out
         return w * (2 * N + 2 * Q + 3 * R + 4 + nc) + 16
-    if kind == 'limdot':                        # Taylor in/out, B, M_T, c^n, c^(s-1), q in/out
-        return w * (4 * N + 4 + N * (N + 1) // 2 + 2 * nc) + 16 + csr
+    if kind == 'limdot':                        # cDot in, out, c^n, c^(s-1), correction rows, q in/out
+        return w * (4 * N + mtRows + 2 * nc) + 16 + csr
     if kind == 'lim':                           # Taylor in, B, q, modal out
         return w * (2 * N + 4 + nc) + 16 + csr
     raise ValueError(kind)
@@ -297,8 +304,9 @@ def large_block(device, flush):
             dom = int(np.argmax(shares))
             peak, peak_kind = measured_peaks()
             kern = {}
+            mtr = mt_rows(s, pd)
             for i in range(3):
-                b = algorithmic_bytes(kinds[i], w, N, Q, R, nc) * K
+                b = algorithmic_bytes(kinds[i], w, N, Q, R, nc, mtr) * K
                 live = ms * shares[i] / tot / (nl[i] / 4.0 * pd.numSteps)
                 kern[names[i]] = {'ms_per_launch_isolated': kpl[i], 'ms_per_launch_live': live,
                                   'share': shares[i] / tot, 'algorithmic_bytes_per_launch': b,
@@ -698,6 +706,7 @@ def kernel_table(s, pd, w, ms_per_solve, profSteps=20):
     kpl, nlaunch = s.profile_kernels(profSteps, 0, pd.tau)
     N, Q, R = pd.N, {0: 1, 1: 3, 2: 6, 3: 12}[pd.p], pd.p + 1
     nc = 1 if pd.typeSlopeLim == 'linear' else pd.p * (pd.p + 1) // 2
+    mtRows = mt_rows(s, pd)
     op_kind = 'op0' if not pd.isSlopeLim else ('op2' if pd.p > 1 else 'op1')
     kinds = [op_kind, 'limdot', 'lim']
     names = ['k_stage_op', 'k_limit_dot', 'k_limit']
@@ -708,7 +717,7 @@ def kernel_table(s, pd, w, ms_per_solve, profSteps=20):
     for i in range(3):
         if not nlaunch[i] or kpl[i] <= 0:
             continue
-        b = algorithmic_bytes(kinds[i], w, N, Q, R, nc) * pd.K
+        b = algorithmic_bytes(kinds[i], w, N, Q, R, nc, mtRows) * pd.K
         per_solve = nlaunch[i] / float(profSteps) * pd.numSteps
         live = ms_per_solve * shares[i] / tot / per_solve
         kern[names[i]] = {'ms_per_launch_isolated': kpl[i], 'ms_per_launch_live': live,
@@ -724,6 +733,15 @@ def kernel_table(s, pd, w, ms_per_solve, profSteps=20):
                       'profiling pass) / launches per solve',
             'achieved_isolated': ai, 'frac_isolated': ai / peak}
     return kern, roof
+
+
+def mt_rows(s, pd):
+    """Per-element rows the time-derivative limiter reads for its Taylor mass correction."""
+    from festung_gb300 import _lib as L
+    N = pd.N
+    if s.get_option(L.OPT_TAYLOR_MASS):
+        return 4
+    return N * (N - 1) if pd.typeSlopeLim == 'linear' else N * (N + 1) // 2 + 4
 
 
 def whole_stage_roofline(pd, w, ms_per_solve):
@@ -768,6 +786,8 @@ def side_path(wl, precision, device, c0, flush, reps, options=None):
     s = pd.solver
     for o, v in (options or {}).items():
         s.set_option(o, v)
+    from festung_gb300 import autotune as AT
+    tuned = AT.tune(s, pd.tau, nSteps=24, reps=2, fused_ok=(pd.typeSlopeLim == 'linear' and precision != 'df32'))[0]
     s.step(pd.numSteps, 0, pd.tau)             # warm-up solve (graph capture, first launches)
     s.sync()
     ts, c = time_solves(s, c0, pd.numSteps, pd.tau, reps, flush)
@@ -776,7 +796,7 @@ def side_path(wl, precision, device, c0, flush, reps, options=None):
     w = 8 if precision in ('fp64', 'df32') else 4
     kern, roof = kernel_table(s, pd, w, ms)
     s.close()
-    return {'value': units / (ms / 1e3), 'unit': 'DOF-stage/s', 'ms_per_solve': ms,
+    return {'value': units / (ms / 1e3), 'unit': 'DOF-stage/s', 'ms_per_solve': ms, 'launch': tuned,
             'kernels': kern, 'roofline': roof, 'whole_stage': whole_stage_roofline(pd, w, ms)}, c
 
 
@@ -970,6 +990,8 @@ def main():
                     help='adjoint profiling case: checkpoint slots (0: every stage stored)')
     ap.add_argument('--ncu-limited', action='store_true', help='adjoint profiling case: linear limiter on')
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64', 'df32'])
+    ap.add_argument('--ncu-option', action='append', default=[],
+                    help='profiling driver: DGADV_OPT_* option as NAME=VALUE (e.g. VOLUME_MMA=1)')
     args = ap.parse_args()
     if args.ncu_case == 'adjoint':
         # one recorded run and its reverse sweep (p = 2, hmax = 2^-e), for profiling
@@ -1002,7 +1024,11 @@ def main():
         pd.solver.close()
         return 0
     if args.ncu_case:
+        from festung_gb300 import _lib as L
         pd = setup_problem(args.ncu_case, args.precision, 0)
+        for o in args.ncu_option:
+            name, val = o.split('=')
+            pd.solver.set_option(getattr(L, 'OPT_' + name), int(val))
         pd.solver.step(args.ncu_steps, 0, pd.tau)
         pd.solver.sync()
         pd.solver.close()

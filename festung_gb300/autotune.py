@@ -6,7 +6,9 @@ configurations this library has and keeps the fastest:
 - programmatic dependent launch on or off;
 - the number of time steps per captured CUDA graph;
 - the stage operator's elements per CTA, 64 or 128 (one thread per element; separate-pass
-  pipeline, and the linked step of an ensemble's degree groups).
+  pipeline, and the linked step of an ensemble's degree groups);
+- with time-derivative limiting, the Taylor mass correction from stored blocks or rebuilt from
+  each element's B (tried on the best configuration of the above).
 Each candidate runs ``nSteps`` steps of the handle's own problem after one warm-up call, timed
 with CUDA events on the handle's stream; the state is restored afterwards.  The choice can be
 kept in a JSON file keyed by the problem's signature and the GPU name, and reused.
@@ -58,6 +60,8 @@ def tune(solver, tau, nSteps=48, reps=3, fused_ok=False, cache=None, key=None):
             solver.set_option(L.OPT_FLAGS, best['flags'])
             solver.set_option(L.OPT_GRAPH_STEPS, best['graphSteps'])
             solver.set_option(L.OPT_OP_BLOCK, best.get('opBlock', 128))
+            if 'taylorMass' in best:
+                solver.set_option(L.OPT_TAYLOR_MASS, best['taylorMass'])
             return best, stored[key]['table']
     state = solver.get_state()
     table = []
@@ -75,6 +79,21 @@ def tune(solver, tau, nSteps=48, reps=3, fused_ok=False, cache=None, key=None):
     solver.set_option(L.OPT_FLAGS, best['flags'])
     solver.set_option(L.OPT_GRAPH_STEPS, best['graphSteps'])
     solver.set_option(L.OPT_OP_BLOCK, best['opBlock'])
+    if solver.p >= 2 and solver.limiter != 'none':
+        # with time-derivative limiting: the Taylor mass correction read from stored blocks or
+        # rebuilt from B, tried once on the best configuration (the stored blocks win where
+        # they stay in L2, the rebuild where they would stream from DRAM)
+        cur = solver.get_option(L.OPT_TAYLOR_MASS)
+        times = {cur: best['ms_per_step']}
+        alt = 1 - cur
+        solver.set_option(L.OPT_TAYLOR_MASS, alt)
+        solver.set_state(state)
+        solver.time_steps(nSteps, 0, tau)
+        times[alt] = min(solver.time_steps(nSteps, 0, tau) for _ in range(reps)) / nSteps
+        table.append(dict(best, taylorMass=alt, ms_per_step=times[alt]))
+        best['taylorMass'] = min(times, key=times.get)
+        best['ms_per_step'] = times[best['taylorMass']]
+        solver.set_option(L.OPT_TAYLOR_MASS, best['taylorMass'])
     solver.set_state(state)
     if cache and key:
         stored = {}

@@ -386,6 +386,7 @@ extern "C" int dgadv_set_velocity_theta(dgadv_handle *h, const double *theta) {
 extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau, int32_t nSnapshots) {
   return guarded(h, [&]() -> int {
   if (!h || nSteps < 1 || !(tau > 0.0)) return DGADV_EINVAL;
+  if (h->poisoned) { h->err = "a bounded wait of a stage kernel timed out earlier: create a new handle"; return DGADV_ETIMEOUT; }
   const PrecOps &o = ops_of(h);
   if (!o.adj_stage) { h->err = "no adjoint kernels for this precision"; return DGADV_EUNSUPPORTED; }
   if (h->flags & DGADV_FLAG_IMPLICIT) { h->err = "the adjoint covers the explicit scheme"; return DGADV_EUNSUPPORTED; }
@@ -488,6 +489,7 @@ extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc
   return guarded(h, [&]() -> int {
   if (!h || !dJdcT) return DGADV_EINVAL;
   if (!h->recorded) { h->err = "no recorded forward run"; return DGADV_EINVAL; }
+  if (h->poisoned) { h->err = "a bounded wait of a stage kernel timed out earlier: create a new handle"; return DGADV_ETIMEOUT; }
   const PrecOps &o = ops_of(h);
   DG_CUDA(cudaSetDevice(h->device));
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;

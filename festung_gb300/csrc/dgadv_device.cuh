@@ -512,6 +512,11 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
+// Ends an mbarrier object's life before its shared memory is put to other use (a kernel that
+// runs several tiles per block, with different row layouts, reuses the locations).
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -527,7 +532,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *flag) {
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, 0))
     if (clock64() - t0 > (1LL << 31)) {
-      atomicOr(flag, 2);
+      atomicOr(flag, 2 | 4);                      // bit 2: a staging copy
       const long long t1 = clock64();
       while (!mbar_try_wait(bar, 0) && clock64() - t1 < (1LL << 31)) {
       }

@@ -130,6 +130,7 @@ struct dgadv_handle {
   int recSteps = 0;
   double recTau = 0.0;
   bool recorded = false;
+  bool poisoned = false;               // a stage kernel's bounded wait gave up: no further steps
   std::string err;
 };
 

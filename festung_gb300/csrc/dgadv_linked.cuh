@@ -27,6 +27,8 @@ template <typename T> struct LinkPart {
   LimOut<T> lo;
   StageScalars sc;
 };
+// Passed as a __grid_constant__ parameter: a block indexes its part in the parameter space
+// directly, instead of every thread copying the table to local memory first.
 template <typename T> struct LinkArgs {
   int n;
   LinkPart<T> part[kMaxLinked];
@@ -42,7 +44,7 @@ __device__ __forceinline__ int link_part(const LinkArgs<T> &a) {
 }
 
 template <typename T, int MASK>
-__global__ void __launch_bounds__(kBlock) k_link_op(const LinkArgs<T> a) {
+__global__ void __launch_bounds__(kBlock) k_link_op(const __grid_constant__ LinkArgs<T> a) {
   const int i = link_part(a);
   const LinkPart<T> &q = a.part[i];
   const int tile = blockIdx.x - q.block0;
@@ -60,7 +62,7 @@ __global__ void __launch_bounds__(kBlock) k_link_op(const LinkArgs<T> a) {
 }
 
 template <typename T, int MASK>
-__global__ void __launch_bounds__(kBlock) k_link_limdot(const LinkArgs<T> a) {
+__global__ void __launch_bounds__(kBlock) k_link_limdot(const __grid_constant__ LinkArgs<T> a) {
   const int i = link_part(a);
   const LinkPart<T> &q = a.part[i];
   const int tile = blockIdx.x - q.block0;
@@ -71,7 +73,7 @@ __global__ void __launch_bounds__(kBlock) k_link_limdot(const LinkArgs<T> a) {
 }
 
 template <typename T, int MASK>
-__global__ void __launch_bounds__(kBlock) k_link_lim(const LinkArgs<T> a) {
+__global__ void __launch_bounds__(kBlock) k_link_lim(const __grid_constant__ LinkArgs<T> a) {
   const int i = link_part(a);
   const LinkPart<T> &q = a.part[i];
   const int tile = blockIdx.x - q.block0;
@@ -179,9 +181,20 @@ static cudaError_t launch_linked_step(dgadv_handle **hs, int n, double /*t0: no 
   return cudaGetLastError();
 }
 
-template <typename T, int MASK>
+// The linked kernels carry the code of every degree they may meet, and their register count is
+// that of the largest: groups without p = 3 (the ensemble workload's degrees 1 and 2) use
+// kernels built for p <= 2 only.
+template <typename T>
+static cudaError_t launch_linked_step_any(dgadv_handle **hs, int n, double t0, double tau) {
+  int pmax = 0;
+  for (int i = 0; i < n; ++i) pmax = std::max(pmax, hs[i]->p);
+  if (pmax <= 2) return launch_linked_step<T, 0x6>(hs, n, t0, tau);
+  return launch_linked_step<T, 0xE>(hs, n, t0, tau);
+}
+
+template <typename T>
 static PrecOps with_linked(PrecOps o) {
-  o.step_linked = launch_linked_step<T, MASK>;
+  o.step_linked = launch_linked_step_any<T>;
   return o;
 }
 

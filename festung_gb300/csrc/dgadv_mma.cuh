@@ -130,7 +130,7 @@ __device__ __forceinline__ bool wait_bounded(uint64_t *bar, uint32_t parity, int
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity))
     if (clock64() - t0 > (1LL << 31)) {
-      atomicOr(flag, 2);
+      atomicOr(flag, 2 | 16);                    // bit 4: the tensor cores
       const long long t1 = clock64();
       while (!mbar_try_wait(bar, parity) && clock64() - t1 < (1LL << 31)) {
       }

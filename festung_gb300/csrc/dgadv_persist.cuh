@@ -53,7 +53,7 @@ __device__ __forceinline__ bool grid_sync(GridBar *b, int *flag) {
     while (*vgen == g0) {
       __nanosleep(32);
       if (clock64() - t0 > (1LL << 31)) {
-        atomicOr(flag, 2);
+        atomicOr(flag, 2 | 8);                   // bit 3: the grid barrier
         ok = 0;
         break;
       }
@@ -78,10 +78,22 @@ template <typename T> struct PersistArgs {
   GridBar *bar;
 };
 
+// After a tile (and the block barrier that follows it): thread 0 ends the life of the tile's
+// mbarrier, which the tile function placed after `nT` staged rows, before the next tile stages
+// rows of another layout over that location.  Tiles past the elements staged nothing.
+template <typename T, int P>
+__device__ __forceinline__ void end_tile_barrier(const Geo<T> &g, int tile, int nT) {
+  if (threadIdx.x == 0 && tile * kBlock < g.K) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    mbar_inval((uint64_t *)(smem + StageRows<T, P>::bar_offset(nT, 1, blockDim.x)));
+  }
+}
+
 // LIMMODE 0: no limiter; 1: linear limiter at p = 1; 2: linear limiter at p >= 2 (with the
 // time-derivative limiter).  Time-independent data without source terms.
 template <typename T, int P, int LIMMODE>
 __global__ void __launch_bounds__(kBlock) k_step_persistent(const PersistArgs<T> a) {
+  using SR = StageRows<T, P>;
 #pragma unroll
   for (int s = 0; s < 3; ++s) {
     if (s >= a.S) break;
@@ -91,6 +103,7 @@ __global__ void __launch_bounds__(kBlock) k_step_persistent(const PersistArgs<T>
       for (int tile = blockIdx.x; tile < a.nTilesK; tile += gridDim.x) {
         stage_op_tile<T, P, 0, false, false>(a.g, in, a.cn, out, a.lo1[s], a.sc[s], tile);
         __syncthreads();
+        end_tile_barrier<T, P>(a.g, tile, SR::op(0, false));
       }
       if (!grid_sync(a.bar, a.sc[s].flag)) return;
       continue;
@@ -99,6 +112,7 @@ __global__ void __launch_bounds__(kBlock) k_step_persistent(const PersistArgs<T>
     for (int tile = blockIdx.x; tile < a.nTiles; tile += gridDim.x) {
       stage_op_tile<T, P, (LIMMODE == 2 ? 2 : 1), false, true>(a.g, in, a.cn, a.tb, a.lo1[s], a.sc[s], tile);
       __syncthreads();
+      end_tile_barrier<T, P>(a.g, tile, SR::op(LIMMODE == 2 ? 2 : 1, true));
     }
     if (!grid_sync(a.bar, a.sc[s].flag)) return;
     if (LIMMODE == 2) {
@@ -106,6 +120,7 @@ __global__ void __launch_bounds__(kBlock) k_step_persistent(const PersistArgs<T>
       for (int tile = blockIdx.x; tile < a.nTiles; tile += gridDim.x) {
         limit_dot_lin_tile<T, P>(a.g, in, a.cn, a.tb, a.tb, a.li1[s], a.lo2[s], a.sc[s], tile);
         __syncthreads();
+        end_tile_barrier<T, P>(a.g, tile, SR::limdot_lin_rows(a.g.mtOnTheFly != 0));
       }
       if (!grid_sync(a.bar, a.sc[s].flag)) return;
     }

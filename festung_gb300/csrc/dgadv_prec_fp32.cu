@@ -14,7 +14,7 @@ DGADV_DEFINE_TABLES(float, cTf)
 namespace dgadv {
 const PrecOps &ops_fp32() {
   static const PrecOps ops =
-      with_linked<float, 0xE>(with_transport<float, 0xF>(with_persistent<float, 0xF>(with_adjoint<float, 0xF>(make_ops<float, 0xF, true>()))));
+      with_linked<float>(with_transport<float, 0xF>(with_persistent<float, 0xF>(with_adjoint<float, 0xF>(make_ops<float, 0xF, true>()))));
   return ops;
 }
 }  // namespace dgadv

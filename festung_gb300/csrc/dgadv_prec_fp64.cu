@@ -14,7 +14,7 @@ DGADV_DEFINE_TABLES(double, cTd)
 namespace dgadv {
 const PrecOps &ops_fp64() {
   static const PrecOps ops =
-      with_linked<double, 0xE>(with_transport<double, 0xF>(with_persistent<double, 0xF>(with_adjoint<double, 0xF>(make_ops<double, 0xF, true>()))));
+      with_linked<double>(with_transport<double, 0xF>(with_persistent<double, 0xF>(with_adjoint<double, 0xF>(make_ops<double, 0xF, true>()))));
   return ops;
 }
 }  // namespace dgadv

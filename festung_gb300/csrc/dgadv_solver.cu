@@ -476,9 +476,12 @@ extern "C" int dgadv_sync(dgadv_handle *h) {
     flag |= f;
   }
   if (flag & 2) {
-    // a block gave up at a barrier: the barrier state is reset for the next launch
+    // a block gave up at a barrier: the barrier state is reset for the next launch; a stage
+    // kernel that gave up may have left copies or MMAs behind, so the handle takes no more steps
     cudaMemset(h->gridBar, 0, kGridBarBytes);
-    h->err = "a bounded device wait timed out";
+    if (flag & (4 | 8 | 16)) h->poisoned = true;
+    h->err = std::string("a bounded device wait timed out:") + ((flag & 4) ? " staging copy" : "") +
+             ((flag & 8) ? " grid barrier" : "") + ((flag & 16) ? " tensor-core MMA" : "");
     return DGADV_ETIMEOUT;
   }
   if (flag & 1) { h->err = "non-finite value in the state"; return DGADV_ENONFINITE; }
@@ -617,6 +620,10 @@ extern "C" int dgadv_step(dgadv_handle *h, int32_t nSteps, int32_t nStep0, doubl
   }
   if (!h->hasVelocity) { if (h) h->err = "dgadv_set_velocity was not called"; return DGADV_EINVAL; }
   if (h->linkedTo) { h->err = "this handle is stepped by the handle it is linked to"; return DGADV_EUNSUPPORTED; }
+  if (h->poisoned) {
+    h->err = "a bounded wait of a stage kernel timed out earlier: the state is undefined, create a new handle";
+    return DGADV_ETIMEOUT;
+  }
   DG_CUDA(cudaSetDevice(h->device));
   if (nSteps == 0) return DGADV_OK;
   if (!h->linked.empty()) return linked_step(h, nSteps, nStep0, tau);

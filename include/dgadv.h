@@ -34,7 +34,10 @@ enum {
   DGADV_ENOMEM = 3,        /* host or device allocation failed                             */
   DGADV_EMESH = 4,         /* inconsistent mesh (non-manifold edge, bad vertex id, ...)     */
   DGADV_ENONFINITE = 5,    /* a kernel found NaN/Inf in the state                          */
-  DGADV_ETIMEOUT = 6,      /* a bounded device-side wait gave up                           */
+  DGADV_ETIMEOUT = 6,      /* a bounded device-side wait gave up; after a wait of the stage
+                              kernels (a staging copy, a grid barrier, a tensor-core MMA) the
+                              handle's state is undefined and every later step or sweep on it
+                              returns DGADV_ETIMEOUT: destroy it and create a new one       */
   DGADV_EUNSUPPORTED = 7,  /* option not supported by this build (e.g. p > 3 on the GPU)  */
   DGADV_EIO = 8,           /* an output file could not be written                          */
   DGADV_ENOCONV = 9        /* an iterative solve stopped before its tolerance               */

@@ -15,7 +15,8 @@ class FakeSolver:
 
     def __init__(self, cost):
         self.cost = cost
-        self.options = {L.OPT_FLAGS: 0, L.OPT_GRAPH_STEPS: 12, L.OPT_ADJ_WARPS: 2, L.OPT_OP_BLOCK: 128}
+        self.options = {L.OPT_FLAGS: 0, L.OPT_GRAPH_STEPS: 12, L.OPT_ADJ_WARPS: 2, L.OPT_OP_BLOCK: 128,
+                        L.OPT_TAYLOR_MASS: 1}
         self.state = np.arange(12.0).reshape(4, 3)
         self.calls = []
 
@@ -69,16 +70,18 @@ def test_tune_adjoint_times_every_width_and_applies_the_fastest(monkeypatch):
 def test_tune_picks_the_fastest_launch_configuration_and_caches_it(tmp_path):
     def cost(o):
         return (1.0 + (0.5 if o[L.OPT_FLAGS] & L.FLAG_NO_PDL else 0.0) + abs(o[L.OPT_GRAPH_STEPS] - 24) / 100
-                + (0.1 if o[L.OPT_OP_BLOCK] == 128 else 0.0))
+                + (0.1 if o[L.OPT_OP_BLOCK] == 128 else 0.0) + 0.05 * o[L.OPT_TAYLOR_MASS])
 
     s = FakeSolver(cost)
     before = s.get_state()
     cache = str(tmp_path / 'tune.json')
     best, table = AT.tune(s, 1e-3, nSteps=8, reps=2, fused_ok=True, cache=cache, key='k')
-    # separate passes: every operator block size; the fused pipeline: its one kernel shape
-    assert len(table) == 2 * len(AT.GRAPH_STEPS) * len(AT.OP_BLOCKS) + 2 * len(AT.GRAPH_STEPS)
+    # separate passes: every operator block size; the fused pipeline: its one kernel shape; then
+    # the other Taylor mass correction once on the best of those
+    assert len(table) == 2 * len(AT.GRAPH_STEPS) * len(AT.OP_BLOCKS) + 2 * len(AT.GRAPH_STEPS) + 1
     assert best['graphSteps'] == 24 and not best['flags'] & L.FLAG_NO_PDL and best['opBlock'] == 64
     assert s.get_option(L.OPT_GRAPH_STEPS) == 24 and s.get_option(L.OPT_OP_BLOCK) == 64
+    assert best['taylorMass'] == 0 and s.get_option(L.OPT_TAYLOR_MASS) == 0
     assert np.array_equal(s.get_state(), before)
     stored = json.load(open(cache))
     assert stored['k']['best']['graphSteps'] == 24
