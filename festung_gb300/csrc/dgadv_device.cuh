@@ -811,6 +811,22 @@ __device__ __forceinline__ void lin_u(const T *c, T *u) {
     u[i] = s.get();
   }
 }
+// The first three rows of u = DM c (mean and the linear part), all the linear limiter's
+// decision needs; the other rows only matter where the limiter acts (lin_alpha_lazy).
+template <typename T, int P>
+__device__ __forceinline__ void lin_u3(const T *c, T *u) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+#pragma unroll
+  for (int i = 0; i < (N < 3 ? N : 3); ++i) {
+    Acc<T> s(T(0));
+#pragma unroll
+    for (int j = 0; j < N; ++j) s.fma(tb.DM[i][j], c[j]);
+    u[i] = s.get();
+  }
+#pragma unroll
+  for (int i = 3; i < N; ++i) u[i] = T(0);
+}
 template <typename T, int P> __device__ __forceinline__ T lin_mean(const T *c) {
   constexpr int N = Dims<P>::N;
   const Tab<T, P> &tb = tab<T, P>();
@@ -843,6 +859,25 @@ __device__ __forceinline__ bool lin_alpha(const LimIn<T> &li, const VKeys<T, NQ>
   return true;
 }
 
+// lin_alpha with only u_0, u_1, u_2 given: the rows u_3.. of DM c are computed where the element
+// is limited (each row as lin_u computes it, so the results are the same).
+template <typename T, int P, int NQ>
+__device__ __forceinline__ bool lin_alpha_lazy(const LimIn<T> &li, const VKeys<T, NQ> &kv, const T *sh, T *u,
+                                               const T *c, int dmask, const T dataV0T[3], T *du) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  if (!lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, dataV0T, du)) return false;
+#pragma unroll
+  for (int i = 3; i < N; ++i) {
+    Acc<T> s(T(0));
+#pragma unroll
+    for (int j = 0; j < N; ++j) s.fma(tb.DM[i][j], c[j]);
+    u[i] = s.get();
+    du[i] = u[i];
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Stage operator.  MODE 0: write c^(s);  MODE 1: write Taylor(c^(s)) and scatter its centroid
 // quantities;  MODE 2: write Taylor(cDot) and scatter its quantities (time-derivative limiting
@@ -860,6 +895,9 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
   // OPF (double-float state only): the operator (volume, flux, hatM^-1 = I) in FP32 arithmetic;
   // the SSP update, the outputs and the limiter's quantities stay in the stored type
   using A = std::conditional_t<OPF, float, T>;
+  // with the mass solve (FP64, double-float) and no source terms, hatM^-1 is folded into the
+  // test-function tables of the volume and flux terms (Fg1, Fg2, Fphi)
+  constexpr bool kFold = sizeof(A) == 8 && !RHS;
   constexpr int NT = StageRows<T, P>::op(MODE, LIN);
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x));
@@ -930,8 +968,10 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
       const A cq = cqa.get();
       const A f1 = as_arith<A>(srow<T>(smem, rF + qq)[t]) * cq;
       const A f2 = as_arith<A>(srow<T>(smem, rF + Q + qq)[t]) * cq;
+      const T(&G1)[Q][N] = kFold ? tb.Fg1 : tb.g1;
+      const T(&G2)[Q][N] = kFold ? tb.Fg2 : tb.g2;
 #pragma unroll
-      for (int i = 0; i < N; ++i) { rhs[i].fma(as_arith<A>(tb.g1[qq][i]), f1); rhs[i].fma(as_arith<A>(tb.g2[qq][i]), f2); }
+      for (int i = 0; i < N; ++i) { rhs[i].fma(as_arith<A>(G1[qq][i]), f1); rhs[i].fma(as_arith<A>(G2[qq][i]), f2); }
     }
     // upwind edge term
     const int code = irow<T>(smem, NT, 0)[t];
@@ -951,13 +991,14 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
           for (int j = 0; j < N; ++j) tr.fma(as_arith<A>(tb.thetaPhi[n][np][r2][j]), cn[n][j]);
         }
         const A fl = v * tr.get();
+        const T(&PR)[3][R][N] = kFold ? tb.Fphi : tb.phi1D;
 #pragma unroll
-        for (int i = 0; i < N; ++i) rhs[i].fms(as_arith<A>(tb.phi1D[n][r2][i]), fl);
+        for (int i = 0; i < N; ++i) rhs[i].fms(as_arith<A>(PR[n][r2][i]), fl);
       }
     }
     // mass solve
     T cdot[N];
-    if constexpr (sizeof(A) == 8) {
+    if constexpr (sizeof(A) == 8 && !kFold) {
       A r[N];
 #pragma unroll
       for (int j = 0; j < N; ++j) r[j] = rhs[j].get();
@@ -1466,10 +1507,10 @@ __device__ __forceinline__ void limit_dot_lin_tile(const Geo<T> g, const T *cin,
     T cd[N], u[N], du[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) cd[i] = srow<T>(smem, rD + i)[t];
-    lin_u<T, P>(cd, u);
+    lin_u3<T, P>(cd, u);
     const int dmask = (irow<T>(smem, NT, 0)[t] >> 9) & 7;
     const T nan3[3] = {T(NAN), T(NAN), T(NAN)};
-    if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, nan3, du)) {
+    if (lin_alpha_lazy<T, P, NQ>(li, kv, sh, u, cd, dmask, nan3, du)) {
       if (fly) {
         const Affine<T> af = affine_from<T>(srow<T>(smem, rQ)[t], srow<T>(smem, rQ + 1)[t],
                                             srow<T>(smem, rQ + 2)[t], srow<T>(smem, rQ + 3)[t]);
@@ -1561,8 +1602,8 @@ __device__ __forceinline__ void limit_lin_tile(const Geo<T> g, const T *cbuf, T 
   __syncthreads();
   if (!active) return;
   T u[N], du[N];
-  lin_u<T, P>(c, u);
-  if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, data, du)) {
+  lin_u3<T, P>(c, u);
+  if (lin_alpha_lazy<T, P, NQ>(li, kv, sh, u, c, dmask, data, du)) {
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc<T> s(c[i]);

@@ -40,6 +40,12 @@ template <typename T, int P> struct Tab {
   T Hg1[Q][N];
   T Hg2[Q][N];
   T Hphi[3][R][N];
+  // forward: the mass solve folded into the volume and flux test functions,
+  // Fg1[q][i] = sum_j hatMinv[i][j] g1[q][j] (likewise Fg2, Fphi), or the tables themselves
+  // where the forward path uses hatM = I (FP32)
+  T Fg1[Q][N];
+  T Fg2[Q][N];
+  T Fphi[3][R][N];
 };
 
 // Static per-element data of one mesh (device pointers, SoA with stride Kp).

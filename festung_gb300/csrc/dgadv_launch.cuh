@@ -59,6 +59,21 @@ static cudaError_t upload_tables(const RefTables &rt) {
   for (int n = 0; n < 3; ++n)
     for (int r = 0; r < R; ++r)
       for (int j = 0; j < N; ++j) t.Hphi[n][r][j] = T(fold(&rt.phi1D[(n * R + r) * N], j));
+  // forward tables: hatM^-1 applied from the left, in FP64, then rounded
+  auto lfold = [&](const double *row, int i) {
+    if (!massSolve) return row[i];
+    double a = 0.0;
+    for (int j = 0; j < N; ++j) a += rt.hatMinv[i * N + j] * row[j];
+    return a;
+  };
+  for (int q = 0; q < Q; ++q)
+    for (int i = 0; i < N; ++i) {
+      t.Fg1[q][i] = T(lfold(&rt.gradQ[q * N], i));
+      t.Fg2[q][i] = T(lfold(&rt.gradQ[Q * N + q * N], i));
+    }
+  for (int n = 0; n < 3; ++n)
+    for (int r = 0; r < R; ++r)
+      for (int i = 0; i < N; ++i) t.Fphi[n][r][i] = T(lfold(&rt.phi1D[(n * R + r) * N], i));
   return cudaMemcpyToSymbol(tab_symbol<T, P>(), &t, sizeof(t));
 }
 

@@ -20,6 +20,7 @@ its own instances (weak scaling); results stay on their rank.
 """
 import numpy as np
 
+from . import _lib as L
 from . import advection_gpu as G
 from . import testcases as TC
 from .solver import DeviceSolver
@@ -76,7 +77,10 @@ class Ensemble:
             self.solvers[p] = s
         # link the groups: the largest group's handle steps all of them
         self.primary = None
-        if linked and len(self.solvers) > 1 and precision in ('fp32', 'fp64'):
+        # (the linked step runs the separate-pass pipeline: handles created for the fused or
+        # the persistent pipeline stay on their own streams)
+        if (linked and len(self.solvers) > 1 and precision in ('fp32', 'fp64')
+                and not flags & (L.FLAG_FUSE | L.FLAG_PERSIST)):
             order = sorted(self.solvers, key=lambda p: -sum(self.problems[i].K for i in self.groups[p]))
             self.primary = self.solvers[order[0]]
             for p in order[1:]:
