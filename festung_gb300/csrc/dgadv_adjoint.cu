@@ -290,7 +290,24 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
           if (h->limdot)
             Cd = h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
                                : (const char *)h->adjScrCdot + (size_t)s * bytes;
-          DG_CUDA(o.vjp_scatter(h, Y, h->adjPass));
+          if (h->limType == DGADV_LIM_HIERARCH_VERT) {
+            // hierarchical limiter (inputs recorded in Taylor form): per limiter its scatter,
+            // its pass and its gather
+            DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
+            v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
+            DG_CUDA(o.lim_vjp(h, v));
+            muY = h->tmpY;
+            if (h->limdot) {
+              DG_CUDA(o.vjp_scatter(h, Cd, h->adjPass, 1));
+              LimVjpArgs d;
+              std::memset(&d, 0, sizeof(d));
+              d.kind = 1; d.x = Cd; d.lamIn = h->tmpY; d.lamOut = h->tmpD; d.scale = (1.0 - omega[s]) * tau;
+              d.pass = h->adjPass++;
+              DG_CUDA(o.lim_vjp(h, d));
+              mp = h->tmpD;
+            }
+          } else {
+          DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
           v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
           v.nextX = Cd;
           v.gatherOut = Cd ? 0 : 1;
@@ -305,6 +322,7 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
             d.gatherOut = 1;
             DG_CUDA(o.lim_vjp(h, d));
             mp = h->tmpD;
+          }
           }
         }
         AdjStageArgs x;
@@ -390,8 +408,8 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
   const PrecOps &o = ops_of(h);
   if (!o.adj_stage) { h->err = "no adjoint kernels for this precision"; return DGADV_EUNSUPPORTED; }
   if (h->flags & DGADV_FLAG_IMPLICIT) { h->err = "the adjoint covers the explicit scheme"; return DGADV_EUNSUPPORTED; }
-  if (h->lim && h->limType != DGADV_LIM_LINEAR) {
-    h->err = "the adjoint covers the unlimited scheme and the linear limiter";
+  if (h->lim && h->limType == DGADV_LIM_STRICT) {
+    h->err = "the adjoint covers the unlimited scheme, the linear and the hierarchical vertex limiter";
     return DGADV_EUNSUPPORTED;
   }
   DG_CUDA(cudaSetDevice(h->device));
@@ -435,19 +453,22 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
     const size_t kb = o.keyBytes;
     const bool perStep = stageSteps > 0;
     if (!h->tmpY) {
+      // per pass nc quantities (1 linear, p(p+1)/2 hierarchical); records: per CSR position one
+      // (linear) or one per order (hierarchical)
+      const size_t nq = (size_t)h->nc, perPos = h->limType == DGADV_LIM_HIERARCH_VERT ? (size_t)h->p : 1;
       if ((st = dev_alloc(h, &h->tmpY, bytes))) return st;
       if ((st = dev_alloc(h, &h->tmpD, bytes))) return st;
       for (int r = 0; r < 2; ++r) {
-        if ((st = dev_alloc(h, (void **)&h->recSlotT[r], 3 * (size_t)h->K * 4))) return st;
-        if ((st = dev_alloc(h, &h->recSlotW[r], 3 * (size_t)h->K * o.realBytes))) return st;
+        if ((st = dev_alloc(h, (void **)&h->recSlotT[r], perPos * 3 * (size_t)h->K * 4))) return st;
+        if ((st = dev_alloc(h, &h->recSlotW[r], perPos * 3 * (size_t)h->K * o.realBytes))) return st;
       }
       if ((st = dev_alloc(h, (void **)&h->csrPos, 3 * (size_t)h->Kp * 4))) return st;
       k_csr_pos<<<(h->K + 127) / 128, 128, 0, h->stream>>>(h->K, h->Kp, h->V0T, h->vptr, h->vidx, h->csrPos);
       DG_CUDA(cudaGetLastError());
-      if ((st = dev_alloc(h, &h->adjMean, (size_t)h->Kp * o.realBytes))) return st;
-      if ((st = dev_alloc(h, &h->adjMeanB, (size_t)h->Kp * o.realBytes))) return st;
-      if ((st = dev_alloc(h, &h->vkeysA, 3 * 2 * (size_t)h->Vp * kb))) return st;
-      if ((st = dev_alloc(h, (void **)&h->gmmA, 3 * (size_t)h->nInst * kSlotCopies * 2 * 8))) return st;
+      if ((st = dev_alloc(h, &h->adjMean, nq * h->Kp * o.realBytes))) return st;
+      if ((st = dev_alloc(h, &h->adjMeanB, nq * h->Kp * o.realBytes))) return st;
+      if ((st = dev_alloc(h, &h->vkeysA, 3 * 2 * nq * h->Vp * kb))) return st;
+      if ((st = dev_alloc(h, (void **)&h->gmmA, 3 * (size_t)h->nInst * kSlotCopies * 2 * nq * 8))) return st;
       if ((st = dev_alloc(h, &h->adjScrY, (size_t)S * bytes))) return st;
       if ((st = dev_alloc(h, &h->adjScrCdot, (size_t)S * bytes))) return st;
     }
@@ -503,12 +524,14 @@ extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc
   DG_CUDA(cudaMemsetAsync(h->aV, 0, 3 * (size_t)h->R * h->Kp * 8, h->stream));
   if (h->lim) {
     // every sweep starts with the limiter adjoint's key sets reset and its pass count at 0
-    const size_t kb = o.keyBytes, vset = 2 * (size_t)h->Vp * kb;
-    for (int set = 0; set < 3; ++set) {
-      DG_CUDA(cudaMemsetAsync((char *)h->vkeysA + set * vset, 0xFF, (size_t)h->Vp * kb, h->stream));
-      DG_CUDA(cudaMemsetAsync((char *)h->vkeysA + set * vset + (size_t)h->Vp * kb, 0, (size_t)h->Vp * kb, h->stream));
-    }
-    std::vector<unsigned long long> init(3 * (size_t)h->nInst * kSlotCopies * 2);
+    const size_t kb = o.keyBytes, vq = (size_t)h->Vp * kb;   // one quantity's min (or max) keys
+    for (int set = 0; set < 3; ++set)
+      for (int q = 0; q < h->nc; ++q) {
+        char *base = (char *)h->vkeysA + ((size_t)set * h->nc + q) * 2 * vq;
+        DG_CUDA(cudaMemsetAsync(base, 0xFF, vq, h->stream));
+        DG_CUDA(cudaMemsetAsync(base + vq, 0, vq, h->stream));
+      }
+    std::vector<unsigned long long> init(3 * (size_t)h->nInst * kSlotCopies * 2 * h->nc);
     for (size_t i = 0; i < init.size(); ++i) init[i] = (i & 1) ? 0ULL : o.slotKeyMax;
     DG_CUDA(cudaMemcpyAsync(h->gmmA, init.data(), init.size() * 8, cudaMemcpyHostToDevice, h->stream));
     DG_CUDA(cudaStreamSynchronize(h->stream));

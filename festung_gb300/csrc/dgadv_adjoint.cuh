@@ -616,6 +616,460 @@ k_lim_vjp_gather(const Geo<T> g, T *lam, const int *slotT, const T *slotW) {
   for (int j = 0; j < N; ++j) lam[(size_t)j * Kp + k] = lam[(size_t)j * Kp + k] + acc * tb.DM[0][j];
 }
 
+// ---------------------------------------------------------------------------------------------
+// Adjoint of the hierarchical vertex-based limiter
+// (core/applySlopeLimiterTaylorHierarchicalVertex.m:124-168), on Taylor coefficients.  With its
+// discrete choices frozen the limiter scales each degree d >= 1 of the Taylor coefficients x by
+//   A_d = max(alpha_P, ..., alpha_d),   alpha_o = min over the sub-limiters i = 1..o of order o
+// and the element's three vertices of the factor of core/computeVertexBasedLimiter.m:78-106,
+// and a factor on an unsaturated branch is raw = dm / den with dm = ext - x[i0],
+// den = x[i1] pt1_n + x[i2] pt2_n -+ tol (i0, i1, i2 the sub-limiter's derivative and its two
+// neighbours, pt the Taylor basis at the vertex), ext the patch extreme of the sub-limiter's
+// quantity (another element's x[i0], the element's own vertex value at a Dirichlet vertex above
+// order 1, or boundary data).  For lambda = dJ/d(limited):
+//   dJ/dx_j   = A_d(j) lambda_j  (+ lambda_0 for the mean)
+//   dJ/dalpha_o = S_o = sum over the degrees d whose A_d is alpha_o of sum_j x_j lambda_j
+//   dJ/draw   = S_o, spread over x[i0], x[i1], x[i2] and ext as the derivatives of dm / den.
+// Terms of an extreme held by another element are recorded (element, its Taylor index, weight)
+// by CSR position and order, and gathered by k_lim_vjp_hier_gather.  The limiter's inputs are
+// recorded in Taylor form; the map from the modal coefficients is T = S DM (to_taylor), so the
+// solution limiter c = T^-1 L(x) gives dJ/dx = L'^T T^-T lambda, and the time-derivative limiter
+// T^-1 ((I - Mcorr) L(x) + Mcorr x) gives Mcorr^T mu + L'^T (I - Mcorr)^T mu with mu = T^-T lambda.
+// Outputs are modal: dJ/d(modal input) = T^T dJ/dx.
+template <typename T, int P> struct HierWin {
+  T raw, den, dm;
+  int act;       // the factor is raw, on a branch and strictly inside (0, 1)
+  int i0, i1, i2, n, s;
+  int src;       // extreme: 0 another element (recorded), 1 the element's own vertex value, 2 data
+  int tgt;       // element holding the extreme (src 0)
+};
+
+// S (modal-derivative u -> Taylor) blocks: S[d][m][j] = idX^d times deriv_block of A = B^-1.
+template <typename T, int P> struct SBlocks {
+  T b[P + 1][P + 1][P + 1];
+};
+template <typename T, int P>
+__device__ __forceinline__ void s_blocks(const Affine<T> &af, SBlocks<T, P> &sb) {
+  sb.b[0][0][0] = T(1);
+  T sc = T(1);
+#pragma unroll
+  for (int d = 1; d <= P; ++d) {
+    sc *= af.idX;
+    if (d == 1) {
+      T S[2][2]; deriv_block<T, 1>(af.A11, af.A21, af.A12, af.A22, S);
+#pragma unroll
+      for (int m = 0; m <= 1; ++m)
+#pragma unroll
+        for (int j = 0; j <= 1; ++j) sb.b[1][m][j] = S[m][j] * sc;
+    } else if (d == 2) {
+      T S[3][3]; deriv_block<T, 2>(af.A11, af.A21, af.A12, af.A22, S);
+#pragma unroll
+      for (int m = 0; m <= 2; ++m)
+#pragma unroll
+        for (int j = 0; j <= 2; ++j) sb.b[2][m][j] = S[m][j] * sc;
+    } else if (d == 3) {
+      T S[4][4]; deriv_block<T, 3>(af.A11, af.A21, af.A12, af.A22, S);
+#pragma unroll
+      for (int m = 0; m <= 3; ++m)
+#pragma unroll
+        for (int j = 0; j <= 3; ++j) sb.b[3][m][j] = S[m][j] * sc;
+    }
+  }
+}
+
+// y = T^T w = DM^T S^T w (Taylor -> modal adjoint).
+template <typename T, int P>
+__device__ __forceinline__ void taylor_T_transpose(const SBlocks<T, P> &sb, const T *w, T *y) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T z[N];
+  z[0] = w[0];
+#pragma unroll
+  for (int d = 1; d <= P; ++d) {
+    const int off = d * (d + 1) / 2;
+#pragma unroll
+    for (int j = 0; j <= d; ++j) {
+      Acc<T> a(T(0));
+#pragma unroll
+      for (int m = 0; m <= d; ++m) a.fma(sb.b[d][m][j], w[off + m]);
+      z[off + j] = a.get();
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    Acc<T> a(T(0));
+#pragma unroll
+    for (int i = 0; i < N; ++i) a.fma(tb.DM[i][c], z[i]);
+    y[c] = a.get();
+  }
+}
+
+// mu = T^-T lambda = S^-T DM^-T lambda (modal -> Taylor adjoint).
+template <typename T, int P>
+__device__ __forceinline__ void taylor_Tinv_transpose(const SinvBlocks<T, P> &si, const T *lam, T *mu) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  T z[N];
+#pragma unroll
+  for (int a = 0; a < N; ++a) {
+    Acc<T> s(T(0));
+#pragma unroll
+    for (int i = 0; i < N; ++i) s.fma(tb.DMinv[i][a], lam[i]);
+    z[a] = s.get();
+  }
+  mu[0] = z[0];
+#pragma unroll
+  for (int d = 1; d <= P; ++d) {
+    const int off = d * (d + 1) / 2;
+#pragma unroll
+    for (int j = 0; j <= d; ++j) {
+      Acc<T> s(T(0));
+#pragma unroll
+      for (int a = 0; a <= d; ++a) s.fma(si.b[d][a][j], z[off + a]);
+      mu[off + j] = s.get();
+    }
+  }
+}
+
+// out = Mcorr^T z with Mcorr = diag(1/diag(M_T)) M_T: the stored packed block, or with
+// M_T = 2|T| S^-T Gr S^-1 (taylor_mcorr) Mcorr^T z = S^-T Gr S^-1 (z ./ D).
+template <typename T, int P>
+__device__ __forceinline__ void mcorr_transpose(const Geo<T> &g, int k, const SinvBlocks<T, P> &si, const T *z,
+                                                T *out) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  if (g.mtOnTheFly) {
+    T w[N], y[N], gy[N];
+    w[0] = z[0] / tb.Gr[0][0];
+#pragma unroll
+    for (int d = 1; d <= P; ++d) {
+      const int off = d * (d + 1) / 2;
+#pragma unroll
+      for (int j = 0; j <= d; ++j) {
+        Acc<T> D(T(0));
+#pragma unroll
+        for (int a = 0; a <= d; ++a) {
+          Acc<T> r(T(0));
+#pragma unroll
+          for (int b = 0; b <= d; ++b) r.fma(tb.Gr[off + a][off + b], si.b[d][b][j]);
+          D.fma(si.b[d][a][j], r.get());
+        }
+        w[off + j] = z[off + j] / D.get();
+      }
+    }
+    y[0] = w[0];
+#pragma unroll
+    for (int d = 1; d <= P; ++d) {
+      const int off = d * (d + 1) / 2;
+#pragma unroll
+      for (int a = 0; a <= d; ++a) {
+        Acc<T> s(T(0));
+#pragma unroll
+        for (int j = 0; j <= d; ++j) s.fma(si.b[d][a][j], w[off + j]);
+        y[off + a] = s.get();
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc<T> s(T(0));
+#pragma unroll
+      for (int j = 0; j < N; ++j) s.fma(tb.Gr[i][j], y[j]);
+      gy[i] = s.get();
+    }
+    out[0] = gy[0];
+#pragma unroll
+    for (int d = 1; d <= P; ++d) {
+      const int off = d * (d + 1) / 2;
+#pragma unroll
+      for (int j = 0; j <= d; ++j) {
+        Acc<T> s(T(0));
+#pragma unroll
+        for (int a = 0; a <= d; ++a) s.fma(si.b[d][a][j], gy[off + a]);
+        out[off + j] = s.get();
+      }
+    }
+  } else {
+    const int Kp = g.Kp;
+    T m[N][N];
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+      for (int b = a; b < N; ++b) {
+        const T v = g.MT[(size_t)(a * N - a * (a - 1) / 2 + (b - a)) * Kp + k];
+        m[a][b] = v;
+        m[b][a] = v;
+      }
+    T w[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) w[i] = z[i] / m[i][i];
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      Acc<T> s(T(0));
+#pragma unroll
+      for (int i = 0; i < N; ++i) s.fma(m[i][j], w[i]);
+      out[j] = s.get();
+    }
+  }
+}
+
+// Taylor coefficients of the limiter input scattered to the adjoint's vertex keys (one quantity
+// per sub-limiter, as the forward's passes), and the quantities stored per element.
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_vjp_scatter_hier(const Geo<T> g, const T *x, const LimOut<T> lo, T *__restrict__ qOut) {
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
+  const int k = blockIdx.x * kBlock + threadIdx.x;
+  pdl_trigger();
+  const bool active = k < g.K;
+  const int Kp = g.Kp;
+  int vid[3] = {0, 0, 0};
+  if (active) { vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k]; }
+  pdl_wait();
+  reset_next<T>(g, lo, k);
+  T qv[NQ];
+#pragma unroll
+  for (int s = 0; s < NQ; ++s) qv[s] = T(0);
+  if (active) {
+    T cT[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cT[i] = x[(size_t)i * Kp + k];
+    centroid_quantities<T, P>(cT, 1, qv);
+#pragma unroll
+    for (int s = 0; s < NQ; ++s) qOut[(size_t)s * Kp + k] = qv[s];
+  }
+  scatter_quantities<T, NQ>(g, lo, qv, vid, active);
+}
+
+// The limiter adjoint of one pass (KIND 0 solution limiter, 1 time-derivative limiter).
+// slotT / slotW: P records per CSR position (order o at o * nnz + position), element * 16 +
+// Taylor index or -1, and the weight.
+template <typename T, int P, int KIND>
+__global__ void __launch_bounds__(kBlock)
+k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, const LimIn<T> li,
+               const StageScalars sc, double scale, const T *__restrict__ qStore, const int *__restrict__ csrPos,
+               int nnz, int *__restrict__ slotT, T *__restrict__ slotW) {
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
+  __shared__ T sh[2 * NQ];
+  const int k = blockIdx.x * kBlock + threadIdx.x;
+  pdl_trigger();
+  const bool active = k < g.K;
+  const int Kp = g.Kp;
+  int vid[3] = {0, 0, 0}, pos[3] = {-1, -1, -1}, dmask = 0;
+  T B[4] = {T(1), T(0), T(0), T(1)};
+  if (active) {
+    vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
+    pos[0] = csrPos[k]; pos[1] = csrPos[Kp + k]; pos[2] = csrPos[2 * Kp + k];
+    dmask = (g.code[k] >> 9) & 7;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) B[r] = g.Bm[(size_t)r * Kp + k];
+  }
+  T data[3] = {T(0), T(0), T(0)};
+  if (KIND == 0 && g.cDV0T && active)
+    for (int m = 0; m < g.nTerms; ++m) {
+      const T gm = T(sc.gco[m]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
+    }
+  pdl_wait();
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
+  T xv[N], lam[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    xv[i] = active ? x[(size_t)i * Kp + k] : T(0);
+    lam[i] = active ? T(scale) * lamIn[(size_t)i * Kp + k] : T(0);
+  }
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
+  if (!active) return;
+  const Affine<T> af = affine_from<T>(B[0], B[1], B[2], B[3]);
+  SinvBlocks<T, P> si;
+  sinv_blocks<T, P>(af, si);
+  T mu[N], lamL[N], mc[N];
+  taylor_Tinv_transpose<T, P>(si, lam, mu);
+  if (KIND == 1) {
+    mcorr_transpose<T, P>(g, k, si, mu, mc);
+#pragma unroll
+    for (int i = 0; i < N; ++i) lamL[i] = mu[i] - mc[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) lamL[i] = mu[i];
+  }
+  // the forward's choices (limit_taylor, LT = 1), with the winners recorded
+  const T tol = T(1.e-8), nan_ = T(NAN);
+  T pt1[3], pt2[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) { pt1[n] = af.ox[n] * af.dX; pt2[n] = af.oy[n] * af.dX; }
+  HierWin<T, P> win[P + 1];
+  T A[P + 1];
+  int winOrd[P + 1];
+  T alphaRun = T(0);
+  int runOrd = P;
+  int s = 0;
+#pragma unroll
+  for (int ord = P; ord >= 1; --ord) {
+    T aOrd = T(1);
+    win[ord].act = 0; win[ord].src = 2; win[ord].tgt = -1; win[ord].n = 0; win[ord].s = 0;
+    win[ord].i0 = win[ord].i1 = win[ord].i2 = 0;
+    win[ord].raw = win[ord].den = win[ord].dm = T(0);
+#pragma unroll
+    for (int i = 1; i <= ord; ++i) {
+      const int i0 = mind(ord - i, i - 1), i1 = mind(ord - i + 1, i - 1), i2 = mind(ord - i, i);
+      T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        v[n] = (xv[i0] * T(1) + xv[i1] * pt1[n]) + xv[i2] * pt2[n];
+        valD[n] = ((dmask >> n) & 1) ? (ord > 1 ? v[n] : (KIND == 0 ? data[n] : nan_)) : nan_;
+      }
+      patch_minmax<T, NQ>(li, kv, sh, s, valD, mn, mx);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        const T cbar = xv[i0];
+        const T dV = v[n] - cbar, dMin = mn[n] - cbar, dMax = mx[n] - cbar;
+        T a = T(1), den = T(0), dm = T(0);
+        int br = 0;
+        if (dV < dMin + tol) { den = dV - tol; dm = dMin; a = fmax(T(0), fmin(T(1), dm / den)); br = 1; }
+        if (dV > dMax - tol) { den = dV + tol; dm = dMax; a = fmax(T(0), fmin(T(1), dm / den)); br = 2; }
+        if (a < aOrd) {   // the first (sub-limiter, vertex) reaching the order's minimum
+          aOrd = a;
+          HierWin<T, P> &w = win[ord];
+          const T raw = dm / den;
+          w.raw = raw; w.den = den; w.dm = dm;
+          w.act = br != 0 && raw > T(0) && raw < T(1);
+          w.i0 = i0; w.i1 = i1; w.i2 = i2; w.n = n; w.s = s;
+          // the extreme's source: the Dirichlet value (which wins a tie) or the patch element
+          const bool isPos = br == 2;
+          const T rawExt = vkey_inv<T>(kv.v[s][isPos ? 1 : 0][n]);
+          const bool hasD = ((dmask >> n) & 1) && !(valD[n] != valD[n]);
+          const bool fromD = hasD && (isPos ? !(valD[n] < rawExt) : !(valD[n] > rawExt));
+          w.src = fromD ? (ord > 1 ? 1 : 2) : 0;
+          w.tgt = -1;
+          if (!fromD && w.act) {
+            const auto key = kv.v[s][isPos ? 1 : 0][n];
+            int best = -1, bestId = 0x7fffffff;
+            const int v0 = vid[n];
+            const int e0 = g.vptr[v0], e1 = g.vptr[v0 + 1];
+            for (int e = e0; e < e1; ++e) {
+              const int k2 = g.vidx[e];
+              if (vkey(qStore[(size_t)s * Kp + k2]) == key && g.permv[k2] < bestId) { best = k2; bestId = g.permv[k2]; }
+            }
+            w.tgt = best;
+          }
+        }
+      }
+      ++s;
+    }
+    if (ord == P || aOrd > alphaRun) runOrd = ord;   // the order whose alpha is the running max
+    alphaRun = fmax(alphaRun, aOrd);
+    A[ord] = alphaRun;
+    winOrd[ord] = runOrd;
+  }
+  // dJ/dx: A_d lambda_j, the mean passed on, then each winning order's factor
+  T gx[N];
+  gx[0] = lamL[0];
+#pragma unroll
+  for (int d = 1; d <= P; ++d)
+#pragma unroll
+    for (int j = d * (d + 1) / 2; j < (d + 1) * (d + 2) / 2; ++j) gx[j] = A[d] * lamL[j];
+  if (KIND == 1) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) gx[i] = gx[i] + mc[i];
+  }
+  int recT[P + 1];
+  T recW[P + 1];
+#pragma unroll
+  for (int o = 1; o <= P; ++o) { recT[o] = -1; recW[o] = T(0); }
+#pragma unroll
+  for (int o = 1; o <= P; ++o) {
+    Acc<T> so(T(0));
+    bool used = false;
+#pragma unroll
+    for (int d = 1; d <= P; ++d)
+      if (winOrd[d] == o) {
+        used = true;
+#pragma unroll
+        for (int j = d * (d + 1) / 2; j < (d + 1) * (d + 2) / 2; ++j) so.fma(xv[j], lamL[j]);
+      }
+    const HierWin<T, P> &w = win[o];
+    if (!used || !w.act) continue;
+    const T So = so.get();
+    const T q = So / w.den, r = So * w.dm / (w.den * w.den);
+    const T p1 = pt1[w.n], p2 = pt2[w.n];
+    gx[w.i0] = gx[w.i0] - q;
+    gx[w.i1] = gx[w.i1] - r * p1;
+    gx[w.i2] = gx[w.i2] - r * p2;
+    if (w.src == 1) {                          // ext = the element's own vertex value
+      gx[w.i0] = gx[w.i0] + q;
+      gx[w.i1] = gx[w.i1] + q * p1;
+      gx[w.i2] = gx[w.i2] + q * p2;
+    } else if (w.src == 0 && w.tgt >= 0) {     // ext = x[i0] of another element (or this one)
+      recT[o] = w.tgt * 16 + w.i0;
+      recW[o] = q;
+    }
+  }
+  T out[N];
+  SBlocks<T, P> sb;
+  s_blocks<T, P>(af, sb);
+  taylor_T_transpose<T, P>(sb, gx, out);
+#pragma unroll
+  for (int i = 0; i < N; ++i) lamOut[(size_t)i * Kp + k] = out[i];
+#pragma unroll
+  for (int o = 1; o <= P; ++o)
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      if (pos[n] >= 0) {
+        const bool mine = win[o].n == n && recT[o] >= 0;
+        slotT[(size_t)(o - 1) * nnz + pos[n]] = mine ? recT[o] : -1;
+        if (mine) slotW[(size_t)(o - 1) * nnz + pos[n]] = recW[o];
+      }
+}
+
+// Gathers the recorded extreme terms: element e adds w T^T e_i for every record (e, i, w) in the
+// slots of its vertex patches (CSR order: deterministic).
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock)
+k_lim_vjp_hier_gather(const Geo<T> g, T *lam, int nnz, const int *slotT, const T *slotW) {
+  constexpr int N = Dims<P>::N;
+  const int k = blockIdx.x * kBlock + threadIdx.x;
+  pdl_trigger();
+  if (k >= g.K) return;
+  const int Kp = g.Kp;
+  const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
+  int i0[3], i1[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) { i0[n] = g.vptr[vid[n]]; i1[n] = g.vptr[vid[n] + 1]; }
+  T B[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) B[r] = g.Bm[(size_t)r * Kp + k];
+  pdl_wait();
+  T acc[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) acc[j] = T(0);
+  bool any = false;
+#pragma unroll
+  for (int n = 0; n < 3; ++n)
+    for (int i = i0[n]; i < i1[n]; ++i)
+#pragma unroll
+      for (int o = 0; o < P; ++o) {
+        const int t = slotT[(size_t)o * nnz + i];
+        if (t >= 0 && (t >> 4) == k) {
+          const int ti = t & 15;
+#pragma unroll
+          for (int j = 0; j < N; ++j)
+            if (j == ti) acc[j] = acc[j] + slotW[(size_t)o * nnz + i];
+          any = true;
+        }
+      }
+  if (!any) return;
+  const Affine<T> af = affine_from<T>(B[0], B[1], B[2], B[3]);
+  SBlocks<T, P> sb;
+  s_blocks<T, P>(af, sb);
+  T add[N];
+  taylor_T_transpose<T, P>(sb, acc, add);
+#pragma unroll
+  for (int j = 0; j < N; ++j) lam[(size_t)j * Kp + k] = lam[(size_t)j * Kp + k] + add[j];
+}
+
 // The solution limiter's pass uses the first record set and the means of vjp_scatter; the
 // time-derivative limiter's pass the second record set and the means its predecessor scattered.
 template <typename T, int P>
@@ -625,6 +1079,21 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   StageScalars sc{};
   sc.flag = h->flag;
   for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = v.gco[m];
+  if (h->limType == DGADV_LIM_HIERARCH_VERT) {   // one pass and its gather, P records per position
+    int *rT = h->recSlotT[v.kind];
+    T *rW = (T *)h->recSlotW[v.kind];
+    const T *q = (const T *)(v.kind == 0 ? h->adjMean : h->adjMeanB);
+    const int nnz = 3 * h->K;
+    if (v.kind == 0)
+      launch_k(h, k_lim_vjp_hier<T, P, 0>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn,
+               (T *)v.lamOut, lim_in_adj<T>(h, v.pass), sc, v.scale, q, (const int *)h->csrPos, nnz, rT, rW);
+    else
+      launch_k(h, k_lim_vjp_hier<T, P, 1>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn,
+               (T *)v.lamOut, lim_in_adj<T>(h, v.pass), sc, v.scale, q, (const int *)h->csrPos, nnz, rT, rW);
+    launch_k(h, k_lim_vjp_hier_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, nnz, (const int *)rT,
+             (const T *)rW);
+    return cudaGetLastError();
+  }
   int *rT = h->recSlotT[v.kind];
   T *rW = (T *)h->recSlotW[v.kind];
   const int *cp = h->csrPos;
@@ -655,10 +1124,14 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
 
 // Means of x scattered to the adjoint's own vertex keys (the limiter's patch extremes).
 template <typename T, int P>
-static cudaError_t launch_vjp_scatter(dgadv_handle *h, const void *x, long long pass) {
+static cudaError_t launch_vjp_scatter(dgadv_handle *h, const void *x, long long pass, int kind) {
   const Geo<T> g = make_geo<T>(h);
   const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
-  launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)x, lim_out_adj<T>(h, pass), (T *)h->adjMean);
+  T *q = (T *)(kind == 0 ? h->adjMean : h->adjMeanB);
+  if (h->limType == DGADV_LIM_HIERARCH_VERT)
+    launch_k(h, k_vjp_scatter_hier<T, P>, grid, (size_t)0, g, (const T *)x, lim_out_adj<T>(h, pass), q);
+  else
+    launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)x, lim_out_adj<T>(h, pass), q);
   return cudaGetLastError();
 }
 
@@ -703,11 +1176,11 @@ static cudaError_t dispatch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   return cudaErrorNotSupported;
 }
 template <typename T, int MASK>
-static cudaError_t dispatch_vjp_scatter(dgadv_handle *h, const void *x, long long pass) {
+static cudaError_t dispatch_vjp_scatter(dgadv_handle *h, const void *x, long long pass, int kind) {
   switch (h->p) {
-    case 1: if constexpr ((MASK & 2) != 0) return launch_vjp_scatter<T, 1>(h, x, pass); break;
-    case 2: if constexpr ((MASK & 4) != 0) return launch_vjp_scatter<T, 2>(h, x, pass); break;
-    case 3: if constexpr ((MASK & 8) != 0) return launch_vjp_scatter<T, 3>(h, x, pass); break;
+    case 1: if constexpr ((MASK & 2) != 0) return launch_vjp_scatter<T, 1>(h, x, pass, kind); break;
+    case 2: if constexpr ((MASK & 4) != 0) return launch_vjp_scatter<T, 2>(h, x, pass, kind); break;
+    case 3: if constexpr ((MASK & 8) != 0) return launch_vjp_scatter<T, 3>(h, x, pass, kind); break;
   }
   return cudaErrorNotSupported;
 }

@@ -1244,8 +1244,10 @@ template <> struct LimBlocks<float> { static constexpr int value = 5; };
 
 template <typename T, int P, int LT>
 __global__ void __launch_bounds__(kBlock, LimDotBlocks<T, LT>::value)
-k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
+k_limit_dot(const Geo<T> g, const T *cin, const T *c0, const T *tbuf, T *tout,
             const LimIn<T> li, const LimOut<T> lo, const StageScalars sc) {
+  // tbuf: Taylor coefficients of cDot (in); tout: those of the new stage value (out; the same
+  // buffer in a plain run, the record slot of the stage in a recorded one)
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   constexpr int NT = StageRows<T, P>::limdot();
   extern __shared__ __align__(128) unsigned char smem[];
@@ -1272,7 +1274,7 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
   reset_next<T>(g, lo, k);
   if (!staged) return;
   if (t == 0) {
-    stage_T(smem, rT, (const T *)tbuf, N, Kp, k0, bar);
+    stage_T(smem, rT, tbuf, N, Kp, k0, bar);
     stage_T(smem, rC0, c0, N, Kp, k0, bar);
     stage_T(smem, rC, cin, N, Kp, k0, bar);
   }
@@ -1350,7 +1352,7 @@ k_limit_dot(const Geo<T> g, const T *cin, const T *c0, T *__restrict__ tbuf,
     T cT2[N];
     to_taylor<T, P>(cnew, af, cT2);
 #pragma unroll
-    for (int i = 0; i < N; ++i) { tbuf[(size_t)i * Kp + k] = cT2[i]; bad |= !finite_(cT2[i]); }
+    for (int i = 0; i < N; ++i) { tout[(size_t)i * Kp + k] = cT2[i]; bad |= !finite_(cT2[i]); }
     centroid_quantities<T, P>(cT2, lo.type, qv);
   }
   scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok);

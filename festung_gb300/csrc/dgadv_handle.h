@@ -194,7 +194,9 @@ struct PrecOps {
   cudaError_t (*step_linked)(dgadv_handle **hs, int n, double t0, double tau);
   cudaError_t (*persist_attributes)(int p);
   cudaError_t (*lim_vjp)(dgadv_handle *h, const LimVjpArgs &a);
-  cudaError_t (*vjp_scatter)(dgadv_handle *h, const void *x, long long pass);
+  // the limiter input's quantities to the adjoint's key set of `pass` and stored per element
+  // (kind 0: solution limiter, 1: time-derivative limiter)
+  cudaError_t (*vjp_scatter)(dgadv_handle *h, const void *x, long long pass, int kind);
   // device copy of a state-sized buffer (bytes a multiple of 16) ordered with dependent launches
   cudaError_t (*copy)(dgadv_handle *h, void *dst, const void *src, size_t bytes);
   // n FP64 values on the device -> stored reals

@@ -128,18 +128,19 @@ static LimIn<T> lim_in_pass(const dgadv_handle *h, long long pass) {
   return i;
 }
 
-// The adjoint's own key sets (the limiter adjoint recomputes the forward's patch extremes).
+// The adjoint's own key sets (the limiter adjoint recomputes the forward's patch extremes), with
+// the forward's quantities per pass (one for the linear limiter, p(p+1)/2 for the hierarchical).
 template <typename T>
 static LimOut<T> lim_out_adj(dgadv_handle *h, long long pass) {
   using K_ = typename KeyOf<T>::type;
   const int set = (int)(pass % 3), next = (set + 1) % 3;
-  const size_t vset = (size_t)2 * h->Vp;
+  const size_t vset = (size_t)2 * h->nc * h->Vp;
   LimOut<T> o;
   o.vkeys = (K_ *)h->vkeysA + set * vset;
   o.vreset = (K_ *)h->vkeysA + next * vset;
-  o.slots = h->gmmA + (size_t)set * h->nInst * kSlotCopies * 2;
-  o.reset = h->gmmA + (size_t)next * h->nInst * kSlotCopies * 2;
-  o.nc = 1; o.type = 0;
+  o.slots = h->gmmA + (size_t)set * h->nInst * kSlotCopies * 2 * h->nc;
+  o.reset = h->gmmA + (size_t)next * h->nInst * kSlotCopies * 2 * h->nc;
+  o.nc = h->nc; o.type = h->limType;
   return o;
 }
 template <typename T>
@@ -147,9 +148,9 @@ static LimIn<T> lim_in_adj(const dgadv_handle *h, long long pass) {
   using K_ = typename KeyOf<T>::type;
   const int set = (int)(pass % 3);
   LimIn<T> i;
-  i.vkeys = (const K_ *)h->vkeysA + (size_t)set * 2 * h->Vp;
-  i.slots = h->gmmA + (size_t)set * h->nInst * kSlotCopies * 2;
-  i.nc = 1; i.type = 0;
+  i.vkeys = (const K_ *)h->vkeysA + (size_t)set * 2 * h->nc * h->Vp;
+  i.slots = h->gmmA + (size_t)set * h->nInst * kSlotCopies * 2 * h->nc;
+  i.nc = h->nc; i.type = h->limType;
   i.shift = (h->flags & DGADV_FLAG_NO_SHIFT) ? 0 : 1;
   return i;
 }
@@ -302,14 +303,14 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     const int mode = h->limdot ? 2 : 1;
     // buffers of the limiter inputs: tb, or in a recorded run of the adjoint this stage's record
     // slots, written directly (cDot before time-derivative limiting; the unlimited stage value)
-    T *cdB = (lin && mode == 2 && h->recCdot[s]) ? (T *)h->recCdot[s] : tb;
-    T *yB = (lin && h->recY[s]) ? (T *)h->recY[s] : tb;
+    T *cdB = (mode == 2 && h->recCdot[s]) ? (T *)h->recCdot[s] : tb;
+    T *yB = h->recY[s] ? (T *)h->recY[s] : tb;
     prof_mark(h, 0);
     bool viaMma = false;
     if constexpr (std::is_same_v<T, float> && P >= 2) {
       if (mode == 2 && h->volumeMma && !rhs) {   // the volume term on the tensor cores
         if (lin) launch_k(h, k_stage_op_mma<P, true>, grid, MmaSmem<P>::bytes(true), g, (const T *)in, cdB, lo1, sc);
-        else launch_k(h, k_stage_op_mma<P, false>, grid, MmaSmem<P>::bytes(false), g, (const T *)in, tb, lo1, sc);
+        else launch_k(h, k_stage_op_mma<P, false>, grid, MmaSmem<P>::bytes(false), g, (const T *)in, cdB, lo1, sc);
         viaMma = true;
       }
     }
@@ -319,16 +320,16 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
         if (rhs) launch_kb(h, stage_kernel<T, P, 2, true, true>(h), gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
         else launch_kb(h, stage_kernel<T, P, 2, false, true>(h), gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
       } else {
-        if (rhs) launch_kb(h, stage_kernel<T, P, 2, true, false>(h), gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, tb, lo1, sc);
-        else launch_kb(h, stage_kernel<T, P, 2, false, false>(h), gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, tb, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 2, true, false>(h), gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, cdB, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 2, false, false>(h), gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, cdB, lo1, sc);
       }
     } else {
       if (lin) {
         if (rhs) launch_kb(h, stage_kernel<T, P, 1, true, true>(h), gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
         else launch_kb(h, stage_kernel<T, P, 1, false, true>(h), gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
       } else {
-        if (rhs) launch_kb(h, stage_kernel<T, P, 1, true, false>(h), gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, tb, lo1, sc);
-        else launch_kb(h, stage_kernel<T, P, 1, false, false>(h), gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, tb, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 1, true, false>(h), gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, yB, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 1, false, false>(h), gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, yB, lo1, sc);
       }
     }
     prof_mark(h, -1);
@@ -339,18 +340,18 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
       prof_mark(h, 1);
       if (lin) launch_k(h, k_limit_dot_lin<T, P>, grid, SR::bytes(SR::limdot_lin_rows(h->mtOnTheFly), 1), g, (const T *)in, (const T *)cn, (const T *)cdB, yB, lim_in<T>(lo1, h), lo2, sc);
       else if (h->limType == DGADV_LIM_STRICT)
-        launch_k(h, k_limit_dot<T, P, 2>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
+        launch_k(h, k_limit_dot<T, P, 2>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, (const T *)cdB, yB, lim_in<T>(lo1, h), lo2, sc);
       else
-        launch_k(h, k_limit_dot<T, P, 1>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, tb, lim_in<T>(lo1, h), lo2, sc);
+        launch_k(h, k_limit_dot<T, P, 1>, grid, SR::bytes(SR::limdot(), 1), g, in, cn, (const T *)cdB, yB, lim_in<T>(lo1, h), lo2, sc);
       prof_mark(h, -1);
       loS = lo2;
     }
     prof_mark(h, 2);
     if (lin) launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)yB, out, lim_in<T>(loS, h), scBC);
     else if (h->limType == DGADV_LIM_STRICT)
-      launch_k(h, k_limit<T, P, 2>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
+      launch_k(h, k_limit<T, P, 2>, grid, SR::bytes(SR::lim(), 1), g, (const T *)yB, out, lim_in<T>(loS, h), scBC);
     else
-      launch_k(h, k_limit<T, P, 1>, grid, SR::bytes(SR::lim(), 1), g, (const T *)tb, out, lim_in<T>(loS, h), scBC);
+      launch_k(h, k_limit<T, P, 1>, grid, SR::bytes(SR::lim(), 1), g, (const T *)yB, out, lim_in<T>(loS, h), scBC);
     prof_mark(h, -1);
   }
   if (S == 1 && nRun == 1 && (const T *)dst == cn) return copy_state(h, dst, cA, (size_t)h->N * h->Kp * sizeof(T));

@@ -219,11 +219,78 @@ def test_limited_theta_gradient_matches_finite_differences(lib):
         pd.solver.close()
 
 
-def test_hierarchical_limiter_has_no_adjoint(lib):
+HIER = [dict(hmax=2 ** -5, p=2, numSteps=20, tEnd=20 * 2e-4),
+        dict(hmax=2 ** -5, p=3, numSteps=10, tEnd=10 * 1e-4, jitter=0.1, meshSeed=5),
+        dict(hmax=2 ** -5, p=1, numSteps=20, tEnd=20 * 2e-4)]
+
+
+def _hier_case(kw, precision='fp64'):
+    from festung_gb300 import adjoint as AD
+    args = dict(kw, isSlopeLim=True, typeSlopeLim='hierarch_vert')
+    tg = AD.setup(precision='fp64', adjointTarget=True, **args)
+    tg.solver.step(kw['numSteps'], 0, tg.tau)
+    cstar = tg.solver.get_state()
+    tg.solver.close()
+    return AD.setup(precision=precision, **args), cstar
+
+
+@pytest.mark.parametrize('kw', HIER, ids=['p2', 'p3-jitter', 'p1'])
+def test_hierarchical_gradient_matches_finite_differences(lib, kw):
+    """The hierarchical vertex limiter's adjoint (core/applySlopeLimiterTaylorHierarchicalVertex.m,
+    choices recomputed from the recorded Taylor inputs) against central differences (h = 1e-6)
+    of the GPU forward run: along velocity directions scaled by |theta|, and along c0 itself
+    (a direction that moves every element together and stays on one side of the switches)."""
+    from festung_gb300 import adjoint as AD
+    pd, cstar = _hier_case(kw)
+    try:
+        c0 = np.asfortranarray(pd._cDisc)
+        J, g0, gth = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
+        h = 1e-6
+        rng = np.random.default_rng(5)
+        for _ in range(2):
+            dt = rng.standard_normal(gth.size) * np.abs(pd.theta)
+            fd = (AD.misfit(pd, c0, pd.theta + h * dt, cstar) - AD.misfit(pd, c0, pd.theta - h * dt, cstar)) / (2 * h)
+            assert abs(fd - gth @ dt) <= 1e-6 * abs(fd), (fd, gth @ dt)
+        fd = (AD.misfit(pd, c0 * (1 + h), pd.theta, cstar) - AD.misfit(pd, c0 * (1 - h), pd.theta, cstar)) / (2 * h)
+        assert abs(fd - float(np.sum(g0 * c0))) <= 1e-6 * abs(fd), (fd, float(np.sum(g0 * c0)))
+    finally:
+        pd.solver.close()
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32'])
+def test_hierarchical_checkpointed_sweep_equals_stored_sweep(lib, precision):
+    from festung_gb300 import adjoint as AD
+    pd, cstar = _hier_case(HIER[0], precision)
+    try:
+        c0 = np.asfortranarray(pd._cDisc)
+        ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
+        for snaps in (3, HIER[0]['numSteps']):
+            got = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=snaps)
+            assert got[0] == ref[0]
+            assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
+    finally:
+        pd.solver.close()
+
+
+def test_hierarchical_fp32_gradient_close_to_fp64(lib):
+    from festung_gb300 import adjoint as AD
+    out = {}
+    for prec in ('fp64', 'fp32'):
+        pd, cstar = _hier_case(HIER[0], prec)
+        try:
+            c0 = np.asfortranarray(pd._cDisc)
+            out[prec] = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
+        finally:
+            pd.solver.close()
+    assert rel(out['fp32'][1], out['fp64'][1]) <= 1e-2
+    assert rel(out['fp32'][2], out['fp64'][2]) <= 1e-2
+
+
+def test_strict_limiter_has_no_adjoint(lib):
     from festung_gb300 import _lib as L
     from festung_gb300 import adjoint as AD
     pd = AD.setup(precision='fp64', hmax=2 ** -3, p=2, numSteps=2, tEnd=4e-4, isSlopeLim=True,
-                  typeSlopeLim='hierarch_vert')
+                  typeSlopeLim='strict')
     try:
         with pytest.raises(L.DgadvError) as e:
             pd.solver.forward_record(2, pd.tau, 0)
