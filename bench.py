@@ -384,14 +384,24 @@ def adjoint_block(reps=3, fd_dirs=16):
     rel = lambda a, b: float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
     out['fp32_vs_fp64_grad_rel_l2'] = {'dJdc0': rel(grads['fp32'][0], grads['fp64'][0]),
                                        'dJdtheta': rel(grads['fp32'][1], grads['fp64'][1])}
-    # the same workload with the linear limiter on (its adjoint through the limiter's choices)
-    lim = {}
-    tg = AD.setup(precision='fp64', adjointTarget=True, isSlopeLim=True, **kw)
+    # the same workload with the linear and with the hierarchical vertex limiter on (the adjoint
+    # through the limiter's choices)
+    out['linear_limiter'] = limited_adjoint_rows(AD, kw, reps, fd_dirs, 'linear')
+    out['hierarchical_limiter'] = limited_adjoint_rows(AD, kw, reps, fd_dirs, 'hierarch_vert')
+    return out
+
+
+def limited_adjoint_rows(AD, kw, reps, fd_dirs, lim):
+    """Backward over forward with the limiter `lim` on, FP64 and FP32, stages stored and 20
+    snapshots; FP64 finite differences in theta over 20 steps and the 200-step sensitivity."""
+    kwl = dict(kw, isSlopeLim=True, typeSlopeLim=lim)
+    rows = {}
+    tg = AD.setup(precision='fp64', adjointTarget=True, **kwl)
     tg.solver.step(kw['numSteps'], 0, tg.tau)
     cstarL = tg.solver.get_state()
     tg.solver.close()
     for prec in ('fp64', 'fp32'):
-        pd = AD.setup(precision=prec, isSlopeLim=True, **kw)
+        pd = AD.setup(precision=prec, **kwl)
         s = pd.solver
         c0 = np.asfortranarray(pd._cDisc)
         s.set_state(c0); s.step(kw['numSteps'], 0, pd.tau); s.sync()
@@ -409,19 +419,18 @@ def adjoint_block(reps=3, fd_dirs=16):
                 t = time.perf_counter(); g0, gth = s.backward(r); tb.append(time.perf_counter() - t)
             row[name] = {'backward_ms': 1e3 * min(tb[1:]), 'backward_over_forward': min(tb[1:]) / min(tf)}
         if prec == 'fp64' and fd_dirs:
-            row['fd_theta'] = limited_fd_check(AD, kw, fd_dirs)
+            row['fd_theta'] = limited_fd_check(AD, kw, fd_dirs, lim=lim)
             row['sensitivity'] = limited_sensitivity(AD, pd, c0, cstarL, kw['numSteps'])
-        lim[prec] = row
+        rows[prec] = row
         s.close()
-    out['linear_limiter'] = lim
-    return out
+    return rows
 
 
-def limited_fd_check(AD, kw, fd_dirs, steps=20, h=1e-7):
+def limited_fd_check(AD, kw, fd_dirs, steps=20, h=1e-7, lim='linear'):
     """Central differences in theta against the limited adjoint on the same mesh over `steps`
     steps.  The limited map is piecewise smooth; over this horizon a perturbation of relative
     size h stays inside one smooth piece."""
-    kw20 = dict(kw, numSteps=steps, tEnd=steps * kw['tEnd'] / kw['numSteps'])
+    kw20 = dict(kw, numSteps=steps, tEnd=steps * kw['tEnd'] / kw['numSteps'], typeSlopeLim=lim)
     tg = AD.setup(precision='fp64', adjointTarget=True, isSlopeLim=True, **kw20)
     tg.solver.step(steps, 0, tg.tau)
     cstar = tg.solver.get_state()
