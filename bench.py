@@ -612,9 +612,9 @@ def transport_block(device, steps=200, with_cpu=True):
 def ensemble_block(rank, world, device, n=256, steps=200, reps=3):
     """The ensemble workload: n seeded instances (2048 to 32768 triangles, p in {1, 2}, their own
     velocity fields), 200 steps in FP32 with the linear limiter.  Each degree group is one
-    stacked handle and the groups are linked (one launch per stage kernel for all instances),
-    autotuned first; for comparison the groups are then unlinked, tuned and timed on their own
-    streams.  Instances are sharded across ranks with no exchange; whole-job DOF-stage/s = all
+    stacked handle; the autotuner tunes the linked step (one launch per stage kernel for all
+    instances) and the groups on their own streams, and keeps the faster schedule, which is then
+    timed.  Instances are sharded across ranks with no exchange; whole-job DOF-stage/s = all
     ranks' work / the slowest rank's time."""
     import torch
     from festung_gb300 import ensemble as E
@@ -623,40 +623,25 @@ def ensemble_block(rank, world, device, n=256, steps=200, reps=3):
     setup_s = time.perf_counter() - t
     flush = torch.empty(512 * 2 ** 20, dtype=torch.uint8, device='cuda')
     units = ens.dof_stages(steps)
-
-    def timed():
+    tuned = ens.tune()
+    ens.step(steps)
+    ens.sync()
+    times = []
+    for _ in range(reps):
+        ens.reset()
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         ens.step(steps)
         ens.sync()
-        times = []
-        for _ in range(reps):
-            ens.reset()
-            flush.zero_()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            ens.step(steps)
-            ens.sync()
-            times.append(time.perf_counter() - t0)
-        dt = min(times)
-        u = float(units)
-        if world > 1:
-            x = torch.tensor([dt, u], dtype=torch.float64, device='cuda')
-            mx = x.clone()
-            torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-            torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.SUM)
-            dt, u = float(mx[0]), float(x[1])
-        return dt, u
-
-    tuned = ens.tune()
-    launches = ens.kernels_per_step()
-    linked = ens.primary is not None
-    dt, u = timed()
-    sep = None
-    if linked:
-        ens.unlink()
-        tunedSep = ens.tune()
-        dts, us = timed()
-        sep = {'value': us / dts, 'ms_per_solve': 1e3 * dts, 'kernels_per_step': ens.kernels_per_step(),
-               'tuned': tunedSep}
+        times.append(time.perf_counter() - t0)
+    dt, u = min(times), float(units)
+    if world > 1:
+        x = torch.tensor([dt, u], dtype=torch.float64, device='cuda')
+        mx = x.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.SUM)
+        dt, u = float(mx[0]), float(x[1])
     out = {'workload': 'ensemble: %d seeded instances, hmax in {2^-5,2^-6,2^-7} with 0.2 h jitter, p in {1,2}, '
                        '8-mode streamfunction velocity, Gaussian hump, %d steps of 5e-4, FP32, linear limiter'
                        % (n, steps),
@@ -664,12 +649,11 @@ def ensemble_block(rank, world, device, n=256, steps=200, reps=3):
            'value': u / dt, 'unit': 'DOF-stage/s', 'ms_per_solve': 1e3 * dt,
            'groups': {int(p): {'instances': len(m), 'elements': int(sum(ens.problems[i].K for i in m))}
                       for p, m in ens.groups.items()},
-           'linked': linked, 'kernels_per_step': launches, 'tuned': tuned,
-           'separate_groups': sep,
+           'schedule': tuned.get('schedule'), 'kernels_per_step': ens.kernels_per_step(), 'tuned': tuned,
            'host_setup_s': setup_s,
-           'timing': 'wall clock of 200 steps after an L2 flush, initial data reset and limited before each; '
-                     'linked: every degree group in one launch per stage kernel; separate_groups: one '
-                     'handle per degree on its own stream'}
+           'timing': 'wall clock of 200 steps after an L2 flush, initial data reset and limited before each, '
+                     'in the schedule the autotuner kept (linked: every degree group in one launch per '
+                     'stage kernel; separate: one handle per degree on its own stream)'}
     ens.close()
     return out
 

@@ -318,8 +318,10 @@ __device__ __forceinline__ void adj_volume_role(const Geo<T> &g, const AdjSplitI
   }
 }
 
+// Up to p = 2, 64 registers at most (8 / W blocks of 128 W threads per SM): a 32768-triangle
+// stage then fits one wave of CTAs with two warps per role.
 template <typename T, int P, int W>
-__global__ void __launch_bounds__(128 * W)
+__global__ void __launch_bounds__(128 * W, P <= 2 ? 8 / W : 1)
 k_adj_stage_split(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__restrict__ muOut,
                   T *__restrict__ accn, double *__restrict__ aF, double *__restrict__ aV, const AdjScalars a) {
   constexpr int N = Dims<P>::N;

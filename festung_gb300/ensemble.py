@@ -81,10 +81,7 @@ class Ensemble:
         # the persistent pipeline stay on their own streams)
         if (linked and len(self.solvers) > 1 and precision in ('fp32', 'fp64')
                 and not flags & (L.FLAG_FUSE | L.FLAG_PERSIST)):
-            order = sorted(self.solvers, key=lambda p: -sum(self.problems[i].K for i in self.groups[p]))
-            self.primary = self.solvers[order[0]]
-            for p in order[1:]:
-                self.primary.link(self.solvers[p])
+            self._link()
         self.reset()
 
     @property
@@ -139,15 +136,52 @@ class Ensemble:
                 out[i] = np.array(c)
         return out
 
+    def _time(self, nSteps, reps):
+        """Wall time (s) of nSteps steps of every instance, best of reps, state restored."""
+        import time
+        saved = {p: s.get_state() for p, s in self.solvers.items()}
+        self.step(nSteps)
+        self.sync()
+        best = float('inf')
+        for _ in range(reps):
+            t = time.perf_counter()
+            self.step(nSteps)
+            self.sync()
+            best = min(best, time.perf_counter() - t)
+        for p, s in self.solvers.items():
+            s.set_state(saved[p])
+        return best
+
+    def _link(self):
+        order = sorted(self.solvers, key=lambda p: -sum(self.problems[i].K for i in self.groups[p]))
+        self.primary = self.solvers[order[0]]
+        for p in order[1:]:
+            self.primary.link(self.solvers[p])
+
     def tune(self, nSteps=48, reps=3, cache=None):
-        """Autotunes every group's launch configuration (festung_gb300.autotune)."""
+        """Autotunes the launch configuration (festung_gb300.autotune): for linked groups, the
+        linked step's configuration, then each group's on its own stream, and keeps the faster
+        of the two schedules (returned under 'schedule' with both times per step)."""
         from . import autotune as AT
         out = {}
         if self.primary is not None:   # the linked step: the primary's launch configuration
             s = self.primary
             key = AT.signature(s, self.tau, s.precision, '|ensemble-linked:%d' % len(self.problems)) if cache else None
             out['linked'] = AT.tune(s, self.tau, nSteps, reps, fused_ok=False, cache=cache, key=key)[0]
+            tLinked = self._time(nSteps, reps) / nSteps
+            self.unlink()
+            out['separate'] = self._tune_groups(nSteps, reps, cache)
+            tSep = self._time(nSteps, reps) / nSteps
+            chosen = 'linked' if tLinked <= tSep else 'separate'
+            if chosen == 'linked':
+                self._link()
+            out['schedule'] = dict(chosen=chosen, ms_per_step={'linked': 1e3 * tLinked, 'separate': 1e3 * tSep})
             return out
+        return self._tune_groups(nSteps, reps, cache)
+
+    def _tune_groups(self, nSteps, reps, cache):
+        from . import autotune as AT
+        out = {}
         for p, s in self.solvers.items():
             pd0 = self.problems[self.groups[p][0]]
             fused_ok = pd0.isSlopeLim and pd0.typeSlopeLim == 'linear' and s.precision != 'df32' and not pd0.cDTerms
