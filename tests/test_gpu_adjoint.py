@@ -272,20 +272,6 @@ def test_hierarchical_checkpointed_sweep_equals_stored_sweep(lib, precision):
         pd.solver.close()
 
 
-def test_hierarchical_fp32_gradient_close_to_fp64(lib):
-    from festung_gb300 import adjoint as AD
-    out = {}
-    for prec in ('fp64', 'fp32'):
-        pd, cstar = _hier_case(HIER[0], prec)
-        try:
-            c0 = np.asfortranarray(pd._cDisc)
-            out[prec] = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
-        finally:
-            pd.solver.close()
-    assert rel(out['fp32'][1], out['fp64'][1]) <= 1e-2
-    assert rel(out['fp32'][2], out['fp64'][2]) <= 1e-2
-
-
 def test_strict_limiter_has_no_adjoint(lib):
     from festung_gb300 import _lib as L
     from festung_gb300 import adjoint as AD
