@@ -133,12 +133,35 @@ void dev_release(dgadv_handle *h, void *&p) {
   p = nullptr;
 }
 
-// Cursor of a schedule run: the step the run stands at, where that state lives (a slot, or the
-// work buffer cn), and which step cn holds.
+// Buffers a forward step of the schedule writes besides its output: its work state, its stage
+// states and its limiter records.  Set 0 is the handle's own (cn, cA, cB, adjScrY, adjScrCdot).
+// With two streams the recomputation alternates between set 0 and set 1 (adjSet1), so that it
+// writes one set while the reverse stages read the other.
+struct WorkSet {
+  void *cn = nullptr, *cA = nullptr, *cB = nullptr, *scrY = nullptr, *scrCdot = nullptr;
+};
+
+// Cursor of a schedule run: the step the run stands at, the slot holding that state (-1: none),
+// and the step each set's work state holds (-1: none).
 struct Cursor {
-  int step = 0;     // state the schedule has reached
-  int slot = -1;    // slot holding that state (-1: only cn holds it)
-  int cnStep = 0;   // step held by cn (-1: none)
+  int step = 0;
+  int slot = -1;
+  int cnStep[2] = {0, -1};
+};
+
+// The streams of a schedule run.  One stream: every action in order on the handle's stream.
+// Two: the forward steps (advances and recomputation) on adjStreamF and the reverse stages on
+// the handle's stream.  A reversed step waits for its recomputation; a forward step that writes
+// a set or a slot first waits for the last reversed step that read it.  The results are bitwise
+// those of one stream: the same kernels read the same data.
+struct Lanes {
+  bool two = false;
+  cudaStream_t rev = nullptr, fwd = nullptr;
+  WorkSet set[2];
+  int cur = 0;                   // the set forward steps write
+  int setReader[2] = {-1, -1};   // event of the last reversed step that read a set (-1: none)
+  std::vector<int> slotReader;   // ... that read a slot
+  int nRev = 0;                  // reversed steps issued
 };
 
 int rk_stages(const dgadv_handle *h, double omega[3]) {
@@ -148,58 +171,76 @@ int rk_stages(const dgadv_handle *h, double omega[3]) {
   return 1;
 }
 
-// One forward step from c^step, read from `src` (cn or a slot), written to `dst` (cn or a slot);
-// with stage storage the step's stage states are written straight into its stage slots.  With
+// The forward stream waits for the reversed step `ev` (an index into adjRevEv), if any.
+int wait_reader(dgadv_handle *h, Lanes &L, int &ev) {
+  if (!L.two || ev < 0) return DGADV_OK;
+  DG_CUDA(cudaStreamWaitEvent(L.fwd, h->adjRevEv[ev], 0));
+  h->pdlBreak = true;
+  ev = -1;
+  return DGADV_OK;
+}
+
+// One forward step from c^step, read from `src` (a work state or a slot), written to `dst`; with
+// stage storage the step's stage states are written straight into its stage slots.  With
 // nStages < S only the first nStages stages run: their outputs (cA, cB) are what the reverse
-// stages of the unlimited scheme read, and c^(step+1) is neither needed nor written.
-int forward_step(dgadv_handle *h, Cursor &w, const void *src, void *dst, int nStages) {
+// stages of the unlimited scheme read.  recordsOnly runs every stage but the last solution
+// limiter: the limiter inputs are what the limiter adjoint reads.  In both cases c^(step+1) is
+// neither needed nor written, and the cursor stays.
+int forward_step(dgadv_handle *h, Cursor &w, Lanes &L, const void *src, void *dst, int nStages,
+                 bool recordsOnly = false) {
   const PrecOps &o = ops_of(h);
   double omega[3];
   const int S = rk_stages(h, omega);
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
   const bool partial = nStages < S;
   if (partial && nStages <= 0) return DGADV_OK;   // one stage: its input c^step is all it needs
+  int st;
+  if ((st = wait_reader(h, L, L.setReader[L.cur]))) return st;
+  const WorkSet &ws = L.set[L.cur];
   void *cA = h->cA, *cB = h->cB;
+  h->cA = ws.cA;
+  h->cB = ws.cB;
   if (h->adjStages && S > 1) {
-    char *st = (char *)h->adjStages + (size_t)w.step * (S - 1) * bytes;
-    h->cA = st;
-    if (S > 2) h->cB = st + bytes;
+    char *sp = (char *)h->adjStages + (size_t)w.step * (S - 1) * bytes;
+    h->cA = sp;
+    if (S > 2) h->cB = sp + bytes;
   }
   if (h->lim) {   // the limiter inputs of every stage: per step (stage storage) or scratch
     for (int s = 0; s < S; ++s) {
       h->recY[s] = h->adjRecY ? (char *)h->adjRecY + ((size_t)w.step * S + s) * bytes
-                              : (char *)h->adjScrY + (size_t)s * bytes;
+                              : (char *)ws.scrY + (size_t)s * bytes;
       if (h->limdot)
         h->recCdot[s] = h->adjRecCdot ? (char *)h->adjRecCdot + ((size_t)w.step * S + s) * bytes
-                                      : (char *)h->adjScrCdot + (size_t)s * bytes;
+                                      : (char *)ws.scrCdot + (size_t)s * bytes;
     }
   }
-  h->stepSrc = src == h->cn ? nullptr : src;
-  h->stepDst = dst == h->cn ? nullptr : dst;
+  h->stepSrc = src;
+  h->stepDst = dst;
   h->stepStages = partial ? nStages : 0;
+  h->stepRecordsOnly = recordsOnly;
   const cudaError_t e = o.step(h, w.step * h->recTau, h->recTau);
   h->cA = cA;
   h->cB = cB;
   h->stepSrc = nullptr;
   h->stepDst = nullptr;
   h->stepStages = 0;
+  h->stepRecordsOnly = false;
   for (int s = 0; s < 3; ++s) h->recY[s] = h->recCdot[s] = nullptr;
   DG_CUDA(e);
-  if (partial) return DGADV_OK;
+  if (partial || recordsOnly) return DGADV_OK;
   ++w.step;
-  if (dst == h->cn) {
-    w.cnStep = w.step;
-    w.slot = -1;
-  }
+  w.slot = -1;
+  w.cnStep[L.cur] = dst == ws.cn ? w.step : -1;
   return DGADV_OK;
 }
 
-// Executes schedule actions [from, to) on the handle's stream.  Restores cost nothing: a step
-// reads c^i from the slot that holds it, and an advance whose next action stores its result
-// writes that result straight into the slot.  With stage storage (every step's stage states kept
-// by the recorded run) a reversed step reads its stages from there and recomputes nothing;
-// without it, the unlimited scheme recomputes only the stages whose inputs it needs.
-int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
+// Executes schedule actions [from, to).  Restores cost nothing: a step reads c^i from the slot
+// that holds it, and an advance whose next action stores its result writes that result straight
+// into the slot.  With stage storage (every step's stage states kept by the recorded run) a
+// reversed step reads its stages from there and recomputes nothing; without it, the unlimited
+// scheme recomputes only the stages whose inputs its reverse stages read, and the limited scheme
+// every stage up to the last limiter inputs.
+int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
   const PrecOps &o = ops_of(h);
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
   const double tau = h->recTau;
@@ -210,12 +251,14 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
   char *stages = (char *)h->adjStages;
   auto stage_ptr = [&](int step, int s) { return stages + ((size_t)step * (S - 1) + (s - 1)) * bytes; };
   auto slot_ptr = [&](int slot) { return slots + (size_t)slot * bytes; };
-  // where c^(w.step) can be read
-  auto current = [&](const void *&src) -> int {
-    if (w.cnStep == w.step) src = h->cn;
-    else if (w.slot >= 0 && h->slotStep[w.slot] == w.step) src = slot_ptr(w.slot);
-    else { h->err = "checkpoint schedule lost its state"; return DGADV_EINVAL; }
-    return DGADV_OK;
+  // where c^(w.step) can be read: its slot, else a work state (the forward set's first)
+  auto current = [&](const void *&src, int &fromSet) -> int {
+    fromSet = -1;
+    if (w.slot >= 0 && h->slotStep[w.slot] == w.step) { src = slot_ptr(w.slot); return DGADV_OK; }
+    for (int k : {L.cur, 1 - L.cur})
+      if (w.cnStep[k] == w.step && L.set[k].cn) { src = L.set[k].cn; fromSet = k; return DGADV_OK; }
+    h->err = "checkpoint schedule lost its state";
+    return DGADV_EINVAL;
   };
   int st;
   for (size_t a = from; a < to; a += 2) {
@@ -224,23 +267,31 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
       w.step = h->slotStep[arg];
       w.slot = arg;
     } else if (op == A_ADVANCE) {
+      h->stream = L.two ? L.fwd : L.rev;
       const bool storeNext = a + 2 < to && h->schedule[a + 2] == A_STORE;
       for (int i = 0; i < arg; ++i) {
         const void *src;
-        if ((st = current(src))) return st;
-        void *dst = h->cn;
+        int fromSet;
+        if ((st = current(src, fromSet))) return st;
+        void *dst = L.set[L.cur].cn;
         const int target = storeNext && i == arg - 1 ? h->schedule[a + 3] : -1;
-        if (target >= 0 && slot_ptr(target) != src) dst = slot_ptr(target);
-        if ((st = forward_step(h, w, src, dst, S))) return st;
-        if (dst != h->cn) {   // the result already sits in the slot the next action stores to
+        if (target >= 0 && slot_ptr(target) != src) {
+          dst = slot_ptr(target);
+          if ((st = wait_reader(h, L, L.slotReader[target]))) return st;
+        }
+        if ((st = forward_step(h, w, L, src, dst, S))) return st;
+        if (dst != L.set[L.cur].cn) {   // the result already sits in the slot the next action stores to
           h->slotStep[target] = w.step;
           w.slot = target;
         }
       }
     } else if (op == A_STORE) {
       if (!(w.slot == arg && h->slotStep[arg] == w.step)) {
+        h->stream = L.two ? L.fwd : L.rev;
         const void *src;
-        if ((st = current(src))) return st;
+        int fromSet;
+        if ((st = current(src, fromSet))) return st;
+        if ((st = wait_reader(h, L, L.slotReader[arg]))) return st;
         DG_CUDA(o.copy(h, slot_ptr(arg), src, bytes));
         h->slotStep[arg] = w.step;
         w.slot = arg;
@@ -248,28 +299,29 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
     } else {   // A_BACKWARD: the stage states of step arg (stored or recomputed), then reversed
       if (w.step != arg) { h->err = "checkpoint schedule out of order"; return DGADV_EINVAL; }
       const void *stageIn[3];
+      int fromSet = -1;
+      const int used = L.cur;   // the set this step's recomputation writes
       if (stages) {
         if (w.slot < 0) { h->err = "checkpoint schedule lost its state"; return DGADV_EINVAL; }
         stageIn[0] = slot_ptr(w.slot);
         for (int s = 1; s < S; ++s) stageIn[s] = stage_ptr(arg, s);
       } else {
+        h->stream = L.two ? L.fwd : L.rev;
         const void *c0;
-        if ((st = current(c0))) return st;
-        if (h->lim) {
-          // the limiter adjoint reads every stage's limiter inputs, so the whole step runs and
-          // its result goes to cn: c^arg read from cn moves to cx first
-          if (c0 == h->cn) {
-            DG_CUDA(o.copy(h, h->cx, h->cn, bytes));
-            c0 = h->cx;
-          }
-          if ((st = forward_step(h, w, c0, h->cn, S))) return st;
-        } else if ((st = forward_step(h, w, c0, h->cn, S - 1))) {
-          return st;
-        }
+        if ((st = current(c0, fromSet))) return st;
+        // unlimited: the stages the reverse stages read; limited: every stage's limiter inputs
+        if ((st = forward_step(h, w, L, c0, nullptr, h->lim ? S : S - 1, h->lim))) return st;
         stageIn[0] = c0;
-        stageIn[1] = h->cA;
-        stageIn[2] = h->cB;
+        stageIn[1] = L.set[used].cA;
+        stageIn[2] = L.set[used].cB;
+        if (L.two) {
+          DG_CUDA(cudaEventRecord(h->adjFEv, L.fwd));
+          DG_CUDA(cudaStreamWaitEvent(L.rev, h->adjFEv, 0));
+          h->pdlBreak = true;
+        }
       }
+      h->stream = L.rev;
+      const WorkSet &ws = L.set[used];
       void *mub[3] = {nullptr, h->mu1, h->mu2};
       for (int s = S - 1; s >= 0; --s) {
         const void *muNext = (s == S - 1) ? h->lam : mub[s + 1];
@@ -277,19 +329,16 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
         if (h->lim) {
           // solution limiter, then (p >= 2) the time-derivative limiter, transposed
           const char *Y = h->adjRecY ? (const char *)h->adjRecY + ((size_t)arg * S + s) * bytes
-                                     : (const char *)h->adjScrY + (size_t)s * bytes;
+                                     : (const char *)ws.scrY + (size_t)s * bytes;
           LimVjpArgs v;
           std::memset(&v, 0, sizeof(v));
           const double tBC = (s + 1 < S) ? (arg + cst[s + 1]) * tau : (arg + 1) * tau;
           for (int m = 0; m < h->nTerms; ++m)
             v.gco[m] = h->timeFn[m] == DGADV_TIME_EXP_NEG ? std::exp(-tBC) : 1.0;
-          // p >= 2: the solution limiter's kernel also scatters the time-derivative limiter's
-          // means, and the time-derivative limiter's kernel gathers the solution limiter's
-          // extreme terms first (5 launches per stage instead of 7)
           const char *Cd = nullptr;
           if (h->limdot)
             Cd = h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
-                               : (const char *)h->adjScrCdot + (size_t)s * bytes;
+                               : (const char *)ws.scrCdot + (size_t)s * bytes;
           if (h->limType == DGADV_LIM_HIERARCH_VERT) {
             // hierarchical limiter (inputs recorded in Taylor form): per limiter its scatter,
             // its pass and its gather
@@ -307,22 +356,25 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
               mp = h->tmpD;
             }
           } else {
-          DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
-          v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
-          v.nextX = Cd;
-          v.gatherOut = Cd ? 0 : 1;
-          DG_CUDA(o.lim_vjp(h, v));
-          muY = h->tmpY;
-          if (h->limdot) {
-            LimVjpArgs d;
-            std::memset(&d, 0, sizeof(d));
-            d.kind = 1; d.x = Cd; d.lamIn = h->tmpY; d.lamOut = h->tmpD; d.scale = (1.0 - omega[s]) * tau;
-            d.pass = h->adjPass++;
-            d.gatherIn = 1;
-            d.gatherOut = 1;
-            DG_CUDA(o.lim_vjp(h, d));
-            mp = h->tmpD;
-          }
+            // p >= 2: the solution limiter's kernel also scatters the time-derivative limiter's
+            // means, and the time-derivative limiter's kernel gathers the solution limiter's
+            // extreme terms first (5 launches per stage instead of 7)
+            DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
+            v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
+            v.nextX = Cd;
+            v.gatherOut = Cd ? 0 : 1;
+            DG_CUDA(o.lim_vjp(h, v));
+            muY = h->tmpY;
+            if (h->limdot) {
+              LimVjpArgs d;
+              std::memset(&d, 0, sizeof(d));
+              d.kind = 1; d.x = Cd; d.lamIn = h->tmpY; d.lamOut = h->tmpD; d.scale = (1.0 - omega[s]) * tau;
+              d.pass = h->adjPass++;
+              d.gatherIn = 1;
+              d.gatherOut = 1;
+              DG_CUDA(o.lim_vjp(h, d));
+              mp = h->tmpD;
+            }
           }
         }
         AdjStageArgs x;
@@ -337,12 +389,100 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w) {
         x.last = s == 0;
         DG_CUDA(o.adj_stage(h, x));
       }
+      if (L.two && !stages) {   // what this step read: its set, and the slot or set of c^arg
+        const int ev = L.nRev++;
+        DG_CUDA(cudaEventRecord(h->adjRevEv[ev], L.rev));
+        L.setReader[used] = ev;
+        if (fromSet >= 0) L.setReader[fromSet] = ev;
+        else if (w.slot >= 0) L.slotReader[w.slot] = ev;
+        L.cur = 1 - used;
+      }
       std::swap(h->lam, h->accn);
       w.step = arg + 1;
       w.slot = -1;
     }
   }
+  h->stream = L.rev;
   return DGADV_OK;
+}
+
+// The lanes of a run: the handle's buffers as set 0; for a reverse sweep that recomputes, with
+// two streams enabled, set 1 and the forward stream (forked from the handle's stream).
+int make_lanes(dgadv_handle *h, Lanes &L, bool sweep) {
+  L.rev = h->stream;
+  L.set[0].cn = h->cn;
+  L.set[0].cA = h->cA;
+  L.set[0].cB = h->cB;
+  L.set[0].scrY = h->adjScrY;
+  L.set[0].scrCdot = h->adjScrCdot;
+  L.slotReader.assign(h->nSlots, -1);
+  // (the resources come from the recorded run: a run recorded with one stream sweeps with one)
+  L.two = sweep && h->adjTwoStreams && h->adjSet1 && (int)h->adjRevEv.size() >= h->recSteps && !h->adjStages &&
+          !h->adjRecY;
+  if (!L.two) return DGADV_OK;
+  const PrecOps &o = ops_of(h);
+  const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
+  double omega[3];
+  const int S = rk_stages(h, omega);
+  char *b = (char *)h->adjSet1;
+  L.set[1].cn = b;
+  L.set[1].cA = b + bytes;
+  L.set[1].cB = b + 2 * bytes;
+  if (h->lim) {
+    L.set[1].scrY = b + 3 * bytes;
+    L.set[1].scrCdot = b + (3 + (size_t)S) * bytes;
+  }
+  L.fwd = h->adjStreamF;
+  DG_CUDA(cudaEventRecord(h->adjFEv, L.rev));
+  DG_CUDA(cudaStreamWaitEvent(L.fwd, h->adjFEv, 0));
+  h->pdlBreak = true;
+  return DGADV_OK;
+}
+
+// Joins the forward stream back into the handle's stream.
+int join_lanes(dgadv_handle *h, Lanes &L) {
+  h->stream = L.rev;
+  if (!L.two) return DGADV_OK;
+  DG_CUDA(cudaEventRecord(h->adjFEv, L.fwd));
+  DG_CUDA(cudaStreamWaitEvent(L.rev, h->adjFEv, 0));
+  h->pdlBreak = true;
+  return DGADV_OK;
+}
+
+// Two-stream resources of a recorded run that recomputes: set 1, the stream and the events.
+int lanes_alloc(dgadv_handle *h, int nSteps) {
+  const PrecOps &o = ops_of(h);
+  const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
+  double omega[3];
+  const int S = rk_stages(h, omega);
+  const size_t states = 3 + (h->lim ? 2 * (size_t)S : 0);
+  int st;
+  if (h->adjSet1States != states) {
+    drop_sweep(h);
+    dev_release(h, h->adjSet1);
+    h->adjSet1States = 0;
+    if ((st = dev_alloc(h, &h->adjSet1, states * bytes))) return st;
+    h->adjSet1States = states;
+  }
+  if (!h->adjStreamF) DG_CUDA(cudaStreamCreateWithFlags(&h->adjStreamF, cudaStreamNonBlocking));
+  if (!h->adjFEv) DG_CUDA(cudaEventCreateWithFlags(&h->adjFEv, cudaEventDisableTiming));
+  while ((int)h->adjRevEv.size() < nSteps) {
+    cudaEvent_t e;
+    DG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->adjRevEv.push_back(e);
+  }
+  return DGADV_OK;
+}
+
+// The reverse sweep: the schedule's actions from the first reversed step on, c^nSteps in cn.
+int reverse_sweep(dgadv_handle *h) {
+  Cursor w;
+  w.step = w.cnStep[0] = h->recSteps;
+  Lanes L;
+  int st = make_lanes(h, L, true);
+  if (st == DGADV_OK) st = run_actions(h, h->schedBackward, h->schedule.size(), w, L);
+  const int sj = join_lanes(h, L);
+  return st ? st : sj;
 }
 
 }  // namespace
@@ -480,6 +620,8 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
     }
     drop_sweep(h);
   }
+  // the reverse sweep recomputes: its second stream and buffer set
+  if (stageSteps == 0 && (S > 1 || h->lim) && h->adjTwoStreams && (st = lanes_alloc(h, nSteps))) return st;
   h->slotStep.assign(nSlots, -1);
   make_schedule(nSteps, nSlots, h->schedule);
   h->schedBackward = backward_start(h->schedule);
@@ -490,17 +632,19 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
   h->slotStep[0] = 0;
   Cursor w;
   w.slot = 0;
-  if ((st = run_actions(h, 0, h->schedBackward, w))) return st;
+  Lanes L;
+  if ((st = make_lanes(h, L, false))) return st;
+  if ((st = run_actions(h, 0, h->schedBackward, w, L))) { h->stream = L.rev; return st; }
   // on to c^nSteps in cn; the state reached may sit in a slot only
-  if (w.cnStep != w.step && (w.slot < 0 || h->slotStep[w.slot] != w.step)) {
+  if (w.cnStep[0] != w.step && (w.slot < 0 || h->slotStep[w.slot] != w.step)) {
     h->err = "checkpoint schedule lost its state";
     return DGADV_EINVAL;
   }
   while (w.step < nSteps) {
-    const void *src = w.cnStep == w.step ? h->cn : (const void *)((char *)h->adjSlots + (size_t)w.slot * bytes);
-    if ((st = forward_step(h, w, src, h->cn, S))) return st;
+    const void *src = w.cnStep[0] == w.step ? h->cn : (const void *)((char *)h->adjSlots + (size_t)w.slot * bytes);
+    if ((st = forward_step(h, w, L, src, h->cn, S))) return st;
   }
-  if (w.cnStep != w.step) DG_CUDA(o.copy(h, h->cn, (char *)h->adjSlots + (size_t)w.slot * bytes, bytes));
+  if (w.cnStep[0] != w.step) DG_CUDA(o.copy(h, h->cn, (char *)h->adjSlots + (size_t)w.slot * bytes, bytes));
   h->recorded = true;
   return DGADV_OK;
   });
@@ -544,11 +688,9 @@ extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc
   int st = DGADV_OK;
   const bool useGraph = !(h->flags & DGADV_FLAG_NO_GRAPH);
   if (useGraph && !h->adjExec) {
-    Cursor w;
-    w.step = w.cnStep = h->recSteps;
     cudaGraph_t graph = nullptr;
     DG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    st = run_actions(h, h->schedBackward, h->schedule.size(), w);
+    st = reverse_sweep(h);
     const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     if (st == DGADV_OK && e != cudaSuccess) {
       h->err = std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e);
@@ -568,9 +710,7 @@ extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc
     }
     if (graph) cudaGraphDestroy(graph);
   } else if (!useGraph) {
-    Cursor w;
-    w.step = w.cnStep = h->recSteps;
-    st = run_actions(h, h->schedBackward, h->schedule.size(), w);
+    st = reverse_sweep(h);
   }
   if (st == DGADV_OK && useGraph) {
     const cudaError_t e = cudaGraphLaunch(h->adjExec, h->stream);

@@ -48,7 +48,10 @@ struct dgadv_handle {
   const void *stepSrc = nullptr;
   void *stepDst = nullptr;
   int stepStages = 0;
+  bool stepRecordsOnly = false;        // ... and the last stage's solution limiter is left out
+  mutable bool pdlBreak = false;       // the next launch waits for its predecessors to complete
   int adjWarps = 2;                    // warps per role of the FP32 adjoint stage (1, 2 or 4)
+  bool adjTwoStreams = true;           // reverse sweep: recomputation on a second stream
   bool mtOnTheFly = false;             // Taylor mass correction rebuilt from B (DGADV_OPT_TAYLOR_MASS)
   bool volumeMma = false;              // volume term on the tensor cores (DGADV_OPT_VOLUME_MMA)
   int opBlock = 128;                   // elements per block of the stage operator (DGADV_OPT_OP_BLOCK)
@@ -114,6 +117,13 @@ struct dgadv_handle {
   void *recY[3] = {nullptr, nullptr, nullptr}, *recCdot[3] = {nullptr, nullptr, nullptr};
   void *adjRecY = nullptr, *adjRecCdot = nullptr;   // per step and stage (stage storage mode)
   void *adjScrY = nullptr, *adjScrCdot = nullptr;   // per stage (recomputing modes)
+  // the reverse sweep's recomputation stream, its second buffer set (state, two stage states,
+  // S + S limiter records) and the events between the two streams (one per reversed step)
+  cudaStream_t adjStreamF = nullptr;
+  void *adjSet1 = nullptr;
+  size_t adjSet1States = 0;
+  cudaEvent_t adjFEv = nullptr;
+  std::vector<cudaEvent_t> adjRevEv;
   void *tmpY = nullptr, *tmpD = nullptr;            // dJ/dy and dJ/dcDot of a reversed stage
   // extreme terms of the limiter adjoint, one record set per limiter kind, stored by position in
   // the vertex-patch CSR (vidx): the element at position i of patch v writes there the element

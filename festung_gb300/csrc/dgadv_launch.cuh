@@ -186,7 +186,8 @@ static void launch_kb(const dgadv_handle *h, void (*kern)(KArgs...), int grid, i
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = (h->flags & DGADV_FLAG_NO_PDL) ? 0 : 1;
+  cfg.numAttrs = ((h->flags & DGADV_FLAG_NO_PDL) || h->pdlBreak) ? 0 : 1;
+  h->pdlBreak = false;
   cudaLaunchKernelEx(&cfg, kern, args...);
 }
 template <typename... KArgs, typename... Args>
@@ -346,6 +347,8 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
       prof_mark(h, -1);
       loS = lo2;
     }
+    // the adjoint's recomputation wants the limiter inputs only: c^(n+1) is not written
+    if (h->stepRecordsOnly && s == S - 1) break;
     prof_mark(h, 2);
     if (lin) launch_k(h, k_limit_lin<T, P>, gridK, (size_t)0, g, (const T *)yB, out, lim_in<T>(loS, h), scBC);
     else if (h->limType == DGADV_LIM_STRICT)
@@ -354,7 +357,7 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
       launch_k(h, k_limit<T, P, 1>, grid, SR::bytes(SR::lim(), 1), g, (const T *)yB, out, lim_in<T>(loS, h), scBC);
     prof_mark(h, -1);
   }
-  if (S == 1 && nRun == 1 && (const T *)dst == cn) return copy_state(h, dst, cA, (size_t)h->N * h->Kp * sizeof(T));
+  if (S == 1 && nRun == 1 && (const T *)dst == cn && !h->stepRecordsOnly) return copy_state(h, dst, cA, (size_t)h->N * h->Kp * sizeof(T));
   return cudaGetLastError();
 }
 

@@ -737,6 +737,9 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
   } else if (option == DGADV_OPT_ADJ_WARPS) {
     if (value != 1 && value != 2 && value != 4) return DGADV_EINVAL;
     h->adjWarps = value;
+  } else if (option == DGADV_OPT_ADJ_STREAMS) {
+    if (value != 1 && value != 2) return DGADV_EINVAL;
+    h->adjTwoStreams = value == 2;
   } else if (option == DGADV_OPT_TAYLOR_MASS) {
     if (value != 0 && value != 1) return DGADV_EINVAL;
     h->mtOnTheFly = value == 1;
@@ -775,6 +778,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   else if (option == DGADV_OPT_FLAGS) *value = h->flags;
   else if (option == DGADV_OPT_PERSIST_BLOCKS) *value = h->persistPerSM;
   else if (option == DGADV_OPT_ADJ_WARPS) *value = h->adjWarps;
+  else if (option == DGADV_OPT_ADJ_STREAMS) *value = h->adjTwoStreams ? 2 : 1;
   else if (option == DGADV_OPT_TAYLOR_MASS) *value = h->mtOnTheFly ? 1 : 0;
   else if (option == DGADV_OPT_VOLUME_MMA) *value = h->volumeMma ? 1 : 0;
   else if (option == DGADV_OPT_OP_BLOCK) *value = h->opBlock;
@@ -908,6 +912,12 @@ extern "C" void dgadv_destroy(dgadv_handle *h) {
   for (int i = 0; i < 3; ++i)
     if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
   if (h->adjExec) cudaGraphExecDestroy(h->adjExec);
+  if (h->adjStreamF) {
+    cudaStreamSynchronize(h->adjStreamF);
+    cudaStreamDestroy(h->adjStreamF);
+  }
+  if (h->adjFEv) cudaEventDestroy(h->adjFEv);
+  for (cudaEvent_t e : h->adjRevEv) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (void *p : h->allocs) cudaFree(p);

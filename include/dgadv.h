@@ -81,10 +81,15 @@ enum {
                                    default): FP32 multiply-adds                                */
   DGADV_OPT_OP_BLOCK = 7,       /* elements per thread block of the stage operator, one thread
                                    per element: 64 or 128 (default); results unchanged        */
-  DGADV_OPT_OPERATOR_FP32 = 8   /* double-float handles: 1 computes the stage operator (volume,
+  DGADV_OPT_OPERATOR_FP32 = 8,  /* double-float handles: 1 computes the stage operator (volume,
                                    flux, mass) in FP32 arithmetic while the state, the SSP
                                    update and the limiter stay double-float; 0 (default): all
                                    double-float                                              */
+  DGADV_OPT_ADJ_STREAMS = 9     /* streams of a reverse sweep that recomputes: 2 (default) runs
+                                   the recomputation on a second stream, one reversed step
+                                   ahead of the reverse stages (one more set of work states and
+                                   limiter records, allocated by dgadv_forward_record); 1: one
+                                   stream.  Gradients bitwise unchanged                        */
 };
 
 /* ---- host helpers: static data ------------------------------------------------------- */

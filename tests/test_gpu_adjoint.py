@@ -272,6 +272,43 @@ def test_hierarchical_checkpointed_sweep_equals_stored_sweep(lib, precision):
         pd.solver.close()
 
 
+STREAM_CASES = [dict(precision='fp32', kw=dict(hmax=2 ** -4, p=2, numSteps=24, tEnd=24 * 1e-4)),
+                dict(precision='fp64', kw=dict(hmax=2 ** -4, p=1, numSteps=16, tEnd=16 * 2e-4, isSlopeLim=True)),
+                dict(precision='fp32', kw=dict(hmax=2 ** -4, p=2, numSteps=16, tEnd=16 * 2e-4, isSlopeLim=True)),
+                dict(precision='fp32', kw=dict(hmax=2 ** -4, p=3, numSteps=10, tEnd=10 * 1e-4, isSlopeLim=True,
+                                               typeSlopeLim='hierarch_vert'))]
+
+
+@pytest.mark.parametrize('case', STREAM_CASES, ids=['unlimited-p2', 'linear-p1', 'linear-p2', 'hier-p3'])
+def test_two_stream_sweep_equals_one_stream_sweep(lib, case):
+    """DGADV_OPT_ADJ_STREAMS: the recomputation on a second stream, one reversed step ahead of
+    the reverse stages, gives bitwise the gradients of one stream, captured in a graph (and
+    replayed) or launched directly, for binomial and every-state checkpoints."""
+    from festung_gb300 import _lib as L
+    from festung_gb300 import adjoint as AD
+    kw = case['kw']
+    tg = AD.setup(precision='fp64', adjointTarget=True, **kw)
+    tg.solver.step(kw['numSteps'], 0, tg.tau)
+    cstar = tg.solver.get_state()
+    tg.solver.close()
+    pd = AD.setup(precision=case['precision'], **kw)
+    try:
+        assert pd.solver.get_option(L.OPT_ADJ_STREAMS) == 2
+        c0 = np.asfortranarray(pd._cDisc)
+        ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
+        for streams in (1, 2):
+            pd.solver.set_option(L.OPT_ADJ_STREAMS, streams)
+            for flags in (0, L.FLAG_NO_GRAPH):
+                pd.solver.set_option(L.OPT_FLAGS, flags)
+                for snaps in (3, 5, kw['numSteps']):
+                    for _ in range(2):
+                        got = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=snaps)
+                        assert got[0] == ref[0]
+                        assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2]), (streams, flags, snaps)
+    finally:
+        pd.solver.close()
+
+
 def test_strict_limiter_has_no_adjoint(lib):
     from festung_gb300 import _lib as L
     from festung_gb300 import adjoint as AD
