@@ -262,6 +262,33 @@ def run_reference(args):
 # from single-kernel ncu captures (-k <kernel> -c 1, cold L2 under ncu) of
 # `bench.py --ncu-case <workload> --precision <p> --ncu-steps 2`, keyed (workload, precision,
 # kernel).
+# FP64 floating-point operations per element of the FP64 stage kernels (2 x DFMA + DADD + DMUL
+# thread instructions, smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum of one
+# single-kernel ncu capture each, divided by the elements), keyed (workload, kernel):
+# profiles/stage_kernels_131k_fp64_full.md.
+MEASURED_FP64_FLOPS = {}
+
+
+def fp64_peak(reps=5, n=4096):
+    """GB300's FP64 rate as a library reaches it: cuBLAS DGEMM (torch.matmul, float64) of n^3,
+    best of reps, CUDA events (TFLOP/s)."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device='cuda')
+    b = torch.randn_like(a)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float('inf')
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
 MEASURED_TRAFFIC = {('gauss_slot_131k_p2', 'fp32', 'k_stage_op'): 18.4e6,
                     ('gauss_slot_131k_p2', 'fp32', 'k_limit_dot'): 28.4e6,
                     ('gauss_slot_131k_p2', 'fp32', 'k_limit'): 5.8e6}
@@ -426,10 +453,13 @@ def limited_adjoint_rows(AD, kw, reps, fd_dirs, lim):
     return rows
 
 
-def limited_fd_check(AD, kw, fd_dirs, steps=20, h=1e-7, lim='linear'):
+def limited_fd_check(AD, kw, fd_dirs, steps=20, hs=(1e-7, 1e-8), lim='linear'):
     """Central differences in theta against the limited adjoint on the same mesh over `steps`
-    steps.  The limited map is piecewise smooth; over this horizon a perturbation of relative
-    size h stays inside one smooth piece."""
+    steps, at each step size in `hs`.  The limited map is piecewise smooth: where a perturbation
+    of relative size h crosses one of the limiter's switches somewhere on the mesh, the central
+    difference averages two slopes.  The hierarchical limiter has many more switches (one per
+    order, vertex and sub-limiter) than the linear one: over 20 steps h = 1e-7 crosses some of
+    them, h = 1e-8 stays inside one piece."""
     kw20 = dict(kw, numSteps=steps, tEnd=steps * kw['tEnd'] / kw['numSteps'], typeSlopeLim=lim)
     tg = AD.setup(precision='fp64', adjointTarget=True, isSlopeLim=True, **kw20)
     tg.solver.step(steps, 0, tg.tau)
@@ -439,13 +469,16 @@ def limited_fd_check(AD, kw, fd_dirs, steps=20, h=1e-7, lim='linear'):
     c0 = np.asfortranarray(pd._cDisc)
     _, _, gth = AD.misfit_gradient(pd, c0, pd.theta, cstar)
     rng = np.random.default_rng(1)
-    errs = []
+    errs = {h: [] for h in hs}
     for _ in range(fd_dirs):
         dt = rng.standard_normal(gth.size) * np.abs(pd.theta)
-        fd = (AD.misfit(pd, c0, pd.theta + h * dt, cstar) - AD.misfit(pd, c0, pd.theta - h * dt, cstar)) / (2 * h)
-        errs.append(abs(fd - float(gth @ dt)) / abs(fd))
+        for h in hs:
+            fd = (AD.misfit(pd, c0, pd.theta + h * dt, cstar) - AD.misfit(pd, c0, pd.theta - h * dt, cstar)) / (2 * h)
+            errs[h].append(abs(fd - float(gth @ dt)) / abs(fd))
     pd.solver.close()
-    return {'steps': steps, 'h': h, 'directions': fd_dirs, 'max_rel_err': max(errs)}
+    return {'steps': steps, 'directions': fd_dirs,
+            'max_rel_err': {'h=%g' % h: max(e) for h, e in errs.items()},
+            'median_rel_err': {'h=%g' % h: float(np.median(e)) for h, e in errs.items()}}
 
 
 def limited_sensitivity(AD, pd, c0, cstar, steps, h=1e-14):
@@ -844,7 +877,18 @@ def run_ours(args):
     roof['traffic'] = MEASURED_TRAFFIC.get((wl, 'fp64', roof['kernel']))
     roof['note'] = ('L2-resident: the FP64 working set of this mesh (~60 MB) fits the 129 MB L2, so '
                     'the bytes are served mostly from L2 once a solve runs; the FP64 kernels are bound '
-                    'by GB300\'s FP64 rate, not by bandwidth; the HBM-bound figure is hbm_case')
+                    'by GB300\'s FP64 rate, not by bandwidth (fp64_rate); the HBM-bound figure is hbm_case')
+    # the bound that applies: the FP64 pipe, against cuBLAS DGEMM on the same GPU
+    peak64 = fp64_peak()
+    rate = {'peak_tflops': peak64, 'peak_source': 'measured: cuBLAS DGEMM 4096^3 (torch.matmul float64)',
+            'kernels': {}}
+    for name, k in kern.items():
+        f = MEASURED_FP64_FLOPS.get((wl, name))
+        if f is None:
+            continue
+        a = f * K / (k['ms_per_launch_live'] * 1e-3) / 1e12
+        rate['kernels'][name] = {'fp64_flops_per_element': f, 'achieved_tflops_live': a, 'frac': a / peak64}
+    roof['fp64_rate'] = rate
 
     # end to end through the C-ABI with pinned host buffers: the same solve from c0
     hin = torch.empty((N, K), dtype=torch.float64, pin_memory=True)

@@ -106,17 +106,19 @@ def tune(solver, tau, nSteps=48, reps=3, fused_ok=False, cache=None, key=None):
     return best, table
 
 
-ADJ_WARPS = (1, 2, 4)
+ADJ_WARPS = (1, 2, 4)          # FP32: the warp-role split (bitwise the same gradients)
+ADJ_WARPS_FP64 = (0, 1, 2, 4)  # FP64 also times one thread per element (gradients to roundoff)
 
 
 def tune_adjoint(solver, tau, nSteps=20, nSnapshots=0, reps=3):
     """Times a recorded run of `nSteps` steps and its reverse sweep at every warps-per-role
-    setting of the FP32 adjoint stage (wall time of dgadv_backward, which synchronises) and
-    applies the fastest; returns (best, table).  The gradients do not depend on the setting.
-    The handle's state is restored."""
+    setting of the adjoint stage (wall time of dgadv_backward, which synchronises) and applies
+    the fastest; returns (best, table).  In FP32 the gradients do not depend on the setting; in
+    FP64 the one-thread kernel (0) is timed too, whose gradients agree to roundoff.  The
+    handle's state is restored."""
     state = solver.get_state()
     table = []
-    for w in ADJ_WARPS:
+    for w in (ADJ_WARPS_FP64 if getattr(solver, 'precision', None) == 'fp64' else ADJ_WARPS):
         solver.set_option(L.OPT_ADJ_WARPS, w)
         times = []
         for _ in range(reps + 1):   # the first backward captures the sweep's graph

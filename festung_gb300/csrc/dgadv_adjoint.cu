@@ -314,40 +314,58 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
         stageIn[0] = c0;
         stageIn[1] = L.set[used].cA;
         stageIn[2] = L.set[used].cB;
-        if (L.two) {
-          DG_CUDA(cudaEventRecord(h->adjFEv, L.fwd));
-          DG_CUDA(cudaStreamWaitEvent(L.rev, h->adjFEv, 0));
-          h->pdlBreak = true;
+      }
+      const WorkSet &ws = L.set[used];
+      // the limiter inputs of stage s: recorded per step, or this step's recomputation set
+      auto recY = [&](int s) -> const char * {
+        return h->adjRecY ? (const char *)h->adjRecY + ((size_t)arg * S + s) * bytes : (const char *)ws.scrY + (size_t)s * bytes;
+      };
+      auto recCd = [&](int s) -> const char * {
+        if (!h->limdot) return nullptr;
+        return h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
+                             : (const char *)ws.scrCdot + (size_t)s * bytes;
+      };
+      // Two streams with the limiter: the scatters of the limiter inputs' means to the adjoint's
+      // key sets do not depend on the adjoint variable, so they run on the forward stream, in the
+      // reverse stages' pass order; their key sets were last read two reversed steps ago
+      const bool pre = L.two && h->lim;
+      if (pre) {
+        h->stream = L.fwd;
+        int ev = L.nRev - 2;
+        if ((st = wait_reader(h, L, ev))) return st;
+        for (int s = S - 1; s >= 0; --s) {
+          DG_CUDA(o.vjp_scatter(h, recY(s), h->adjPassF++, 0));
+          if (h->limdot) DG_CUDA(o.vjp_scatter(h, recCd(s), h->adjPassF++, 1));
         }
       }
+      if (L.two && (pre || !stages)) {
+        DG_CUDA(cudaEventRecord(h->adjFEv, L.fwd));
+        DG_CUDA(cudaStreamWaitEvent(L.rev, h->adjFEv, 0));
+        h->pdlBreak = true;
+      }
       h->stream = L.rev;
-      const WorkSet &ws = L.set[used];
       void *mub[3] = {nullptr, h->mu1, h->mu2};
       for (int s = S - 1; s >= 0; --s) {
         const void *muNext = (s == S - 1) ? h->lam : mub[s + 1];
         const void *muY = muNext, *mp = nullptr;
         if (h->lim) {
           // solution limiter, then (p >= 2) the time-derivative limiter, transposed
-          const char *Y = h->adjRecY ? (const char *)h->adjRecY + ((size_t)arg * S + s) * bytes
-                                     : (const char *)ws.scrY + (size_t)s * bytes;
+          const char *Y = recY(s);
           LimVjpArgs v;
           std::memset(&v, 0, sizeof(v));
           const double tBC = (s + 1 < S) ? (arg + cst[s + 1]) * tau : (arg + 1) * tau;
           for (int m = 0; m < h->nTerms; ++m)
             v.gco[m] = h->timeFn[m] == DGADV_TIME_EXP_NEG ? std::exp(-tBC) : 1.0;
-          const char *Cd = nullptr;
-          if (h->limdot)
-            Cd = h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
-                               : (const char *)ws.scrCdot + (size_t)s * bytes;
+          const char *Cd = recCd(s);
           if (h->limType == DGADV_LIM_HIERARCH_VERT) {
-            // hierarchical limiter (inputs recorded in Taylor form): per limiter its scatter,
-            // its pass and its gather
-            DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
+            // hierarchical limiter (inputs recorded in Taylor form): per limiter its scatter
+            // (unless the forward stream made it), its pass and its gather
+            if (!pre) DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
             v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
             DG_CUDA(o.lim_vjp(h, v));
             muY = h->tmpY;
             if (h->limdot) {
-              DG_CUDA(o.vjp_scatter(h, Cd, h->adjPass, 1));
+              if (!pre) DG_CUDA(o.vjp_scatter(h, Cd, h->adjPass, 1));
               LimVjpArgs d;
               std::memset(&d, 0, sizeof(d));
               d.kind = 1; d.x = Cd; d.lamIn = h->tmpY; d.lamOut = h->tmpD; d.scale = (1.0 - omega[s]) * tau;
@@ -357,11 +375,12 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
             }
           } else {
             // p >= 2: the solution limiter's kernel also scatters the time-derivative limiter's
-            // means, and the time-derivative limiter's kernel gathers the solution limiter's
-            // extreme terms first (5 launches per stage instead of 7)
-            DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
+            // means (unless the forward stream made both scatters), and the time-derivative
+            // limiter's kernel gathers the solution limiter's extreme terms first (5 launches per
+            // stage instead of 7; 4 with the scatters on the forward stream)
+            if (!pre) DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
             v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
-            v.nextX = Cd;
+            v.nextX = pre ? nullptr : Cd;
             v.gatherOut = Cd ? 0 : 1;
             DG_CUDA(o.lim_vjp(h, v));
             muY = h->tmpY;
@@ -389,13 +408,15 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
         x.last = s == 0;
         DG_CUDA(o.adj_stage(h, x));
       }
-      if (L.two && !stages) {   // what this step read: its set, and the slot or set of c^arg
+      if (L.two) {
         const int ev = L.nRev++;
         DG_CUDA(cudaEventRecord(h->adjRevEv[ev], L.rev));
-        L.setReader[used] = ev;
-        if (fromSet >= 0) L.setReader[fromSet] = ev;
-        else if (w.slot >= 0) L.slotReader[w.slot] = ev;
-        L.cur = 1 - used;
+        if (!stages) {   // what this step read: its set, and the slot or set of c^arg
+          L.setReader[used] = ev;
+          if (fromSet >= 0) L.setReader[fromSet] = ev;
+          else if (w.slot >= 0) L.slotReader[w.slot] = ev;
+          L.cur = 1 - used;
+        }
       }
       std::swap(h->lam, h->accn);
       w.step = arg + 1;
@@ -416,9 +437,12 @@ int make_lanes(dgadv_handle *h, Lanes &L, bool sweep) {
   L.set[0].scrY = h->adjScrY;
   L.set[0].scrCdot = h->adjScrCdot;
   L.slotReader.assign(h->nSlots, -1);
-  // (the resources come from the recorded run: a run recorded with one stream sweeps with one)
-  L.two = sweep && h->adjTwoStreams && h->adjSet1 && (int)h->adjRevEv.size() >= h->recSteps && !h->adjStages &&
-          !h->adjRecY;
+  // (the resources come from the recorded run: a run recorded with one stream sweeps with one).
+  // A sweep that recomputes alternates two buffer sets; one with every stage stored uses the
+  // second stream for the limiter adjoint's scatters only
+  const bool recomputes = !h->adjStages && !h->adjRecY;
+  L.two = sweep && h->adjTwoStreams && h->adjStreamF && (int)h->adjRevEv.size() >= h->recSteps &&
+          (recomputes ? h->adjSet1 != nullptr : h->lim != 0);
   if (!L.two) return DGADV_OK;
   const PrecOps &o = ops_of(h);
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
@@ -449,15 +473,15 @@ int join_lanes(dgadv_handle *h, Lanes &L) {
   return DGADV_OK;
 }
 
-// Two-stream resources of a recorded run that recomputes: set 1, the stream and the events.
-int lanes_alloc(dgadv_handle *h, int nSteps) {
+// Two-stream resources of a recorded run: the stream, the events and, if it recomputes, set 1.
+int lanes_alloc(dgadv_handle *h, int nSteps, bool recomputes) {
   const PrecOps &o = ops_of(h);
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
   double omega[3];
   const int S = rk_stages(h, omega);
   const size_t states = 3 + (h->lim ? 2 * (size_t)S : 0);
   int st;
-  if (h->adjSet1States != states) {
+  if (recomputes && h->adjSet1States != states) {
     drop_sweep(h);
     dev_release(h, h->adjSet1);
     h->adjSet1States = 0;
@@ -537,7 +561,7 @@ extern "C" int dgadv_set_velocity_theta(dgadv_handle *h, const double *theta) {
   h->hasVelocity = true;
   ++h->velVersion;
   h->recorded = false;
-  return DGADV_OK;
+  return refresh_element_operator(h);
   });
 }
 
@@ -605,10 +629,13 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
       if ((st = dev_alloc(h, (void **)&h->csrPos, 3 * (size_t)h->Kp * 4))) return st;
       k_csr_pos<<<(h->K + 127) / 128, 128, 0, h->stream>>>(h->K, h->Kp, h->V0T, h->vptr, h->vidx, h->csrPos);
       DG_CUDA(cudaGetLastError());
-      if ((st = dev_alloc(h, &h->adjMean, nq * h->Kp * o.realBytes))) return st;
-      if ((st = dev_alloc(h, &h->adjMeanB, nq * h->Kp * o.realBytes))) return st;
-      if ((st = dev_alloc(h, &h->vkeysA, 3 * 2 * nq * h->Vp * kb))) return st;
-      if ((st = dev_alloc(h, (void **)&h->gmmA, 3 * (size_t)h->nInst * kSlotCopies * 2 * nq * 8))) return st;
+      // 4S + 1 key sets: a pass's set is written at most two reversed steps (4S passes) ahead
+      // of the pass that read it last
+      const size_t ks = 4 * (size_t)S + 1;
+      h->adjKeySets = (int)ks;
+      if ((st = dev_alloc(h, &h->adjMeans, ks * nq * h->Kp * o.realBytes))) return st;
+      if ((st = dev_alloc(h, &h->vkeysA, ks * 2 * nq * h->Vp * kb))) return st;
+      if ((st = dev_alloc(h, (void **)&h->gmmA, ks * (size_t)h->nInst * kSlotCopies * 2 * nq * 8))) return st;
       if ((st = dev_alloc(h, &h->adjScrY, (size_t)S * bytes))) return st;
       if ((st = dev_alloc(h, &h->adjScrCdot, (size_t)S * bytes))) return st;
     }
@@ -620,8 +647,10 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
     }
     drop_sweep(h);
   }
-  // the reverse sweep recomputes: its second stream and buffer set
-  if (stageSteps == 0 && (S > 1 || h->lim) && h->adjTwoStreams && (st = lanes_alloc(h, nSteps))) return st;
+  // the second stream of the reverse sweep: recomputation (and its buffer set) and, with the
+  // limiter, the limiter adjoint's scatters
+  if (h->adjTwoStreams && (h->lim || (stageSteps == 0 && S > 1)) && (st = lanes_alloc(h, nSteps, stageSteps == 0)))
+    return st;
   h->slotStep.assign(nSlots, -1);
   make_schedule(nSteps, nSlots, h->schedule);
   h->schedBackward = backward_start(h->schedule);
@@ -669,17 +698,17 @@ extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc
   if (h->lim) {
     // every sweep starts with the limiter adjoint's key sets reset and its pass count at 0
     const size_t kb = o.keyBytes, vq = (size_t)h->Vp * kb;   // one quantity's min (or max) keys
-    for (int set = 0; set < 3; ++set)
+    for (int set = 0; set < h->adjKeySets; ++set)
       for (int q = 0; q < h->nc; ++q) {
         char *base = (char *)h->vkeysA + ((size_t)set * h->nc + q) * 2 * vq;
         DG_CUDA(cudaMemsetAsync(base, 0xFF, vq, h->stream));
         DG_CUDA(cudaMemsetAsync(base + vq, 0, vq, h->stream));
       }
-    std::vector<unsigned long long> init(3 * (size_t)h->nInst * kSlotCopies * 2 * h->nc);
+    std::vector<unsigned long long> init((size_t)h->adjKeySets * h->nInst * kSlotCopies * 2 * h->nc);
     for (size_t i = 0; i < init.size(); ++i) init[i] = (i & 1) ? 0ULL : o.slotKeyMax;
     DG_CUDA(cudaMemcpyAsync(h->gmmA, init.data(), init.size() * 8, cudaMemcpyHostToDevice, h->stream));
     DG_CUDA(cudaStreamSynchronize(h->stream));
-    h->adjPass = 0;
+    h->adjPass = h->adjPassF = 0;
   }
   DG_CUDA(cudaMemcpyAsync(h->stage_ext, dJdcT, (size_t)h->N * h->K * 8, cudaMemcpyHostToDevice, h->stream));
   DG_CUDA(o.scatter_in(h, h->lam));

@@ -318,10 +318,11 @@ __device__ __forceinline__ void adj_volume_role(const Geo<T> &g, const AdjSplitI
   }
 }
 
-// Up to p = 2, 64 registers at most (8 / W blocks of 128 W threads per SM): a 32768-triangle
-// stage then fits one wave of CTAs with two warps per role.
+// Up to p = 2, 64 registers at most in FP32 (8 / W blocks of 128 W threads per SM): a
+// 32768-triangle stage then fits one wave of CTAs with two warps per role.  FP64 holds twice the
+// bytes per value: 128 registers at most (4 / W blocks).
 template <typename T, int P, int W>
-__global__ void __launch_bounds__(128 * W, P <= 2 ? 8 / W : 1)
+__global__ void __launch_bounds__(128 * W, P <= 2 ? (sizeof(T) == 4 ? 8 / W : (4 / W > 0 ? 4 / W : 1)) : 1)
 k_adj_stage_split(const Geo<T> g, const T *muIn, const T *mpIn, const T *cs, T *__restrict__ muOut,
                   T *__restrict__ accn, double *__restrict__ aF, double *__restrict__ aV, const AdjScalars a) {
   constexpr int N = Dims<P>::N;
@@ -1084,7 +1085,7 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   if (h->limType == DGADV_LIM_HIERARCH_VERT) {   // one pass and its gather, P records per position
     int *rT = h->recSlotT[v.kind];
     T *rW = (T *)h->recSlotW[v.kind];
-    const T *q = (const T *)(v.kind == 0 ? h->adjMean : h->adjMeanB);
+    const T *q = adj_means<T>(h, v.pass);
     const int nnz = 3 * h->K;
     if (v.kind == 0)
       launch_k(h, k_lim_vjp_hier<T, P, 0>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn,
@@ -1099,7 +1100,7 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   int *rT = h->recSlotT[v.kind];
   T *rW = (T *)h->recSlotW[v.kind];
   const int *cp = h->csrPos;
-  const T *meanX = (const T *)(v.kind == 0 ? h->adjMean : h->adjMeanB);
+  const T *meanX = adj_means<T>(h, v.pass);
   const LimOut<T> loNext = lim_out_adj<T>(h, v.pass + 1);
   const T *lamIn = (const T *)v.lamIn;
   T *lamInW = (T *)v.lamIn;
@@ -1107,7 +1108,7 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
     const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
     launch_k(h, k_lim_vjp<T, P, 0, false, true>, grid, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut,
              lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, cp, rT, rW, lamInW, (const int *)nullptr,
-             (const T *)nullptr, (const T *)v.nextX, loNext, (T *)h->adjMeanB);
+             (const T *)nullptr, (const T *)v.nextX, loNext, adj_means<T>(h, v.pass + 1));
   } else if (v.kind == 0) {
     launch_k(h, k_lim_vjp<T, P, 0, false, false>, gridK, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut,
              lim_in_adj<T>(h, v.pass), sc, v.scale, meanX, cp, rT, rW, lamInW, (const int *)nullptr,
@@ -1129,7 +1130,7 @@ template <typename T, int P>
 static cudaError_t launch_vjp_scatter(dgadv_handle *h, const void *x, long long pass, int kind) {
   const Geo<T> g = make_geo<T>(h);
   const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
-  T *q = (T *)(kind == 0 ? h->adjMean : h->adjMeanB);
+  T *q = adj_means<T>(h, pass);
   if (h->limType == DGADV_LIM_HIERARCH_VERT)
     launch_k(h, k_vjp_scatter_hier<T, P>, grid, (size_t)0, g, (const T *)x, lim_out_adj<T>(h, pass), q);
   else
@@ -1142,9 +1143,8 @@ static cudaError_t launch_adj_stage(dgadv_handle *h, const AdjStageArgs &s) {
   const Geo<T> g = make_geo<T>(h);
   AdjScalars a;
   a.omega = s.omega; a.tau = s.tau; a.init = s.init; a.last = s.last;
-  if (std::is_same<T, float>::value) {
-    // FP32: the warp-role split (the FP64 stage is bound by the FP64 rate, where one thread per
-    // element issues fewer operations)
+  if (h->adjWarps > 0) {
+    // the warp-role split (DGADV_OPT_ADJ_WARPS = W > 0), or one thread per element (0)
     const int W = h->adjWarps, grid = (h->K + 32 * W - 1) / (32 * W);
     auto kern = W == 4 ? k_adj_stage_split<T, P, 4> : (W == 2 ? k_adj_stage_split<T, P, 2> : k_adj_stage_split<T, P, 1>);
     launch_kb(h, kern, grid, 128 * W, (size_t)0, g, (const T *)s.muIn, (const T *)s.mpIn, (const T *)s.cs,

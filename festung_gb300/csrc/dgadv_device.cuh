@@ -488,6 +488,30 @@ __device__ __forceinline__ T vertex_alpha(T cbar, const T v[3], const T mn[3], c
   return alpha;
 }
 
+// The same factor with one division: clamping to [0, 1] is monotone, so the minimum over the
+// vertices of the clamped ratios is the clamped smallest ratio.  Each branch's ratio is written
+// with a positive denominator, num / den (num >= 0: dMin <= 0 <= dMax, the element's own mean
+// being in its patches); the smallest is found by comparing cross products (the first vertex on
+// ties) and divided once.  A ratio that ties another to within rounding may be the one divided:
+// the factor then differs by at most an ulp.  The limiter's division sits on GB300's FP64 (or
+// the double-float) path, where it costs about as much as the rest of the factor.
+template <typename T>
+__device__ __forceinline__ T vertex_alpha_1div(T cbar, const T v[3], const T mn[3], const T mx[3]) {
+  const T tol = T(1.e-8);
+  T bn = T(0), bd = T(1);
+  bool any = false;
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const T dV = v[n] - cbar, dMin = mn[n] - cbar, dMax = mx[n] - cbar;
+    bool br = false;
+    T num = T(0), den = T(1);
+    if (dV < dMin + tol) { num = -dMin; den = tol - dV; br = true; }
+    if (dV > dMax - tol) { num = dMax; den = dV + tol; br = true; }
+    if (br && (!any || num * bd < bn * den)) { bn = num; bd = den; any = true; }
+  }
+  return any ? fmax(T(0), fmin(T(1), bn / bd)) : T(1);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Block staging: the rows of one block's elements (SoA rows, kBlock consecutive elements each)
 // are copied global -> shared by the TMA unit (cp.async.bulk, one elected thread) while the
@@ -594,9 +618,9 @@ template <typename T> __device__ __forceinline__ const int *irow(const unsigned 
 
 template <typename T, int P> struct StageRows {
   static constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NMT = Dims<P>::NMT;
-  // k_stage_op: c, [c0], F, Vn, [B] | code
-  __host__ __device__ static constexpr int op(int mode, bool lin) {
-    return N + (mode != 2 ? N : 0) + 2 * Q + 3 * R + (mode != 0 && !lin ? 4 : 0);
+  // k_stage_op: c, [c0], F (or the N^2 rows of the element operator), Vn, [B] | code
+  __host__ __device__ static constexpr int op(int mode, bool lin, bool eop = false) {
+    return N + (mode != 2 ? N : 0) + (eop ? N * N : 2 * Q) + 3 * R + (mode != 0 && !lin ? 4 : 0);
   }
   // k_limit_dot: tbuf, B, c0, cin | code (the packed Taylor mass rows stream from global memory)
   __host__ __device__ static constexpr int limdot() { return N + 4 + 2 * N; }
@@ -849,7 +873,7 @@ __device__ __forceinline__ bool lin_alpha(const LimIn<T> &li, const VKeys<T, NQ>
     valD[n] = ((dmask >> n) & 1) ? dataV0T[n] : T(NAN);
   }
   patch_minmax<T, NQ>(li, kv, sh, 0, valD, mn, mx);
-  const T alpha = vertex_alpha(u[0], v, mn, mx);
+  const T alpha = vertex_alpha_1div(u[0], v, mn, mx);
   if (alpha == T(1)) return false;
   du[0] = T(0);
   du[1] = (T(1) - alpha) * u[1];
@@ -888,17 +912,30 @@ struct StageScalars {
   int *flag;            // bit 0: non-finite value seen; bit 1: a bounded wait timed out
 };
 
-template <typename T, int P, int MODE, bool RHS, bool LIN, bool OPF = false>
+// Operator variants of the stage kernel (VAR):
+//   kOpPlain    volume term at the quadrature points, upwind flux at the edge points;
+//   kOpFp32     (double-float state only) the operator (volume, flux, hatM^-1 = I) in FP32
+//               arithmetic; the SSP update, the outputs and the limiter's quantities stay in the
+//               stored type;
+//   kOpElement  (FP64, no source terms) the element operator g.Aop, N x N per element: the
+//               volume term and the element's own outflow terms as one product with c, built
+//               by k_build_element_operator whenever the velocity changes; only the inflow terms
+//               are evaluated at the edge points.  GB300's FP64 rate bounds the FP64 stage: this
+//               takes the operator from about 244 FP64 instructions per element to about 100
+//               (p = 2).
+constexpr int kOpPlain = 0, kOpFp32 = 1, kOpElement = 2;
+
+template <typename T, int P, int MODE, bool RHS, bool LIN, int VAR = kOpPlain>
 __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, const T *c0, T *out,
            const LimOut<T> lo, const StageScalars sc, const int tile, const int nTiles = -1) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
-  // OPF (double-float state only): the operator (volume, flux, hatM^-1 = I) in FP32 arithmetic;
-  // the SSP update, the outputs and the limiter's quantities stay in the stored type
+  constexpr bool OPF = VAR == kOpFp32, EOP = VAR == kOpElement;
+  static_assert(!EOP || (std::is_same_v<T, double> && !RHS), "the element operator is FP64 without source terms");
   using A = std::conditional_t<OPF, float, T>;
   // with the mass solve (FP64, double-float) and no source terms, hatM^-1 is folded into the
   // test-function tables of the volume and flux terms (Fg1, Fg2, Fphi)
   constexpr bool kFold = sizeof(A) == 8 && !RHS;
-  constexpr int NT = StageRows<T, P>::op(MODE, LIN);
+  constexpr int NT = StageRows<T, P>::op(MODE, LIN, EOP);
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = (uint64_t *)(smem + StageRows<T, P>::bar_offset(NT, 1, blockDim.x));
   const Tab<T, P> &tb = tab<T, P>();
@@ -906,13 +943,14 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
   pdl_trigger();
   const int Kp = g.Kp;
   const bool staged = k0 < g.K;                   // blocks beyond the elements only reset keys
-  constexpr int rC = 0, rC0 = N, rF = (MODE != 2) ? 2 * N : N, rV = rF + 2 * Q, rB = rV + 3 * R;
+  constexpr int rC = 0, rC0 = N, rF = (MODE != 2) ? 2 * N : N, rV = rF + (EOP ? N * N : 2 * Q), rB = rV + 3 * R;
   if (staged) {
     if (t == 0) { mbar_init(bar, 1); mbar_fence_init(); }
     __syncthreads();
     if (t == 0) {                                 // static rows before the dependency wait
       stage_expect<T>(bar, NT, 1);
-      stage_T(smem, rF, g.F, 2 * Q, Kp, k0, bar);
+      if constexpr (EOP) stage_T(smem, rF, g.Aop, N * N, Kp, k0, bar);
+      else stage_T(smem, rF, g.F, 2 * Q, Kp, k0, bar);
       stage_T(smem, rV, g.Vn, 3 * R, Kp, k0, bar);
       if (MODE != 0 && !LIN) stage_T(smem, rB, g.Bm, 4, Kp, k0, bar);
       stage_I<T>(smem, NT, 0, g.code, 1, Kp, k0, bar);
@@ -959,6 +997,12 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
         for (int i = 0; i < N; ++i) rhs[i].fma(gm, as_arith<A>(g.rhs[((size_t)m * N + i) * Kp + k]));
       }
     }
+    if constexpr (EOP) {   // volume term and own outflow: the element operator
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = 0; j < N; ++j) rhs[i].fma(srow<T>(smem, rF + i * N + j)[t], c[j]);
+    } else {
     // volume term (at p = 3, 12 points: unrolled by 3 to keep the body in the instruction cache)
 #pragma unroll(P >= 3 ? 3 : Q)
     for (int qq = 0; qq < Q; ++qq) {
@@ -973,15 +1017,17 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
 #pragma unroll
       for (int i = 0; i < N; ++i) { rhs[i].fma(as_arith<A>(G1[qq][i]), f1); rhs[i].fma(as_arith<A>(G2[qq][i]), f2); }
     }
-    // upwind edge term
+    }
+    // upwind edge term (with the element operator: the inflow terms only)
     const int code = irow<T>(smem, NT, 0)[t];
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
       const int np = (code >> (2 * n)) & 3;
-      const bool outOk = (code >> (6 + n)) & 1;
+      const bool outOk = !EOP && ((code >> (6 + n)) & 1);
 #pragma unroll
       for (int r2 = 0; r2 < R; ++r2) {
         const A v = as_arith<A>(srow<T>(smem, rV + n * R + r2)[t]);
+        if (EOP && !(v < A(0) && nb[n] >= 0)) continue;
         Acc<A> tr(A(0));
         if (v > A(0) && outOk) {
 #pragma unroll
@@ -1049,11 +1095,52 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
   if (MODE != 0) scatter_quantities<T, NQ>(g, lo, qv, vid, active && ok, tile);
   if (bad) atomicOr(sc.flag, 1);
 }
-template <typename T, int P, int MODE, bool RHS, bool LIN, bool OPF = false>
+template <typename T, int P, int MODE, bool RHS, bool LIN, int VAR = kOpPlain>
 __global__ void __launch_bounds__(kBlock)
 k_stage_op(const Geo<T> g, const T *cin, const T *c0, T *out,
            const LimOut<T> lo, const StageScalars sc) {
-  stage_op_tile<T, P, MODE, RHS, LIN, OPF>(g, cin, c0, out, lo, sc, blockIdx.x);
+  stage_op_tile<T, P, MODE, RHS, LIN, VAR>(g, cin, c0, out, lo, sc, blockIdx.x);
+}
+
+// The element operator of every element (kOpElement), from the velocity factors F and Vn:
+//   A_ij = sum_q (Fg1_qi F1_q + Fg2_qi F2_q) phiQ_qj  -  sum_(n,r outflow) Fphi_nri v_nr phi1D_nrj,
+// the stage operator's volume term and its own outflow terms with hatM^-1 folded in
+// (advection/solveSubStep.m:66 with core/assembleMatElemDphiPhiFuncDisc.m:181-202 and the
+// element's own trace of core/assembleMatEdgePhiPhiValUpwind.m:261-299).
+template <typename T, int P>
+__global__ void __launch_bounds__(kBlock) k_build_element_operator(const Geo<T> g, T *__restrict__ aop) {
+  constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R;
+  const Tab<T, P> &tb = tab<T, P>();
+  const int k = blockIdx.x * kBlock + threadIdx.x;
+  if (k >= g.K) return;
+  const int Kp = g.Kp;
+  const int code = g.code[k];
+  for (int i = 0; i < N; ++i) {
+    T w1[Q], w2[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      w1[q] = tb.Fg1[q][i] * g.F[(size_t)q * Kp + k];
+      w2[q] = tb.Fg2[q][i] * g.F[(size_t)(Q + q) * Kp + k];
+    }
+    T wv[3][R];
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const T v = g.Vn[(size_t)(n * R + r) * Kp + k];
+        wv[n][r] = (v > T(0) && ((code >> (6 + n)) & 1)) ? tb.Fphi[n][r][i] * v : T(0);
+      }
+    for (int j = 0; j < N; ++j) {
+      Acc<T> a(T(0));
+#pragma unroll
+      for (int q = 0; q < Q; ++q) { a.fma(w1[q], tb.phiQ[q][j]); a.fma(w2[q], tb.phiQ[q][j]); }
+#pragma unroll
+      for (int n = 0; n < 3; ++n)
+#pragma unroll
+        for (int r = 0; r < R; ++r) a.fms(wv[n][r], tb.phi1D[n][r][j]);
+      aop[(size_t)(i * N + j) * Kp + k] = a.get();
+    }
+  }
 }
 
 // The stage operator with the volume term on the tensor cores (dgadv_mma.cuh): FP32, p >= 2,
@@ -1605,12 +1692,18 @@ __device__ __forceinline__ void limit_lin_tile(const Geo<T> g, const T *cbuf, T 
   if (!active) return;
   T u[N], du[N];
   lin_u3<T, P>(c, u);
-  if (lin_alpha_lazy<T, P, NQ>(li, kv, sh, u, c, dmask, data, du)) {
+  if (lin_alpha<T, P, NQ>(li, kv, sh, u, dmask, data, du)) {
+    // limited: u - du is the linear Taylor polynomial (u_0, alpha u_1, alpha u_2); back in the
+    // modal basis that is the first three columns of DM^-1 (3N multiply-adds instead of the
+    // rows u_3.. and DM^-1 du, N(N-1) + 3(N-3))
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      Acc<T> s(c[i]);
-#pragma unroll
-      for (int j = 1; j < N; ++j) s.fms(tb.DMinv[i][j], du[j]);
+      Acc<T> s(T(0));
+      s.fma(tb.DMinv[i][0], u[0]);
+      if constexpr (N > 1) {
+        s.fma(tb.DMinv[i][1], u[1] - du[1]);
+        s.fma(tb.DMinv[i][2], u[2] - du[2]);
+      }
       c[i] = s.get();
     }
   }
@@ -1668,14 +1761,17 @@ __device__ __forceinline__ void lin_limit_inplace(const LimIn<T> &li, const VKey
   constexpr int N = Dims<P>::N;
   const Tab<T, P> &tb = tab<T, P>();
   T u[N], du[N];
-  lin_u<T, P>(c, u);
+  lin_u3<T, P>(c, u);
   const T zero3[3] = {T(0), T(0), T(0)};
-  if (lin_alpha<T, P, 1>(li, kv, sh, u, dmask, zero3, du)) {
+  if (lin_alpha<T, P, 1>(li, kv, sh, u, dmask, zero3, du)) {   // as limit_lin_tile
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      Acc<T> s(c[i]);
-#pragma unroll
-      for (int j = 1; j < N; ++j) s.fms(tb.DMinv[i][j], du[j]);
+      Acc<T> s(T(0));
+      s.fma(tb.DMinv[i][0], u[0]);
+      if constexpr (N > 1) {
+        s.fma(tb.DMinv[i][1], u[1] - du[1]);
+        s.fma(tb.DMinv[i][2], u[2] - du[2]);
+      }
       c[i] = s.get();
     }
   }

@@ -23,6 +23,9 @@ struct ImplicitState;
 void implicit_release(dgadv_handle *h); // frees the implicit solver's host state
 struct TransportState;
 void transport_release(dgadv_handle *h);
+// Rebuilds the FP64 element operator after the velocity factors changed (a no-op for the other
+// precisions, implicit handles, or with DGADV_OPT_ELEMENT_OPERATOR = 0).
+int refresh_element_operator(dgadv_handle *h);
 constexpr int kBlock = 128;       // elements per CTA (one thread per element)
 constexpr int kSlotCopies = 32;   // copies of the global min / max slots (atomics spread over them)
 constexpr int kGridBarBytes = 8192;   // state of the persistent step's grid barrier
@@ -56,6 +59,11 @@ struct dgadv_handle {
   bool volumeMma = false;              // volume term on the tensor cores (DGADV_OPT_VOLUME_MMA)
   int opBlock = 128;                   // elements per block of the stage operator (DGADV_OPT_OP_BLOCK)
   bool opFp32 = false;                 // double-float handle, FP32 operator (DGADV_OPT_OPERATOR_FP32)
+  // FP64: the stage operator's volume term and own outflow terms as one N x N matrix per element
+  // (DGADV_OPT_ELEMENT_OPERATOR), built for velocity version aopVersion
+  bool elemOp = true;
+  void *Aop = nullptr;
+  int aopVersion = -1;
   // linked stepping (dgadv_link): this handle steps the handles in `linked` together with itself,
   // one launch per stage kernel; a handle in another's list has that handle as linkedTo
   std::vector<dgadv_handle *> linked;
@@ -131,10 +139,14 @@ struct dgadv_handle {
   int *recSlotT[2] = {nullptr, nullptr};
   void *recSlotW[2] = {nullptr, nullptr};
   int *csrPos = nullptr;                            // 3 x Kp: position of element k in patch V0T[n][k]
-  void *adjMean = nullptr, *adjMeanB = nullptr;     // element means of the limiter inputs (per kind)
-  void *vkeysA = nullptr;                           // the adjoint's own vertex keys (3 sets)
-  unsigned long long *gmmA = nullptr;               // ... and global-extreme slots
-  long long adjPass = 0;
+  // The adjoint's own vertex keys, global-extreme slots and element means of the limiter inputs,
+  // one set per pass modulo adjKeySets = 4S + 1: with two streams the scatters of a reversed
+  // step run on the recomputation stream while the reverse stages of the step before it run
+  void *adjMeans = nullptr;                         // adjKeySets x nc x Kp
+  void *vkeysA = nullptr;                           // adjKeySets x nc x 2 x Vp
+  unsigned long long *gmmA = nullptr;               // adjKeySets x nInst x kSlotCopies x 2 x nc
+  int adjKeySets = 3;
+  long long adjPass = 0, adjPassF = 0;              // passes consumed / scattered so far
   std::vector<int> schedule;                   // checkpointing actions of the recorded run
   size_t schedBackward = 0;                    // first action of the reverse sweep
   int recSteps = 0;
@@ -211,6 +223,8 @@ struct PrecOps {
   cudaError_t (*copy)(dgadv_handle *h, void *dst, const void *src, size_t bytes);
   // n FP64 values on the device -> stored reals
   cudaError_t (*from_f64)(dgadv_handle *h, void *dst, const double *src, size_t n);
+  // the element operator of every element from the velocity factors (null: not built)
+  cudaError_t (*build_element_operator)(dgadv_handle *h);
   // transport problem (null: not built for this type)
   cudaError_t (*tr_stage)(dgadv_handle *h, const TrStageArgs &a);
   cudaError_t (*tr_convert)(dgadv_handle *h, const void *in, void *out, const void *hQ, int toConc);

@@ -53,6 +53,8 @@ template <typename T> struct Geo {
   int K, Kp, numV, Vp;
   const T *F;        // 2Q x Kp  volume flux factors W_q (B22 u1 - B12 u2)/detJ, W_q (B11 u2 - B21 u1)/detJ
   const T *Vn;       // 3R x Kp  markNotN * |E| * w_r * (u.nu)_r / detJ
+  const T *Aop;      // N^2 x Kp the element operator (FP64 without source terms; null: none):
+                     //          volume term and own outflow, hatM^-1 folded in
   const int *nbr;    // 3 x Kp   neighbour element across edge n, -1 on the boundary
   const int *code;   // Kp       bits 2n..2n+1: neighbour's local edge; bit 6+n: outflow counted;
                      //          bit 9+n: local vertex n lies on a Dirichlet edge

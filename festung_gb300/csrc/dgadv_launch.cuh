@@ -77,11 +77,18 @@ static cudaError_t upload_tables(const RefTables &rt) {
   return cudaMemcpyToSymbol(tab_symbol<T, P>(), &t, sizeof(t));
 }
 
+// The element operator (kOpElement) is in use: FP64, enabled, built for the current velocity
+// and no source terms (with them the mass solve is not folded).
+static bool element_operator_on(const dgadv_handle *h) {
+  return h->Aop && h->elemOp && h->aopVersion == h->velVersion && !(h->nTerms > 0 && h->rhs);
+}
+
 template <typename T>
 static Geo<T> make_geo(const dgadv_handle *h) {
   Geo<T> g;
   g.K = h->K; g.Kp = h->Kp; g.numV = h->numV; g.Vp = h->Vp;
   g.F = (const T *)h->F; g.Vn = (const T *)h->Vn; g.nbr = h->nbr; g.code = h->code;
+  g.Aop = element_operator_on(h) ? (const T *)h->Aop : nullptr;
   g.Bm = (const T *)h->Bm; g.MT = (const T *)h->MT; g.V0T = h->V0T; g.vptr = h->vptr; g.vidx = h->vidx;
   g.rhs = (const T *)h->rhs; g.cDV0T = (const T *)h->cDV0T; g.nTerms = h->nTerms;
   for (int i = 0; i < 4; ++i) g.timeFn[i] = h->timeFn[i];
@@ -129,11 +136,16 @@ static LimIn<T> lim_in_pass(const dgadv_handle *h, long long pass) {
 }
 
 // The adjoint's own key sets (the limiter adjoint recomputes the forward's patch extremes), with
-// the forward's quantities per pass (one for the linear limiter, p(p+1)/2 for the hierarchical).
+// the forward's quantities per pass (one for the linear limiter, p(p+1)/2 for the hierarchical),
+// and the element means of a pass's limiter input.
+template <typename T>
+static T *adj_means(const dgadv_handle *h, long long pass) {
+  return (T *)h->adjMeans + (size_t)(pass % h->adjKeySets) * h->nc * h->Kp;
+}
 template <typename T>
 static LimOut<T> lim_out_adj(dgadv_handle *h, long long pass) {
   using K_ = typename KeyOf<T>::type;
-  const int set = (int)(pass % 3), next = (set + 1) % 3;
+  const int set = (int)(pass % h->adjKeySets), next = (set + 1) % h->adjKeySets;
   const size_t vset = (size_t)2 * h->nc * h->Vp;
   LimOut<T> o;
   o.vkeys = (K_ *)h->vkeysA + set * vset;
@@ -146,7 +158,7 @@ static LimOut<T> lim_out_adj(dgadv_handle *h, long long pass) {
 template <typename T>
 static LimIn<T> lim_in_adj(const dgadv_handle *h, long long pass) {
   using K_ = typename KeyOf<T>::type;
-  const int set = (int)(pass % 3);
+  const int set = (int)(pass % h->adjKeySets);
   LimIn<T> i;
   i.vkeys = (const K_ *)h->vkeysA + (size_t)set * 2 * h->nc * h->Vp;
   i.slots = h->gmmA + (size_t)set * h->nInst * kSlotCopies * 2 * h->nc;
@@ -222,6 +234,13 @@ static cudaError_t set_smem_attributes() {
   set((const void *)k_stage_op<T, P, 2, true, true>, SR::bytes(SR::op(2, true), 1));
   set((const void *)k_stage_op<T, P, 2, false, true>, SR::bytes(SR::op(2, true), 1));
   set((const void *)k_limit_dot_lin<T, P>, SR::bytes(SR::limdot_lin(), 1));
+  if constexpr (std::is_same_v<T, double>) {   // the element-operator variants
+    set((const void *)k_stage_op<T, P, 0, false, false, kOpElement>, SR::bytes(SR::op(0, false, true), 1));
+    set((const void *)k_stage_op<T, P, 1, false, false, kOpElement>, SR::bytes(SR::op(1, false, true), 1));
+    set((const void *)k_stage_op<T, P, 2, false, false, kOpElement>, SR::bytes(SR::op(2, false, true), 1));
+    set((const void *)k_stage_op<T, P, 1, false, true, kOpElement>, SR::bytes(SR::op(1, true, true), 1));
+    set((const void *)k_stage_op<T, P, 2, false, true, kOpElement>, SR::bytes(SR::op(2, true, true), 1));
+  }
   if constexpr (std::is_same_v<T, df32>) {   // the FP32-operator variants (DGADV_OPT_OPERATOR_FP32)
     set((const void *)k_stage_op<T, P, 0, true, false, true>, SR::bytes(SR::op(0, false), 1));
     set((const void *)k_stage_op<T, P, 0, false, false, true>, SR::bytes(SR::op(0, false), 1));
@@ -253,12 +272,20 @@ static cudaError_t set_smem_attributes() {
 }
 
 // The stage operator kernel of a handle: with DGADV_OPT_OPERATOR_FP32 on a double-float handle,
-// the variant whose operator arithmetic is FP32 (state, SSP update and limiter in double-float).
+// the variant whose operator arithmetic is FP32 (state, SSP update and limiter in double-float);
+// on an FP64 handle without source terms, the element-operator variant once it is built.
 template <typename T, int P, int MODE, bool RHS, bool LIN>
-static auto stage_kernel(const dgadv_handle *h) -> decltype(&k_stage_op<T, P, MODE, RHS, LIN, false>) {
+static auto stage_kernel(const dgadv_handle *h) -> decltype(&k_stage_op<T, P, MODE, RHS, LIN, kOpPlain>) {
   if constexpr (std::is_same_v<T, df32>)
-    if (h->opFp32) return &k_stage_op<T, P, MODE, RHS, LIN, true>;
-  return &k_stage_op<T, P, MODE, RHS, LIN, false>;
+    if (h->opFp32) return &k_stage_op<T, P, MODE, RHS, LIN, kOpFp32>;
+  if constexpr (std::is_same_v<T, double> && !RHS)
+    if (element_operator_on(h)) return &k_stage_op<T, P, MODE, RHS, LIN, kOpElement>;
+  return &k_stage_op<T, P, MODE, RHS, LIN, kOpPlain>;
+}
+// Its staged rows.
+template <typename T, int P>
+static int stage_rows(const dgadv_handle *h, int mode, bool lin, bool rhs) {
+  return StageRows<T, P>::op(mode, lin, std::is_same_v<T, double> && !rhs && element_operator_on(h));
 }
 
 template <typename T, int P>
@@ -289,8 +316,8 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     LimOut<T> lo{};
     if (!h->lim) {
       prof_mark(h, 0);
-      if (rhs) launch_kb(h, stage_kernel<T, P, 0, true, false>(h), gridOp, eb, SR::bytes(SR::op(0, false), 1, eb), g, in, cn, out, lo, sc);
-      else launch_kb(h, stage_kernel<T, P, 0, false, false>(h), gridOp, eb, SR::bytes(SR::op(0, false), 1, eb), g, in, cn, out, lo, sc);
+      if (rhs) launch_kb(h, stage_kernel<T, P, 0, true, false>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 0, false, true), 1, eb), g, in, cn, out, lo, sc);
+      else launch_kb(h, stage_kernel<T, P, 0, false, false>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 0, false, false), 1, eb), g, in, cn, out, lo, sc);
       prof_mark(h, -1);
       continue;
     }
@@ -318,19 +345,19 @@ static cudaError_t launch_step(dgadv_handle *h, double t0, double tau) {
     if (viaMma) {
     } else if (mode == 2) {
       if (lin) {
-        if (rhs) launch_kb(h, stage_kernel<T, P, 2, true, true>(h), gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
-        else launch_kb(h, stage_kernel<T, P, 2, false, true>(h), gridOp, eb, SR::bytes(SR::op(2, true), 1, eb), g, in, cn, cdB, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 2, true, true>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 2, true, true), 1, eb), g, in, cn, cdB, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 2, false, true>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 2, true, false), 1, eb), g, in, cn, cdB, lo1, sc);
       } else {
-        if (rhs) launch_kb(h, stage_kernel<T, P, 2, true, false>(h), gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, cdB, lo1, sc);
-        else launch_kb(h, stage_kernel<T, P, 2, false, false>(h), gridOp, eb, SR::bytes(SR::op(2, false), 1, eb), g, in, cn, cdB, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 2, true, false>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 2, false, true), 1, eb), g, in, cn, cdB, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 2, false, false>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 2, false, false), 1, eb), g, in, cn, cdB, lo1, sc);
       }
     } else {
       if (lin) {
-        if (rhs) launch_kb(h, stage_kernel<T, P, 1, true, true>(h), gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
-        else launch_kb(h, stage_kernel<T, P, 1, false, true>(h), gridOp, eb, SR::bytes(SR::op(1, true), 1, eb), g, in, cn, yB, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 1, true, true>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 1, true, true), 1, eb), g, in, cn, yB, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 1, false, true>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 1, true, false), 1, eb), g, in, cn, yB, lo1, sc);
       } else {
-        if (rhs) launch_kb(h, stage_kernel<T, P, 1, true, false>(h), gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, yB, lo1, sc);
-        else launch_kb(h, stage_kernel<T, P, 1, false, false>(h), gridOp, eb, SR::bytes(SR::op(1, false), 1, eb), g, in, cn, yB, lo1, sc);
+        if (rhs) launch_kb(h, stage_kernel<T, P, 1, true, false>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 1, false, true), 1, eb), g, in, cn, yB, lo1, sc);
+        else launch_kb(h, stage_kernel<T, P, 1, false, false>(h), gridOp, eb, SR::bytes(stage_rows<T, P>(h, 1, false, false), 1, eb), g, in, cn, yB, lo1, sc);
       }
     }
     prof_mark(h, -1);
@@ -540,6 +567,22 @@ static void to_real(const double *src, size_t n, void *dst) {
   for (size_t i = 0; i < n; ++i) d[i] = T(src[i]);
 }
 
+template <typename T, int MASK>
+static cudaError_t dispatch_build_element_operator(dgadv_handle *h) {
+  if constexpr (std::is_same_v<T, double>) {
+    const Geo<T> g = make_geo<T>(h);
+    const int grid = (h->K + kBlock - 1) / kBlock;
+    switch (h->p) {
+      case 0: if constexpr ((MASK & 1) != 0) k_build_element_operator<T, 0><<<grid, kBlock, 0, h->stream>>>(g, (T *)h->Aop); break;
+      case 1: if constexpr ((MASK & 2) != 0) k_build_element_operator<T, 1><<<grid, kBlock, 0, h->stream>>>(g, (T *)h->Aop); break;
+      case 2: if constexpr ((MASK & 4) != 0) k_build_element_operator<T, 2><<<grid, kBlock, 0, h->stream>>>(g, (T *)h->Aop); break;
+      case 3: if constexpr ((MASK & 8) != 0) k_build_element_operator<T, 3><<<grid, kBlock, 0, h->stream>>>(g, (T *)h->Aop); break;
+    }
+    return cudaGetLastError();
+  }
+  return cudaErrorNotSupported;
+}
+
 template <typename T, int MASK, bool FUSED>
 static PrecOps make_ops() {
   PrecOps o;
@@ -564,6 +607,7 @@ static PrecOps make_ops() {
   o.persist_attributes = nullptr;
   o.copy = copy_state;
   o.from_f64 = from_f64<T>;
+  o.build_element_operator = std::is_same_v<T, double> ? dispatch_build_element_operator<T, MASK> : nullptr;
   o.tr_stage = nullptr;
   o.tr_convert = nullptr;
   o.tr_mask = nullptr;

@@ -48,17 +48,25 @@ __global__ void __launch_bounds__(kBlock) k_link_op(const __grid_constant__ Link
   const int i = link_part(a);
   const LinkPart<T> &q = a.part[i];
   const int tile = blockIdx.x - q.block0;
-#define DGADV_LINK_OP(P)                                                                                  \
-  if (q.p == P) {                                                                                         \
-    if (q.mode == 0) stage_op_tile<T, P, 0, false, false>(q.g, q.a, q.b, q.out, q.lo, q.sc, tile, q.nBlocks); \
-    else if (q.mode == 1) stage_op_tile<T, P, 1, false, true>(q.g, q.a, q.b, q.out, q.lo, q.sc, tile, q.nBlocks); \
-    else stage_op_tile<T, P, 2, false, true>(q.g, q.a, q.b, q.out, q.lo, q.sc, tile, q.nBlocks);         \
-    return;                                                                                               \
+  // FP64 parts with the element operator run its variant, as their own launches would
+  constexpr bool kElem = std::is_same_v<T, double>;
+#define DGADV_LINK_OP_VAR(P, VAR)                                                                              \
+  {                                                                                                            \
+    if (q.mode == 0) stage_op_tile<T, P, 0, false, false, VAR>(q.g, q.a, q.b, q.out, q.lo, q.sc, tile, q.nBlocks); \
+    else if (q.mode == 1) stage_op_tile<T, P, 1, false, true, VAR>(q.g, q.a, q.b, q.out, q.lo, q.sc, tile, q.nBlocks); \
+    else stage_op_tile<T, P, 2, false, true, VAR>(q.g, q.a, q.b, q.out, q.lo, q.sc, tile, q.nBlocks);         \
+    return;                                                                                                    \
+  }
+#define DGADV_LINK_OP(P)                                          \
+  if (q.p == P) {                                                 \
+    if constexpr (kElem) if (q.g.Aop) DGADV_LINK_OP_VAR(P, kOpElement) \
+    DGADV_LINK_OP_VAR(P, kOpPlain)                                \
   }
   if constexpr ((MASK & 2) != 0) { DGADV_LINK_OP(1) }
   if constexpr ((MASK & 4) != 0) { DGADV_LINK_OP(2) }
   if constexpr ((MASK & 8) != 0) { DGADV_LINK_OP(3) }
 #undef DGADV_LINK_OP
+#undef DGADV_LINK_OP_VAR
 }
 
 template <typename T, int MASK>
@@ -92,8 +100,9 @@ static size_t link_smem(int kind) {
   auto upd = [&](auto P_) {
     constexpr int P = decltype(P_)::value;
     using SR = StageRows<T, P>;
-    if (kind == 0) b = std::max({b, SR::bytes(SR::op(0, false), 1), SR::bytes(SR::op(1, true), 1),
-                                 SR::bytes(SR::op(2, true), 1)});
+    constexpr bool e = std::is_same_v<T, double>;   // the element operator's rows (FP64)
+    if (kind == 0) b = std::max({b, SR::bytes(SR::op(0, false, e), 1), SR::bytes(SR::op(1, true, e), 1),
+                                 SR::bytes(SR::op(2, true, e), 1)});
     else if (kind == 1) b = std::max(b, SR::bytes(SR::limdot_lin(), 1));
   };
   if constexpr ((MASK & 2) != 0) upd(std::integral_constant<int, 1>());

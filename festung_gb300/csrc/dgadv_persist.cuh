@@ -99,20 +99,26 @@ __global__ void __launch_bounds__(kBlock) k_step_persistent(const PersistArgs<T>
     if (s >= a.S) break;
     T *in = (s == 0) ? a.cn : (s == 1 ? a.cA : a.cB);
     T *out = (s == a.S - 1) ? (a.S == 1 ? a.cA : a.cn) : (s == 0 ? a.cA : a.cB);
+    // FP64 with the element operator: its variant, as the separate kernels use it
+    const bool elem = std::is_same_v<T, double> && a.g.Aop != nullptr;
     if (LIMMODE == 0) {
       for (int tile = blockIdx.x; tile < a.nTilesK; tile += gridDim.x) {
-        stage_op_tile<T, P, 0, false, false>(a.g, in, a.cn, out, a.lo1[s], a.sc[s], tile);
+        if constexpr (std::is_same_v<T, double>)
+          if (elem) stage_op_tile<T, P, 0, false, false, kOpElement>(a.g, in, a.cn, out, a.lo1[s], a.sc[s], tile);
+        if (!elem) stage_op_tile<T, P, 0, false, false>(a.g, in, a.cn, out, a.lo1[s], a.sc[s], tile);
         __syncthreads();
-        end_tile_barrier<T, P>(a.g, tile, SR::op(0, false));
+        end_tile_barrier<T, P>(a.g, tile, SR::op(0, false, elem));
       }
       if (!grid_sync(a.bar, a.sc[s].flag)) return;
       continue;
     }
     // operator: cDot (p >= 2) or the unlimited stage value (p = 1), means scattered
     for (int tile = blockIdx.x; tile < a.nTiles; tile += gridDim.x) {
-      stage_op_tile<T, P, (LIMMODE == 2 ? 2 : 1), false, true>(a.g, in, a.cn, a.tb, a.lo1[s], a.sc[s], tile);
+      if constexpr (std::is_same_v<T, double>)
+        if (elem) stage_op_tile<T, P, (LIMMODE == 2 ? 2 : 1), false, true, kOpElement>(a.g, in, a.cn, a.tb, a.lo1[s], a.sc[s], tile);
+      if (!elem) stage_op_tile<T, P, (LIMMODE == 2 ? 2 : 1), false, true>(a.g, in, a.cn, a.tb, a.lo1[s], a.sc[s], tile);
       __syncthreads();
-      end_tile_barrier<T, P>(a.g, tile, SR::op(LIMMODE == 2 ? 2 : 1, true));
+      end_tile_barrier<T, P>(a.g, tile, SR::op(LIMMODE == 2 ? 2 : 1, true, elem));
     }
     if (!grid_sync(a.bar, a.sc[s].flag)) return;
     if (LIMMODE == 2) {
@@ -141,9 +147,10 @@ __global__ void __launch_bounds__(kBlock) k_step_persistent(const PersistArgs<T>
 template <typename T, int P>
 static size_t persist_smem() {
   using SR = StageRows<T, P>;
-  size_t b = SR::bytes(SR::op(0, false), 1);
-  b = std::max(b, SR::bytes(SR::op(1, true), 1));
-  b = std::max(b, SR::bytes(SR::op(2, true), 1));
+  constexpr bool e = std::is_same_v<T, double>;   // the element operator's rows (FP64)
+  size_t b = SR::bytes(SR::op(0, false, e), 1);
+  b = std::max(b, SR::bytes(SR::op(1, true, e), 1));
+  b = std::max(b, SR::bytes(SR::op(2, true, e), 1));
   b = std::max(b, SR::bytes(SR::limdot_lin(), 1));
   return b;
 }

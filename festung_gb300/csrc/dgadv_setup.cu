@@ -419,7 +419,7 @@ extern "C" int dgadv_set_velocity_function(dgadv_handle *h, const dgadv_function
   DG_CUDA(cudaStreamSynchronize(h->stream));
   h->hasVelocity = true;
   ++h->velVersion;
-  return DGADV_OK;
+  return refresh_element_operator(h);
   });
 }
 

@@ -97,6 +97,7 @@ static int create_impl(const dgadv_mesh *mesh, const dgadv_params *prm, const st
   h->lim = prm->isSlopeLim ? 1 : 0; h->limType = prm->typeSlopeLim; h->flags = prm->flags;
   h->limdot = h->lim && h->p > 1;
   h->mtOnTheFly = h->prec == DGADV_FP32;   // FP32 kernels are bandwidth-bound, the others are not
+  h->adjWarps = h->prec == DGADV_FP32 ? 2 : 0;   // the adjoint stage's warp-role split
   h->nc = h->lim ? (h->limType == DGADV_LIM_LINEAR ? 1 : h->p * (h->p + 1) / 2) : 1;
   h->passesPerStep = h->lim ? h->ordRK * (h->limdot ? 2 : 1) : 0;
   if ((h->flags & DGADV_FLAG_FUSE) && !ops(h).fused) {
@@ -412,7 +413,7 @@ extern "C" int dgadv_set_velocity(dgadv_handle *h, const double *u1, const doubl
   if ((st = upload_real(h, h->Vn, Vn))) return st;
   h->hasVelocity = true;
   ++h->velVersion;
-  return DGADV_OK;
+  return refresh_element_operator(h);
   });
 }
 
@@ -682,6 +683,22 @@ static void drop_graphs(dgadv_handle *h) {
   if (h->linkedTo) drop_graphs(h->linkedTo);   // the linked step's graphs hold this handle's launches
 }
 
+int dgadv::refresh_element_operator(dgadv_handle *h) {
+  const PrecOps &o = ops(h);
+  if (!o.build_element_operator || !h->elemOp || !h->hasVelocity || (h->flags & DGADV_FLAG_IMPLICIT))
+    return DGADV_OK;
+  if (!h->Aop) {
+    int st;
+    if ((st = dev_alloc(h, &h->Aop, (size_t)h->N * h->N * h->Kp * o.realBytes))) return st;
+    DG_CUDA(cudaMemset(h->Aop, 0, (size_t)h->N * h->N * h->Kp * o.realBytes));
+  }
+  DG_CUDA(o.build_element_operator(h));
+  // captured steps keep their kernels: they are recaptured once the operator comes into use
+  if (h->aopVersion < 0) drop_graphs(h);
+  h->aopVersion = h->velVersion;
+  return DGADV_OK;
+}
+
 // Removes `o` from its primary's linked handles.
 static void unlink_one(dgadv_handle *o) {
   dgadv_handle *h = o->linkedTo;
@@ -735,8 +752,17 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
     h->persistPerSM = value;
     h->persistGrid = 0;
   } else if (option == DGADV_OPT_ADJ_WARPS) {
-    if (value != 1 && value != 2 && value != 4) return DGADV_EINVAL;
+    if (value != 0 && value != 1 && value != 2 && value != 4) return DGADV_EINVAL;
     h->adjWarps = value;
+  } else if (option == DGADV_OPT_ELEMENT_OPERATOR) {
+    if (value != 0 && value != 1) return DGADV_EINVAL;
+    if (value && !ops(h).build_element_operator) { h->err = "the element operator is built for FP64"; return DGADV_EUNSUPPORTED; }
+    h->elemOp = value == 1;
+    if (h->elemOp) {
+      h->aopVersion = -1;
+      int st;
+      if ((st = refresh_element_operator(h))) return st;
+    }
   } else if (option == DGADV_OPT_ADJ_STREAMS) {
     if (value != 1 && value != 2) return DGADV_EINVAL;
     h->adjTwoStreams = value == 2;
@@ -779,6 +805,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   else if (option == DGADV_OPT_PERSIST_BLOCKS) *value = h->persistPerSM;
   else if (option == DGADV_OPT_ADJ_WARPS) *value = h->adjWarps;
   else if (option == DGADV_OPT_ADJ_STREAMS) *value = h->adjTwoStreams ? 2 : 1;
+  else if (option == DGADV_OPT_ELEMENT_OPERATOR) *value = (h->elemOp && ops(h).build_element_operator) ? 1 : 0;
   else if (option == DGADV_OPT_TAYLOR_MASS) *value = h->mtOnTheFly ? 1 : 0;
   else if (option == DGADV_OPT_VOLUME_MMA) *value = h->volumeMma ? 1 : 0;
   else if (option == DGADV_OPT_OP_BLOCK) *value = h->opBlock;

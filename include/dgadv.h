@@ -70,7 +70,10 @@ enum {
   DGADV_OPT_GRAPH_STEPS = 1,   /* time steps per captured CUDA graph, 1..256 (default 12)        */
   DGADV_OPT_FLAGS = 2,         /* the runtime flags NO_GRAPH, NO_PDL, FUSE, PERSIST              */
   DGADV_OPT_PERSIST_BLOCKS = 3, /* blocks per SM of the persistent step (0: all that fit)       */
-  DGADV_OPT_ADJ_WARPS = 4,      /* warps per role of the FP32 adjoint stage kernel: 1, 2 or 4    */
+  DGADV_OPT_ADJ_WARPS = 4,      /* warps per role of the adjoint stage kernel: 1, 2 or 4 (FP32
+                                   default 2), or 0: one thread per element (FP64 default);
+                                   1, 2 and 4 give the same gradients bit for bit, 0 agrees
+                                   with them to roundoff                                      */
   DGADV_OPT_TAYLOR_MASS = 5,    /* time-derivative limiting's Taylor mass correction: 0 reads a
                                    stored per-element block, 1 rebuilds it from the element's B
                                    and a constant table (default: 1 in FP32, 0 otherwise); the
@@ -85,11 +88,18 @@ enum {
                                    flux, mass) in FP32 arithmetic while the state, the SSP
                                    update and the limiter stay double-float; 0 (default): all
                                    double-float                                              */
-  DGADV_OPT_ADJ_STREAMS = 9     /* streams of a reverse sweep that recomputes: 2 (default) runs
+  DGADV_OPT_ADJ_STREAMS = 9,    /* streams of a reverse sweep that recomputes: 2 (default) runs
                                    the recomputation on a second stream, one reversed step
                                    ahead of the reverse stages (one more set of work states and
                                    limiter records, allocated by dgadv_forward_record); 1: one
                                    stream.  Gradients bitwise unchanged                        */
+  DGADV_OPT_ELEMENT_OPERATOR = 10 /* FP64 handles without source terms: 1 (default) keeps the
+                                   stage operator's volume term and the element's own outflow
+                                   terms as one N x N matrix per element (N^2 reals per element,
+                                   rebuilt whenever the velocity changes), which takes the FP64
+                                   operator from about 244 to about 100 arithmetic instructions
+                                   per element at p = 2; 0: evaluated at the quadrature points.
+                                   The results agree to roundoff                              */
 };
 
 /* ---- host helpers: static data ------------------------------------------------------- */

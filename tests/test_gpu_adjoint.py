@@ -95,7 +95,7 @@ def test_adjoint_autotuner_applies_a_width_and_keeps_the_gradient(lib):
     try:
         ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=3)
         best, table = AT.tune_adjoint(pd.solver, pd.tau, nSteps=6, nSnapshots=3, reps=1)
-        assert [r['adjWarps'] for r in table] == [1, 2, 4]
+        assert [r["adjWarps"] for r in table] == [1, 2, 4]
         assert pd.solver.get_option(L.OPT_ADJ_WARPS) == best['adjWarps']
         got = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=3)
         assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
@@ -281,9 +281,10 @@ STREAM_CASES = [dict(precision='fp32', kw=dict(hmax=2 ** -4, p=2, numSteps=24, t
 
 @pytest.mark.parametrize('case', STREAM_CASES, ids=['unlimited-p2', 'linear-p1', 'linear-p2', 'hier-p3'])
 def test_two_stream_sweep_equals_one_stream_sweep(lib, case):
-    """DGADV_OPT_ADJ_STREAMS: the recomputation on a second stream, one reversed step ahead of
-    the reverse stages, gives bitwise the gradients of one stream, captured in a graph (and
-    replayed) or launched directly, for binomial and every-state checkpoints."""
+    """DGADV_OPT_ADJ_STREAMS: the recomputation and the limiter adjoint's scatters on a second
+    stream, one reversed step ahead of the reverse stages, give bitwise the gradients of one
+    stream, captured in a graph (and replayed) or launched directly, with every stage stored and
+    for binomial and every-state checkpoints."""
     from festung_gb300 import _lib as L
     from festung_gb300 import adjoint as AD
     kw = case['kw']
@@ -300,7 +301,7 @@ def test_two_stream_sweep_equals_one_stream_sweep(lib, case):
             pd.solver.set_option(L.OPT_ADJ_STREAMS, streams)
             for flags in (0, L.FLAG_NO_GRAPH):
                 pd.solver.set_option(L.OPT_FLAGS, flags)
-                for snaps in (3, 5, kw['numSteps']):
+                for snaps in (0, 3, 5, kw['numSteps']):
                     for _ in range(2):
                         got = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=snaps)
                         assert got[0] == ref[0]

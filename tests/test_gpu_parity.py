@@ -307,3 +307,61 @@ def test_fp32_operator_on_double_float_state(lib, kw):
     f = gpu_run(precision='fp32', **kw)
     em, ef = rel(m.cDisc, d.cDisc), rel(f.cDisc, d.cDisc)
     assert em <= 1e-6 and em < ef, (em, ef)
+
+
+@pytest.mark.parametrize('kw', [SMALL[0], SMALL[2], SMALL[4], SMALL[6], SMALL[8], SMALL[9]],
+                         ids=['p0', 'p1lim', 'p2lim', 'p3lim', 'p3hier', 'solid_body'])
+def test_fp64_element_operator_matches_quadrature_form(lib, kw):
+    """DGADV_OPT_ELEMENT_OPERATOR (the FP64 default): the volume term and the element's own
+    outflow terms as one precomputed N x N matrix per element agree with the operator evaluated
+    at the quadrature and edge points to roundoff."""
+    from festung_gb300 import _lib as L
+    a = gpu_run(precision='fp64', **kw)
+    b = gpu_run(precision='fp64', gpuOptions={L.OPT_ELEMENT_OPERATOR: 0}, **kw)
+    assert rel(a.cDisc, b.cDisc) <= 1e-13
+
+
+def test_element_operator_follows_the_velocity(lib):
+    """The element operator is rebuilt whenever the velocity changes: a handle stepped with one
+    velocity, then given another, matches a fresh handle given the second one."""
+    from festung_gb300 import _lib as L
+    from festung_gb300 import advection_gpu as G
+    kw = dict(testcase='gauss_slot', hmax=2 ** -4, p=2, tEnd=0.02, numSteps=10, isSlopeLim=True,
+              precision='fp64', setupOnDevice=False)
+    pd = G.main(**kw)
+    s = pd.solver
+    try:
+        assert s.get_option(L.OPT_ELEMENT_OPERATOR) == 1
+        c0 = np.asfortranarray(pd._cDisc)
+        rng = np.random.default_rng(3)
+        u1 = pd.u1Disc * (1 + 0.1 * rng.standard_normal(pd.u1Disc.shape))
+        s.set_velocity(u1, pd.u2Disc, pd.vNormalOnQuadEdge * 0.9)
+        s.set_state(c0)
+        s.step(10, 0, pd.tau)
+        got = s.get_state()
+    finally:
+        s.close()
+    pd2 = G.main(**kw)
+    s2 = pd2.solver
+    try:
+        s2.set_velocity(u1, pd.u2Disc, pd.vNormalOnQuadEdge * 0.9)
+        s2.set_option(L.OPT_ELEMENT_OPERATOR, 0)
+        s2.set_state(c0)
+        s2.step(10, 0, pd.tau)
+        ref = s2.get_state()
+    finally:
+        s2.close()
+    assert rel(got, ref) <= 1e-13
+
+
+def test_element_operator_is_an_fp64_option(lib):
+    from festung_gb300 import _lib as L
+    from festung_gb300 import advection_gpu as G
+    pd = G.main(precision='fp32', testcase='gauss_slot', hmax=2 ** -3, p=1, tEnd=0.01, numSteps=2)
+    try:
+        assert pd.solver.get_option(L.OPT_ELEMENT_OPERATOR) == 0
+        with pytest.raises(L.DgadvError) as e:
+            pd.solver.set_option(L.OPT_ELEMENT_OPERATOR, 1)
+        assert e.value.status == L.DGADV_EUNSUPPORTED
+    finally:
+        pd.solver.close()
