@@ -266,7 +266,9 @@ def run_reference(args):
 # thread instructions, smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum of one
 # single-kernel ncu capture each, divided by the elements), keyed (workload, kernel):
 # profiles/stage_kernels_131k_fp64_full.md.
-MEASURED_FP64_FLOPS = {}
+MEASURED_FP64_FLOPS = {('gauss_slot_131k_p2', 'k_stage_op'): 197.1,
+                       ('gauss_slot_131k_p2', 'k_limit_dot'): 192.4,
+                       ('gauss_slot_131k_p2', 'k_limit'): 117.5}
 
 
 def fp64_peak(reps=5, n=4096):

@@ -325,17 +325,41 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
         return h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
                              : (const char *)ws.scrCdot + (size_t)s * bytes;
       };
-      // Two streams with the limiter: the scatters of the limiter inputs' means to the adjoint's
-      // key sets do not depend on the adjoint variable, so they run on the forward stream, in the
-      // reverse stages' pass order; their key sets were last read two reversed steps ago
-      const bool pre = L.two && h->lim;
+      // Two streams with the limiter and every stage stored: the scatters of the limiter inputs'
+      // means to the adjoint's key sets do not depend on the adjoint variable, so they run on the
+      // forward stream, in the reverse stages' pass order; their key sets were last read two
+      // reversed steps ago
+      // (with every stage stored; when the sweep recomputes, the recomputation already keeps
+      // the forward stream the busier one)
+      const bool pre = L.two && h->lim && stages;
+      // the linear limiter's choices too (k_lim_choice), leaving the reverse stream k_lim_apply
+      const bool preChoice = pre && h->limType == DGADV_LIM_LINEAR && h->adjChoice;
+      // time factors of the Dirichlet data at the solution limiter of stage s
+      auto gcoBC = [&](int s, double *gco) {
+        const double tBC = (s + 1 < S) ? (arg + cst[s + 1]) * tau : (arg + 1) * tau;
+        for (int m = 0; m < h->nTerms; ++m) gco[m] = h->timeFn[m] == DGADV_TIME_EXP_NEG ? std::exp(-tBC) : 1.0;
+      };
       if (pre) {
         h->stream = L.fwd;
         int ev = L.nRev - 2;
         if ((st = wait_reader(h, L, ev))) return st;
         for (int s = S - 1; s >= 0; --s) {
+          const long long p0 = h->adjPassF;
           DG_CUDA(o.vjp_scatter(h, recY(s), h->adjPassF++, 0));
           if (h->limdot) DG_CUDA(o.vjp_scatter(h, recCd(s), h->adjPassF++, 1));
+          if (preChoice) {
+            LimVjpArgs c;
+            std::memset(&c, 0, sizeof(c));
+            c.kind = 0; c.x = recY(s); c.pass = p0;
+            gcoBC(s, c.gco);
+            DG_CUDA(o.lim_choice(h, c));
+            if (h->limdot) {
+              LimVjpArgs d;
+              std::memset(&d, 0, sizeof(d));
+              d.kind = 1; d.x = recCd(s); d.pass = p0 + 1;
+              DG_CUDA(o.lim_choice(h, d));
+            }
+          }
         }
       }
       if (L.two && (pre || !stages)) {
@@ -353,9 +377,7 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
           const char *Y = recY(s);
           LimVjpArgs v;
           std::memset(&v, 0, sizeof(v));
-          const double tBC = (s + 1 < S) ? (arg + cst[s + 1]) * tau : (arg + 1) * tau;
-          for (int m = 0; m < h->nTerms; ++m)
-            v.gco[m] = h->timeFn[m] == DGADV_TIME_EXP_NEG ? std::exp(-tBC) : 1.0;
+          gcoBC(s, v.gco);
           const char *Cd = recCd(s);
           if (h->limType == DGADV_LIM_HIERARCH_VERT) {
             // hierarchical limiter (inputs recorded in Taylor form): per limiter its scatter
@@ -382,6 +404,7 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
             v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
             v.nextX = pre ? nullptr : Cd;
             v.gatherOut = Cd ? 0 : 1;
+            v.apply = preChoice ? 1 : 0;
             DG_CUDA(o.lim_vjp(h, v));
             muY = h->tmpY;
             if (h->limdot) {
@@ -391,6 +414,7 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
               d.pass = h->adjPass++;
               d.gatherIn = 1;
               d.gatherOut = 1;
+              d.apply = preChoice ? 1 : 0;
               DG_CUDA(o.lim_vjp(h, d));
               mp = h->tmpD;
             }
@@ -634,6 +658,9 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
       const size_t ks = 4 * (size_t)S + 1;
       h->adjKeySets = (int)ks;
       if ((st = dev_alloc(h, &h->adjMeans, ks * nq * h->Kp * o.realBytes))) return st;
+      if (h->limType == DGADV_LIM_LINEAR &&
+          (st = dev_alloc(h, &h->adjChoice, ks * h->Kp * (3 * o.realBytes + 2 * sizeof(int)))))
+        return st;
       if ((st = dev_alloc(h, &h->vkeysA, ks * 2 * nq * h->Vp * kb))) return st;
       if ((st = dev_alloc(h, (void **)&h->gmmA, ks * (size_t)h->nInst * kSlotCopies * 2 * nq * 8))) return st;
       if ((st = dev_alloc(h, &h->adjScrY, (size_t)S * bytes))) return st;

@@ -586,6 +586,236 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
   if (pos[ns] >= 0) slotW[pos[ns]] = w;
 }
 
+// k_lim_vjp in two halves, for the sweep on two streams.  The choices depend on the recorded
+// input x only, not on lambda: k_lim_choice makes them on the recomputation stream, one reversed
+// step ahead, and records per element the factor, the chosen vertex and branch, den, dm / den^2
+// and the element holding the extreme; k_lim_apply applies lambda on the reverse stream without
+// the keys, the shifts or the patch walk for the extreme.  Both compute k_lim_vjp's expressions
+// in its order, so the gradients are bitwise those of the one-kernel form.
+template <typename T> struct LimChoice {
+  T *alpha, *den, *q;   // per element (Kp)
+  int *tgt, *info;      // info: bits 0-1 the vertex, bit 2 limited, bit 3 the clip is active
+};
+
+// The record set of a pass's linear-limiter choices (k_lim_choice -> k_lim_apply).
+template <typename T>
+static LimChoice<T> lim_choice_rec(const dgadv_handle *h, long long pass) {
+  const size_t Kp = h->Kp;
+  char *b = (char *)h->adjChoice + (size_t)(pass % h->adjKeySets) * Kp * (3 * sizeof(T) + 2 * sizeof(int));
+  LimChoice<T> r;
+  r.alpha = (T *)b;
+  r.den = (T *)(b + Kp * sizeof(T));
+  r.q = (T *)(b + 2 * Kp * sizeof(T));
+  r.tgt = (int *)(b + 3 * Kp * sizeof(T));
+  r.info = (int *)(b + 3 * Kp * sizeof(T) + Kp * sizeof(int));
+  return r;
+}
+
+template <typename T, int P, int KIND>
+__global__ void __launch_bounds__(kBlock)
+k_lim_choice(const Geo<T> g, const T *x, const LimIn<T> li, const StageScalars sc,
+             const T *__restrict__ meanX, const LimChoice<T> rec) {
+  constexpr int N = Dims<P>::N;
+  __shared__ T sh[2];
+  const int k = blockIdx.x * kBlock + threadIdx.x;
+  pdl_trigger();
+  const bool active = k < g.K;
+  const int Kp = g.Kp;
+  int vid[3] = {0, 0, 0}, dmask = 0;
+  if (active) {
+    vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
+    if (KIND == 0) dmask = (g.code[k] >> 9) & 7;
+  }
+  T data[3] = {T(0), T(0), T(0)};
+  if (KIND == 0 && g.cDV0T && active)
+    for (int m = 0; m < g.nTerms; ++m) {
+      const T gm = T(sc.gco[m]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
+    }
+  int vp0[3] = {0, 0, 0}, vp1[3] = {0, 0, 0};
+  if (active) {
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      vp0[n] = g.vptr[vid[n]];
+      vp1[n] = g.vptr[vid[n] + 1];
+    }
+  }
+  pdl_wait();
+  const int tile = min((int)blockIdx.x, (g.K - 1) / kBlock);
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc, tile), li.nc, sh);
+  T xv[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) xv[i] = active ? x[(size_t)i * Kp + k] : T(0);
+  VKeys<T, 1> kv;
+  load_vkeys<T, 1>(g, li, vid, kv);
+  __syncthreads();
+  if (!active) return;
+  T u[N];
+  lin_u<T, P>(xv, u);
+  const T third = T(1) / T(3), two3 = T(2) / T(3), tol = T(1.e-8);
+  const T hx[3] = {-third, two3, -third}, hy[3] = {-third, -third, two3};
+  T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    v[n] = (u[0] * T(1) + u[1] * hx[n]) + u[2] * hy[n];
+    valD[n] = ((dmask >> n) & 1) ? data[n] : T(NAN);
+  }
+  patch_minmax<T, 1>(li, kv, sh, 0, valD, mn, mx);
+  T an[3];
+  int br[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const T dV = v[n] - u[0], dMin = mn[n] - u[0], dMax = mx[n] - u[0];
+    an[n] = T(1);
+    br[n] = 0;
+    if (dV < dMin + tol) { an[n] = fmax(T(0), fmin(T(1), dMin / (dV - tol))); br[n] = 1; }
+    if (dV > dMax - tol) { an[n] = fmax(T(0), fmin(T(1), dMax / (dV + tol))); br[n] = 2; }
+  }
+  const T alpha = fmin(fmin(an[0], an[1]), an[2]);
+  int ns = 0;
+  if (!(an[0] == alpha)) ns = (an[1] == alpha) ? 1 : 2;
+  int info = ns, tgt = -1;
+  T den = T(1), q = T(0);
+  if (alpha < T(1)) {
+    info |= 4;
+    const T dV = v[ns] - u[0];
+    const bool isPos = br[ns] == 2;
+    den = isPos ? dV + tol : dV - tol;
+    const T dm = (isPos ? mx[ns] : mn[ns]) - u[0];
+    const T raw = dm / den;
+    if (br[ns] != 0 && raw > T(0) && raw < T(1)) {
+      info |= 8;
+      q = dm / (den * den);
+      const T rawExt = vkey_inv<T>(kv.v[0][isPos ? 1 : 0][ns]);
+      const bool fromData = ((dmask >> ns) & 1) && (isPos ? !(data[ns] < rawExt) : !(data[ns] > rawExt));
+      if (!fromData) {
+        const auto key = kv.v[0][isPos ? 1 : 0][ns];
+        int best = -1, bestId = 0x7fffffff;
+        const int i0 = ns == 0 ? vp0[0] : (ns == 1 ? vp0[1] : vp0[2]);
+        const int i1 = ns == 0 ? vp1[0] : (ns == 1 ? vp1[1] : vp1[2]);
+#pragma unroll 4
+        for (int i = i0; i < i1; ++i) {
+          const int k2 = g.vidx[i];
+          if (vkey(meanX[k2]) == key && g.permv[k2] < bestId) { best = k2; bestId = g.permv[k2]; }
+        }
+        tgt = best;
+      }
+    }
+  }
+  rec.alpha[k] = alpha;
+  rec.den[k] = den;
+  rec.q[k] = q;
+  rec.tgt[k] = tgt;
+  rec.info[k] = info;
+}
+
+template <typename T, int P, int KIND, bool GIN>
+__global__ void __launch_bounds__(kBlock)
+k_lim_apply(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, const LimChoice<T> rec,
+            double scale, const int *__restrict__ csrPos, int *__restrict__ slotT, T *__restrict__ slotW,
+            T *lamInW, const int *__restrict__ pSlotT, const T *__restrict__ pSlotW) {
+  constexpr int N = Dims<P>::N;
+  const Tab<T, P> &tb = tab<T, P>();
+  const int k = blockIdx.x * kBlock + threadIdx.x;
+  pdl_trigger();
+  if (k >= g.K) return;
+  const int Kp = g.Kp;
+  const int pos[3] = {csrPos[k], csrPos[Kp + k], csrPos[2 * Kp + k]};
+  int vp0[3] = {0, 0, 0}, vp1[3] = {0, 0, 0};
+  if constexpr (GIN) {
+    const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      vp0[n] = g.vptr[vid[n]];
+      vp1[n] = g.vptr[vid[n] + 1];
+    }
+  }
+  constexpr bool kPrefetchMT = KIND == 1 && N <= 6;
+  T mtv[kPrefetchMT ? N * (N - 1) : 1];
+  if constexpr (kPrefetchMT) {
+#pragma unroll
+    for (int i = 0; i < N * (N - 1); ++i) mtv[i] = g.MT[(size_t)i * Kp + k];
+  }
+  pdl_wait();
+  const int info = rec.info[k];
+  const int ns = info & 3;
+  T lam[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) lam[i] = lamIn[(size_t)i * Kp + k];
+  if constexpr (GIN) {
+    T acc = T(0);
+    bool any = false;
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+#pragma unroll 4
+      for (int i = vp0[n]; i < vp1[n]; ++i)
+        if (pSlotT[i] == k) { acc = acc + pSlotW[i]; any = true; }
+    }
+    if (any) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        lam[j] = lam[j] + acc * tb.DM[0][j];
+        lamInW[(size_t)j * Kp + k] = lam[j];
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) lam[i] = T(scale) * lam[i];
+  T out[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) out[i] = lam[i];
+  int tgt = -1;
+  T w = T(0);
+  if (info & 4) {
+    const T third = T(1) / T(3), two3 = T(2) / T(3);
+    const T hx[3] = {-third, two3, -third}, hy[3] = {-third, -third, two3};
+    const T alpha = rec.alpha[k];
+    T xv[N], u[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) xv[i] = x[(size_t)i * Kp + k];
+    lin_u3<T, P>(xv, u);   // rows 0..2 as lin_u computes them
+    T r[N];
+    r[0] = T(0);
+#pragma unroll
+    for (int j = 1; j < N; ++j) {
+      Acc<T> a(T(0));
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        if (KIND == 0) a.fms(tb.DMinv[i][j], lam[i]);
+        else if constexpr (kPrefetchMT) a.fma(mtv[i * (N - 1) + (j - 1)], lam[i]);
+        else a.fma(g.MT[(size_t)(i * (N - 1) + (j - 1)) * Kp + k], lam[i]);
+      }
+      r[j] = a.get();
+    }
+    T gu[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) gu[j] = (j == 0) ? T(0) : (j <= 2 ? (T(1) - alpha) * r[j] : r[j]);
+    if (info & 8) {
+      const T den = rec.den[k], q = rec.q[k];
+      const T sa = -(r[1] * u[1] + r[2] * u[2]);
+      gu[0] = gu[0] - sa / den;
+      gu[1] = gu[1] - sa * q * hx[ns];
+      gu[2] = gu[2] - sa * q * hy[ns];
+      tgt = rec.tgt[k];
+      if (tgt >= 0) w = sa / den;
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      Acc<T> a(out[j]);
+#pragma unroll
+      for (int i = 0; i < N; ++i) a.fma(tb.DM[i][j], gu[i]);
+      out[j] = a.get();
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) lamOut[(size_t)i * Kp + k] = out[i];
+#pragma unroll
+  for (int n = 0; n < 3; ++n)
+    if (pos[n] >= 0) slotT[pos[n]] = n == ns ? tgt : -1;
+  if (pos[ns] >= 0) slotW[pos[ns]] = w;
+}
+
 // Gathers the recorded extreme terms: element e adds w DM0 for every element of its vertex
 // patches whose limiter factor took its extreme from e at that vertex (CSR order: deterministic).
 template <typename T, int P>
@@ -1100,6 +1330,23 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   int *rT = h->recSlotT[v.kind];
   T *rW = (T *)h->recSlotW[v.kind];
   const int *cp = h->csrPos;
+  if (v.apply) {   // the choices were recorded by lim_choice
+    const LimChoice<T> rec = lim_choice_rec<T>(h, v.pass);
+    const T *lamIn = (const T *)v.lamIn;
+    T *lamInW = (T *)v.lamIn;
+    if (v.kind == 0)
+      launch_k(h, k_lim_apply<T, P, 0, false>, gridK, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut, rec,
+               v.scale, cp, rT, rW, lamInW, (const int *)nullptr, (const T *)nullptr);
+    else if (v.gatherIn)
+      launch_k(h, k_lim_apply<T, P, 1, true>, gridK, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut, rec,
+               v.scale, cp, rT, rW, lamInW, (const int *)h->recSlotT[0], (const T *)h->recSlotW[0]);
+    else
+      launch_k(h, k_lim_apply<T, P, 1, false>, gridK, (size_t)0, g, (const T *)v.x, lamIn, (T *)v.lamOut, rec,
+               v.scale, cp, rT, rW, lamInW, (const int *)nullptr, (const T *)nullptr);
+    if (v.gatherOut)
+      launch_k(h, k_lim_vjp_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, (const int *)rT, (const T *)rW);
+    return cudaGetLastError();
+  }
   const T *meanX = adj_means<T>(h, v.pass);
   const LimOut<T> loNext = lim_out_adj<T>(h, v.pass + 1);
   const T *lamIn = (const T *)v.lamIn;
@@ -1122,6 +1369,24 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   }
   if (v.gatherOut)
     launch_k(h, k_lim_vjp_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, (const int *)rT, (const T *)rW);
+  return cudaGetLastError();
+}
+
+// The linear limiter's choices of one pass (k_lim_choice), from its keys and means.
+template <typename T, int P>
+static cudaError_t launch_lim_choice(dgadv_handle *h, const LimVjpArgs &v) {
+  const Geo<T> g = make_geo<T>(h);
+  const int gridK = (h->K + kBlock - 1) / kBlock;
+  StageScalars sc{};
+  sc.flag = h->flag;
+  for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = v.gco[m];
+  const LimChoice<T> rec = lim_choice_rec<T>(h, v.pass);
+  if (v.kind == 0)
+    launch_k(h, k_lim_choice<T, P, 0>, gridK, (size_t)0, g, (const T *)v.x, lim_in_adj<T>(h, v.pass), sc,
+             (const T *)adj_means<T>(h, v.pass), rec);
+  else
+    launch_k(h, k_lim_choice<T, P, 1>, gridK, (size_t)0, g, (const T *)v.x, lim_in_adj<T>(h, v.pass), sc,
+             (const T *)adj_means<T>(h, v.pass), rec);
   return cudaGetLastError();
 }
 
@@ -1187,12 +1452,23 @@ static cudaError_t dispatch_vjp_scatter(dgadv_handle *h, const void *x, long lon
   return cudaErrorNotSupported;
 }
 
+template <typename T, int MASK>
+static cudaError_t dispatch_lim_choice(dgadv_handle *h, const LimVjpArgs &v) {
+  switch (h->p) {
+    case 1: if constexpr ((MASK & 2) != 0) return launch_lim_choice<T, 1>(h, v); break;
+    case 2: if constexpr ((MASK & 4) != 0) return launch_lim_choice<T, 2>(h, v); break;
+    case 3: if constexpr ((MASK & 8) != 0) return launch_lim_choice<T, 3>(h, v); break;
+  }
+  return cudaErrorNotSupported;
+}
+
 // The operation table of a unit with the adjoint kernels added.
 template <typename T, int MASK>
 static PrecOps with_adjoint(PrecOps o) {
   o.adj_stage = dispatch_adj_stage<T, MASK>;
   o.lim_vjp = dispatch_lim_vjp<T, MASK>;
   o.vjp_scatter = dispatch_vjp_scatter<T, MASK>;
+  o.lim_choice = dispatch_lim_choice<T, MASK>;
   return o;
 }
 

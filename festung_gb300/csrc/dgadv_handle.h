@@ -143,6 +143,7 @@ struct dgadv_handle {
   // one set per pass modulo adjKeySets = 4S + 1: with two streams the scatters of a reversed
   // step run on the recomputation stream while the reverse stages of the step before it run
   void *adjMeans = nullptr;                         // adjKeySets x nc x Kp
+  void *adjChoice = nullptr;                        // adjKeySets x Kp x (3 reals + 2 ints)
   void *vkeysA = nullptr;                           // adjKeySets x nc x 2 x Vp
   unsigned long long *gmmA = nullptr;               // adjKeySets x nInst x kSlotCopies x 2 x nc
   int adjKeySets = 3;
@@ -183,6 +184,8 @@ struct LimVjpArgs {
   int gatherIn;        // time-derivative limiter: first add the solution limiter's extreme
                        // terms into lamIn (written back), in place of their own gather launch
   int gatherOut;       // launch the gather of this pass's extreme terms into lamOut
+  int apply;           // linear limiter: the choices of this pass were made by lim_choice (its
+                       // record set, pass mod adjKeySets); only lambda is applied here
 };
 
 // One stage of one transported species (dgadv_transport.cu): c h out from c h in, the
@@ -219,6 +222,9 @@ struct PrecOps {
   // the limiter input's quantities to the adjoint's key set of `pass` and stored per element
   // (kind 0: solution limiter, 1: time-derivative limiter)
   cudaError_t (*vjp_scatter)(dgadv_handle *h, const void *x, long long pass, int kind);
+  // linear limiter: the choices of pass a.pass for input a.x (kind, Dirichlet factors a.gco),
+  // recorded for a later lim_vjp with a.apply
+  cudaError_t (*lim_choice)(dgadv_handle *h, const LimVjpArgs &a);
   // device copy of a state-sized buffer (bytes a multiple of 16) ordered with dependent launches
   cudaError_t (*copy)(dgadv_handle *h, void *dst, const void *src, size_t bytes);
   // n FP64 values on the device -> stored reals

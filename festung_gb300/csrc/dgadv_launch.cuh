@@ -602,6 +602,7 @@ static PrecOps make_ops() {
   o.adj_stage = nullptr;
   o.lim_vjp = nullptr;
   o.vjp_scatter = nullptr;
+  o.lim_choice = nullptr;
   o.step_persist = nullptr;
   o.step_linked = nullptr;
   o.persist_attributes = nullptr;
