@@ -49,6 +49,15 @@ def signature(solver, tau, precision, extra=''):
     return '%s|K=%d|p=%d|%s|%s|tau=%g%s' % (name, solver.K, solver.p, precision, solver.limiter, tau, extra)
 
 
+def apply(solver, best):
+    """Sets a configuration returned by `tune` on `solver`."""
+    solver.set_option(L.OPT_FLAGS, best['flags'])
+    solver.set_option(L.OPT_GRAPH_STEPS, best['graphSteps'])
+    solver.set_option(L.OPT_OP_BLOCK, best.get('opBlock', 128))
+    if 'taylorMass' in best:
+        solver.set_option(L.OPT_TAYLOR_MASS, best['taylorMass'])
+
+
 def tune(solver, tau, nSteps=48, reps=3, fused_ok=False, cache=None, key=None):
     """Times every candidate on `solver` and applies the fastest; returns (best, table).
     `cache`: optional JSON path; with `key`, a stored choice is applied without timing."""
@@ -57,11 +66,7 @@ def tune(solver, tau, nSteps=48, reps=3, fused_ok=False, cache=None, key=None):
             stored = json.load(f)
         if key in stored:
             best = stored[key]['best']
-            solver.set_option(L.OPT_FLAGS, best['flags'])
-            solver.set_option(L.OPT_GRAPH_STEPS, best['graphSteps'])
-            solver.set_option(L.OPT_OP_BLOCK, best.get('opBlock', 128))
-            if 'taylorMass' in best:
-                solver.set_option(L.OPT_TAYLOR_MASS, best['taylorMass'])
+            apply(solver, best)
             return best, stored[key]['table']
     state = solver.get_state()
     table = []

@@ -495,10 +495,12 @@ __device__ __forceinline__ T vertex_alpha(T cbar, const T v[3], const T mn[3], c
 // ties) and divided once.  A ratio that ties another to within rounding may be the one divided:
 // the factor then differs by at most an ulp.  The limiter's division sits on GB300's FP64 (or
 // the double-float) path, where it costs about as much as the rest of the factor.
+// A patch extreme that the global shift rounded past the element's own value can leave a
+// branch's denominator at or below zero; such a ratio is divided on its own, as vertex_alpha does.
 template <typename T>
 __device__ __forceinline__ T vertex_alpha_1div(T cbar, const T v[3], const T mn[3], const T mx[3]) {
   const T tol = T(1.e-8);
-  T bn = T(0), bd = T(1);
+  T bn = T(0), bd = T(1), extra = T(1);
   bool any = false;
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
@@ -507,9 +509,15 @@ __device__ __forceinline__ T vertex_alpha_1div(T cbar, const T v[3], const T mn[
     T num = T(0), den = T(1);
     if (dV < dMin + tol) { num = -dMin; den = tol - dV; br = true; }
     if (dV > dMax - tol) { num = dMax; den = dV + tol; br = true; }
-    if (br && (!any || num * bd < bn * den)) { bn = num; bd = den; any = true; }
+    if (br) {
+      if (den > T(0)) {
+        if (!any || num * bd < bn * den) { bn = num; bd = den; any = true; }
+      } else {
+        extra = fmin(extra, fmax(T(0), fmin(T(1), num / den)));
+      }
+    }
   }
-  return any ? fmax(T(0), fmin(T(1), bn / bd)) : T(1);
+  return fmin(any ? fmax(T(0), fmin(T(1), bn / bd)) : T(1), extra);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -732,7 +740,7 @@ __device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, 
       valD[n] = ((dmask >> n) & 1) ? dataV0T[n] : nan_;
     }
     patch_minmax<T, NQ>(li, kv, sh, 0, valD, mn, mx);
-    const T alpha = vertex_alpha(cT[0], v, mn, mx);
+    const T alpha = vertex_alpha_1div(cT[0], v, mn, mx);
     cT[1] *= alpha; cT[2] *= alpha;
     const T keep = (alpha == T(1)) ? T(1) : T(0);
 #pragma unroll
@@ -764,7 +772,7 @@ __device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, 
           valD[n] = ((dmask >> n) & 1) ? (ord > 1 ? v[n] : dataV0T[n]) : nan_;
         }
         patch_minmax<T, NQ>(li, kv, sh, s, valD, mn, mx);
-        aOrd = fmin(aOrd, vertex_alpha(cT[i0], v, mn, mx));
+        aOrd = fmin(aOrd, vertex_alpha_1div(cT[i0], v, mn, mx));
         ++s;
       }
 #pragma unroll
@@ -789,7 +797,7 @@ __device__ __forceinline__ void limit_taylor(const LimIn<T> &li, const VKeys<T, 
           valD[n] = ((dmask >> n) & 1) ? (ord > 1 ? v[n] : dataV0T[n]) : nan_;
         }
         patch_minmax<T, NQ>(li, kv, sh, s, valD, mn, mx);
-        aOrd = fmin(aOrd, vertex_alpha(orig[i0], v, mn, mx));
+        aOrd = fmin(aOrd, vertex_alpha_1div(orig[i0], v, mn, mx));
         ++s;
       }
       alpha = fmax(alpha, aOrd);

@@ -175,6 +175,8 @@ class Ensemble:
             chosen = 'linked' if tLinked <= tSep else 'separate'
             if chosen == 'linked':
                 self._link()
+                # the primary took its own group's configuration while the groups were tuned
+                AT.apply(self.primary, out['linked'])
             out['schedule'] = dict(chosen=chosen, ms_per_step={'linked': 1e3 * tLinked, 'separate': 1e3 * tSep})
             return out
         return self._tune_groups(nSteps, reps, cache)
