@@ -815,7 +815,7 @@ def side_path(wl, precision, device, c0, flush, reps, options=None):
     for o, v in (options or {}).items():
         s.set_option(o, v)
     from festung_gb300 import autotune as AT
-    tuned = AT.tune(s, pd.tau, nSteps=24, reps=2, fused_ok=(pd.typeSlopeLim == 'linear' and precision != 'df32'))[0]
+    tuned = AT.tune(s, pd.tau, nSteps=48, reps=3, fused_ok=(pd.typeSlopeLim == "linear" and precision != "df32"))[0]
     s.step(pd.numSteps, 0, pd.tau)             # warm-up solve (graph capture, first launches)
     s.sync()
     ts, c = time_solves(s, c0, pd.numSteps, pd.tau, reps, flush)
@@ -853,7 +853,7 @@ def run_ours(args):
     flush = torch.empty(512 * 2 ** 20, dtype=torch.uint8, device='cuda')
     # launch configuration from the autotuner (graph length, dependent launch, pipeline)
     from festung_gb300 import autotune as AT
-    tuned = AT.tune(s, pd.tau, nSteps=24, reps=2, fused_ok=(pd.typeSlopeLim == 'linear'))[0] \
+    tuned = AT.tune(s, pd.tau, nSteps=48, reps=3, fused_ok=(pd.typeSlopeLim == "linear"))[0] \
         if not args.no_tune else None
 
     # every solve, warm-up and timed, runs the configured 500 steps from c0 at t = 0

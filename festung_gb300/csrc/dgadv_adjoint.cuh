@@ -507,19 +507,21 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
     valD[n] = ((dmask >> n) & 1) ? data[n] : T(NAN);
   }
   patch_minmax<T, 1>(li, kv, sh, 0, valD, mn, mx);
-  T an[3];
-  int br[3];
+  // the first vertex whose clamped ratio is the smallest (one division, for that vertex)
+  RatioWin<T> rw;
+  int ns = 0, brW = 0;
+  T dmW = T(0), denW = T(1);
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
     const T dV = v[n] - u[0], dMin = mn[n] - u[0], dMax = mx[n] - u[0];
-    an[n] = T(1);
-    br[n] = 0;
-    if (dV < dMin + tol) { an[n] = fmax(T(0), fmin(T(1), dMin / (dV - tol))); br[n] = 1; }
-    if (dV > dMax - tol) { an[n] = fmax(T(0), fmin(T(1), dMax / (dV + tol))); br[n] = 2; }
+    int br = 0;
+    T dm = T(0), dn = T(1);
+    if (dV < dMin + tol) { dm = dMin; dn = dV - tol; br = 1; }
+    if (dV > dMax - tol) { dm = dMax; dn = dV + tol; br = 2; }
+    if (br != 0 && rw.offer(dm, dn)) { ns = n; brW = br; dmW = dm; denW = dn; }
   }
-  const T alpha = fmin(fmin(an[0], an[1]), an[2]);
-  int ns = 0;
-  if (!(an[0] == alpha)) ns = (an[1] == alpha) ? 1 : 2;
+  const T rawW = dmW / denW;
+  const T alpha = brW != 0 ? fmax(T(0), fmin(T(1), rawW)) : T(1);
   T out[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) out[i] = lam[i];
@@ -542,12 +544,9 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
     T gu[N];   // dJ/du
 #pragma unroll
     for (int j = 0; j < N; ++j) gu[j] = (j == 0) ? T(0) : (j <= 2 ? (T(1) - alpha) * r[j] : r[j]);
-    const T dV = v[ns] - u[0];
-    const bool isPos = br[ns] == 2;
-    const T den = isPos ? dV + tol : dV - tol;
-    const T dm = (isPos ? mx[ns] : mn[ns]) - u[0];
-    const T raw = dm / den;
-    if (br[ns] != 0 && raw > T(0) && raw < T(1)) {
+    const bool isPos = brW == 2;
+    const T den = denW, dm = dmW, raw = rawW;
+    if (brW != 0 && raw > T(0) && raw < T(1)) {
       const T sa = -(r[1] * u[1] + r[2] * u[2]);                  // dJ / d alpha
       const T q = dm / (den * den);
       gu[0] = gu[0] - sa / den;                                   // d dm / d u0 = -1
@@ -662,29 +661,29 @@ k_lim_choice(const Geo<T> g, const T *x, const LimIn<T> li, const StageScalars s
     valD[n] = ((dmask >> n) & 1) ? data[n] : T(NAN);
   }
   patch_minmax<T, 1>(li, kv, sh, 0, valD, mn, mx);
-  T an[3];
-  int br[3];
+  // the first vertex whose clamped ratio is the smallest (one division, for that vertex)
+  RatioWin<T> rw;
+  int ns = 0, brW = 0;
+  T dmW = T(0), denW = T(1);
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
     const T dV = v[n] - u[0], dMin = mn[n] - u[0], dMax = mx[n] - u[0];
-    an[n] = T(1);
-    br[n] = 0;
-    if (dV < dMin + tol) { an[n] = fmax(T(0), fmin(T(1), dMin / (dV - tol))); br[n] = 1; }
-    if (dV > dMax - tol) { an[n] = fmax(T(0), fmin(T(1), dMax / (dV + tol))); br[n] = 2; }
+    int br = 0;
+    T dm = T(0), dn = T(1);
+    if (dV < dMin + tol) { dm = dMin; dn = dV - tol; br = 1; }
+    if (dV > dMax - tol) { dm = dMax; dn = dV + tol; br = 2; }
+    if (br != 0 && rw.offer(dm, dn)) { ns = n; brW = br; dmW = dm; denW = dn; }
   }
-  const T alpha = fmin(fmin(an[0], an[1]), an[2]);
-  int ns = 0;
-  if (!(an[0] == alpha)) ns = (an[1] == alpha) ? 1 : 2;
+  const T rawW = dmW / denW;
+  const T alpha = brW != 0 ? fmax(T(0), fmin(T(1), rawW)) : T(1);
   int info = ns, tgt = -1;
   T den = T(1), q = T(0);
   if (alpha < T(1)) {
     info |= 4;
-    const T dV = v[ns] - u[0];
-    const bool isPos = br[ns] == 2;
-    den = isPos ? dV + tol : dV - tol;
-    const T dm = (isPos ? mx[ns] : mn[ns]) - u[0];
-    const T raw = dm / den;
-    if (br[ns] != 0 && raw > T(0) && raw < T(1)) {
+    const bool isPos = brW == 2;
+    den = denW;
+    const T dm = dmW, raw = rawW;
+    if (brW != 0 && raw > T(0) && raw < T(1)) {
       info |= 8;
       q = dm / (den * den);
       const T rawExt = vkey_inv<T>(kv.v[0][isPos ? 1 : 0][ns]);
@@ -875,6 +874,8 @@ template <typename T, int P> struct HierWin {
   int i0, i1, i2, n, s;
   int src;       // extreme: 0 another element (recorded), 1 the element's own vertex value, 2 data
   int tgt;       // element holding the extreme (src 0)
+  int vtx;       // the winning vertex (a global vertex id) and its extreme's key
+  typename KeyOf<T>::type key;
 };
 
 // S (modal-derivative u -> Taylor) blocks: S[d][m][j] = idX^d times deriv_block of A = B^-1.
@@ -1141,8 +1142,9 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
   int s = 0;
 #pragma unroll
   for (int ord = P; ord >= 1; --ord) {
-    T aOrd = T(1);
+    RatioWin<T> rw;   // the order's winner, compared without dividing
     win[ord].act = 0; win[ord].src = 2; win[ord].tgt = -1; win[ord].n = 0; win[ord].s = 0;
+    win[ord].vtx = 0; win[ord].key = 0;
     win[ord].i0 = win[ord].i1 = win[ord].i2 = 0;
     win[ord].raw = win[ord].den = win[ord].dm = T(0);
 #pragma unroll
@@ -1159,16 +1161,13 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
       for (int n = 0; n < 3; ++n) {
         const T cbar = xv[i0];
         const T dV = v[n] - cbar, dMin = mn[n] - cbar, dMax = mx[n] - cbar;
-        T a = T(1), den = T(0), dm = T(0);
+        T den = T(0), dm = T(0);
         int br = 0;
-        if (dV < dMin + tol) { den = dV - tol; dm = dMin; a = fmax(T(0), fmin(T(1), dm / den)); br = 1; }
-        if (dV > dMax - tol) { den = dV + tol; dm = dMax; a = fmax(T(0), fmin(T(1), dm / den)); br = 2; }
-        if (a < aOrd) {   // the first (sub-limiter, vertex) reaching the order's minimum
-          aOrd = a;
+        if (dV < dMin + tol) { den = dV - tol; dm = dMin; br = 1; }
+        if (dV > dMax - tol) { den = dV + tol; dm = dMax; br = 2; }
+        if (br != 0 && rw.offer(dm, den)) {   // the first (sub-limiter, vertex) reaching the order's minimum
           HierWin<T, P> &w = win[ord];
-          const T raw = dm / den;
-          w.raw = raw; w.den = den; w.dm = dm;
-          w.act = br != 0 && raw > T(0) && raw < T(1);
+          w.den = den; w.dm = dm;
           w.i0 = i0; w.i1 = i1; w.i2 = i2; w.n = n; w.s = s;
           // the extreme's source: the Dirichlet value (which wins a tie) or the patch element
           const bool isPos = br == 2;
@@ -1177,20 +1176,33 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
           const bool fromD = hasD && (isPos ? !(valD[n] < rawExt) : !(valD[n] > rawExt));
           w.src = fromD ? (ord > 1 ? 1 : 2) : 0;
           w.tgt = -1;
-          if (!fromD && w.act) {
-            const auto key = kv.v[s][isPos ? 1 : 0][n];
-            int best = -1, bestId = 0x7fffffff;
-            const int v0 = vid[n];
-            const int e0 = g.vptr[v0], e1 = g.vptr[v0 + 1];
-            for (int e = e0; e < e1; ++e) {
-              const int k2 = g.vidx[e];
-              if (vkey(qStore[(size_t)s * Kp + k2]) == key && g.permv[k2] < bestId) { best = k2; bestId = g.permv[k2]; }
-            }
-            w.tgt = best;
-          }
+          w.vtx = vid[n];
+          w.key = kv.v[s][isPos ? 1 : 0][n];
         }
       }
       ++s;
+    }
+    // the winner's factor (one division) and the element holding its extreme, found once the
+    // winner is known
+    T aOrd = T(1);
+    {
+      HierWin<T, P> &w = win[ord];
+      if (rw.cls < 2) {
+        const T raw = w.dm / w.den;
+        w.raw = raw;
+        w.act = raw > T(0) && raw < T(1);
+        aOrd = fmax(T(0), fmin(T(1), raw));
+      }
+      if (w.src == 0 && w.act) {
+        const auto key = w.key;
+        int best = -1, bestId = 0x7fffffff;
+        const int e0 = g.vptr[w.vtx], e1 = g.vptr[w.vtx + 1];
+        for (int e = e0; e < e1; ++e) {
+          const int k2 = g.vidx[e];
+          if (vkey(qStore[(size_t)w.s * Kp + k2]) == key && g.permv[k2] < bestId) { best = k2; bestId = g.permv[k2]; }
+        }
+        w.tgt = best;
+      }
     }
     if (ord == P || aOrd > alphaRun) runOrd = ord;   // the order whose alpha is the running max
     alphaRun = fmax(alphaRun, aOrd);

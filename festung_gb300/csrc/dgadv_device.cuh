@@ -520,6 +520,28 @@ __device__ __forceinline__ T vertex_alpha_1div(T cbar, const T v[3], const T mn[
   return fmin(any ? fmax(T(0), fmin(T(1), bn / bd)) : T(1), extra);
 }
 
+// The adjoint's side of the same choice: which (sub-limiter, vertex) gives the factor, found
+// without dividing.  A branch's ratio dm / den is compared in its positive-denominator form by
+// cross products, with a class for the clamped values (0: ratio <= 0, 1: inside (0, 1), 2: >= 1,
+// NaN or no branch), so that "clamp(r) < clamp(r_winner)" keeps the first of equal clamped
+// factors, as a loop of divisions would; a zero or NaN denominator is divided on its own.
+template <typename T> struct RatioWin {
+  int cls = 2;
+  T pn = T(1), pd = T(1);
+  // offers the ratio dm / den of a branch; true if it is now the winner
+  __device__ __forceinline__ bool offer(T dm, T den) {
+    T n = den < T(0) ? -dm : dm, d = den < T(0) ? -den : den;
+    if (!(d > T(0))) {   // zero or NaN denominator: the clamped quotient itself
+      n = fmax(T(0), fmin(T(1), dm / den));
+      d = T(1);
+    }
+    const int c = (n != n) ? 2 : (n <= T(0) ? 0 : (n >= d ? 2 : 1));
+    const bool less = c < cls || (c == 1 && cls == 1 && n * pd < pn * d);
+    if (less) { cls = c; pn = n; pd = d; }
+    return less;
+  }
+};
+
 // ---------------------------------------------------------------------------------------------
 // Block staging: the rows of one block's elements (SoA rows, kBlock consecutive elements each)
 // are copied global -> shared by the TMA unit (cp.async.bulk, one elected thread) while the
@@ -925,7 +947,7 @@ struct StageScalars {
 //   kOpFp32     (double-float state only) the operator (volume, flux, hatM^-1 = I) in FP32
 //               arithmetic; the SSP update, the outputs and the limiter's quantities stay in the
 //               stored type;
-//   kOpElement  (FP64, no source terms) the element operator g.Aop, N x N per element: the
+//   kOpElement  (FP64 or double-float, no source terms) the element operator g.Aop, N x N per element: the
 //               volume term and the element's own outflow terms as one product with c, built
 //               by k_build_element_operator whenever the velocity changes; only the inflow terms
 //               are evaluated at the edge points.  GB300's FP64 rate bounds the FP64 stage: this
@@ -938,7 +960,8 @@ __device__ __forceinline__ void stage_op_tile(const Geo<T> g, const T *cin, cons
            const LimOut<T> lo, const StageScalars sc, const int tile, const int nTiles = -1) {
   constexpr int N = Dims<P>::N, Q = Dims<P>::Q, R = Dims<P>::R, NQ = NCQ<P>::value;
   constexpr bool OPF = VAR == kOpFp32, EOP = VAR == kOpElement;
-  static_assert(!EOP || (std::is_same_v<T, double> && !RHS), "the element operator is FP64 without source terms");
+  static_assert(!EOP || ((std::is_same_v<T, double> || std::is_same_v<T, df32>) && !RHS),
+                "the element operator is FP64 or double-float without source terms");
   using A = std::conditional_t<OPF, float, T>;
   // with the mass solve (FP64, double-float) and no source terms, hatM^-1 is folded into the
   // test-function tables of the volume and flux terms (Fg1, Fg2, Fphi)

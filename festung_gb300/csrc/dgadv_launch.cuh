@@ -77,11 +77,13 @@ static cudaError_t upload_tables(const RefTables &rt) {
   return cudaMemcpyToSymbol(tab_symbol<T, P>(), &t, sizeof(t));
 }
 
-// The element operator (kOpElement) is in use: FP64, enabled, built for the current velocity
-// and no source terms (with them the mass solve is not folded).
+// The element operator (kOpElement) is in use: FP64 or double-float, enabled, built for the
+// current velocity and no source terms (with them the mass solve is not folded); a
+// double-float handle with the FP32 operator keeps that one.
 static bool element_operator_on(const dgadv_handle *h) {
-  return h->Aop && h->elemOp && h->aopVersion == h->velVersion && !(h->nTerms > 0 && h->rhs);
+  return h->Aop && h->elemOp && h->aopVersion == h->velVersion && !(h->nTerms > 0 && h->rhs) && !h->opFp32;
 }
+template <typename T> constexpr bool kHasElementOperator = std::is_same_v<T, double> || std::is_same_v<T, df32>;
 
 template <typename T>
 static Geo<T> make_geo(const dgadv_handle *h) {
@@ -234,7 +236,7 @@ static cudaError_t set_smem_attributes() {
   set((const void *)k_stage_op<T, P, 2, true, true>, SR::bytes(SR::op(2, true), 1));
   set((const void *)k_stage_op<T, P, 2, false, true>, SR::bytes(SR::op(2, true), 1));
   set((const void *)k_limit_dot_lin<T, P>, SR::bytes(SR::limdot_lin(), 1));
-  if constexpr (std::is_same_v<T, double>) {   // the element-operator variants
+  if constexpr (kHasElementOperator<T>) {   // the element-operator variants
     set((const void *)k_stage_op<T, P, 0, false, false, kOpElement>, SR::bytes(SR::op(0, false, true), 1));
     set((const void *)k_stage_op<T, P, 1, false, false, kOpElement>, SR::bytes(SR::op(1, false, true), 1));
     set((const void *)k_stage_op<T, P, 2, false, false, kOpElement>, SR::bytes(SR::op(2, false, true), 1));
@@ -278,14 +280,14 @@ template <typename T, int P, int MODE, bool RHS, bool LIN>
 static auto stage_kernel(const dgadv_handle *h) -> decltype(&k_stage_op<T, P, MODE, RHS, LIN, kOpPlain>) {
   if constexpr (std::is_same_v<T, df32>)
     if (h->opFp32) return &k_stage_op<T, P, MODE, RHS, LIN, kOpFp32>;
-  if constexpr (std::is_same_v<T, double> && !RHS)
+  if constexpr (kHasElementOperator<T> && !RHS)
     if (element_operator_on(h)) return &k_stage_op<T, P, MODE, RHS, LIN, kOpElement>;
   return &k_stage_op<T, P, MODE, RHS, LIN, kOpPlain>;
 }
 // Its staged rows.
 template <typename T, int P>
 static int stage_rows(const dgadv_handle *h, int mode, bool lin, bool rhs) {
-  return StageRows<T, P>::op(mode, lin, std::is_same_v<T, double> && !rhs && element_operator_on(h));
+  return StageRows<T, P>::op(mode, lin, kHasElementOperator<T> && !rhs && element_operator_on(h));
 }
 
 template <typename T, int P>
@@ -569,7 +571,7 @@ static void to_real(const double *src, size_t n, void *dst) {
 
 template <typename T, int MASK>
 static cudaError_t dispatch_build_element_operator(dgadv_handle *h) {
-  if constexpr (std::is_same_v<T, double>) {
+  if constexpr (kHasElementOperator<T>) {
     const Geo<T> g = make_geo<T>(h);
     const int grid = (h->K + kBlock - 1) / kBlock;
     switch (h->p) {
@@ -608,7 +610,7 @@ static PrecOps make_ops() {
   o.persist_attributes = nullptr;
   o.copy = copy_state;
   o.from_f64 = from_f64<T>;
-  o.build_element_operator = std::is_same_v<T, double> ? dispatch_build_element_operator<T, MASK> : nullptr;
+  o.build_element_operator = kHasElementOperator<T> ? dispatch_build_element_operator<T, MASK> : nullptr;
   o.tr_stage = nullptr;
   o.tr_convert = nullptr;
   o.tr_mask = nullptr;

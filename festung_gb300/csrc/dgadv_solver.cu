@@ -756,7 +756,10 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
     h->adjWarps = value;
   } else if (option == DGADV_OPT_ELEMENT_OPERATOR) {
     if (value != 0 && value != 1) return DGADV_EINVAL;
-    if (value && !ops(h).build_element_operator) { h->err = "the element operator is built for FP64"; return DGADV_EUNSUPPORTED; }
+    if (value && !ops(h).build_element_operator) {
+      h->err = "the element operator is built for FP64 and double-float";
+      return DGADV_EUNSUPPORTED;
+    }
     h->elemOp = value == 1;
     if (h->elemOp) {
       h->aopVersion = -1;

@@ -93,7 +93,8 @@ enum {
                                    ahead of the reverse stages (one more set of work states and
                                    limiter records, allocated by dgadv_forward_record); 1: one
                                    stream.  Gradients bitwise unchanged                        */
-  DGADV_OPT_ELEMENT_OPERATOR = 10 /* FP64 handles without source terms: 1 (default) keeps the
+  DGADV_OPT_ELEMENT_OPERATOR = 10 /* FP64 and double-float handles without source terms (and,
+                                   double-float, without the FP32 operator): 1 (default) keeps the
                                    stage operator's volume term and the element's own outflow
                                    terms as one N x N matrix per element (N^2 reals per element,
                                    rebuilt whenever the velocity changes), which takes the FP64

@@ -309,16 +309,17 @@ def test_fp32_operator_on_double_float_state(lib, kw):
     assert em <= 1e-6 and em < ef, (em, ef)
 
 
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-13), ('df32', 1e-11)])
 @pytest.mark.parametrize('kw', [SMALL[0], SMALL[2], SMALL[4], SMALL[6], SMALL[8], SMALL[9]],
                          ids=['p0', 'p1lim', 'p2lim', 'p3lim', 'p3hier', 'solid_body'])
-def test_fp64_element_operator_matches_quadrature_form(lib, kw):
-    """DGADV_OPT_ELEMENT_OPERATOR (the FP64 default): the volume term and the element's own
-    outflow terms as one precomputed N x N matrix per element agree with the operator evaluated
-    at the quadrature and edge points to roundoff."""
+def test_element_operator_matches_quadrature_form(lib, kw, precision, tol):
+    """DGADV_OPT_ELEMENT_OPERATOR (the FP64 and double-float default): the volume term and the
+    element's own outflow terms as one precomputed N x N matrix per element agree with the
+    operator evaluated at the quadrature and edge points to roundoff."""
     from festung_gb300 import _lib as L
-    a = gpu_run(precision='fp64', **kw)
-    b = gpu_run(precision='fp64', gpuOptions={L.OPT_ELEMENT_OPERATOR: 0}, **kw)
-    assert rel(a.cDisc, b.cDisc) <= 1e-13
+    a = gpu_run(precision=precision, **kw)
+    b = gpu_run(precision=precision, gpuOptions={L.OPT_ELEMENT_OPERATOR: 0}, **kw)
+    assert rel(a.cDisc, b.cDisc) <= tol
 
 
 def test_element_operator_follows_the_velocity(lib):
