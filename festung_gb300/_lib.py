@@ -18,7 +18,7 @@ LIM_LINEAR, LIM_HIERARCH_VERT, LIM_STRICT = 0, 1, 2
 TIME_CONST, TIME_EXP_NEG = 0, 1
 FLAG_NO_REORDER, FLAG_NO_SHIFT, FLAG_NO_GRAPH, FLAG_NO_PDL, FLAG_FUSE, FLAG_PERSIST = 1, 2, 4, 8, 16, 32
 OPT_GRAPH_STEPS, OPT_FLAGS, OPT_PERSIST_BLOCKS, OPT_ADJ_WARPS, OPT_TAYLOR_MASS, OPT_VOLUME_MMA, OPT_OP_BLOCK, \
-    OPT_OPERATOR_FP32, OPT_ADJ_STREAMS, OPT_ELEMENT_OPERATOR = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
+    OPT_OPERATOR_FP32, OPT_ADJ_STREAMS, OPT_ELEMENT_OPERATOR, OPT_ADJ_GRAPH = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11
 OUT_VTK, OUT_TEC = 1, 2
 FN_CONST, FN_POLY3, FN_SOLID_BODY, FN_GAUSS_SLOT, FN_GAUSS, FN_TRANSIENT, FN_COS7 = 0, 1, 2, 3, 4, 5, 6
 VEL_ROTATION, VEL_TRANSIENT, VEL_STREAM, VEL_CONST = 16, 17, 18, 19

@@ -13,8 +13,9 @@ Each candidate runs ``nSteps`` steps of the handle's own problem after one warm-
 with CUDA events on the handle's stream; the state is restored afterwards.  The choice can be
 kept in a JSON file keyed by the problem's signature and the GPU name, and reused.
 
-``tune_adjoint`` does the same for the FP32 adjoint stage kernel: warps per role, i.e. 32, 64 or
-128 elements per CTA with four warp roles (three edges, the volume points) per element.
+``tune_adjoint`` does the same for the reverse sweep: the adjoint stage kernel's warps per role,
+i.e. 32, 64 or 128 elements per CTA with four warp roles (three edges, the volume points) per
+element, then the sweep as one CUDA graph or launched directly.
 
 The limiter kernels keep 128 elements per CTA (the padding unit of every per-element array).
 """
@@ -122,9 +123,8 @@ def tune_adjoint(solver, tau, nSteps=20, nSnapshots=0, reps=3):
     FP64 the one-thread kernel (0) is timed too, whose gradients agree to roundoff.  The
     handle's state is restored."""
     state = solver.get_state()
-    table = []
-    for w in (ADJ_WARPS_FP64 if getattr(solver, 'precision', None) == 'fp64' else ADJ_WARPS):
-        solver.set_option(L.OPT_ADJ_WARPS, w)
+
+    def timed():
         times = []
         for _ in range(reps + 1):   # the first backward captures the sweep's graph
             solver.set_state(state)
@@ -133,8 +133,23 @@ def tune_adjoint(solver, tau, nSteps=20, nSnapshots=0, reps=3):
             t = time.perf_counter()
             solver.backward(g)
             times.append(time.perf_counter() - t)
-        table.append(dict(adjWarps=w, ms_backward=1e3 * min(times[1:])))
+        return 1e3 * min(times[1:])
+
+    table = []
+    for w in (ADJ_WARPS_FP64 if getattr(solver, 'precision', None) == 'fp64' else ADJ_WARPS):
+        solver.set_option(L.OPT_ADJ_WARPS, w)
+        table.append(dict(adjWarps=w, ms_backward=timed()))
     best = min(table, key=lambda r: r['ms_backward'])
     solver.set_option(L.OPT_ADJ_WARPS, best['adjWarps'])
+    # then the sweep as one CUDA graph or launched directly, on that width
+    if hasattr(L, 'OPT_ADJ_GRAPH'):
+        cur = solver.get_option(L.OPT_ADJ_GRAPH)
+        best = dict(best, adjGraph=cur)
+        solver.set_option(L.OPT_ADJ_GRAPH, 1 - cur)
+        alt = timed()
+        table.append(dict(adjWarps=best['adjWarps'], adjGraph=1 - cur, ms_backward=alt))
+        if alt < best['ms_backward']:
+            best = dict(best, adjGraph=1 - cur, ms_backward=alt)
+        solver.set_option(L.OPT_ADJ_GRAPH, best['adjGraph'])
     solver.set_state(state)
     return best, table

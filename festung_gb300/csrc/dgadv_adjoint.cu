@@ -742,7 +742,10 @@ extern "C" int dgadv_backward(dgadv_handle *h, const double *dJdcT, double *dJdc
   // The reverse sweep (about 2S + 1 launches per step) runs as one CUDA graph, captured on the
   // first backward of a run length / step / snapshot count and replayed afterwards.
   int st = DGADV_OK;
-  const bool useGraph = !(h->flags & DGADV_FLAG_NO_GRAPH);
+  // one CUDA graph for the whole sweep (DGADV_OPT_ADJ_GRAPH; default: without the limiter, whose
+  // sweeps of thousands of launches over two streams ran faster launched directly)
+  const int ag = h->adjGraph < 0 ? (h->lim ? 0 : 1) : h->adjGraph;
+  const bool useGraph = !(h->flags & DGADV_FLAG_NO_GRAPH) && ag == 1;
   if (useGraph && !h->adjExec) {
     cudaGraph_t graph = nullptr;
     DG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));

@@ -55,6 +55,7 @@ struct dgadv_handle {
   mutable bool pdlBreak = false;       // the next launch waits for its predecessors to complete
   int adjWarps = 2;                    // warps per role of the FP32 adjoint stage (1, 2 or 4)
   bool adjTwoStreams = true;           // reverse sweep: recomputation on a second stream
+  int adjGraph = -1;                   // reverse sweep as one CUDA graph: 1, 0, or -1 (by limiter)
   bool mtOnTheFly = false;             // Taylor mass correction rebuilt from B (DGADV_OPT_TAYLOR_MASS)
   bool volumeMma = false;              // volume term on the tensor cores (DGADV_OPT_VOLUME_MMA)
   int opBlock = 128;                   // elements per block of the stage operator (DGADV_OPT_OP_BLOCK)

@@ -766,6 +766,9 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
       int st;
       if ((st = refresh_element_operator(h))) return st;
     }
+  } else if (option == DGADV_OPT_ADJ_GRAPH) {
+    if (value != -1 && value != 0 && value != 1) return DGADV_EINVAL;
+    h->adjGraph = value;
   } else if (option == DGADV_OPT_ADJ_STREAMS) {
     if (value != 1 && value != 2) return DGADV_EINVAL;
     h->adjTwoStreams = value == 2;
@@ -808,6 +811,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   else if (option == DGADV_OPT_PERSIST_BLOCKS) *value = h->persistPerSM;
   else if (option == DGADV_OPT_ADJ_WARPS) *value = h->adjWarps;
   else if (option == DGADV_OPT_ADJ_STREAMS) *value = h->adjTwoStreams ? 2 : 1;
+  else if (option == DGADV_OPT_ADJ_GRAPH) *value = h->adjGraph < 0 ? (h->lim ? 0 : 1) : h->adjGraph;
   else if (option == DGADV_OPT_ELEMENT_OPERATOR) *value = (h->elemOp && ops(h).build_element_operator) ? 1 : 0;
   else if (option == DGADV_OPT_TAYLOR_MASS) *value = h->mtOnTheFly ? 1 : 0;
   else if (option == DGADV_OPT_VOLUME_MMA) *value = h->volumeMma ? 1 : 0;

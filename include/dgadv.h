@@ -93,7 +93,7 @@ enum {
                                    ahead of the reverse stages (one more set of work states and
                                    limiter records, allocated by dgadv_forward_record); 1: one
                                    stream.  Gradients bitwise unchanged                        */
-  DGADV_OPT_ELEMENT_OPERATOR = 10 /* FP64 and double-float handles without source terms (and,
+  DGADV_OPT_ELEMENT_OPERATOR = 10, /* FP64 and double-float handles without source terms (and,
                                    double-float, without the FP32 operator): 1 (default) keeps the
                                    stage operator's volume term and the element's own outflow
                                    terms as one N x N matrix per element (N^2 reals per element,
@@ -101,6 +101,9 @@ enum {
                                    operator from about 244 to about 100 arithmetic instructions
                                    per element at p = 2; 0: evaluated at the quadrature points.
                                    The results agree to roundoff                              */
+  DGADV_OPT_ADJ_GRAPH = 11      /* the reverse sweep captured as one CUDA graph (1) or launched
+                                   directly (0); -1 (default): 1 without the limiter, 0 with it.
+                                   Gradients bitwise unchanged                                */
 };
 
 /* ---- host helpers: static data ------------------------------------------------------- */

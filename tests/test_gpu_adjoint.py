@@ -95,7 +95,7 @@ def test_adjoint_autotuner_applies_a_width_and_keeps_the_gradient(lib):
     try:
         ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=3)
         best, table = AT.tune_adjoint(pd.solver, pd.tau, nSteps=6, nSnapshots=3, reps=1)
-        assert [r["adjWarps"] for r in table] == [1, 2, 4]
+        assert [r["adjWarps"] for r in table if "adjGraph" not in r] == [1, 2, 4]
         assert pd.solver.get_option(L.OPT_ADJ_WARPS) == best['adjWarps']
         got = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=3)
         assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
