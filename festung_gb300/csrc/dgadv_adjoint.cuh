@@ -497,7 +497,7 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
   if (!active) return;
   T u[N];
   lin_u<T, P>(xv, u);
-  // the forward's factor, vertex by vertex (vertex_alpha), with its branch and raw ratio
+  // the forward's factor (vertex_alpha_1div), with the vertex, branch and raw ratio that set it
   const T third = T(1) / T(3), two3 = T(2) / T(3), tol = T(1.e-8);
   const T hx[3] = {-third, two3, -third}, hy[3] = {-third, -third, two3};
   T v[3], valD[3], mn[3], mx[3];

@@ -472,31 +472,18 @@ __device__ __forceinline__ void load_shifts(const unsigned long long *slots, int
   }
 }
 
-// alpha of one computeVertexBasedLimiter call (core/computeVertexBasedLimiter.m:78-106)
-template <typename T>
-__device__ __forceinline__ T vertex_alpha(T cbar, const T v[3], const T mn[3], const T mx[3]) {
-  const T tol = T(1.e-8);
-  T alpha = T(1);
-#pragma unroll
-  for (int n = 0; n < 3; ++n) {
-    const T dV = v[n] - cbar, dMin = mn[n] - cbar, dMax = mx[n] - cbar;
-    T a = T(1);
-    if (dV < dMin + tol) a = fmax(T(0), fmin(T(1), dMin / (dV - tol)));
-    if (dV > dMax - tol) a = fmax(T(0), fmin(T(1), dMax / (dV + tol)));
-    alpha = (n == 0) ? a : fmin(alpha, a);
-  }
-  return alpha;
-}
-
-// The same factor with one division: clamping to [0, 1] is monotone, so the minimum over the
-// vertices of the clamped ratios is the clamped smallest ratio.  Each branch's ratio is written
+// alpha of one computeVertexBasedLimiter call (core/computeVertexBasedLimiter.m:78-106): at each
+// vertex n on a branch (dV = v_n - cbar below dMin + tol, or above dMax - tol) the clamped ratio
+// clamp01(dMin / (dV - tol)) or clamp01(dMax / (dV + tol)), else 1; alpha is their minimum.
+// With one division: clamping to [0, 1] is monotone, so the minimum over the vertices of the
+// clamped ratios is the clamped smallest ratio.  Each branch's ratio is written
 // with a positive denominator, num / den (num >= 0: dMin <= 0 <= dMax, the element's own mean
 // being in its patches); the smallest is found by comparing cross products (the first vertex on
 // ties) and divided once.  A ratio that ties another to within rounding may be the one divided:
 // the factor then differs by at most an ulp.  The limiter's division sits on GB300's FP64 (or
 // the double-float) path, where it costs about as much as the rest of the factor.
 // A patch extreme that the global shift rounded past the element's own value can leave a
-// branch's denominator at or below zero; such a ratio is divided on its own, as vertex_alpha does.
+// branch's denominator at or below zero; such a ratio is clamped and divided on its own.
 template <typename T>
 __device__ __forceinline__ T vertex_alpha_1div(T cbar, const T v[3], const T mn[3], const T mx[3]) {
   const T tol = T(1.e-8);
