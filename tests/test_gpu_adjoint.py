@@ -283,8 +283,9 @@ STREAM_CASES = [dict(precision='fp32', kw=dict(hmax=2 ** -4, p=2, numSteps=24, t
 def test_two_stream_sweep_equals_one_stream_sweep(lib, case):
     """DGADV_OPT_ADJ_STREAMS: the recomputation and the limiter adjoint's scatters on a second
     stream, one reversed step ahead of the reverse stages, give bitwise the gradients of one
-    stream, captured in a graph (and replayed) or launched directly, with every stage stored and
-    for binomial and every-state checkpoints."""
+    stream; DGADV_OPT_ADJ_GRAPH: the sweep captured in a graph (and replayed) or launched
+    directly gives the same bits; with every stage stored and for binomial and every-state
+    checkpoints."""
     from festung_gb300 import _lib as L
     from festung_gb300 import adjoint as AD
     kw = case['kw']
@@ -299,13 +300,13 @@ def test_two_stream_sweep_equals_one_stream_sweep(lib, case):
         ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
         for streams in (1, 2):
             pd.solver.set_option(L.OPT_ADJ_STREAMS, streams)
-            for flags in (0, L.FLAG_NO_GRAPH):
-                pd.solver.set_option(L.OPT_FLAGS, flags)
+            for graph in (1, 0):                  # the sweep as one CUDA graph, or launched directly
+                pd.solver.set_option(L.OPT_ADJ_GRAPH, graph)
                 for snaps in (0, 3, 5, kw['numSteps']):
                     for _ in range(2):
                         got = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=snaps)
                         assert got[0] == ref[0]
-                        assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2]), (streams, flags, snaps)
+                        assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2]), (streams, graph, snaps)
     finally:
         pd.solver.close()
 
