@@ -364,10 +364,20 @@ def large_block(device, flush):
 ADJOINT_WORKLOAD = dict(hmax=2 ** -7, p=2, numSteps=200, tEnd=200 * 2e-4)
 
 
+def tuned_sweep(s, pd, snaps):
+    """The reverse sweep's launch configuration for a checkpoint mode (autotune.tune_adjoint:
+    warps per role, graph or direct launches, one or two streams), tuned on a 40-step run with
+    the same kind of checkpoints; returns the choice."""
+    from festung_gb300 import autotune as AT
+    best = AT.tune_adjoint(s, pd.tau, nSteps=40, nSnapshots=0 if snaps == 0 else 4, reps=2)[0]
+    return {k: v for k, v in best.items() if k != 'ms_backward'}
+
+
 def adjoint_block(reps=3, fd_dirs=16):
     """Adjoint cost on the gradient workload (32768 triangles, p = 2, 200 SSP-RK3 steps): wall
     time of dgadv_backward over the wall time of the same run forward (dgadv_set_state +
-    dgadv_step + sync), with every stage state stored and with 20 binomial snapshots; FP64
+    dgadv_step + sync), with every stage state stored and with 20 binomial snapshots, each with
+    the sweep's launch configuration tuned for it (tuned_sweep); FP64
     central differences (h = 1e-6) against the adjoint's directional derivatives; FP32
     gradients against FP64."""
     from festung_gb300 import adjoint as AD
@@ -389,6 +399,7 @@ def adjoint_block(reps=3, fd_dirs=16):
             tf.append(time.perf_counter() - t)
         row = {'forward_ms': 1e3 * min(tf)}
         for name, snaps in (('stages_stored', 0), ('snapshots_20', 20)):
+            launch = tuned_sweep(s, pd, snaps)
             tb, trec = [], []
             for _ in range(reps + 1):
                 s.set_velocity_theta(pd.theta); s.set_state(c0)
@@ -397,7 +408,7 @@ def adjoint_block(reps=3, fd_dirs=16):
                 r = s.get_state() - cstar
                 t = time.perf_counter(); g0, gth = s.backward(r); tb.append(time.perf_counter() - t)
             row[name] = {'record_ms': 1e3 * min(trec), 'backward_ms': 1e3 * min(tb[1:]),
-                         'backward_over_forward': min(tb[1:]) / min(tf)}
+                         'backward_over_forward': min(tb[1:]) / min(tf), 'launch': launch}
         grads[prec] = (g0, gth)
         if prec == 'fp64' and fd_dirs:
             rng = np.random.default_rng(0)
@@ -444,13 +455,15 @@ def limited_adjoint_rows(AD, kw, reps, fd_dirs, lim):
             tf.append(time.perf_counter() - t)
         row = {'forward_ms': 1e3 * min(tf)}
         for name, snaps in (('stages_stored', 0), ('snapshots_20', 20)):
+            launch = tuned_sweep(s, pd, snaps)
             tb = []
             for _ in range(reps + 1):
                 s.set_velocity_theta(pd.theta); s.set_state(c0)
                 s.forward_record(kw['numSteps'], pd.tau, snaps); s.sync()
                 r = s.get_state() - cstarL
                 t = time.perf_counter(); g0, gth = s.backward(r); tb.append(time.perf_counter() - t)
-            row[name] = {'backward_ms': 1e3 * min(tb[1:]), 'backward_over_forward': min(tb[1:]) / min(tf)}
+            row[name] = {'backward_ms': 1e3 * min(tb[1:]), 'backward_over_forward': min(tb[1:]) / min(tf),
+                         'launch': launch}
         if prec == 'fp64' and fd_dirs:
             row['fd_theta'] = limited_fd_check(AD, kw, fd_dirs, lim=lim)
             row['sensitivity'] = limited_sensitivity(AD, pd, c0, cstarL, kw['numSteps'])

@@ -15,7 +15,7 @@ kept in a JSON file keyed by the problem's signature and the GPU name, and reuse
 
 ``tune_adjoint`` does the same for the reverse sweep: the adjoint stage kernel's warps per role,
 i.e. 32, 64 or 128 elements per CTA with four warp roles (three edges, the volume points) per
-element, then the sweep as one CUDA graph or launched directly.
+element, then the sweep as one CUDA graph or launched directly, then on one stream or two.
 
 The limiter kernels keep 128 elements per CTA (the padding unit of every per-element array).
 """
@@ -151,5 +151,16 @@ def tune_adjoint(solver, tau, nSteps=20, nSnapshots=0, reps=3):
         if alt < best['ms_backward']:
             best = dict(best, adjGraph=1 - cur, ms_backward=alt)
         solver.set_option(L.OPT_ADJ_GRAPH, best['adjGraph'])
+    # and the sweep on one stream or two
+    if hasattr(L, 'OPT_ADJ_STREAMS'):
+        cur = solver.get_option(L.OPT_ADJ_STREAMS)
+        best = dict(best, adjStreams=cur)
+        alt = 3 - cur
+        solver.set_option(L.OPT_ADJ_STREAMS, alt)
+        t = timed()
+        table.append(dict(adjWarps=best['adjWarps'], adjGraph=best.get('adjGraph'), adjStreams=alt, ms_backward=t))
+        if t < best['ms_backward']:
+            best = dict(best, adjStreams=alt, ms_backward=t)
+        solver.set_option(L.OPT_ADJ_STREAMS, best['adjStreams'])
     solver.set_state(state)
     return best, table
