@@ -151,16 +151,16 @@ def tune_adjoint(solver, tau, nSteps=20, nSnapshots=0, reps=3):
         if alt < best['ms_backward']:
             best = dict(best, adjGraph=1 - cur, ms_backward=alt)
         solver.set_option(L.OPT_ADJ_GRAPH, best['adjGraph'])
-    # and the sweep on one stream or two
+    # and the sweep on one, two or three streams
     if hasattr(L, 'OPT_ADJ_STREAMS'):
         cur = solver.get_option(L.OPT_ADJ_STREAMS)
         best = dict(best, adjStreams=cur)
-        alt = 3 - cur
-        solver.set_option(L.OPT_ADJ_STREAMS, alt)
-        t = timed()
-        table.append(dict(adjWarps=best['adjWarps'], adjGraph=best.get('adjGraph'), adjStreams=alt, ms_backward=t))
-        if t < best['ms_backward']:
-            best = dict(best, adjStreams=alt, ms_backward=t)
+        for alt in (n for n in (1, 2, 3) if n != cur):
+            solver.set_option(L.OPT_ADJ_STREAMS, alt)
+            t = timed()
+            table.append(dict(adjWarps=best['adjWarps'], adjGraph=best.get('adjGraph'), adjStreams=alt, ms_backward=t))
+            if t < best['ms_backward']:
+                best = dict(best, adjStreams=alt, ms_backward=t)
         solver.set_option(L.OPT_ADJ_STREAMS, best['adjStreams'])
     solver.set_state(state)
     return best, table

@@ -133,35 +133,57 @@ void dev_release(dgadv_handle *h, void *&p) {
   p = nullptr;
 }
 
-// Buffers a forward step of the schedule writes besides its output: its work state, its stage
-// states and its limiter records.  Set 0 is the handle's own (cn, cA, cB, adjScrY, adjScrCdot).
-// With two streams the recomputation alternates between set 0 and set 1 (adjSet1), so that it
-// writes one set while the reverse stages read the other.
+// Buffers a forward step of the schedule writes besides its output: its stage states and its
+// limiter records (and, for the sets of the recomputation with two streams, a work state).  Set
+// 0 is the handle's own (cn, cA, cB, adjScrY, adjScrCdot).  With two or three streams the
+// recomputation alternates between set 0 and set 1 (adjSet1), so that it writes one set while
+// the reverse stages read the other.
 struct WorkSet {
   void *cn = nullptr, *cA = nullptr, *cB = nullptr, *scrY = nullptr, *scrCdot = nullptr;
 };
 
-// Cursor of a schedule run: the step the run stands at, the slot holding that state (-1: none),
-// and the step each set's work state holds (-1: none).
+// Cursor of a schedule run: the step the run stands at, the logical slot holding that state
+// (-1: none), and the step each work state holds (-1: none).
 struct Cursor {
   int step = 0;
   int slot = -1;
   int cnStep[2] = {0, -1};
 };
 
-// The streams of a schedule run.  One stream: every action in order on the handle's stream.
-// Two: the forward steps (advances and recomputation) on adjStreamF and the reverse stages on
-// the handle's stream.  A reversed step waits for its recomputation; a forward step that writes
-// a set or a slot first waits for the last reversed step that read it.  The results are bitwise
-// those of one stream: the same kernels read the same data.
+enum { kRev = 0, kFwd = 1, kAdv = 2 };
+
+// The streams of a schedule run.
+// - One stream: every action in order on the handle's stream.
+// - Two: the forward steps (advances and recomputation) on adjStreamF, the reverse stages on the
+//   handle's stream.
+// - Three: the recomputation of the reversed steps on adjStreamF, the advances between
+//   checkpoints on adjStreamA, with their own stage states, limiter records and limiter key
+//   sets, so that they run while the reverse stages and the recomputation of other steps run.
+// A reversed step waits for its recomputation.  A write into a set, a slot or a work state
+// first waits for the last reads of it on other streams; a read of a slot or a work state that
+// the advance stream wrote waits for that write.  The results are bitwise those of one stream:
+// the same kernels read the same data.
+//
+// Buffers are numbered 0 .. nSlots - 1 (physical slots), then the two work states.  A store
+// into a logical slot of the schedule may go to another physical slot: with several streams,
+// to the free one whose readers finished first, instead of the one the schedule reuses, which
+// the reversed step just issued is often still reading.  A slot is free when no checkpoint that
+// is still to be read (a step not yet reversed) sits in it.
 struct Lanes {
-  bool two = false;
-  cudaStream_t rev = nullptr, fwd = nullptr;
-  WorkSet set[2];
-  int cur = 0;                   // the set forward steps write
-  int setReader[2] = {-1, -1};   // event of the last reversed step that read a set (-1: none)
-  std::vector<int> slotReader;   // ... that read a slot
-  int nRev = 0;                  // reversed steps issued
+  int n = 1;
+  bool two = false;                    // n >= 2
+  cudaStream_t st[3] = {nullptr, nullptr, nullptr};   // kRev, kFwd, kAdv (shared when n < 3)
+  bool brk[3] = {false, false, false};   // the stream's next launch follows a cross-stream wait
+  WorkSet set[2];                      // the recomputation's sets
+  WorkSet aset;                        // the advances' stage states and records (n == 3)
+  void *work[2] = {nullptr, nullptr};  // the work states an advance writes when it stores nothing
+  int cur = 0;                         // the set the next recomputation writes
+  int setReader[2] = {-1, -1};         // reversed step that last read a set (-1: none)
+  std::vector<int> phys;               // physical slot of each logical slot
+  std::vector<int> revReader, tapeReader;   // per buffer: last reversed step / recomputation reading it
+  std::vector<char> advWrote;          // per buffer: written by the advances since the recomputation waited
+  int nRev = 0;                        // reversed steps issued
+  int frontier = 0;                    // the next step to reverse: checkpoints of later steps are dead
 };
 
 int rk_stages(const dgadv_handle *h, double omega[3]) {
@@ -171,32 +193,41 @@ int rk_stages(const dgadv_handle *h, double omega[3]) {
   return 1;
 }
 
-// The forward stream waits for the reversed step `ev` (an index into adjRevEv), if any.
-int wait_reader(dgadv_handle *h, Lanes &L, int &ev) {
-  if (!L.two || ev < 0) return DGADV_OK;
-  DG_CUDA(cudaStreamWaitEvent(L.fwd, h->adjRevEv[ev], 0));
-  h->pdlBreak = true;
-  ev = -1;
+int canon(const Lanes &L, int s) { return L.n == 1 ? kRev : (L.n == 2 && s == kAdv ? kFwd : s); }
+
+// Stream s waits for event e, recorded on stream `from`; nothing when they are one stream.
+int wait_event(dgadv_handle *h, Lanes &L, int s, int from, cudaEvent_t e) {
+  const int c = canon(L, s);
+  if (c == canon(L, from)) return DGADV_OK;
+  DG_CUDA(cudaStreamWaitEvent(L.st[c], e, 0));
+  L.brk[c] = true;
   return DGADV_OK;
 }
 
-// One forward step from c^step, read from `src` (a work state or a slot), written to `dst`; with
-// stage storage the step's stage states are written straight into its stage slots.  With
-// nStages < S only the first nStages stages run: their outputs (cA, cB) are what the reverse
-// stages of the unlimited scheme read.  recordsOnly runs every stage but the last solution
-// limiter: the limiter inputs are what the limiter adjoint reads.  In both cases c^(step+1) is
-// neither needed nor written, and the cursor stays.
-int forward_step(dgadv_handle *h, Cursor &w, Lanes &L, const void *src, void *dst, int nStages,
-                 bool recordsOnly = false) {
+// Stream s becomes the launch stream; its first launch after a cross-stream wait goes without
+// programmatic dependent launch.
+void use_stream(dgadv_handle *h, Lanes &L, int s) {
+  const int c = canon(L, s);
+  h->stream = L.st[c];
+  if (L.brk[c]) h->pdlBreak = true;
+  L.brk[c] = false;
+}
+
+// One forward step from c^step, read from `src`, written to `dst`, through the stage states and
+// limiter records of `ws`; advKeys: with the advance stream's limiter key sets.  With stage
+// storage the step's stage states are written straight into its stage slots.  With nStages < S
+// only the first nStages stages run: their outputs (cA, cB) are what the reverse stages of the
+// unlimited scheme read.  recordsOnly runs every stage but the last solution limiter: the limiter
+// inputs are what the limiter adjoint reads.  In both cases c^(step+1) is neither needed nor
+// written, and the cursor stays.
+int forward_step(dgadv_handle *h, Cursor &w, const WorkSet &ws, const void *src, void *dst, int nStages,
+                 bool recordsOnly = false, bool advKeys = false) {
   const PrecOps &o = ops_of(h);
   double omega[3];
   const int S = rk_stages(h, omega);
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
   const bool partial = nStages < S;
   if (partial && nStages <= 0) return DGADV_OK;   // one stage: its input c^step is all it needs
-  int st;
-  if ((st = wait_reader(h, L, L.setReader[L.cur]))) return st;
-  const WorkSet &ws = L.set[L.cur];
   void *cA = h->cA, *cB = h->cB;
   h->cA = ws.cA;
   h->cB = ws.cB;
@@ -214,11 +245,22 @@ int forward_step(dgadv_handle *h, Cursor &w, Lanes &L, const void *src, void *ds
                                       : (char *)ws.scrCdot + (size_t)s * bytes;
     }
   }
+  const bool swapKeys = advKeys && h->lim;
+  if (swapKeys) {
+    std::swap(h->vkeys, h->vkeysAdv);
+    std::swap(h->gmm, h->gmmAdv);
+    std::swap(h->limPass, h->limPassAdv);
+  }
   h->stepSrc = src;
   h->stepDst = dst;
   h->stepStages = partial ? nStages : 0;
   h->stepRecordsOnly = recordsOnly;
   const cudaError_t e = o.step(h, w.step * h->recTau, h->recTau);
+  if (swapKeys) {
+    std::swap(h->vkeys, h->vkeysAdv);
+    std::swap(h->gmm, h->gmmAdv);
+    std::swap(h->limPass, h->limPassAdv);
+  }
   h->cA = cA;
   h->cB = cB;
   h->stepSrc = nullptr;
@@ -229,8 +271,60 @@ int forward_step(dgadv_handle *h, Cursor &w, Lanes &L, const void *src, void *ds
   DG_CUDA(e);
   if (partial || recordsOnly) return DGADV_OK;
   ++w.step;
-  w.slot = -1;
-  w.cnStep[L.cur] = dst == ws.cn ? w.step : -1;
+  return DGADV_OK;
+}
+
+// The physical slot a store into logical slot l writes (see Lanes); `avoid` (the store's source)
+// only if nothing else is free.
+int store_buffer(const dgadv_handle *h, Lanes &L, int l, int avoid) {
+  if (!L.two) return L.phys[l];
+  std::vector<char> held(h->nSlots, 0);
+  held[0] = 1;   // c^0 stays where the end of the sweep reads it
+  for (int k = 0; k < h->nSlots; ++k)
+    if (k != l && h->slotStep[k] >= 0 && h->slotStep[k] <= L.frontier) held[L.phys[k]] = 1;
+  int best = -1, bestR = 0;
+  for (int p = 1; p < h->nSlots; ++p) {
+    if (held[p] || p == avoid) continue;
+    const int r = std::max(L.revReader[p], L.tapeReader[p]);
+    if (best < 0 || r < bestR || (r == bestR && p == L.phys[l])) {
+      best = p;
+      bestR = r;
+    }
+  }
+  if (best >= 0) L.phys[l] = best;
+  return L.phys[l];
+}
+
+// The work state an advance that stores nothing writes: the other one than its source, else
+// the one whose readers finished first (in place with one work state).
+int work_buffer(const dgadv_handle *h, const Lanes &L, int src) {
+  const int nS = h->nSlots;
+  if (!L.work[1]) return nS;
+  if (src >= nS) return nS + (1 - (src - nS));
+  const int r0 = std::max(L.revReader[nS], L.tapeReader[nS]);
+  const int r1 = std::max(L.revReader[nS + 1], L.tapeReader[nS + 1]);
+  return r1 < r0 ? nS + 1 : nS;
+}
+
+// The advance stream is about to write buffer b: it waits for b's readers on the other streams.
+int before_write(dgadv_handle *h, Lanes &L, int b) {
+  int st;
+  if (L.revReader[b] >= 0) {
+    if ((st = wait_event(h, L, kAdv, kRev, h->adjRevEv[L.revReader[b]]))) return st;
+    L.revReader[b] = -1;
+  }
+  if (L.tapeReader[b] >= 0) {
+    if ((st = wait_event(h, L, kAdv, kFwd, h->adjTapeEv[L.tapeReader[b]]))) return st;
+    L.tapeReader[b] = -1;
+  }
+  return DGADV_OK;
+}
+
+// ... and has written it.
+int after_write(dgadv_handle *h, Lanes &L, int b) {
+  if (L.n < 3) return DGADV_OK;
+  DG_CUDA(cudaEventRecord(h->adjBufEv[b], L.st[kAdv]));
+  L.advWrote[b] = 1;
   return DGADV_OK;
 }
 
@@ -247,16 +341,17 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
   double omega[3];
   const int S = rk_stages(h, omega);
   const double cst[3] = {0.0, 1.0, 0.5};   // stage times (core/rungeKuttaExplicit.m:64-78)
-  char *slots = (char *)h->adjSlots;
+  const int nS = h->nSlots;
   char *stages = (char *)h->adjStages;
   auto stage_ptr = [&](int step, int s) { return stages + ((size_t)step * (S - 1) + (s - 1)) * bytes; };
-  auto slot_ptr = [&](int slot) { return slots + (size_t)slot * bytes; };
-  // where c^(w.step) can be read: its slot, else a work state (the forward set's first)
-  auto current = [&](const void *&src, int &fromSet) -> int {
-    fromSet = -1;
-    if (w.slot >= 0 && h->slotStep[w.slot] == w.step) { src = slot_ptr(w.slot); return DGADV_OK; }
-    for (int k : {L.cur, 1 - L.cur})
-      if (w.cnStep[k] == w.step && L.set[k].cn) { src = L.set[k].cn; fromSet = k; return DGADV_OK; }
+  auto buf_ptr = [&](int b) -> void * {
+    return b < nS ? (void *)((char *)h->adjSlots + (size_t)b * bytes) : L.work[b - nS];
+  };
+  // the buffer holding c^(w.step): its slot, else a work state
+  auto current = [&](int &b) -> int {
+    if (w.slot >= 0 && h->slotStep[w.slot] == w.step) { b = L.phys[w.slot]; return DGADV_OK; }
+    for (int k = 0; k < 2; ++k)
+      if (L.work[k] && w.cnStep[k] == w.step) { b = nS + k; return DGADV_OK; }
     h->err = "checkpoint schedule lost its state";
     return DGADV_EINVAL;
   };
@@ -267,51 +362,73 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
       w.step = h->slotStep[arg];
       w.slot = arg;
     } else if (op == A_ADVANCE) {
-      h->stream = L.two ? L.fwd : L.rev;
       const bool storeNext = a + 2 < to && h->schedule[a + 2] == A_STORE;
       for (int i = 0; i < arg; ++i) {
-        const void *src;
-        int fromSet;
-        if ((st = current(src, fromSet))) return st;
-        void *dst = L.set[L.cur].cn;
-        const int target = storeNext && i == arg - 1 ? h->schedule[a + 3] : -1;
-        if (target >= 0 && slot_ptr(target) != src) {
-          dst = slot_ptr(target);
-          if ((st = wait_reader(h, L, L.slotReader[target]))) return st;
+        int src;
+        if ((st = current(src))) return st;
+        int target = storeNext && i == arg - 1 ? h->schedule[a + 3] : -1;
+        int dst = target >= 0 ? store_buffer(h, L, target, src) : work_buffer(h, L, src);
+        if (target >= 0 && dst == src) {   // no other slot free: through a work state, then copied
+          target = -1;
+          dst = work_buffer(h, L, src);
         }
-        if ((st = forward_step(h, w, L, src, dst, S))) return st;
-        if (dst != L.set[L.cur].cn) {   // the result already sits in the slot the next action stores to
+        if ((st = before_write(h, L, dst))) return st;
+        // the advances' stage states and records: their own set, or the set the next
+        // recomputation writes
+        if (L.n < 3 && L.setReader[L.cur] >= 0) {
+          if ((st = wait_event(h, L, kAdv, kRev, h->adjRevEv[L.setReader[L.cur]]))) return st;
+          L.setReader[L.cur] = -1;
+        }
+        use_stream(h, L, kAdv);
+        if ((st = forward_step(h, w, L.n == 3 ? L.aset : L.set[L.cur], buf_ptr(src), buf_ptr(dst), S, false, L.n == 3)))
+          return st;
+        if ((st = after_write(h, L, dst))) return st;
+        if (target >= 0) {   // the result already sits in the slot the next action stores to
           h->slotStep[target] = w.step;
           w.slot = target;
+        } else {
+          w.cnStep[dst - nS] = w.step;
+          w.slot = -1;
         }
       }
     } else if (op == A_STORE) {
       if (!(w.slot == arg && h->slotStep[arg] == w.step)) {
-        h->stream = L.two ? L.fwd : L.rev;
-        const void *src;
-        int fromSet;
-        if ((st = current(src, fromSet))) return st;
-        if ((st = wait_reader(h, L, L.slotReader[arg]))) return st;
-        DG_CUDA(o.copy(h, slot_ptr(arg), src, bytes));
+        int src;
+        if ((st = current(src))) return st;
+        const int dst = store_buffer(h, L, arg, src);
+        if (dst != src) {
+          if ((st = before_write(h, L, dst))) return st;
+          use_stream(h, L, kAdv);
+          DG_CUDA(o.copy(h, buf_ptr(dst), buf_ptr(src), bytes));
+          if ((st = after_write(h, L, dst))) return st;
+        }
         h->slotStep[arg] = w.step;
         w.slot = arg;
       }
     } else {   // A_BACKWARD: the stage states of step arg (stored or recomputed), then reversed
       if (w.step != arg) { h->err = "checkpoint schedule out of order"; return DGADV_EINVAL; }
       const void *stageIn[3];
-      int fromSet = -1;
+      int cb = -1;              // the buffer of c^arg, when recomputed
       const int used = L.cur;   // the set this step's recomputation writes
+      const int ev = L.nRev;    // this reversed step's events
       if (stages) {
         if (w.slot < 0) { h->err = "checkpoint schedule lost its state"; return DGADV_EINVAL; }
-        stageIn[0] = slot_ptr(w.slot);
+        stageIn[0] = buf_ptr(L.phys[w.slot]);
         for (int s = 1; s < S; ++s) stageIn[s] = stage_ptr(arg, s);
       } else {
-        h->stream = L.two ? L.fwd : L.rev;
-        const void *c0;
-        if ((st = current(c0, fromSet))) return st;
+        if ((st = current(cb))) return st;
+        if (L.n == 3 && L.advWrote[cb]) {
+          if ((st = wait_event(h, L, kFwd, kAdv, h->adjBufEv[cb]))) return st;
+          L.advWrote[cb] = 0;
+        }
+        if (L.setReader[used] >= 0) {
+          if ((st = wait_event(h, L, kFwd, kRev, h->adjRevEv[L.setReader[used]]))) return st;
+          L.setReader[used] = -1;
+        }
+        use_stream(h, L, kFwd);
         // unlimited: the stages the reverse stages read; limited: every stage's limiter inputs
-        if ((st = forward_step(h, w, L, c0, nullptr, h->lim ? S : S - 1, h->lim))) return st;
-        stageIn[0] = c0;
+        if ((st = forward_step(h, w, L.set[used], buf_ptr(cb), nullptr, h->lim ? S : S - 1, h->lim != 0))) return st;
+        stageIn[0] = buf_ptr(cb);
         stageIn[1] = L.set[used].cA;
         stageIn[2] = L.set[used].cB;
       }
@@ -325,12 +442,11 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
         return h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
                              : (const char *)ws.scrCdot + (size_t)s * bytes;
       };
-      // Two streams with the limiter and every stage stored: the scatters of the limiter inputs'
-      // means to the adjoint's key sets do not depend on the adjoint variable, so they run on the
-      // forward stream, in the reverse stages' pass order; their key sets were last read two
-      // reversed steps ago
-      // (with every stage stored; when the sweep recomputes, the recomputation already keeps
-      // the forward stream the busier one)
+      // Several streams with the limiter and every stage stored: the scatters of the limiter
+      // inputs' means to the adjoint's key sets do not depend on the adjoint variable, so they
+      // run on the recomputation stream, in the reverse stages' pass order; their key sets were
+      // last read two reversed steps ago (when the sweep recomputes, the recomputation already
+      // keeps that stream the busier one)
       const bool pre = L.two && h->lim && stages;
       // the linear limiter's choices too (k_lim_choice), leaving the reverse stream k_lim_apply
       const bool preChoice = pre && h->limType == DGADV_LIM_LINEAR && h->adjChoice;
@@ -340,9 +456,8 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
         for (int m = 0; m < h->nTerms; ++m) gco[m] = h->timeFn[m] == DGADV_TIME_EXP_NEG ? std::exp(-tBC) : 1.0;
       };
       if (pre) {
-        h->stream = L.fwd;
-        int ev = L.nRev - 2;
-        if ((st = wait_reader(h, L, ev))) return st;
+        if (L.nRev >= 2 && (st = wait_event(h, L, kFwd, kRev, h->adjRevEv[L.nRev - 2]))) return st;
+        use_stream(h, L, kFwd);
         for (int s = S - 1; s >= 0; --s) {
           const long long p0 = h->adjPassF;
           DG_CUDA(o.vjp_scatter(h, recY(s), h->adjPassF++, 0));
@@ -363,11 +478,10 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
         }
       }
       if (L.two && (pre || !stages)) {
-        DG_CUDA(cudaEventRecord(h->adjFEv, L.fwd));
-        DG_CUDA(cudaStreamWaitEvent(L.rev, h->adjFEv, 0));
-        h->pdlBreak = true;
+        DG_CUDA(cudaEventRecord(h->adjTapeEv[ev], L.st[kFwd]));
+        if ((st = wait_event(h, L, kRev, kFwd, h->adjTapeEv[ev]))) return st;
       }
-      h->stream = L.rev;
+      use_stream(h, L, kRev);
       void *mub[3] = {nullptr, h->mu1, h->mu2};
       for (int s = S - 1; s >= 0; --s) {
         const void *muNext = (s == S - 1) ? h->lam : mub[s + 1];
@@ -381,7 +495,7 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
           const char *Cd = recCd(s);
           if (h->limType == DGADV_LIM_HIERARCH_VERT) {
             // hierarchical limiter (inputs recorded in Taylor form): per limiter its scatter
-            // (unless the forward stream made it), its pass and its gather
+            // (unless the recomputation stream made it), its pass and its gather
             if (!pre) DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
             v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
             DG_CUDA(o.lim_vjp(h, v));
@@ -397,9 +511,9 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
             }
           } else {
             // p >= 2: the solution limiter's kernel also scatters the time-derivative limiter's
-            // means (unless the forward stream made both scatters), and the time-derivative
+            // means (unless the recomputation stream made both scatters), and the time-derivative
             // limiter's kernel gathers the solution limiter's extreme terms first (5 launches per
-            // stage instead of 7; 4 with the scatters on the forward stream)
+            // stage instead of 7; 4 with the scatters on the recomputation stream)
             if (!pre) DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
             v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
             v.nextX = pre ? nullptr : Cd;
@@ -433,101 +547,163 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
         DG_CUDA(o.adj_stage(h, x));
       }
       if (L.two) {
-        const int ev = L.nRev++;
-        DG_CUDA(cudaEventRecord(h->adjRevEv[ev], L.rev));
-        if (!stages) {   // what this step read: its set, and the slot or set of c^arg
+        DG_CUDA(cudaEventRecord(h->adjRevEv[ev], L.st[kRev]));
+        L.nRev = ev + 1;
+        if (!stages) {   // what this step read: its set, and the buffer of c^arg
           L.setReader[used] = ev;
-          if (fromSet >= 0) L.setReader[fromSet] = ev;
-          else if (w.slot >= 0) L.slotReader[w.slot] = ev;
+          L.revReader[cb] = ev;
+          if (L.n == 3) L.tapeReader[cb] = ev;
           L.cur = 1 - used;
         }
       }
+      L.frontier = arg - 1;
       std::swap(h->lam, h->accn);
       w.step = arg + 1;
       w.slot = -1;
     }
   }
-  h->stream = L.rev;
+  h->stream = L.st[kRev];
   return DGADV_OK;
 }
 
-// The lanes of a run: the handle's buffers as set 0; for a reverse sweep that recomputes, with
-// two streams enabled, set 1 and the forward stream (forked from the handle's stream).
+// The lanes of a run: the handle's buffers as set 0 and its state as the one work state; for a
+// reverse sweep, with the streams enabled: set 1, the second work state and the recomputation
+// stream (forked from the handle's stream), and when it recomputes with three streams, the
+// advances' stream, set and work states.
 int make_lanes(dgadv_handle *h, Lanes &L, bool sweep) {
-  L.rev = h->stream;
+  L.st[kRev] = L.st[kFwd] = L.st[kAdv] = h->stream;
   L.set[0].cn = h->cn;
   L.set[0].cA = h->cA;
   L.set[0].cB = h->cB;
   L.set[0].scrY = h->adjScrY;
   L.set[0].scrCdot = h->adjScrCdot;
-  L.slotReader.assign(h->nSlots, -1);
+  L.work[0] = h->cn;
+  L.phys.resize(h->nSlots);
+  for (int k = 0; k < h->nSlots; ++k) L.phys[k] = k;
+  L.revReader.assign(h->nSlots + 2, -1);
+  L.tapeReader.assign(h->nSlots + 2, -1);
+  L.advWrote.assign(h->nSlots + 2, 0);
+  L.frontier = h->recSteps - 1;
   // (the resources come from the recorded run: a run recorded with one stream sweeps with one).
   // A sweep that recomputes alternates two buffer sets; one with every stage stored uses the
   // second stream for the limiter adjoint's scatters only
   const bool recomputes = !h->adjStages && !h->adjRecY;
-  L.two = sweep && h->adjTwoStreams && h->adjStreamF && (int)h->adjRevEv.size() >= h->recSteps &&
-          (recomputes ? h->adjSet1 != nullptr : h->lim != 0);
-  if (!L.two) return DGADV_OK;
+  const bool two = sweep && h->adjStreams >= 2 && h->adjStreamF && (int)h->adjRevEv.size() >= h->recSteps &&
+                   (int)h->adjTapeEv.size() >= h->recSteps && (recomputes ? h->adjSet1 != nullptr : h->lim != 0);
+  if (!two) return DGADV_OK;
+  L.n = 2;
+  L.two = true;
   const PrecOps &o = ops_of(h);
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
   double omega[3];
   const int S = rk_stages(h, omega);
-  char *b = (char *)h->adjSet1;
-  L.set[1].cn = b;
-  L.set[1].cA = b + bytes;
-  L.set[1].cB = b + 2 * bytes;
-  if (h->lim) {
-    L.set[1].scrY = b + 3 * bytes;
-    L.set[1].scrCdot = b + (3 + (size_t)S) * bytes;
+  if (recomputes) {
+    char *b = (char *)h->adjSet1;
+    L.set[1].cn = b;
+    L.set[1].cA = b + bytes;
+    L.set[1].cB = b + 2 * bytes;
+    if (h->lim) {
+      L.set[1].scrY = b + 3 * bytes;
+      L.set[1].scrCdot = b + (3 + (size_t)S) * bytes;
+    }
+    L.work[1] = L.set[1].cn;
   }
-  L.fwd = h->adjStreamF;
-  DG_CUDA(cudaEventRecord(h->adjFEv, L.rev));
-  DG_CUDA(cudaStreamWaitEvent(L.fwd, h->adjFEv, 0));
-  h->pdlBreak = true;
+  L.st[kFwd] = L.st[kAdv] = h->adjStreamF;
+  if (recomputes && h->adjStreams == 3 && h->adjStreamA && h->adjSetA && (int)h->adjBufEv.size() >= h->nSlots + 2) {
+    L.n = 3;
+    L.st[kAdv] = h->adjStreamA;
+    char *b = (char *)h->adjSetA;
+    L.work[0] = b;
+    L.work[1] = b + bytes;
+    L.aset.cA = b + 2 * bytes;
+    L.aset.cB = b + 3 * bytes;
+    if (h->lim) {
+      L.aset.scrY = b + 4 * bytes;
+      L.aset.scrCdot = b + (4 + (size_t)S) * bytes;
+    }
+  }
+  DG_CUDA(cudaEventRecord(h->adjFEv, L.st[kRev]));
+  DG_CUDA(cudaStreamWaitEvent(L.st[kFwd], h->adjFEv, 0));
+  if (L.n == 3) DG_CUDA(cudaStreamWaitEvent(L.st[kAdv], h->adjFEv, 0));
+  L.brk[kFwd] = L.brk[kAdv] = true;
   return DGADV_OK;
 }
 
-// Joins the forward stream back into the handle's stream.
+// Joins the other streams back into the handle's stream.
 int join_lanes(dgadv_handle *h, Lanes &L) {
-  h->stream = L.rev;
+  h->stream = L.st[kRev];
   if (!L.two) return DGADV_OK;
-  DG_CUDA(cudaEventRecord(h->adjFEv, L.fwd));
-  DG_CUDA(cudaStreamWaitEvent(L.rev, h->adjFEv, 0));
+  for (int s = kFwd; s < L.n; ++s) {
+    DG_CUDA(cudaEventRecord(h->adjFEv, L.st[s]));
+    DG_CUDA(cudaStreamWaitEvent(L.st[kRev], h->adjFEv, 0));
+  }
   h->pdlBreak = true;
   return DGADV_OK;
 }
 
-// Two-stream resources of a recorded run: the stream, the events and, if it recomputes, set 1.
-int lanes_alloc(dgadv_handle *h, int nSteps, bool recomputes) {
+int make_events(dgadv_handle *h, std::vector<cudaEvent_t> &v, size_t n) {
+  while (v.size() < n) {
+    cudaEvent_t e;
+    DG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    v.push_back(e);
+  }
+  return DGADV_OK;
+}
+
+// Stream resources of a recorded run: the recomputation stream, the events and, if it
+// recomputes, set 1; with three streams also the advances' stream, set, key sets and events.
+int lanes_alloc(dgadv_handle *h, int nSteps, int nSlots, bool recomputes) {
   const PrecOps &o = ops_of(h);
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
   double omega[3];
   const int S = rk_stages(h, omega);
-  const size_t states = 3 + (h->lim ? 2 * (size_t)S : 0);
+  const size_t records = h->lim ? 2 * (size_t)S : 0;
   int st;
-  if (recomputes && h->adjSet1States != states) {
+  if (recomputes && h->adjSet1States != 3 + records) {
     drop_sweep(h);
     dev_release(h, h->adjSet1);
     h->adjSet1States = 0;
-    if ((st = dev_alloc(h, &h->adjSet1, states * bytes))) return st;
-    h->adjSet1States = states;
+    if ((st = dev_alloc(h, &h->adjSet1, (3 + records) * bytes))) return st;
+    h->adjSet1States = 3 + records;
   }
   if (!h->adjStreamF) DG_CUDA(cudaStreamCreateWithFlags(&h->adjStreamF, cudaStreamNonBlocking));
   if (!h->adjFEv) DG_CUDA(cudaEventCreateWithFlags(&h->adjFEv, cudaEventDisableTiming));
-  while ((int)h->adjRevEv.size() < nSteps) {
-    cudaEvent_t e;
-    DG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    h->adjRevEv.push_back(e);
+  if ((st = make_events(h, h->adjRevEv, nSteps))) return st;
+  if ((st = make_events(h, h->adjTapeEv, nSteps))) return st;
+  if (!recomputes || h->adjStreams < 3) return DGADV_OK;
+  if (h->adjSetAStates != 4 + records) {
+    drop_sweep(h);
+    dev_release(h, h->adjSetA);
+    h->adjSetAStates = 0;
+    if ((st = dev_alloc(h, &h->adjSetA, (4 + records) * bytes))) return st;
+    h->adjSetAStates = 4 + records;
   }
-  return DGADV_OK;
+  if (h->lim && !h->vkeysAdv) {
+    // the advances' limiter passes: three key and slot sets, all reset (each pass resets the
+    // next set, as in the handle's own)
+    const size_t kb = o.keyBytes, vk = 3 * 2 * (size_t)h->nc * h->Vp * kb;
+    const size_t ns = 3 * (size_t)h->nInst * kSlotCopies * 2 * (size_t)h->nc;
+    if ((st = dev_alloc(h, &h->vkeysAdv, vk))) return st;
+    if ((st = dev_alloc(h, (void **)&h->gmmAdv, ns * 8))) return st;
+    std::vector<unsigned char> keys(vk, 0);
+    for (size_t q = 0; q < 3 * (size_t)h->nc; ++q) std::memset(keys.data() + q * 2 * h->Vp * kb, 0xFF, (size_t)h->Vp * kb);
+    DG_CUDA(cudaMemcpy(h->vkeysAdv, keys.data(), vk, cudaMemcpyHostToDevice));
+    std::vector<unsigned long long> init(ns);
+    for (size_t i = 0; i < ns; ++i) init[i] = (i & 1) ? 0ULL : o.slotKeyMax;
+    DG_CUDA(cudaMemcpy(h->gmmAdv, init.data(), ns * 8, cudaMemcpyHostToDevice));
+    h->limPassAdv = 0;
+  }
+  if (!h->adjStreamA) DG_CUDA(cudaStreamCreateWithFlags(&h->adjStreamA, cudaStreamNonBlocking));
+  return make_events(h, h->adjBufEv, (size_t)nSlots + 2);
 }
 
 // The reverse sweep: the schedule's actions from the first reversed step on, c^nSteps in cn.
 int reverse_sweep(dgadv_handle *h) {
   Cursor w;
-  w.step = w.cnStep[0] = h->recSteps;
+  w.step = h->recSteps;
   Lanes L;
   int st = make_lanes(h, L, true);
+  w.cnStep[0] = L.n == 3 ? -1 : h->recSteps;
   if (st == DGADV_OK) st = run_actions(h, h->schedBackward, h->schedule.size(), w, L);
   const int sj = join_lanes(h, L);
   return st ? st : sj;
@@ -676,7 +852,7 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
   }
   // the second stream of the reverse sweep: recomputation (and its buffer set) and, with the
   // limiter, the limiter adjoint's scatters
-  if (h->adjTwoStreams && (h->lim || (stageSteps == 0 && S > 1)) && (st = lanes_alloc(h, nSteps, stageSteps == 0)))
+  if (h->adjStreams >= 2 && (h->lim || (stageSteps == 0 && S > 1)) && (st = lanes_alloc(h, nSteps, nSlots, stageSteps == 0)))
     return st;
   h->slotStep.assign(nSlots, -1);
   make_schedule(nSteps, nSlots, h->schedule);
@@ -690,7 +866,7 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
   w.slot = 0;
   Lanes L;
   if ((st = make_lanes(h, L, false))) return st;
-  if ((st = run_actions(h, 0, h->schedBackward, w, L))) { h->stream = L.rev; return st; }
+  if ((st = run_actions(h, 0, h->schedBackward, w, L))) { h->stream = L.st[kRev]; return st; }
   // on to c^nSteps in cn; the state reached may sit in a slot only
   if (w.cnStep[0] != w.step && (w.slot < 0 || h->slotStep[w.slot] != w.step)) {
     h->err = "checkpoint schedule lost its state";
@@ -698,7 +874,9 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
   }
   while (w.step < nSteps) {
     const void *src = w.cnStep[0] == w.step ? h->cn : (const void *)((char *)h->adjSlots + (size_t)w.slot * bytes);
-    if ((st = forward_step(h, w, L, src, h->cn, S))) return st;
+    if ((st = forward_step(h, w, L.set[0], src, h->cn, S))) return st;
+    w.cnStep[0] = w.step;
+    w.slot = -1;
   }
   if (w.cnStep[0] != w.step) DG_CUDA(o.copy(h, h->cn, (char *)h->adjSlots + (size_t)w.slot * bytes, bytes));
   h->recorded = true;

@@ -54,7 +54,8 @@ struct dgadv_handle {
   bool stepRecordsOnly = false;        // ... and the last stage's solution limiter is left out
   mutable bool pdlBreak = false;       // the next launch waits for its predecessors to complete
   int adjWarps = 2;                    // warps per role of the FP32 adjoint stage (1, 2 or 4)
-  bool adjTwoStreams = true;           // reverse sweep: recomputation on a second stream
+  int adjStreams = 3;                  // reverse sweep: streams (1; 2 with the recomputation on a
+                                       // second; 3 with the advances on a third)
   int adjGraph = -1;                   // reverse sweep as one CUDA graph: 1, 0, or -1 (by limiter)
   bool mtOnTheFly = false;             // Taylor mass correction rebuilt from B (DGADV_OPT_TAYLOR_MASS)
   bool volumeMma = false;              // volume term on the tensor cores (DGADV_OPT_VOLUME_MMA)
@@ -132,7 +133,17 @@ struct dgadv_handle {
   void *adjSet1 = nullptr;
   size_t adjSet1States = 0;
   cudaEvent_t adjFEv = nullptr;
-  std::vector<cudaEvent_t> adjRevEv;
+  std::vector<cudaEvent_t> adjRevEv, adjTapeEv;   // per reversed step: its reverse stages, its recomputation
+  // the advances of a three-stream sweep: their stream, their buffer set (two work states, two
+  // stage states, S + S limiter records), their own limiter key sets and pass count, and per
+  // buffer (physical slot, then the two work states) the event of its last write
+  cudaStream_t adjStreamA = nullptr;
+  void *adjSetA = nullptr;
+  size_t adjSetAStates = 0;
+  void *vkeysAdv = nullptr;
+  unsigned long long *gmmAdv = nullptr;
+  long long limPassAdv = 0;
+  std::vector<cudaEvent_t> adjBufEv;
   void *tmpY = nullptr, *tmpD = nullptr;            // dJ/dy and dJ/dcDot of a reversed stage
   // extreme terms of the limiter adjoint, one record set per limiter kind, stored by position in
   // the vertex-patch CSR (vidx): the element at position i of patch v writes there the element

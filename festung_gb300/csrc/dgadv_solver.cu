@@ -770,8 +770,8 @@ extern "C" int dgadv_set_option(dgadv_handle *h, int32_t option, int32_t value) 
     if (value != -1 && value != 0 && value != 1) return DGADV_EINVAL;
     h->adjGraph = value;
   } else if (option == DGADV_OPT_ADJ_STREAMS) {
-    if (value != 1 && value != 2) return DGADV_EINVAL;
-    h->adjTwoStreams = value == 2;
+    if (value < 1 || value > 3) return DGADV_EINVAL;
+    h->adjStreams = value;
   } else if (option == DGADV_OPT_TAYLOR_MASS) {
     if (value != 0 && value != 1) return DGADV_EINVAL;
     h->mtOnTheFly = value == 1;
@@ -810,7 +810,7 @@ extern "C" int dgadv_get_option(const dgadv_handle *h, int32_t option, int32_t *
   else if (option == DGADV_OPT_FLAGS) *value = h->flags;
   else if (option == DGADV_OPT_PERSIST_BLOCKS) *value = h->persistPerSM;
   else if (option == DGADV_OPT_ADJ_WARPS) *value = h->adjWarps;
-  else if (option == DGADV_OPT_ADJ_STREAMS) *value = h->adjTwoStreams ? 2 : 1;
+  else if (option == DGADV_OPT_ADJ_STREAMS) *value = h->adjStreams;
   else if (option == DGADV_OPT_ADJ_GRAPH) *value = h->adjGraph < 0 ? (h->lim ? 0 : 1) : h->adjGraph;
   else if (option == DGADV_OPT_ELEMENT_OPERATOR) *value = (h->elemOp && ops(h).build_element_operator) ? 1 : 0;
   else if (option == DGADV_OPT_TAYLOR_MASS) *value = h->mtOnTheFly ? 1 : 0;
@@ -950,8 +950,14 @@ extern "C" void dgadv_destroy(dgadv_handle *h) {
     cudaStreamSynchronize(h->adjStreamF);
     cudaStreamDestroy(h->adjStreamF);
   }
+  if (h->adjStreamA) {
+    cudaStreamSynchronize(h->adjStreamA);
+    cudaStreamDestroy(h->adjStreamA);
+  }
   if (h->adjFEv) cudaEventDestroy(h->adjFEv);
   for (cudaEvent_t e : h->adjRevEv) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->adjTapeEv) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->adjBufEv) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (void *p : h->allocs) cudaFree(p);

@@ -88,11 +88,16 @@ enum {
                                    flux, mass) in FP32 arithmetic while the state, the SSP
                                    update and the limiter stay double-float; 0 (default): all
                                    double-float                                              */
-  DGADV_OPT_ADJ_STREAMS = 9,    /* streams of a reverse sweep that recomputes: 2 (default) runs
-                                   the recomputation on a second stream, one reversed step
-                                   ahead of the reverse stages (one more set of work states and
-                                   limiter records, allocated by dgadv_forward_record); 1: one
-                                   stream.  Gradients bitwise unchanged                        */
+  DGADV_OPT_ADJ_STREAMS = 9,    /* streams of a reverse sweep that recomputes: 3 (default) runs
+                                   the recomputation of the reversed steps on a second stream,
+                                   one reversed step ahead of the reverse stages, and the
+                                   advances between checkpoints on a third, with checkpoint
+                                   slots renamed so that an advance need not wait for the slot
+                                   the schedule reuses; 2: recomputation and advances on one
+                                   second stream; 1: one stream.  2 and 3 take one and two more
+                                   sets of work states and limiter records (and with 3 the
+                                   limiter's key sets), allocated by dgadv_forward_record.
+                                   Gradients bitwise unchanged                                 */
   DGADV_OPT_ELEMENT_OPERATOR = 10, /* FP64 and double-float handles without source terms (and,
                                    double-float, without the FP32 operator): 1 (default) keeps the
                                    stage operator's volume term and the element's own outflow
@@ -373,12 +378,14 @@ const char *dgadv_status_string(int status);
 void dgadv_destroy(dgadv_handle *h);
 
 /* ---- discrete adjoint ------------------------------------------------------------------
- * Gradients of a functional J(c(T)) of the final state of an unlimited run with respect to the
- * initial coefficients and to the coefficients theta of a velocity u = sum_m theta_m u_m.  The
- * reference has no adjoint; these follow the torch.autograd.Function contract (forward records,
- * backward maps dJ/dc(T) to the input gradients).  The upwind choice is frozen at the recorded
- * velocity (the flux is piecewise linear in u); right-hand-side vectors set with
- * dgadv_set_source_terms are treated as independent of theta. */
+ * Gradients of a functional J(c(T)) of the final state of an explicit run (unlimited, or with
+ * the linear or the hierarchical vertex-based limiter) with respect to the initial coefficients
+ * and to the coefficients theta of a velocity u = sum_m theta_m u_m.  The reference has no
+ * adjoint; these follow the torch.autograd.Function contract (forward records, backward maps
+ * dJ/dc(T) to the input gradients).  The upwind choice is frozen at the recorded velocity (the
+ * flux is piecewise linear in u), and so are the limiters' choices (which vertex bound and which
+ * order is active): the gradient is that of the piecewise-smooth map on the recorded piece.
+ * Right-hand-side vectors set with dgadv_set_source_terms are treated as independent of theta. */
 
 /* Velocity modes u_m, each given like dgadv_set_velocity: u1Modes, u2Modes K x N x nModes,
  * vNModes K x 3 x R x nModes. */
@@ -391,7 +398,7 @@ int dgadv_set_velocity_theta(dgadv_handle *h, const double *theta);
  * recomputation; nSteps x ordRK state-sized buffers); nSnapshots >= nSteps keeps every step
  * state (each reversed step recomputes its stages); otherwise nSnapshots states are placed by
  * binomial checkpointing.  The final state is then the handle's state (dgadv_get_state).
- * DGADV_EUNSUPPORTED with the limiter on or in DF32. */
+ * DGADV_EUNSUPPORTED with the strict limiter, with DGADV_FLAG_IMPLICIT, or in DF32. */
 int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau, int32_t nSnapshots);
 /* Reverse sweep of the last recorded run: dJdcT (K x N) in, dJdc0 (K x N, may be NULL) and
  * dJdtheta (nModes, may be NULL) out.  Recomputes what was not stored; the handle's state is

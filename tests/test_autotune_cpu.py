@@ -16,7 +16,7 @@ class FakeSolver:
     def __init__(self, cost):
         self.cost = cost
         self.options = {L.OPT_FLAGS: 0, L.OPT_GRAPH_STEPS: 12, L.OPT_ADJ_WARPS: 2, L.OPT_OP_BLOCK: 128,
-                        L.OPT_TAYLOR_MASS: 1, L.OPT_ADJ_GRAPH: 1, L.OPT_ADJ_STREAMS: 2}
+                        L.OPT_TAYLOR_MASS: 1, L.OPT_ADJ_GRAPH: 1, L.OPT_ADJ_STREAMS: 3}
         self.state = np.arange(12.0).reshape(4, 3)
         self.calls = []
 
@@ -54,24 +54,25 @@ def test_tune_adjoint_times_every_width_and_applies_the_fastest(monkeypatch):
     _now[0] = 0.0
     monkeypatch.setattr(AT.time, 'perf_counter', lambda: _now[0])
     costs = {1: 3.0, 2: 1.0, 4: 5.0}
-    # the sweep launched directly (adjGraph 0) is faster here
-    s = FakeSolver(lambda o: costs[o[L.OPT_ADJ_WARPS]] * (0.5 if o[L.OPT_ADJ_GRAPH] == 0 else 1.0))
+    # the sweep launched directly (adjGraph 0) is faster here, and three streams
+    s = FakeSolver(lambda o: costs[o[L.OPT_ADJ_WARPS]] * (0.5 if o[L.OPT_ADJ_GRAPH] == 0 else 1.0)
+                   * (1.0 if o[L.OPT_ADJ_STREAMS] == 3 else 1.5))
     before = s.get_state()
     best, table = AT.tune_adjoint(s, 1e-3, nSteps=4, nSnapshots=2, reps=2)
     assert [r['adjWarps'] for r in table if 'adjGraph' not in r] == [1, 2, 4]
     assert best['adjWarps'] == 2 and s.get_option(L.OPT_ADJ_WARPS) == 2
-    # then the other sweep form on the best width, then the other stream count (no faster here)
-    assert table[-2]['adjWarps'] == 2 and table[-2]['adjGraph'] == 0
-    assert abs(table[-2]['ms_backward'] - 0.5) < 1e-9
+    # then the other sweep form on the best width, then the other stream counts (no faster here)
+    assert table[-3]['adjWarps'] == 2 and table[-3]['adjGraph'] == 0
+    assert abs(table[-3]['ms_backward'] - 0.5) < 1e-9
     assert best['adjGraph'] == 0 and s.get_option(L.OPT_ADJ_GRAPH) == 0
-    assert table[-1]['adjStreams'] == 1
-    assert best['adjStreams'] == 2 and s.get_option(L.OPT_ADJ_STREAMS) == 2
+    assert [r['adjStreams'] for r in table[-2:]] == [1, 2]
+    assert best['adjStreams'] == 3 and s.get_option(L.OPT_ADJ_STREAMS) == 3
     assert np.array_equal(s.get_state(), before)
     # every width: reps + 1 recorded runs (the first captures the sweep's graph), each with the
-    # requested snapshots, and a backward after each; the best width three times (both sweep
-    # forms, then the other stream count)
+    # requested snapshots, and a backward after each; the best width four times (both sweep
+    # forms, then the two other stream counts)
     for w in (1, 2, 4):
-        n = 9 if w == 2 else 3
+        n = 12 if w == 2 else 3
         assert s.calls.count(('record', w, 2)) == n
         assert s.calls.count(('backward', w)) == n
 

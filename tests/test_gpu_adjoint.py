@@ -280,12 +280,12 @@ STREAM_CASES = [dict(precision='fp32', kw=dict(hmax=2 ** -4, p=2, numSteps=24, t
 
 
 @pytest.mark.parametrize('case', STREAM_CASES, ids=['unlimited-p2', 'linear-p1', 'linear-p2', 'hier-p3'])
-def test_two_stream_sweep_equals_one_stream_sweep(lib, case):
+def test_stream_sweeps_equal_one_stream_sweep(lib, case):
     """DGADV_OPT_ADJ_STREAMS: the recomputation and the limiter adjoint's scatters on a second
-    stream, one reversed step ahead of the reverse stages, give bitwise the gradients of one
-    stream; DGADV_OPT_ADJ_GRAPH: the sweep captured in a graph (and replayed) or launched
-    directly gives the same bits; with every stage stored and for binomial and every-state
-    checkpoints."""
+    stream, one reversed step ahead of the reverse stages, and the advances between checkpoints
+    on a third (with renamed checkpoint slots), give bitwise the gradients of one stream;
+    DGADV_OPT_ADJ_GRAPH: the sweep captured in a graph (and replayed) or launched directly gives
+    the same bits; with every stage stored and for binomial and every-state checkpoints."""
     from festung_gb300 import _lib as L
     from festung_gb300 import adjoint as AD
     kw = case['kw']
@@ -295,10 +295,10 @@ def test_two_stream_sweep_equals_one_stream_sweep(lib, case):
     tg.solver.close()
     pd = AD.setup(precision=case['precision'], **kw)
     try:
-        assert pd.solver.get_option(L.OPT_ADJ_STREAMS) == 2
+        assert pd.solver.get_option(L.OPT_ADJ_STREAMS) == 3
         c0 = np.asfortranarray(pd._cDisc)
         ref = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=0)
-        for streams in (1, 2):
+        for streams in (1, 2, 3):
             pd.solver.set_option(L.OPT_ADJ_STREAMS, streams)
             for graph in (1, 0):                  # the sweep as one CUDA graph, or launched directly
                 pd.solver.set_option(L.OPT_ADJ_GRAPH, graph)
