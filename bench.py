@@ -428,10 +428,11 @@ def adjoint_block(reps=3, fd_dirs=16):
     rel = lambda a, b: float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
     out['fp32_vs_fp64_grad_rel_l2'] = {'dJdc0': rel(grads['fp32'][0], grads['fp64'][0]),
                                        'dJdtheta': rel(grads['fp32'][1], grads['fp64'][1])}
-    # the same workload with the linear and with the hierarchical vertex limiter on (the adjoint
-    # through the limiter's choices)
+    # the same workload with the linear, the hierarchical vertex and the strict limiter on (the
+    # adjoint through the limiter's choices)
     out['linear_limiter'] = limited_adjoint_rows(AD, kw, reps, fd_dirs, 'linear')
     out['hierarchical_limiter'] = limited_adjoint_rows(AD, kw, reps, fd_dirs, 'hierarch_vert')
+    out['strict_limiter'] = limited_adjoint_rows(AD, kw, reps, fd_dirs, 'strict')
     return out
 
 

@@ -493,9 +493,9 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
           std::memset(&v, 0, sizeof(v));
           gcoBC(s, v.gco);
           const char *Cd = recCd(s);
-          if (h->limType == DGADV_LIM_HIERARCH_VERT) {
-            // hierarchical limiter (inputs recorded in Taylor form): per limiter its scatter
-            // (unless the recomputation stream made it), its pass and its gather
+          if (h->limType != DGADV_LIM_LINEAR) {
+            // hierarchical and strict limiter (inputs recorded in Taylor form): per limiter its
+            // scatter (unless the recomputation stream made it), its pass and its gather
             if (!pre) DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
             v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
             DG_CUDA(o.lim_vjp(h, v));
@@ -772,10 +772,6 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
   const PrecOps &o = ops_of(h);
   if (!o.adj_stage) { h->err = "no adjoint kernels for this precision"; return DGADV_EUNSUPPORTED; }
   if (h->flags & DGADV_FLAG_IMPLICIT) { h->err = "the adjoint covers the explicit scheme"; return DGADV_EUNSUPPORTED; }
-  if (h->lim && h->limType == DGADV_LIM_STRICT) {
-    h->err = "the adjoint covers the unlimited scheme, the linear and the hierarchical vertex limiter";
-    return DGADV_EUNSUPPORTED;
-  }
   DG_CUDA(cudaSetDevice(h->device));
   const int nSlots = (nSnapshots <= 0 || nSnapshots >= nSteps) ? nSteps : nSnapshots;
   const size_t bytes = (size_t)h->N * h->Kp * o.realBytes;
@@ -819,7 +815,7 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
     if (!h->tmpY) {
       // per pass nc quantities (1 linear, p(p+1)/2 hierarchical); records: per CSR position one
       // (linear) or one per order (hierarchical)
-      const size_t nq = (size_t)h->nc, perPos = h->limType == DGADV_LIM_HIERARCH_VERT ? (size_t)h->p : 1;
+      const size_t nq = (size_t)h->nc, perPos = h->limType == DGADV_LIM_LINEAR ? 1 : (size_t)h->p;
       if ((st = dev_alloc(h, &h->tmpY, bytes))) return st;
       if ((st = dev_alloc(h, &h->tmpD, bytes))) return st;
       for (int r = 0; r < 2; ++r) {

@@ -1269,6 +1269,234 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
       }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Adjoint of the strict limiter (core/applySlopeLimiterTaylorStrict.m:111-150), on Taylor
+// coefficients.  The forward limits the orders ord = P..1 in turn, each on the data the higher
+// orders already limited: y^(P+1) = x, and y^(ord) is y^(ord+1) with every DOF of degree >= ord
+// scaled by alpha_ord, the minimum over the order's sub-limiters and vertices of the factor of
+// core/computeVertexBasedLimiter.m:78-106.  A sub-limiter's vertex values are the degree
+// (P - ord + 1) reconstruction from y^(ord+1) about a derivative of order ord - 1, x[i0], which
+// no higher order has rescaled (so its patch extremes are those of the hierarchical limiter's
+// quantities).  With the choices frozen and lambda = dJ/dy^(1), the orders are reversed,
+// ord = 1..P, on ybar = dJ/dy^(ord):
+//   S_ord = sum over the DOFs j of degree >= ord of ybar_j y^(ord+1)_j     (dJ/dalpha_ord)
+//   ybar_j <- alpha_ord ybar_j on those DOFs
+//   and on an unsaturated branch S_ord spread, as the derivatives of dm / den, over x[i0]
+//   (dm = ext - x[i0]), the reconstruction's DOFs (den = v_n - x[i0] -+ tol) and the extreme
+//   (another element's x[i0], recorded as for the hierarchical limiter, or the element's own
+//   vertex value at a Dirichlet vertex above order 1).
+// The forward's factor itself (vertex_alpha_1div, minimum over the sub-limiters) is recomputed
+// as the forward computes it, so that y^(ord) is bitwise the forward's; the winner's ratio
+// dm / den gives the derivative.
+template <typename T, int P> struct StrictWin {
+  T raw, den, dm;
+  int act;       // the factor is raw, on a branch and strictly inside (0, 1)
+  int i, n, s;   // sub-limiter, vertex and quantity of the winner
+  int src;       // extreme: 0 another element (recorded), 1 the element's own vertex value, 2 data
+  int tgt;       // element holding the extreme (src 0)
+  int vtx;       // the winning vertex (a global vertex id) and its extreme's key
+  typename KeyOf<T>::type key;
+};
+
+template <typename T, int P, int KIND>
+__global__ void __launch_bounds__(kBlock)
+k_lim_vjp_strict(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, const LimIn<T> li,
+                 const StageScalars sc, double scale, const T *__restrict__ qStore, const int *__restrict__ csrPos,
+                 int nnz, int *__restrict__ slotT, T *__restrict__ slotW) {
+  constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
+  __shared__ T sh[2 * NQ];
+  const int k = blockIdx.x * kBlock + threadIdx.x;
+  pdl_trigger();
+  const bool active = k < g.K;
+  const int Kp = g.Kp;
+  int vid[3] = {0, 0, 0}, pos[3] = {-1, -1, -1}, dmask = 0;
+  T B[4] = {T(1), T(0), T(0), T(1)};
+  if (active) {
+    vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
+    pos[0] = csrPos[k]; pos[1] = csrPos[Kp + k]; pos[2] = csrPos[2 * Kp + k];
+    dmask = (g.code[k] >> 9) & 7;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) B[r] = g.Bm[(size_t)r * Kp + k];
+  }
+  T data[3] = {T(0), T(0), T(0)};
+  if (KIND == 0 && g.cDV0T && active)
+    for (int m = 0; m < g.nTerms; ++m) {
+      const T gm = T(sc.gco[m]);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) data[n] += gm * g.cDV0T[((size_t)m * 3 + n) * Kp + k];
+    }
+  pdl_wait();
+  if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
+  T xv[N], lam[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    xv[i] = active ? x[(size_t)i * Kp + k] : T(0);
+    lam[i] = active ? T(scale) * lamIn[(size_t)i * Kp + k] : T(0);
+  }
+  VKeys<T, NQ> kv;
+  load_vkeys<T, NQ>(g, li, vid, kv);
+  __syncthreads();
+  if (!active) return;
+  const Affine<T> af = affine_from<T>(B[0], B[1], B[2], B[3]);
+  SinvBlocks<T, P> si;
+  sinv_blocks<T, P>(af, si);
+  T mu[N], lamL[N], mc[N];
+  taylor_Tinv_transpose<T, P>(si, lam, mu);
+  if (KIND == 1) {
+    mcorr_transpose<T, P>(g, k, si, mu, mc);
+#pragma unroll
+    for (int i = 0; i < N; ++i) lamL[i] = mu[i] - mc[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) lamL[i] = mu[i];
+  }
+  // the forward's orders (limit_taylor, LT = 2), with the winners recorded
+  const T tol = T(1.e-8), nan_ = T(NAN);
+  T phi[3][N];
+  taylor_vertex_basis<T, P>(af, phi);
+  StrictWin<T, P> win[P + 1];
+  T alpha[P + 1];
+  T y[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) y[i] = xv[i];
+  int s = 0;
+#pragma unroll
+  for (int ord = P; ord >= 1; --ord) {
+    RatioWin<T> rw;   // the order's winner, compared without dividing
+    StrictWin<T, P> &w = win[ord];
+    w.act = 0; w.src = 2; w.tgt = -1; w.i = 1; w.n = 0; w.s = 0; w.vtx = 0; w.key = 0;
+    w.raw = w.den = w.dm = T(0);
+    T aOrd = T(1);
+#pragma unroll
+    for (int i = 1; i <= ord; ++i) {
+      const int ba = ord - i, bb = i - 1, i0 = mind(ba, bb);
+      T v[3], valD[3], mn[3], mx[3];
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        T acc = T(0);
+#pragma unroll
+        for (int a = 0; a <= P - ord + 1; ++a)
+#pragma unroll
+          for (int b = 0; a + b <= P - ord + 1; ++b) acc = acc + y[mind(ba + a, bb + b)] * phi[n][mind(a, b)];
+        v[n] = acc;
+        valD[n] = ((dmask >> n) & 1) ? (ord > 1 ? v[n] : (KIND == 0 ? data[n] : nan_)) : nan_;
+      }
+      patch_minmax<T, NQ>(li, kv, sh, s, valD, mn, mx);
+      aOrd = fmin(aOrd, vertex_alpha_1div(y[i0], v, mn, mx));
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        const T cbar = y[i0];
+        const T dV = v[n] - cbar, dMin = mn[n] - cbar, dMax = mx[n] - cbar;
+        T den = T(0), dm = T(0);
+        int br = 0;
+        if (dV < dMin + tol) { den = dV - tol; dm = dMin; br = 1; }
+        if (dV > dMax - tol) { den = dV + tol; dm = dMax; br = 2; }
+        if (br != 0 && rw.offer(dm, den)) {   // the first (sub-limiter, vertex) reaching the order's minimum
+          w.den = den; w.dm = dm;
+          w.i = i; w.n = n; w.s = s;
+          // the extreme's source: the Dirichlet value (which wins a tie) or the patch element
+          const bool isPos = br == 2;
+          const T rawExt = vkey_inv<T>(kv.v[s][isPos ? 1 : 0][n]);
+          const bool hasD = ((dmask >> n) & 1) && !(valD[n] != valD[n]);
+          const bool fromD = hasD && (isPos ? !(valD[n] < rawExt) : !(valD[n] > rawExt));
+          w.src = fromD ? (ord > 1 ? 1 : 2) : 0;
+          w.tgt = -1;
+          w.vtx = vid[n];
+          w.key = kv.v[s][isPos ? 1 : 0][n];
+        }
+      }
+      ++s;
+    }
+    if (rw.cls < 2) {
+      w.raw = w.dm / w.den;
+      w.act = w.raw > T(0) && w.raw < T(1);
+    }
+    if (w.src == 0 && w.act) {   // the element holding the winner's extreme (lowest original id)
+      const auto key = w.key;
+      int best = -1, bestId = 0x7fffffff;
+      const int e0 = g.vptr[w.vtx], e1 = g.vptr[w.vtx + 1];
+      for (int e = e0; e < e1; ++e) {
+        const int k2 = g.vidx[e];
+        if (vkey(qStore[(size_t)w.s * Kp + k2]) == key && g.permv[k2] < bestId) { best = k2; bestId = g.permv[k2]; }
+      }
+      w.tgt = best;
+    }
+    alpha[ord] = aOrd;
+#pragma unroll
+    for (int j = ord * (ord + 1) / 2; j < N; ++j) y[j] = aOrd * y[j];
+  }
+  // the orders reversed: gx = dJ/dy^(ord) on entry to order ord, dJ/dx at the end
+  T gx[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) gx[i] = lamL[i];
+  int recT[P + 1];
+  T recW[P + 1];
+#pragma unroll
+  for (int o = 1; o <= P; ++o) { recT[o] = -1; recW[o] = T(0); }
+#pragma unroll
+  for (int ord = 1; ord <= P; ++ord) {
+    const int off = ord * (ord + 1) / 2;
+    // y^(ord+1): x rescaled by the orders above ord, in the forward's order
+    T yp[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) yp[j] = xv[j];
+#pragma unroll
+    for (int o = P; o > ord; --o)
+#pragma unroll
+      for (int j = o * (o + 1) / 2; j < N; ++j) yp[j] = alpha[o] * yp[j];
+    Acc<T> so(T(0));
+#pragma unroll
+    for (int j = off; j < N; ++j) so.fma(yp[j], gx[j]);
+#pragma unroll
+    for (int j = off; j < N; ++j) gx[j] = alpha[ord] * gx[j];
+    const StrictWin<T, P> &w = win[ord];
+    if (!w.act) continue;
+    const T So = so.get();
+    const T q = So / w.den, r = So * w.dm / (w.den * w.den);
+#pragma unroll
+    for (int i = 1; i <= ord; ++i) {
+      if (i != w.i) continue;
+      const int ba = ord - i, bb = i - 1, i0 = mind(ba, bb);
+      // dm = ext - x[i0]; den = (reconstruction at vertex n) - x[i0] -+ tol, whose x[i0] terms cancel
+      gx[i0] = gx[i0] - q;
+#pragma unroll
+      for (int a = 0; a <= P - ord + 1; ++a)
+#pragma unroll
+        for (int b = 0; a + b <= P - ord + 1; ++b) {
+          if (a + b == 0) continue;
+          const int m = mind(a, b), j = mind(ba + a, bb + b);
+          const T ph = w.n == 0 ? phi[0][m] : (w.n == 1 ? phi[1][m] : phi[2][m]);
+          gx[j] = gx[j] - r * ph;
+          if (w.src == 1) gx[j] = gx[j] + q * ph;   // ext = the element's own vertex value
+        }
+      if (w.src == 1) gx[i0] = gx[i0] + q;
+      else if (w.src == 0 && w.tgt >= 0) {        // ext = x[i0] of another element (or this one)
+        recT[ord] = w.tgt * 16 + i0;
+        recW[ord] = q;
+      }
+    }
+  }
+  if (KIND == 1) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) gx[i] = gx[i] + mc[i];
+  }
+  T out[N];
+  SBlocks<T, P> sb;
+  s_blocks<T, P>(af, sb);
+  taylor_T_transpose<T, P>(sb, gx, out);
+#pragma unroll
+  for (int i = 0; i < N; ++i) lamOut[(size_t)i * Kp + k] = out[i];
+#pragma unroll
+  for (int o = 1; o <= P; ++o)
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      if (pos[n] >= 0) {
+        const bool mine = win[o].n == n && recT[o] >= 0;
+        slotT[(size_t)(o - 1) * nnz + pos[n]] = mine ? recT[o] : -1;
+        if (mine) slotW[(size_t)(o - 1) * nnz + pos[n]] = recW[o];
+      }
+}
+
 // Gathers the recorded extreme terms: element e adds w T^T e_i for every record (e, i, w) in the
 // slots of its vertex patches (CSR order: deterministic).
 template <typename T, int P>
@@ -1324,17 +1552,16 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
   StageScalars sc{};
   sc.flag = h->flag;
   for (int m = 0; m < h->nTerms; ++m) sc.gco[m] = v.gco[m];
-  if (h->limType == DGADV_LIM_HIERARCH_VERT) {   // one pass and its gather, P records per position
+  if (h->limType != DGADV_LIM_LINEAR) {   // one pass and its gather, P records per position
     int *rT = h->recSlotT[v.kind];
     T *rW = (T *)h->recSlotW[v.kind];
     const T *q = adj_means<T>(h, v.pass);
     const int nnz = 3 * h->K;
-    if (v.kind == 0)
-      launch_k(h, k_lim_vjp_hier<T, P, 0>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn,
-               (T *)v.lamOut, lim_in_adj<T>(h, v.pass), sc, v.scale, q, (const int *)h->csrPos, nnz, rT, rW);
-    else
-      launch_k(h, k_lim_vjp_hier<T, P, 1>, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn,
-               (T *)v.lamOut, lim_in_adj<T>(h, v.pass), sc, v.scale, q, (const int *)h->csrPos, nnz, rT, rW);
+    const bool strict = h->limType == DGADV_LIM_STRICT;
+    auto kern = strict ? (v.kind == 0 ? k_lim_vjp_strict<T, P, 0> : k_lim_vjp_strict<T, P, 1>)
+                       : (v.kind == 0 ? k_lim_vjp_hier<T, P, 0> : k_lim_vjp_hier<T, P, 1>);
+    launch_k(h, kern, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn, (T *)v.lamOut,
+             lim_in_adj<T>(h, v.pass), sc, v.scale, q, (const int *)h->csrPos, nnz, rT, rW);
     launch_k(h, k_lim_vjp_hier_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, nnz, (const int *)rT,
              (const T *)rW);
     return cudaGetLastError();
@@ -1408,7 +1635,7 @@ static cudaError_t launch_vjp_scatter(dgadv_handle *h, const void *x, long long 
   const Geo<T> g = make_geo<T>(h);
   const int grid = (std::max(h->K, h->numV) + kBlock - 1) / kBlock;
   T *q = adj_means<T>(h, pass);
-  if (h->limType == DGADV_LIM_HIERARCH_VERT)
+  if (h->limType != DGADV_LIM_LINEAR)   // the hierarchical and the strict limiter's quantities
     launch_k(h, k_vjp_scatter_hier<T, P>, grid, (size_t)0, g, (const T *)x, lim_out_adj<T>(h, pass), q);
   else
     launch_k(h, k_mean_lin<T, P>, grid, (size_t)0, g, (const T *)x, lim_out_adj<T>(h, pass), q);

@@ -379,12 +379,13 @@ void dgadv_destroy(dgadv_handle *h);
 
 /* ---- discrete adjoint ------------------------------------------------------------------
  * Gradients of a functional J(c(T)) of the final state of an explicit run (unlimited, or with
- * the linear or the hierarchical vertex-based limiter) with respect to the initial coefficients
- * and to the coefficients theta of a velocity u = sum_m theta_m u_m.  The reference has no
- * adjoint; these follow the torch.autograd.Function contract (forward records, backward maps
- * dJ/dc(T) to the input gradients).  The upwind choice is frozen at the recorded velocity (the
- * flux is piecewise linear in u), and so are the limiters' choices (which vertex bound and which
- * order is active): the gradient is that of the piecewise-smooth map on the recorded piece.
+ * the linear, the hierarchical vertex-based or the strict limiter) with respect to the initial
+ * coefficients and to the coefficients theta of a velocity u = sum_m theta_m u_m.  The
+ * reference has no adjoint; these follow the torch.autograd.Function contract (forward
+ * records, backward maps dJ/dc(T) to the input gradients).  The upwind choice is frozen at the
+ * recorded velocity (the flux is piecewise linear in u), and so are the limiters' choices
+ * (which vertex bound and which order is active): the gradient is that of the
+ * piecewise-smooth map on the recorded piece.
  * Right-hand-side vectors set with dgadv_set_source_terms are treated as independent of theta. */
 
 /* Velocity modes u_m, each given like dgadv_set_velocity: u1Modes, u2Modes K x N x nModes,
@@ -398,7 +399,7 @@ int dgadv_set_velocity_theta(dgadv_handle *h, const double *theta);
  * recomputation; nSteps x ordRK state-sized buffers); nSnapshots >= nSteps keeps every step
  * state (each reversed step recomputes its stages); otherwise nSnapshots states are placed by
  * binomial checkpointing.  The final state is then the handle's state (dgadv_get_state).
- * DGADV_EUNSUPPORTED with the strict limiter, with DGADV_FLAG_IMPLICIT, or in DF32. */
+ * DGADV_EUNSUPPORTED with DGADV_FLAG_IMPLICIT or in DF32. */
 int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau, int32_t nSnapshots);
 /* Reverse sweep of the last recorded run: dJdcT (K x N) in, dJdc0 (K x N, may be NULL) and
  * dJdtheta (nModes, may be NULL) out.  Recomputes what was not stored; the handle's state is
