@@ -442,12 +442,14 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
         return h->adjRecCdot ? (const char *)h->adjRecCdot + ((size_t)arg * S + s) * bytes
                              : (const char *)ws.scrCdot + (size_t)s * bytes;
       };
-      // Several streams with the limiter and every stage stored: the scatters of the limiter
-      // inputs' means to the adjoint's key sets do not depend on the adjoint variable, so they
-      // run on the recomputation stream, in the reverse stages' pass order; their key sets were
-      // last read two reversed steps ago (when the sweep recomputes, the recomputation already
-      // keeps that stream the busier one)
-      const bool pre = L.two && h->lim && stages;
+      // With the limiter and every stage stored, or with the hierarchical or strict limiter on
+      // three streams: the scatters of the limiter inputs' quantities to the adjoint's key sets
+      // do not depend on the adjoint variable, so they run on the recomputation stream (after
+      // the step's recomputation), in the reverse stages' pass order; their key sets were last
+      // read two reversed steps ago.  (Measured with 20 snapshots on three streams: the
+      // hierarchical and strict sweeps gain 8-10 %, the linear one, whose choices would move
+      // too, loses 15-25 %; with two streams the advances keep that stream the busier one.)
+      const bool pre = L.two && h->lim && (stages || (L.n == 3 && h->limType != DGADV_LIM_LINEAR));
       // the linear limiter's choices too (k_lim_choice), leaving the reverse stream k_lim_apply
       const bool preChoice = pre && h->limType == DGADV_LIM_LINEAR && h->adjChoice;
       // time factors of the Dirichlet data at the solution limiter of stage s
