@@ -500,6 +500,7 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
             // scatter (unless the recomputation stream made it), its pass and its gather
             if (!pre) DG_CUDA(o.vjp_scatter(h, Y, h->adjPass, 0));
             v.kind = 0; v.x = Y; v.lamIn = muNext; v.lamOut = h->tmpY; v.scale = 1.0; v.pass = h->adjPass++;
+            v.gatherOut = h->limdot ? 0 : 1;   // else gathered by the time-derivative limiter's pass
             DG_CUDA(o.lim_vjp(h, v));
             muY = h->tmpY;
             if (h->limdot) {
@@ -508,6 +509,8 @@ int run_actions(dgadv_handle *h, size_t from, size_t to, Cursor &w, Lanes &L) {
               std::memset(&d, 0, sizeof(d));
               d.kind = 1; d.x = Cd; d.lamIn = h->tmpY; d.lamOut = h->tmpD; d.scale = (1.0 - omega[s]) * tau;
               d.pass = h->adjPass++;
+              d.gatherIn = 1;
+              d.gatherOut = 1;
               DG_CUDA(o.lim_vjp(h, d));
               mp = h->tmpD;
             }

@@ -1074,6 +1074,62 @@ k_vjp_scatter_hier(const Geo<T> g, const T *x, const LimOut<T> lo, T *__restrict
   scatter_quantities<T, NQ>(g, lo, qv, vid, active);
 }
 
+// The records of element k in the slots of its three vertex patches (CSR order, every order o
+// at o * nnz + position), summed per Taylor index into acc; false if there are none.
+template <typename T, int P>
+__device__ __forceinline__ bool hier_records(const Geo<T> &g, int k, const int vid[3], int nnz, const int *slotT,
+                                             const T *slotW, T *acc) {
+  constexpr int N = Dims<P>::N;
+#pragma unroll
+  for (int j = 0; j < N; ++j) acc[j] = T(0);
+  bool any = false;
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    const int i0 = g.vptr[vid[n]], i1 = g.vptr[vid[n] + 1];
+    for (int i = i0; i < i1; ++i)
+#pragma unroll
+      for (int o = 0; o < P; ++o) {
+        const int t = slotT[(size_t)o * nnz + i];
+        if (t >= 0 && (t >> 4) == k) {
+          const int ti = t & 15;
+#pragma unroll
+          for (int j = 0; j < N; ++j)
+            if (j == ti) acc[j] = acc[j] + slotW[(size_t)o * nnz + i];
+          any = true;
+        }
+      }
+  }
+  return any;
+}
+
+// lamIn of a time-derivative limiter pass with the solution limiter's extreme terms gathered in
+// first (gInT != null; the sum is written back, as k_lim_vjp_hier_gather would have written it),
+// scaled: lam = scale (lamIn + T^T records).
+template <typename T, int P>
+__device__ __forceinline__ void hier_lam_in(const Geo<T> &g, int k, const int vid[3], int nnz, const int *gInT,
+                                            const T *gInW, T *lamInW, const SBlocks<T, P> &sb, const T *lraw,
+                                            double scale, T *lam) {
+  constexpr int N = Dims<P>::N;
+  const int Kp = g.Kp;
+  T v[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = lraw[i];
+  if (gInT) {
+    T acc[N];
+    if (hier_records<T, P>(g, k, vid, nnz, gInT, gInW, acc)) {
+      T add[N];
+      taylor_T_transpose<T, P>(sb, acc, add);
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        v[j] = v[j] + add[j];
+        lamInW[(size_t)j * Kp + k] = v[j];
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) lam[i] = T(scale) * v[i];
+}
+
 // The limiter adjoint of one pass (KIND 0 solution limiter, 1 time-derivative limiter).
 // slotT / slotW: P records per CSR position (order o at o * nnz + position), element * 16 +
 // Taylor index or -1, and the weight.
@@ -1081,7 +1137,8 @@ template <typename T, int P, int KIND>
 __global__ void __launch_bounds__(kBlock)
 k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, const LimIn<T> li,
                const StageScalars sc, double scale, const T *__restrict__ qStore, const int *__restrict__ csrPos,
-               int nnz, int *__restrict__ slotT, T *__restrict__ slotW) {
+               int nnz, int *__restrict__ slotT, T *__restrict__ slotW, const int *gInT, const T *gInW,
+               T *lamInW) {
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   __shared__ T sh[2 * NQ];
   const int k = blockIdx.x * kBlock + threadIdx.x;
@@ -1106,17 +1163,21 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
     }
   pdl_wait();
   if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
-  T xv[N], lam[N];
+  T xv[N], lraw[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
     xv[i] = active ? x[(size_t)i * Kp + k] : T(0);
-    lam[i] = active ? T(scale) * lamIn[(size_t)i * Kp + k] : T(0);
+    lraw[i] = active ? lamIn[(size_t)i * Kp + k] : T(0);
   }
   VKeys<T, NQ> kv;
   load_vkeys<T, NQ>(g, li, vid, kv);
   __syncthreads();
   if (!active) return;
   const Affine<T> af = affine_from<T>(B[0], B[1], B[2], B[3]);
+  SBlocks<T, P> sb;
+  s_blocks<T, P>(af, sb);
+  T lam[N];
+  hier_lam_in<T, P>(g, k, vid, nnz, KIND == 1 ? gInT : nullptr, gInW, lamInW, sb, lraw, scale, lam);
   SinvBlocks<T, P> si;
   sinv_blocks<T, P>(af, si);
   T mu[N], lamL[N], mc[N];
@@ -1253,8 +1314,6 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
     }
   }
   T out[N];
-  SBlocks<T, P> sb;
-  s_blocks<T, P>(af, sb);
   taylor_T_transpose<T, P>(sb, gx, out);
 #pragma unroll
   for (int i = 0; i < N; ++i) lamOut[(size_t)i * Kp + k] = out[i];
@@ -1302,7 +1361,8 @@ template <typename T, int P, int KIND>
 __global__ void __launch_bounds__(kBlock)
 k_lim_vjp_strict(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, const LimIn<T> li,
                  const StageScalars sc, double scale, const T *__restrict__ qStore, const int *__restrict__ csrPos,
-                 int nnz, int *__restrict__ slotT, T *__restrict__ slotW) {
+                 int nnz, int *__restrict__ slotT, T *__restrict__ slotW, const int *gInT, const T *gInW,
+               T *lamInW) {
   constexpr int N = Dims<P>::N, NQ = NCQ<P>::value;
   __shared__ T sh[2 * NQ];
   const int k = blockIdx.x * kBlock + threadIdx.x;
@@ -1327,17 +1387,21 @@ k_lim_vjp_strict(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lam
     }
   pdl_wait();
   if (li.shift) load_shifts<T>(li.slots + slot_base(g, li.nc), li.nc, sh);
-  T xv[N], lam[N];
+  T xv[N], lraw[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
     xv[i] = active ? x[(size_t)i * Kp + k] : T(0);
-    lam[i] = active ? T(scale) * lamIn[(size_t)i * Kp + k] : T(0);
+    lraw[i] = active ? lamIn[(size_t)i * Kp + k] : T(0);
   }
   VKeys<T, NQ> kv;
   load_vkeys<T, NQ>(g, li, vid, kv);
   __syncthreads();
   if (!active) return;
   const Affine<T> af = affine_from<T>(B[0], B[1], B[2], B[3]);
+  SBlocks<T, P> sb;
+  s_blocks<T, P>(af, sb);
+  T lam[N];
+  hier_lam_in<T, P>(g, k, vid, nnz, KIND == 1 ? gInT : nullptr, gInW, lamInW, sb, lraw, scale, lam);
   SinvBlocks<T, P> si;
   sinv_blocks<T, P>(af, si);
   T mu[N], lamL[N], mc[N];
@@ -1481,8 +1545,6 @@ k_lim_vjp_strict(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lam
     for (int i = 0; i < N; ++i) gx[i] = gx[i] + mc[i];
   }
   T out[N];
-  SBlocks<T, P> sb;
-  s_blocks<T, P>(af, sb);
   taylor_T_transpose<T, P>(sb, gx, out);
 #pragma unroll
   for (int i = 0; i < N; ++i) lamOut[(size_t)i * Kp + k] = out[i];
@@ -1508,32 +1570,12 @@ k_lim_vjp_hier_gather(const Geo<T> g, T *lam, int nnz, const int *slotT, const T
   if (k >= g.K) return;
   const int Kp = g.Kp;
   const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
-  int i0[3], i1[3];
-#pragma unroll
-  for (int n = 0; n < 3; ++n) { i0[n] = g.vptr[vid[n]]; i1[n] = g.vptr[vid[n] + 1]; }
   T B[4];
 #pragma unroll
   for (int r = 0; r < 4; ++r) B[r] = g.Bm[(size_t)r * Kp + k];
   pdl_wait();
   T acc[N];
-#pragma unroll
-  for (int j = 0; j < N; ++j) acc[j] = T(0);
-  bool any = false;
-#pragma unroll
-  for (int n = 0; n < 3; ++n)
-    for (int i = i0[n]; i < i1[n]; ++i)
-#pragma unroll
-      for (int o = 0; o < P; ++o) {
-        const int t = slotT[(size_t)o * nnz + i];
-        if (t >= 0 && (t >> 4) == k) {
-          const int ti = t & 15;
-#pragma unroll
-          for (int j = 0; j < N; ++j)
-            if (j == ti) acc[j] = acc[j] + slotW[(size_t)o * nnz + i];
-          any = true;
-        }
-      }
-  if (!any) return;
+  if (!hier_records<T, P>(g, k, vid, nnz, slotT, slotW, acc)) return;
   const Affine<T> af = affine_from<T>(B[0], B[1], B[2], B[3]);
   SBlocks<T, P> sb;
   s_blocks<T, P>(af, sb);
@@ -1560,10 +1602,16 @@ static cudaError_t launch_lim_vjp(dgadv_handle *h, const LimVjpArgs &v) {
     const bool strict = h->limType == DGADV_LIM_STRICT;
     auto kern = strict ? (v.kind == 0 ? k_lim_vjp_strict<T, P, 0> : k_lim_vjp_strict<T, P, 1>)
                        : (v.kind == 0 ? k_lim_vjp_hier<T, P, 0> : k_lim_vjp_hier<T, P, 1>);
+    // the time-derivative limiter's pass gathers the solution limiter's extreme terms into its
+    // input itself (gatherIn), in place of that pass's gather launch
+    const bool gin = v.kind == 1 && v.gatherIn;
     launch_k(h, kern, gridK, (size_t)0, g, (const T *)v.x, (const T *)v.lamIn, (T *)v.lamOut,
-             lim_in_adj<T>(h, v.pass), sc, v.scale, q, (const int *)h->csrPos, nnz, rT, rW);
-    launch_k(h, k_lim_vjp_hier_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, nnz, (const int *)rT,
-             (const T *)rW);
+             lim_in_adj<T>(h, v.pass), sc, v.scale, q, (const int *)h->csrPos, nnz, rT, rW,
+             gin ? (const int *)h->recSlotT[0] : (const int *)nullptr,
+             gin ? (const T *)h->recSlotW[0] : (const T *)nullptr, (T *)v.lamIn);
+    if (v.gatherOut)
+      launch_k(h, k_lim_vjp_hier_gather<T, P>, gridK, (size_t)0, g, (T *)v.lamOut, nnz, (const int *)rT,
+               (const T *)rW);
     return cudaGetLastError();
   }
   int *rT = h->recSlotT[v.kind];
