@@ -293,7 +293,11 @@ def fp64_peak(reps=5, n=4096):
 
 MEASURED_TRAFFIC = {('gauss_slot_131k_p2', 'fp32', 'k_stage_op'): 18.4e6,
                     ('gauss_slot_131k_p2', 'fp32', 'k_limit_dot'): 28.4e6,
-                    ('gauss_slot_131k_p2', 'fp32', 'k_limit'): 5.8e6}
+                    ('gauss_slot_131k_p2', 'fp32', 'k_limit'): 5.8e6,
+                    # FP64, element operator on (ncu, one cold launch each; dram read + write)
+                    ('gauss_slot_131k_p2', 'fp64', 'k_stage_op'): 58.5e6,
+                    ('gauss_slot_131k_p2', 'fp64', 'k_limit_dot'): 54.8e6,
+                    ('gauss_slot_131k_p2', 'fp64', 'k_limit'): 9.5e6}
 
 
 def large_block(device, flush):
@@ -898,8 +902,9 @@ def run_ours(args):
     value = world * units / (ms_per_step / 1e3)
     kern, roof = kernel_table(s, pd, 8, ms_per_step)
     roof['traffic'] = MEASURED_TRAFFIC.get((wl, 'fp64', roof['kernel']))
-    roof['note'] = ('L2-resident: the FP64 working set of this mesh (~60 MB) fits the 129 MB L2, so '
-                    'the bytes are served mostly from L2 once a solve runs; the FP64 kernels are bound '
+    roof['note'] = ('L2-resident: the bytes a FP64 stage touches on this mesh (about 120 MB cold per '
+                    'stage with the element operator, traffic) fit the 129 MB L2 for the most part, so '
+                    'they are served mostly from L2 once a solve runs; the FP64 kernels are bound '
                     'by GB300\'s FP64 rate, not by bandwidth (fp64_rate); the HBM-bound figure is hbm_case')
     # the bound that applies: the FP64 pipe, against cuBLAS DGEMM on the same GPU
     peak64 = fp64_peak()

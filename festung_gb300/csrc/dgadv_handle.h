@@ -128,7 +128,7 @@ struct dgadv_handle {
   void *adjRecY = nullptr, *adjRecCdot = nullptr;   // per step and stage (stage storage mode)
   void *adjScrY = nullptr, *adjScrCdot = nullptr;   // per stage (recomputing modes)
   // the reverse sweep's recomputation stream, its second buffer set (state, two stage states,
-  // S + S limiter records) and the events between the two streams (one per reversed step)
+  // S + S limiter records) and the events between the streams
   cudaStream_t adjStreamF = nullptr;
   void *adjSet1 = nullptr;
   size_t adjSet1States = 0;
@@ -152,8 +152,9 @@ struct dgadv_handle {
   void *recSlotW[2] = {nullptr, nullptr};
   int *csrPos = nullptr;                            // 3 x Kp: position of element k in patch V0T[n][k]
   // The adjoint's own vertex keys, global-extreme slots and element means of the limiter inputs,
-  // one set per pass modulo adjKeySets = 4S + 1: with two streams the scatters of a reversed
-  // step run on the recomputation stream while the reverse stages of the step before it run
+  // one set per pass modulo adjKeySets = 4S + 1: with several streams the scatters of a
+  // reversed step may run on the recomputation stream while the reverse stages of the step
+  // before it run
   void *adjMeans = nullptr;                         // adjKeySets x nc x Kp
   void *adjChoice = nullptr;                        // adjKeySets x Kp x (3 reals + 2 ints)
   void *vkeysA = nullptr;                           // adjKeySets x nc x 2 x Vp
