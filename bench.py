@@ -1053,7 +1053,9 @@ def main():
                     help='adjoint profiling case: hmax = 2^-e (9: 524288 triangles, 7: 32768)')
     ap.add_argument('--ncu-snapshots', type=int, default=0,
                     help='adjoint profiling case: checkpoint slots (0: every stage stored)')
-    ap.add_argument('--ncu-limited', action='store_true', help='adjoint profiling case: linear limiter on')
+    ap.add_argument('--ncu-limited', action='store_true', help='adjoint profiling case: limiter on')
+    ap.add_argument('--ncu-lim-type', default='linear', choices=['linear', 'hierarch_vert', 'strict'],
+                    help='adjoint profiling case: the limiter (with --ncu-limited)')
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64', 'df32'])
     ap.add_argument('--ncu-option', action='append', default=[],
                     help='profiling driver: DGADV_OPT_* option as NAME=VALUE (e.g. VOLUME_MMA=1)')
@@ -1062,7 +1064,8 @@ def main():
         # one recorded run and its reverse sweep (p = 2, hmax = 2^-e), for profiling
         from festung_gb300 import adjoint as AD
         pd = AD.setup(precision=args.precision, hmax=2.0 ** -args.ncu_hmax_exp, p=2, numSteps=args.ncu_steps,
-                      tEnd=args.ncu_steps * 2e-5, **({'isSlopeLim': True} if args.ncu_limited else {}))
+                      tEnd=args.ncu_steps * 2e-5,
+                      **({'isSlopeLim': True, 'typeSlopeLim': args.ncu_lim_type} if args.ncu_limited else {}))
         c0 = np.asfortranarray(pd._cDisc)
         AD.misfit_gradient(pd, c0, pd.theta, 0.9 * c0, nSnapshots=args.ncu_snapshots)
         pd.solver.close()

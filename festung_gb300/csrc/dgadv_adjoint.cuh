@@ -871,7 +871,8 @@ k_lim_vjp_gather(const Geo<T> g, T *lam, const int *slotT, const T *slotW) {
 template <typename T, int P> struct HierWin {
   T raw, den, dm;
   int act;       // the factor is raw, on a branch and strictly inside (0, 1)
-  int i0, i1, i2, n, s;
+  int n, s;      // the winning vertex and quantity
+  int si;        // the winning sub-limiter of the order (1..order)
   int src;       // extreme: 0 another element (recorded), 1 the element's own vertex value, 2 data
   int tgt;       // element holding the extreme (src 0)
   int vtx;       // the winning vertex (a global vertex id) and its extreme's key
@@ -1077,7 +1078,7 @@ k_vjp_scatter_hier(const Geo<T> g, const T *x, const LimOut<T> lo, T *__restrict
 // The records of element k in the slots of its three vertex patches (CSR order, every order o
 // at o * nnz + position), summed per Taylor index into acc; false if there are none.
 template <typename T, int P>
-__device__ __forceinline__ bool hier_records(const Geo<T> &g, int k, const int vid[3], int nnz, const int *slotT,
+__device__ __forceinline__ bool hier_records(int k, const int i0[3], const int i1[3], int nnz, const int *slotT,
                                              const T *slotW, T *acc) {
   constexpr int N = Dims<P>::N;
 #pragma unroll
@@ -1085,8 +1086,7 @@ __device__ __forceinline__ bool hier_records(const Geo<T> &g, int k, const int v
   bool any = false;
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
-    const int i0 = g.vptr[vid[n]], i1 = g.vptr[vid[n] + 1];
-    for (int i = i0; i < i1; ++i)
+    for (int i = i0[n]; i < i1[n]; ++i)
 #pragma unroll
       for (int o = 0; o < P; ++o) {
         const int t = slotT[(size_t)o * nnz + i];
@@ -1104,11 +1104,11 @@ __device__ __forceinline__ bool hier_records(const Geo<T> &g, int k, const int v
 
 // lamIn of a time-derivative limiter pass with the solution limiter's extreme terms gathered in
 // first (gInT != null; the sum is written back, as k_lim_vjp_hier_gather would have written it),
-// scaled: lam = scale (lamIn + T^T records).
+// scaled: lam = scale (lamIn + T^T records).  i0 / i1: the element's three CSR patch ranges.
 template <typename T, int P>
-__device__ __forceinline__ void hier_lam_in(const Geo<T> &g, int k, const int vid[3], int nnz, const int *gInT,
-                                            const T *gInW, T *lamInW, const SBlocks<T, P> &sb, const T *lraw,
-                                            double scale, T *lam) {
+__device__ __forceinline__ void hier_lam_in(const Geo<T> &g, int k, const int i0[3], const int i1[3], int nnz,
+                                            const int *gInT, const T *gInW, T *lamInW, const SBlocks<T, P> &sb,
+                                            const T *lraw, double scale, T *lam) {
   constexpr int N = Dims<P>::N;
   const int Kp = g.Kp;
   T v[N];
@@ -1116,7 +1116,7 @@ __device__ __forceinline__ void hier_lam_in(const Geo<T> &g, int k, const int vi
   for (int i = 0; i < N; ++i) v[i] = lraw[i];
   if (gInT) {
     T acc[N];
-    if (hier_records<T, P>(g, k, vid, nnz, gInT, gInW, acc)) {
+    if (hier_records<T, P>(k, i0, i1, nnz, gInT, gInW, acc)) {
       T add[N];
       taylor_T_transpose<T, P>(sb, acc, add);
 #pragma unroll
@@ -1146,11 +1146,16 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
   const bool active = k < g.K;
   const int Kp = g.Kp;
   int vid[3] = {0, 0, 0}, pos[3] = {-1, -1, -1}, dmask = 0;
+  int pr0[3] = {0, 0, 0}, pr1[3] = {0, 0, 0};   // patch ranges of the fused gather (KIND 1)
   T B[4] = {T(1), T(0), T(0), T(1)};
   if (active) {
     vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
     pos[0] = csrPos[k]; pos[1] = csrPos[Kp + k]; pos[2] = csrPos[2 * Kp + k];
     dmask = (g.code[k] >> 9) & 7;
+    if (KIND == 1 && gInT) {
+#pragma unroll
+      for (int n = 0; n < 3; ++n) { pr0[n] = g.vptr[vid[n]]; pr1[n] = g.vptr[vid[n] + 1]; }
+    }
 #pragma unroll
     for (int r = 0; r < 4; ++r) B[r] = g.Bm[(size_t)r * Kp + k];
   }
@@ -1177,7 +1182,7 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
   SBlocks<T, P> sb;
   s_blocks<T, P>(af, sb);
   T lam[N];
-  hier_lam_in<T, P>(g, k, vid, nnz, KIND == 1 ? gInT : nullptr, gInW, lamInW, sb, lraw, scale, lam);
+  hier_lam_in<T, P>(g, k, pr0, pr1, nnz, KIND == 1 ? gInT : nullptr, gInW, lamInW, sb, lraw, scale, lam);
   SinvBlocks<T, P> si;
   sinv_blocks<T, P>(af, si);
   T mu[N], lamL[N], mc[N];
@@ -1204,9 +1209,8 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
 #pragma unroll
   for (int ord = P; ord >= 1; --ord) {
     RatioWin<T> rw;   // the order's winner, compared without dividing
-    win[ord].act = 0; win[ord].src = 2; win[ord].tgt = -1; win[ord].n = 0; win[ord].s = 0;
+    win[ord].act = 0; win[ord].src = 2; win[ord].tgt = -1; win[ord].n = 0; win[ord].s = 0; win[ord].si = 1;
     win[ord].vtx = 0; win[ord].key = 0;
-    win[ord].i0 = win[ord].i1 = win[ord].i2 = 0;
     win[ord].raw = win[ord].den = win[ord].dm = T(0);
 #pragma unroll
     for (int i = 1; i <= ord; ++i) {
@@ -1229,7 +1233,7 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
         if (br != 0 && rw.offer(dm, den)) {   // the first (sub-limiter, vertex) reaching the order's minimum
           HierWin<T, P> &w = win[ord];
           w.den = den; w.dm = dm;
-          w.i0 = i0; w.i1 = i1; w.i2 = i2; w.n = n; w.s = s;
+          w.n = n; w.s = s; w.si = i;
           // the extreme's source: the Dirichlet value (which wins a tie) or the patch element
           const bool isPos = br == 2;
           const T rawExt = vkey_inv<T>(kv.v[s][isPos ? 1 : 0][n]);
@@ -1300,17 +1304,24 @@ k_lim_vjp_hier(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOu
     if (!used || !w.act) continue;
     const T So = so.get();
     const T q = So / w.den, r = So * w.dm / (w.den * w.den);
-    const T p1 = pt1[w.n], p2 = pt2[w.n];
-    gx[w.i0] = gx[w.i0] - q;
-    gx[w.i1] = gx[w.i1] - r * p1;
-    gx[w.i2] = gx[w.i2] - r * p2;
-    if (w.src == 1) {                          // ext = the element's own vertex value
-      gx[w.i0] = gx[w.i0] + q;
-      gx[w.i1] = gx[w.i1] + q * p1;
-      gx[w.i2] = gx[w.i2] + q * p2;
-    } else if (w.src == 0 && w.tgt >= 0) {     // ext = x[i0] of another element (or this one)
-      recT[o] = w.tgt * 16 + w.i0;
-      recW[o] = q;
+    const T p1 = w.n == 0 ? pt1[0] : (w.n == 1 ? pt1[1] : pt1[2]);
+    const T p2 = w.n == 0 ? pt2[0] : (w.n == 1 ? pt2[1] : pt2[2]);
+    // the winning sub-limiter's DOFs, as compile-time indices (registers, not local memory)
+#pragma unroll
+    for (int i = 1; i <= o; ++i) {
+      if (i != w.si) continue;
+      const int i0 = mind(o - i, i - 1), i1 = mind(o - i + 1, i - 1), i2 = mind(o - i, i);
+      gx[i0] = gx[i0] - q;
+      gx[i1] = gx[i1] - r * p1;
+      gx[i2] = gx[i2] - r * p2;
+      if (w.src == 1) {                          // ext = the element's own vertex value
+        gx[i0] = gx[i0] + q;
+        gx[i1] = gx[i1] + q * p1;
+        gx[i2] = gx[i2] + q * p2;
+      } else if (w.src == 0 && w.tgt >= 0) {     // ext = x[i0] of another element (or this one)
+        recT[o] = w.tgt * 16 + i0;
+        recW[o] = q;
+      }
     }
   }
   T out[N];
@@ -1370,11 +1381,16 @@ k_lim_vjp_strict(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lam
   const bool active = k < g.K;
   const int Kp = g.Kp;
   int vid[3] = {0, 0, 0}, pos[3] = {-1, -1, -1}, dmask = 0;
+  int pr0[3] = {0, 0, 0}, pr1[3] = {0, 0, 0};   // patch ranges of the fused gather (KIND 1)
   T B[4] = {T(1), T(0), T(0), T(1)};
   if (active) {
     vid[0] = g.V0T[k]; vid[1] = g.V0T[Kp + k]; vid[2] = g.V0T[2 * Kp + k];
     pos[0] = csrPos[k]; pos[1] = csrPos[Kp + k]; pos[2] = csrPos[2 * Kp + k];
     dmask = (g.code[k] >> 9) & 7;
+    if (KIND == 1 && gInT) {
+#pragma unroll
+      for (int n = 0; n < 3; ++n) { pr0[n] = g.vptr[vid[n]]; pr1[n] = g.vptr[vid[n] + 1]; }
+    }
 #pragma unroll
     for (int r = 0; r < 4; ++r) B[r] = g.Bm[(size_t)r * Kp + k];
   }
@@ -1401,7 +1417,7 @@ k_lim_vjp_strict(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lam
   SBlocks<T, P> sb;
   s_blocks<T, P>(af, sb);
   T lam[N];
-  hier_lam_in<T, P>(g, k, vid, nnz, KIND == 1 ? gInT : nullptr, gInW, lamInW, sb, lraw, scale, lam);
+  hier_lam_in<T, P>(g, k, pr0, pr1, nnz, KIND == 1 ? gInT : nullptr, gInW, lamInW, sb, lraw, scale, lam);
   SinvBlocks<T, P> si;
   sinv_blocks<T, P>(af, si);
   T mu[N], lamL[N], mc[N];
@@ -1570,12 +1586,15 @@ k_lim_vjp_hier_gather(const Geo<T> g, T *lam, int nnz, const int *slotT, const T
   if (k >= g.K) return;
   const int Kp = g.Kp;
   const int vid[3] = {g.V0T[k], g.V0T[Kp + k], g.V0T[2 * Kp + k]};
+  int i0[3], i1[3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) { i0[n] = g.vptr[vid[n]]; i1[n] = g.vptr[vid[n] + 1]; }
   T B[4];
 #pragma unroll
   for (int r = 0; r < 4; ++r) B[r] = g.Bm[(size_t)r * Kp + k];
   pdl_wait();
   T acc[N];
-  if (!hier_records<T, P>(g, k, vid, nnz, slotT, slotW, acc)) return;
+  if (!hier_records<T, P>(k, i0, i1, nnz, slotT, slotW, acc)) return;
   const Affine<T> af = affine_from<T>(B[0], B[1], B[2], B[3]);
   SBlocks<T, P> sb;
   s_blocks<T, P>(af, sb);
