@@ -851,8 +851,8 @@ extern "C" int dgadv_forward_record(dgadv_handle *h, int32_t nSteps, double tau,
     }
     drop_sweep(h);
   }
-  // the second stream of the reverse sweep: recomputation (and its buffer set) and, with the
-  // limiter, the limiter adjoint's scatters
+  // the other streams of the reverse sweep: recomputation (and its buffer set), advances (with
+  // three streams) and, with the limiter, the limiter adjoint's scatters
   if (h->adjStreams >= 2 && (h->lim || (stageSteps == 0 && S > 1)) && (st = lanes_alloc(h, nSteps, nSlots, stageSteps == 0)))
     return st;
   h->slotStep.assign(nSlots, -1);

@@ -585,12 +585,13 @@ k_lim_vjp(const Geo<T> g, const T *x, const T *lamIn, T *__restrict__ lamOut, co
   if (pos[ns] >= 0) slotW[pos[ns]] = w;
 }
 
-// k_lim_vjp in two halves, for the sweep on two streams.  The choices depend on the recorded
-// input x only, not on lambda: k_lim_choice makes them on the recomputation stream, one reversed
-// step ahead, and records per element the factor, the chosen vertex and branch, den, dm / den^2
-// and the element holding the extreme; k_lim_apply applies lambda on the reverse stream without
-// the keys, the shifts or the patch walk for the extreme.  Both compute k_lim_vjp's expressions
-// in its order, so the gradients are bitwise those of the one-kernel form.
+// k_lim_vjp in two halves, for the sweep on several streams.  The choices depend on the
+// recorded input x only, not on lambda: k_lim_choice makes them on the recomputation stream,
+// one reversed step ahead, and records per element the factor, the chosen vertex and branch,
+// den, dm / den^2 and the element holding the extreme; k_lim_apply applies lambda on the
+// reverse stream without the keys, the shifts or the patch walk for the extreme.  Both compute
+// k_lim_vjp's expressions in its order, so the gradients are bitwise those of the one-kernel
+// form.
 template <typename T> struct LimChoice {
   T *alpha, *den, *q;   // per element (Kp)
   int *tgt, *info;      // info: bits 0-1 the vertex, bit 2 limited, bit 3 the clip is active
