@@ -341,3 +341,162 @@ class LimitedAdjointOracle:
                 mu = (1 - w) * muY + self.op.AT(flat).reshape(K, N)
             lam = accn + mu
         return lam, gth
+
+
+# ---------------------------------------------------------------------------------------------
+# The strict limiter (core/applySlopeLimiterTaylorStrict.m:111-150) with its choices frozen.
+# The forward limits the orders o = p..1 in turn, each on the data already limited: a
+# sub-limiter's vertex values are the degree-(p - o + 1) reconstruction about a derivative of
+# order o - 1, and every DOF of degree >= o is scaled by the order's factor.  With the choices
+# held (per order and element: the winning sub-limiter, vertex and branch, and the source of the
+# patch extreme: an element, the element's own vertex value above order 1, or boundary data),
+# the run is a smooth function of its input, and central differences of that replay give the
+# exact directional derivative of the piece the run sits on, with no switch to cross.  That is
+# what the GPU's strict-limiter adjoint is checked against.
+
+
+def strict_choices(mf, cT, markV0TbdrD, dataV0T):
+    """Runs the strict limiter on Taylor coefficients cT as the forward does (matfree.limit_taylor)
+    and returns (limited, choices): per order o, alpha_o and the winner of each element (the
+    first sub-limiter and vertex attaining alpha_o), whether alpha_o varies with the data there
+    (a branch ratio strictly inside (0, 1)), and the extreme's source (patch_extremes)."""
+    from . import basis as B
+    from . import limiter as L
+    phiV = mf.pd.basesOnQuad.phiTaylorV0T
+    K, N = cT.shape
+    p = B.p_of_N(N)
+    r = np.arange(K)
+    lim = cT.copy()
+    chs = {}
+    for o in range(p, 0, -1):
+        facs, raws, dms, poss, srcs, mvals, subs = [], [], [], [], [], [], []
+        aO = np.ones(K)
+        for i in range(1, o + 1):
+            ind = L.mult2ind(np.array([o - i, i - 1])[None, :] + L.multiindex(p - o + 1))
+            v = A.computeFuncDiscAtPoints(lim[:, ind], phiV[:, :, 0:ind.size])
+            data = v if o > 1 else dataV0T
+            aO = np.fmin(aO, mf.vertex_limiter(lim[:, ind[0]], v, markV0TbdrD, data))
+            c = lim[:, ind[0]]
+            mn, mx, sMin, sMax = patch_extremes(mf, c, markV0TbdrD, data)
+            dV, dMin, dMax = v - c[:, None], mn - c[:, None], mx - c[:, None]
+            neg = dV < dMin + TOL
+            pos = dV > dMax - TOL
+            with np.errstate(divide='ignore', invalid='ignore'):
+                raw = np.where(pos, dMax / (dV + TOL), np.where(neg, dMin / (dV - TOL), np.nan))
+            for n in range(3):
+                br = neg[:, n] | pos[:, n]
+                facs.append(np.where(br, np.fmax(0, np.fmin(1, raw[:, n])), 1.0))
+                raws.append(raw[:, n])
+                dms.append(np.where(pos[:, n], dMax[:, n], dMin[:, n]))
+                poss.append(pos[:, n])
+                srcs.append(np.where(pos[:, n], sMax[:, n], sMin[:, n]))
+                mvals.append(np.where(pos[:, n], mx[:, n], mn[:, n]))
+                subs.append(i)
+        F = np.stack(facs, axis=1)
+        w = np.argmax(F == aO[:, None], axis=1)                    # first winner
+        pick = lambda arrs: np.stack(arrs, axis=1)[r, w]
+        rw = pick(raws)
+        chs[o] = dict(alpha=aO, i=np.array(subs)[w], n=w % 3, isPos=pick(poss), src=pick(srcs),
+                      mval=pick(mvals), active=(aO < 1) & (rw > 0) & (rw < 1))
+        lim[:, o * (o + 1) // 2:] = aO[:, None] * lim[:, o * (o + 1) // 2:]
+    return lim, chs
+
+
+def strict_frozen(mf, cT, chs):
+    """The strict limiter with the choices chs held: on the elements where alpha_o varies with
+    the data it is the winner's ratio (ext - c) / (v_n - c +- tol), recomputed from cT; elsewhere
+    the recorded factor."""
+    from . import basis as B
+    from . import limiter as L
+    phiV = mf.pd.basesOnQuad.phiTaylorV0T
+    K, N = cT.shape
+    p = B.p_of_N(N)
+    lim = cT.copy()
+    for o in range(p, 0, -1):
+        ch = chs[o]
+        alpha = ch['alpha'].astype(cT.dtype)
+        for i in range(1, o + 1):
+            sel = np.nonzero(ch['active'] & (ch['i'] == i))[0]
+            if sel.size == 0:
+                continue
+            ind = L.mult2ind(np.array([o - i, i - 1])[None, :] + L.multiindex(p - o + 1))
+            n = ch['n'][sel]
+            v = np.sum(lim[sel][:, ind] * phiV[sel, n, 0:ind.size], axis=1)
+            c = lim[sel, ind[0]]
+            src = ch['src'][sel]
+            own = v if o > 1 else ch['mval'][sel]                    # Dirichlet: own value / data
+            ext = np.where(src >= 0, cT[np.maximum(src, 0), ind[0]], own)
+            den = (v - c) + np.where(ch['isPos'][sel], TOL, -TOL)
+            alpha[sel] = (ext - c) / den
+        lim[:, o * (o + 1) // 2:] = alpha[:, None] * lim[:, o * (o + 1) // 2:]
+    return lim
+
+
+class StrictReplayOracle:
+    """Forward run of the scheme with the strict limiter (solution limiting, and time-derivative
+    limiting with the Taylor mass correction at p >= 2, advection/solveSubStep.m:69-98); with
+    frozen=True the run replays the choices of the last unfrozen run.  The replay is rational in
+    c0 and takes complex input: Im J(c0 + i h d) / h is the exact directional derivative of the
+    piece (complex step, Squire and Trapp 1998), also next to the poles of dm / den where a
+    winner's v_n - c is of the order of tol and real differences need h below |den|."""
+
+    def __init__(self, **kw):
+        kw = dict(kw)
+        kw.setdefault('testcase', 'adjoint')
+        kw['isSlopeLim'] = True
+        kw['typeSlopeLim'] = 'strict'
+        self.op = AdjointOracle.__new__(AdjointOracle)
+        AdjointOracle.__init__(self.op, **dict(kw, isSlopeLim=False))
+        pd = adv.Struct(kw)
+        pd.problemName = 'advection'
+        for f in (adv.configureProblem, adv.preprocessProblem, adv.initializeProblem):
+            pd = f(pd)
+        self.pd = pd
+        self.mf = MF.MatFree(pd)
+        self.P = np.linalg.solve(self.mf.MDT, self.mf.M)
+        self.Pinv = np.linalg.solve(self.mf.M, self.mf.MDT)
+        self.omega = self.op.omega
+
+    def T(self, c):
+        return np.einsum('kij,kj->ki', self.P, c)
+
+    def Tinv(self, cT):
+        return np.einsum('kij,kj->ki', self.Pinv, cT)
+
+    def forward(self, c0, nSteps, frozen=False):
+        pd, g = self.pd, self.pd.g
+        K, N = pd.K, pd.N
+        tau = pd.tau
+        nan3 = np.full((K, 3), np.nan)
+        cD = np.zeros((K, 3))                                   # the adjoint case: c_D = 0
+        c = np.array(c0, dtype=np.complex128 if np.iscomplexobj(c0) else np.float64).reshape(K, N)
+        if not frozen:
+            self.choices = []
+        def opA(v):   # the real operator on a real or complex state
+            if np.iscomplexobj(v):
+                return self.op.A(v.real.copy()) + 1j * self.op.A(v.imag.copy())
+            return self.op.A(v)
+        for n in range(nSteps):
+            cn = c
+            chs = []
+            for s, w in enumerate(self.omega):
+                cdot = opA(c.reshape(-1)).reshape(K, N)
+                chd = None
+                if pd.p > 1:
+                    cT = self.T(cdot)
+                    if frozen:
+                        cTL = strict_frozen(self.mf, cT, self.choices[n][s][0])
+                    else:   # the Dirichlet vertices with no data (advection/solveSubStep.m:76)
+                        cTL, chd = strict_choices(self.mf, cT, g.markV0TbdrD, nan3)
+                    cdot = self.Tinv(cTL + np.einsum('kij,kj->ki', self.mf.Mcorr, cT - cTL))
+                y = w * cn + (1 - w) * (c + tau * cdot)
+                yT = self.T(y)
+                if frozen:
+                    c = self.Tinv(strict_frozen(self.mf, yT, self.choices[n][s][1]))
+                else:
+                    yL, chs_y = strict_choices(self.mf, yT, g.markV0TbdrD, cD)
+                    chs.append((chd, chs_y))
+                    c = self.Tinv(yL)
+            if not frozen:
+                self.choices.append(chs)
+        return c
