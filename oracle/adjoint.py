@@ -432,19 +432,114 @@ def strict_frozen(mf, cT, chs):
     return lim
 
 
-class StrictReplayOracle:
-    """Forward run of the scheme with the strict limiter (solution limiting, and time-derivative
+def hier_choices(mf, cT, markV0TbdrD, dataV0T):
+    """The hierarchical vertex limiter (core/applySlopeLimiterTaylorHierarchicalVertex.m:124-168)
+    on Taylor coefficients cT, as the forward runs it (matfree.limit_taylor), with its choices:
+    per order o the factor alpha_o of its sub-limiters (linear reconstructions of the input) and
+    the winner as in strict_choices, and per degree d the order whose alpha holds the running
+    maximum A_d = max(alpha_p, ..., alpha_d) (the first, highest, on ties)."""
+    from . import basis as B
+    from . import limiter as L
+    phiV = mf.pd.basesOnQuad.phiTaylorV0T
+    K, N = cT.shape
+    p = B.p_of_N(N)
+    r = np.arange(K)
+    lim = np.zeros_like(cT)
+    lim[:, 0] = cT[:, 0]
+    run = np.zeros(K)
+    runOrd = np.full(K, p)
+    chs = {'runOrd': {}}
+    for o in range(p, 0, -1):
+        facs, raws, poss, srcs, mvals, subs = [], [], [], [], [], []
+        aO = np.ones(K)
+        for i in range(1, o + 1):
+            ind = L.mult2ind(np.array([o - i, i - 1])[None, :] + L.multiindex(1))
+            v = A.computeFuncDiscAtPoints(cT[:, ind], phiV[:, :, 0:3])
+            data = v if o > 1 else dataV0T
+            aO = np.fmin(aO, mf.vertex_limiter(cT[:, ind[0]], v, markV0TbdrD, data))
+            c = cT[:, ind[0]]
+            mn, mx, sMin, sMax = patch_extremes(mf, c, markV0TbdrD, data)
+            dV, dMin, dMax = v - c[:, None], mn - c[:, None], mx - c[:, None]
+            neg = dV < dMin + TOL
+            pos = dV > dMax - TOL
+            with np.errstate(divide='ignore', invalid='ignore'):
+                raw = np.where(pos, dMax / (dV + TOL), np.where(neg, dMin / (dV - TOL), np.nan))
+            for n in range(3):
+                br = neg[:, n] | pos[:, n]
+                facs.append(np.where(br, np.fmax(0, np.fmin(1, raw[:, n])), 1.0))
+                raws.append(raw[:, n])
+                poss.append(pos[:, n])
+                srcs.append(np.where(pos[:, n], sMax[:, n], sMin[:, n]))
+                mvals.append(np.where(pos[:, n], mx[:, n], mn[:, n]))
+                subs.append(i)
+        F = np.stack(facs, axis=1)
+        w = np.argmax(F == aO[:, None], axis=1)
+        pick = lambda arrs: np.stack(arrs, axis=1)[r, w]
+        rw = pick(raws)
+        chs[o] = dict(alpha=aO, i=np.array(subs)[w], n=w % 3, isPos=pick(poss), src=pick(srcs),
+                      mval=pick(mvals), active=(aO < 1) & (rw > 0) & (rw < 1))
+        runOrd = np.where((o == p) | (aO > run), o, runOrd)
+        run = np.fmax(run, aO)
+        chs['runOrd'][o] = runOrd.copy()
+        d = np.arange(o * (o + 1) // 2, (o + 1) * (o + 2) // 2)
+        lim[:, d] = run[:, None] * cT[:, d]
+    return lim, chs
+
+
+def hier_frozen(mf, cT, chs):
+    """The hierarchical limiter with the choices chs held: each order's factor is its winner's
+    ratio where it varies with the data (else the recorded factor), computed from the input cT,
+    and degree d is scaled by the factor of the order recorded as holding A_d."""
+    from . import basis as B
+    from . import limiter as L
+    phiV = mf.pd.basesOnQuad.phiTaylorV0T
+    K, N = cT.shape
+    p = B.p_of_N(N)
+    r = np.arange(K)
+    fac = {}
+    for o in range(p, 0, -1):
+        ch = chs[o]
+        alpha = ch['alpha'].astype(cT.dtype)
+        for i in range(1, o + 1):
+            sel = np.nonzero(ch['active'] & (ch['i'] == i))[0]
+            if sel.size == 0:
+                continue
+            ind = L.mult2ind(np.array([o - i, i - 1])[None, :] + L.multiindex(1))
+            n = ch['n'][sel]
+            v = np.sum(cT[sel][:, ind] * phiV[sel, n, 0:3], axis=1)
+            c = cT[sel, ind[0]]
+            src = ch['src'][sel]
+            own = v if o > 1 else ch['mval'][sel]
+            ext = np.where(src >= 0, cT[np.maximum(src, 0), ind[0]], own)
+            den = (v - c) + np.where(ch['isPos'][sel], TOL, -TOL)
+            alpha[sel] = (ext - c) / den
+        fac[o] = alpha
+    lim = np.zeros_like(cT)
+    lim[:, 0] = cT[:, 0]
+    for o in range(p, 0, -1):
+        F = np.stack([fac[q] for q in range(1, p + 1)], axis=1)      # column q - 1: order q
+        A_d = F[r, chs['runOrd'][o] - 1]
+        d = np.arange(o * (o + 1) // 2, (o + 1) * (o + 2) // 2)
+        lim[:, d] = A_d[:, None] * cT[:, d]
+    return lim
+
+
+class LimiterReplayOracle:
+    """Forward run of the scheme with the strict (or, typ='hierarch_vert', the hierarchical
+    vertex) limiter (solution limiting, and time-derivative
     limiting with the Taylor mass correction at p >= 2, advection/solveSubStep.m:69-98); with
     frozen=True the run replays the choices of the last unfrozen run.  The replay is rational in
     c0 and takes complex input: Im J(c0 + i h d) / h is the exact directional derivative of the
     piece (complex step, Squire and Trapp 1998), also next to the poles of dm / den where a
     winner's v_n - c is of the order of tol and real differences need h below |den|."""
 
-    def __init__(self, **kw):
+    def __init__(self, typ='strict', **kw):
         kw = dict(kw)
         kw.setdefault('testcase', 'adjoint')
         kw['isSlopeLim'] = True
-        kw['typeSlopeLim'] = 'strict'
+        kw['typeSlopeLim'] = typ
+        self.choose, self.frozen = {'strict': (strict_choices, strict_frozen),
+                                    'hierarch_vert': (hier_choices, hier_frozen)}[typ]
         self.op = AdjointOracle.__new__(AdjointOracle)
         AdjointOracle.__init__(self.op, **dict(kw, isSlopeLim=False))
         pd = adv.Struct(kw)
@@ -485,16 +580,16 @@ class StrictReplayOracle:
                 if pd.p > 1:
                     cT = self.T(cdot)
                     if frozen:
-                        cTL = strict_frozen(self.mf, cT, self.choices[n][s][0])
+                        cTL = self.frozen(self.mf, cT, self.choices[n][s][0])
                     else:   # the Dirichlet vertices with no data (advection/solveSubStep.m:76)
-                        cTL, chd = strict_choices(self.mf, cT, g.markV0TbdrD, nan3)
+                        cTL, chd = self.choose(self.mf, cT, g.markV0TbdrD, nan3)
                     cdot = self.Tinv(cTL + np.einsum('kij,kj->ki', self.mf.Mcorr, cT - cTL))
                 y = w * cn + (1 - w) * (c + tau * cdot)
                 yT = self.T(y)
                 if frozen:
-                    c = self.Tinv(strict_frozen(self.mf, yT, self.choices[n][s][1]))
+                    c = self.Tinv(self.frozen(self.mf, yT, self.choices[n][s][1]))
                 else:
-                    yL, chs_y = strict_choices(self.mf, yT, g.markV0TbdrD, cD)
+                    yL, chs_y = self.choose(self.mf, yT, g.markV0TbdrD, cD)
                     chs.append((chd, chs_y))
                     c = self.Tinv(yL)
             if not frozen:

@@ -161,7 +161,7 @@ def test_strict_replay_is_the_run_and_its_complex_step_is_its_derivative():
     replay at a step below the smallest winner's |v_n - c -+ tol|."""
     from oracle import adjoint as OA
     kw = dict(hmax=2 ** -3, p=3, numSteps=2, tEnd=2 * 1e-4)
-    o = OA.StrictReplayOracle(**kw)
+    o = OA.LimiterReplayOracle(**kw)
     c0 = o.pd.cDisc
     cT = o.forward(c0, kw['numSteps'])
     cR = o.forward(c0, kw['numSteps'], frozen=True)

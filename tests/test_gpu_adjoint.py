@@ -194,25 +194,27 @@ def test_limited_fp64_gradient_matches_oracle(lib, kw, snaps):
     assert rel(gth, ogth) <= 1e-11
 
 
-STRICT_ORACLE = [dict(hmax=2 ** -3, p=2, numSteps=4, tEnd=4 * 2e-4),
+REPLAY_CASES = [dict(hmax=2 ** -3, p=2, numSteps=4, tEnd=4 * 2e-4),
                  dict(hmax=2 ** -3, p=3, numSteps=3, tEnd=3 * 1e-4)]
 
 
-@pytest.mark.parametrize('kw', STRICT_ORACLE, ids=['p2', 'p3'])
-def test_strict_gradient_matches_oracle_replay(lib, kw):
-    """The strict limiter's adjoint against the oracle's replay of the same run with its choices
-    frozen: the complex-step derivative Im J(c0 + i h d) / h of that replay is the exact
-    directional derivative of the piece the run sits on (real differences would need h below
-    the smallest |v_n - c -+ tol| of a winner, about 1e-10 here).  Along random directions of
-    the initial coefficients, with stored stages and with recomputing checkpoints."""
+@pytest.mark.parametrize('lim', ['strict', 'hierarch_vert'])
+@pytest.mark.parametrize('kw', REPLAY_CASES, ids=['p2', 'p3'])
+def test_taylor_limiter_gradient_matches_oracle_replay(lib, kw, lim):
+    """The strict and the hierarchical limiter's adjoints against the oracle's replay of the same
+    run with its choices frozen: the complex-step derivative Im J(c0 + i h d) / h of that replay
+    is the exact directional derivative of the piece the run sits on (real differences would
+    need h below the smallest |v_n - c -+ tol| of a winner, about 1e-10 here).  Along random
+    directions of the initial coefficients, with stored stages and with recomputing
+    checkpoints."""
     from oracle import adjoint as OA
     from festung_gb300 import adjoint as AD
-    o = OA.StrictReplayOracle(**kw)
+    o = OA.LimiterReplayOracle(typ=lim, **kw)
     c0 = o.pd.cDisc
-    cstar = OA.StrictReplayOracle(adjointTarget=True, **kw).forward(c0, kw['numSteps'])
+    cstar = OA.LimiterReplayOracle(typ=lim, adjointTarget=True, **kw).forward(c0, kw['numSteps'])
     cT = o.forward(c0, kw['numSteps'])
     Jo = 0.5 * float(np.sum((cT - cstar) ** 2))
-    pd = AD.setup(precision='fp64', isSlopeLim=True, typeSlopeLim='strict', **kw)
+    pd = AD.setup(precision='fp64', isSlopeLim=True, typeSlopeLim=lim, **kw)
     try:
         for snaps in (0, 2):
             J, g0, gth = AD.misfit_gradient(pd, c0, pd.theta, cstar, nSnapshots=snaps)
