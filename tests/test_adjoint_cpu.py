@@ -155,24 +155,26 @@ def test_limited_oracle_forward_is_the_reference_run():
     assert np.linalg.norm(o.forward(o.pd.cDisc, 5) - ref) <= 1e-14 * np.linalg.norm(ref)
 
 
-def test_strict_replay_is_the_run_and_its_complex_step_is_its_derivative():
-    """The oracle's frozen replay of a strict-limiter run (used to check the GPU adjoint)
-    reproduces the run, and its complex-step derivative agrees with central differences of the
-    replay at a step below the smallest winner's |v_n - c -+ tol|."""
+@pytest.mark.parametrize('typ', ['strict', 'hierarch_vert'])
+def test_limiter_replay_is_the_run_and_its_complex_step_is_its_derivative(typ):
+    """The oracle's frozen replay of a strict- or hierarchical-limiter run (used to check the
+    GPU adjoints) reproduces the run, and its complex-step derivative agrees with central
+    differences of the replay at a step below the smallest winner's |v_n - c -+ tol|."""
     from oracle import adjoint as OA
     kw = dict(hmax=2 ** -3, p=3, numSteps=2, tEnd=2 * 1e-4)
-    o = OA.LimiterReplayOracle(**kw)
+    o = OA.LimiterReplayOracle(typ=typ, **kw)
     c0 = o.pd.cDisc
     cT = o.forward(c0, kw['numSteps'])
     cR = o.forward(c0, kw['numSteps'], frozen=True)
     assert np.linalg.norm(cR - cT) <= 1e-13 * np.linalg.norm(cT)
-    assert sum(int(ch[1][q]['active'].sum()) for st in o.choices for ch in st for q in ch[1]) > 0
+    assert sum(int(ch[1][q]['active'].sum()) for st in o.choices for ch in st for q in ch[1]
+               if isinstance(q, int)) > 0
     w = np.random.default_rng(2).standard_normal(c0.shape)
     J = lambda c: np.sum(w * c)
     d = np.random.default_rng(3).standard_normal(c0.shape)
     cs = float(np.imag(J(o.forward(c0 + 1e-30j * d, kw['numSteps'], frozen=True)))) / 1e-30
-    # this run has a winner within about 1e-10 of a pole: central differences converge like h^2
-    # only below it (3.7e-3, 3.8e-5, 6.7e-7 at h = 1e-11, 1e-12, 1e-13)
+    # these runs have a winner within about 1e-10 of a pole: central differences converge like
+    # h^2 only below it (strict: 3.7e-3, 3.8e-5, 6.7e-7 at h = 1e-11, 1e-12, 1e-13)
     err = []
     for h in (1e-12, 1e-13):
         fd = (J(o.forward(c0 + h * d, kw['numSteps'], frozen=True)) - J(o.forward(c0 - h * d, kw['numSteps'], frozen=True))) / (2 * h)
